@@ -1,0 +1,992 @@
+// C ABI of the GB300 cg-gcmc-bd inner loop (include/bromoc_gpu.h).
+//
+// The context owns every device allocation and a KP parameter block whose
+// pointers are passed by value to the kernels.  Module state uploaded by the
+// set_* calls corresponds to what the reference's deck interpreter leaves in
+// its Fortran modules; the particle arrays stay device-resident between
+// calls, and GCMC edits them in place on the device.
+#include <cmath>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bromoc_gpu.h"
+#include "launch.h"
+
+using namespace bgpu;
+
+namespace {
+constexpr int kMaxChunks = 64;
+constexpr int kPairTile = 128;
+constexpr int kSMs = 152;
+}  // namespace
+
+struct bromoc_ctx {
+  KP kp{};
+  std::string err;
+  cudaStream_t stream = nullptr;
+  bool own_stream = false;
+  int precision = BROMOC_FP64;
+  std::vector<void *> allocs;
+  // host mirrors
+  int ntype = 0, nold = 0, nttyp = 0, ndna = 0, ntc = 0, cnt = 0;
+  int nbuffer = 0, cntpts = 0;
+  bool have_sys = false, have_types = false, have_pairs = false;
+  bromoc_system sys{};
+  std::vector<double> diffusion;  // 1-based
+  // live ntot bookkeeping (see ntot_ub)
+  int ntot_known = 0;
+  long long attempts_total = 0, attempts_at_known = 0;
+  int *h_ntot = nullptr;  // pinned
+  cudaEvent_t ev_ntot = nullptr;
+  bool rb_pending = false;
+  long long rb_attempts = 0;
+  // scratch
+  bool have_scratch = false;
+  int nslot_cap = 0;
+  double *d_dener = nullptr;
+  // last energy plan (for dynamics())
+  AssembleFlags last_fl{};
+  bool have_forces = false;
+};
+
+namespace {
+
+int set_err(bromoc_ctx *c, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (c) c->err = buf;
+  return code;
+}
+
+#define CU(call)                                                             \
+  do {                                                                       \
+    cudaError_t e_ = (call);                                                 \
+    if (e_ != cudaSuccess)                                                   \
+      return set_err(ctx, BROMOC_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
+  } while (0)
+
+template <class T>
+int dalloc(bromoc_ctx *ctx, T **p, size_t n) {
+  *p = nullptr;
+  if (n == 0) n = 1;
+  cudaError_t e = cudaMalloc((void **)p, n * sizeof(T));
+  if (e != cudaSuccess)
+    return set_err(ctx, BROMOC_E_NOMEM, "cudaMalloc(%zu bytes): %s",
+                   n * sizeof(T), cudaGetErrorString(e));
+  ctx->allocs.push_back((void *)*p);
+  return BROMOC_OK;
+}
+
+void dfree(bromoc_ctx *ctx, void *p) {
+  if (!p) return;
+  for (auto &a : ctx->allocs)
+    if (a == p) {
+      cudaFree(p);
+      a = nullptr;
+    }
+}
+
+// allocate (replacing a previous allocation) and copy n host elements
+template <class T>
+int upload(bromoc_ctx *ctx, T **dst, const T *src, size_t n) {
+  if (*dst) dfree(ctx, (void *)*dst);
+  int rc = dalloc(ctx, dst, n);
+  if (rc) return rc;
+  if (src && n) CU(cudaMemcpy((void *)*dst, src, n * sizeof(T), cudaMemcpyHostToDevice));
+  return BROMOC_OK;
+}
+
+// copy into a fresh 1-based device array of n+1 elements
+template <class T>
+int upload1(bromoc_ctx *ctx, const T **dst, const T *src, int n, T fill = T()) {
+  std::vector<T> v(n + 1, fill);
+  if (src)
+    for (int i = 0; i < n; ++i) v[i + 1] = src[i];
+  T *d = const_cast<T *>(*dst);
+  int rc = upload(ctx, &d, v.data(), v.size());
+  *dst = d;
+  return rc;
+}
+
+Grid3 make_grid(const bromoc_grid &g) {
+  Grid3 r{};
+  r.nclx = g.nclx;
+  r.ncly = g.ncly;
+  r.nclz = g.nclz;
+  r.dcel = g.dcel;
+  r.idcel = 1.0 / g.dcel;
+  r.tranx = 0.5 * (g.nclx - 1) * g.dcel;  // readphi.f90:49-51
+  r.trany = 0.5 * (g.ncly - 1) * g.dcel;
+  r.tranz = 0.5 * (g.nclz - 1) * g.dcel;
+  r.xbcen = g.xbcen;
+  r.ybcen = g.ybcen;
+  r.zbcen = g.zbcen;
+  return r;
+}
+
+bool grid_ok(const bromoc_grid *g) {
+  return g && g->nclx >= 2 && g->ncly >= 2 && g->nclz >= 2 && g->dcel > 0.0;
+}
+
+// Upper bound of the device-resident ntot, without a host round trip.
+int ntot_ub(bromoc_ctx *c) {
+  if (c->rb_pending && cudaEventQuery(c->ev_ntot) == cudaSuccess) {
+    c->ntot_known = *c->h_ntot;
+    c->attempts_at_known = c->rb_attempts;
+    c->rb_pending = false;
+  }
+  long long ub = c->ntot_known + (c->attempts_total - c->attempts_at_known);
+  return (int)std::min<long long>(ub, c->kp.cap);
+}
+
+int sync_ntot(bromoc_ctx *ctx) {
+  CU(cudaMemcpyAsync(ctx->h_ntot, &ctx->kp.st->ntot, sizeof(int),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->ntot_known = *ctx->h_ntot;
+  ctx->attempts_at_known = ctx->attempts_total;
+  ctx->rb_pending = false;
+  return BROMOC_OK;
+}
+
+int ensure_scratch(bromoc_ctx *ctx) {
+  if (ctx->have_scratch) return BROMOC_OK;
+  KP &p = ctx->kp;
+  const size_t cap = p.cap;
+  int rc;
+  if ((rc = dalloc(ctx, &p.ffield, 3 * cap))) return rc;
+  if ((rc = dalloc(ctx, &p.fii, (size_t)kMaxChunks * 3 * cap))) return rc;
+  if ((rc = dalloc(ctx, &p.fis, 3 * cap))) return rc;
+  if ((rc = dalloc(ctx, &p.frf, (size_t)kMaxChunks * 3 * cap))) return rc;
+  const int tiles = (int)((cap + kPairTile - 1) / kPairTile) + 1;
+  ctx->nslot_cap = tiles * (2 * kMaxChunks + 4) + 8;
+  if ((rc = dalloc(ctx, &p.epart, (size_t)ctx->nslot_cap * kNTerms))) return rc;
+  if ((rc = dalloc(ctx, &p.ipart, (size_t)tiles + 2))) return rc;
+  if ((rc = dalloc(ctx, &p.rf_srfe, cap))) return rc;
+  if ((rc = dalloc(ctx, &p.rf_reff, cap))) return rc;
+  if ((rc = dalloc(ctx, &p.rf_d1, 3 * cap))) return rc;
+  if ((rc = dalloc(ctx, &p.rf_d2, 3 * cap))) return rc;
+  if ((rc = dalloc(ctx, &p.rf_in, cap))) return rc;
+  if ((rc = dalloc(ctx, &p.dids, 5 * cap))) return rc;
+  CU(cudaMemset(p.dids, 0, 5 * cap * sizeof(double)));
+  if ((rc = dalloc(ctx, &p.eterms, kNTerms))) return rc;
+  if ((rc = dalloc(ctx, &p.trial, 1))) return rc;
+  if ((rc = dalloc(ctx, &ctx->d_dener, 1))) return rc;
+  ctx->have_scratch = true;
+  return BROMOC_OK;
+}
+
+// Source chunking of the pair kernels: enough blocks for ~2 waves of the
+// 152 SMs, chunks a multiple of the 128-particle tile.
+void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
+  if (ntargets <= 0 || nsources <= 0) {
+    nchunk = 0;
+    chunk = kPairTile;
+    return;
+  }
+  const int tiles = (ntargets + kPairTile - 1) / kPairTile;
+  const int stiles = (nsources + kPairTile - 1) / kPairTile;
+  int want = (2 * kSMs + tiles - 1) / tiles;
+  want = std::max(1, std::min(std::min(want, stiles), kMaxChunks));
+  int per = (stiles + want - 1) / want;  // source tiles per chunk
+  chunk = per * kPairTile;
+  nchunk = (nsources + chunk - 1) / chunk;
+}
+
+int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
+                AssembleFlags &fl) {
+  KP &p = ctx->kp;
+  plan.ntot_ub = ntot_ub(ctx);
+  plan.fp32 = ctx->precision == BROMOC_FP32;
+  plan.reduce_energy = reduce;
+  const int nion = plan.ntot_ub - p.nsites;
+  const int nmob = nion - p.nfix;
+  chunking(nmob, nion, plan.nchunk_ii, p.chunk_ii);
+  p.nchunk_ii = plan.nchunk_ii;
+  chunking(nion, nion, plan.nchunk_rf, p.chunk_rf);
+  p.nchunk_rf = plan.nchunk_rf;
+  fl = AssembleFlags{};
+  fl.ii = (mask & BROMOC_M_NONBOND) && nmob > 0 && plan.nchunk_ii > 0;
+  fl.nchunk_ii = fl.ii ? plan.nchunk_ii : 0;
+  fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
+  fl.rf = (mask & BROMOC_M_RFPAR) && p.qrfpar && nion > 0 && plan.nchunk_rf > 0;
+  fl.nchunk_rf = fl.rf ? plan.nchunk_rf : 0;
+  if (energy_slots(p, plan, mask) > ctx->nslot_cap)
+    return set_err(ctx, BROMOC_E_ARG, "energy slots exceed scratch");
+  return BROMOC_OK;
+}
+
+int check_ready(bromoc_ctx *ctx) {
+  if (!ctx->have_sys || !ctx->have_types || !ctx->have_pairs)
+    return set_err(ctx, BROMOC_E_STATE,
+                   "set_system, set_types and set_pairs are required");
+  return ensure_scratch(ctx);
+}
+
+int check_device_err(bromoc_ctx *ctx) {
+  int e = 0;
+  CU(cudaMemcpyAsync(ctx->h_ntot + 1, &ctx->kp.st->err, sizeof(int),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  e = ctx->h_ntot[1];
+  if (e) {
+    CU(cudaMemsetAsync(&ctx->kp.st->err, 0, sizeof(int), ctx->stream));
+    if (e & kErrCapacity)
+      return set_err(ctx, BROMOC_E_CAPACITY, "grand: ntot is greater than capacity");
+    return set_err(ctx, BROMOC_E_DEVICE, "device error flags 0x%x", e);
+  }
+  return BROMOC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bromoc_gpu_abi_version(void) { return BROMOC_ABI_VERSION; }
+
+const char *bromoc_gpu_last_error(const bromoc_ctx *ctx) {
+  return ctx ? ctx->err.c_str() : "null context";
+}
+
+int bromoc_gpu_create(int32_t capacity, int32_t precision, void *stream,
+                      bromoc_ctx **out) {
+  if (!out) return BROMOC_E_ARG;
+  *out = nullptr;
+  if (capacity <= 0 || (precision != BROMOC_FP64 && precision != BROMOC_FP32))
+    return BROMOC_E_ARG;
+  int ndev = 0;
+  if (cudaGetDeviceCount(&ndev) != cudaSuccess || ndev == 0) return BROMOC_E_CUDA;
+  bromoc_ctx *ctx = new bromoc_ctx();
+  ctx->precision = precision;
+  KP &p = ctx->kp;
+  p.cap = capacity;
+  p.celec = 1.60217656535E-19 * 1.60217656535E-19 /
+            (4.0 * kPi * 8.854187817620E-12 * (4184.0 / 6.0221412927E23) * 1E-10);
+  int rc = BROMOC_OK;
+  if (stream) {
+    ctx->stream = (cudaStream_t)stream;
+  } else {
+    if (cudaStreamCreateWithFlags(&ctx->stream, cudaStreamNonBlocking) != cudaSuccess)
+      rc = BROMOC_E_CUDA;
+    ctx->own_stream = true;
+  }
+  if (!rc && cudaMallocHost((void **)&ctx->h_ntot, 4 * sizeof(int)) != cudaSuccess)
+    rc = BROMOC_E_CUDA;
+  if (!rc && cudaEventCreateWithFlags(&ctx->ev_ntot, cudaEventDisableTiming) != cudaSuccess)
+    rc = BROMOC_E_CUDA;
+  if (!rc) rc = dalloc(ctx, &p.st, 1);
+  if (!rc) rc = dalloc(ctx, &p.x, capacity);
+  if (!rc) rc = dalloc(ctx, &p.y, capacity);
+  if (!rc) rc = dalloc(ctx, &p.z, capacity);
+  if (!rc) rc = dalloc(ctx, &p.typei, capacity);
+  if (!rc) rc = dalloc(ctx, &p.ibuffer, capacity);
+  if (!rc) rc = dalloc(ctx, &p.fx, capacity);
+  if (!rc) rc = dalloc(ctx, &p.fy, capacity);
+  if (!rc) rc = dalloc(ctx, &p.fz, capacity);
+  if (!rc && cudaMemset(p.st, 0, sizeof(DevState)) != cudaSuccess) rc = BROMOC_E_CUDA;
+  if (!rc && cudaMemset(p.ibuffer, 0, capacity * sizeof(int)) != cudaSuccess) rc = BROMOC_E_CUDA;
+  if (rc) {
+    bromoc_gpu_destroy(ctx);
+    return rc;
+  }
+  *out = ctx;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_destroy(bromoc_ctx *ctx) {
+  if (!ctx) return BROMOC_OK;
+  if (ctx->stream) cudaStreamSynchronize(ctx->stream);
+  for (void *a : ctx->allocs)
+    if (a) cudaFree(a);
+  if (ctx->h_ntot) cudaFreeHost(ctx->h_ntot);
+  if (ctx->ev_ntot) cudaEventDestroy(ctx->ev_ntot);
+  if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
+  delete ctx;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_system(bromoc_ctx *ctx, const bromoc_system *q) {
+  if (!ctx || !q) return set_err(ctx, BROMOC_E_ARG, "set_system: null");
+  if (q->kbt <= 0.0 || q->dt <= 0.0)
+    return set_err(ctx, BROMOC_E_ARG, "set_system: kbt and dt must be positive");
+  KP &p = ctx->kp;
+  ctx->sys = *q;
+  p.shape = q->shape;
+  p.qcountion = q->qcountion;
+  p.lx = q->lx;
+  p.ly = q->ly;
+  p.lz = q->lz;
+  p.cx = q->cx;
+  p.cy = q->cy;
+  p.cz = q->cz;
+  p.rsphe = q->rsphe;
+  p.rsphe2 = q->rsphe * q->rsphe;
+  p.iecx = q->shape == BROMOC_ECYL ? 2.0 / q->lx : 0.0;
+  p.iecy = q->shape == BROMOC_ECYL ? 2.0 / q->ly : 0.0;
+  p.lx2p = q->cx + 0.5 * q->lx;  // shell_simul.f90:914-919
+  p.ly2p = q->cy + 0.5 * q->ly;
+  p.lz2p = q->cz + 0.5 * q->lz;
+  p.lx2m = q->cx - 0.5 * q->lx;
+  p.ly2m = q->cy - 0.5 * q->ly;
+  p.lz2m = q->cz - 0.5 * q->lz;
+  p.ikbt = 1.0 / q->kbt;
+  p.kbtdt = q->dt * p.ikbt;  // simul1.f90:342
+  p.dt = q->dt;
+  p.bdmax = q->bdmax;
+  ctx->have_sys = true;
+  if (ctx->have_types) {  // fact1a/fact2a depend on both (simul1.f90:345-348)
+    std::vector<double> f1(ctx->ntype + 1, 0.0), f2(ctx->ntype + 1, 0.0);
+    for (int i = 1; i <= ctx->ntype; ++i) {
+      f1[i] = ctx->diffusion[i] * p.kbtdt;
+      f2[i] = std::sqrt(2.0 * q->dt * ctx->diffusion[i]);
+    }
+    double *d1 = const_cast<double *>(p.fact1a), *d2 = const_cast<double *>(p.fact2a);
+    int rc = upload(ctx, &d1, f1.data(), f1.size());
+    if (!rc) rc = upload(ctx, &d2, f2.data(), f2.size());
+    p.fact1a = d1;
+    p.fact2a = d2;
+    if (rc) return rc;
+  }
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_types(bromoc_ctx *ctx, const bromoc_types *t) {
+  if (!ctx || !t || !t->nwtype || !t->cg || !t->diffusion)
+    return set_err(ctx, BROMOC_E_ARG, "set_types: null");
+  if (t->ntype < 1 || t->nttyp < 1 || t->nttyp > kMaxTypes || t->ndna < 0 ||
+      t->nold < 0 || t->nold > t->ntype)
+    return set_err(ctx, BROMOC_E_ARG, "set_types: bad sizes");
+  for (int i = t->nold; i < t->ntype; ++i)
+    if (t->nwtype[i] < 1 || t->nwtype[i] > t->nttyp)
+      return set_err(ctx, BROMOC_E_ARG, "set_types: nwtype out of range");
+  KP &p = ctx->kp;
+  ctx->ntype = p.ntype = t->ntype;
+  ctx->nold = p.nold = t->nold;
+  ctx->nttyp = p.nttyp = t->nttyp;
+  ctx->ndna = p.ndna = t->ndna;
+  ctx->diffusion.assign(t->ntype + 1, 0.0);
+  for (int i = 0; i < t->ntype; ++i) ctx->diffusion[i + 1] = t->diffusion[i];
+  int rc = upload1(ctx, &p.nwtype, t->nwtype, t->ntype);
+  if (!rc) rc = upload1(ctx, &p.cg, t->cg, t->ntype);
+  if (!rc) rc = upload1(ctx, &p.diffusion, t->diffusion, t->ntype);
+  if (rc) return rc;
+  int *w = nullptr;
+  if ((rc = dalloc(ctx, &w, t->nttyp + 1))) return rc;
+  CU(cudaMemset(w, 0, (t->nttyp + 1) * sizeof(int)));
+  p.warn = w;
+  ctx->have_types = true;
+  if (ctx->have_sys) return bromoc_gpu_set_system(ctx, &ctx->sys);
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
+  if (!ctx || !q) return set_err(ctx, BROMOC_E_ARG, "set_pairs: null");
+  if (!ctx->have_types) return set_err(ctx, BROMOC_E_STATE, "set_pairs before set_types");
+  const int ntc = q->ntc, nt = ctx->nttyp, ndna = ctx->ndna;
+  const int nion = nt - ndna;
+  if (ntc != (nt + ndna + 1) * nion / 2)
+    return set_err(ctx, BROMOC_E_ARG, "set_pairs: ntc %d != (nttyp+ndna+1)*nion/2", ntc);
+  if (!q->qchr || !q->qlj || !q->qsrpmf || !q->qefpot || !q->fct || !q->epp4 ||
+      !q->sgp2 || !q->c0 || !q->c1 || !q->c2 || !q->c3 || !q->c4)
+    return set_err(ctx, BROMOC_E_ARG, "set_pairs: null table");
+  KP &p = ctx->kp;
+  // packed pair index of every combined-type pair (nindex.f90:19-35)
+  std::vector<int> pidx((size_t)nt * nt, -1);
+  for (int a = 1; a <= nt; ++a)
+    for (int b = 1; b <= nt; ++b) {
+      if (a <= ndna && b <= ndna) continue;  // no site-site pair law
+      int maxi, mini;
+      if (a > b) {
+        maxi = a - ndna;
+        mini = b;
+      } else {
+        maxi = b - ndna;
+        mini = a;
+      }
+      int is = mini > ndna ? maxi * (maxi - 1) / 2 + mini - ndna + ndna * nion
+                           : (mini - 1) * nion + maxi;
+      pidx[(size_t)(a - 1) * nt + (b - 1)] = is - 1;
+    }
+  const bool anyef = [&] {
+    for (int k = 0; k < ntc; ++k)
+      if (q->qefpot[k]) return true;
+    return false;
+  }();
+  if (anyef && (!q->ep || !q->sc || !q->dm2 || !q->dmi || !q->nxi || q->cnt < 1 || q->res <= 0))
+    return set_err(ctx, BROMOC_E_ARG, "set_pairs: effective-potential tables missing");
+  // pieces per pair: up to the next pair's first piece
+  std::vector<int> npieces(ntc, 0);
+  for (int k = 0; k < ntc; ++k) {
+    if (!q->qefpot[k]) continue;
+    int next = q->cnt + 1;
+    for (int m = 0; m < ntc; ++m)
+      if (q->qefpot[m] && q->nxi[m] > q->nxi[k]) next = std::min(next, q->nxi[m]);
+    npieces[k] = next - q->nxi[k];
+    if (q->nxi[k] < 1 || npieces[k] < 1)
+      return set_err(ctx, BROMOC_E_ARG, "set_pairs: bad nxi for pair %d", k + 1);
+  }
+  std::vector<PairParam> pp(ntc);
+  std::vector<PairParamF> pf(ntc);
+  std::vector<float4> ep32(anyef ? q->cnt : 1, make_float4(0, 0, 0, 0));
+  for (int k = 0; k < ntc; ++k) {
+    PairParam &a = pp[k];
+    a = PairParam{};
+    a.flags = (q->qchr[k] ? kChr : 0) | (q->qlj[k] ? kLj : 0) |
+              (q->qsrpmf[k] ? kSrp : 0) | (q->qefpot[k] ? kEfp : 0);
+    a.fct = q->fct[k];
+    a.epp4 = q->epp4[k];
+    a.sgp2 = q->sgp2[k];
+    a.c0 = q->c0[k];
+    a.c1 = q->c1[k];
+    a.c2 = q->c2[k];
+    a.c3 = q->c3[k];
+    a.c4 = q->c4[k];
+    if (q->qefpot[k]) {
+      a.sc0 = q->sc[3 * k];
+      a.sc1 = q->sc[3 * k + 1];
+      a.sc2 = q->sc[3 * k + 2];
+      a.dm2lo = q->dm2[2 * k];
+      a.dm2hi = q->dm2[2 * k + 1];
+      a.dmi = q->dmi[k];
+      a.nxi = q->nxi[k] - 1;
+      a.npieces = npieces[k];
+      // local form about the bin start x_k = dmi + (k - nxi) res
+      for (int m = 0; m < npieces[k]; ++m) {
+        const int g = a.nxi + m;
+        const double xk = a.dmi + m * q->res;
+        const double p1 = q->ep[3 * g], p2 = q->ep[3 * g + 1], p3 = q->ep[3 * g + 2];
+        ep32[g] = make_float4((float)(p1 + xk * (p2 + xk * p3)),
+                              (float)(p2 + 2.0 * p3 * xk), (float)p3, (float)xk);
+      }
+    }
+    PairParamF &f = pf[k];
+    f.fct = (float)a.fct;
+    f.epp4 = (float)a.epp4;
+    f.sgp2 = (float)a.sgp2;
+    f.c0 = (float)a.c0;
+    f.c1 = (float)a.c1;
+    f.c2 = (float)a.c2;
+    f.c3 = (float)a.c3;
+    f.c4 = (float)a.c4;
+    f.sc0 = (float)a.sc0;
+    f.sc1 = (float)a.sc1;
+    f.sc2 = (float)a.sc2;
+    f.dm2lo = (float)a.dm2lo;
+    f.dm2hi = (float)a.dm2hi;
+    f.dmi = (float)a.dmi;
+    f.flags = a.flags | (a.npieces << 8);
+    f.nxi = a.nxi;
+  }
+  p.rth = q->rth;
+  p.srpx = q->srpx;
+  p.srpk = q->srpk;
+  p.srpy = q->srpy;
+  p.res = q->res;
+  p.ires = q->res > 0 ? 1.0 / q->res : 0.0;
+  p.cnt = anyef ? q->cnt : 0;
+  ctx->ntc = p.ntc = ntc;
+  PairParam *dpp = const_cast<PairParam *>(p.pp);
+  PairParamF *dpf = const_cast<PairParamF *>(p.ppf);
+  int *dpi = const_cast<int *>(p.pidx);
+  double *dep = const_cast<double *>(p.ep);
+  float4 *de32 = const_cast<float4 *>(p.ep32);
+  int rc = upload(ctx, &dpp, pp.data(), pp.size());
+  if (!rc) rc = upload(ctx, &dpf, pf.data(), pf.size());
+  if (!rc) rc = upload(ctx, &dpi, pidx.data(), pidx.size());
+  if (!rc) rc = upload(ctx, &dep, anyef ? q->ep : nullptr, anyef ? 3 * (size_t)q->cnt : 3);
+  if (!rc) rc = upload(ctx, &de32, ep32.data(), ep32.size());
+  p.pp = dpp;
+  p.ppf = dpf;
+  p.pidx = dpi;
+  p.ep = dep;
+  p.ep32 = de32;
+  if (rc) return rc;
+  ctx->have_pairs = true;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
+  if (!ctx || !s) return set_err(ctx, BROMOC_E_ARG, "set_sites: null");
+  if (s->nsites < 0 || s->nsites > 1024)
+    return set_err(ctx, BROMOC_E_ARG, "set_sites: nsites must be in [0, 1024]");
+  KP &p = ctx->kp;
+  p.nsites = s->nsites;
+  if (s->nsites == 0) return BROMOC_OK;
+  if (!s->typtyp || !s->charge || !s->stfree)
+    return set_err(ctx, BROMOC_E_ARG, "set_sites: null");
+  for (int i = 0; i < s->nsites; ++i)
+    if (s->typtyp[i] < 1 || s->typtyp[i] > ctx->ndna)
+      return set_err(ctx, BROMOC_E_ARG, "set_sites: typtyp out of range");
+  int *t = const_cast<int *>(p.typtyp);
+  double *c = const_cast<double *>(p.sitecharge);
+  uint8_t *f = const_cast<uint8_t *>(p.stfree);
+  int rc = upload(ctx, &t, s->typtyp, s->nsites);
+  if (!rc) rc = upload(ctx, &c, s->charge, s->nsites);
+  if (!rc) rc = upload(ctx, &f, s->stfree, s->nsites);
+  p.typtyp = t;
+  p.sitecharge = c;
+  p.stfree = f;
+  if (!rc && s->phiv_map) {
+    int *m = const_cast<int *>(p.site_map);
+    rc = upload(ctx, &m, s->phiv_map, s->nsites);
+    p.site_map = m;
+  }
+  return rc;
+}
+
+int bromoc_gpu_set_phix(bromoc_ctx *ctx, const bromoc_grid *g, const float *phix) {
+  if (!ctx || !grid_ok(g) || !phix) return set_err(ctx, BROMOC_E_ARG, "set_phix: bad grid");
+  KP &p = ctx->kp;
+  p.g1 = make_grid(*g);
+  float *d = const_cast<float *>(p.phix);
+  int rc = upload(ctx, &d, phix, (size_t)g->nclx * g->ncly * g->nclz);
+  p.phix = d;
+  if (!rc) p.qphix = 1;
+  return rc;
+}
+
+int bromoc_gpu_set_phiv(bromoc_ctx *ctx, const bromoc_grid *g, const int8_t *phiv,
+                        const bromoc_phiv_opts *o) {
+  if (!ctx || !grid_ok(g) || !phiv || !o || o->nmaps < 1)
+    return set_err(ctx, BROMOC_E_ARG, "set_phiv: bad arguments");
+  if (o->nmcden && !o->map_of_type)
+    return set_err(ctx, BROMOC_E_ARG, "set_phiv: nmcden needs map_of_type");
+  KP &p = ctx->kp;
+  p.g2 = make_grid(*g);
+  int8_t *d = const_cast<int8_t *>(p.phiv);
+  int rc = upload(ctx, &d, phiv, (size_t)o->nmaps * g->nclx * g->ncly * g->nclz);
+  p.phiv = d;
+  if (rc) return rc;
+  p.qtrln = o->trilinear != 0;
+  p.qnmcden = o->nmcden != 0;
+  p.svdw = o->svdw;
+  p.vzmin = o->vzmin;
+  p.vzmax = o->vzmax;
+  p.thold8 = o->thold8;
+  p.thold27 = o->thold27;
+  if (o->map_of_type) {
+    for (int i = ctx->nold; i < ctx->ntype; ++i)
+      if (o->map_of_type[i] < 0 || o->map_of_type[i] >= o->nmaps)
+        return set_err(ctx, BROMOC_E_ARG, "set_phiv: map_of_type out of range");
+    if ((rc = upload1(ctx, &p.phiv_map_of_type, o->map_of_type, ctx->ntype))) return rc;
+  }
+  p.qsvdw = o->scal != nullptr;
+  if (o->scal && (rc = upload1(ctx, &p.scal, o->scal, ctx->nttyp))) return rc;
+  p.qphiv = 1;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_rfpar(bromoc_ctx *ctx, const bromoc_grid *g, int32_t nmaps,
+                         const float *gsrfen, const float *greff, double reffac,
+                         const int32_t *map_of_type) {
+  if (!ctx || !grid_ok(g) || !gsrfen || !greff || nmaps < 1 || reffac < 0)
+    return set_err(ctx, BROMOC_E_ARG, "set_rfpar: bad arguments");
+  KP &p = ctx->kp;
+  p.g3 = make_grid(*g);
+  const size_t n = (size_t)nmaps * g->nclx * g->ncly * g->nclz;
+  float *a = const_cast<float *>(p.gsrfen), *b = const_cast<float *>(p.greff);
+  int rc = upload(ctx, &a, gsrfen, n);
+  if (!rc) rc = upload(ctx, &b, greff, n);
+  p.gsrfen = a;
+  p.greff = b;
+  if (rc) return rc;
+  p.sqrfac = std::sqrt(reffac);  // shell_simul.f90:2860
+  p.qrfpsin = map_of_type == nullptr;
+  if (map_of_type) {
+    for (int i = ctx->nold; i < ctx->ntype; ++i)
+      if (map_of_type[i] < 0 || map_of_type[i] >= nmaps)
+        return set_err(ctx, BROMOC_E_ARG, "set_rfpar: map_of_type out of range");
+    if ((rc = upload1(ctx, &p.rfpar_map_of_type, map_of_type, ctx->ntype))) return rc;
+  }
+  p.qrfpar = 1;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_membrane(bromoc_ctx *ctx, const bromoc_membrane *m) {
+  if (!ctx || !m || !m->ampl1 || !m->p1 || !m->ampl2 || !m->p2 || !m->rcylinder)
+    return set_err(ctx, BROMOC_E_ARG, "set_membrane: null");
+  if (!ctx->have_types) return set_err(ctx, BROMOC_E_STATE, "set_membrane before set_types");
+  KP &p = ctx->kp;
+  const int n = ctx->nttyp;
+  std::vector<double> p1a(n), p1b(n), p2a(n), p2b(n);
+  for (int i = 0; i < n; ++i) {
+    p1a[i] = m->p1[2 * i];
+    p1b[i] = m->p1[2 * i + 1];
+    p2a[i] = m->p2[2 * i];
+    p2b[i] = m->p2[2 * i + 1];
+  }
+  int rc = upload1(ctx, &p.ampl1, m->ampl1, n);
+  if (!rc) rc = upload1(ctx, &p.ampl2, m->ampl2, n);
+  if (!rc) rc = upload1(ctx, &p.rcyl, m->rcylinder, n);
+  if (!rc) rc = upload1(ctx, &p.p1a, p1a.data(), n, 1.0);
+  if (!rc) rc = upload1(ctx, &p.p1b, p1b.data(), n, 1.0);
+  if (!rc) rc = upload1(ctx, &p.p2a, p2a.data(), n, 1.0);
+  if (!rc) rc = upload1(ctx, &p.p2b, p2b.data(), n, 1.0);
+  if (rc) return rc;
+  p.qpore = m->qpore;
+  p.voltage = m->voltage;
+  p.afact = m->afact;
+  p.ikappa = m->ikappa;
+  p.ceps = m->ceps;
+  p.zmemb1 = m->zmemb1;
+  p.zmemb2 = m->zmemb2;
+  p.qmemb = 1;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_diffusion(bromoc_ctx *ctx, const bromoc_diffusion *d) {
+  if (!ctx || !d) return set_err(ctx, BROMOC_E_ARG, "set_diffusion: null");
+  if (!ctx->have_types) return set_err(ctx, BROMOC_E_STATE, "set_diffusion before set_types");
+  KP &p = ctx->kp;
+  int rc = upload1(ctx, &p.ampl3, d->ampl3, ctx->ntype);
+  if (!rc) rc = upload1(ctx, &p.p3, d->p3, ctx->ntype, 1.0);
+  if (rc) return rc;
+  p.plength2 = d->plength2;
+  p.pcenter = d->pcenter;
+  p.nspline = d->nspline;
+  if (d->nspline > 0) {
+    if (!d->xs || !d->ys || !d->b || !d->c || !d->d)
+      return set_err(ctx, BROMOC_E_ARG, "set_diffusion: spline arrays missing");
+    rc = upload1(ctx, &p.xs, d->xs, d->nspline);
+    if (!rc) rc = upload1(ctx, &p.ys, d->ys, d->nspline);
+    if (!rc) rc = upload1(ctx, &p.sb, d->b, d->nspline);
+    if (!rc) rc = upload1(ctx, &p.scc, d->c, d->nspline);
+    if (!rc) rc = upload1(ctx, &p.sd, d->d, d->nspline);
+    if (rc) return rc;
+  }
+  p.diff0 = d->diff0;
+  p.ibeta = d->ibeta;
+  p.diffcutoff = d->diffcutoff;
+  p.qproxdiff = d->diffcutoff > 0.0;
+  p.fact0n1 = d->fact0n1;
+  p.fact0n2 = d->fact0n2;
+  p.qdnafree = d->qdnafree;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_countions(bromoc_ctx *ctx, int32_t cntpts, const double *zcont) {
+  if (!ctx || cntpts < 0 || (cntpts > 0 && !zcont))
+    return set_err(ctx, BROMOC_E_ARG, "set_countions: bad arguments");
+  if (!ctx->have_types) return set_err(ctx, BROMOC_E_STATE, "set_countions before set_types");
+  KP &p = ctx->kp;
+  ctx->cntpts = p.cntpts = cntpts;
+  if (cntpts == 0) return BROMOC_OK;
+  double *z = const_cast<double *>(p.zcont);
+  int rc = upload(ctx, &z, zcont, cntpts);
+  p.zcont = z;
+  const size_t n = (size_t)(ctx->ntype - ctx->nold) * cntpts;
+  if (!rc) rc = upload<int>(ctx, &p.nforward, nullptr, n);
+  if (!rc) rc = upload<int>(ctx, &p.nbackward, nullptr, n);
+  if (rc) return rc;
+  CU(cudaMemset(p.nforward, 0, n * sizeof(int)));
+  CU(cudaMemset(p.nbackward, 0, n * sizeof(int)));
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_buffers(bromoc_ctx *ctx, const bromoc_buffers *b) {
+  if (!ctx || !b) return set_err(ctx, BROMOC_E_ARG, "set_buffers: null");
+  if (b->nbuffer < 0 || b->nbuffer > kMaxBuffers)
+    return set_err(ctx, BROMOC_E_ARG, "set_buffers: nbuffer must be in [0, %d]", kMaxBuffers);
+  KP &p = ctx->kp;
+  const int n = b->nbuffer;
+  ctx->nbuffer = p.nbuffer = n;
+  if (n == 0) return BROMOC_OK;
+  if (!b->ibfftyp || !b->avnum || !b->mu || !b->kb || !b->lzmin || !b->lzmax ||
+      !b->qbufferbias || !b->nat || !b->ntotat)
+    return set_err(ctx, BROMOC_E_ARG, "set_buffers: null array");
+  int rc = upload1(ctx, &p.ibfftyp, b->ibfftyp, n);
+  if (!rc) rc = upload1(ctx, &p.avnum, b->avnum, n);
+  if (!rc) rc = upload1(ctx, &p.mu, b->mu, n);
+  if (!rc) rc = upload1(ctx, &p.kbb, b->kb, n);
+  if (!rc) rc = upload1(ctx, &p.lzmin, b->lzmin, n);
+  if (!rc) rc = upload1(ctx, &p.lzmax, b->lzmax, n);
+  if (!rc) rc = upload1(ctx, &p.rmin, b->rmin, n);
+  if (!rc) rc = upload1(ctx, &p.rmax, b->rmax, n);
+  if (!rc) rc = upload1(ctx, &p.qbufferbias, b->qbufferbias, n);
+  if (!rc) rc = upload<int>(ctx, &p.prob, nullptr, (size_t)n * (p.cap + 1));
+  if (rc) return rc;
+  CU(cudaMemset(p.prob, 0, (size_t)n * (p.cap + 1) * sizeof(int)));
+  DevState h{};
+  CU(cudaMemcpy(&h, p.st, sizeof h, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < n; ++i) {
+    h.nat[i] = b->nat[i];
+    h.ntotat[i] = b->ntotat[i];
+    h.ninsert[i] = 0;
+    h.nremove[i] = 0;
+  }
+  CU(cudaMemcpy(p.st, &h, sizeof h, cudaMemcpyHostToDevice));
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
+                             int32_t nfix, const double *x, const double *y,
+                             const double *z, const int32_t *typei,
+                             const int32_t *ibuffer) {
+  if (!ctx || !x || !y || !z || !typei) return set_err(ctx, BROMOC_E_ARG, "set_particles: null");
+  KP &p = ctx->kp;
+  if (ntot < 0 || ntot > p.cap)
+    return set_err(ctx, BROMOC_E_CAPACITY, "set_particles: ntot %d exceeds capacity %d", ntot, p.cap);
+  if (nsites != p.nsites)
+    return set_err(ctx, BROMOC_E_STATE, "set_particles: nsites %d differs from set_sites (%d)",
+                   nsites, p.nsites);
+  if (nfix < 0 || nsites + nfix > ntot)
+    return set_err(ctx, BROMOC_E_ARG, "set_particles: bad nfix");
+  if (!ctx->have_types) return set_err(ctx, BROMOC_E_STATE, "set_particles before set_types");
+  for (int i = nsites; i < ntot; ++i) {
+    const int t = typei[i] < 0 ? -typei[i] : typei[i];
+    if (t <= ctx->nold || t > ctx->ntype)
+      return set_err(ctx, BROMOC_E_ARG, "set_particles: typei(%d) = %d is not an ion type",
+                     i + 1, typei[i]);
+  }
+  CU(cudaStreamSynchronize(ctx->stream));
+  p.nfix = nfix;
+  const size_t n = (size_t)std::max(ntot, 1);
+  CU(cudaMemcpyAsync(p.x, x, ntot * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(p.y, y, ntot * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(p.z, z, ntot * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(p.typei, typei, ntot * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  if (ibuffer)
+    CU(cudaMemcpyAsync(p.ibuffer, ibuffer, ntot * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  else
+    CU(cudaMemsetAsync(p.ibuffer, 0, n * sizeof(int), ctx->stream));
+  *ctx->h_ntot = ntot;
+  CU(cudaMemcpyAsync(&p.st->ntot, ctx->h_ntot, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->ntot_known = ntot;
+  ctx->attempts_at_known = ctx->attempts_total;
+  ctx->rb_pending = false;
+  ctx->have_forces = false;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_get_particles(bromoc_ctx *ctx, int32_t *ntot, double *x, double *y,
+                             double *z, int32_t *typei, int32_t *ibuffer) {
+  if (!ctx) return BROMOC_E_ARG;
+  int rc = sync_ntot(ctx);
+  if (rc) return rc;
+  const int n = ctx->ntot_known;
+  KP &p = ctx->kp;
+  if (ntot) *ntot = n;
+  if (x) CU(cudaMemcpyAsync(x, p.x, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (y) CU(cudaMemcpyAsync(y, p.y, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (z) CU(cudaMemcpyAsync(z, p.z, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  if (typei) CU(cudaMemcpyAsync(typei, p.typei, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  if (ibuffer)
+    CU(cudaMemcpyAsync(ibuffer, p.ibuffer, n * sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_energy(bromoc_ctx *ctx, uint32_t terms, int32_t qforces, double *fx,
+                      double *fy, double *fz, double *eterms, int32_t *warn) {
+  if (!ctx) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  KP &p = ctx->kp;
+  EnergyPlan plan{};
+  AssembleFlags fl{};
+  if ((rc = plan_energy(ctx, terms, true, plan, fl))) return rc;
+  CU(cudaMemsetAsync(p.warn, 0, (ctx->nttyp + 1) * sizeof(int), ctx->stream));
+  launch_energy(p, plan, terms, qforces, ctx->stream);
+  launch_assemble(p, plan.ntot_ub, fl, 0, 0, 0, 0, ctx->stream);
+  CU(cudaGetLastError());
+  if ((rc = sync_ntot(ctx))) return rc;
+  const int n = ctx->ntot_known;
+  if (eterms)
+    CU(cudaMemcpyAsync(eterms, p.eterms, kNTerms * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  if (qforces) {
+    if (fx) CU(cudaMemcpyAsync(fx, p.fx, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (fy) CU(cudaMemcpyAsync(fy, p.fy, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    if (fz) CU(cudaMemcpyAsync(fz, p.fz, n * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  }
+  if (warn)
+    CU(cudaMemcpyAsync(warn, p.warn + 1, ctx->nttyp * sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_forces = qforces != 0;
+  return check_device_err(ctx);
+}
+
+int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj, double zj,
+                        int32_t jtype, int32_t j, double *dener) {
+  if (!ctx || !dener) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if ((rc = sync_ntot(ctx))) return rc;
+  KP &p = ctx->kp;
+  const int ntot = ctx->ntot_known;
+  if (j < 1 || j > ntot + 1) return set_err(ctx, BROMOC_E_ARG, "interact: j out of range");
+  if (j == ntot + 1 && ntot + 1 > p.cap)
+    return set_err(ctx, BROMOC_E_CAPACITY, "interact: no room for the trial slot");
+  const bool beion = j > p.nsites;
+  if (beion && (jtype <= ctx->nold || jtype > ctx->ntype))
+    return set_err(ctx, BROMOC_E_ARG, "interact: jtype %d is not an ion type", jtype);
+  Trial t{};
+  t.valid = 1;
+  t.insert = j == ntot + 1;
+  t.itype = jtype;
+  t.j = j;
+  t.x = xj;
+  t.y = yj;
+  t.z = zj;
+  CU(cudaMemcpyAsync(p.trial, &t, sizeof t, cudaMemcpyHostToDevice, ctx->stream));
+  launch_interact(p, ntot, terms, 1, ctx->d_dener, ctx->stream);
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(dener, ctx->d_dener, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return check_device_err(ctx);
+}
+
+int bromoc_gpu_dynamics(bromoc_ctx *ctx, int32_t variant, uint64_t seed, uint64_t step) {
+  if (!ctx) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (!ctx->have_forces)
+    return set_err(ctx, BROMOC_E_STATE, "dynamics: call energy with forces first");
+  if (variant < 0 || variant > 3) return set_err(ctx, BROMOC_E_ARG, "dynamics: bad variant");
+  KP &p = ctx->kp;
+  if (variant == BROMOC_DYN2 && p.nspline < 2)
+    return set_err(ctx, BROMOC_E_STATE, "dynamics2 needs a PROFILE spline");
+  AssembleFlags fl{};  // forces already assembled into fx,fy,fz: re-add nothing
+  // k_assemble starts from ffield; with all partial flags cleared and ffield
+  // holding the assembled forces the update uses exactly fx,fy,fz.
+  CU(cudaMemcpyAsync(p.ffield, p.fx, p.cap * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
+  CU(cudaMemcpyAsync(p.ffield + p.cap, p.fy, p.cap * sizeof(double), cudaMemcpyDeviceToDevice,
+                     ctx->stream));
+  CU(cudaMemcpyAsync(p.ffield + 2 * (size_t)p.cap, p.fz, p.cap * sizeof(double),
+                     cudaMemcpyDeviceToDevice, ctx->stream));
+  launch_assemble(p, ntot_ub(ctx), fl, 1, variant, seed, step, ctx->stream);
+  CU(cudaGetLastError());
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->have_forces = false;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_t nsteps,
+                        uint64_t seed, uint64_t step0, double *eterms) {
+  if (!ctx) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (variant < 0 || variant > 3) return set_err(ctx, BROMOC_E_ARG, "bd_steps: bad variant");
+  if (nsteps < 0) return set_err(ctx, BROMOC_E_ARG, "bd_steps: nsteps < 0");
+  KP &p = ctx->kp;
+  if (variant == BROMOC_DYN2 && p.nspline < 2)
+    return set_err(ctx, BROMOC_E_STATE, "dynamics2 needs a PROFILE spline");
+  if (variant == BROMOC_DYN3 && !p.qproxdiff)
+    return set_err(ctx, BROMOC_E_STATE, "dynamics3 needs PROXDIFF (diffcutoff > 0)");
+  EnergyPlan plan{};
+  AssembleFlags fl{};
+  for (int k = 0; k < nsteps; ++k) {
+    const bool last = k + 1 == nsteps;
+    if ((rc = plan_energy(ctx, terms, last && eterms, plan, fl))) return rc;
+    launch_energy(p, plan, terms, 1, ctx->stream);
+    launch_assemble(p, plan.ntot_ub, fl, 1, variant, seed, step0 + k, ctx->stream);
+  }
+  CU(cudaGetLastError());
+  ctx->have_forces = false;
+  if (eterms && nsteps > 0) {
+    CU(cudaMemcpyAsync(eterms, p.eterms, kNTerms * sizeof(double), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    return check_device_err(ctx);
+  }
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_t nsteps,
+                             uint64_t seed, uint64_t step0, int32_t ntot, int32_t nsites,
+                             int32_t nfix, double *x, double *y, double *z,
+                             const int32_t *typei, double *eterms) {
+  if (!ctx || !x || !y || !z || !typei) return set_err(ctx, BROMOC_E_ARG, "bd_steps_host: null");
+  int rc = bromoc_gpu_set_particles(ctx, ntot, nsites, nfix, x, y, z, typei, nullptr);
+  if (!rc) rc = bromoc_gpu_bd_steps(ctx, terms, variant, nsteps, seed, step0, eterms);
+  if (!rc) {
+    KP &p = ctx->kp;
+    CU(cudaMemcpyAsync(x, p.x, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(y, p.y, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaMemcpyAsync(z, p.z, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+  return rc;
+}
+
+int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t seed,
+                     uint64_t cycle, double *dener_sum) {
+  if (!ctx) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  KP &p = ctx->kp;
+  if (ngcmc < 0 || cycle < 1) return set_err(ctx, BROMOC_E_ARG, "grand: bad ngcmc or cycle");
+  if (p.nbuffer < 1) return set_err(ctx, BROMOC_E_STATE, "grand: no buffers");
+  CU(cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), ctx->stream));
+  for (int a = 0; a < ngcmc; ++a) {
+    const int ub = ntot_ub(ctx);
+    launch_gcmc_attempt(p, ub, terms, seed, cycle, (uint32_t)a, ctx->stream);
+    ctx->attempts_total += 1;
+  }
+  CU(cudaGetLastError());
+  if (!ctx->rb_pending) {  // refresh the ntot bound without blocking
+    CU(cudaMemcpyAsync(ctx->h_ntot, &p.st->ntot, sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CU(cudaEventRecord(ctx->ev_ntot, ctx->stream));
+    ctx->rb_pending = true;
+    ctx->rb_attempts = ctx->attempts_total;
+  }
+  ctx->have_forces = false;
+  if (dener_sum) {
+    CU(cudaMemcpyAsync(ctx->h_ntot + 2, &p.st->dener_sum, sizeof(double),
+                       cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    std::memcpy(dener_sum, ctx->h_ntot + 2, sizeof(double));
+    return check_device_err(ctx);
+  }
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_get_buffers(bromoc_ctx *ctx, int32_t *nat, int32_t *ninsert, int32_t *nremove,
+                           int32_t *prob) {
+  if (!ctx) return BROMOC_E_ARG;
+  KP &p = ctx->kp;
+  DevState h{};
+  CU(cudaStreamSynchronize(ctx->stream));
+  CU(cudaMemcpy(&h, p.st, sizeof h, cudaMemcpyDeviceToHost));
+  for (int i = 0; i < ctx->nbuffer; ++i) {
+    if (nat) nat[i] = h.nat[i];
+    if (ninsert) ninsert[i] = h.ninsert[i];
+    if (nremove) nremove[i] = h.nremove[i];
+  }
+  if (prob && ctx->nbuffer > 0)
+    CU(cudaMemcpy(prob, p.prob, (size_t)ctx->nbuffer * (p.cap + 1) * sizeof(int),
+                  cudaMemcpyDeviceToHost));
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_get_countions(bromoc_ctx *ctx, int32_t *nf, int32_t *nb) {
+  if (!ctx) return BROMOC_E_ARG;
+  KP &p = ctx->kp;
+  const size_t n = (size_t)(ctx->ntype - ctx->nold) * ctx->cntpts;
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (n == 0) return BROMOC_OK;
+  if (nf) CU(cudaMemcpy(nf, p.nforward, n * sizeof(int), cudaMemcpyDeviceToHost));
+  if (nb) CU(cudaMemcpy(nb, p.nbackward, n * sizeof(int), cudaMemcpyDeviceToHost));
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_get_dids(bromoc_ctx *ctx, double *dids) {
+  if (!ctx || !dids) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if ((rc = sync_ntot(ctx))) return rc;
+  CU(cudaMemcpy(dids, ctx->kp.dids, 5 * (size_t)ctx->ntot_known * sizeof(double),
+                cudaMemcpyDeviceToHost));
+  return BROMOC_OK;
+}
+
+}  // extern "C"

@@ -1,0 +1,133 @@
+// Shared device-side definitions of the GB300 cg-gcmc-bd inner loop.
+//
+// Layout in HBM (one context):
+//   particles  SoA double x,y,z [cap], int typei,ibuffer [cap]; sites first,
+//              then fixed ions, then mobile ions (energy.mono.f90:120-123)
+//   forces     double fx,fy,fz [cap] (assembled), partial-force scratch
+//   pair laws  PairParam[ntc] + pair index table [nttyp*nttyp] (nindex.f90)
+//   tables     ep double[3*cnt] (reference form) and a float4 local form
+//   maps       phix float, phiv int8, gsrfen/greff float; z fastest
+//   live state DevState {ntot, nat[], counters, error flag}: device-resident
+//              so that GCMC insertions/deletions need no host round trip.
+#pragma once
+#include <cstdint>
+#include <cuda_runtime.h>
+
+namespace bgpu {
+
+constexpr double kPi = 3.14159265358979323846264338327950288419716939937510;
+constexpr double kTwoPi = 2.0 * kPi;
+constexpr double kRsmall = 1E-3;  // constamod.f90:83
+constexpr int kNTerms = 14;       // BROMOC_NTERMS
+constexpr int kMaxBuffers = 64;
+constexpr int kMaxTypes = 64;
+
+// error flags raised by kernels (bit mask in DevState::err)
+enum : int {
+  kErrCapacity = 1,     // an insertion would exceed capacity
+  kErrTableIndex = 2,   // an effective-potential piece index out of range
+  kErrFind = 4,         // GCMC deletion could not find the particle
+};
+
+// packed pair-law switches
+enum : int { kChr = 1, kLj = 2, kSrp = 4, kEfp = 8 };
+
+struct PairParam {
+  double fct, epp4, sgp2;
+  double c0, c1, c2, c3, c4;
+  double sc0, sc1, sc2;     // core a/r^12 + b, tail a/r^6
+  double dm2lo, dm2hi, dmi;
+  int flags;
+  int nxi;                  // 0-based first piece
+  int npieces;
+  int pad;
+};
+
+// Device-resident live counters of one context.
+struct DevState {
+  int ntot;
+  int err;
+  int nat[kMaxBuffers];
+  int ninsert[kMaxBuffers];
+  int nremove[kMaxBuffers];
+  int ntotat[kMaxBuffers];
+  double dener_sum;         // accumulated GCMC energy change
+};
+
+// GCMC trial of one attempt (written by the proposal kernel).
+struct Trial {
+  int valid;                // 0: attempt rejected before INTERACT
+  int insert;               // 1 insertion, 0 deletion
+  int ib;                   // 1-based buffer
+  int itype;                // ion type
+  int j;                    // 1-based slot (ntot+1 on insertion)
+  int draw;                 // next uniform draw index of the attempt
+  double x, y, z;
+};
+
+// ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
+__host__ __device__ inline void philox4x32_10(uint32_t c0, uint32_t c1,
+                                              uint32_t c2, uint32_t c3,
+                                              uint32_t k0, uint32_t k1,
+                                              uint32_t out[4]) {
+#pragma unroll
+  for (int r = 0; r < 10; ++r) {
+#ifdef __CUDA_ARCH__
+    uint32_t hi0 = __umulhi(0xD2511F53u, c0), lo0 = 0xD2511F53u * c0;
+    uint32_t hi1 = __umulhi(0xCD9E8D57u, c2), lo1 = 0xCD9E8D57u * c2;
+#else
+    uint64_t a = (uint64_t)0xD2511F53u * c0, b = (uint64_t)0xCD9E8D57u * c2;
+    uint32_t hi0 = (uint32_t)(a >> 32), lo0 = (uint32_t)a;
+    uint32_t hi1 = (uint32_t)(b >> 32), lo1 = (uint32_t)b;
+#endif
+    uint32_t n0 = hi1 ^ c1 ^ k0, n2 = hi0 ^ c3 ^ k1;
+    c0 = n0;
+    c1 = lo1;
+    c2 = n2;
+    c3 = lo0;
+    k0 += 0x9E3779B9u;
+    k1 += 0xBB67AE85u;
+  }
+  out[0] = c0;
+  out[1] = c1;
+  out[2] = c2;
+  out[3] = c3;
+}
+
+__host__ __device__ inline double u01(uint32_t w) { return (double)w * 0x1p-32; }
+
+// Box-Muller, cosine branch (rgauss.f90:24): uniform a -> angle,
+// 1 - uniform b -> radius.
+__device__ inline double box_muller(uint32_t wa, uint32_t wb) {
+  return cos(u01(wa) * kTwoPi) * sqrt(-2.0 * log(1.0 - u01(wb)));
+}
+
+// BD noise: 3 Gaussians of particle slot `slot` at step `step`.
+__device__ inline void bd_noise3(uint64_t seed, uint64_t step, uint32_t slot,
+                                 double g[3]) {
+  uint32_t w[4];
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const uint32_t s2 = (uint32_t)step,
+                 s3 = ((uint32_t)(step >> 32) & 0x00FFFFFFu) | (1u << 24);
+  philox4x32_10(slot, 0u, s2, s3, k0, k1, w);
+  g[0] = box_muller(w[0], w[1]);
+  g[1] = box_muller(w[2], w[3]);
+  philox4x32_10(slot, 1u, s2, s3, k0, k1, w);
+  g[2] = box_muller(w[0], w[1]);
+}
+
+// GCMC uniform draw `draw` of attempt `attempt` of cycle `cycle`.
+__host__ __device__ inline double gcmc_uniform(uint64_t seed, uint64_t cycle,
+                                               uint32_t attempt, uint32_t draw) {
+  uint32_t w[4];
+  philox4x32_10(attempt, draw >> 2, (uint32_t)cycle,
+                ((uint32_t)(cycle >> 32) & 0x00FFFFFFu) | (2u << 24),
+                (uint32_t)seed, (uint32_t)(seed >> 32), w);
+  return u01(w[draw & 3]);
+}
+
+__host__ __device__ inline double fsign(double a, double b) {
+  return b >= 0.0 ? fabs(a) : -fabs(a);
+}
+
+}  // namespace bgpu

@@ -1,0 +1,38 @@
+// Host-side launch interface between the C ABI (api.cu) and the kernels.
+#pragma once
+#include "kparams.cuh"
+
+namespace bgpu {
+
+struct EnergyPlan {
+  int ntot_ub;        // host upper bound of the device-resident ntot
+  int nchunk_ii;      // source chunks of the ion-ion kernel
+  int nchunk_rf;      // source chunks of the RFPAR cross kernel
+  bool fp32;
+  bool reduce_energy; // launch the final energy reduction
+};
+
+struct AssembleFlags {
+  int ii, is, rf;     // which partial-force buffers are valid
+  int nchunk_ii, nchunk_rf;
+};
+
+// energy.cu
+int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
+                  int qforces, cudaStream_t stream);
+int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask);
+
+// dyn.cu: force assembly, optionally fused with the BD update
+void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,
+                     int do_bd, int variant, uint64_t seed, uint64_t step,
+                     cudaStream_t stream);
+
+// gcmc.cu
+void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
+                     double *dener_dev, cudaStream_t stream);
+void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask,
+                         uint64_t seed, uint64_t cycle, uint32_t attempt,
+                         cudaStream_t stream);
+int interact_slots(int ntot_ub);
+
+}  // namespace bgpu

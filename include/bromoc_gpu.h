@@ -1,0 +1,302 @@
+/*
+ * bromoc_gpu.h -- C ABI of the GB300 (sm_103a) cg-gcmc-bd inner loop.
+ *
+ * The library replaces the hot subroutines of BROMOC's cg-gcmc-bd simulator
+ * (Fortran 90, module-global state, no argument lists) with a context object
+ * that holds the same state on the device.  Every entry point returns an int
+ * status (BROMOC_OK == 0) and never aborts the host process; the message of
+ * the last failure is available from bromoc_gpu_last_error().
+ *
+ * Conventions mirror the reference:
+ *   - particle order: DNA sites 1..nsites, fixed ions nsites+1..nsites+nfix,
+ *     mobile ions nsites+nfix+1..ntot (cg-gcmc-bd/src/energy.mono.f90:120-123);
+ *   - typei(i) is the signed ion type, sign = side of cz
+ *     (cg-gcmc-bd/src/grand.f90:73-74, count.f90:58-62);
+ *   - units: Angstrom, ps, kcal/mol, e;  "real" == double;
+ *   - pair parameter tables are indexed by the packed pair index "is" of
+ *     cg-gcmc-bd/src/nindex.f90:19-35 (1-based in the tables passed here).
+ *
+ * Arrays passed in are host memory and are copied; the caller keeps
+ * ownership.  One host thread per context.
+ */
+#ifndef BROMOC_GPU_H
+#define BROMOC_GPU_H
+
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define BROMOC_ABI_VERSION 1
+
+/* ---- status codes ------------------------------------------------------ */
+enum {
+  BROMOC_OK = 0,
+  BROMOC_E_ARG = 1,      /* bad argument (null pointer, size out of range)   */
+  BROMOC_E_STATE = 2,    /* call order: a required set_* call is missing      */
+  BROMOC_E_CUDA = 3,     /* a CUDA runtime call failed                        */
+  BROMOC_E_CAPACITY = 4, /* ntot would exceed the context capacity (datom)    */
+  BROMOC_E_NOMEM = 5,    /* device allocation failed                          */
+  BROMOC_E_DEVICE = 6    /* a kernel reported an error flag (e.g. bad index)  */
+};
+
+/* ---- energy term slots (grandmod.f90:56, gsbpmod.f90:173) -------------- */
+enum {
+  BROMOC_ENER = 0,     /* total                                            */
+  BROMOC_EELEC,        /* ion-ion Coulomb                                  */
+  BROMOC_EVDW,         /* ion-ion Lennard-Jones                            */
+  BROMOC_ESRPMF,       /* ion-ion short-range PMF                          */
+  BROMOC_EEFPOT,       /* ion-ion tabulated effective potential            */
+  BROMOC_EQQMX,        /* ion-site Coulomb                                 */
+  BROMOC_EVDWMX,       /* ion-site Lennard-Jones                           */
+  BROMOC_ESRPMFMX,     /* ion-site short-range PMF                         */
+  BROMOC_EEFPOTMX,     /* ion-site tabulated effective potential           */
+  BROMOC_EMEMB,        /* membrane (membrane.f90)                          */
+  BROMOC_EGSBPA,       /* static field (staticf1.f90)                      */
+  BROMOC_EGSBPB,       /* reaction field (rfpar.f90 copies erfpar here)    */
+  BROMOC_EVDWGD,       /* grid repulsion (vdwgd1trln/spln.f90)             */
+  BROMOC_ERFPAR,       /* reaction-field parameters (rfpar.f90)            */
+  BROMOC_NTERMS
+};
+
+/* ---- term switches (the ENERGY/INTERACT/TEST keyword masks,
+ *      shell_simul.f90:1428-1465) ----------------------------------------- */
+enum {
+  BROMOC_M_NONBOND = 1u << 0, /* Qnonbond: ion-ion and ion-site pairs      */
+  BROMOC_M_MEMB = 1u << 1,    /* Qmemb                                     */
+  BROMOC_M_PHIX = 1u << 2,    /* Qphix                                     */
+  BROMOC_M_PHIV = 1u << 3,    /* Qphiv                                     */
+  BROMOC_M_RFPAR = 1u << 4,   /* Qrfpar                                    */
+  BROMOC_M_ALL = 0x1fu
+};
+
+enum { BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2 };
+
+/* pair arithmetic: FP64 mirrors the reference's -fdefault-real-8 build;
+ * FP32 evaluates pair laws in single precision with double accumulation. */
+enum { BROMOC_FP64 = 0, BROMOC_FP32 = 1 };
+
+/* BD update variants: dynamics0 (uniform D), dynamics1 (z-switch D,
+ * DIFFUSION), dynamics2 (spline D(z), PROFILE), dynamics3 (DNA-proximity D,
+ * PROXDIFF) -- simul1.f90:369-379. */
+enum { BROMOC_DYN0 = 0, BROMOC_DYN1 = 1, BROMOC_DYN2 = 2, BROMOC_DYN3 = 3 };
+
+/* ---- parameter blocks --------------------------------------------------- */
+
+/* SYSTEM + SIMUL scalars: shell_simul.f90:782-947, 1198-1413. */
+typedef struct bromoc_system {
+  int32_t shape;         /* BROMOC_BOX / BROMOC_SPHERE / BROMOC_ECYL          */
+  int32_t qcountion;     /* count z-plane crossings (countions.f90)           */
+  double lx, ly, lz;     /* box edges, or ellipse diameters + length (ECYL)   */
+  double cx, cy, cz;     /* system centre                                     */
+  double rsphe;          /* sphere radius (SPHERE)                            */
+  double temp;           /* K                                                 */
+  double kbt;            /* kcal/mol: kboltz*temp/kcalmol (shell_simul:865)   */
+  double cdie;           /* solvent dielectric                                */
+  double dt;             /* ps                                                */
+  double bdmax;          /* per-component BD displacement clamp (Angstrom)    */
+} bromoc_system;
+
+/* Ion types (PARTICLES) and combined types (reasig.f90). */
+typedef struct bromoc_types {
+  int32_t ntype;             /* typei values are +-[nold+1, ntype]           */
+  int32_t nold;              /* types defined before PARTICLES (DNA)         */
+  int32_t nttyp;             /* combined types: DNA site types + ion types   */
+  int32_t ndna;              /* combined types 1..ndna are DNA site types    */
+  const int32_t *nwtype;     /* [ntype] ion type -> combined type (1-based)  */
+  const double *cg;          /* [ntype] charge (e)                           */
+  const double *diffusion;   /* [ntype] diffusion constant (A^2/ps)          */
+} bromoc_types;
+
+/* Pair laws: Coulomb (fct), LJ 12-6 (epp4, sgp2), SRPMF (c0..c4) and the
+ * tabulated effective potential (efpmod).  All arrays indexed by "is". */
+typedef struct bromoc_pairs {
+  int32_t ntc;               /* number of packed pair indices               */
+  const uint8_t *qchr, *qlj, *qsrpmf, *qefpot;   /* [ntc] law switches       */
+  const double *fct;         /* [ntc] celec*qi*qj/cdie                       */
+  const double *epp4;        /* [ntc] 4*eps                                  */
+  const double *sgp2;        /* [ntc] sigma^2                                */
+  const double *c0, *c1, *c2, *c3, *c4; /* [ntc] SRPMF, c2 already 1/c2      */
+  double rth;                /* SRPMF cutoff SQUARED (shell_simul:1686)     */
+  double srpx, srpk, srpy;   /* SRPMF taper (shell_simul:1683-1685)         */
+  /* tabulated effective potential (efpmod.f90, polynom.f90:172-254) */
+  int32_t cnt;               /* number of quadratic pieces                   */
+  const double *ep;          /* [3*cnt] (p1,p2,p3) of piece k at ep[3k..]    */
+  const double *sc;          /* [3*ntc] core a/r^12+b and tail a/r^6 consts  */
+  const double *dm2;         /* [2*ntc] (mindist^2, maxdist^2)               */
+  const double *dmi;         /* [ntc] mindist                                */
+  const int32_t *nxi;        /* [ntc] 1-based first piece of the pair        */
+  double res;                /* table spacing                                */
+} bromoc_pairs;
+
+/* DNA interaction sites (NUCLEOTIDES). */
+typedef struct bromoc_sites {
+  int32_t nsites;
+  const int32_t *typtyp;     /* [nsites] combined type 1..ndna               */
+  const double *charge;      /* [nsites] cgnuc for 'P' sites, else 0         */
+  const uint8_t *stfree;     /* [nsites] site moves (not FIXSITE)            */
+  const int32_t *phiv_map;   /* [nsites] nmcden repulsion map, or NULL       */
+} bromoc_sites;
+
+/* Grid header of a PB map file: readphi.f90:43-52 (z fastest, x slowest). */
+typedef struct bromoc_grid {
+  int32_t nclx, ncly, nclz;
+  double dcel;
+  double xbcen, ybcen, zbcen;
+} bromoc_grid;
+
+/* Repulsion map options: GSBP phiv keywords, shell_simul.f90:2703-2777. */
+typedef struct bromoc_phiv_opts {
+  int32_t nmaps;             /* 1, or one map per type under nmcden          */
+  int32_t trilinear;         /* 1 = vdwgd*trln, 0 = vdwgd*spln (bspline)     */
+  int32_t nmcden;            /* per-type maps                                */
+  double svdw, vzmin, vzmax, thold8, thold27;
+  const int32_t *map_of_type;/* [ntype] 0-based map per ion type (nmcden)   */
+  const double *scal;        /* [nttyp] SVDW scale per combined type or NULL */
+} bromoc_phiv_opts;
+
+/* Membrane (MEMBRANE + SYSTEM volt/ionic), shell_simul.f90:1563-1669. */
+typedef struct bromoc_membrane {
+  int32_t qpore;
+  double voltage;            /* kcal/mol/e (volt*Coulomb/kcalmol)            */
+  double afact, ikappa, ceps, zmemb1, zmemb2;
+  const double *ampl1;       /* [nttyp]                                      */
+  const double *p1;          /* [2*nttyp] (pmemb, 1/pmemb)                   */
+  const double *ampl2;       /* [nttyp]                                      */
+  const double *p2;          /* [2*nttyp] (ppore, 1/ppore)                   */
+  const double *rcylinder;   /* [nttyp]                                      */
+} bromoc_membrane;
+
+/* Space-dependent diffusion models and DNA-site BD factors. */
+typedef struct bromoc_diffusion {
+  double plength2, pcenter;  /* DIFFUSION: half pore length, pore centre     */
+  const double *ampl3;       /* [ntype] lowfraction                          */
+  const double *p3;          /* [ntype] switchlength                         */
+  int32_t nspline;           /* PROFILE cubic spline D(z)/D0                 */
+  const double *xs, *ys, *b, *c, *d;
+  double diff0, ibeta, diffcutoff;   /* PROXDIFF                             */
+  double fact0n1, fact0n2;   /* DNA sites: diffnuc*kbtdna*dt, sqrt(2 dt D)   */
+  int32_t qdnafree;          /* DNA not clamped to the system               */
+} bromoc_diffusion;
+
+/* GCMC buffers (BUFFERS), grandmod.f90:41-47. */
+typedef struct bromoc_buffers {
+  int32_t nbuffer;
+  const int32_t *ibfftyp;    /* [nbuffer] ion type                           */
+  const double *avnum, *mu, *kb, *lzmin, *lzmax, *rmin, *rmax;
+  const uint8_t *qbufferbias;
+  const int32_t *nat;        /* [nbuffer] ions currently in the buffer       */
+  const int32_t *ntotat;     /* [nbuffer] running total used by kb bias      */
+} bromoc_buffers;
+
+typedef struct bromoc_ctx bromoc_ctx;
+
+/* ---- context -------------------------------------------------------------
+ * capacity: maximum ntot (the reference's static datom = 23000,
+ *           grandmod.f90:24); precision: BROMOC_FP64 or BROMOC_FP32;
+ * stream:   cudaStream_t to launch on (NULL = a stream owned by the ctx).   */
+int bromoc_gpu_create(int32_t capacity, int32_t precision, void *stream,
+                      bromoc_ctx **out);
+int bromoc_gpu_destroy(bromoc_ctx *ctx);
+const char *bromoc_gpu_last_error(const bromoc_ctx *ctx);
+int bromoc_gpu_abi_version(void);
+
+/* ---- module state (replaces the deck-time fills of the Fortran modules) */
+int bromoc_gpu_set_system(bromoc_ctx *ctx, const bromoc_system *sys);
+int bromoc_gpu_set_types(bromoc_ctx *ctx, const bromoc_types *types);
+int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *pairs);
+int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *sites);
+/* static field phix (readphi PHIX, gsbpmod phix) -- staticf1/staticf0 */
+int bromoc_gpu_set_phix(bromoc_ctx *ctx, const bromoc_grid *g,
+                        const float *phix);
+/* repulsion map phiv after binarisation and repwalls (values 0..127) */
+int bromoc_gpu_set_phiv(bromoc_ctx *ctx, const bromoc_grid *g,
+                        const int8_t *phiv, const bromoc_phiv_opts *opts);
+/* reaction-field parameter grids gsrfen/greff (readrfpar, rfpar.f90:373) */
+int bromoc_gpu_set_rfpar(bromoc_ctx *ctx, const bromoc_grid *g, int32_t nmaps,
+                         const float *gsrfen, const float *greff,
+                         double reffac, const int32_t *map_of_type);
+int bromoc_gpu_set_membrane(bromoc_ctx *ctx, const bromoc_membrane *m);
+int bromoc_gpu_set_diffusion(bromoc_ctx *ctx, const bromoc_diffusion *d);
+int bromoc_gpu_set_countions(bromoc_ctx *ctx, int32_t cntpts,
+                             const double *zcont);
+int bromoc_gpu_set_buffers(bromoc_ctx *ctx, const bromoc_buffers *b);
+
+/* ---- particles (grandmod x,y,z,typei,ibuffer) ------------------------- */
+int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
+                             int32_t nfix, const double *x, const double *y,
+                             const double *z, const int32_t *typei,
+                             const int32_t *ibuffer);
+int bromoc_gpu_get_particles(bromoc_ctx *ctx, int32_t *ntot, double *x,
+                             double *y, double *z, int32_t *typei,
+                             int32_t *ibuffer);
+
+/* ---- hot path ------------------------------------------------------------
+ * ENERGY (energy.mono.f90:19-692 minus DNA bonded terms): total energy with
+ * the term breakdown in eterms[BROMOC_NTERMS]; forces into fx/fy/fz (host,
+ * length ntot, may be NULL) when qforces != 0; warn[nttyp] (may be NULL)
+ * receives the "particle inside membrane or protein" counters. */
+int bromoc_gpu_energy(bromoc_ctx *ctx, uint32_t terms, int32_t qforces,
+                      double *fx, double *fy, double *fz, double *eterms,
+                      int32_t *warn);
+
+/* INTERACT (interact.f90:19-419): FP64 energy of particle j (1-based; j ==
+ * ntot+1 is an insertion trial) of combined-or-ion type jtype placed at
+ * (xj,yj,zj) with the rest of the system. */
+int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj,
+                        double zj, int32_t jtype, int32_t j, double *dener);
+
+/* One BD update with the forces of the last bromoc_gpu_energy(qforces)
+ * call: dynamics{0,1,2,3} on the mobile ions, dynamics0nuc on free DNA
+ * sites, fixcoor, countions.  Noise is Philox4x32-10 keyed by
+ * (seed, step, particle slot, component). */
+int bromoc_gpu_dynamics(bromoc_ctx *ctx, int32_t variant, uint64_t seed,
+                        uint64_t step);
+
+/* nsteps x (ENERGY with forces + BD update), device resident; steps are
+ * numbered step0, step0+1, ... for the noise stream.  eterms (may be NULL)
+ * receives the energy of the last step's ENERGY call. */
+int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant,
+                        int32_t nsteps, uint64_t seed, uint64_t step0,
+                        double *eterms);
+
+/* Drop-in for simul1.f90's BD loop over HOST arrays: uploads x,y,z,typei,
+ * runs nsteps, downloads x,y,z (the arrays are updated in place). */
+int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant,
+                             int32_t nsteps, uint64_t seed, uint64_t step0,
+                             int32_t ntot, int32_t nsites, int32_t nfix,
+                             double *x, double *y, double *z,
+                             const int32_t *typei, double *eterms);
+
+/* GRAND (grand.f90:19-121): ngcmc grand-canonical insertion/deletion
+ * attempts of cycle `cycle` (1-based icycle), device resident.  Uniforms are
+ * Philox4x32-10 keyed by (seed, cycle, attempt, draw).  dener_sum (may be
+ * NULL) receives the accumulated energy change (ener += dener). */
+int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc,
+                     uint64_t seed, uint64_t cycle, double *dener_sum);
+/* Buffer counters after GRAND: nat, ninsert, nremove [nbuffer] and the
+ * occupancy histogram prob[nbuffer*(capacity+1)] (prob(ib,n) of simul1). */
+int bromoc_gpu_get_buffers(bromoc_ctx *ctx, int32_t *nat, int32_t *ninsert,
+                           int32_t *nremove, int32_t *prob);
+/* countions crossing counters [(ntype-nold)*cntpts], type-major */
+int bromoc_gpu_get_countions(bromoc_ctx *ctx, int32_t *nforward,
+                             int32_t *nbackward);
+
+/* Per-particle PROXDIFF nearest-site record dids(5,ntot) of the last
+ * ENERGY call (energy.mono.f90:603-621), 5 doubles per particle. */
+int bromoc_gpu_get_dids(bromoc_ctx *ctx, double *dids);
+
+/* ---- effective-potential table build (setup; polynom.f90, splinepot.f90,
+ * discretize.f90).  Host-side C++; writes the quadratic pieces of one pair
+ * into ep[3*n] and the core/tail constants into sc3[3], dm2o[2], dmio. ---- */
+/* from a read table of n knots (r_k, U_k) (splinepot.f90:19-96) */
+int bromoc_gpu_efpot_from_knots(int32_t n, const double *xx, const double *yy,
+                                double fct, int32_t qchr, double *ep,
+                                double *sc3, double *dm2o, double *dmio);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* BROMOC_GPU_H */

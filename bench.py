@@ -1,0 +1,397 @@
+#!/usr/bin/env python
+"""particle-steps/s of the cg-gcmc-bd inner loop on GB300.
+
+Workload (the nanopore system with grid maps): 120x120x180 maps at 1 A
+(static field = 1 V drop + seeded Gaussians, RFPAR Born-like wall penalty,
+repulsion slab with a 10 A pore, repwalls layers), ~2000 K+/Cl- ions with
+Coulomb/cdie 80 + LJ + SRPMF pairs, four GCMC buffers (1 M) at both ends.
+One bench step = one simul1 cycle: GRAND with 4 attempts, then 10 BD steps
+(ENERGY with forces + dynamics0).  Pair arithmetic FP32 with FP64
+accumulation; fields, BD update and GCMC ΔE in FP64.  Synthetic inputs (the
+reference ships no maps or decks).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
+
+N > 1 (torchrun): replicas only -- every rank advances its own replica (its
+own seed), no data-path collective; value = all ranks' particle-steps / the
+slowest rank's time.  --impl reference times the CPU restatement of the
+reference routines (the Fortran reference cannot be built here) on the
+host cores, rank 0 only.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes as C
+import json
+import math
+import os
+import re
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+sys.path.insert(0, str(ROOT))
+
+from bromoc_gb300 import abi, synth  # noqa: E402
+
+METRIC = ("particle-steps/s, 1 GB300: plain vs batched+adjoint, force rel err "
+          "≤1e-5 vs FP64")
+NGCMC, NBD = 4, 10
+NIONS = 2000
+SEED = 1234
+L2_FLUSH_BYTES = 256 << 20  # > 129 MB L2
+PAIR_FLOP = 38              # LJ + Coulomb pair, algorithmic FLOP per pair
+RF_FLOP = 32                # RFPAR cross term, FLOP per unordered pair
+
+
+def workload(rank: int = 0, precision=abi.FP32):
+    maps = synth.pore_maps(seed=102)
+    spec = synth.pore(seed=3 + 1000 * rank, nions=NIONS, maps=maps,
+                      precision=precision, buffers=True)
+    return spec
+
+
+def config_dict():
+    return {"workload": f"nanopore-{NIONS}: 120x120x180 maps (phix, phiv+repwalls, "
+                        "rfpar), K+/Cl- Coulomb+LJ+SRPMF, 4 GCMC buffers",
+            "step": f"one cycle = GRAND({NGCMC} attempts) + {NBD} BD steps",
+            "nions": NIONS, "grid": [120, 120, 180], "ngcmc": NGCMC, "nbd": NBD,
+            "pairs": "FP32 arithmetic, FP64 accumulation; no cutoff (all pairs)",
+            "l2": "flushed between timed steps (256 MB write outside the events)"}
+
+
+# ---------------------------------------------------------------------------
+class ClockSampler:
+    """nvidia-smi clocks and throttle reasons while the timed region runs."""
+
+    Q = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+         "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+         "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, gpu_index: int):
+        self.idx = gpu_index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.idx}", f"--query-gpu={self.Q}",
+                 "--format=csv,noheader,nounits", "-lms", "200"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.t = threading.Thread(target=self._read, daemon=True)
+            self.t.start()
+        except OSError:
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+            self.t.join(timeout=2)
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown",
+                 "sw_power_cap"]
+        for ln in self.lines:
+            parts = [x.strip() for x in ln.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for nm, v in zip(names, parts[5:9]):
+                if v.lower().startswith("active"):
+                    reasons.add(nm)
+        return {"sm_mhz": statistics.median(sm) if sm else None,
+                "sm_max_mhz": mx, "reasons": sorted(reasons),
+                "samples": len(sm)}
+
+
+# ---------------------------------------------------------------------------
+def measured_peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        return json.loads(p.read_text()), "measured"
+    return {"hbm_gbs": 6800.0, "bf16_tflops": 1900.0}, "fallback"
+
+
+def profile_traffic(kernel: str):
+    """DRAM bytes per launch of `kernel` from the committed ncu summary."""
+    for f in sorted((ROOT / "profiles").glob("*.md")):
+        txt = f.read_text()
+        m = re.search(r"^traffic_bytes_per_launch\[%s\]:\s*([0-9.eE+]+)" % kernel,
+                      txt, re.M)
+        if m:
+            return float(m.group(1)), f.name
+    return None, None
+
+
+def oracle_baseline(steps_budget_s: float, nthreads: int | None = None):
+    """The CPU restatement (OpenMP build) on the same workload for a bounded
+    sample: whole cycles until the time budget is spent."""
+    from oracle import oracle
+    if nthreads:
+        os.environ["OMP_NUM_THREADS"] = str(nthreads)
+    spec = workload(0, precision=abi.FP64)
+    eng = oracle.create(23000, omp=True)
+    spec.push(eng)
+    cores = oracle.load(omp=True).bromoc_ref_threads()
+    done_ps, cyc, t0 = 0, 0, time.perf_counter()
+    while True:
+        cyc += 1
+        eng.grand(NGCMC, SEED, cyc)
+        n = eng.live_ntot()
+        eng.bd_steps(NBD, SEED, (cyc - 1) * NBD)
+        done_ps += NBD * (n - spec.nsites - spec.nfix)
+        if time.perf_counter() - t0 >= steps_budget_s:
+            break
+    dt = time.perf_counter() - t0
+    return {"value": done_ps / dt, "unit": "particle-steps/s", "cores": cores,
+            "kind": "port",
+            "sample": f"{cyc} cycles ({cyc * NBD} BD steps, {cyc * NGCMC} GCMC "
+                      f"attempts) of the same workload, FP64, {dt:.1f} s"}
+
+
+# ---------------------------------------------------------------------------
+def run_reference(args, rank, world):
+    if rank != 0:
+        return
+    budget = float(os.environ.get("BROMOC_REF_STEP_S", "3.0"))
+    from oracle import oracle
+    os.environ.setdefault("OMP_NUM_THREADS", str(os.cpu_count() or 1))
+    spec = workload(0, precision=abi.FP64)
+    eng = oracle.create(23000, omp=True)
+    spec.push(eng)
+    cores = oracle.load(omp=True).bromoc_ref_threads()
+
+    def one_cycle(cyc):
+        eng.grand(NGCMC, SEED, cyc)
+        n = eng.live_ntot()
+        eng.bd_steps(NBD, SEED, (cyc - 1) * NBD)
+        return NBD * (n - spec.nsites - spec.nfix)
+
+    for c in range(1, args.warmup + 1):
+        one_cycle(c)
+    tot_ps, t0 = 0, time.perf_counter()
+    for c in range(args.warmup + 1, args.warmup + args.steps + 1):
+        tot_ps += one_cycle(c)
+    dt = time.perf_counter() - t0
+    v = tot_ps / dt
+    line = {"metric": METRIC, "value": v, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64",
+            "data": "synthetic", "config": config_dict(), "impl": "reference",
+            "cpu_baseline": {"value": v, "unit": "particle-steps/s",
+                             "cores": cores, "kind": "port",
+                             "sample": f"{args.steps} full cycles of the workload "
+                                       "(CPU FP64 restatement, OpenMP)"},
+            "e2e": {"value": v, "unit": "particle-steps/s",
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+# ---------------------------------------------------------------------------
+def run_gpu(args, rank, world, local_rank):
+    import torch
+    from bromoc_gb300 import _lib
+    torch.cuda.set_device(local_rank)
+    dist = None
+    if world > 1:
+        import torch.distributed as dist
+        dist.init_process_group("nccl")
+    stream = torch.cuda.current_stream()
+    sh = stream.cuda_stream
+
+    # accuracy of the FP32 pair path against the FP64 path (validated
+    # against the FP64 oracle by the parity tests) on this workload
+    spec64 = workload(rank, precision=abi.FP64)
+    g64 = _lib.create(23000, abi.FP64, sh)
+    spec64.push(g64)
+    _, f64, _ = g64.energy(abi.M_ALL, forces=True)
+    g32a = _lib.create(23000, abi.FP32, sh)
+    spec64.push(g32a)
+    _, f32, _ = g32a.energy(abi.M_ALL, forces=True)
+    force_rel = float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))
+    del g64, g32a
+
+    spec = workload(rank, precision=abi.FP32)
+    eng = _lib.create(23000, abi.FP32, sh)
+    spec.push(eng)
+    flush = torch.empty(L2_FLUSH_BYTES // 4, dtype=torch.float32, device="cuda")
+    nfix = spec.nsites + spec.nfix
+
+    def step(cyc):
+        eng.grand(NGCMC, SEED, cyc, )
+        eng.bd_steps(NBD, SEED, (cyc - 1) * NBD)
+
+    for c in range(1, args.warmup + 1):
+        step(c)
+    torch.cuda.synchronize()
+    # particle counts per step (GCMC changes ntot): read before each step
+    # outside the events
+    ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
+          for _ in range(args.steps)]
+    nmob = []
+    _lib.kernel_timing(eng, True)
+    l0 = _lib.launch_count(eng)
+    if dist:
+        dist.barrier()
+    torch.cuda.synchronize()
+    with ClockSampler(local_rank) as clk:
+        w0 = time.perf_counter()
+        for k in range(args.steps):
+            nmob.append(eng.live_ntot() - nfix)
+            flush.zero_()
+            ev[k][0].record(stream)
+            step(args.warmup + 1 + k)
+            ev[k][1].record(stream)
+        torch.cuda.synchronize()
+        wall = time.perf_counter() - w0
+    launches = _lib.launch_count(eng) - l0
+    t_ms = sum(a.elapsed_time(b) for a, b in ev)
+    ps = NBD * sum(nmob)
+    tmax = t_ms
+    if dist:
+        tt = torch.tensor([t_ms, ps], dtype=torch.float64, device="cuda")
+        tm = tt[:1].clone()
+        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
+        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
+        tmax, ps = float(tm[0]), float(tt[1])
+    value = ps / (tmax * 1e-3)
+    # per-kernel timing over the timed region
+    kt = {name: _lib.kernel_time(eng, k) for name, k in
+          (("pairs", _lib.K_PAIRS), ("rfcross", _lib.K_RFCROSS),
+           ("fields", _lib.K_FIELDS), ("assemble", _lib.K_ASSEMBLE))}
+    _lib.kernel_timing(eng, False)
+
+    # e2e through the host-array C ABI entry point (pinned host buffers)
+    cap = 23000
+    pin = {k: torch.empty(cap, dtype=dt, pin_memory=True)
+           for k, dt in (("x", torch.float64), ("y", torch.float64),
+                         ("z", torch.float64), ("t", torch.int32),
+                         ("ib", torch.int32))}
+    x, y, z, t, ib = eng.get_particles()
+    n0 = len(x)
+    for k, a in (("x", x), ("y", y), ("z", z), ("t", t), ("ib", ib)):
+        pin[k][:n0] = torch.from_numpy(np.ascontiguousarray(a))
+    ntot = C.c_int32(n0)
+    lib = _lib.load()
+    e2e_steps = max(3, args.steps // 2)
+    h2d = d2h = 0
+    e2e_ps = 0
+    cyc0 = args.warmup + args.steps + 1
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for k in range(e2e_steps):
+        n_before = ntot.value
+        rc = lib.bromoc_gpu_simul_cycles_host(
+            eng.h, abi.M_ALL, abi.DYN0, 1, NGCMC, NBD, SEED, cyc0 + k,
+            C.byref(ntot), spec.nsites, spec.nfix, pin["x"].data_ptr(),
+            pin["y"].data_ptr(), pin["z"].data_ptr(), pin["t"].data_ptr(),
+            pin["ib"].data_ptr(), None)
+        if rc:
+            raise abi.BromocError(rc, lib.bromoc_gpu_last_error(eng.h).decode())
+        h2d += n_before * (3 * 8 + 4 + 4)
+        d2h += ntot.value * (3 * 8 + 4 + 4)
+        e2e_ps += NBD * (n_before - nfix)
+    e2e_dt = time.perf_counter() - t0
+    e2e_val = e2e_ps / e2e_dt
+
+    if rank != 0:
+        if dist:
+            dist.destroy_process_group()
+        return
+    # roofline of the dominant kernel (by measured time share)
+    peak_fp32 = _lib.fp32_peak(sh)
+    peaks, src = measured_peaks()
+    tot_k = sum(v[0] for v in kt.values()) or 1.0
+    dom = max(kt, key=lambda k: kt[k][0])
+    n_ion = statistics.mean(nmob) + spec.nfix
+    pairs = n_ion * (n_ion - 1) / 2
+    if dom in ("pairs", "rfcross"):
+        per = PAIR_FLOP if dom == "pairs" else RF_FLOP
+        ms, nl = kt[dom]
+        achieved = per * pairs / (ms / nl * 1e-3) / 1e12
+        traffic, prof = profile_traffic("k_ionion32" if dom == "pairs" else "k_rfcross")
+        roof = {"kernel": "k_ionion32" if dom == "pairs" else "k_rfcross",
+                "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
+                "unit": "TFLOP/s", "frac": achieved / peak_fp32,
+                "traffic": traffic,
+                "peak_source": "FP32 FMA probe kernel measured in this run "
+                               "(MEASURED_PEAKS.json has no FP32 figure)",
+                "algorithmic": f"{per} FLOP x N(N-1)/2 unordered pairs, N = "
+                               f"{n_ion:.0f} ions",
+                "launch_ms": ms / nl, "share": kt[dom][0] / tot_k}
+    else:
+        ms, nl = kt[dom]
+        nbytes = n_ion * (32 + 8 + 64 + 48) if dom == "fields" else n_ion * 200
+        achieved = nbytes / (ms / nl * 1e-3) / 1e9
+        roof = {"kernel": dom, "bound": "hbm", "achieved": achieved,
+                "peak": peaks["hbm_gbs"], "unit": "GB/s",
+                "frac": achieved / peaks["hbm_gbs"], "traffic": None,
+                "peak_source": src, "launch_ms": ms / nl,
+                "share": kt[dom][0] / tot_k}
+    cpu = oracle_baseline(float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15")))
+    clocks = clk.summary()
+    line = {"metric": METRIC, "value": value, "unit": "particle-steps/s",
+            "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": tmax / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic", "config": config_dict(),
+            "force_rel_err_fp32_vs_fp64": force_rel,
+            "roofline": roof,
+            "kernel_ms": {k: {"total_ms": v[0], "launches": v[1],
+                              "share": v[0] / tot_k} for k, v in kt.items()},
+            "cpu_baseline": cpu,
+            "e2e": {"value": e2e_val, "unit": "particle-steps/s",
+                    "h2d_bytes_per_step": h2d // e2e_steps,
+                    "d2h_bytes_per_step": d2h // e2e_steps,
+                    "steps": e2e_steps,
+                    "path": "bromoc_gpu_simul_cycles_host, pinned host arrays"},
+            "gpu_launches": launches,
+            "wall_s": wall, "clocks": clocks}
+    print(json.dumps(line), flush=True)
+    if dist:
+        dist.destroy_process_group()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=100)
+    ap.add_argument("--warmup", type=int, default=5)
+    ap.add_argument("--impl", default="gb300", choices=["gb300", "reference"])
+    args = ap.parse_args()
+    args.warmup = max(args.warmup, 3)
+    rank = int(os.environ.get("RANK", "0"))
+    world = int(os.environ.get("WORLD_SIZE", str(args.gpus)))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1 and "RANK" not in os.environ:
+        raise SystemExit("--gpus N > 1 must be launched with torchrun")
+    if args.impl == "reference":
+        run_reference(args, rank, world)
+    else:
+        run_gpu(args, rank, world, local)
+
+
+if __name__ == "__main__":
+    main()

@@ -24,6 +24,25 @@ def load() -> C.CDLL:
         lib.bromoc_gpu_create.argtypes = [C.c_int32, C.c_int32, C.c_void_p,
                                           C.POINTER(C.c_void_p)]
         lib.bromoc_gpu_abi_version.restype = C.c_int
+        d, i32 = C.POINTER(C.c_double), C.POINTER(C.c_int32)
+        lib.bromoc_gpu_simul_cycles_host.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+            C.c_uint64, C.c_uint64, i32, C.c_int32, C.c_int32, C.c_void_p,
+            C.c_void_p, C.c_void_p, C.c_void_p, C.c_void_p, d]
+        lib.bromoc_gpu_simul_cycles_host.restype = C.c_int
+        lib.bromoc_gpu_bd_steps_host.argtypes = [
+            C.c_void_p, C.c_uint32, C.c_int32, C.c_int32, C.c_uint64,
+            C.c_uint64, C.c_int32, C.c_int32, C.c_int32, d, d, d, i32, d]
+        lib.bromoc_gpu_bd_steps_host.restype = C.c_int
+        lib.bromoc_gpu_launch_count.argtypes = [C.c_void_p]
+        lib.bromoc_gpu_launch_count.restype = C.c_int64
+        lib.bromoc_gpu_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
+        lib.bromoc_gpu_kernel_timing.restype = C.c_int
+        lib.bromoc_gpu_kernel_time.argtypes = [C.c_void_p, C.c_int32, d,
+                                               C.POINTER(C.c_int64)]
+        lib.bromoc_gpu_kernel_time.restype = C.c_int
+        lib.bromoc_gpu_fp32_peak.argtypes = [C.c_void_p, d]
+        lib.bromoc_gpu_fp32_peak.restype = C.c_int
         _lib = lib
     return _lib
 
@@ -44,3 +63,31 @@ def create(capacity: int = 23000, precision: int = abi.FP64,
 
 def efpot_from_knots(r, u, fct, qchr):
     return abi.efpot_from_knots(load(), PREFIX, r, u, fct, qchr)
+
+
+K_PAIRS, K_RFCROSS, K_FIELDS, K_ASSEMBLE = 0, 1, 2, 3
+
+
+def kernel_timing(eng: abi.Engine, on: bool) -> None:
+    eng._chk(load().bromoc_gpu_kernel_timing(eng.h, int(on)), "kernel_timing")
+
+
+def kernel_time(eng: abi.Engine, which: int):
+    """(total ms, timed launches) of one kernel family since timing on."""
+    ms, n = C.c_double(0.0), C.c_int64(0)
+    eng._chk(load().bromoc_gpu_kernel_time(eng.h, which, C.byref(ms),
+                                           C.byref(n)), "kernel_time")
+    return ms.value, n.value
+
+
+def launch_count(eng: abi.Engine) -> int:
+    return int(load().bromoc_gpu_launch_count(eng.h))
+
+
+def fp32_peak(stream: int | None = None) -> float:
+    t = C.c_double(0.0)
+    rc = load().bromoc_gpu_fp32_peak(C.c_void_p(stream) if stream else None,
+                                     C.byref(t))
+    if rc != abi.OK:
+        raise abi.BromocError(rc, "bromoc_gpu_fp32_peak")
+    return t.value

@@ -6,7 +6,9 @@ product library is libbromoc_gpu.so with prefix ``bromoc_gpu``.
 """
 from __future__ import annotations
 
+import atexit
 import ctypes as C
+import weakref
 
 import numpy as np
 
@@ -156,6 +158,23 @@ class BromocError(RuntimeError):
         self.code = code
 
 
+# Contexts must be destroyed before the CUDA runtime linked into the library
+# tears itself down at process exit: Python's atexit hooks run first.
+_LIVE = weakref.WeakSet()
+_SHUTDOWN = False
+
+
+@atexit.register
+def _close_all():
+    global _SHUTDOWN
+    for eng in list(_LIVE):
+        try:
+            eng.close()
+        except Exception:
+            pass
+    _SHUTDOWN = True
+
+
 class Engine:
     """One context of a library exporting the bromoc ABI.
 
@@ -175,6 +194,7 @@ class Engine:
         self.nold = 0
         self.nbuffer = 0
         self.cntpts = 0
+        _LIVE.add(self)
 
     def _fn(self, name):
         return getattr(self.lib, f"{self.prefix}_{name}")
@@ -191,6 +211,8 @@ class Engine:
             self.h = None
 
     def __del__(self):
+        if _SHUTDOWN:
+            return
         try:
             self.close()
         except Exception:
@@ -233,18 +255,29 @@ class Engine:
         self.ntot = k
         return x[:k], y[:k], z[:k], t[:k], ib[:k]
 
+    def live_ntot(self) -> int:
+        """Current particle count (GCMC changes it on the device)."""
+        n = C.c_int32(0)
+        self._chk(self._fn("get_particles")(self.h, C.byref(n), None, None,
+                                            None, None, None), "get_particles")
+        self.ntot = n.value
+        return n.value
+
     # -- hot path -----------------------------------------------------------
     def energy(self, terms=M_ALL, forces=True):
-        n = self.ntot
-        fx, fy, fz = np.zeros(n), np.zeros(n), np.zeros(n)
+        # capacity-sized outputs: the live ntot may exceed the last upload
+        cap = self.capacity
+        fx, fy, fz = np.zeros(cap), np.zeros(cap), np.zeros(cap)
         e = np.zeros(NTERMS)
         warn = np.zeros(max(self.nttyp, 1), np.int32)
         self._chk(self._fn("energy")(
             self.h, terms, 1 if forces else 0, ptr(fx, C.c_double),
             ptr(fy, C.c_double), ptr(fz, C.c_double), ptr(e, C.c_double),
             ptr(warn, C.c_int32)), "energy")
+        n = self.live_ntot()
         terms_d = dict(zip(TERM_NAMES, e.tolist()))
-        return terms_d, (np.stack([fx, fy, fz], 1) if forces else None), warn
+        f = np.stack([fx[:n], fy[:n], fz[:n]], 1) if forces else None
+        return terms_d, f, warn
 
     def interact(self, xj, yj, zj, jtype, j, terms=M_ALL):
         d = C.c_double(0.0)
@@ -286,9 +319,9 @@ class Engine:
         return nf, nb
 
     def get_dids(self):
-        d = np.zeros(5 * max(self.ntot, 1))
+        d = np.zeros(5 * max(self.capacity, 1))
         self._chk(self._fn("get_dids")(self.h, ptr(d, C.c_double)), "get_dids")
-        return d.reshape(-1, 5)[: self.ntot]
+        return d.reshape(-1, 5)[: self.live_ntot()]
 
     def efpot_from_knots(self, xx, yy, fct, qchr):
         return efpot_from_knots(self.lib, self.prefix, xx, yy, fct, qchr)

@@ -36,6 +36,8 @@ struct bromoc_ctx {
   bool have_sys = false, have_types = false, have_pairs = false;
   bromoc_system sys{};
   std::vector<double> diffusion;  // 1-based
+  std::vector<int> site_map;      // per-site repulsion map (nmcden)
+  int phiv_nmaps = 0;
   // live ntot bookkeeping (see ntot_ub)
   int ntot_known = 0;
   long long attempts_total = 0, attempts_at_known = 0;
@@ -50,6 +52,11 @@ struct bromoc_ctx {
   // last energy plan (for dynamics())
   AssembleFlags last_fl{};
   bool have_forces = false;
+  long long launches = 0;  // kernels launched by this context
+  // diagnostic kernel timing: event pairs per kernel family
+  bool timing = false;
+  std::vector<KTimer> tpool[BROMOC_K_NKINDS];
+  int tused[BROMOC_K_NKINDS] = {};
 };
 
 namespace {
@@ -182,6 +189,19 @@ int ensure_scratch(bromoc_ctx *ctx) {
   return BROMOC_OK;
 }
 
+// Next free event pair of a kernel family, or nullptr when timing is off.
+KTimer *next_timer(bromoc_ctx *c, int kind) {
+  if (!c->timing) return nullptr;
+  std::vector<KTimer> &v = c->tpool[kind];
+  if (c->tused[kind] == (int)v.size()) {
+    KTimer t{};
+    if (cudaEventCreate(&t.a) != cudaSuccess || cudaEventCreate(&t.b) != cudaSuccess)
+      return nullptr;
+    v.push_back(t);
+  }
+  return &v[c->tused[kind]++];
+}
+
 // Source chunking of the pair kernels: enough blocks for ~2 waves of the
 // 152 SMs, chunks a multiple of the 128-particle tile.
 void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
@@ -217,6 +237,9 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
   fl.rf = (mask & BROMOC_M_RFPAR) && p.qrfpar && nion > 0 && plan.nchunk_rf > 0;
   fl.nchunk_rf = fl.rf ? plan.nchunk_rf : 0;
+  plan.t_pairs = fl.ii ? next_timer(ctx, BROMOC_K_PAIRS) : nullptr;
+  plan.t_rf = fl.rf ? next_timer(ctx, BROMOC_K_RFCROSS) : nullptr;
+  plan.t_fields = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_FIELDS) : nullptr;
   if (energy_slots(p, plan, mask) > ctx->nslot_cap)
     return set_err(ctx, BROMOC_E_ARG, "energy slots exceed scratch");
   return BROMOC_OK;
@@ -236,10 +259,15 @@ int check_device_err(bromoc_ctx *ctx) {
   CU(cudaStreamSynchronize(ctx->stream));
   e = ctx->h_ntot[1];
   if (e) {
-    CU(cudaMemsetAsync(&ctx->kp.st->err, 0, sizeof(int), ctx->stream));
-    if (e & kErrCapacity)
+    int bad[3] = {0, 0, 0};
+    CU(cudaMemcpy(bad, &ctx->kp.st->bad_site, sizeof bad, cudaMemcpyDeviceToHost));
+    CU(cudaMemsetAsync(&ctx->kp.st->err, 0, 4 * sizeof(int), ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    if (e == kErrCapacity)
       return set_err(ctx, BROMOC_E_CAPACITY, "grand: ntot is greater than capacity");
-    return set_err(ctx, BROMOC_E_DEVICE, "device error flags 0x%x", e);
+    return set_err(ctx, BROMOC_E_DEVICE,
+                   "device error flags 0x%x (guard site %d: index %d, bound %d)", e,
+                   bad[0], bad[1], bad[2]);
   }
   return BROMOC_OK;
 }
@@ -304,6 +332,11 @@ int bromoc_gpu_destroy(bromoc_ctx *ctx) {
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (void *a : ctx->allocs)
     if (a) cudaFree(a);
+  for (auto &pool : ctx->tpool)
+    for (KTimer &t : pool) {
+      cudaEventDestroy(t.a);
+      cudaEventDestroy(t.b);
+    }
   if (ctx->h_ntot) cudaFreeHost(ctx->h_ntot);
   if (ctx->ev_ntot) cudaEventDestroy(ctx->ev_ntot);
   if (ctx->own_stream && ctx->stream) cudaStreamDestroy(ctx->stream);
@@ -532,10 +565,20 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
   p.typtyp = t;
   p.sitecharge = c;
   p.stfree = f;
+  ctx->site_map.clear();
   if (!rc && s->phiv_map) {
+    if (p.qphiv && p.qnmcden) {
+      int nmaps = ctx->phiv_nmaps;
+      for (int i = 0; i < s->nsites; ++i)
+        if (s->phiv_map[i] < 0 || s->phiv_map[i] >= nmaps)
+          return set_err(ctx, BROMOC_E_ARG, "set_sites: phiv_map out of range");
+    }
+    ctx->site_map.assign(s->phiv_map, s->phiv_map + s->nsites);
     int *m = const_cast<int *>(p.site_map);
     rc = upload(ctx, &m, s->phiv_map, s->nsites);
     p.site_map = m;
+  } else if (p.qphiv && p.qnmcden) {
+    return set_err(ctx, BROMOC_E_ARG, "set_sites: nmcden needs per-site maps");
   }
   return rc;
 }
@@ -558,6 +601,18 @@ int bromoc_gpu_set_phiv(bromoc_ctx *ctx, const bromoc_grid *g, const int8_t *phi
   if (o->nmcden && !o->map_of_type)
     return set_err(ctx, BROMOC_E_ARG, "set_phiv: nmcden needs map_of_type");
   KP &p = ctx->kp;
+  {
+    const Grid3 gg = make_grid(*g);  // vzmin/vzmax inside the map (shell_simul:2759,2763)
+    if (o->vzmax > gg.zbcen + gg.tranz || o->vzmin < gg.zbcen - gg.tranz)
+      return set_err(ctx, BROMOC_E_ARG, "set_phiv: vzmin/vzmax outside the map");
+    if (o->nmcden && p.nsites > 0) {
+      if (ctx->site_map.empty())
+        return set_err(ctx, BROMOC_E_ARG, "set_phiv: nmcden needs per-site maps");
+      for (int m : ctx->site_map)
+        if (m < 0 || m >= o->nmaps)
+          return set_err(ctx, BROMOC_E_ARG, "set_phiv: site map out of range");
+    }
+  }
   p.g2 = make_grid(*g);
   int8_t *d = const_cast<int8_t *>(p.phiv);
   int rc = upload(ctx, &d, phiv, (size_t)o->nmaps * g->nclx * g->ncly * g->nclz);
@@ -578,6 +633,7 @@ int bromoc_gpu_set_phiv(bromoc_ctx *ctx, const bromoc_grid *g, const int8_t *phi
   }
   p.qsvdw = o->scal != nullptr;
   if (o->scal && (rc = upload1(ctx, &p.scal, o->scal, ctx->nttyp))) return rc;
+  ctx->phiv_nmaps = o->nmaps;
   p.qphiv = 1;
   return BROMOC_OK;
 }
@@ -700,6 +756,14 @@ int bromoc_gpu_set_buffers(bromoc_ctx *ctx, const bromoc_buffers *b) {
   if (!b->ibfftyp || !b->avnum || !b->mu || !b->kb || !b->lzmin || !b->lzmax ||
       !b->qbufferbias || !b->nat || !b->ntotat)
     return set_err(ctx, BROMOC_E_ARG, "set_buffers: null array");
+  if (!ctx->have_types) return set_err(ctx, BROMOC_E_STATE, "set_buffers before set_types");
+  for (int i = 0; i < n; ++i) {
+    if (b->ibfftyp[i] <= ctx->nold || b->ibfftyp[i] > ctx->ntype)
+      return set_err(ctx, BROMOC_E_ARG, "set_buffers: buffer %d ion type %d out of range",
+                     i + 1, b->ibfftyp[i]);
+    if (b->nat[i] < 0 || b->nat[i] > p.cap)
+      return set_err(ctx, BROMOC_E_ARG, "set_buffers: nat(%d) out of range", i + 1);
+  }
   int rc = upload1(ctx, &p.ibfftyp, b->ibfftyp, n);
   if (!rc) rc = upload1(ctx, &p.avnum, b->avnum, n);
   if (!rc) rc = upload1(ctx, &p.mu, b->mu, n);
@@ -793,8 +857,9 @@ int bromoc_gpu_energy(bromoc_ctx *ctx, uint32_t terms, int32_t qforces, double *
   AssembleFlags fl{};
   if ((rc = plan_energy(ctx, terms, true, plan, fl))) return rc;
   CU(cudaMemsetAsync(p.warn, 0, (ctx->nttyp + 1) * sizeof(int), ctx->stream));
-  launch_energy(p, plan, terms, qforces, ctx->stream);
+  ctx->launches += launch_energy(p, plan, terms, qforces, ctx->stream);
   launch_assemble(p, plan.ntot_ub, fl, 0, 0, 0, 0, ctx->stream);
+  ctx->launches += plan.ntot_ub > 0;
   CU(cudaGetLastError());
   if ((rc = sync_ntot(ctx))) return rc;
   const int n = ctx->ntot_known;
@@ -838,6 +903,7 @@ int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj, d
   t.z = zj;
   CU(cudaMemcpyAsync(p.trial, &t, sizeof t, cudaMemcpyHostToDevice, ctx->stream));
   launch_interact(p, ntot, terms, 1, ctx->d_dener, ctx->stream);
+  ctx->launches += 2;
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(dener, ctx->d_dener, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -863,6 +929,7 @@ int bromoc_gpu_dynamics(bromoc_ctx *ctx, int32_t variant, uint64_t seed, uint64_
   CU(cudaMemcpyAsync(p.ffield + 2 * (size_t)p.cap, p.fz, p.cap * sizeof(double),
                      cudaMemcpyDeviceToDevice, ctx->stream));
   launch_assemble(p, ntot_ub(ctx), fl, 1, variant, seed, step, ctx->stream);
+  ctx->launches += 1;
   CU(cudaGetLastError());
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_forces = false;
@@ -886,8 +953,12 @@ int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_
   for (int k = 0; k < nsteps; ++k) {
     const bool last = k + 1 == nsteps;
     if ((rc = plan_energy(ctx, terms, last && eterms, plan, fl))) return rc;
-    launch_energy(p, plan, terms, 1, ctx->stream);
+    ctx->launches += launch_energy(p, plan, terms, 1, ctx->stream);
+    KTimer *ta = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_ASSEMBLE) : nullptr;
+    if (ta) cudaEventRecord(ta->a, ctx->stream);
     launch_assemble(p, plan.ntot_ub, fl, 1, variant, seed, step0 + k, ctx->stream);
+    if (ta) cudaEventRecord(ta->b, ctx->stream);
+    ctx->launches += plan.ntot_ub > 0;
   }
   CU(cudaGetLastError());
   ctx->have_forces = false;
@@ -929,6 +1000,7 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   for (int a = 0; a < ngcmc; ++a) {
     const int ub = ntot_ub(ctx);
     launch_gcmc_attempt(p, ub, terms, seed, cycle, (uint32_t)a, ctx->stream);
+    ctx->launches += 3;
     ctx->attempts_total += 1;
   }
   CU(cudaGetLastError());
@@ -977,6 +1049,56 @@ int bromoc_gpu_get_countions(bromoc_ctx *ctx, int32_t *nf, int32_t *nb) {
   if (nf) CU(cudaMemcpy(nf, p.nforward, n * sizeof(int), cudaMemcpyDeviceToHost));
   if (nb) CU(cudaMemcpy(nb, p.nbackward, n * sizeof(int), cudaMemcpyDeviceToHost));
   return BROMOC_OK;
+}
+
+int64_t bromoc_gpu_launch_count(const bromoc_ctx *ctx) {
+  return ctx ? (int64_t)ctx->launches : -1;
+}
+
+int bromoc_gpu_kernel_timing(bromoc_ctx *ctx, int32_t on) {
+  if (!ctx) return BROMOC_E_ARG;
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->timing = on != 0;
+  for (int k = 0; k < BROMOC_K_NKINDS; ++k) ctx->tused[k] = 0;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_kernel_time(bromoc_ctx *ctx, int32_t which, double *total_ms,
+                           int64_t *launches) {
+  if (!ctx || which < 0 || which >= BROMOC_K_NKINDS || !total_ms || !launches)
+    return set_err(ctx, BROMOC_E_ARG, "kernel_time: bad arguments");
+  CU(cudaStreamSynchronize(ctx->stream));
+  double sum = 0.0;
+  for (int i = 0; i < ctx->tused[which]; ++i) {
+    float ms = 0.f;
+    CU(cudaEventElapsedTime(&ms, ctx->tpool[which][i].a, ctx->tpool[which][i].b));
+    sum += ms;
+  }
+  *total_ms = sum;
+  *launches = ctx->tused[which];
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant,
+                                 int32_t ncycle, int32_t ngcmc, int32_t nbd, uint64_t seed,
+                                 uint64_t cycle0, int32_t *ntot, int32_t nsites, int32_t nfix,
+                                 double *x, double *y, double *z, int32_t *typei,
+                                 int32_t *ibuffer, double *eterms) {
+  if (!ctx || !ntot || !x || !y || !z || !typei || !ibuffer)
+    return set_err(ctx, BROMOC_E_ARG, "simul_cycles_host: null");
+  if (ncycle < 0 || ngcmc < 0 || nbd < 0 || cycle0 < 1)
+    return set_err(ctx, BROMOC_E_ARG, "simul_cycles_host: bad counts");
+  int rc = bromoc_gpu_set_particles(ctx, *ntot, nsites, nfix, x, y, z, typei, ibuffer);
+  for (int c = 0; !rc && c < ncycle; ++c) {
+    const uint64_t cyc = cycle0 + c;
+    if (ngcmc > 0) rc = bromoc_gpu_grand(ctx, terms, ngcmc, seed, cyc, nullptr);
+    if (!rc && nbd > 0)
+      rc = bromoc_gpu_bd_steps(ctx, terms, variant, nbd, seed, (cyc - 1) * nbd,
+                               c + 1 == ncycle ? eterms : nullptr);
+  }
+  if (!rc) rc = bromoc_gpu_get_particles(ctx, ntot, x, y, z, typei, ibuffer);
+  if (!rc) rc = check_device_err(ctx);
+  return rc;
 }
 
 int bromoc_gpu_get_dids(bromoc_ctx *ctx, double *dids) {

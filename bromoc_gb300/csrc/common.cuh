@@ -27,6 +27,7 @@ enum : int {
   kErrCapacity = 1,     // an insertion would exceed capacity
   kErrTableIndex = 2,   // an effective-potential piece index out of range
   kErrFind = 4,         // GCMC deletion could not find the particle
+  kErrBounds = 8,       // a guarded index was out of range (access skipped)
 };
 
 // packed pair-law switches
@@ -47,6 +48,7 @@ struct PairParam {
 struct DevState {
   int ntot;
   int err;
+  int bad_site, bad_index, bad_bound, pad_;  // first guarded violation
   int nat[kMaxBuffers];
   int ninsert[kMaxBuffers];
   int nremove[kMaxBuffers];

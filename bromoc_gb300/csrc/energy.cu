@@ -92,7 +92,7 @@ __global__ void __launch_bounds__(kFieldThreads)
     p.ffield[p.cap + i] = f[1];
     p.ffield[2 * p.cap + i] = f[2];
   }
-  double tot[4];
+  __shared__ double tot[4];
   block_sum<4>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
@@ -166,7 +166,7 @@ __global__ void __launch_bounds__(kPairThreads)
     f[2 * p.cap + t] = fza;
   }
   if (err) atomicOr(&p.st->err, err);
-  double tot[4];
+  __shared__ double tot[4];
   block_sum<4>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
@@ -258,7 +258,7 @@ __global__ void __launch_bounds__(kPairThreads)
     f[p.cap + t] = fya;
     f[2 * p.cap + t] = fza;
   }
-  double tot[4];
+  __shared__ double tot[4];
   block_sum<4>(ed, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
@@ -338,7 +338,7 @@ __global__ void __launch_bounds__(kPairThreads)
       for (int m = 0; m < 5; ++m) p.dids[5 * i + m] = dd[m];
   }
   if (err) atomicOr(&p.st->err, err);
-  double tot[4];
+  __shared__ double tot[4];
   // site terms: eqqmx(5) evdwmx(6) esrpmfmx(7) eefpotmx(8)
   block_sum<4>(e, red, tot);
   if (threadIdx.x == 0) {
@@ -379,7 +379,7 @@ __global__ void __launch_bounds__(kPairThreads) k_siteforce(KP p) {
       f[2] -= de * dz;
     }
   }
-  double tot[3];
+  __shared__ double tot[3];
   block_sum<3>(f, red, tot);
   if (threadIdx.x == 0) {
     p.fis[j] = tot[0];
@@ -495,8 +495,109 @@ __global__ void __launch_bounds__(kPairThreads)
     f[p.cap + t] = fo[1];
     f[2 * p.cap + t] = fo[2];
   }
-  double tot[1];
+  __shared__ double tot[1];
   block_sum<1>(&e, red, tot);
+  if (threadIdx.x == 0) {
+    double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
+    for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
+    dst[13] = tot[0];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// RFPAR cross term in single precision: hi/lo coordinates, FP32 pair math,
+// per-tile FP32 and cross-tile FP64 accumulation (no FP64 in the inner loop).
+// Source tile: (x_hi, y_hi, z_hi, srfe) (x_lo, y_lo, z_lo, reff) (q, flags).
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPairThreads)
+    k_rfcross32(KP p, int qforces, int slot0) {
+  __shared__ float4 sh[kPairThreads], sl[kPairThreads];
+  __shared__ float2 sqf[kPairThreads];
+  __shared__ double red[(kPairThreads / 32) * 1];
+  const int ntot = p.st->ntot;
+  const int m0 = p.nsites + p.nfix;
+  const int t = p.nsites + blockIdx.x * kPairThreads + threadIdx.x;
+  const bool tv = t < ntot && p.rf_in[t];
+  const int s0 = p.nsites + blockIdx.y * p.chunk_rf;
+  const int s1 = min(ntot, s0 + p.chunk_rf);
+  float xh = 0, yh = 0, zh = 0, xl = 0, yl = 0, zl = 0, srt = 0, rft = 0, ct = 0;
+  if (tv) {
+    split2(p.x[t], xh, xl);
+    split2(p.y[t], yh, yl);
+    split2(p.z[t], zh, zl);
+    srt = (float)p.rf_srfe[t];
+    rft = (float)p.rf_reff[t];
+    ct = (float)(p.celec * p.cg[abs(p.typei[t])]);
+  }
+  const bool tmob = t >= m0;
+  double Ad = 0, Bd = 0, Pd[3] = {0, 0, 0}, ed = 0;
+  for (int base = s0; base < s1; base += kPairThreads) {
+    const int s = base + threadIdx.x;
+    __syncthreads();
+    if (s < s1) {
+      float4 h, l;
+      split2(p.x[s], h.x, l.x);
+      split2(p.y[s], h.y, l.y);
+      split2(p.z[s], h.z, l.z);
+      h.w = (float)p.rf_srfe[s];
+      l.w = (float)p.rf_reff[s];
+      sh[threadIdx.x] = h;
+      sl[threadIdx.x] = l;
+      sqf[threadIdx.x] = make_float2((float)p.cg[abs(p.typei[s])],
+                                     __int_as_float(p.rf_in[s] | ((s >= m0) << 1)));
+    }
+    __syncthreads();
+    const int n = min(kPairThreads, s1 - base);
+    if (tv) {
+      float A = 0.f, B = 0.f, P0 = 0.f, P1 = 0.f, P2 = 0.f, e = 0.f;
+      for (int k = 0; k < n; ++k) {
+        const int s = base + k;
+        const float2 qf = sqf[k];
+        const int fl = __float_as_int(qf.y);
+        if (s == t || !(fl & 1)) continue;
+        const float4 h = sh[k], l = sl[k];
+        const bool t_is_i = t > s;
+        const bool i_mobile = t_is_i ? tmob : ((fl >> 1) & 1);
+        const float srj = t_is_i ? h.w : srt;
+        if (!i_mobile || srj == 0.0f) continue;
+        const float dx = (xh - h.x) + (xl - l.x);
+        const float dy = (yh - h.y) + (yl - l.y);
+        const float dz = (zh - h.z) + (zl - l.z);
+        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float rij = l.w * rft, srij = h.w * srt;
+        const float rfdn = rsqrtf(fmaf(rij, rij, d2));
+        const float aux0 = ct * qf.x;
+        const float a1 = aux0 * rij * rfdn;
+        if (t_is_i) e = fmaf(a1, srij, e);
+        const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
+        const float aux3 = -a2 * fmaf(rij, 0.5f, d2);
+        A = fmaf(-a1, h.w, A);
+        B = fmaf(aux3, l.w, B);
+        const float pr = a2 * rij;
+        P0 = fmaf(pr, dx, P0);
+        P1 = fmaf(pr, dy, P1);
+        P2 = fmaf(pr, dz, P2);
+      }
+      Ad += A;
+      Bd += B;
+      Pd[0] += P0;
+      Pd[1] += P1;
+      Pd[2] += P2;
+      ed += e;
+    }
+  }
+  if (t < ntot) {
+    double *f = p.frf + (size_t)blockIdx.y * 3 * p.cap;
+    double fo[3] = {0, 0, 0};
+    if (tv && qforces)
+      for (int k = 0; k < 3; ++k)
+        fo[k] = Ad * p.rf_d1[3 * t + k] + Bd * p.rf_d2[3 * t + k] + Pd[k];
+    f[t] = fo[0];
+    f[p.cap + t] = fo[1];
+    f[2 * p.cap + t] = fo[2];
+  }
+  __shared__ double tot[1];
+  block_sum<1>(&ed, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
     for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
@@ -519,13 +620,15 @@ __global__ void __launch_bounds__(256) k_ereduce(KP p, int nslot, int rfpar_on) 
 #pragma unroll
     for (int k = 1; k < kNTerms; ++k) v[k] += src[k];
   }
-  double tot[kNTerms];
+  __shared__ double tot[kNTerms];
   block_sum<kNTerms>(v, red, tot);
   if (threadIdx.x == 0) {
-    tot[11] = rfpar_on ? tot[13] : 0.0;  // egsbpb = erfpar
-    tot[0] = tot[9] + tot[10] + tot[12] + tot[13] + tot[1] + tot[2] + tot[3] +
-             tot[7] + tot[5] + tot[6] + tot[4] + tot[8];
-    for (int k = 0; k < kNTerms; ++k) p.eterms[k] = tot[k];
+    double o[kNTerms];
+    for (int k = 0; k < kNTerms; ++k) o[k] = tot[k];
+    o[11] = rfpar_on ? o[13] : 0.0;  // egsbpb = erfpar
+    o[0] = o[9] + o[10] + o[12] + o[13] + o[1] + o[2] + o[3] + o[7] + o[5] +
+           o[6] + o[4] + o[8];
+    for (int k = 0; k < kNTerms; ++k) p.eterms[k] = o[k];
   }
 }
 
@@ -534,20 +637,28 @@ __global__ void __launch_bounds__(256) k_ereduce(KP p, int nslot, int rfpar_on) 
 // ---------------------------------------------------------------------------
 int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
                   int qforces, cudaStream_t stream) {
-  int slot = 0;
+  int slot = 0, nk = 0;
   const int nub = plan.ntot_ub;
   const int nfb = (nub + kFieldThreads - 1) / kFieldThreads;
-  k_fields<<<nfb, kFieldThreads, 0, stream>>>(p, mask, qforces, slot);
-  slot += nfb;
+  if (nfb > 0) {
+    if (plan.t_fields) cudaEventRecord(plan.t_fields->a, stream);
+    k_fields<<<nfb, kFieldThreads, 0, stream>>>(p, mask, qforces, slot);
+    if (plan.t_fields) cudaEventRecord(plan.t_fields->b, stream);
+    slot += nfb;
+    ++nk;
+  }
   const bool nonbond = (mask & 1u) != 0;
   const int nmob_ub = nub - p.nsites - p.nfix;
   if (nonbond && nmob_ub > 0 && plan.nchunk_ii > 0) {
     dim3 g((nmob_ub + kPairThreads - 1) / kPairThreads, plan.nchunk_ii);
+    if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
     if (plan.fp32)
       k_ionion32<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
     else
       k_ionion64<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
+    if (plan.t_pairs) cudaEventRecord(plan.t_pairs->b, stream);
     slot += g.x * g.y;
+    ++nk;
   }
   if (nonbond && p.nsites > 0 && nub > p.nsites) {
     const int nion_ub = nub - p.nsites;
@@ -561,18 +672,24 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
       if (qforces) k_siteforce<false><<<p.nsites, kPairThreads, 0, stream>>>(p);
     }
     slot += nb;
+    nk += qforces ? 2 : 1;
   }
   if ((mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0) {
     dim3 g((nub - p.nsites + kPairThreads - 1) / kPairThreads, plan.nchunk_rf);
+    if (plan.t_rf) cudaEventRecord(plan.t_rf->a, stream);
     if (plan.fp32)
-      k_rfcross<true><<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
+      k_rfcross32<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
     else
       k_rfcross<false><<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
+    if (plan.t_rf) cudaEventRecord(plan.t_rf->b, stream);
     slot += g.x * g.y;
+    ++nk;
   }
-  if (plan.reduce_energy)
+  if (plan.reduce_energy) {
     k_ereduce<<<1, 256, 0, stream>>>(p, slot, (mask & 16u) && p.qrfpar);
-  return slot;
+    ++nk;
+  }
+  return nk;  // kernels launched
 }
 
 int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {

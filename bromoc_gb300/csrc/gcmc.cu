@@ -34,8 +34,11 @@ __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mas
   const Trial tr = *p.trial;
   const int ntot = p.st->ntot;
   const int j0 = tr.j - 1;
-  const bool beion = j0 >= p.nsites;
-  const int jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
+  // an invalid trial (rejected before INTERACT) carries no slot or type
+  const bool beion = tr.valid && j0 >= p.nsites;
+  int jt2 = 0;
+  if (tr.valid && !guard_bad(p.st, j0, (long long)p.cap + 1, 29))
+    jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
   const bool rf = (mask & 16u) && p.qrfpar && beion;
   if (threadIdx.x == 0) {
     double sj = 0, rj = 0;
@@ -49,10 +52,14 @@ __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mas
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double u = 0.0;
   int err = 0;
-  if (tr.valid && i < ntot && i != j0) {
+  const bool ion_i = i >= p.nsites;
+  bool ok = tr.valid && i < ntot && i != j0 &&
+            !guard_bad(p.st, jt2 - 1, p.nttyp, 30);
+  if (ok && ion_i)
+    ok = !guard_bad(p.st, abs(p.typei[i]) - p.nold - 1, p.ntype - p.nold, 31);
+  if (ok) {
     const double dx = p.x[i] - tr.x, dy = p.y[i] - tr.y, dz = p.z[i] - tr.z;
     const double d2 = dx * dx + dy * dy + dz * dz;
-    const bool ion_i = i >= p.nsites;
     if (mask & 1u) {
       if (beion && ion_i) {  // interact.f90:173-210
         const int is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
@@ -78,9 +85,9 @@ __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mas
     }
   }
   if (err) atomicOr(&p.st->err, err);
-  double tot;
-  block_sum<1>(&u, red, &tot);
-  if (threadIdx.x == 0) p.ipart[blockIdx.x] = tot;
+  __shared__ double tot[1];
+  block_sum<1>(&u, red, tot);
+  if (threadIdx.x == 0) p.ipart[blockIdx.x] = tot[0];
 }
 
 // Single-particle terms of the trial + sum of the partials: the full ΔE.
@@ -88,9 +95,10 @@ __device__ double interact_final(const KP &p, const Trial &tr, uint32_t mask,
                                  int nblk, int qalert, double *red) {
   double v = 0.0;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += p.ipart[b];
-  double pairs;
-  block_sum<1>(&v, red, &pairs);
+  __shared__ double tot[1];
+  block_sum<1>(&v, red, tot);
   if (threadIdx.x != 0) return 0.0;
+  const double pairs = tot[0];
   const int j0 = tr.j - 1;
   const bool beion = j0 >= p.nsites;
   const int jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
@@ -218,15 +226,20 @@ __global__ void __launch_bounds__(kPropThreads)
     s = t;
   }
   __syncthreads();
-  if (s.valid && !s.insert) {
-    // find.f90: the ip-th particle of buffer ib in slot order
+  // every thread reads the proposal before anyone edits it
+  const int valid = s.valid, insert = s.insert, ib = s.ib, rank = s.j;
+  __shared__ int found;
+  if (threadIdx.x == 0) found = -1;
+  __syncthreads();
+  if (valid && !insert) {
+    // find.f90: the rank-th particle of buffer ib in slot order
     const int ntot = p.st->ntot;
     const int lo = p.nsites + p.nfix;
     const int n = ntot - lo;
     const int per = (n + kPropThreads - 1) / kPropThreads;
     const int a = lo + threadIdx.x * per, b = min(ntot, a + per);
     int c = 0;
-    for (int k = a; k < b; ++k) c += (p.ibuffer[k] == s.ib);
+    for (int k = a; k < b; ++k) c += (p.ibuffer[k] == ib);
     counts[threadIdx.x] = c;
     __syncthreads();
     if (threadIdx.x == 0) {  // exclusive scan, fixed order
@@ -238,28 +251,27 @@ __global__ void __launch_bounds__(kPropThreads)
       }
     }
     __syncthreads();
-    const int rank = s.j;
     const int before = counts[threadIdx.x];
-    if (rank > before && rank <= before + c) {
+    if (rank > before && rank <= before + c) {  // exactly one thread
       int r = before;
-      for (int k = a; k < b; ++k) {
-        if (p.ibuffer[k] == s.ib && ++r == rank) {
-          s.j = k + 1;
-          s.x = p.x[k];
-          s.y = p.y[k];
-          s.z = p.z[k];
-          s.draw |= 1 << 30;  // mark found
+      for (int k = a; k < b; ++k)
+        if (p.ibuffer[k] == ib && ++r == rank) {
+          found = k;
           break;
         }
-      }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      if (!(s.draw & (1 << 30))) {
+      const int k = found;
+      if (k < 0 || guard_bad(p.st, k, ntot, 11)) {
         s.valid = 0;
         atomicOr(&p.st->err, kErrFind);
+      } else {
+        s.j = k + 1;
+        s.x = p.x[k];
+        s.y = p.y[k];
+        s.z = p.z[k];
       }
-      s.draw &= ~(1 << 30);
     }
     __syncthreads();
   }
@@ -278,7 +290,7 @@ __global__ void __launch_bounds__(kIaThreads)
   if (tr.valid) dener = interact_final(p, tr, mask, nblk, tr.insert ? 0 : 1, red);
   if (threadIdx.x != 0) return;
   DevState *st = p.st;
-  if (tr.valid) {
+  if (tr.valid && !guard_bad(st, tr.ib - 1, p.nbuffer, 21)) {
     const int ib = tr.ib, b = ib - 1;
     const int nat = st->nat[b];
     const double boltz = exp(-(dener - p.mu[ib]) * p.ikbt);
@@ -305,7 +317,7 @@ __global__ void __launch_bounds__(kIaThreads)
       if (tr.insert) {
         if (ntot + 1 > p.cap) {
           st->err |= kErrCapacity;
-        } else {
+        } else if (!guard_bad(st, ntot, p.cap, 22)) {
           st->dener_sum += dener;
           st->nat[b] = nat + 1;
           p.x[ntot] = tr.x;
@@ -316,7 +328,8 @@ __global__ void __launch_bounds__(kIaThreads)
           st->ntot = ntot + 1;
           st->ninsert[b] += 1;
         }
-      } else {
+      } else if (!guard_bad(st, tr.j - 1, ntot, 23) &&
+                 !guard_bad(st, ntot - 1, p.cap, 24)) {
         const int iat = tr.j - 1, last = ntot - 1;
         st->dener_sum -= dener;
         st->nremove[b] += 1;
@@ -331,7 +344,8 @@ __global__ void __launch_bounds__(kIaThreads)
     }
   }
   for (int b = 0; b < p.nbuffer; ++b)  // prob(ib, nat(ib)) += 1
-    p.prob[(size_t)b * (p.cap + 1) + st->nat[b]] += 1;
+    if (!guard_bad(st, st->nat[b], p.cap + 1, 25))
+      p.prob[(size_t)b * (p.cap + 1) + st->nat[b]] += 1;
 }
 
 void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask,

@@ -4,12 +4,18 @@
 
 namespace bgpu {
 
+// A pair of CUDA events bracketing one launch (diagnostic timing).
+struct KTimer {
+  cudaEvent_t a, b;
+};
+
 struct EnergyPlan {
   int ntot_ub;        // host upper bound of the device-resident ntot
   int nchunk_ii;      // source chunks of the ion-ion kernel
   int nchunk_rf;      // source chunks of the RFPAR cross kernel
   bool fp32;
   bool reduce_energy; // launch the final energy reduction
+  KTimer *t_pairs = nullptr, *t_rf = nullptr, *t_fields = nullptr;
 };
 
 struct AssembleFlags {

@@ -595,10 +595,11 @@ __device__ __forceinline__ size_t rfpar_ifir(const KP &p, int itype) {
 }
 
 // ---- block reductions (fixed tree: deterministic for a fixed blockDim) --
+// Sums v[0..N) over the block; the totals land in the SHARED array out[N],
+// visible to every thread on return.  smem: (blockDim.x/32) * N doubles.
 template <int N>
-__device__ __forceinline__ void block_sum(double v[N], double *smem,
-                                          double *dst) {
-  // smem: (blockDim.x/32) * N doubles
+__device__ __forceinline__ void block_sum(const double v[N], double *smem,
+                                          double *out) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int nw = (blockDim.x + 31) >> 5;
 #pragma unroll
@@ -612,9 +613,22 @@ __device__ __forceinline__ void block_sum(double v[N], double *smem,
   if (threadIdx.x < N) {
     double s = 0.0;
     for (int w = 0; w < nw; ++w) s += smem[w * N + threadIdx.x];
-    dst[threadIdx.x] = s;
+    out[threadIdx.x] = s;
   }
   __syncthreads();
+}
+
+// Bounds guard of the GCMC/INTERACT kernels: records the first violation
+// (site code, index, bound) in DevState and tells the caller to skip.
+__device__ __forceinline__ bool guard_bad(DevState *st, long long idx,
+                                          long long bound, int site) {
+  if (idx >= 0 && idx < bound) return false;
+  if (atomicCAS(&st->bad_site, 0, site) == 0) {
+    st->bad_index = (int)idx;
+    st->bad_bound = (int)bound;
+  }
+  atomicOr(&st->err, kErrBounds);
+  return true;
 }
 
 }  // namespace bgpu

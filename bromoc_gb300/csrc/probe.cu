@@ -1,0 +1,68 @@
+// FP32 FMA throughput probe: the denominator of the pair kernel's roofline
+// (the pair laws run on the FP32 pipe, not on tensor cores).  Eight
+// independent FMA chains per thread, two waves of 8 blocks x 256 threads per
+// SM, timed with CUDA events on the caller's stream.
+#include <algorithm>
+
+#include <cuda_runtime.h>
+
+#include "../../include/bromoc_gpu.h"
+
+namespace {
+
+__global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters,
+                                                  float b, float c) {
+  float a0 = threadIdx.x * 1e-7f, a1 = a0 + 1.0f, a2 = a0 + 2.0f, a3 = a0 + 3.0f;
+  float a4 = a0 + 4.0f, a5 = a0 + 5.0f, a6 = a0 + 6.0f, a7 = a0 + 7.0f;
+  for (int i = 0; i < iters; ++i) {
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      a0 = fmaf(a0, b, c);
+      a1 = fmaf(a1, b, c);
+      a2 = fmaf(a2, b, c);
+      a3 = fmaf(a3, b, c);
+      a4 = fmaf(a4, b, c);
+      a5 = fmaf(a5, b, c);
+      a6 = fmaf(a6, b, c);
+      a7 = fmaf(a7, b, c);
+    }
+  }
+  const float s = a0 + a1 + a2 + a3 + a4 + a5 + a6 + a7;
+  if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
+}
+
+}  // namespace
+
+extern "C" int bromoc_gpu_fp32_peak(void *stream, double *tflops) {
+  if (!tflops) return BROMOC_E_ARG;
+  cudaStream_t s = (cudaStream_t)stream;
+  int dev = 0, sms = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess ||
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    return BROMOC_E_CUDA;
+  const int blocks = sms * 16, threads = 256, iters = 4096;
+  float *out = nullptr;
+  cudaEvent_t e0, e1;
+  if (cudaMalloc(&out, (size_t)blocks * threads * sizeof(float)) != cudaSuccess)
+    return BROMOC_E_NOMEM;
+  cudaEventCreate(&e0);
+  cudaEventCreate(&e1);
+  double best = 0.0;
+  for (int rep = 0; rep < 5; ++rep) {
+    cudaEventRecord(e0, s);
+    k_fma_peak<<<blocks, threads, 0, s>>>(out, iters, 1.0000001f, 1e-7f);
+    cudaEventRecord(e1, s);
+    cudaEventSynchronize(e1);
+    float ms = 0.f;
+    cudaEventElapsedTime(&ms, e0, e1);
+    const double flops = 2.0 * 64.0 * iters * (double)blocks * threads;
+    if (rep > 0 && ms > 0.f) best = std::max(best, flops / (ms * 1e-3) / 1e12);
+  }
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  cudaFree(out);
+  const cudaError_t err = cudaGetLastError();
+  if (err != cudaSuccess) return BROMOC_E_CUDA;
+  *tflops = best;
+  return BROMOC_OK;
+}

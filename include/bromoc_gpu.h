@@ -235,8 +235,11 @@ int bromoc_gpu_get_particles(bromoc_ctx *ctx, int32_t *ntot, double *x,
 /* ---- hot path ------------------------------------------------------------
  * ENERGY (energy.mono.f90:19-692 minus DNA bonded terms): total energy with
  * the term breakdown in eterms[BROMOC_NTERMS]; forces into fx/fy/fz (host,
- * length ntot, may be NULL) when qforces != 0; warn[nttyp] (may be NULL)
- * receives the "particle inside membrane or protein" counters. */
+ * may be NULL) when qforces != 0 -- they receive the CURRENT device ntot
+ * values, which GCMC may have raised above the last upload, so pass
+ * capacity-sized buffers (the reference's datom-sized arrays); warn[nttyp]
+ * (may be NULL) receives the "particle inside membrane or protein"
+ * counters. */
 int bromoc_gpu_energy(bromoc_ctx *ctx, uint32_t terms, int32_t qforces,
                       double *fx, double *fy, double *fz, double *eterms,
                       int32_t *warn);
@@ -268,6 +271,41 @@ int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant,
                              int32_t ntot, int32_t nsites, int32_t nfix,
                              double *x, double *y, double *z,
                              const int32_t *typei, double *eterms);
+
+/* Drop-in for one or more cycles of simul1.f90:351-390 over HOST arrays:
+ * per cycle GRAND(ngcmc) then nbd x (ENERGY with forces + DYNAMICSn).  The
+ * particle arrays (capacity-sized buffers) are uploaded, advanced on the
+ * device and written back with the new *ntot (GCMC changes it).  Cycles are
+ * numbered cycle0, cycle0+1, ...; BD steps (cycle-1)*nbd + istep - 1. */
+int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms,
+                                 int32_t variant, int32_t ncycle,
+                                 int32_t ngcmc, int32_t nbd, uint64_t seed,
+                                 uint64_t cycle0, int32_t *ntot,
+                                 int32_t nsites, int32_t nfix, double *x,
+                                 double *y, double *z, int32_t *typei,
+                                 int32_t *ibuffer, double *eterms);
+
+/* Number of kernels this context has launched so far. */
+int64_t bromoc_gpu_launch_count(const bromoc_ctx *ctx);
+
+/* ---- diagnostics (no counterpart in the reference) ----------------------
+ * Per-kernel timing with CUDA events recorded on the launching stream around
+ * every launch of the kernel family `which` while timing is on. */
+enum {
+  BROMOC_K_PAIRS = 0,    /* ion-ion pair kernel                            */
+  BROMOC_K_RFCROSS = 1,  /* RFPAR cross-term pair kernel                   */
+  BROMOC_K_FIELDS = 2,   /* single-particle map/membrane kernel            */
+  BROMOC_K_ASSEMBLE = 3, /* force assembly + BD update                     */
+  BROMOC_K_NKINDS = 4
+};
+int bromoc_gpu_kernel_timing(bromoc_ctx *ctx, int32_t on);
+/* total milliseconds and number of timed launches since timing was turned
+ * on (synchronises the context's stream) */
+int bromoc_gpu_kernel_time(bromoc_ctx *ctx, int32_t which, double *total_ms,
+                           int64_t *launches);
+/* Measured FP32 FMA throughput of the current device (TFLOP/s), the
+ * denominator of the pair kernels' roofline. */
+int bromoc_gpu_fp32_peak(void *stream, double *tflops);
 
 /* GRAND (grand.f90:19-121): ngcmc grand-canonical insertion/deletion
  * attempts of cycle `cycle` (1-based icycle), device resident.  Uniforms are

@@ -274,6 +274,19 @@ int check_device_err(bromoc_ctx *ctx) {
 
 }  // namespace
 
+bool bromoc_ctx_pair_view(const bromoc_ctx *ctx, const KP **kp, cudaStream_t *stream,
+                          int *precision) {
+  if (!ctx || !ctx->have_sys || !ctx->have_types || !ctx->have_pairs) return false;
+  *kp = &ctx->kp;
+  *stream = ctx->stream;
+  *precision = ctx->precision;
+  return true;
+}
+
+int bromoc_ctx_fail(bromoc_ctx *ctx, int code, const char *msg) {
+  return set_err(ctx, code, "%s", msg);
+}
+
 extern "C" {
 
 int bromoc_gpu_abi_version(void) { return BROMOC_ABI_VERSION; }

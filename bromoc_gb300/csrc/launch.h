@@ -42,3 +42,10 @@ void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask,
 int interact_slots(int ntot_ub);
 
 }  // namespace bgpu
+
+// Read-only view of a context's uploaded pair laws, for entry points that
+// live outside api.cu.  Returns false until set_system/types/pairs are done.
+struct bromoc_ctx;
+bool bromoc_ctx_pair_view(const bromoc_ctx *ctx, const bgpu::KP **kp,
+                          cudaStream_t *stream, int *precision);
+int bromoc_ctx_fail(bromoc_ctx *ctx, int code, const char *msg);

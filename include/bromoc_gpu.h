@@ -285,6 +285,30 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms,
                                  double *y, double *z, int32_t *typei,
                                  int32_t *ibuffer, double *eterms);
 
+/* Ion-ion pair energy and forces for callers that must not allocate device
+ * memory while they run -- e.g. a host program that reserves its whole GPU
+ * memory budget at start-up and treats any later allocation as a failure,
+ * or an embedding whose device allocator belongs to another runtime.  It
+ * has no counterpart in the reference.
+ *
+ * Inputs and outputs are caller-owned DEVICE buffers: x,y,z,typei [n] (ions
+ * only, the first nfix fixed; typei signed ion types), fx,fy,fz [n] and
+ * eterms4 [4] = (eelec, evdw, esrpmf, eefpot).  The pair laws come from ctx
+ * (set_system/set_types/set_pairs; its precision selects FP64 or FP32 pair
+ * arithmetic); results equal bromoc_gpu_energy with BROMOC_M_NONBOND on a
+ * system without sites.  The scratch is a static device array sized for at
+ * most 4096 ions (about 1.6 MB per device, held until the process exits);
+ * n > 4096 returns BROMOC_E_CAPACITY.  No allocation or free happens in the
+ * call.  All calls on a device share that scratch: calls that overlap on
+ * the GPU race.  The first call on a device resolves the scratch address
+ * (cudaGetSymbolAddress with that device current) -- make it before any
+ * stream capture.  The call returns after the results are written. */
+int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t nfix,
+                                  const double *x, const double *y,
+                                  const double *z, const int32_t *typei,
+                                  double *fx, double *fy, double *fz,
+                                  double *eterms4);
+
 /* Number of kernels this context has launched so far. */
 int64_t bromoc_gpu_launch_count(const bromoc_ctx *ctx);
 

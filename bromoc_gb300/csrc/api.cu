@@ -19,7 +19,7 @@ using namespace bgpu;
 
 namespace {
 constexpr int kMaxChunks = 64;
-constexpr int kPairTile = 128;
+constexpr int kPairTile = 64;  // == kPairThreads of energy.cu
 constexpr int kSMs = 152;
 }  // namespace
 
@@ -172,7 +172,9 @@ int ensure_scratch(bromoc_ctx *ctx) {
   if ((rc = dalloc(ctx, &p.fis, 3 * cap))) return rc;
   if ((rc = dalloc(ctx, &p.frf, (size_t)kMaxChunks * 3 * cap))) return rc;
   const int tiles = (int)((cap + kPairTile - 1) / kPairTile) + 1;
-  ctx->nslot_cap = tiles * (2 * kMaxChunks + 4) + 8;
+  // fields (one block per 4 particles) + ion-ion and RFPAR (tiles x chunks)
+  // + ion-site (tiles)
+  ctx->nslot_cap = fields_blocks((int)cap) + tiles * (2 * kMaxChunks + 4) + 8;
   if ((rc = dalloc(ctx, &p.epart, (size_t)ctx->nslot_cap * kNTerms))) return rc;
   if ((rc = dalloc(ctx, &p.ipart, (size_t)tiles + 2))) return rc;
   if ((rc = dalloc(ctx, &p.rf_srfe, cap))) return rc;
@@ -212,7 +214,7 @@ void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
   }
   const int tiles = (ntargets + kPairTile - 1) / kPairTile;
   const int stiles = (nsources + kPairTile - 1) / kPairTile;
-  int want = (2 * kSMs + tiles - 1) / tiles;
+  int want = (8 * kSMs + tiles - 1) / tiles;  // ~8 two-warp blocks per SM
   want = std::max(1, std::min(std::min(want, stiles), kMaxChunks));
   int per = (stiles + want - 1) / want;  // source tiles per chunk
   chunk = per * kPairTile;
@@ -232,6 +234,7 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   chunking(nion, nion, plan.nchunk_rf, p.chunk_rf);
   p.nchunk_rf = plan.nchunk_rf;
   fl = AssembleFlags{};
+  fl.fp32_noise = plan.fp32;
   fl.ii = (mask & BROMOC_M_NONBOND) && nmob > 0 && plan.nchunk_ii > 0;
   fl.nchunk_ii = fl.ii ? plan.nchunk_ii : 0;
   fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
@@ -535,8 +538,29 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
   p.srpy = q->srpy;
   p.res = q->res;
   p.ires = q->res > 0 ? 1.0 / q->res : 0.0;
+  p.rthf = (float)p.rth;
+  p.srpxf = (float)p.srpx;
+  p.srpkf = (float)p.srpk;
+  p.srpyf = (float)p.srpy;
+  p.iresf = (float)p.ires;
   p.cnt = anyef ? q->cnt : 0;
   ctx->ntc = p.ntc = ntc;
+  std::vector<float4> pk(4 * (size_t)ntc);
+  auto bits = [](int v) {
+    float f;
+    std::memcpy(&f, &v, sizeof f);
+    return f;
+  };
+  for (int k = 0; k < ntc; ++k) {
+    const PairParamF &f = pf[k];
+    pk[4 * k + 0] = make_float4(f.fct, f.epp4, f.sgp2, bits(f.flags));
+    pk[4 * k + 1] = make_float4(f.c0, f.c1, f.c2, f.c3);
+    pk[4 * k + 2] = make_float4(f.c4, f.sc0, f.sc1, f.sc2);
+    pk[4 * k + 3] = make_float4(f.dm2lo, f.dm2hi, f.dmi, bits(f.nxi));
+  }
+  float4 *dpk = const_cast<float4 *>(p.ppk);
+  if (int rc2 = upload(ctx, &dpk, pk.data(), pk.size())) return rc2;
+  p.ppk = dpk;
   PairParam *dpp = const_cast<PairParam *>(p.pp);
   PairParamF *dpf = const_cast<PairParamF *>(p.ppf);
   int *dpi = const_cast<int *>(p.pidx);
@@ -916,7 +940,7 @@ int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj, d
   t.z = zj;
   CU(cudaMemcpyAsync(p.trial, &t, sizeof t, cudaMemcpyHostToDevice, ctx->stream));
   launch_interact(p, ntot, terms, 1, ctx->d_dener, ctx->stream);
-  ctx->launches += 2;
+  ctx->launches += 3;
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(dener, ctx->d_dener, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -934,6 +958,7 @@ int bromoc_gpu_dynamics(bromoc_ctx *ctx, int32_t variant, uint64_t seed, uint64_
   if (variant == BROMOC_DYN2 && p.nspline < 2)
     return set_err(ctx, BROMOC_E_STATE, "dynamics2 needs a PROFILE spline");
   AssembleFlags fl{};  // forces already assembled into fx,fy,fz: re-add nothing
+  fl.fp32_noise = ctx->precision == BROMOC_FP32;
   // k_assemble starts from ffield; with all partial flags cleared and ffield
   // holding the assembled forces the update uses exactly fx,fy,fz.
   CU(cudaMemcpyAsync(p.ffield, p.fx, p.cap * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));

@@ -65,6 +65,12 @@ struct Trial {
   int j;                    // 1-based slot (ntot+1 on insertion)
   int draw;                 // next uniform draw index of the attempt
   double x, y, z;
+  // single-particle part of INTERACT, filled by one warp before the pair
+  // sum: membrane + RFPAR self + static field + repulsion
+  double e_single;
+  double srfe, reff;        // RFPAR gathers of the trial (0 outside the map)
+  int rf_in;                // trial inside the RFPAR map
+  int pad;
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
@@ -116,6 +122,28 @@ __device__ inline void bd_noise3(uint64_t seed, uint64_t step, uint32_t slot,
   g[1] = box_muller(w[2], w[3]);
   philox4x32_10(slot, 1u, s2, s3, k0, k1, w);
   g[2] = box_muller(w[0], w[1]);
+}
+
+// Single-precision Box-Muller on the same Philox words: the radius uses
+// 1 - u formed exactly in integers (2^32 - w, never 0), the angle
+// cos(2 pi u) = cospi(2u).  Differs from the FP64 form by ~1e-7 relative.
+__device__ inline float box_muller_f(uint32_t wa, uint32_t wb) {
+  const float ua = (float)wa * 0x1p-32f;
+  const float u2 = wb == 0u ? 1.0f : (float)(0u - wb) * 0x1p-32f;
+  return cospif(2.0f * ua) * sqrtf(-2.0f * logf(u2));
+}
+
+__device__ inline void bd_noise3_f(uint64_t seed, uint64_t step, uint32_t slot,
+                                   double g[3]) {
+  uint32_t w[4];
+  const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
+  const uint32_t s2 = (uint32_t)step,
+                 s3 = ((uint32_t)(step >> 32) & 0x00FFFFFFu) | (1u << 24);
+  philox4x32_10(slot, 0u, s2, s3, k0, k1, w);
+  g[0] = box_muller_f(w[0], w[1]);
+  g[1] = box_muller_f(w[2], w[3]);
+  philox4x32_10(slot, 1u, s2, s3, k0, k1, w);
+  g[2] = box_muller_f(w[0], w[1]);
 }
 
 // GCMC uniform draw `draw` of attempt `attempt` of cycle `cycle`.

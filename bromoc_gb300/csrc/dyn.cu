@@ -8,7 +8,7 @@
 
 namespace bgpu {
 
-constexpr int kBdThreads = 256;
+constexpr int kBdThreads = 64;
 
 __device__ __forceinline__ void clamp_bd(double bdmax, double &d) {
   if (fabs(d) > bdmax) d = fsign(bdmax, d);
@@ -85,7 +85,10 @@ __global__ void __launch_bounds__(kBdThreads)
     clamp_bd(p.bdmax, dy);
     clamp_bd(p.bdmax, dz);
     double g[3];
-    bd_noise3(seed, step, slot, g);
+    if (fl.fp32_noise)
+      bd_noise3_f(seed, step, slot, g);
+    else
+      bd_noise3(seed, step, slot, g);
     double x = p.x[i] + dx + p.fact0n2 * g[0];
     double y = p.y[i] + dy + p.fact0n2 * g[1];
     double z = p.z[i] + dz + p.fact0n2 * g[2];
@@ -191,7 +194,10 @@ __global__ void __launch_bounds__(kBdThreads)
   clamp_bd(p.bdmax, dy);
   clamp_bd(p.bdmax, dz);
   double g[3];
-  bd_noise3(seed, step, slot, g);
+  if (fl.fp32_noise)
+    bd_noise3_f(seed, step, slot, g);
+  else
+    bd_noise3(seed, step, slot, g);
   double x = p.x[i] + dx + fact2 * g[0] + dDx;
   double y = p.y[i] + dy + fact2 * g[1] + dDy;
   double z = zold + dz + fact2 * g[2] + dDz;

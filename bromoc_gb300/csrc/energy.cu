@@ -7,102 +7,7 @@
 
 namespace bgpu {
 
-constexpr int kFieldThreads = 128;
-constexpr int kPairThreads = 128;  // targets per block == source tile size
-
-// ---------------------------------------------------------------------------
-// Single-particle terms: membrane, static field, repulsion map, RFPAR gather
-// and self term.  Thread per particle (sites, fixed ions, mobile ions).
-// Energy slot layout: (ememb, egsbpa, evdwgd, erfpar_self).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kFieldThreads)
-    k_fields(KP p, uint32_t mask, int qforces, int slot0) {
-  __shared__ double red[(kFieldThreads / 32) * 4];
-  const int ntot = p.st->ntot;
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  double e[4] = {0.0, 0.0, 0.0, 0.0};
-  if (i < ntot) {
-    const bool site = i < p.nsites;
-    const bool fixed = !site && i < p.nsites + p.nfix;
-    const double x = p.x[i], y = p.y[i], z = p.z[i];
-    const int iontype = site ? 0 : abs(p.typei[i]);
-    const int itype2 = site ? p.typtyp[i] : p.nwtype[iontype];
-    const double charge = site ? p.sitecharge[i] : p.cg[iontype];
-    const bool qf = qforces != 0;
-    double f[3] = {0.0, 0.0, 0.0};
-    if ((mask & 2u) && p.qmemb) {
-      const bool lgiat = !fixed && qf;
-      if (membrane_one(p, itype2, charge, x, y, z, lgiat, false, e[0], f))
-        atomicAdd(&p.warn[itype2], 1);
-    }
-    if ((mask & 4u) && p.qphix && !fixed && (!site || charge != 0.0))
-      staticf_one(p, x, y, z, charge, qf, e[1], f);
-    if ((mask & 8u) && p.qphiv && !fixed) {
-      const Grid3 &g = p.g2;
-      bool ok;
-      if (p.qtrln)
-        ok = x <= g.xbcen + g.tranx && x >= g.xbcen - g.tranx &&
-             y <= g.ybcen + g.trany && y >= g.ybcen - g.trany &&
-             z <= p.vzmax && z >= p.vzmin;
-      else
-        ok = x <= g.xbcen + g.tranx - g.dcel && x >= g.xbcen - g.tranx + g.dcel &&
-             y <= g.ybcen + g.trany - g.dcel && y >= g.ybcen - g.trany + g.dcel &&
-             z <= p.vzmax && z >= p.vzmin;
-      if (ok) {
-        size_t ifir;
-        double esvdw;
-        int it2;
-        phiv_select(p, i, iontype, ifir, esvdw, it2);
-        const double xi = x + g.tranx - g.xbcen, yi = y + g.trany - g.ybcen,
-                     zi = z + g.tranz - g.zbcen;
-        double phisum;
-        if (p.qtrln) {
-          phisum = vdwgd_trln_one(p, xi, yi, zi, ifir, esvdw, qf, e[2], f);
-          if (phisum >= p.thold8) atomicAdd(&p.warn[it2], 1);
-        } else {
-          phisum = vdwgd_spln_one(p, xi, yi, zi, ifir, esvdw, qf, e[2], f);
-          if (phisum >= p.thold27) atomicAdd(&p.warn[it2], 1);
-        }
-      }
-    }
-    if ((mask & 16u) && p.qrfpar && !site) {
-      double a1 = 0.0, a2 = 0.0, d1[3] = {0, 0, 0}, d2[3] = {0, 0, 0};
-      const bool in = in_grid(p.g3, x, y, z);
-      if (in) rfpar_gather(p, x, y, z, rfpar_ifir(p, iontype), qf, a1, a2, d1, d2);
-      p.rf_in[i] = in ? 1 : 0;
-      p.rf_srfe[i] = a1;
-      p.rf_reff[i] = a2;
-#pragma unroll
-      for (int k = 0; k < 3; ++k) {
-        p.rf_d1[3 * i + k] = d1[k];
-        p.rf_d2[3 * i + k] = d2[k];
-      }
-      if (in && !fixed) {  // self term, rfpar.f90:161-176
-        const double tau = p.celec * charge;
-        const double aux = tau * charge * a1;
-        e[3] += 0.5 * aux * a1;
-        if (qf) {
-          f[0] -= aux * d1[0];
-          f[1] -= aux * d1[1];
-          f[2] -= aux * d1[2];
-        }
-      }
-    }
-    p.ffield[i] = f[0];
-    p.ffield[p.cap + i] = f[1];
-    p.ffield[2 * p.cap + i] = f[2];
-  }
-  __shared__ double tot[4];
-  block_sum<4>(e, red, tot);
-  if (threadIdx.x == 0) {
-    double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
-    for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
-    dst[9] = tot[0];   // EMEMB
-    dst[10] = tot[1];  // EGSBPA
-    dst[12] = tot[2];  // EVDWGD
-    dst[13] = tot[3];  // ERFPAR
-  }
-}
+constexpr int kPairThreads = 64;  // targets per block == source tile size
 
 // ---------------------------------------------------------------------------
 // Ion-ion pairs, FP64.  Block (tx, cy): 128 mobile targets x source chunk cy.
@@ -232,13 +137,13 @@ __global__ void __launch_bounds__(kPairThreads)
         if (base + k == t) continue;
         const float4 h = sh[k], l = sl[k];
         const int code = __float_as_int(h.w);
-        const PairParamF &q = p.ppf[p.pidx[row + (code & 0xffff)]];
+        const int is = __ldg(p.pidx + row + (code & 0xffff));
         const float dx = (xh - h.x) + (xl - l.x);
         const float dy = (yh - h.y) + (yl - l.y);
         const float dz = (zh - h.z) + (zl - l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const float w = (code >> 16) ? 0.5f : 1.0f;
-        const float de = law32(p, q, r2, w, e, err);
+        const float de = law32k(p, is, r2, w, e);
         fx = fmaf(de, dx, fx);
         fy = fmaf(de, dy, fy);
         fz = fmaf(de, dz, fz);
@@ -639,10 +544,10 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
                   int qforces, cudaStream_t stream) {
   int slot = 0, nk = 0;
   const int nub = plan.ntot_ub;
-  const int nfb = (nub + kFieldThreads - 1) / kFieldThreads;
+  const int nfb = fields_blocks(nub);
   if (nfb > 0) {
     if (plan.t_fields) cudaEventRecord(plan.t_fields->a, stream);
-    k_fields<<<nfb, kFieldThreads, 0, stream>>>(p, mask, qforces, slot);
+    launch_fields(p, nub, mask, qforces, plan.fp32, slot, stream);
     if (plan.t_fields) cudaEventRecord(plan.t_fields->b, stream);
     slot += nfb;
     ++nk;
@@ -694,7 +599,7 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
 
 int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {
   const int nub = plan.ntot_ub;
-  int slot = (nub + kFieldThreads - 1) / kFieldThreads;
+  int slot = fields_blocks(nub);
   const int nmob_ub = nub - p.nsites - p.nfix;
   if ((mask & 1u) && nmob_ub > 0 && plan.nchunk_ii > 0)
     slot += ((nmob_ub + kPairThreads - 1) / kPairThreads) * plan.nchunk_ii;

@@ -1,27 +1,136 @@
 // INTERACT (interact.f90) and GRAND (grand.f90, insert.f90, find.f90) on the
 // device, all in FP64.  A GCMC attempt is three launches with no host round
-// trip: proposal (1 block) -> partial ΔE (grid over particles) -> final ΔE +
-// Im-Roux acceptance + insertion/deletion (1 block).  The live particle count
-// stays on the device (DevState::ntot).
+// trip: proposal + the trial's single-particle terms (1 block) -> pair and
+// RFPAR cross sums over the other particles (grid) -> total ΔE + Im-Roux
+// acceptance + insertion/deletion (1 block).  The live particle count stays
+// on the device (DevState::ntot).
 #include "launch.h"
 #include "physics.cuh"
 
 namespace bgpu {
 
-constexpr int kIaThreads = 128;
+constexpr int kIaThreads = 64;
 constexpr int kPropThreads = 256;
 
 int interact_slots(int ntot_ub) { return (ntot_ub + kIaThreads - 1) / kIaThreads; }
 
-// RFPAR gather of the trial particle (no derivatives).
-__device__ __forceinline__ void trial_rfpar(const KP &p, const Trial &tr,
-                                            double &sj, double &rj, bool &in) {
-  sj = rj = 0.0;
-  in = in_grid(p.g3, tr.x, tr.y, tr.z);
-  if (in) {
-    double d1[3], d2[3];
-    rfpar_gather(p, tr.x, tr.y, tr.z, rfpar_ifir(p, tr.itype), false, sj, rj,
-                 d1, d2);
+__device__ __forceinline__ double wsum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+__device__ __forceinline__ double seg8(double v) {
+  v += __shfl_xor_sync(0xffffffffu, v, 4);
+  v += __shfl_xor_sync(0xffffffffu, v, 2);
+  v += __shfl_xor_sync(0xffffffffu, v, 1);
+  return v;
+}
+
+// Single-particle terms of INTERACT for the trial, one full warp: lane 0 the
+// membrane (interact.f90:59-119), lanes 8g+corner the trilinear nodes of the
+// static field (staticf0.f90), repulsion (vdwgd0trln.f90), gsrfen and greff
+// (rfpar.f90:312-344 with its early exit); lanes 0..26 the B-spline nodes
+// (vdwgd0spln.f90).  Fills e_single, srfe, reff, rf_in of tr (lane 0).
+__device__ void trial_single_warp(const KP &p, Trial &tr, uint32_t mask, int qalert) {
+  const int lane = threadIdx.x & 31;
+  const int j0 = tr.j - 1;
+  const bool beion = j0 >= p.nsites;
+  const int jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
+  const double charge = beion ? p.cg[tr.itype] : p.sitecharge[j0];
+  const double x = tr.x, y = tr.y, z = tr.z;
+  const int g = lane >> 3, c = lane & 7;
+  const int ca = (c >> 2) & 1, cb = (c >> 1) & 1, cc = c & 1;
+  const bool do_phix = (mask & 4u) && p.qphix && (beion || charge != 0.0) &&
+                       in_grid(p.g1, x, y, z);
+  const Grid3 &g2 = p.g2;
+  const bool do_phiv = (mask & 8u) && p.qphiv && x <= g2.xbcen + g2.tranx &&
+                       x >= g2.xbcen - g2.tranx && y <= g2.ybcen + g2.trany &&
+                       y >= g2.ybcen - g2.trany && z <= p.vzmax && z >= p.vzmin;
+  const bool do_rf = (mask & 16u) && p.qrfpar && beion && in_grid(p.g3, x, y, z);
+  size_t vifir = 0;
+  double esvdw = 0.0;
+  int vit2 = 0;
+  if (do_phiv) phiv_select(p, j0, beion ? tr.itype : 0, vifir, esvdw, vit2);
+
+  double v = 0.0, psum = 0.0, gs_own = 0.0;
+  bool active = false;
+  double w = 0.0;
+  if ((g == 0 && do_phix) || (g == 1 && do_phiv && p.qtrln) || (g >= 2 && do_rf)) {
+    const Grid3 &gg = g == 0 ? p.g1 : (g == 1 ? p.g2 : p.g3);
+    const double xi = x + gg.tranx - gg.xbcen, yi = y + gg.trany - gg.ybcen,
+                 zi = z + gg.tranz - gg.zbcen;
+    int ix, iy, iz;
+    cell_of(gg, xi, yi, zi, ix, iy, iz);
+    const double ai = 1.0 - fabs(xi - (ix + ca) * gg.dcel) * gg.idcel;
+    const double bi = 1.0 - fabs(yi - (iy + cb) * gg.dcel) * gg.idcel;
+    const double ci = 1.0 - fabs(zi - (iz + cc) * gg.dcel) * gg.idcel;
+    w = ai * bi * ci;
+    const size_t node = (size_t)(ix + ca) * gg.ncly * gg.nclz + (size_t)(iy + cb) * gg.nclz +
+                        iz + cc;
+    if (g == 0) {
+      v = (double)__ldg(p.phix + node) * charge * p.celec;
+    } else if (g == 1) {
+      const double phis = (double)__ldg(p.phiv + vifir + node);
+      psum = phis;
+      v = esvdw * phis;
+    } else {
+      const size_t n3 = rfpar_ifir(p, tr.itype) + node;
+      gs_own = (double)__ldg(p.gsrfen + n3);
+      v = g == 2 ? gs_own : p.sqrfac * (double)__ldg(p.greff + n3);
+    }
+    active = true;
+  }
+  const double gs_c0 = __shfl_sync(0xffffffffu, gs_own, lane & ~1);
+  if (g >= 2 && active && !(gs_c0 != 0.0 && (cc == 0 || gs_own != 0.0))) active = false;
+  double le = active ? w * v : 0.0;
+  le = seg8(le);
+  psum = seg8(psum);
+  double be = 0.0, bsum = 0.0;
+  if (do_phiv && !p.qtrln) {  // warp-uniform
+    double e1 = 0.0, s1 = 0.0;
+    if (lane < 27) {
+      const double xi = x + g2.tranx - g2.xbcen, yi = y + g2.trany - g2.ybcen,
+                   zi = z + g2.tranz - g2.zbcen;
+      int ix, iy, iz;
+      spln_cell(g2, xi, yi, zi, ix, iy, iz);
+      const int k = ix - 1 + lane / 9, l = iy - 1 + (lane / 3) % 3, m = iz - 1 + lane % 3;
+      const double fi = m3(1.5 - (xi - k * g2.dcel) * g2.idcel) *
+                        m3(1.5 - (yi - l * g2.dcel) * g2.idcel) *
+                        m3(1.5 - (zi - m * g2.dcel) * g2.idcel);
+      if (fi != 0.0) {
+        const double phis = (double)__ldg(p.phiv + vifir + (size_t)k * g2.ncly * g2.nclz +
+                                          (size_t)l * g2.nclz + m);
+        s1 = phis;
+        e1 = fi * esvdw * phis;
+      }
+    }
+    be = wsum(e1);
+    bsum = wsum(s1);
+  }
+  const double e_v = __shfl_sync(0xffffffffu, le, 8), s_v = __shfl_sync(0xffffffffu, psum, 8);
+  const double sj = __shfl_sync(0xffffffffu, le, 16), rj = __shfl_sync(0xffffffffu, le, 24);
+  if (lane == 0) {
+    double e = 0.0;
+    if ((mask & 2u) && p.qmemb) {
+      double f[3];
+      if (membrane_one(p, jt2, charge, x, y, z, false, true, e, f) && qalert)
+        atomicAdd(&p.warn[jt2], 1);
+    }
+    if (do_rf) e += 0.5 * p.celec * p.cg[tr.itype] * p.cg[tr.itype] * sj * sj;
+    if (do_phix) e += le;
+    if (do_phiv) {
+      double ev = p.qtrln ? e_v : be;
+      const double ps = p.qtrln ? s_v : bsum;
+      if (ps >= (p.qtrln ? p.thold8 : p.thold27)) {
+        ev = 1.0e10;
+        if (qalert) atomicAdd(&p.warn[jt2], 1);
+      }
+      e += ev;
+    }
+    tr.e_single = e;
+    tr.srfe = do_rf ? sj : 0.0;
+    tr.reff = do_rf ? rj : 0.0;
+    tr.rf_in = do_rf ? 1 : 0;
   }
 }
 
@@ -29,8 +138,7 @@ __device__ __forceinline__ void trial_rfpar(const KP &p, const Trial &tr,
 // the RFPAR cross term (rfpar.f90:356-367).
 __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mask) {
   __shared__ double red[kIaThreads / 32];
-  __shared__ double s_sj, s_rj;
-  __shared__ int s_in;
+  __shared__ double tot[1];
   const Trial tr = *p.trial;
   const int ntot = p.st->ntot;
   const int j0 = tr.j - 1;
@@ -39,138 +147,85 @@ __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mas
   int jt2 = 0;
   if (tr.valid && !guard_bad(p.st, j0, (long long)p.cap + 1, 29))
     jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
-  const bool rf = (mask & 16u) && p.qrfpar && beion;
-  if (threadIdx.x == 0) {
-    double sj = 0, rj = 0;
-    bool in = false;
-    if (tr.valid && rf) trial_rfpar(p, tr, sj, rj, in);
-    s_sj = sj;
-    s_rj = rj;
-    s_in = in;
-  }
-  __syncthreads();
+  const bool rf = tr.valid && tr.rf_in;
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double u = 0.0;
   int err = 0;
   const bool ion_i = i >= p.nsites;
-  bool ok = tr.valid && i < ntot && i != j0 &&
-            !guard_bad(p.st, jt2 - 1, p.nttyp, 30);
+  bool ok = tr.valid && i < ntot && i != j0 && !guard_bad(p.st, jt2 - 1, p.nttyp, 30);
   if (ok && ion_i)
     ok = !guard_bad(p.st, abs(p.typei[i]) - p.nold - 1, p.ntype - p.nold, 31);
   if (ok) {
     const double dx = p.x[i] - tr.x, dy = p.y[i] - tr.y, dz = p.z[i] - tr.z;
     const double d2 = dx * dx + dy * dy + dz * dz;
     if (mask & 1u) {
-      if (beion && ion_i) {  // interact.f90:173-210
-        const int is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
-        u += law_interact64(p, p.pp[is], d2, err);
-      } else if (beion && !ion_i) {  // interact.f90:351-381
-        const int is = p.pidx[(p.typtyp[i] - 1) * p.nttyp + jt2 - 1];
-        u += law_interact64(p, p.pp[is], d2, err);
-      } else if (!beion && ion_i) {  // interact.f90:383-413
-        const int is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
-        u += law_interact64(p, p.pp[is], d2, err);
-      }
+      int is = -1;
+      if (beion && ion_i)  // interact.f90:173-210
+        is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
+      else if (beion && !ion_i)  // interact.f90:351-381
+        is = p.pidx[(p.typtyp[i] - 1) * p.nttyp + jt2 - 1];
+      else if (!beion && ion_i)  // interact.f90:383-413
+        is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
+      if (is >= 0) u += law_interact64(p, p.pp[is], d2, err);
     }
-    if (rf && s_in && ion_i && in_grid(p.g3, p.x[i], p.y[i], p.z[i])) {
+    if (rf && ion_i && in_grid(p.g3, p.x[i], p.y[i], p.z[i])) {
       double si, ri, d1[3], dd2[3];
       const int it = abs(p.typei[i]);
-      rfpar_gather(p, p.x[i], p.y[i], p.z[i], rfpar_ifir(p, it), false, si, ri,
-                   d1, dd2);
+      rfpar_gather(p, p.x[i], p.y[i], p.z[i], rfpar_ifir(p, it), false, si, ri, d1, dd2);
       if (si != 0.0) {
         const double tau = p.celec * p.cg[tr.itype];
-        const double reffij = s_rj * ri;
-        u += tau * p.cg[it] * reffij * s_sj * si / sqrt(reffij * reffij + d2);
+        const double reffij = tr.reff * ri;
+        u += tau * p.cg[it] * reffij * tr.srfe * si / sqrt(reffij * reffij + d2);
       }
     }
   }
   if (err) atomicOr(&p.st->err, err);
-  __shared__ double tot[1];
   block_sum<1>(&u, red, tot);
   if (threadIdx.x == 0) p.ipart[blockIdx.x] = tot[0];
 }
 
-// Single-particle terms of the trial + sum of the partials: the full ΔE.
-__device__ double interact_final(const KP &p, const Trial &tr, uint32_t mask,
-                                 int nblk, int qalert, double *red) {
+// Sum of the partials plus the trial's single-particle part: the full ΔE.
+__device__ double interact_total(const KP &p, const Trial &tr, int nblk, double *red,
+                                 double *tot) {
   double v = 0.0;
   for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += p.ipart[b];
-  __shared__ double tot[1];
   block_sum<1>(&v, red, tot);
-  if (threadIdx.x != 0) return 0.0;
-  const double pairs = tot[0];
-  const int j0 = tr.j - 1;
-  const bool beion = j0 >= p.nsites;
-  const int jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
-  const double charge = beion ? p.cg[tr.itype] : p.sitecharge[j0];
-  double dener = 0.0;
-  if ((mask & 2u) && p.qmemb) {  // interact.f90:59-119
-    double e = 0.0, f[3];
-    if (membrane_one(p, jt2, charge, tr.x, tr.y, tr.z, false, true, e, f) && qalert)
-      atomicAdd(&p.warn[jt2], 1);
-    dener = e;
-  }
-  if ((mask & 16u) && p.qrfpar && beion) {  // rfpar.f90:350-354 self part
-    double sj, rj;
-    bool in;
-    trial_rfpar(p, tr, sj, rj, in);
-    if (in) dener += 0.5 * p.celec * p.cg[tr.itype] * p.cg[tr.itype] * sj * sj;
-  }
-  if ((mask & 4u) && p.qphix && (beion || charge != 0.0)) {  // staticf0.f90
-    double e = 0.0, f[3];
-    staticf_one(p, tr.x, tr.y, tr.z, charge, false, e, f);
-    dener += e;
-  }
-  if ((mask & 8u) && p.qphiv) {  // vdwgd0trln.f90 / vdwgd0spln.f90
-    const Grid3 &g = p.g2;
-    const bool ok = tr.x <= g.xbcen + g.tranx && tr.x >= g.xbcen - g.tranx &&
-                    tr.y <= g.ybcen + g.trany && tr.y >= g.ybcen - g.trany &&
-                    tr.z <= p.vzmax && tr.z >= p.vzmin;
-    if (ok) {
-      size_t ifir;
-      double esvdw;
-      int it2;
-      phiv_select(p, j0, beion ? tr.itype : 0, ifir, esvdw, it2);
-      const double xi = tr.x + g.tranx - g.xbcen, yi = tr.y + g.trany - g.ybcen,
-                   zi = tr.z + g.tranz - g.zbcen;
-      double e = 0.0, f[3] = {0, 0, 0};
-      if (p.qtrln) {
-        if (vdwgd_trln_one(p, xi, yi, zi, ifir, esvdw, false, e, f) >= p.thold8) {
-          e = 1.0e10;
-          if (qalert) atomicAdd(&p.warn[jt2], 1);
-        }
-      } else {
-        if (vdwgd_spln0(p, xi, yi, zi, ifir, esvdw, e) >= p.thold27) {
-          e = 1.0e10;
-          if (qalert) atomicAdd(&p.warn[jt2], 1);
-        }
-      }
-      dener += e;
-    }
-  }
-  return dener + pairs;
+  return tr.e_single + tot[0];
+}
+
+// INTERACT entry: the host wrote the trial; one warp fills its single part.
+__global__ void __launch_bounds__(32) k_interact_prep(KP p, uint32_t mask, int qalert) {
+  __shared__ Trial s;
+  if (threadIdx.x == 0) s = *p.trial;
+  __syncwarp();
+  Trial t = s;
+  trial_single_warp(p, t, mask, qalert);
+  if (threadIdx.x == 0) *p.trial = t;
 }
 
 __global__ void __launch_bounds__(kIaThreads)
-    k_interact_final(KP p, uint32_t mask, int nblk, int qalert, double *out) {
+    k_interact_final(KP p, int nblk, double *out) {
   __shared__ double red[kIaThreads / 32];
+  __shared__ double tot[1];
   const Trial tr = *p.trial;
-  const double d = interact_final(p, tr, mask, nblk, qalert, red);
+  const double d = interact_total(p, tr, nblk, red, tot);
   if (threadIdx.x == 0) *out = d;
 }
 
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream) {
   const int nb = interact_slots(ntot_ub + 1);
+  k_interact_prep<<<1, 32, 0, stream>>>(p, mask, qalert);
   k_interact_part<<<nb, kIaThreads, 0, stream>>>(p, mask);
-  k_interact_final<<<1, kIaThreads, 0, stream>>>(p, mask, nb, qalert, dener_dev);
+  k_interact_final<<<1, kIaThreads, 0, stream>>>(p, nb, dener_dev);
 }
 
 // ---------------------------------------------------------------------------
-// GCMC proposal (grand.f90:42-86, insert.f90, find.f90).
+// GCMC proposal (grand.f90:42-86, insert.f90, find.f90) and the trial's
+// single-particle terms.
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kPropThreads)
-    k_gcmc_propose(KP p, uint64_t seed, uint64_t cycle, uint32_t attempt) {
+    k_gcmc_propose(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, uint32_t attempt) {
   __shared__ Trial s;
   __shared__ int counts[kPropThreads];
   if (threadIdx.x == 0) {
@@ -196,8 +251,7 @@ __global__ void __launch_bounds__(kPropThreads)
           t.z = p.lzmin[ib] + (p.lzmax[ib] - p.lzmin[ib]) * u3;
           ok = true;
           if (p.shape == 1) {
-            const double r2 = (t.x - p.cx) * (t.x - p.cx) +
-                              (t.y - p.cy) * (t.y - p.cy) +
+            const double r2 = (t.x - p.cx) * (t.x - p.cx) + (t.y - p.cy) * (t.y - p.cy) +
                               (t.z - p.cz) * (t.z - p.cz);
             ok = r2 > p.rmin[ib] * p.rmin[ib] && r2 < p.rmax[ib] * p.rmax[ib];
           } else if (p.shape == 2) {
@@ -275,6 +329,14 @@ __global__ void __launch_bounds__(kPropThreads)
     }
     __syncthreads();
   }
+  // the trial's single-particle terms (deletion trials raise warnings as
+  // INTERACT with Qalert does, insertion trials do not: grand.f90:48,86)
+  if (threadIdx.x < 32 && s.valid) {
+    Trial t = s;
+    trial_single_warp(p, t, mask, t.insert ? 0 : 1);
+    if (threadIdx.x == 0) s = t;
+  }
+  __syncthreads();
   if (threadIdx.x == 0) *p.trial = s;
 }
 
@@ -282,12 +344,12 @@ __global__ void __launch_bounds__(kPropThreads)
 // ΔE + acceptance + bookkeeping (grand.f90:48-116).
 // ---------------------------------------------------------------------------
 __global__ void __launch_bounds__(kIaThreads)
-    k_gcmc_accept(KP p, uint32_t mask, int nblk, uint64_t seed, uint64_t cycle,
-                  uint32_t attempt) {
+    k_gcmc_accept(KP p, int nblk, uint64_t seed, uint64_t cycle, uint32_t attempt) {
   __shared__ double red[kIaThreads / 32];
+  __shared__ double tot[1];
   const Trial tr = *p.trial;
   double dener = 0.0;
-  if (tr.valid) dener = interact_final(p, tr, mask, nblk, tr.insert ? 0 : 1, red);
+  if (tr.valid) dener = interact_total(p, tr, nblk, red, tot);
   if (threadIdx.x != 0) return;
   DevState *st = p.st;
   if (tr.valid && !guard_bad(st, tr.ib - 1, p.nbuffer, 21)) {
@@ -348,13 +410,12 @@ __global__ void __launch_bounds__(kIaThreads)
       p.prob[(size_t)b * (p.cap + 1) + st->nat[b]] += 1;
 }
 
-void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask,
-                         uint64_t seed, uint64_t cycle, uint32_t attempt,
-                         cudaStream_t stream) {
-  k_gcmc_propose<<<1, kPropThreads, 0, stream>>>(p, seed, cycle, attempt);
+void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask, uint64_t seed,
+                         uint64_t cycle, uint32_t attempt, cudaStream_t stream) {
+  k_gcmc_propose<<<1, kPropThreads, 0, stream>>>(p, mask, seed, cycle, attempt);
   const int nb = interact_slots(ntot_ub + 1);
   k_interact_part<<<nb, kIaThreads, 0, stream>>>(p, mask);
-  k_gcmc_accept<<<1, kIaThreads, 0, stream>>>(p, mask, nb, seed, cycle, attempt);
+  k_gcmc_accept<<<1, kIaThreads, 0, stream>>>(p, nb, seed, cycle, attempt);
 }
 
 }  // namespace bgpu

@@ -35,11 +35,15 @@ struct KP {
   // ---- pair laws ----
   const PairParam *pp;    // [ntc]
   const PairParamF *ppf;  // [ntc]
+  // [4*ntc] packed FP32 laws: (fct, epp4, sgp2, flags|npieces<<8),
+  // (c0, c1, c2, c3), (c4, sc0, sc1, sc2), (dm2lo, dm2hi, dmi, nxi)
+  const float4 *ppk;
   const int *pidx;        // [nttyp*nttyp] 0-based pair index, -1 none
   const double *ep;       // [3*cnt] reference form (p1,p2,p3)
   const float4 *ep32;     // [cnt] local form (a, b, c, x_k)
   int cnt;
   double rth, srpx, srpk, srpy, res, ires;
+  float rthf, srpxf, srpkf, srpyf, iresf;  // FP32 copies for the fast path
   // ---- sites ----
   const int *typtyp;      // [nsites] 1-based combined type
   const double *sitecharge;

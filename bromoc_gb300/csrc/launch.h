@@ -21,7 +21,13 @@ struct EnergyPlan {
 struct AssembleFlags {
   int ii, is, rf;     // which partial-force buffers are valid
   int nchunk_ii, nchunk_rf;
+  int fp32_noise;     // single-precision Box-Muller (FP32 mode)
 };
+
+// fields.cu: single-particle terms, one warp per particle
+int fields_blocks(int ntot_ub);
+void launch_fields(const KP &p, int ntot_ub, uint32_t mask, int qforces, bool fp32,
+                   int slot0, cudaStream_t stream);
 
 // energy.cu
 int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,

@@ -76,7 +76,7 @@ __device__ __forceinline__ float efp32(const KP &p, const PairParamF &q,
   }
   float ir = rsqrtf(x2);
   float r = x2 * ir;
-  int i = (int)((r - q.dmi) * (float)p.ires) + q.nxi;
+  int i = (int)((r - q.dmi) * p.iresf) + q.nxi;
   const int last = q.nxi + (q.flags >> 8) - 1;  // npieces packed in flags
   if (i < q.nxi || i > last) i = min(max(i, q.nxi), last);
   const float4 c = p.ep32[i];
@@ -153,7 +153,7 @@ __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
     e[1] += w * q.epp4 * (d12 - d6);
     de += q.epp4 * 6.0f * ir2 * (2.0f * d12 - d6);
   }
-  if ((q.flags & kSrp) && r2 <= (float)p.rth) {
+  if ((q.flags & kSrp) && r2 <= p.rthf) {
     float r = r2 * ir;
     float s, c;
     sincospif(q.c3 * (q.c1 - r), &s, &c);  // cos(c3 pi (c1 - r))
@@ -161,12 +161,85 @@ __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
     float e3 = pow6f(q.c1 * ir);
     float e0 = q.c0 * e1 * c + q.c4 * e3;
     float dc = (-q.c2 * c + q.c3 * (float)kPi * s) * q.c0 * e1 - 6.0f * q.c4 * e3 * ir;
-    if (r >= (float)p.srpx) {
-      float fdf = expf(-(float)p.srpk * (r - (float)p.srpx)) - (float)p.srpy;
-      dc = dc * fdf - e0 * (float)p.srpk * (fdf + (float)p.srpy);
+    if (r >= p.srpxf) {
+      float fdf = expf(-p.srpkf * (r - p.srpxf)) - p.srpyf;
+      dc = dc * fdf - e0 * p.srpkf * (fdf + p.srpyf);
       e0 = e0 * fdf;
     }
     e[2] += w * e0;
+    de -= dc * ir;
+  }
+  return de;
+}
+
+// ---- analytic pair law, FP32, packed table (p.ppk) ----------------------
+// The common Coulomb + LJ path needs one 16-byte load per pair; SRPMF
+// coefficients and the table constants are fetched only when used.
+__device__ __forceinline__ float law32k(const KP &p, int is, float r2, float w,
+                                        float e[4]) {
+  const float4 *q = p.ppk + 4 * is;
+  const float4 q0 = __ldg(q);
+  const int fl = __float_as_int(q0.w);
+  if (fl & kEfp) {
+    const float4 q2 = __ldg(q + 2), q3 = __ldg(q + 3);
+    float y, yp;
+    if (r2 < q3.x) {
+      const float ix2 = 1.0f / r2;
+      const float c = q2.y * pow6f(ix2);
+      yp = 12.0f * c * ix2;
+      y = c + q2.z;
+    } else if (r2 > q3.y) {
+      const float ix2 = 1.0f / r2;
+      const float c = q2.w * pow3f(ix2);
+      if (fl & kChr) {
+        const float f = q0.x * sqrtf(ix2);
+        yp = (6.0f * c + f) * ix2;
+        y = c + f;
+      } else {
+        yp = 6.0f * c * ix2;
+        y = c;
+      }
+    } else {
+      const float ir = rsqrtf(r2), r = r2 * ir;
+      const int nxi = __float_as_int(q3.w), last = nxi + (fl >> 8) - 1;
+      int i = (int)((r - q3.z) * p.iresf) + nxi;
+      i = min(max(i, nxi), last);
+      const float4 c = __ldg(p.ep32 + i);
+      const float t = r - c.w;
+      yp = -(c.y + 2.0f * c.z * t) * ir;
+      y = c.x + t * (c.y + t * c.z);
+    }
+    e[3] = fmaf(w, y, e[3]);
+    return yp;
+  }
+  const float ir = rsqrtf(r2), ir2 = ir * ir;
+  float de = 0.0f;
+  if (fl & kChr) {
+    const float cofo = q0.x * ir;
+    e[0] = fmaf(w, cofo, e[0]);
+    de = cofo * ir2;
+  }
+  if (fl & kLj) {
+    const float d6 = pow3f(q0.z * ir2), d12 = d6 * d6;
+    e[1] = fmaf(w, q0.y * (d12 - d6), e[1]);
+    de = fmaf(q0.y * 6.0f * ir2, 2.0f * d12 - d6, de);
+  }
+  if ((fl & kSrp) && r2 <= p.rthf) {
+    const float4 q1 = __ldg(q + 1);
+    const float c4 = __ldg(q + 2).x;
+    const float r = r2 * ir;
+    float s, c;
+    sincospif(q1.w * (q1.y - r), &s, &c);
+    const float e1 = expf((q1.y - r) * q1.z);
+    const float e3 = pow6f(q1.y * ir);
+    float e0 = q1.x * e1 * c + c4 * e3;
+    float dc = (-q1.z * c + q1.w * (float)kPi * s) * q1.x * e1 - 6.0f * c4 * e3 * ir;
+    if (r >= p.srpxf) {
+      const float fdf = expf(-p.srpkf * (r - p.srpxf)) - p.srpyf;
+      dc = dc * fdf - e0 * p.srpkf * (fdf + p.srpyf);
+      e0 = e0 * fdf;
+    }
+    e[2] = fmaf(w, e0, e[2]);
     de -= dc * ir;
   }
   return de;

@@ -127,6 +127,20 @@ def test_bd_steps(gpu_lib, oracle_mod, family):
     assert np.abs(pg - po).max() <= 1e-7
 
 
+@pytest.mark.parametrize("family", ["pairs", "maps_trln", "efpot"])
+def test_bd_step_fp32(gpu_lib, oracle_mod, family):
+    """FP32 pair path + single-precision Box-Muller: one BD step lands within
+    1e-5 A of the FP64 oracle (force error 1e-5 relative times D dt / kT,
+    plus ~1e-7 relative noise error)."""
+    spec = systems.all_families()[family](precision=abi.FP32)
+    g, o = _engines(spec, gpu_lib, oracle_mod)
+    g.bd_steps(1, seed=77, step0=3)
+    o.bd_steps(1, seed=77, step0=3)
+    pg = np.stack(g.get_particles()[:3], 1)
+    po = np.stack(o.get_particles()[:3], 1)
+    assert np.abs(pg - po).max() <= 1e-5
+
+
 @pytest.mark.parametrize("variant", [abi.DYN1, abi.DYN2, abi.DYN3])
 def test_dynamics_variants(gpu_lib, oracle_mod, variant):
     """dynamics1 (z-switch D), dynamics2 (spline D(z)), dynamics3 (DNA

@@ -251,7 +251,6 @@ def run_gpu(args, rank, world, local_rank):
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
     nmob = []
-    _lib.kernel_timing(eng, True)
     l0 = _lib.launch_count(eng)
     if dist:
         dist.barrier()
@@ -277,10 +276,19 @@ def run_gpu(args, rank, world, local_rank):
         dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
         tmax, ps = float(tm[0]), float(tt[1])
     value = ps / (tmax * 1e-3)
-    # per-kernel timing over the timed region
+    # per-kernel CUDA-event timing in a separate pass after the timed region
+    # (the event records would perturb it), same workload and step sequence
+    ktsteps = min(args.steps, 10)
+    cyc_k = args.warmup + args.steps + 1
+    _lib.kernel_timing(eng, True)
+    for k in range(ktsteps):
+        flush.zero_()
+        step(cyc_k + k)
+    torch.cuda.synchronize()
     kt = {name: _lib.kernel_time(eng, k) for name, k in
           (("pairs", _lib.K_PAIRS), ("rfcross", _lib.K_RFCROSS),
            ("fields", _lib.K_FIELDS), ("assemble", _lib.K_ASSEMBLE))}
+    kt = {k: v for k, v in kt.items() if v[1] > 0}
     _lib.kernel_timing(eng, False)
 
     # e2e through the host-array C ABI entry point (pinned host buffers)
@@ -298,7 +306,7 @@ def run_gpu(args, rank, world, local_rank):
     e2e_steps = max(3, args.steps // 2)
     h2d = d2h = 0
     e2e_ps = 0
-    cyc0 = args.warmup + args.steps + 1
+    cyc0 = args.warmup + args.steps + ktsteps + 1
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for k in range(e2e_steps):
@@ -327,12 +335,14 @@ def run_gpu(args, rank, world, local_rank):
     dom = max(kt, key=lambda k: kt[k][0])
     n_ion = statistics.mean(nmob) + spec.nfix
     pairs = n_ion * (n_ion - 1) / 2
-    if dom in ("pairs", "rfcross"):
-        per = PAIR_FLOP if dom == "pairs" else RF_FLOP
+    if dom == "pairs":
+        # the FP32 pair kernel evaluates the ion-ion law and the RFPAR cross
+        # term of every pair in one pass
+        per = PAIR_FLOP + RF_FLOP
         ms, nl = kt[dom]
         achieved = per * pairs / (ms / nl * 1e-3) / 1e12
-        traffic, prof = profile_traffic("k_ionion32" if dom == "pairs" else "k_rfcross")
-        roof = {"kernel": "k_ionion32" if dom == "pairs" else "k_rfcross",
+        traffic, prof = profile_traffic("k_pairs32")
+        roof = {"kernel": "k_pairs32",
                 "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                 "unit": "TFLOP/s", "frac": achieved / peak_fp32,
                 "traffic": traffic,

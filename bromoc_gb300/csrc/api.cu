@@ -52,6 +52,8 @@ struct bromoc_ctx {
   // last energy plan (for dynamics())
   AssembleFlags last_fl{};
   bool have_forces = false;
+  // FP32 mode: which copy of the positions is current (both after a pack)
+  bool ff_fresh = false, dbl_fresh = true;
   long long launches = 0;  // kernels launched by this context
   // diagnostic kernel timing: event pairs per kernel family
   bool timing = false;
@@ -162,6 +164,71 @@ int sync_ntot(bromoc_ctx *ctx) {
   return BROMOC_OK;
 }
 
+void split_ff(double v, float &h, float &l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+// One axis of one grid for the float-float cell search; an unset grid gets
+// bounds that no position satisfies.
+void fill_axis(AxisF &A, const Grid3 &g, int axis, bool set, double ub, double lb) {
+  A = AxisF{};
+  if (!set || g.dcel <= 0.0) {
+    A.ubh = -INFINITY;
+    A.lbh = INFINITY;
+    return;
+  }
+  const double tran = axis == 0 ? g.tranx : (axis == 1 ? g.trany : g.tranz);
+  const double cen = axis == 0 ? g.xbcen : (axis == 1 ? g.ybcen : g.zbcen);
+  split_ff(tran - cen, A.oh, A.ol);
+  split_ff(g.dcel, A.dh, A.dl);
+  A.idc = (float)g.idcel;
+  split_ff(ub, A.ubh, A.ubl);
+  split_ff(lb, A.lbh, A.lbl);
+  A.ncl = axis == 0 ? g.nclx : (axis == 1 ? g.ncly : g.nclz);
+}
+
+// Single-precision constants of the FP32 kernels (KP::f) from the FP64 state.
+void fill_f32(bromoc_ctx *ctx) {
+  KP &p = ctx->kp;
+  F32C &f = p.f;
+  const Grid3 *gs[3] = {&p.g1, &p.g2, &p.g3};
+  const bool set[3] = {p.qphix != 0, p.qphiv != 0, p.qrfpar != 0};
+  for (int m = 0; m < 3; ++m)
+    for (int a = 0; a < 3; ++a) {
+      const Grid3 &g = *gs[m];
+      const double cen = a == 0 ? g.xbcen : (a == 1 ? g.ybcen : g.zbcen);
+      const double tran = a == 0 ? g.tranx : (a == 1 ? g.trany : g.tranz);
+      // in-map tests of staticf1.f90:64-68, vdwgd1trln.f90, vdwgd1spln.f90:52
+      // (one cell narrower for the B-spline), rfpar.f90:80-85; repulsion z
+      // between vzmin and vzmax
+      const double mg = (m == 1 && !p.qtrln) ? g.dcel : 0.0;
+      double ub = cen + tran - mg, lb = cen - tran + mg;
+      if (m == 1 && a == 2) {
+        ub = p.vzmax;
+        lb = p.vzmin;
+      }
+      fill_axis(f.ax[3 * m + a], g, a, set[m], ub, lb);
+    }
+  for (int a = 0; a < 3; ++a) fill_axis(f.ax[9 + a], p.g2, a, set[1], 0.0, 0.0);
+  f.celec = (float)p.celec;
+  f.sqrfac = (float)p.sqrfac;
+  f.thold8 = (float)p.thold8;
+  f.thold27 = (float)p.thold27;
+  f.kbtdt = (float)p.kbtdt;
+  f.bdmax = (float)p.bdmax;
+  f.fact0n1 = (float)p.fact0n1;
+  f.fact0n2 = (float)p.fact0n2;
+  f.rsphe = (float)p.rsphe;
+  f.rsphe2 = (float)p.rsphe2;
+  f.iecx = (float)p.iecx;
+  f.iecy = (float)p.iecy;
+  const double b[6] = {p.lx2m, p.lx2p, p.ly2m, p.ly2p, p.lz2m, p.lz2p};
+  for (int k = 0; k < 6; ++k) split_ff(b[k], f.bh[k], f.bl[k]);
+  const double c[3] = {p.cx, p.cy, p.cz};
+  for (int k = 0; k < 3; ++k) split_ff(c[k], f.ch[k], f.cl[k]);
+}
+
 int ensure_scratch(bromoc_ctx *ctx) {
   if (ctx->have_scratch) return BROMOC_OK;
   KP &p = ctx->kp;
@@ -171,6 +238,16 @@ int ensure_scratch(bromoc_ctx *ctx) {
   if ((rc = dalloc(ctx, &p.fii, (size_t)kMaxChunks * 3 * cap))) return rc;
   if ((rc = dalloc(ctx, &p.fis, 3 * cap))) return rc;
   if ((rc = dalloc(ctx, &p.frf, (size_t)kMaxChunks * 3 * cap))) return rc;
+  if (ctx->precision == BROMOC_FP32) {
+    if ((rc = dalloc(ctx, &p.fii_f, (size_t)kMaxChunks * 3 * cap))) return rc;
+    if ((rc = dalloc(ctx, &p.frf_f, (size_t)kMaxChunks * 3 * cap))) return rc;
+    if ((rc = dalloc(ctx, &p.pk1, cap))) return rc;
+    if ((rc = dalloc(ctx, &p.pk2, cap))) return rc;
+    if ((rc = dalloc(ctx, &p.pk3, cap))) return rc;
+    if ((rc = dalloc(ctx, &p.rfd, 2 * cap))) return rc;
+    if ((rc = dalloc(ctx, &p.ffield_f, 3 * cap))) return rc;
+    if ((rc = dalloc(ctx, &p.fis_f, 3 * cap))) return rc;
+  }
   const int tiles = (int)((cap + kPairTile - 1) / kPairTile) + 1;
   // fields (one block per 4 particles) + ion-ion and RFPAR (tiles x chunks)
   // + ion-site (tiles)
@@ -229,17 +306,29 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   plan.reduce_energy = reduce;
   const int nion = plan.ntot_ub - p.nsites;
   const int nmob = nion - p.nfix;
-  chunking(nmob, nion, plan.nchunk_ii, p.chunk_ii);
-  p.nchunk_ii = plan.nchunk_ii;
-  chunking(nion, nion, plan.nchunk_rf, p.chunk_rf);
-  p.nchunk_rf = plan.nchunk_rf;
   fl = AssembleFlags{};
   fl.fp32_noise = plan.fp32;
-  fl.ii = (mask & BROMOC_M_NONBOND) && nmob > 0 && plan.nchunk_ii > 0;
-  fl.nchunk_ii = fl.ii ? plan.nchunk_ii : 0;
+  fl.fp32_partials = plan.fp32;
   fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
-  fl.rf = (mask & BROMOC_M_RFPAR) && p.qrfpar && nion > 0 && plan.nchunk_rf > 0;
-  fl.nchunk_rf = fl.rf ? plan.nchunk_rf : 0;
+  if (plan.fp32) {  // one fused pair kernel (ion-ion + RFPAR cross)
+    const PairCfg32 pc = pair_cfg32(p, plan.ntot_ub, mask);
+    chunking(pc.ntg, nion, plan.nchunk_ii, p.chunk_ii);
+    p.nchunk_ii = plan.nchunk_ii;
+    plan.nchunk_rf = p.nchunk_rf = 0;
+    fl.ii = pc.ntg > 0 && plan.nchunk_ii > 0;
+    fl.ii_from = pc.t0;
+    fl.nchunk_ii = fl.ii ? plan.nchunk_ii : 0;
+  } else {
+    chunking(nmob, nion, plan.nchunk_ii, p.chunk_ii);
+    p.nchunk_ii = plan.nchunk_ii;
+    chunking(nion, nion, plan.nchunk_rf, p.chunk_rf);
+    p.nchunk_rf = plan.nchunk_rf;
+    fl.ii = (mask & BROMOC_M_NONBOND) && nmob > 0 && plan.nchunk_ii > 0;
+    fl.ii_from = p.nsites + p.nfix;
+    fl.nchunk_ii = fl.ii ? plan.nchunk_ii : 0;
+    fl.rf = (mask & BROMOC_M_RFPAR) && p.qrfpar && nion > 0 && plan.nchunk_rf > 0;
+    fl.nchunk_rf = fl.rf ? plan.nchunk_rf : 0;
+  }
   plan.t_pairs = fl.ii ? next_timer(ctx, BROMOC_K_PAIRS) : nullptr;
   plan.t_rf = fl.rf ? next_timer(ctx, BROMOC_K_RFCROSS) : nullptr;
   plan.t_fields = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_FIELDS) : nullptr;
@@ -252,7 +341,29 @@ int check_ready(bromoc_ctx *ctx) {
   if (!ctx->have_sys || !ctx->have_types || !ctx->have_pairs)
     return set_err(ctx, BROMOC_E_STATE,
                    "set_system, set_types and set_pairs are required");
+  if (ctx->precision == BROMOC_FP32) fill_f32(ctx);
   return ensure_scratch(ctx);
+}
+
+// FP32 mode keeps the positions as float-float records while the per-step
+// kernels run (they never read the FP64 arrays); these make one form current
+// from the other.  No-ops in FP64 mode.
+int ensure_ff(bromoc_ctx *ctx) {
+  if (ctx->precision != BROMOC_FP32 || ctx->ff_fresh) return BROMOC_OK;
+  launch_pack(ctx->kp, ntot_ub(ctx), true, ctx->stream);
+  ctx->launches += 1;
+  ctx->ff_fresh = true;
+  CU(cudaGetLastError());
+  return BROMOC_OK;
+}
+
+int ensure_dbl(bromoc_ctx *ctx) {
+  if (ctx->precision != BROMOC_FP32 || ctx->dbl_fresh) return BROMOC_OK;
+  launch_pack(ctx->kp, ntot_ub(ctx), false, ctx->stream);
+  ctx->launches += 1;
+  ctx->dbl_fresh = true;
+  CU(cudaGetLastError());
+  return BROMOC_OK;
 }
 
 int check_device_err(bromoc_ctx *ctx) {
@@ -395,11 +506,16 @@ int bromoc_gpu_set_system(bromoc_ctx *ctx, const bromoc_system *q) {
       f1[i] = ctx->diffusion[i] * p.kbtdt;
       f2[i] = std::sqrt(2.0 * q->dt * ctx->diffusion[i]);
     }
+    std::vector<float2> ff(ctx->ntype + 1);
+    for (int i = 0; i <= ctx->ntype; ++i) ff[i] = make_float2((float)f1[i], (float)f2[i]);
     double *d1 = const_cast<double *>(p.fact1a), *d2 = const_cast<double *>(p.fact2a);
+    float2 *d3 = const_cast<float2 *>(p.fact_f);
     int rc = upload(ctx, &d1, f1.data(), f1.size());
     if (!rc) rc = upload(ctx, &d2, f2.data(), f2.size());
+    if (!rc) rc = upload(ctx, &d3, ff.data(), ff.size());
     p.fact1a = d1;
     p.fact2a = d2;
+    p.fact_f = d3;
     if (rc) return rc;
   }
   return BROMOC_OK;
@@ -577,6 +693,27 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
   p.ep = dep;
   p.ep32 = de32;
   if (rc) return rc;
+  {  // dense ion-ion table of the FP32 pair kernel
+    const int nion = nt - ndna;
+    std::vector<float4> tab((size_t)nion * nion);
+    bool ok = nion <= kIonTabTypes;
+    for (int a = 0; a < nion && ok; ++a)
+      for (int b = 0; b < nion; ++b) {
+        const int is = pidx[(size_t)(a + ndna) * nt + (b + ndna)];
+        const PairParamF &f = pf[is];
+        if (f.flags & kEfp) ok = false;
+        const int fl = f.flags & 15;
+        tab[(size_t)a * nion + b] =
+            make_float4((fl & kChr) ? f.fct : 0.0f, (fl & kLj) ? f.epp4 : 0.0f,
+                        (fl & kLj) ? f.sgp2 : 0.0f, bits((is << 4) | fl));
+      }
+    float4 *dt = const_cast<float4 *>(p.ipq);
+    if (!rc) rc = upload(ctx, &dt, tab.data(), std::max<size_t>(tab.size(), 1));
+    p.ipq = dt;
+    p.nion_t = nion;
+    p.ipq_ok = ok ? 1 : 0;
+    if (rc) return rc;
+  }
   ctx->have_pairs = true;
   return BROMOC_OK;
 }
@@ -670,6 +807,15 @@ int bromoc_gpu_set_phiv(bromoc_ctx *ctx, const bromoc_grid *g, const int8_t *phi
   }
   p.qsvdw = o->scal != nullptr;
   if (o->scal && (rc = upload1(ctx, &p.scal, o->scal, ctx->nttyp))) return rc;
+  {  // repulsion scale per combined type for the FP32 kernels (phiv_select)
+    std::vector<float> es(ctx->nttyp + 1, (float)o->svdw);
+    if (!o->nmcden && o->scal)
+      for (int t = 1; t <= ctx->nttyp; ++t) es[t] = (float)(o->svdw * o->scal[t - 1]);
+    float *d = const_cast<float *>(p.esvdw_f);
+    rc = upload(ctx, &d, es.data(), es.size());
+    p.esvdw_f = d;
+    if (rc) return rc;
+  }
   ctx->phiv_nmaps = o->nmaps;
   p.qphiv = 1;
   return BROMOC_OK;
@@ -773,6 +919,11 @@ int bromoc_gpu_set_countions(bromoc_ctx *ctx, int32_t cntpts, const double *zcon
   double *z = const_cast<double *>(p.zcont);
   int rc = upload(ctx, &z, zcont, cntpts);
   p.zcont = z;
+  std::vector<float2> zf(cntpts);
+  for (int j = 0; j < cntpts; ++j) split_ff(zcont[j], zf[j].x, zf[j].y);
+  float2 *zd = const_cast<float2 *>(p.zcont_ff);
+  if (!rc) rc = upload(ctx, &zd, zf.data(), zf.size());
+  p.zcont_ff = zd;
   const size_t n = (size_t)(ctx->ntype - ctx->nold) * cntpts;
   if (!rc) rc = upload<int>(ctx, &p.nforward, nullptr, n);
   if (!rc) rc = upload<int>(ctx, &p.nbackward, nullptr, n);
@@ -863,13 +1014,16 @@ int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
   ctx->attempts_at_known = ctx->attempts_total;
   ctx->rb_pending = false;
   ctx->have_forces = false;
+  ctx->ff_fresh = false;
+  ctx->dbl_fresh = true;
   return BROMOC_OK;
 }
 
 int bromoc_gpu_get_particles(bromoc_ctx *ctx, int32_t *ntot, double *x, double *y,
                              double *z, int32_t *typei, int32_t *ibuffer) {
   if (!ctx) return BROMOC_E_ARG;
-  int rc = sync_ntot(ctx);
+  int rc = ensure_dbl(ctx);
+  if (!rc) rc = sync_ntot(ctx);
   if (rc) return rc;
   const int n = ctx->ntot_known;
   KP &p = ctx->kp;
@@ -893,6 +1047,7 @@ int bromoc_gpu_energy(bromoc_ctx *ctx, uint32_t terms, int32_t qforces, double *
   EnergyPlan plan{};
   AssembleFlags fl{};
   if ((rc = plan_energy(ctx, terms, true, plan, fl))) return rc;
+  if ((rc = ensure_ff(ctx))) return rc;
   CU(cudaMemsetAsync(p.warn, 0, (ctx->nttyp + 1) * sizeof(int), ctx->stream));
   ctx->launches += launch_energy(p, plan, terms, qforces, ctx->stream);
   launch_assemble(p, plan.ntot_ub, fl, 0, 0, 0, 0, ctx->stream);
@@ -921,6 +1076,7 @@ int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj, d
   if (!ctx || !dener) return BROMOC_E_ARG;
   int rc = check_ready(ctx);
   if (rc) return rc;
+  if ((rc = ensure_dbl(ctx))) return rc;
   if ((rc = sync_ntot(ctx))) return rc;
   KP &p = ctx->kp;
   const int ntot = ctx->ntot_known;
@@ -957,20 +1113,17 @@ int bromoc_gpu_dynamics(bromoc_ctx *ctx, int32_t variant, uint64_t seed, uint64_
   KP &p = ctx->kp;
   if (variant == BROMOC_DYN2 && p.nspline < 2)
     return set_err(ctx, BROMOC_E_STATE, "dynamics2 needs a PROFILE spline");
-  AssembleFlags fl{};  // forces already assembled into fx,fy,fz: re-add nothing
+  AssembleFlags fl{};  // the force is fx,fy,fz as the last energy call left it
   fl.fp32_noise = ctx->precision == BROMOC_FP32;
-  // k_assemble starts from ffield; with all partial flags cleared and ffield
-  // holding the assembled forces the update uses exactly fx,fy,fz.
-  CU(cudaMemcpyAsync(p.ffield, p.fx, p.cap * sizeof(double), cudaMemcpyDeviceToDevice, ctx->stream));
-  CU(cudaMemcpyAsync(p.ffield + p.cap, p.fy, p.cap * sizeof(double), cudaMemcpyDeviceToDevice,
-                     ctx->stream));
-  CU(cudaMemcpyAsync(p.ffield + 2 * (size_t)p.cap, p.fz, p.cap * sizeof(double),
-                     cudaMemcpyDeviceToDevice, ctx->stream));
+  fl.fp32_partials = ctx->precision == BROMOC_FP32;
+  fl.use_total = 1;
+  if ((rc = ensure_ff(ctx))) return rc;
   launch_assemble(p, ntot_ub(ctx), fl, 1, variant, seed, step, ctx->stream);
   ctx->launches += 1;
   CU(cudaGetLastError());
   CU(cudaStreamSynchronize(ctx->stream));
   ctx->have_forces = false;
+  if (ctx->precision == BROMOC_FP32) ctx->dbl_fresh = false;
   return BROMOC_OK;
 }
 
@@ -988,6 +1141,8 @@ int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_
     return set_err(ctx, BROMOC_E_STATE, "dynamics3 needs PROXDIFF (diffcutoff > 0)");
   EnergyPlan plan{};
   AssembleFlags fl{};
+  if ((rc = ensure_ff(ctx))) return rc;
+  if (ctx->precision == BROMOC_FP32 && nsteps > 0) ctx->dbl_fresh = false;
   for (int k = 0; k < nsteps; ++k) {
     const bool last = k + 1 == nsteps;
     if ((rc = plan_energy(ctx, terms, last && eterms, plan, fl))) return rc;
@@ -1016,6 +1171,7 @@ int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant, i
   if (!ctx || !x || !y || !z || !typei) return set_err(ctx, BROMOC_E_ARG, "bd_steps_host: null");
   int rc = bromoc_gpu_set_particles(ctx, ntot, nsites, nfix, x, y, z, typei, nullptr);
   if (!rc) rc = bromoc_gpu_bd_steps(ctx, terms, variant, nsteps, seed, step0, eterms);
+  if (!rc) rc = ensure_dbl(ctx);
   if (!rc) {
     KP &p = ctx->kp;
     CU(cudaMemcpyAsync(x, p.x, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
@@ -1034,6 +1190,8 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   KP &p = ctx->kp;
   if (ngcmc < 0 || cycle < 1) return set_err(ctx, BROMOC_E_ARG, "grand: bad ngcmc or cycle");
   if (p.nbuffer < 1) return set_err(ctx, BROMOC_E_STATE, "grand: no buffers");
+  if ((rc = ensure_dbl(ctx))) return rc;
+  if (ngcmc > 0) ctx->ff_fresh = false;  // GCMC edits the FP64 arrays
   CU(cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), ctx->stream));
   for (int a = 0; a < ngcmc; ++a) {
     const int ub = ntot_ub(ctx);

@@ -21,6 +21,7 @@ constexpr double kRsmall = 1E-3;  // constamod.f90:83
 constexpr int kNTerms = 14;       // BROMOC_NTERMS
 constexpr int kMaxBuffers = 64;
 constexpr int kMaxTypes = 64;
+constexpr int kIonTabTypes = 16;  // ion types of the shared-memory pair table
 
 // error flags raised by kernels (bit mask in DevState::err)
 enum : int {
@@ -134,7 +135,7 @@ __device__ inline float box_muller_f(uint32_t wa, uint32_t wb) {
 }
 
 __device__ inline void bd_noise3_f(uint64_t seed, uint64_t step, uint32_t slot,
-                                   double g[3]) {
+                                   float g[3]) {
   uint32_t w[4];
   const uint32_t k0 = (uint32_t)seed, k1 = (uint32_t)(seed >> 32);
   const uint32_t s2 = (uint32_t)step,

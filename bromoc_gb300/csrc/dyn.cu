@@ -1,14 +1,15 @@
 // Force assembly and the Ermak-McCammon BD update (dynamics0-3.mono.f90,
 // dynamics0nuc.f90, fixcoor.f90, countions.f90), fused in one kernel: one
-// thread per particle sums its partial forces in a fixed order, writes
+// warp per particle sums its partial forces in a fixed order, writes
 // fx,fy,fz and, for a BD step, moves the particle with in-register Philox
 // noise.
+#include "ff.cuh"
 #include "launch.h"
 #include "physics.cuh"
 
 namespace bgpu {
 
-constexpr int kBdThreads = 64;
+constexpr int kAsmWarps = 8;  // particles per assembly block
 
 __device__ __forceinline__ void clamp_bd(double bdmax, double &d) {
   if (fabs(d) > bdmax) d = fsign(bdmax, d);
@@ -54,54 +55,12 @@ __device__ __forceinline__ void fixcoor(const KP &p, double &x, double &y,
   }
 }
 
-__global__ void __launch_bounds__(kBdThreads)
-    k_assemble(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,
-               uint64_t step) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  const int ntot = p.st->ntot;
-  if (i >= ntot) return;
-  const int cap = p.cap;
-  const int m0 = p.nsites + p.nfix;
-  double f[3];
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    double v = p.ffield[k * cap + i];
-    if (fl.ii && i >= m0)
-      for (int c = 0; c < fl.nchunk_ii; ++c) v += p.fii[((size_t)c * 3 + k) * cap + i];
-    if (fl.is) v += p.fis[k * cap + i];
-    if (fl.rf && i >= p.nsites)
-      for (int c = 0; c < fl.nchunk_rf; ++c) v += p.frf[((size_t)c * 3 + k) * cap + i];
-    f[k] = v;
-  }
-  p.fx[i] = f[0];
-  p.fy[i] = f[1];
-  p.fz[i] = f[2];
-  if (!do_bd) return;
-  const uint32_t slot = (uint32_t)i;
-  if (i < p.nsites) {  // dynamics0nuc.f90:31-44
-    if (!p.stfree[i]) return;
-    double dx = f[0] * p.fact0n1, dy = f[1] * p.fact0n1, dz = f[2] * p.fact0n1;
-    clamp_bd(p.bdmax, dx);
-    clamp_bd(p.bdmax, dy);
-    clamp_bd(p.bdmax, dz);
-    double g[3];
-    if (fl.fp32_noise)
-      bd_noise3_f(seed, step, slot, g);
-    else
-      bd_noise3(seed, step, slot, g);
-    double x = p.x[i] + dx + p.fact0n2 * g[0];
-    double y = p.y[i] + dy + p.fact0n2 * g[1];
-    double z = p.z[i] + dz + p.fact0n2 * g[2];
-    if (!p.qdnafree) fixcoor(p, x, y, z);
-    p.x[i] = x;
-    p.y[i] = y;
-    p.z[i] = z;
-    return;
-  }
-  if (i < m0) return;  // fixed ions do not move
-  const int itype = abs(p.typei[i]);
-  double fact1, fact2, dDx = 0.0, dDy = 0.0, dDz = 0.0;
-  const double zold = p.z[i];
+// Diffusion model of ion i at height zold: the drift and noise factors and
+// the gradient drift dD (dynamics0-3.mono.f90).
+__device__ __forceinline__ void diff_model(const KP &p, int variant, int i, int itype,
+                                           double zold, double &fact1, double &fact2,
+                                           double dD[3]) {
+  dD[0] = dD[1] = dD[2] = 0.0;
   if (variant == 1) {  // dynamics1.mono.f90:39-72
     const double pp3 = p.p3[itype];
     const double pore1 = -p.plength2 + p.pcenter, pore2 = p.plength2 + p.pcenter;
@@ -132,7 +91,7 @@ __global__ void __launch_bounds__(kBdThreads)
     const double didif = D * (1.0 - p.ampl3[itype]) * dsw;
     fact1 = idif * p.kbtdt;
     fact2 = sqrt(2.0 * p.dt * idif);
-    dDz = didif * p.dt;
+    dD[2] = didif * p.dt;
   } else if (variant == 2) {  // dynamics2.mono.f90:41-74
     const int n = p.nspline;
     double sw = 0.0, dsw = 0.0;
@@ -167,7 +126,7 @@ __global__ void __launch_bounds__(kBdThreads)
     const double idif = D * sw;
     fact1 = idif * p.kbtdt;
     fact2 = sqrt(2.0 * p.dt * idif);
-    dDz = D * dsw * p.dt;
+    dD[2] = D * dsw * p.dt;
   } else if (variant == 3) {  // dynamics3.mono.f90:40-59
     const double *dd = p.dids + 5 * (size_t)i;
     if (dd[0] > 0.0 && dd[0] <= p.diffcutoff) {
@@ -178,9 +137,9 @@ __global__ void __launch_bounds__(kBdThreads)
       const double idist = 1.0 / dd[1];
       fact1 = idif * p.kbtdt;
       fact2 = sqrt(2.0 * p.dt * idif);
-      dDx = didif * p.dt * dd[2] * idist;
-      dDy = didif * p.dt * dd[3] * idist;
-      dDz = didif * p.dt * dd[4] * idist;
+      dD[0] = didif * p.dt * dd[2] * idist;
+      dD[1] = didif * p.dt * dd[3] * idist;
+      dD[2] = didif * p.dt * dd[4] * idist;
     } else {
       fact1 = p.fact1a[itype];
       fact2 = p.fact2a[itype];
@@ -189,40 +148,290 @@ __global__ void __launch_bounds__(kBdThreads)
     fact1 = p.fact1a[itype];
     fact2 = p.fact2a[itype];
   }
+}
+
+// countions.f90:25-31
+__device__ __forceinline__ void count_crossings(const KP &p, int itype, double zold,
+                                                double z) {
+  const int it = itype - p.nold - 1;
+  for (int j = 0; j < p.cntpts; ++j) {
+    const double zc = p.zcont[j];
+    if (zold < zc && z >= zc)
+      atomicAdd(&p.nforward[it * p.cntpts + j], 1);
+    else if (zold >= zc && z < zc)
+      atomicAdd(&p.nbackward[it * p.cntpts + j], 1);
+  }
+}
+
+// BD move of particle i under the assembled force f (dynamics*.f90), FP64.
+__device__ __forceinline__ void bd_move(const KP &p, const AssembleFlags &fl,
+                                        int variant, uint64_t seed,
+                                        uint64_t step, int i, const double f[3]) {
+  const int m0 = p.nsites + p.nfix;
+  const uint32_t slot = (uint32_t)i;
+  double g[3];
+  if (i < m0 && (i >= p.nsites || !p.stfree[i])) return;  // fixed ions, frozen sites
+  if (fl.fp32_noise) {
+    float gf[3];
+    bd_noise3_f(seed, step, slot, gf);
+    g[0] = gf[0];
+    g[1] = gf[1];
+    g[2] = gf[2];
+  } else {
+    bd_noise3(seed, step, slot, g);
+  }
+  if (i < p.nsites) {  // dynamics0nuc.f90:31-44
+    double dx = f[0] * p.fact0n1, dy = f[1] * p.fact0n1, dz = f[2] * p.fact0n1;
+    clamp_bd(p.bdmax, dx);
+    clamp_bd(p.bdmax, dy);
+    clamp_bd(p.bdmax, dz);
+    double x = p.x[i] + dx + p.fact0n2 * g[0];
+    double y = p.y[i] + dy + p.fact0n2 * g[1];
+    double z = p.z[i] + dz + p.fact0n2 * g[2];
+    if (!p.qdnafree) fixcoor(p, x, y, z);
+    p.x[i] = x;
+    p.y[i] = y;
+    p.z[i] = z;
+    return;
+  }
+  const int itype = abs(p.typei[i]);
+  const double zold = p.z[i];
+  double fact1, fact2, dD[3];
+  diff_model(p, variant, i, itype, zold, fact1, fact2, dD);
   double dx = f[0] * fact1, dy = f[1] * fact1, dz = f[2] * fact1;
   clamp_bd(p.bdmax, dx);
   clamp_bd(p.bdmax, dy);
   clamp_bd(p.bdmax, dz);
-  double g[3];
-  if (fl.fp32_noise)
-    bd_noise3_f(seed, step, slot, g);
-  else
-    bd_noise3(seed, step, slot, g);
-  double x = p.x[i] + dx + fact2 * g[0] + dDx;
-  double y = p.y[i] + dy + fact2 * g[1] + dDy;
-  double z = zold + dz + fact2 * g[2] + dDz;
-  if (p.qcountion) {  // countions.f90:25-31
-    const int it = itype - p.nold - 1;
-    for (int j = 0; j < p.cntpts; ++j) {
-      const double zc = p.zcont[j];
-      if (zold < zc && z >= zc)
-        atomicAdd(&p.nforward[it * p.cntpts + j], 1);
-      else if (zold >= zc && z < zc)
-        atomicAdd(&p.nbackward[it * p.cntpts + j], 1);
-    }
-  }
+  double x = p.x[i] + dx + fact2 * g[0] + dD[0];
+  double y = p.y[i] + dy + fact2 * g[1] + dD[1];
+  double z = zold + dz + fact2 * g[2] + dD[2];
+  if (p.qcountion) count_crossings(p, itype, zold, z);
   fixcoor(p, x, y, z);
   p.x[i] = x;
   p.y[i] = y;
   p.z[i] = z;
 }
 
+// One warp per particle: lane c adds chunk partials c, c+32, ...; a fixed
+// shuffle tree sums the lanes, so the order is the same every run.
+__global__ void __launch_bounds__(32 * kAsmWarps)
+    k_assemble(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,
+               uint64_t step) {
+  const int i = blockIdx.x * kAsmWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int ntot = p.st->ntot;
+  if (i >= ntot) return;  // warp-uniform
+  const int cap = p.cap;
+  const int m0 = p.nsites + p.nfix;
+  double v[3] = {0.0, 0.0, 0.0};
+  if (fl.ii && i >= fl.ii_from)
+    for (int c = lane; c < fl.nchunk_ii; c += 32)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) v[k] += p.fii[((size_t)c * 3 + k) * cap + i];
+  if (fl.rf && i >= p.nsites)
+    for (int c = lane; c < fl.nchunk_rf; c += 32)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) v[k] += p.frf[((size_t)c * 3 + k) * cap + i];
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int k = 0; k < 3; ++k) v[k] += __shfl_xor_sync(0xffffffffu, v[k], o);
+  if (lane != 0) return;
+  double f[3];
+  if (fl.use_total) {
+    f[0] = p.fx[i];
+    f[1] = p.fy[i];
+    f[2] = p.fz[i];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      double w = p.ffield[k * cap + i] + v[k];
+      if (fl.is) w += p.fis[k * cap + i];
+      f[k] = w;
+    }
+    p.fx[i] = f[0];
+    p.fy[i] = f[1];
+    p.fz[i] = f[2];
+  }
+  if (do_bd) bd_move(p, fl, variant, seed, step, i, f);
+}
+
+// ---------------------------------------------------------------------------
+// FP32 mode.  Compensated float sums of the partial forces (two_sum), and
+// the BD move on the float-float position records.  Variants 1-3 evaluate
+// their diffusion profile in FP64 (options off the hot path); variant 0 and
+// everything else stay on the FP32 pipe.
+// ---------------------------------------------------------------------------
+__device__ __forceinline__ void clamp_f(float bdmax, float &d) {
+  if (fabsf(d) > bdmax) d = copysignf(bdmax, d);
+}
+
+// fixcoor.f90:19-68 on float-float coordinates
+__device__ __forceinline__ void fixcoor_ff(const KP &p, float h[3], float l[3]) {
+  const F32C &c = p.f;
+  if (p.shape == 1) {  // sphere: reflect through the wall
+    const float d0 = ff_diff(h[0], l[0], c.ch[0], c.cl[0]);
+    const float d1 = ff_diff(h[1], l[1], c.ch[1], c.cl[1]);
+    const float d2 = ff_diff(h[2], l[2], c.ch[2], c.cl[2]);
+    const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+    if (r2 > c.rsphe2) {
+      const float lzrad = 2.0f * c.rsphe * rsqrtf(r2) - 1.0f;
+      const float d[3] = {d0, d1, d2};
+      for (int k = 0; k < 3; ++k) {
+        h[k] = c.ch[k];
+        l[k] = c.cl[k];
+        ff_add(h[k], l[k], lzrad * d[k]);
+      }
+    }
+    return;
+  }
+  int k0 = 0;
+  if (p.shape == 2) {  // elliptic cylinder
+    const float ex = ff_diff(h[0], l[0], c.ch[0], c.cl[0]) * c.iecx;
+    const float ey = ff_diff(h[1], l[1], c.ch[1], c.cl[1]) * c.iecy;
+    const float r2 = fmaf(ex, ex, ey * ey);
+    if (r2 > 1.0f) {
+      const float r = 0.99999994f * rsqrtf(r2);
+      for (int k = 0; k < 2; ++k) {
+        const float d = ff_diff(h[k], l[k], c.ch[k], c.cl[k]);
+        h[k] = c.ch[k];
+        l[k] = c.cl[k];
+        ff_add(h[k], l[k], r * d);
+      }
+    }
+    k0 = 2;
+  }
+  for (int k = k0; k < 3; ++k) {  // box clamp (z only for the cylinder)
+    if (ff_diff(h[k], l[k], c.bh[2 * k], c.bl[2 * k]) < 0.0f) {
+      h[k] = c.bh[2 * k];
+      l[k] = c.bl[2 * k];
+    } else if (ff_diff(h[k], l[k], c.bh[2 * k + 1], c.bl[2 * k + 1]) > 0.0f) {
+      h[k] = c.bh[2 * k + 1];
+      l[k] = c.bl[2 * k + 1];
+    }
+  }
+}
+
+__device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t seed,
+                                            uint64_t step, int i, const float F[3]) {
+  const int m0 = p.nsites + p.nfix;
+  if (i < m0 && (i >= p.nsites || !p.stfree[i])) return;  // fixed ions, frozen sites
+  float4 h4 = p.pk1[i], l4 = p.pk2[i];
+  float h[3] = {h4.x, h4.y, h4.z}, l[3] = {l4.x, l4.y, l4.z};
+  float g[3];
+  bd_noise3_f(seed, step, (uint32_t)i, g);
+  if (i < p.nsites) {  // dynamics0nuc.f90:31-44
+    for (int k = 0; k < 3; ++k) {
+      float d = F[k] * p.f.fact0n1;
+      clamp_f(p.f.bdmax, d);
+      ff_add(h[k], l[k], fmaf(p.f.fact0n2, g[k], d));
+    }
+    if (!p.qdnafree) fixcoor_ff(p, h, l);
+  } else {
+    const int itype = abs(p.typei[i]);
+    float fact1, fact2, dD[3] = {0.0f, 0.0f, 0.0f};
+    if (variant == 0) {
+      const float2 fa = p.fact_f[itype];
+      fact1 = fa.x;
+      fact2 = fa.y;
+    } else {
+      double f1, f2, dd[3];
+      diff_model(p, variant, i, itype, (double)h[2] + (double)l[2], f1, f2, dd);
+      fact1 = (float)f1;
+      fact2 = (float)f2;
+      dD[0] = (float)dd[0];
+      dD[1] = (float)dd[1];
+      dD[2] = (float)dd[2];
+    }
+    const float zh0 = h[2], zl0 = l[2];
+    for (int k = 0; k < 3; ++k) {
+      float d = F[k] * fact1;
+      clamp_f(p.f.bdmax, d);
+      ff_add(h[k], l[k], fmaf(fact2, g[k], d) + dD[k]);
+    }
+    if (p.qcountion) {  // countions.f90:25-31, crossing tests in float-float
+      const int it = itype - p.nold - 1;
+      for (int j = 0; j < p.cntpts; ++j) {
+        const float2 zc = p.zcont_ff[j];
+        const bool was_below = ff_diff(zh0, zl0, zc.x, zc.y) < 0.0f;
+        const bool is_below = ff_diff(h[2], l[2], zc.x, zc.y) < 0.0f;
+        if (was_below && !is_below)
+          atomicAdd(&p.nforward[it * p.cntpts + j], 1);
+        else if (!was_below && is_below)
+          atomicAdd(&p.nbackward[it * p.cntpts + j], 1);
+      }
+    }
+    fixcoor_ff(p, h, l);
+  }
+  h4.x = h[0];
+  h4.y = h[1];
+  h4.z = h[2];
+  l4.x = l[0];
+  l4.y = l[1];
+  l4.z = l[2];
+  p.pk1[i] = h4;
+  p.pk2[i] = l4;
+}
+
+__global__ void __launch_bounds__(32 * kAsmWarps)
+    k_assemble_f32(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,
+                   uint64_t step) {
+  const int i = blockIdx.x * kAsmWarps + (threadIdx.x >> 5);
+  const int lane = threadIdx.x & 31;
+  const int ntot = p.st->ntot;
+  if (i >= ntot) return;  // warp-uniform
+  const int cap = p.cap;
+  const int m0 = p.nsites + p.nfix;
+  float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+  if (!fl.use_total) {
+    if (fl.ii && i >= fl.ii_from)
+      for (int ch = lane; ch < fl.nchunk_ii; ch += 32)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc2(s[k], c[k], p.fii_f[((size_t)ch * 3 + k) * cap + i]);
+    if (fl.rf && i >= p.nsites)
+      for (int ch = lane; ch < fl.nchunk_rf; ch += 32)
+#pragma unroll
+        for (int k = 0; k < 3; ++k) acc2(s[k], c[k], p.frf_f[((size_t)ch * 3 + k) * cap + i]);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+      for (int k = 0; k < 3; ++k) {
+        const float s2 = __shfl_xor_sync(0xffffffffu, s[k], o);
+        const float c2 = __shfl_xor_sync(0xffffffffu, c[k], o);
+        acc2p(s[k], c[k], s2, c2);
+      }
+  }
+  if (lane != 0) return;
+  float F[3];
+  if (fl.use_total) {
+    F[0] = (float)p.fx[i];
+    F[1] = (float)p.fy[i];
+    F[2] = (float)p.fz[i];
+  } else {
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      acc2(s[k], c[k], p.ffield_f[k * cap + i]);
+      if (fl.is) acc2(s[k], c[k], p.fis_f[k * cap + i]);
+      F[k] = s[k] + c[k];
+    }
+    if (!do_bd) {  // forces for the host (energy calls)
+      p.fx[i] = F[0];
+      p.fy[i] = F[1];
+      p.fz[i] = F[2];
+    }
+  }
+  if (do_bd) bd_move_f32(p, variant, seed, step, i, F);
+}
+
 void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,
                      int do_bd, int variant, uint64_t seed, uint64_t step,
                      cudaStream_t stream) {
   if (ntot_ub <= 0) return;
-  const int nb = (ntot_ub + kBdThreads - 1) / kBdThreads;
-  k_assemble<<<nb, kBdThreads, 0, stream>>>(p, fl, do_bd, variant, seed, step);
+  const int nb = (ntot_ub + kAsmWarps - 1) / kAsmWarps;
+  if (fl.fp32_partials)
+    k_assemble_f32<<<nb, 32 * kAsmWarps, 0, stream>>>(p, fl, do_bd, variant, seed, step);
+  else
+    k_assemble<<<nb, 32 * kAsmWarps, 0, stream>>>(p, fl, do_bd, variant, seed, step);
 }
 
 }  // namespace bgpu

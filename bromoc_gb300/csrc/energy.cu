@@ -2,6 +2,7 @@
 // terms).  One launch per term family; partial forces and block-partial
 // energies go to scratch and are reduced in a fixed order, so a run is
 // bit-reproducible.
+#include "ff.cuh"
 #include "launch.h"
 #include "physics.cuh"
 
@@ -83,88 +84,134 @@ __global__ void __launch_bounds__(kPairThreads)
   }
 }
 
-// hi/lo split of a double coordinate: x == hi + lo to ~2^-48 relative, so
-// (hi_i - hi_j) + (lo_i - lo_j) keeps ~1e-7 relative accuracy of dx even
-// when |x| >> |dx|.
-__device__ __forceinline__ void split2(double v, float &hi, float &lo) {
-  hi = (float)v;
-  lo = (float)(v - (double)hi);
-}
-
 // ---------------------------------------------------------------------------
-// Ion-ion pairs, FP32 arithmetic with per-tile FP32 and cross-tile FP64
-// accumulation.  Same decomposition as k_ionion64.
+// FP32 pair kernel: ion-ion laws and the RFPAR cross term in one pass over
+// (target, source) pairs.  Block (tx, cy): 64 targets x source chunk cy;
+// sources staged in shared memory from the float-float records (pk1 hi +
+// code, pk2 lo + srfe, pk3 reff/charge/flags).  No double-precision
+// instruction: dx = (hi_t - hi_s) + (lo_t - lo_s); forces and energies
+// accumulate in FP32 within the chunk and leave as FP32 partials (fii_f).
+//
+//   ion-ion (II): mobile targets against every other ion; weight 1/2 for a
+//     mobile source (the pair is summed by both), 1 for a fixed one.  With
+//     a dense type table (!EFP) the law is branch-free Coulomb + LJ (absent
+//     terms have zero coefficients) plus the SRPMF branch inside rth.
+//   RFPAR (RF): pair i = max(t, s), j = min: counts when i is mobile and in
+//     the map and srfe(j) != 0 (rfpar.f90:177-223); the energy is added by
+//     the target playing i; F_t = A sd1_t + B sd2_t + sum pr (r_t - r_s),
+//     the last sum folded into the per-pair radial factor.
 // ---------------------------------------------------------------------------
+template <bool II, bool RF, bool EFP>
 __global__ void __launch_bounds__(kPairThreads)
-    k_ionion32(KP p, int qforces, int slot0) {
-  __shared__ float4 sh[kPairThreads];
-  __shared__ float4 sl[kPairThreads];
-  __shared__ double red[(kPairThreads / 32) * 4];
+    k_pairs32(KP p, int qforces, int slot0, int t0) {
+  __shared__ float4 sh[kPairThreads], sl[kPairThreads], sq[RF ? kPairThreads : 1];
+  __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
+  __shared__ float red[(kPairThreads / 32) * 5];
+  __shared__ float tot[5];
+  const int nt = p.nion_t;
+  if (II && !EFP)
+    for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   const int ntot = p.st->ntot;
   const int m0 = p.nsites + p.nfix;
-  const int t = m0 + blockIdx.x * kPairThreads + threadIdx.x;
-  const bool tv = t < ntot;
+  const int t = t0 + blockIdx.x * kPairThreads + threadIdx.x;
+  float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th, tq = th;
+  int row = 0, tb = 0;
+  if (t < ntot) {
+    th = p.pk1[t];
+    tl = p.pk2[t];
+    if (RF) tq = p.pk3[t];
+    tb = __float_as_int(tq.z);
+    const int code = __float_as_int(th.w) & 0xffff;
+    row = EFP ? code * p.nttyp : (code - p.ndna) * nt;
+  }
+  const bool tmob = II && t < ntot && t >= m0;
+  const bool trf = RF && t < ntot && (tb & 1);
+  const float srt = tl.w, rft = tq.x, ct = p.f.celec * tq.y;
   const int s0 = p.nsites + blockIdx.y * p.chunk_ii;
   const int s1 = min(ntot, s0 + p.chunk_ii);
-  float xh = 0, yh = 0, zh = 0, xl = 0, yl = 0, zl = 0;
-  int row = 0;
-  if (tv) {
-    split2(p.x[t], xh, xl);
-    split2(p.y[t], yh, yl);
-    split2(p.z[t], zh, zl);
-    row = (p.nwtype[abs(p.typei[t])] - 1) * p.nttyp;
-  }
-  double fxa = 0.0, fya = 0.0, fza = 0.0, ed[4] = {0, 0, 0, 0};
-  int err = 0;
+  float fx = 0.f, fy = 0.f, fz = 0.f, A = 0.f, B = 0.f;
+  float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
   for (int base = s0; base < s1; base += kPairThreads) {
     const int s = base + threadIdx.x;
     __syncthreads();
     if (s < s1) {
-      float4 h, l;
-      split2(p.x[s], h.x, l.x);
-      split2(p.y[s], h.y, l.y);
-      split2(p.z[s], h.z, l.z);
-      h.w = __int_as_float((p.nwtype[abs(p.typei[s])] - 1) | ((s >= m0) << 16));
-      l.w = 0.0f;
-      sh[threadIdx.x] = h;
-      sl[threadIdx.x] = l;
+      sh[threadIdx.x] = p.pk1[s];
+      sl[threadIdx.x] = p.pk2[s];
+      if (RF) sq[threadIdx.x] = p.pk3[s];
     }
     __syncthreads();
     const int n = min(kPairThreads, s1 - base);
-    if (tv) {
-      float fx = 0.f, fy = 0.f, fz = 0.f, e[4] = {0.f, 0.f, 0.f, 0.f};
+    if (tmob || trf) {
+#pragma unroll 2
       for (int k = 0; k < n; ++k) {
-        if (base + k == t) continue;
+        const int s = base + k;
+        if (s == t) continue;
         const float4 h = sh[k], l = sl[k];
-        const int code = __float_as_int(h.w);
-        const int is = __ldg(p.pidx + row + (code & 0xffff));
-        const float dx = (xh - h.x) + (xl - l.x);
-        const float dy = (yh - h.y) + (yl - l.y);
-        const float dz = (zh - h.z) + (zl - l.z);
+        const float dx = (th.x - h.x) + (tl.x - l.x);
+        const float dy = (th.y - h.y) + (tl.y - l.y);
+        const float dz = (th.z - h.z) + (tl.z - l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float w = (code >> 16) ? 0.5f : 1.0f;
-        const float de = law32k(p, is, r2, w, e);
+        float de = 0.0f;
+        if (II && tmob) {
+          const int code = __float_as_int(h.w);
+          const float w = (code >> 16) ? 0.5f : 1.0f;
+          if (EFP) {
+            de = law32k(p, __ldg(p.pidx + row + (code & 0xffff)), r2, w, e);
+          } else {
+            const float4 q = tab[row + (code & 0xffff) - p.ndna];
+            const float ir = rsqrtf(r2), ir2 = ir * ir;
+            const float cofo = q.x * ir;
+            e[0] = fmaf(w, cofo, e[0]);
+            float d6 = q.z * ir2;
+            d6 = d6 * d6 * d6;
+            const float d12 = d6 * d6;
+            e[1] = fmaf(w, q.y * (d12 - d6), e[1]);
+            de = fmaf(cofo, ir2, (6.0f * q.y) * ir2 * fmaf(2.0f, d12, -d6));
+            const int qf = __float_as_int(q.w);
+            if ((qf & kSrp) && r2 <= p.rthf) de += srpmf32(p, qf >> 4, r2, ir, w, e);
+          }
+        }
+        if (RF && trf) {
+          const float4 q = sq[k];
+          const int sb = __float_as_int(q.z);
+          const bool t_is_i = t > s;
+          if (t_is_i ? ((tb & 4) && (sb & 8)) : ((sb & 4) && (tb & 8))) {
+            const float rij = q.x * rft, srij = l.w * srt;
+            const float rfdn = rsqrtf(fmaf(rij, rij, r2));
+            const float aux0 = ct * q.y;
+            const float a1 = aux0 * rij * rfdn;
+            if (t_is_i) e[4] = fmaf(a1, srij, e[4]);
+            const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
+            A = fmaf(-a1, l.w, A);
+            B = fmaf(-a2 * fmaf(rij, 0.5f, r2), q.x, B);
+            de = fmaf(a2, rij, de);
+          }
+        }
         fx = fmaf(de, dx, fx);
         fy = fmaf(de, dy, fy);
         fz = fmaf(de, dz, fz);
       }
-      if (qforces) {
-        fxa += fx;
-        fya += fy;
-        fza += fz;
-      }
-#pragma unroll
-      for (int m = 0; m < 4; ++m) ed[m] += e[m];
     }
   }
-  if (tv) {
-    double *f = p.fii + (size_t)blockIdx.y * 3 * p.cap;
-    f[t] = fxa;
-    f[p.cap + t] = fya;
-    f[2 * p.cap + t] = fza;
+  if (t < ntot) {
+    float fo[3] = {0.f, 0.f, 0.f};
+    if (qforces) {
+      fo[0] = fx;
+      fo[1] = fy;
+      fo[2] = fz;
+      if (trf) {
+        const float4 d1 = p.rfd[2 * (size_t)t], d2 = p.rfd[2 * (size_t)t + 1];
+        fo[0] = fmaf(A, d1.x, fmaf(B, d2.x, fo[0]));
+        fo[1] = fmaf(A, d1.y, fmaf(B, d2.y, fo[1]));
+        fo[2] = fmaf(A, d1.z, fmaf(B, d2.z, fo[2]));
+      }
+    }
+    float *f = p.fii_f + (size_t)blockIdx.y * 3 * p.cap;
+    f[t] = fo[0];
+    f[p.cap + t] = fo[1];
+    f[2 * p.cap + t] = fo[2];
   }
-  __shared__ double tot[4];
-  block_sum<4>(ed, red, tot);
+  block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
     for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
@@ -172,6 +219,7 @@ __global__ void __launch_bounds__(kPairThreads)
     dst[2] = tot[1];
     dst[3] = tot[2];
     dst[4] = tot[3];
+    dst[13] = tot[4];
   }
 }
 
@@ -181,7 +229,6 @@ __global__ void __launch_bounds__(kPairThreads)
 // seeded by site 1 exactly as the reference).  Energies of all pairs, forces
 // on mobile ions.  Sites are staged in shared memory (nsites <= 1024).
 // ---------------------------------------------------------------------------
-template <bool FP32>
 __global__ void __launch_bounds__(kPairThreads)
     k_ionsite(KP p, int qforces, int slot0) {
   extern __shared__ double sm[];
@@ -208,18 +255,8 @@ __global__ void __launch_bounds__(kPairThreads)
       const int is = p.pidx[row + sts[j]];
       const double dx = xi - sxs[j], dy = yi - sys[j], dz = zi - szs[j];
       const double d2 = dx * dx + dy * dy + dz * dz;
-      double de, dist = 0.0;
-      if (FP32) {
-        float ef[4] = {0.f, 0.f, 0.f, 0.f};
-        const float r2 = (float)d2;
-        de = (double)law32(p, p.ppf[is], r2, 1.0f, ef, err);
-        for (int m = 0; m < 4; ++m) e[m] += (double)ef[m];
-        if (p.qproxdiff && (p.pp[is].flags & kEfp) && d2 >= p.pp[is].dm2lo &&
-            d2 <= p.pp[is].dm2hi)
-          dist = sqrt(d2);
-      } else {
-        de = law64(p, p.pp[is], d2, 1.0, e, dist, err);
-      }
+      double dist = 0.0;
+      const double de = law64(p, p.pp[is], d2, 1.0, e, dist, err);
       if (p.qproxdiff && (p.pp[is].flags & kEfp) && dist > 0.0) {
         const double dm = dist - p.pp[is].dmi;
         if (j == 0 || dm < dd[0]) {
@@ -257,7 +294,6 @@ __global__ void __launch_bounds__(kPairThreads)
 }
 
 // Forces on free sites: block per site, threads over ions, fixed-tree sum.
-template <bool FP32>
 __global__ void __launch_bounds__(kPairThreads) k_siteforce(KP p) {
   __shared__ double red[(kPairThreads / 32) * 3];
   const int j = blockIdx.x;
@@ -271,14 +307,8 @@ __global__ void __launch_bounds__(kPairThreads) k_siteforce(KP p) {
       const int is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + col];
       const double dx = p.x[i] - xj, dy = p.y[i] - yj, dz = p.z[i] - zj;
       const double d2 = dx * dx + dy * dy + dz * dz;
-      double de, dist;
-      if (FP32) {
-        float ef[4];
-        de = (double)law32(p, p.ppf[is], (float)d2, 0.0f, ef, err);
-      } else {
-        double ed[4];
-        de = law64(p, p.pp[is], d2, 0.0, ed, dist, err);
-      }
+      double ed[4], dist;
+      const double de = law64(p, p.pp[is], d2, 0.0, ed, dist, err);
       f[0] -= de * dx;
       f[1] -= de * dy;
       f[2] -= de * dz;
@@ -294,13 +324,111 @@ __global__ void __launch_bounds__(kPairThreads) k_siteforce(KP p) {
 }
 
 // ---------------------------------------------------------------------------
+// Ion-site pairs in FP32 from the float-float records: the ion-centred walk
+// over the sites (energies, forces on ions, PROXDIFF record) and the
+// site-centred force sum, as the FP64 kernels above.
+// ---------------------------------------------------------------------------
+__global__ void __launch_bounds__(kPairThreads)
+    k_ionsite32(KP p, int qforces, int slot0) {
+  extern __shared__ float4 smf[];
+  float4 *sh = smf, *sl = smf + p.nsites;
+  __shared__ float red[(kPairThreads / 32) * 4];
+  __shared__ float tot[4];
+  for (int k = threadIdx.x; k < p.nsites; k += blockDim.x) {
+    sh[k] = p.pk1[k];
+    sl[k] = p.pk2[k];
+  }
+  __syncthreads();
+  const int ntot = p.st->ntot;
+  const int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x;
+  float e[4] = {0.f, 0.f, 0.f, 0.f};
+  int err = 0;
+  if (i < ntot) {
+    const bool mobile = i >= p.nsites + p.nfix;
+    const float4 th = p.pk1[i], tl = p.pk2[i];
+    const int row = (__float_as_int(th.w) & 0xffff) * p.nttyp;
+    float f[3] = {0.f, 0.f, 0.f}, dd[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int j = 0; j < p.nsites; ++j) {
+      const float4 h = sh[j], l = sl[j];
+      const int is = p.pidx[row + (__float_as_int(h.w) & 0xffff)];
+      const PairParamF &q = p.ppf[is];
+      const float dx = ff_diff(th.x, tl.x, h.x, l.x), dy = ff_diff(th.y, tl.y, h.y, l.y),
+                  dz = ff_diff(th.z, tl.z, h.z, l.z);
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      const float de = law32(p, q, r2, 1.0f, e, err);
+      if (p.qproxdiff && (q.flags & kEfp) && r2 >= q.dm2lo && r2 <= q.dm2hi) {
+        const float dist = sqrtf(r2);
+        const float dm = dist - q.dmi;
+        if (dist > 0.0f && (j == 0 || dm < dd[0])) {
+          dd[0] = dm;
+          dd[1] = dist;
+          dd[2] = dx;
+          dd[3] = dy;
+          dd[4] = dz;
+        }
+      }
+      if (qforces && mobile) {
+        f[0] = fmaf(de, dx, f[0]);
+        f[1] = fmaf(de, dy, f[1]);
+        f[2] = fmaf(de, dz, f[2]);
+      }
+    }
+    p.fis_f[i] = f[0];
+    p.fis_f[p.cap + i] = f[1];
+    p.fis_f[2 * p.cap + i] = f[2];
+    if (p.qproxdiff)
+      for (int m = 0; m < 5; ++m) p.dids[5 * (size_t)i + m] = (double)dd[m];
+  }
+  if (err) atomicOr(&p.st->err, err);
+  block_sum_f<4>(e, red, tot);
+  if (threadIdx.x == 0) {
+    double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
+    for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
+    dst[5] = tot[0];
+    dst[6] = tot[1];
+    dst[7] = tot[2];
+    dst[8] = tot[3];
+  }
+}
+
+__global__ void __launch_bounds__(kPairThreads) k_siteforce32(KP p) {
+  __shared__ float red[(kPairThreads / 32) * 3];
+  __shared__ float tot[3];
+  const int j = blockIdx.x;
+  const int ntot = p.st->ntot;
+  float f[3] = {0.f, 0.f, 0.f};
+  int err = 0;
+  if (p.stfree[j]) {
+    const float4 sh = p.pk1[j], sl = p.pk2[j];
+    const int col = __float_as_int(sh.w) & 0xffff;
+    for (int i = p.nsites + threadIdx.x; i < ntot; i += blockDim.x) {
+      const float4 h = p.pk1[i], l = p.pk2[i];
+      const int is = p.pidx[(__float_as_int(h.w) & 0xffff) * p.nttyp + col];
+      const float dx = ff_diff(h.x, l.x, sh.x, sl.x), dy = ff_diff(h.y, l.y, sh.y, sl.y),
+                  dz = ff_diff(h.z, l.z, sh.z, sl.z);
+      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+      float ef[4];
+      const float de = law32(p, p.ppf[is], r2, 0.0f, ef, err);
+      f[0] = fmaf(-de, dx, f[0]);
+      f[1] = fmaf(-de, dy, f[1]);
+      f[2] = fmaf(-de, dz, f[2]);
+    }
+  }
+  block_sum_f<3>(f, red, tot);
+  if (threadIdx.x == 0) {
+    p.fis_f[j] = tot[0];
+    p.fis_f[p.cap + j] = tot[1];
+    p.fis_f[2 * p.cap + j] = tot[2];
+  }
+}
+
+// ---------------------------------------------------------------------------
 // RFPAR cross term (rfpar.f90:177-223), target-centred over in-grid ions.
 // Pair (i > j) counts when i is mobile and srfe(j) != 0; its energy is added
 // by the target that plays i, each side adds its own force:
 //   F_t = A sd1_t + B sd2_t + P,  A = sum -a1 srfe_s,  B = sum aux3 reff_s,
 //   P = sum a2 reff_ts (r_t - r_s).
 // ---------------------------------------------------------------------------
-template <bool FP32>
 __global__ void __launch_bounds__(kPairThreads)
     k_rfcross(KP p, int qforces, int slot0) {
   __shared__ double sx[kPairThreads], sy[kPairThreads], sz[kPairThreads];
@@ -350,42 +478,22 @@ __global__ void __launch_bounds__(kPairThreads)
         const double srj = t_is_i ? ss[k] : srt;
         if (!i_mobile || srj == 0.0) continue;
         const double dx = xt - sx[k], dy = yt - sy[k], dz = zt - sz[k];
-        if (FP32) {
-          const float d2 = (float)(dx * dx + dy * dy + dz * dz);
-          const float rij = (float)(sr[k] * rft);
-          const float srij = (float)(ss[k] * srt);
-          const float rfdn = rsqrtf(fmaf(rij, rij, d2));
-          const float aux0 = (float)(p.celec * qt * sq[k]);
-          const float a1 = aux0 * rij * rfdn;
-          if (t_is_i) e += (double)(a1 * srij);
-          if (qforces) {
-            const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
-            const float aux3 = -a2 * (d2 + rij * 0.5f);
-            A += (double)(-a1 * (float)ss[k]);
-            B += (double)(aux3 * (float)sr[k]);
-            const float pr = a2 * rij;
-            P[0] += (double)pr * dx;
-            P[1] += (double)pr * dy;
-            P[2] += (double)pr * dz;
-          }
-        } else {
-          const double d2 = dx * dx + dy * dy + dz * dz;
-          const double rij = sr[k] * rft;
-          const double srij = ss[k] * srt;
-          const double rfdn = 1.0 / sqrt(rij * rij + d2);
-          const double aux0 = p.celec * qt * sq[k];
-          const double a1 = aux0 * (rij * rfdn);
-          if (t_is_i) e += a1 * srij;
-          if (qforces) {
-            const double a2 = aux0 * srij * rfdn * rfdn * rfdn;
-            const double aux3 = -a2 * (d2 + rij * 0.5);
-            A += -a1 * ss[k];
-            B += aux3 * sr[k];
-            const double pr = a2 * rij;
-            P[0] += pr * dx;
-            P[1] += pr * dy;
-            P[2] += pr * dz;
-          }
+        const double d2 = dx * dx + dy * dy + dz * dz;
+        const double rij = sr[k] * rft;
+        const double srij = ss[k] * srt;
+        const double rfdn = 1.0 / sqrt(rij * rij + d2);
+        const double aux0 = p.celec * qt * sq[k];
+        const double a1 = aux0 * (rij * rfdn);
+        if (t_is_i) e += a1 * srij;
+        if (qforces) {
+          const double a2 = aux0 * srij * rfdn * rfdn * rfdn;
+          const double aux3 = -a2 * (d2 + rij * 0.5);
+          A += -a1 * ss[k];
+          B += aux3 * sr[k];
+          const double pr = a2 * rij;
+          P[0] += pr * dx;
+          P[1] += pr * dy;
+          P[2] += pr * dz;
         }
       }
     }
@@ -402,107 +510,6 @@ __global__ void __launch_bounds__(kPairThreads)
   }
   __shared__ double tot[1];
   block_sum<1>(&e, red, tot);
-  if (threadIdx.x == 0) {
-    double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
-    for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
-    dst[13] = tot[0];
-  }
-}
-
-// ---------------------------------------------------------------------------
-// RFPAR cross term in single precision: hi/lo coordinates, FP32 pair math,
-// per-tile FP32 and cross-tile FP64 accumulation (no FP64 in the inner loop).
-// Source tile: (x_hi, y_hi, z_hi, srfe) (x_lo, y_lo, z_lo, reff) (q, flags).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kPairThreads)
-    k_rfcross32(KP p, int qforces, int slot0) {
-  __shared__ float4 sh[kPairThreads], sl[kPairThreads];
-  __shared__ float2 sqf[kPairThreads];
-  __shared__ double red[(kPairThreads / 32) * 1];
-  const int ntot = p.st->ntot;
-  const int m0 = p.nsites + p.nfix;
-  const int t = p.nsites + blockIdx.x * kPairThreads + threadIdx.x;
-  const bool tv = t < ntot && p.rf_in[t];
-  const int s0 = p.nsites + blockIdx.y * p.chunk_rf;
-  const int s1 = min(ntot, s0 + p.chunk_rf);
-  float xh = 0, yh = 0, zh = 0, xl = 0, yl = 0, zl = 0, srt = 0, rft = 0, ct = 0;
-  if (tv) {
-    split2(p.x[t], xh, xl);
-    split2(p.y[t], yh, yl);
-    split2(p.z[t], zh, zl);
-    srt = (float)p.rf_srfe[t];
-    rft = (float)p.rf_reff[t];
-    ct = (float)(p.celec * p.cg[abs(p.typei[t])]);
-  }
-  const bool tmob = t >= m0;
-  double Ad = 0, Bd = 0, Pd[3] = {0, 0, 0}, ed = 0;
-  for (int base = s0; base < s1; base += kPairThreads) {
-    const int s = base + threadIdx.x;
-    __syncthreads();
-    if (s < s1) {
-      float4 h, l;
-      split2(p.x[s], h.x, l.x);
-      split2(p.y[s], h.y, l.y);
-      split2(p.z[s], h.z, l.z);
-      h.w = (float)p.rf_srfe[s];
-      l.w = (float)p.rf_reff[s];
-      sh[threadIdx.x] = h;
-      sl[threadIdx.x] = l;
-      sqf[threadIdx.x] = make_float2((float)p.cg[abs(p.typei[s])],
-                                     __int_as_float(p.rf_in[s] | ((s >= m0) << 1)));
-    }
-    __syncthreads();
-    const int n = min(kPairThreads, s1 - base);
-    if (tv) {
-      float A = 0.f, B = 0.f, P0 = 0.f, P1 = 0.f, P2 = 0.f, e = 0.f;
-      for (int k = 0; k < n; ++k) {
-        const int s = base + k;
-        const float2 qf = sqf[k];
-        const int fl = __float_as_int(qf.y);
-        if (s == t || !(fl & 1)) continue;
-        const float4 h = sh[k], l = sl[k];
-        const bool t_is_i = t > s;
-        const bool i_mobile = t_is_i ? tmob : ((fl >> 1) & 1);
-        const float srj = t_is_i ? h.w : srt;
-        if (!i_mobile || srj == 0.0f) continue;
-        const float dx = (xh - h.x) + (xl - l.x);
-        const float dy = (yh - h.y) + (yl - l.y);
-        const float dz = (zh - h.z) + (zl - l.z);
-        const float d2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float rij = l.w * rft, srij = h.w * srt;
-        const float rfdn = rsqrtf(fmaf(rij, rij, d2));
-        const float aux0 = ct * qf.x;
-        const float a1 = aux0 * rij * rfdn;
-        if (t_is_i) e = fmaf(a1, srij, e);
-        const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
-        const float aux3 = -a2 * fmaf(rij, 0.5f, d2);
-        A = fmaf(-a1, h.w, A);
-        B = fmaf(aux3, l.w, B);
-        const float pr = a2 * rij;
-        P0 = fmaf(pr, dx, P0);
-        P1 = fmaf(pr, dy, P1);
-        P2 = fmaf(pr, dz, P2);
-      }
-      Ad += A;
-      Bd += B;
-      Pd[0] += P0;
-      Pd[1] += P1;
-      Pd[2] += P2;
-      ed += e;
-    }
-  }
-  if (t < ntot) {
-    double *f = p.frf + (size_t)blockIdx.y * 3 * p.cap;
-    double fo[3] = {0, 0, 0};
-    if (tv && qforces)
-      for (int k = 0; k < 3; ++k)
-        fo[k] = Ad * p.rf_d1[3 * t + k] + Bd * p.rf_d2[3 * t + k] + Pd[k];
-    f[t] = fo[0];
-    f[p.cap + t] = fo[1];
-    f[2 * p.cap + t] = fo[2];
-  }
-  __shared__ double tot[1];
-  block_sum<1>(&ed, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
     for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
@@ -554,13 +561,27 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
   }
   const bool nonbond = (mask & 1u) != 0;
   const int nmob_ub = nub - p.nsites - p.nfix;
-  if (nonbond && nmob_ub > 0 && plan.nchunk_ii > 0) {
+  const PairCfg32 pc = pair_cfg32(p, nub, mask);
+  if (plan.fp32 && pc.ntg > 0 && plan.nchunk_ii > 0) {
+    dim3 g((pc.ntg + kPairThreads - 1) / kPairThreads, plan.nchunk_ii);
+    if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
+    const bool efp = !p.ipq_ok;
+    if (pc.ii && pc.rf)
+      (efp ? k_pairs32<true, true, true> : k_pairs32<true, true, false>)
+          <<<g, kPairThreads, 0, stream>>>(p, qforces, slot, pc.t0);
+    else if (pc.ii)
+      (efp ? k_pairs32<true, false, true> : k_pairs32<true, false, false>)
+          <<<g, kPairThreads, 0, stream>>>(p, qforces, slot, pc.t0);
+    else
+      k_pairs32<false, true, true><<<g, kPairThreads, 0, stream>>>(p, qforces, slot, pc.t0);
+    if (plan.t_pairs) cudaEventRecord(plan.t_pairs->b, stream);
+    slot += g.x * g.y;
+    ++nk;
+  }
+  if (!plan.fp32 && nonbond && nmob_ub > 0 && plan.nchunk_ii > 0) {
     dim3 g((nmob_ub + kPairThreads - 1) / kPairThreads, plan.nchunk_ii);
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
-    if (plan.fp32)
-      k_ionion32<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
-    else
-      k_ionion64<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
+    k_ionion64<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->b, stream);
     slot += g.x * g.y;
     ++nk;
@@ -568,24 +589,22 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
   if (nonbond && p.nsites > 0 && nub > p.nsites) {
     const int nion_ub = nub - p.nsites;
     const int nb = (nion_ub + kPairThreads - 1) / kPairThreads;
-    const size_t smem = (size_t)p.nsites * (3 * sizeof(double) + sizeof(int));
     if (plan.fp32) {
-      k_ionsite<true><<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
-      if (qforces) k_siteforce<true><<<p.nsites, kPairThreads, 0, stream>>>(p);
+      const size_t smem = (size_t)p.nsites * 2 * sizeof(float4);
+      k_ionsite32<<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
+      if (qforces) k_siteforce32<<<p.nsites, kPairThreads, 0, stream>>>(p);
     } else {
-      k_ionsite<false><<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
-      if (qforces) k_siteforce<false><<<p.nsites, kPairThreads, 0, stream>>>(p);
+      const size_t smem = (size_t)p.nsites * (3 * sizeof(double) + sizeof(int));
+      k_ionsite<<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
+      if (qforces) k_siteforce<<<p.nsites, kPairThreads, 0, stream>>>(p);
     }
     slot += nb;
     nk += qforces ? 2 : 1;
   }
-  if ((mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0) {
+  if (!plan.fp32 && (mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0) {
     dim3 g((nub - p.nsites + kPairThreads - 1) / kPairThreads, plan.nchunk_rf);
     if (plan.t_rf) cudaEventRecord(plan.t_rf->a, stream);
-    if (plan.fp32)
-      k_rfcross32<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
-    else
-      k_rfcross<false><<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
+    k_rfcross<<<g, kPairThreads, 0, stream>>>(p, qforces, slot);
     if (plan.t_rf) cudaEventRecord(plan.t_rf->b, stream);
     slot += g.x * g.y;
     ++nk;
@@ -601,11 +620,16 @@ int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {
   const int nub = plan.ntot_ub;
   int slot = fields_blocks(nub);
   const int nmob_ub = nub - p.nsites - p.nfix;
-  if ((mask & 1u) && nmob_ub > 0 && plan.nchunk_ii > 0)
+  if (plan.fp32) {
+    const PairCfg32 pc = pair_cfg32(p, nub, mask);
+    if (pc.ntg > 0 && plan.nchunk_ii > 0)
+      slot += ((pc.ntg + kPairThreads - 1) / kPairThreads) * plan.nchunk_ii;
+  } else if ((mask & 1u) && nmob_ub > 0 && plan.nchunk_ii > 0) {
     slot += ((nmob_ub + kPairThreads - 1) / kPairThreads) * plan.nchunk_ii;
+  }
   if ((mask & 1u) && p.nsites > 0 && nub > p.nsites)
     slot += (nub - p.nsites + kPairThreads - 1) / kPairThreads;
-  if ((mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0)
+  if (!plan.fp32 && (mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0)
     slot += ((nub - p.nsites + kPairThreads - 1) / kPairThreads) * plan.nchunk_rf;
   return slot;
 }

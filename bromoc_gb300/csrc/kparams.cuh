@@ -15,6 +15,28 @@ struct PairParamF {  // FP32 copy of PairParam for the single-precision path
   int flags, nxi;
 };
 
+// One coordinate axis of one grid for the float-float cell search (ff.cuh).
+struct AxisF {
+  float oh, ol;    // tran - bcen as hi + lo
+  float dh, dl;    // dcel as hi + lo
+  float idc;       // 1 / dcel
+  float ubh, ubl;  // in-map test: lb <= position <= ub, each as hi + lo
+  float lbh, lbl;
+  int ncl;
+};
+
+// Single-precision constants of the FP32 path, filled on the host so that
+// no kernel of that path converts a double.
+struct F32C {
+  // lanes 3m+a: axis a of grid m (0 static field, 1 repulsion, 2 RFPAR);
+  // 9..11: the repulsion grid for the B-spline stencil
+  AxisF ax[12];
+  float celec, sqrfac, thold8, thold27, kbtdt, bdmax, fact0n1, fact0n2;
+  float rsphe, rsphe2, iecx, iecy;
+  float bh[6], bl[6];  // box bounds x-,x+,y-,y+,z-,z+ (hi, lo)
+  float ch[3], cl[3];  // shape centre (hi, lo)
+};
+
 struct KP {
   // ---- sizes (host-known) ----
   int cap, nsites, nfix, ntype, nold, nttyp, ndna, ntc;
@@ -39,6 +61,12 @@ struct KP {
   // (c0, c1, c2, c3), (c4, sc0, sc1, sc2), (dm2lo, dm2hi, dmi, nxi)
   const float4 *ppk;
   const int *pidx;        // [nttyp*nttyp] 0-based pair index, -1 none
+  // dense ion-ion law table for the FP32 pair kernel: [nion_t * nion_t] of
+  // (fct, epp4, sgp2, bits(is << 4 | flags)), fct/epp4 zeroed where the pair
+  // has no Coulomb/LJ term; ipq_ok when it applies (no tabulated ion-ion
+  // law, nion_t <= kIonTabTypes)
+  const float4 *ipq;
+  int nion_t, ipq_ok;
   const double *ep;       // [3*cnt] reference form (p1,p2,p3)
   const float4 *ep32;     // [cnt] local form (a, b, c, x_k)
   int cnt;
@@ -99,6 +127,19 @@ struct KP {
   double *fis;                  // [3*cap] ion-site forces (ions and sites)
   double *frf;                  // [nchunk_rf*3*cap] RFPAR cross partials
   int nchunk_rf, chunk_rf;
+  // FP32 path.  Particle records: positions as float-float pairs (the
+  // authoritative coordinates while the host marks them fresh), pair-law
+  // type code and charge (written by k_pack), RFPAR data (field kernel).
+  F32C f;
+  float4 *pk1;                  // [cap] (x_hi, y_hi, z_hi, bits(type-1 | mobile<<16))
+  float4 *pk2;                  // [cap] (x_lo, y_lo, z_lo, srfe)
+  float4 *pk3;                  // [cap] (reff, q, bits(rf flags), 0), flags in fields.cu
+  float4 *rfd;                  // [2*cap] srfe and reff gradients (xyz, 0)
+  float *ffield_f, *fis_f;      // [3*cap] single-particle / ion-site forces
+  float *fii_f, *frf_f;         // [nchunk*3*cap] partial forces
+  const float2 *fact_f;         // [ntype+1] (fact1a, fact2a)
+  const float2 *zcont_ff;       // [cntpts] crossing planes (hi, lo)
+  const float *esvdw_f;         // [nttyp+1] repulsion scale per combined type
   double *epart;                // [nslot*kNTerms] block partial energies
   double *eterms;               // [kNTerms] reduced energies
   int *warn;                    // [nttyp+1]

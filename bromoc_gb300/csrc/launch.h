@@ -18,16 +18,37 @@ struct EnergyPlan {
   KTimer *t_pairs = nullptr, *t_rf = nullptr, *t_fields = nullptr;
 };
 
+// Targets of the FP32 pair kernel: ion-ion terms act on mobile ions, the
+// RFPAR cross term on every ion in the map, so with RFPAR on the targets
+// start at the first ion, else at the first mobile ion.
+struct PairCfg32 {
+  bool ii, rf;
+  int t0, ntg;  // first target, number of target slots below ntot_ub
+};
+inline PairCfg32 pair_cfg32(const KP &p, int ntot_ub, uint32_t mask) {
+  PairCfg32 c{};
+  c.ii = (mask & 1u) && ntot_ub > p.nsites + p.nfix;
+  c.rf = (mask & 16u) && p.qrfpar && ntot_ub > p.nsites;
+  c.t0 = c.rf ? p.nsites : p.nsites + p.nfix;
+  c.ntg = (c.ii || c.rf) ? ntot_ub - c.t0 : 0;
+  return c;
+}
+
 struct AssembleFlags {
   int ii, is, rf;     // which partial-force buffers are valid
+  int ii_from;        // first particle with ion-ion (fused FP32: pair) partials
   int nchunk_ii, nchunk_rf;
   int fp32_noise;     // single-precision Box-Muller (FP32 mode)
+  int fp32_partials;  // FP32 mode: float partials, float-float positions
+  int use_total;      // the force is fx,fy,fz as assembled earlier (dynamics())
 };
 
 // fields.cu: single-particle terms, one warp per particle
 int fields_blocks(int ntot_ub);
 void launch_fields(const KP &p, int ntot_ub, uint32_t mask, int qforces, bool fp32,
                    int slot0, cudaStream_t stream);
+// FP32 mode: FP64 coordinates -> float-float records (to_records) or back
+void launch_pack(const KP &p, int ntot_ub, bool to_records, cudaStream_t stream);
 
 // energy.cu
 int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,

@@ -172,6 +172,30 @@ __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
   return de;
 }
 
+// ---- SRPMF of pair type is inside rth, FP32 (energy.mono.f90:147-175):
+// c0 exp((c1 - r) c2) cos(c3 pi (c1 - r)) + c4 (c1 / r)^6 with the taper
+// beyond srpx; adds w E to e[2] and returns its -(dE/dr)/r term.
+__device__ __forceinline__ float srpmf32(const KP &p, int is, float r2, float ir, float w,
+                                         float e[4]) {
+  const float4 *q = p.ppk + 4 * is;
+  const float4 q1 = __ldg(q + 1);
+  const float c4 = __ldg(q + 2).x;
+  const float r = r2 * ir;
+  float s, c;
+  sincospif(q1.w * (q1.y - r), &s, &c);
+  const float e1 = expf((q1.y - r) * q1.z);
+  const float e3 = pow6f(q1.y * ir);
+  float e0 = q1.x * e1 * c + c4 * e3;
+  float dc = (-q1.z * c + q1.w * (float)kPi * s) * q1.x * e1 - 6.0f * c4 * e3 * ir;
+  if (r >= p.srpxf) {
+    const float fdf = expf(-p.srpkf * (r - p.srpxf)) - p.srpyf;
+    dc = dc * fdf - e0 * p.srpkf * (fdf + p.srpyf);
+    e0 = e0 * fdf;
+  }
+  e[2] = fmaf(w, e0, e[2]);
+  return -dc * ir;
+}
+
 // ---- analytic pair law, FP32, packed table (p.ppk) ----------------------
 // The common Coulomb + LJ path needs one 16-byte load per pair; SRPMF
 // coefficients and the table constants are fetched only when used.
@@ -224,24 +248,7 @@ __device__ __forceinline__ float law32k(const KP &p, int is, float r2, float w,
     e[1] = fmaf(w, q0.y * (d12 - d6), e[1]);
     de = fmaf(q0.y * 6.0f * ir2, 2.0f * d12 - d6, de);
   }
-  if ((fl & kSrp) && r2 <= p.rthf) {
-    const float4 q1 = __ldg(q + 1);
-    const float c4 = __ldg(q + 2).x;
-    const float r = r2 * ir;
-    float s, c;
-    sincospif(q1.w * (q1.y - r), &s, &c);
-    const float e1 = expf((q1.y - r) * q1.z);
-    const float e3 = pow6f(q1.y * ir);
-    float e0 = q1.x * e1 * c + c4 * e3;
-    float dc = (-q1.z * c + q1.w * (float)kPi * s) * q1.x * e1 - 6.0f * c4 * e3 * ir;
-    if (r >= p.srpxf) {
-      const float fdf = expf(-p.srpkf * (r - p.srpxf)) - p.srpyf;
-      dc = dc * fdf - e0 * p.srpkf * (fdf + p.srpyf);
-      e0 = e0 * fdf;
-    }
-    e[2] = fmaf(w, e0, e[2]);
-    de -= dc * ir;
-  }
+  if ((fl & kSrp) && r2 <= p.rthf) de += srpmf32(p, is, r2, ir, w, e);
   return de;
 }
 

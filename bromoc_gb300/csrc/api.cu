@@ -48,6 +48,8 @@ struct bromoc_ctx {
   // scratch
   bool have_scratch = false;
   int nslot_cap = 0;
+  int ipart_slots = 0;
+  int tp_tiles = 0;  // tiles the Newton-3 partial buffers hold
   double *d_dener = nullptr;
   // last energy plan (for dynamics())
   AssembleFlags last_fl{};
@@ -254,6 +256,8 @@ int ensure_scratch(bromoc_ctx *ctx) {
   ctx->nslot_cap = fields_blocks((int)cap) + tiles * (2 * kMaxChunks + 4) + 8;
   if ((rc = dalloc(ctx, &p.epart, (size_t)ctx->nslot_cap * kNTerms))) return rc;
   if ((rc = dalloc(ctx, &p.ipart, (size_t)tiles + 2))) return rc;
+  ctx->ipart_slots = tiles + 2;
+  if ((rc = dalloc(ctx, &p.gc_rf, cap))) return rc;
   if ((rc = dalloc(ctx, &p.rf_srfe, cap))) return rc;
   if ((rc = dalloc(ctx, &p.rf_reff, cap))) return rc;
   if ((rc = dalloc(ctx, &p.rf_d1, 3 * cap))) return rc;
@@ -310,7 +314,28 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   fl.fp32_noise = plan.fp32;
   fl.fp32_partials = plan.fp32;
   fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
-  if (plan.fp32) {  // one fused pair kernel (ion-ion + RFPAR cross)
+  plan.ntile = p.ntile = 0;
+  if (plan.fp32 && nion > 0 && (nion + 31) / 32 <= kN3MaxTiles &&
+      pair_cfg32(p, plan.ntot_ub, mask).ntg > 0) {  // Newton-3 pair kernel
+    const int T = (nion + 31) / 32;
+    if (T > ctx->tp_tiles) {  // grow the tile-pair partials (rare)
+      const int Ta = std::min(kN3MaxTiles, T + 8);
+      CU(cudaStreamSynchronize(ctx->stream));
+      dfree(ctx, p.tpf);
+      dfree(ctx, p.tpb);
+      p.tpf = nullptr;
+      p.tpb = nullptr;
+      ctx->tp_tiles = 0;
+      int rc = dalloc(ctx, &p.tpf, (size_t)n3_pairs(Ta) * 64);
+      if (!rc) rc = dalloc(ctx, &p.tpb, (size_t)n3_pairs(Ta) * 64);
+      if (rc) return rc;
+      ctx->tp_tiles = Ta;
+    }
+    plan.ntile = p.ntile = T;
+    plan.nchunk_ii = plan.nchunk_rf = p.nchunk_ii = p.nchunk_rf = 0;
+    fl.ntile = T;
+    fl.rf_ab = pair_cfg32(p, plan.ntot_ub, mask).rf;
+  } else if (plan.fp32) {  // one fused pair kernel (ion-ion + RFPAR cross)
     const PairCfg32 pc = pair_cfg32(p, plan.ntot_ub, mask);
     chunking(pc.ntg, nion, plan.nchunk_ii, p.chunk_ii);
     p.nchunk_ii = plan.nchunk_ii;
@@ -329,7 +354,7 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
     fl.rf = (mask & BROMOC_M_RFPAR) && p.qrfpar && nion > 0 && plan.nchunk_rf > 0;
     fl.nchunk_rf = fl.rf ? plan.nchunk_rf : 0;
   }
-  plan.t_pairs = fl.ii ? next_timer(ctx, BROMOC_K_PAIRS) : nullptr;
+  plan.t_pairs = (fl.ii || fl.ntile) ? next_timer(ctx, BROMOC_K_PAIRS) : nullptr;
   plan.t_rf = fl.rf ? next_timer(ctx, BROMOC_K_RFCROSS) : nullptr;
   plan.t_fields = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_FIELDS) : nullptr;
   if (energy_slots(p, plan, mask) > ctx->nslot_cap)
@@ -379,6 +404,9 @@ int check_device_err(bromoc_ctx *ctx) {
     CU(cudaStreamSynchronize(ctx->stream));
     if (e == kErrCapacity)
       return set_err(ctx, BROMOC_E_CAPACITY, "grand: ntot is greater than capacity");
+    if (e & kErrBarrier)
+      return set_err(ctx, BROMOC_E_DEVICE,
+                     "grand: a grid barrier timed out (flags 0x%x); the kernel returned early", e);
     return set_err(ctx, BROMOC_E_DEVICE,
                    "device error flags 0x%x (guard site %d: index %d, bound %d)", e,
                    bad[0], bad[1], bad[2]);
@@ -1193,11 +1221,11 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   if ((rc = ensure_dbl(ctx))) return rc;
   if (ngcmc > 0) ctx->ff_fresh = false;  // GCMC edits the FP64 arrays
   CU(cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), ctx->stream));
-  for (int a = 0; a < ngcmc; ++a) {
-    const int ub = ntot_ub(ctx);
-    launch_gcmc_attempt(p, ub, terms, seed, cycle, (uint32_t)a, ctx->stream);
-    ctx->launches += 3;
-    ctx->attempts_total += 1;
+  if (ngcmc > 0) {
+    CU(launch_grand(p, ntot_ub(ctx), ctx->ipart_slots, terms, seed, cycle, ngcmc,
+                    ctx->stream));
+    ctx->launches += 1;
+    ctx->attempts_total += ngcmc;
   }
   CU(cudaGetLastError());
   if (!ctx->rb_pending) {  // refresh the ntot bound without blocking

@@ -29,6 +29,7 @@ enum : int {
   kErrTableIndex = 2,   // an effective-potential piece index out of range
   kErrFind = 4,         // GCMC deletion could not find the particle
   kErrBounds = 8,       // a guarded index was out of range (access skipped)
+  kErrBarrier = 16,     // a grid barrier gave up waiting (the kernel returned)
 };
 
 // packed pair-law switches
@@ -55,6 +56,8 @@ struct DevState {
   int nremove[kMaxBuffers];
   int ntotat[kMaxBuffers];
   double dener_sum;         // accumulated GCMC energy change
+  unsigned bar_count;       // grid barrier of the GRAND kernel: arrivals,
+  unsigned bar_gen;         // and generation (zeroed count before each launch)
 };
 
 // GCMC trial of one attempt (written by the proposal kernel).
@@ -71,7 +74,7 @@ struct Trial {
   double e_single;
   double srfe, reff;        // RFPAR gathers of the trial (0 outside the map)
   int rf_in;                // trial inside the RFPAR map
-  int pad;
+  int ntot;                 // live particle count when the trial was made
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------

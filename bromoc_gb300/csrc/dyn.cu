@@ -382,7 +382,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps)
   if (i >= ntot) return;  // warp-uniform
   const int cap = p.cap;
   const int m0 = p.nsites + p.nfix;
-  float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};
+  float s[3] = {0.f, 0.f, 0.f}, c[3] = {0.f, 0.f, 0.f};  // compensated sums
   if (!fl.use_total) {
     if (fl.ii && i >= fl.ii_from)
       for (int ch = lane; ch < fl.nchunk_ii; ch += 32)
@@ -412,8 +412,9 @@ __global__ void __launch_bounds__(32 * kAsmWarps)
     for (int k = 0; k < 3; ++k) {
       acc2(s[k], c[k], p.ffield_f[k * cap + i]);
       if (fl.is) acc2(s[k], c[k], p.fis_f[k * cap + i]);
-      F[k] = s[k] + c[k];
     }
+#pragma unroll
+    for (int k = 0; k < 3; ++k) F[k] = s[k] + c[k];
     if (!do_bd) {  // forces for the host (energy calls)
       p.fx[i] = F[0];
       p.fy[i] = F[1];
@@ -423,10 +424,110 @@ __global__ void __launch_bounds__(32 * kAsmWarps)
   if (do_bd) bd_move_f32(p, variant, seed, step, i, F);
 }
 
+// FP32 assembly for the Newton-3 partials: one block per tile of 32
+// particles (site tiles first, then the ion tiles of the pair kernel).  The
+// eight warps take every eighth tile pair of the ion tile, four at a time
+// with all loads issued first, each partial one coalesced 512-byte row;
+// their compensated sums meet in shared memory in a fixed order; warp 0 then
+// assembles and moves its 32 particles, one lane each.
+constexpr int kTileWarps = 8;
+
+__global__ void __launch_bounds__(32 * kTileWarps)
+    k_assemble_tiles(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,
+                     uint64_t step, int site_blocks) {
+  __shared__ float part[kTileWarps][10][32];
+  const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const bool ionblk = (int)blockIdx.x >= site_blocks;
+  const int Ti = blockIdx.x - site_blocks;
+  const int i = ionblk ? p.nsites + 32 * Ti + lane : 32 * blockIdx.x + lane;
+  const int ntot = p.st->ntot;
+  float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  if (ionblk) {
+    const int T = fl.ntile;
+    // batches of four tile pairs per warp: all loads issued before the sums
+    for (int u0 = w; u0 < T; u0 += 4 * kTileWarps) {
+      float4 va[4], vb[4];
+      float ba[4], bb[4];
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        const int u = u0 + j * kTileWarps;
+        va[j] = vb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ba[j] = bb[j] = 0.f;
+        if (u < T) {
+          const int q = u < Ti ? n3_index(T, u, Ti) : n3_index(T, Ti, u);
+          const size_t o = (size_t)q * 64 + (u < Ti ? 32 : 0) + lane;
+          va[j] = p.tpf[o];
+          if (fl.rf_ab) ba[j] = p.tpb[o];
+          if (u == Ti) {  // diagonal tile pair: the column side too
+            vb[j] = p.tpf[o + 32];
+            if (fl.rf_ab) bb[j] = p.tpb[o + 32];
+          }
+        }
+      }
+#pragma unroll
+      for (int j = 0; j < 4; ++j) {
+        acc2(s[0], c[0], va[j].x);
+        acc2(s[1], c[1], va[j].y);
+        acc2(s[2], c[2], va[j].z);
+        acc2(s[3], c[3], va[j].w);
+        acc2(s[4], c[4], ba[j]);
+        if (u0 + j * kTileWarps == Ti) {
+          acc2(s[0], c[0], vb[j].x);
+          acc2(s[1], c[1], vb[j].y);
+          acc2(s[2], c[2], vb[j].z);
+          acc2(s[3], c[3], vb[j].w);
+          acc2(s[4], c[4], bb[j]);
+        }
+      }
+    }
+  }
+  if (w > 0)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) {
+      part[w][k][lane] = s[k];
+      part[w][5 + k][lane] = c[k];
+    }
+  __syncthreads();
+  if (w != 0) return;
+  for (int ww = 1; ww < kTileWarps; ++ww)
+#pragma unroll
+    for (int k = 0; k < 5; ++k) acc2p(s[k], c[k], part[ww][k][lane], part[ww][5 + k][lane]);
+  if (i >= ntot || (!ionblk && i >= p.nsites)) return;
+  const int cap = p.cap;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    acc2(s[k], c[k], p.ffield_f[k * cap + i]);
+    if (fl.is) acc2(s[k], c[k], p.fis_f[k * cap + i]);
+  }
+  if (fl.rf_ab && ionblk) {  // A sd1 + B sd2 of the cross term, rfpar.f90:177-223
+    const float A = s[3] + c[3], B = s[4] + c[4];
+    const float4 d1 = p.rfd[2 * (size_t)i], d2 = p.rfd[2 * (size_t)i + 1];
+    acc2(s[0], c[0], fmaf(A, d1.x, B * d2.x));
+    acc2(s[1], c[1], fmaf(A, d1.y, B * d2.y));
+    acc2(s[2], c[2], fmaf(A, d1.z, B * d2.z));
+  }
+  float F[3];
+#pragma unroll
+  for (int k = 0; k < 3; ++k) F[k] = s[k] + c[k];
+  if (!do_bd) {  // forces for the host (energy calls)
+    p.fx[i] = F[0];
+    p.fy[i] = F[1];
+    p.fz[i] = F[2];
+    return;
+  }
+  bd_move_f32(p, variant, seed, step, i, F);
+}
+
 void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,
                      int do_bd, int variant, uint64_t seed, uint64_t step,
                      cudaStream_t stream) {
   if (ntot_ub <= 0) return;
+  if (fl.fp32_partials && fl.ntile > 0 && !fl.use_total) {
+    const int sb = (p.nsites + 31) / 32;
+    k_assemble_tiles<<<sb + fl.ntile, 32 * kTileWarps, 0, stream>>>(p, fl, do_bd, variant, seed,
+                                                                    step, sb);
+    return;
+  }
   const int nb = (ntot_ub + kAsmWarps - 1) / kAsmWarps;
   if (fl.fp32_partials)
     k_assemble_f32<<<nb, 32 * kAsmWarps, 0, stream>>>(p, fl, do_bd, variant, seed, step);

@@ -1,16 +1,17 @@
 // INTERACT (interact.f90) and GRAND (grand.f90, insert.f90, find.f90) on the
-// device, all in FP64.  A GCMC attempt is three launches with no host round
-// trip: proposal + the trial's single-particle terms (1 block) -> pair and
-// RFPAR cross sums over the other particles (grid) -> total ΔE + Im-Roux
-// acceptance + insertion/deletion (1 block).  The live particle count stays
-// on the device (DevState::ntot).
+// device, all in FP64.  INTERACT alone is four launches (RFPAR prepass, the
+// trial's single-particle terms, the O(N) sum, the total); GRAND runs all
+// its attempts in one cooperative launch (k_grand).  The live particle count
+// stays on the device (DevState::ntot).
+#include <algorithm>
+#include <cuda/atomic>
+
 #include "launch.h"
 #include "physics.cuh"
 
 namespace bgpu {
 
 constexpr int kIaThreads = 64;
-constexpr int kPropThreads = 256;
 
 int interact_slots(int ntot_ub) { return (ntot_ub + kIaThreads - 1) / kIaThreads; }
 
@@ -134,51 +135,89 @@ __device__ void trial_single_warp(const KP &p, Trial &tr, uint32_t mask, int qal
   }
 }
 
-// Partial ΔE over the other particles: pair terms (ion-ion, ion-site) and
-// the RFPAR cross term (rfpar.f90:356-367).
+// RFPAR (srfe, reff) of one ion at (x, y, z): the values INTERACT's cross
+// term gathers for every other ion (rfpar.f90:356-367); (0, 0) off the map.
+// Positions do not move during GRAND, so the GRAND kernel gathers them once
+// and keeps them current through insertions and deletions.
+__device__ __forceinline__ double2 rf_single(const KP &p, double x, double y, double z,
+                                             int itype) {
+  if (!in_grid(p.g3, x, y, z)) return make_double2(0.0, 0.0);
+  double si, ri, d1[3], d2[3];
+  rfpar_gather(p, x, y, z, rfpar_ifir(p, itype), false, si, ri, d1, d2);
+  return make_double2(si, ri);
+}
+
+// Trial read past L1: within the GRAND kernel another block wrote it.
+__device__ __forceinline__ Trial load_trial_cg(const Trial *t) {
+  Trial r;
+  const uint2 *src = reinterpret_cast<const uint2 *>(t);
+  uint2 *dst = reinterpret_cast<uint2 *>(&r);
+#pragma unroll
+  for (int k = 0; k < (int)(sizeof(Trial) / sizeof(uint2)); ++k) dst[k] = __ldcg(src + k);
+  return r;
+}
+
+// ΔE term of particle i (pair law + RFPAR cross) against the trial, the
+// O(N) part of INTERACT.  Particle data are read past L1 (__ldcg) because
+// inside the GRAND kernel they change between attempts.
+__device__ double interact_one(const KP &p, const Trial &tr, uint32_t mask, int i,
+                               int jt2, bool beion, bool rf, int &err) {
+  const bool ion_i = i >= p.nsites;
+  const int ti = __ldcg(p.typei + i);
+  if (ion_i && guard_bad(p.st, abs(ti) - p.nold - 1, p.ntype - p.nold, 31)) return 0.0;
+  const double dx = __ldcg(p.x + i) - tr.x, dy = __ldcg(p.y + i) - tr.y,
+               dz = __ldcg(p.z + i) - tr.z;
+  const double d2 = dx * dx + dy * dy + dz * dz;
+  double u = 0.0;
+  if (mask & 1u) {
+    int is = -1;
+    if (beion && ion_i)  // interact.f90:173-210
+      is = p.pidx[(p.nwtype[abs(ti)] - 1) * p.nttyp + jt2 - 1];
+    else if (beion && !ion_i)  // interact.f90:351-381
+      is = p.pidx[(p.typtyp[i] - 1) * p.nttyp + jt2 - 1];
+    else if (!beion && ion_i)  // interact.f90:383-413
+      is = p.pidx[(p.nwtype[abs(ti)] - 1) * p.nttyp + jt2 - 1];
+    if (is >= 0) u += law_interact64(p, p.pp[is], d2, err);
+  }
+  if (rf && ion_i) {
+    const double2 g = __ldcg(p.gc_rf + i);
+    if (g.x != 0.0) {
+      const double tau = p.celec * p.cg[tr.itype];
+      const double reffij = tr.reff * g.y;
+      u += tau * p.cg[abs(ti)] * reffij * tr.srfe * g.x / sqrt(reffij * reffij + d2);
+    }
+  }
+  return u;
+}
+
+// Combined type of the trial particle, 0 (and a guard record) when invalid.
+__device__ __forceinline__ int trial_type2(const KP &p, const Trial &tr) {
+  const int j0 = tr.j - 1;
+  if (!tr.valid || guard_bad(p.st, j0, (long long)p.cap + 1, 29)) return 0;
+  const int jt2 = j0 >= p.nsites ? p.nwtype[tr.itype] : p.typtyp[j0];
+  return guard_bad(p.st, jt2 - 1, p.nttyp, 30) ? 0 : jt2;
+}
+
+// RFPAR prepass of INTERACT: (srfe, reff) of every ion at its position.
+__global__ void k_rf_prepass(KP p) {
+  const int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.st->ntot) return;
+  p.gc_rf[i] = rf_single(p, p.x[i], p.y[i], p.z[i], abs(p.typei[i]));
+}
+
+// Partial ΔE over the other particles, one thread per particle.
 __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mask) {
   __shared__ double red[kIaThreads / 32];
   __shared__ double tot[1];
   const Trial tr = *p.trial;
   const int ntot = p.st->ntot;
-  const int j0 = tr.j - 1;
-  // an invalid trial (rejected before INTERACT) carries no slot or type
-  const bool beion = tr.valid && j0 >= p.nsites;
-  int jt2 = 0;
-  if (tr.valid && !guard_bad(p.st, j0, (long long)p.cap + 1, 29))
-    jt2 = beion ? p.nwtype[tr.itype] : p.typtyp[j0];
-  const bool rf = tr.valid && tr.rf_in;
+  const int jt2 = trial_type2(p, tr);
+  const bool beion = tr.valid && tr.j - 1 >= p.nsites;
+  const bool rf = tr.valid && tr.rf_in && (mask & 16u);
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
   double u = 0.0;
   int err = 0;
-  const bool ion_i = i >= p.nsites;
-  bool ok = tr.valid && i < ntot && i != j0 && !guard_bad(p.st, jt2 - 1, p.nttyp, 30);
-  if (ok && ion_i)
-    ok = !guard_bad(p.st, abs(p.typei[i]) - p.nold - 1, p.ntype - p.nold, 31);
-  if (ok) {
-    const double dx = p.x[i] - tr.x, dy = p.y[i] - tr.y, dz = p.z[i] - tr.z;
-    const double d2 = dx * dx + dy * dy + dz * dz;
-    if (mask & 1u) {
-      int is = -1;
-      if (beion && ion_i)  // interact.f90:173-210
-        is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
-      else if (beion && !ion_i)  // interact.f90:351-381
-        is = p.pidx[(p.typtyp[i] - 1) * p.nttyp + jt2 - 1];
-      else if (!beion && ion_i)  // interact.f90:383-413
-        is = p.pidx[(p.nwtype[abs(p.typei[i])] - 1) * p.nttyp + jt2 - 1];
-      if (is >= 0) u += law_interact64(p, p.pp[is], d2, err);
-    }
-    if (rf && ion_i && in_grid(p.g3, p.x[i], p.y[i], p.z[i])) {
-      double si, ri, d1[3], dd2[3];
-      const int it = abs(p.typei[i]);
-      rfpar_gather(p, p.x[i], p.y[i], p.z[i], rfpar_ifir(p, it), false, si, ri, d1, dd2);
-      if (si != 0.0) {
-        const double tau = p.celec * p.cg[tr.itype];
-        const double reffij = tr.reff * ri;
-        u += tau * p.cg[it] * reffij * tr.srfe * si / sqrt(reffij * reffij + d2);
-      }
-    }
-  }
+  if (jt2 > 0 && i < ntot && i != tr.j - 1) u = interact_one(p, tr, mask, i, jt2, beion, rf, err);
   if (err) atomicOr(&p.st->err, err);
   block_sum<1>(&u, red, tot);
   if (threadIdx.x == 0) p.ipart[blockIdx.x] = tot[0];
@@ -188,7 +227,7 @@ __global__ void __launch_bounds__(kIaThreads) k_interact_part(KP p, uint32_t mas
 __device__ double interact_total(const KP &p, const Trial &tr, int nblk, double *red,
                                  double *tot) {
   double v = 0.0;
-  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += p.ipart[b];
+  for (int b = threadIdx.x; b < nblk; b += blockDim.x) v += __ldcg(p.ipart + b);
   block_sum<1>(&v, red, tot);
   return tr.e_single + tot[0];
 }
@@ -215,45 +254,126 @@ __global__ void __launch_bounds__(kIaThreads)
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream) {
   const int nb = interact_slots(ntot_ub + 1);
+  if ((mask & 16u) && p.qrfpar && ntot_ub > p.nsites)
+    k_rf_prepass<<<(ntot_ub - p.nsites + 127) / 128, 128, 0, stream>>>(p);
   k_interact_prep<<<1, 32, 0, stream>>>(p, mask, qalert);
   k_interact_part<<<nb, kIaThreads, 0, stream>>>(p, mask);
   k_interact_final<<<1, kIaThreads, 0, stream>>>(p, nb, dener_dev);
 }
 
 // ---------------------------------------------------------------------------
-// GCMC proposal (grand.f90:42-86, insert.f90, find.f90) and the trial's
-// single-particle terms.
+// GRAND (grand.f90:19-121, insert.f90, find.f90): every attempt of one call
+// in one cooperative launch.  Block 0 owns the GCMC state (live count,
+// buffer counters, buffer parameters) in shared memory for the whole launch
+// and writes it back at the end; the other blocks only sum ΔE.  Per attempt:
+//   block 0: proposal + the trial's single-particle terms; publish the
+//            trial (generation flag, release);
+//   every block: its share of the O(N) ΔE sum -> ipart[block]; arrive on a
+//            counter (release);
+//   block 0: waits for every arrival (acquire), total ΔE, Im-Roux
+//            acceptance, insertion/deletion, counters; then straight on to
+//            the next proposal.
+// One synchronisation per attempt.  Each thread owns the same particles in
+// every phase (round-robin over blocks), so the RFPAR prepass of a particle
+// is read only by the thread that wrote it until block 0 edits it.  Data
+// that another block wrote during the launch are read past L1 (__ldcg).
+// Every wait is bounded: it gives up after kWaitSpins polls, or as soon as
+// another block has given up, records kErrBarrier and the launch returns.
 // ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kPropThreads)
-    k_gcmc_propose(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, uint32_t attempt) {
-  __shared__ Trial s;
-  __shared__ int counts[kPropThreads];
+constexpr int kGrandThreads = 128;
+constexpr int kWaitSpins = 1 << 23;  // ~0.5-1 s of polling at most
+
+struct GrandState {
+  Trial s;                  // current trial
+  double2 trial_rf;         // RFPAR (srfe, reff) at an insertion trial
+  int ntot;
+  int nat[kMaxBuffers], ninsert[kMaxBuffers], nremove[kMaxBuffers], ntotat[kMaxBuffers];
+  double dener_sum;
+  // buffer parameters, 1-based as in KP
+  double avnum[kMaxBuffers + 1], mu[kMaxBuffers + 1], kbb[kMaxBuffers + 1];
+  double lzmin[kMaxBuffers + 1], lzmax[kMaxBuffers + 1];
+  double rmin[kMaxBuffers + 1], rmax[kMaxBuffers + 1];
+  int ibfftyp[kMaxBuffers + 1], qbias[kMaxBuffers + 1];
+  int scan[kGrandThreads / 32];
+  int found;
+  double red[kGrandThreads / 32], tot[1];
+};
+
+// The attempt's uniform draws, gcmc_uniform(seed, cycle, attempt, n) for
+// n = 0, 1, ..., with one Philox block per four draws.
+struct Draws {
+  uint64_t seed, cycle;
+  uint32_t attempt, n = 0, blk = 0xffffffffu;
+  uint32_t w[4];
+  __device__ double next() {
+    if ((n >> 2) != blk) {
+      blk = n >> 2;
+      philox4x32_10(attempt, blk, (uint32_t)cycle,
+                    ((uint32_t)(cycle >> 32) & 0x00FFFFFFu) | (2u << 24), (uint32_t)seed,
+                    (uint32_t)(seed >> 32), w);
+    }
+    return u01(w[n++ & 3]);
+  }
+};
+
+// Bounded polls (thread 0 of a block), acquire ordering.
+__device__ bool wait_at_least(unsigned *ctr, unsigned target, DevState *st) {
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
+  volatile int *err = &st->err;
+  for (int spin = 0; a.load(cuda::memory_order_acquire) < target; ++spin) {
+    if (spin > kWaitSpins || ((spin & 1023) == 1023 && (*err & kErrBarrier))) {
+      atomicOr(&st->err, kErrBarrier);
+      return false;
+    }
+    __nanosleep(32);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void release_add(unsigned *ctr, unsigned v) {
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
+  a.fetch_add(v, cuda::memory_order_release);
+}
+
+// Block-wide: thread 0 waits, everyone learns the outcome.
+__device__ bool block_wait(unsigned *ctr, unsigned target, DevState *st, int *flag) {
+  if (threadIdx.x == 0) *flag = wait_at_least(ctr, target, st) ? 1 : 0;
+  __syncthreads();
+  const bool ok = *flag != 0;
+  __syncthreads();
+  return ok;
+}
+
+// Proposal of one attempt (grand.f90:42-86): insertion point by rejection
+// sampling inside the buffer (insert.f90) or the rank-th ion of the buffer
+// in slot order (find.f90), then the trial's single-particle terms (warp 0)
+// and, for an insertion, its RFPAR (srfe, reff) (warp 1).
+__device__ void propose(const KP &p, uint32_t mask, uint64_t seed, uint64_t cycle,
+                        uint32_t attempt, GrandState &g) {
+  __syncthreads();
   if (threadIdx.x == 0) {
     Trial t{};
-    uint32_t draw = 0;
-    const int nbuf = p.nbuffer;
-    const int ntot = p.st->ntot;
-    if (gcmc_uniform(seed, cycle, attempt, draw++) < 0.5) {
-      const int ib = (int)((double)nbuf * gcmc_uniform(seed, cycle, attempt, draw++)) + 1;
+    Draws d{seed, cycle, attempt};
+    const int nbuf = p.nbuffer, ntot = g.ntot;
+    if (d.next() < 0.5) {
+      const int ib = (int)((double)nbuf * d.next()) + 1;
       t.insert = 1;
       t.ib = ib;
-      if (ib <= nbuf && p.avnum[ib] > 0.0) {
-        t.itype = p.ibfftyp[ib];
+      if (ib <= nbuf && g.avnum[ib] > 0.0) {
+        t.itype = g.ibfftyp[ib];
         t.j = ntot + 1;
         t.valid = 1;
         bool ok = false;
         for (int it = 0; it < (1 << 20) && !ok; ++it) {
-          const double u1 = gcmc_uniform(seed, cycle, attempt, draw++);
-          const double u2 = gcmc_uniform(seed, cycle, attempt, draw++);
-          const double u3 = gcmc_uniform(seed, cycle, attempt, draw++);
+          const double u1 = d.next(), u2 = d.next(), u3 = d.next();
           t.x = p.lx * (u1 - 0.5) + p.cx;
           t.y = p.ly * (u2 - 0.5) + p.cy;
-          t.z = p.lzmin[ib] + (p.lzmax[ib] - p.lzmin[ib]) * u3;
+          t.z = g.lzmin[ib] + (g.lzmax[ib] - g.lzmin[ib]) * u3;
           ok = true;
           if (p.shape == 1) {
             const double r2 = (t.x - p.cx) * (t.x - p.cx) + (t.y - p.cy) * (t.y - p.cy) +
                               (t.z - p.cz) * (t.z - p.cz);
-            ok = r2 > p.rmin[ib] * p.rmin[ib] && r2 < p.rmax[ib] * p.rmax[ib];
+            ok = r2 > g.rmin[ib] * g.rmin[ib] && r2 < g.rmax[ib] * g.rmax[ib];
           } else if (p.shape == 2) {
             const double ex = (t.x - p.cx) * p.iecx, ey = (t.y - p.cy) * p.iecy;
             ok = ex * ex + ey * ey < 1.0;
@@ -265,157 +385,261 @@ __global__ void __launch_bounds__(kPropThreads)
         }
       }
     } else {
-      const int ib = (int)((double)nbuf * gcmc_uniform(seed, cycle, attempt, draw++)) + 1;
-      const int natb = ib <= nbuf ? p.st->nat[ib - 1] : 0;
-      const int ip = (int)((double)natb * gcmc_uniform(seed, cycle, attempt, draw++)) + 1;
+      const int ib = (int)((double)nbuf * d.next()) + 1;
+      const int natb = ib <= nbuf ? g.nat[ib - 1] : 0;
+      const int ip = (int)((double)natb * d.next()) + 1;
       t.insert = 0;
       t.ib = ib;
       if (ib <= nbuf && ip <= natb) {
-        t.itype = p.ibfftyp[ib];
+        t.itype = g.ibfftyp[ib];
         t.valid = 1;
         t.j = ip;  // rank within the buffer; resolved to a slot below
       }
     }
-    t.draw = (int)draw;
-    s = t;
+    t.draw = (int)d.n;
+    t.ntot = ntot;
+    g.s = t;
+    g.found = -1;
   }
   __syncthreads();
-  // every thread reads the proposal before anyone edits it
-  const int valid = s.valid, insert = s.insert, ib = s.ib, rank = s.j;
-  __shared__ int found;
-  if (threadIdx.x == 0) found = -1;
-  __syncthreads();
-  if (valid && !insert) {
-    // find.f90: the rank-th particle of buffer ib in slot order
-    const int ntot = p.st->ntot;
-    const int lo = p.nsites + p.nfix;
-    const int n = ntot - lo;
-    const int per = (n + kPropThreads - 1) / kPropThreads;
+  const Trial &s = g.s;
+  if (s.valid && !s.insert) {  // find.f90: the rank-th ion of buffer ib in slot order
+    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+    const int lo = p.nsites + p.nfix, ntot = g.ntot;
+    const int per = (ntot - lo + (int)blockDim.x - 1) / (int)blockDim.x;
     const int a = lo + threadIdx.x * per, b = min(ntot, a + per);
     int c = 0;
-    for (int k = a; k < b; ++k) c += (p.ibuffer[k] == ib);
-    counts[threadIdx.x] = c;
-    __syncthreads();
-    if (threadIdx.x == 0) {  // exclusive scan, fixed order
-      int acc = 0;
-      for (int k = 0; k < kPropThreads; ++k) {
-        const int v = counts[k];
-        counts[k] = acc;
-        acc += v;
-      }
+    for (int k = a; k < b; ++k) c += (p.ibuffer[k] == s.ib);
+    int incl = c;  // inclusive scan: warp shuffles, then the warp totals
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
     }
+    if (lane == 31) g.scan[wid] = incl;
     __syncthreads();
-    const int before = counts[threadIdx.x];
+    int before = incl - c;
+    for (int w = 0; w < wid; ++w) before += g.scan[w];
+    const int rank = s.j;
     if (rank > before && rank <= before + c) {  // exactly one thread
       int r = before;
       for (int k = a; k < b; ++k)
-        if (p.ibuffer[k] == ib && ++r == rank) {
-          found = k;
+        if (p.ibuffer[k] == s.ib && ++r == rank) {
+          g.found = k;
           break;
         }
     }
     __syncthreads();
     if (threadIdx.x == 0) {
-      const int k = found;
+      const int k = g.found;
       if (k < 0 || guard_bad(p.st, k, ntot, 11)) {
-        s.valid = 0;
+        g.s.valid = 0;
         atomicOr(&p.st->err, kErrFind);
       } else {
-        s.j = k + 1;
-        s.x = p.x[k];
-        s.y = p.y[k];
-        s.z = p.z[k];
+        g.s.j = k + 1;
+        g.s.x = p.x[k];
+        g.s.y = p.y[k];
+        g.s.z = p.z[k];
       }
     }
     __syncthreads();
   }
   // the trial's single-particle terms (deletion trials raise warnings as
   // INTERACT with Qalert does, insertion trials do not: grand.f90:48,86)
-  if (threadIdx.x < 32 && s.valid) {
-    Trial t = s;
+  if (threadIdx.x < 32 && g.s.valid) {
+    Trial t = g.s;
     trial_single_warp(p, t, mask, t.insert ? 0 : 1);
-    if (threadIdx.x == 0) s = t;
+    if (threadIdx.x == 0) g.s = t;
+  } else if (threadIdx.x == 32 && g.s.valid && g.s.insert && (mask & 16u) && p.qrfpar) {
+    g.trial_rf = rf_single(p, g.s.x, g.s.y, g.s.z, g.s.itype);
   }
   __syncthreads();
-  if (threadIdx.x == 0) *p.trial = s;
 }
 
-// ---------------------------------------------------------------------------
-// ΔE + acceptance + bookkeeping (grand.f90:48-116).
-// ---------------------------------------------------------------------------
-__global__ void __launch_bounds__(kIaThreads)
-    k_gcmc_accept(KP p, int nblk, uint64_t seed, uint64_t cycle, uint32_t attempt) {
-  __shared__ double red[kIaThreads / 32];
-  __shared__ double tot[1];
-  const Trial tr = *p.trial;
+// Total ΔE, Im-Roux acceptance and the insertion/deletion (grand.f90:48-116)
+// of the current trial; block 0, state in g.
+__device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint64_t cycle,
+                       uint32_t attempt, GrandState &g) {
+  const Trial &tr = g.s;
+  const bool rf_on = (mask & 16u) && p.qrfpar;
   double dener = 0.0;
-  if (tr.valid) dener = interact_total(p, tr, nblk, red, tot);
-  if (threadIdx.x != 0) return;
-  DevState *st = p.st;
-  if (tr.valid && !guard_bad(st, tr.ib - 1, p.nbuffer, 21)) {
+  if (tr.valid) dener = interact_total(p, tr, nblk, g.red, g.tot);
+  if (threadIdx.x == 0 && tr.valid && !guard_bad(p.st, tr.ib - 1, p.nbuffer, 21)) {
     const int ib = tr.ib, b = ib - 1;
-    const int nat = st->nat[b];
-    const double boltz = exp(-(dener - p.mu[ib]) * p.ikbt);
+    const int nat = g.nat[b];
+    const double boltz = exp(-(dener - g.mu[ib]) * p.ikbt);
     double rate;
     if (tr.insert) {
-      if (p.qbufferbias[ib]) {
-        rate = p.avnum[ib] + p.kbb[ib] * (p.avnum[ib] - (double)(st->ntotat[b] / (long long)cycle));
+      if (g.qbias[ib]) {
+        rate = g.avnum[ib] + g.kbb[ib] * (g.avnum[ib] - (double)(g.ntotat[b] / (long long)cycle));
         rate = rate * boltz / (double)(nat + 1);
       } else {
-        rate = (p.avnum[ib] / (nat + 1)) * boltz;
+        rate = (g.avnum[ib] / (nat + 1)) * boltz;
       }
       rate = rate / (1.0 + rate);
     } else {
-      if (p.qbufferbias[ib]) {
-        rate = p.avnum[ib] + p.kbb[ib] * (p.avnum[ib] - (double)(st->ntotat[b] / (long long)cycle));
+      if (g.qbias[ib]) {
+        rate = g.avnum[ib] + g.kbb[ib] * (g.avnum[ib] - (double)(g.ntotat[b] / (long long)cycle));
         rate = rate * boltz / (double)nat;
       } else {
-        rate = (p.avnum[ib] / nat) * boltz;
+        rate = (g.avnum[ib] / nat) * boltz;
       }
       rate = 1.0 / (1.0 + rate);
     }
     if (gcmc_uniform(seed, cycle, attempt, (uint32_t)tr.draw) <= rate) {
-      const int ntot = st->ntot;
+      const int ntot = g.ntot;
       if (tr.insert) {
         if (ntot + 1 > p.cap) {
-          st->err |= kErrCapacity;
-        } else if (!guard_bad(st, ntot, p.cap, 22)) {
-          st->dener_sum += dener;
-          st->nat[b] = nat + 1;
+          atomicOr(&p.st->err, kErrCapacity);
+        } else if (!guard_bad(p.st, ntot, p.cap, 22)) {
+          g.dener_sum += dener;
+          g.nat[b] = nat + 1;
           p.x[ntot] = tr.x;
           p.y[ntot] = tr.y;
           p.z[ntot] = tr.z;
           p.typei[ntot] = tr.z < p.cz ? -tr.itype : tr.itype;
           p.ibuffer[ntot] = ib;
-          st->ntot = ntot + 1;
-          st->ninsert[b] += 1;
+          if (rf_on) p.gc_rf[ntot] = g.trial_rf;
+          g.ntot = ntot + 1;
+          g.ninsert[b] += 1;
         }
-      } else if (!guard_bad(st, tr.j - 1, ntot, 23) &&
-                 !guard_bad(st, ntot - 1, p.cap, 24)) {
+      } else if (!guard_bad(p.st, tr.j - 1, ntot, 23) &&
+                 !guard_bad(p.st, ntot - 1, p.cap, 24)) {
         const int iat = tr.j - 1, last = ntot - 1;
-        st->dener_sum -= dener;
-        st->nremove[b] += 1;
+        g.dener_sum -= dener;
+        g.nremove[b] += 1;
         p.x[iat] = p.x[last];
         p.y[iat] = p.y[last];
         p.z[iat] = p.z[last];
         p.typei[iat] = p.typei[last];
         p.ibuffer[iat] = p.ibuffer[last];
-        st->nat[b] = nat - 1;
-        st->ntot = ntot - 1;
+        if (rf_on) p.gc_rf[iat] = __ldcg(p.gc_rf + last);
+        g.nat[b] = nat - 1;
+        g.ntot = ntot - 1;
       }
     }
   }
-  for (int b = 0; b < p.nbuffer; ++b)  // prob(ib, nat(ib)) += 1
-    if (!guard_bad(st, st->nat[b], p.cap + 1, 25))
-      p.prob[(size_t)b * (p.cap + 1) + st->nat[b]] += 1;
+  __syncthreads();
+  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x)  // prob(ib, nat(ib)) += 1
+    if (!guard_bad(p.st, g.nat[b], p.cap + 1, 25))
+      atomicAdd(&p.prob[(size_t)b * (p.cap + 1) + g.nat[b]], 1);
 }
 
-void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask, uint64_t seed,
-                         uint64_t cycle, uint32_t attempt, cudaStream_t stream) {
-  k_gcmc_propose<<<1, kPropThreads, 0, stream>>>(p, mask, seed, cycle, attempt);
-  const int nb = interact_slots(ntot_ub + 1);
-  k_interact_part<<<nb, kIaThreads, 0, stream>>>(p, mask);
-  k_gcmc_accept<<<1, kIaThreads, 0, stream>>>(p, nb, seed, cycle, attempt);
+__global__ void __launch_bounds__(kGrandThreads)
+    k_grand(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, int ngcmc) {
+  __shared__ GrandState g;
+  __shared__ int flag;
+  DevState *st = p.st;
+  const bool b0 = blockIdx.x == 0;
+  const int nthr = gridDim.x * blockDim.x;
+  const int gtid = threadIdx.x * gridDim.x + blockIdx.x;  // round-robin over blocks
+  if (b0) {  // GCMC state into shared memory
+    const int nb = p.nbuffer;
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
+      g.nat[b] = st->nat[b];
+      g.ninsert[b] = st->ninsert[b];
+      g.nremove[b] = st->nremove[b];
+      g.ntotat[b] = st->ntotat[b];
+    }
+    for (int ib = threadIdx.x; ib <= nb; ib += blockDim.x) {
+      g.avnum[ib] = p.avnum[ib];
+      g.mu[ib] = p.mu[ib];
+      g.kbb[ib] = p.kbb[ib];
+      g.lzmin[ib] = p.lzmin[ib];
+      g.lzmax[ib] = p.lzmax[ib];
+      g.rmin[ib] = p.rmin[ib];
+      g.rmax[ib] = p.rmax[ib];
+      g.ibfftyp[ib] = p.ibfftyp[ib];
+      g.qbias[ib] = p.qbufferbias[ib];
+    }
+    if (threadIdx.x == 0) {
+      g.ntot = st->ntot;
+      g.dener_sum = st->dener_sum;
+    }
+  }
+  const int ntot0 = st->ntot;
+  if ((mask & 16u) && p.qrfpar)  // RFPAR prepass, each thread its own particles
+    for (int i = gtid; i < ntot0; i += nthr)
+      if (i >= p.nsites) p.gc_rf[i] = rf_single(p, p.x[i], p.y[i], p.z[i], abs(p.typei[i]));
+  bool ok = true;
+  if (b0) {
+    propose(p, mask, seed, cycle, 0u, g);
+    if (threadIdx.x == 0) {
+      *p.trial = g.s;
+      release_add(&st->bar_gen, 1u);
+    }
+  }
+  for (int a = 0; a < ngcmc && ok; ++a) {
+    if (!b0 && !(ok = block_wait(&st->bar_gen, (unsigned)(a + 1), st, &flag))) break;
+    const Trial tr = b0 ? g.s : load_trial_cg(p.trial);
+    const int jt2 = trial_type2(p, tr);
+    const bool beion = tr.valid && tr.j - 1 >= p.nsites;
+    const bool rf = tr.valid && tr.rf_in && (mask & 16u);
+    double u = 0.0;
+    int err = 0;
+    if (jt2 > 0)
+      for (int i = gtid; i < tr.ntot; i += nthr)
+        if (i != tr.j - 1) u += interact_one(p, tr, mask, i, jt2, beion, rf, err);
+    if (err) atomicOr(&st->err, err);
+    double *red = g.red, *tot = g.tot;
+    block_sum<1>(&u, red, tot);
+    if (threadIdx.x == 0) {
+      p.ipart[blockIdx.x] = tot[0];
+      release_add(&st->bar_count, 1u);
+    }
+    if (b0) {
+      if (!(ok = block_wait(&st->bar_count, (unsigned)(gridDim.x * (a + 1)), st, &flag))) break;
+      accept(p, mask, gridDim.x, seed, cycle, (uint32_t)a, g);
+      if (a + 1 < ngcmc) {
+        propose(p, mask, seed, cycle, (uint32_t)(a + 1), g);
+        if (threadIdx.x == 0) {
+          *p.trial = g.s;
+          release_add(&st->bar_gen, 1u);
+        }
+      }
+    }
+  }
+  if (b0) {  // GCMC state back to the device record (also after a failed wait)
+    __syncthreads();
+    for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) {
+      st->nat[b] = g.nat[b];
+      st->ninsert[b] = g.ninsert[b];
+      st->nremove[b] = g.nremove[b];
+    }
+    if (threadIdx.x == 0) {
+      st->ntot = g.ntot;
+      st->dener_sum = g.dener_sum;
+    }
+  }
+}
+
+// Blocks of the GRAND launch: about one per 64 particles, all co-resident,
+// at most the ipart slots the context holds (ipart_slots).
+cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
+                         uint64_t seed, uint64_t cycle, int ngcmc, cudaStream_t stream) {
+  static int max_res[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  if (max_res[dev] == 0) {
+    int per_sm = 0, nsm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, k_grand, kGrandThreads,
+                                                           0)) != cudaSuccess)
+      return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return e;
+    max_res[dev] = std::max(1, per_sm * nsm);
+  }
+  int grid = (ntot_ub + ngcmc + 63) / 64;
+  grid = std::max(1, std::min(std::min(grid, max_res[dev]), ipart_slots));
+  // both launch counters start at zero
+  if ((e = cudaMemsetAsync(&p.st->bar_count, 0, 2 * sizeof(unsigned), stream)) != cudaSuccess)
+    return e;
+  KP pc = p;
+  void *args[] = {(void *)&pc, (void *)&mask, (void *)&seed, (void *)&cycle, (void *)&ngcmc};
+  return cudaLaunchCooperativeKernel((const void *)k_grand, dim3(grid), dim3(kGrandThreads),
+                                     args, 0, stream);
 }
 
 }  // namespace bgpu

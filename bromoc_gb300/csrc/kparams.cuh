@@ -120,6 +120,8 @@ struct KP {
   const uint8_t *qbufferbias;
   int *prob;                    // [nbuffer*(cap+1)]
   Trial *trial;
+  double2 *gc_rf;               // [cap] RFPAR (srfe, reff) of each ion for
+                                // INTERACT's cross term, (0,0) off the map
   // ---- scratch ----
   double *ffield;               // [3*cap] single-particle field forces
   double *fii;                  // [nchunk_ii*3*cap] ion-ion partial forces
@@ -137,6 +139,11 @@ struct KP {
   float4 *rfd;                  // [2*cap] srfe and reff gradients (xyz, 0)
   float *ffield_f, *fis_f;      // [3*cap] single-particle / ion-site forces
   float *fii_f, *frf_f;         // [nchunk*3*cap] partial forces
+  // Newton's-third-law pair kernel: per tile pair q and side (0 = row tile,
+  // 1 = column tile), per lane: (fx, fy, fz, A) and B of the RFPAR chain
+  float4 *tpf;                  // [npairs][2][32]
+  float *tpb;                   // [npairs][2][32]
+  int ntile;                    // ion tiles of 32 (0: chunked pair kernel)
   const float2 *fact_f;         // [ntype+1] (fact1a, fact2a)
   const float2 *zcont_ff;       // [cntpts] crossing planes (hi, lo)
   const float *esvdw_f;         // [nttyp+1] repulsion scale per combined type

@@ -13,10 +13,19 @@ struct EnergyPlan {
   int ntot_ub;        // host upper bound of the device-resident ntot
   int nchunk_ii;      // source chunks of the ion-ion kernel
   int nchunk_rf;      // source chunks of the RFPAR cross kernel
+  int ntile;          // FP32: ion tiles of the Newton-3 pair kernel (0: chunked)
   bool fp32;
   bool reduce_energy; // launch the final energy reduction
   KTimer *t_pairs = nullptr, *t_rf = nullptr, *t_fields = nullptr;
 };
+
+// Tile pairs (I <= J) of the Newton-3 pair kernel, row-major: row I holds
+// J = I..T-1 and starts at offset I T - I (I - 1) / 2.
+constexpr int kN3MaxTiles = 256;  // up to 8192 ions; beyond, the chunked kernel
+__host__ __device__ inline int n3_pairs(int T) { return T * (T + 1) / 2; }
+__host__ __device__ inline int n3_index(int T, int I, int J) {
+  return I * T - I * (I - 1) / 2 + (J - I);
+}
 
 // Targets of the FP32 pair kernel: ion-ion terms act on mobile ions, the
 // RFPAR cross term on every ion in the map, so with RFPAR on the targets
@@ -41,6 +50,8 @@ struct AssembleFlags {
   int fp32_noise;     // single-precision Box-Muller (FP32 mode)
   int fp32_partials;  // FP32 mode: float partials, float-float positions
   int use_total;      // the force is fx,fy,fz as assembled earlier (dynamics())
+  int ntile;          // FP32: partials are per tile pair (Newton-3 kernel)
+  int rf_ab;          // FP32 Newton-3: add A sd1 + B sd2 of the RFPAR chain
 };
 
 // fields.cu: single-particle terms, one warp per particle
@@ -54,6 +65,7 @@ void launch_pack(const KP &p, int ntot_ub, bool to_records, cudaStream_t stream)
 int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
                   int qforces, cudaStream_t stream);
 int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask);
+int n3_blocks(int ntile);  // blocks (energy slots) of the Newton-3 pair kernel
 
 // dyn.cu: force assembly, optionally fused with the BD update
 void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,
@@ -63,9 +75,9 @@ void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,
 // gcmc.cu
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream);
-void launch_gcmc_attempt(const KP &p, int ntot_ub, uint32_t mask,
-                         uint64_t seed, uint64_t cycle, uint32_t attempt,
-                         cudaStream_t stream);
+// GRAND: ngcmc attempts in one cooperative launch (gcmc.cu)
+cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
+                         uint64_t seed, uint64_t cycle, int ngcmc, cudaStream_t stream);
 int interact_slots(int ntot_ub);
 
 }  // namespace bgpu

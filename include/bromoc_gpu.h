@@ -73,8 +73,10 @@ enum {
 
 enum { BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2 };
 
-/* pair arithmetic: FP64 mirrors the reference's -fdefault-real-8 build;
- * FP32 evaluates pair laws in single precision with double accumulation. */
+/* FP64 mirrors the reference's -fdefault-real-8 build.  FP32 runs ENERGY and
+ * the BD update in single precision: positions as float-float pairs, pair
+ * laws and map gathers in FP32, compensated force sums, energy totals
+ * accumulated in FP64 across blocks.  GCMC (INTERACT, GRAND) stays FP64. */
 enum { BROMOC_FP64 = 0, BROMOC_FP32 = 1 };
 
 /* BD update variants: dynamics0 (uniform D), dynamics1 (z-switch D,

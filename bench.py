@@ -6,9 +6,13 @@ Workload (the nanopore system with grid maps): 120x120x180 maps at 1 A
 repulsion slab with a 10 A pore, repwalls layers), ~2000 K+/Cl- ions with
 Coulomb/cdie 80 + LJ + SRPMF pairs, four GCMC buffers (1 M) at both ends.
 One bench step = one simul1 cycle: GRAND with 4 attempts, then 10 BD steps
-(ENERGY with forces + dynamics0).  Pair arithmetic FP32 with FP64
-accumulation; fields, BD update and GCMC ΔE in FP64.  Synthetic inputs (the
-reference ships no maps or decks).
+(ENERGY with forces + dynamics0).  ENERGY and the BD update in FP32
+(float-float positions, compensated force sums, FP64 energy totals); GCMC ΔE
+in FP64.  Synthetic inputs (the reference ships no maps or decks).
+
+The line also carries "batched": 256 bulk KCl replicas of 200-8000 ions
+(1 M, cube boxes, the same maps) advanced by the replica-batch engine, timed
+against the plain path run replica by replica through one context.
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -62,7 +66,8 @@ def config_dict():
                         "rfpar), K+/Cl- Coulomb+LJ+SRPMF, 4 GCMC buffers",
             "step": f"one cycle = GRAND({NGCMC} attempts) + {NBD} BD steps",
             "nions": NIONS, "grid": [120, 120, 180], "ngcmc": NGCMC, "nbd": NBD,
-            "pairs": "FP32 arithmetic, FP64 accumulation; no cutoff (all pairs)",
+            "pairs": "FP32 arithmetic, compensated FP32 force sums, FP64 energy "
+                     "totals; no cutoff (all pairs)",
             "l2": "flushed between timed steps (256 MB write outside the events)"}
 
 
@@ -126,6 +131,78 @@ class ClockSampler:
 
 
 # ---------------------------------------------------------------------------
+BATCH_NREP = 256
+
+
+def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
+    """Batched replicas (256 bulk KCl systems, N uniform in [200, 8000], 1 M,
+    cube boxes, the nanopore maps) against the plain path launched replica
+    by replica through one context; CUDA events on the shared stream, L2
+    flushed before every timed launch outside the events."""
+    import torch
+    from bromoc_gb300 import _lib
+    from bromoc_gb300.batch import Batch
+    spec = synth.pore(seed=3, nions=NIONS, maps=synth.pore_maps(seed=102),
+                      precision=abi.FP32, buffers=False)
+    counts, edges, parts = synth.batch_replicas(nrep=BATCH_NREP)
+    systems = []
+    for L in edges:
+        sy = spec.system_struct()
+        sy.lx = sy.ly = sy.lz = float(L)
+        sy.cx = sy.cy = sy.cz = 0.0
+        systems.append(sy)
+    proto = _lib.create(NIONS + 64, abi.FP32, sh)
+    spec.push(proto)
+    b = Batch(proto, counts)
+    b.set_systems(systems)
+    for r, (x, y, z, t) in enumerate(parts):
+        b.set_particles(r, x, y, z, t)
+    seeds = np.arange(BATCH_NREP, dtype=np.uint64) + SEED
+    stream = torch.cuda.current_stream()
+    b.bd_steps(warm, seeds, 0)
+    torch.cuda.synchronize()
+    l0 = b.launch_count()
+    tb = 0.0
+    for k in range(steps):
+        flush.zero_()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        b.bd_steps(1, seeds, warm + k)
+        e.record(stream)
+        torch.cuda.synchronize()
+        tb += a.elapsed_time(e)
+    launches = b.launch_count() - l0
+    nions = int(counts.sum())
+    value = nions * steps / (tb * 1e-3)
+    b.close()
+    # plain path, replica by replica
+    g = _lib.create(int(counts.max()) + 64, abi.FP32, sh)
+    spec.push(g)
+    tp = 0.0
+    for r, (x, y, z, t) in enumerate(parts):
+        g.call("set_system", C.byref(systems[r]))
+        g.set_particles(x, y, z, t)
+        g.bd_steps(1, int(seeds[r]), 0)
+        torch.cuda.synchronize()
+        flush.zero_()
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        a.record(stream)
+        g.bd_steps(plain_steps, int(seeds[r]), 1)
+        e.record(stream)
+        torch.cuda.synchronize()
+        tp += a.elapsed_time(e)
+    plain = nions * plain_steps / (tp * 1e-3)
+    del g, proto
+    return {"workload": f"{BATCH_NREP} bulk KCl replicas, N uniform in [200, 8000] "
+                        f"({nions} ions), 1 M, cube boxes, shared 120x120x180 maps, "
+                        "ENERGY (Coulomb+LJ+SRPMF, fields, RFPAR) + dynamics0, FP32",
+            "value": value, "unit": "particle-steps/s", "ms_per_step": tb / steps,
+            "steps": steps, "gpu_launches": launches,
+            "plain_per_replica": {"value": plain, "ms_per_step": tp / plain_steps,
+                                  "steps": plain_steps},
+            "speedup_vs_plain": value / plain}
+
+
 def measured_peaks():
     p = ROOT / "MEASURED_PEAKS.json"
     if p.exists():
@@ -218,7 +295,11 @@ def run_gpu(args, rank, world, local_rank):
     if world > 1:
         import torch.distributed as dist
         dist.init_process_group("nccl")
-    stream = torch.cuda.current_stream()
+    # a stream of our own: torch's default (legacy) stream does not order
+    # with the library's non-blocking streams, so the contexts adopt this one
+    # and every event and the L2 flush are recorded on it
+    stream = torch.cuda.Stream()
+    torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
 
     # accuracy of the FP32 pair path against the FP64 path (validated
@@ -360,6 +441,7 @@ def run_gpu(args, rank, world, local_rank):
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None,
                 "peak_source": src, "launch_ms": ms / nl,
                 "share": kt[dom][0] / tot_k}
+    batched = batch_measure(sh, flush)
     cpu = oracle_baseline(float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15")))
     clocks = clk.summary()
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s",
@@ -378,6 +460,7 @@ def run_gpu(args, rank, world, local_rank):
                     "steps": e2e_steps,
                     "path": "bromoc_gpu_simul_cycles_host, pinned host arrays"},
             "gpu_launches": launches,
+            "batched": batched,
             "wall_s": wall, "clocks": clocks}
     print(json.dumps(line), flush=True)
     if dist:

@@ -43,6 +43,25 @@ def load() -> C.CDLL:
         lib.bromoc_gpu_kernel_time.restype = C.c_int
         lib.bromoc_gpu_fp32_peak.argtypes = [C.c_void_p, d]
         lib.bromoc_gpu_fp32_peak.restype = C.c_int
+        vp = C.c_void_p
+        for name, args in (
+                ("create", [vp, C.c_int32, i32, C.POINTER(vp)]),
+                ("destroy", [vp]),
+                ("set_systems", [vp, vp]),
+                ("set_particles", [vp, C.c_int32, C.c_int32, d, d, d, i32]),
+                ("get_particles", [vp, C.c_int32, i32, d, d, d]),
+                ("bd_steps", [vp, C.c_uint32, C.c_int32, C.POINTER(C.c_uint64),
+                              C.c_uint64, d]),
+                ("energy", [vp, C.c_uint32, d, d]),
+                ("offset", [vp, C.c_int32]),
+                ("slots", [vp])):
+            f = getattr(lib, "bromoc_batch_" + name)
+            f.argtypes = args
+            f.restype = C.c_int
+        lib.bromoc_batch_last_error.argtypes = [vp]
+        lib.bromoc_batch_last_error.restype = C.c_char_p
+        lib.bromoc_batch_launch_count.argtypes = [vp]
+        lib.bromoc_batch_launch_count.restype = C.c_int64
         _lib = lib
     return _lib
 

@@ -1,0 +1,87 @@
+"""Python face of the replica-batch C ABI (bromoc_batch_* in
+include/bromoc_gpu.h): many independent ion systems sharing one FP32
+prototype context's types, pair laws and grid maps."""
+from __future__ import annotations
+
+import ctypes as C
+
+import numpy as np
+
+from . import _lib, abi
+
+
+class Batch:
+    def __init__(self, proto: abi.Engine, capacities):
+        self.lib = _lib.load()
+        self.proto = proto  # keeps the prototype alive as long as the batch
+        caps = np.ascontiguousarray(capacities, dtype=np.int32)
+        self.nrep = len(caps)
+        h = C.c_void_p()
+        rc = self.lib.bromoc_batch_create(
+            proto.h, self.nrep, caps.ctypes.data_as(C.POINTER(C.c_int32)), C.byref(h))
+        if rc != abi.OK:
+            raise abi.BromocError(rc, self.lib.bromoc_gpu_last_error(proto.h).decode())
+        self.h = h
+
+    def _chk(self, rc, what):
+        if rc != abi.OK:
+            raise abi.BromocError(
+                rc, f"{what}: {self.lib.bromoc_batch_last_error(self.h).decode()}")
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.lib.bromoc_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_systems(self, systems):
+        """systems: one abi.System (the ctypes bromoc_system) per replica."""
+        arr = (abi.System * self.nrep)(*systems)
+        self._chk(self.lib.bromoc_batch_set_systems(self.h, C.cast(arr, C.c_void_p)),
+                  "set_systems")
+
+    def set_particles(self, r, x, y, z, typei):
+        x, y, z = (np.ascontiguousarray(a, np.float64) for a in (x, y, z))
+        t = np.ascontiguousarray(typei, np.int32)
+        dp = C.POINTER(C.c_double)
+        self._chk(self.lib.bromoc_batch_set_particles(
+            self.h, r, len(x), x.ctypes.data_as(dp), y.ctypes.data_as(dp),
+            z.ctypes.data_as(dp), t.ctypes.data_as(C.POINTER(C.c_int32))), "set_particles")
+
+    def get_particles(self, r, nmax):
+        x, y, z = (np.zeros(nmax) for _ in range(3))
+        n = C.c_int32(0)
+        dp = C.POINTER(C.c_double)
+        self._chk(self.lib.bromoc_batch_get_particles(
+            self.h, r, C.byref(n), x.ctypes.data_as(dp), y.ctypes.data_as(dp),
+            z.ctypes.data_as(dp)), "get_particles")
+        return x[:n.value], y[:n.value], z[:n.value]
+
+    def bd_steps(self, nsteps, seeds, step0=0, terms=abi.M_ALL, energies=False):
+        s = np.ascontiguousarray(seeds, np.uint64)
+        et = np.zeros((self.nrep, abi.NTERMS)) if energies else None
+        self._chk(self.lib.bromoc_batch_bd_steps(
+            self.h, terms, nsteps, s.ctypes.data_as(C.POINTER(C.c_uint64)), step0,
+            et.ctypes.data_as(C.POINTER(C.c_double)) if et is not None else None), "bd_steps")
+        return et
+
+    def energy(self, terms=abi.M_ALL, forces=True):
+        et = np.zeros((self.nrep, abi.NTERMS))
+        nsl = self.lib.bromoc_batch_slots(self.h)
+        f = np.zeros((nsl, 3)) if forces else None
+        dp = C.POINTER(C.c_double)
+        self._chk(self.lib.bromoc_batch_energy(
+            self.h, terms, f.ctypes.data_as(dp) if f is not None else None,
+            et.ctypes.data_as(dp)), "energy")
+        return et, f
+
+    def offset(self, r):
+        return self.lib.bromoc_batch_offset(self.h, r)
+
+    def launch_count(self):
+        return self.lib.bromoc_batch_launch_count(self.h)

@@ -190,6 +190,21 @@ void fill_axis(AxisF &A, const Grid3 &g, int axis, bool set, double ub, double l
   A.ncl = axis == 0 ? g.nclx : (axis == 1 ? g.ncly : g.nclz);
 }
 
+// fixcoor constants of one system in float-float (shell_simul.f90:914-919).
+void fill_box(const bromoc_system &q, BoxF &b) {
+  b = BoxF{};
+  b.shape = q.shape;
+  b.rsphe = (float)q.rsphe;
+  b.rsphe2 = (float)(q.rsphe * q.rsphe);
+  b.iecx = q.shape == BROMOC_ECYL ? (float)(2.0 / q.lx) : 0.0f;
+  b.iecy = q.shape == BROMOC_ECYL ? (float)(2.0 / q.ly) : 0.0f;
+  const double bd[6] = {q.cx - 0.5 * q.lx, q.cx + 0.5 * q.lx, q.cy - 0.5 * q.ly,
+                        q.cy + 0.5 * q.ly, q.cz - 0.5 * q.lz, q.cz + 0.5 * q.lz};
+  for (int k = 0; k < 6; ++k) split_ff(bd[k], b.bh[k], b.bl[k]);
+  const double c[3] = {q.cx, q.cy, q.cz};
+  for (int k = 0; k < 3; ++k) split_ff(c[k], b.ch[k], b.cl[k]);
+}
+
 // Single-precision constants of the FP32 kernels (KP::f) from the FP64 state.
 void fill_f32(bromoc_ctx *ctx) {
   KP &p = ctx->kp;
@@ -221,14 +236,7 @@ void fill_f32(bromoc_ctx *ctx) {
   f.bdmax = (float)p.bdmax;
   f.fact0n1 = (float)p.fact0n1;
   f.fact0n2 = (float)p.fact0n2;
-  f.rsphe = (float)p.rsphe;
-  f.rsphe2 = (float)p.rsphe2;
-  f.iecx = (float)p.iecx;
-  f.iecy = (float)p.iecy;
-  const double b[6] = {p.lx2m, p.lx2p, p.ly2m, p.ly2p, p.lz2m, p.lz2p};
-  for (int k = 0; k < 6; ++k) split_ff(b[k], f.bh[k], f.bl[k]);
-  const double c[3] = {p.cx, p.cy, p.cz};
-  for (int k = 0; k < 3; ++k) split_ff(c[k], f.ch[k], f.cl[k]);
+  fill_box(ctx->sys, f.box);
 }
 
 int ensure_scratch(bromoc_ctx *ctx) {
@@ -423,6 +431,17 @@ bool bromoc_ctx_pair_view(const bromoc_ctx *ctx, const KP **kp, cudaStream_t *st
   *stream = ctx->stream;
   *precision = ctx->precision;
   return true;
+}
+
+int bromoc_ctx_prepare_f32(bromoc_ctx *ctx, const KP **kp, cudaStream_t *stream) {
+  if (!ctx) return BROMOC_E_ARG;
+  if (ctx->precision != BROMOC_FP32)
+    return set_err(ctx, BROMOC_E_STATE, "batch: the prototype context must be FP32");
+  const int rc = check_ready(ctx);
+  if (rc) return rc;
+  *kp = &ctx->kp;
+  *stream = ctx->stream;
+  return BROMOC_OK;
 }
 
 int bromoc_ctx_fail(bromoc_ctx *ctx, int code, const char *msg) {

@@ -1,0 +1,599 @@
+// Replica batches on the device (scope-table configuration C4): many
+// independent systems of uneven size advance together, two launches per BD
+// step for the whole batch.
+//
+//   k_batch_fields (fields.cu): the FP32 field terms of every live slot.
+//   k_batch_rows:  one warp owns 32 ions of one replica and sweeps every
+//                  ion of that replica, 32 at a time through shared memory;
+//                  its forces (ion-ion laws + RFPAR cross term) complete in
+//                  registers, so the warp then assembles them and makes the
+//                  BD move (dynamics0) at once, writing the other position
+//                  buffer so that no warp reads a moved source.
+//
+// Each unordered pair is evaluated by both of its ions (no partial buffers,
+// no reduction pass).  Work items (replica, row tile) are sorted longest
+// first for load balance.  Replica r draws its noise from seed_r with the
+// same counters as a single context, so a batch replica follows the
+// trajectory of bromoc_gpu_bd_steps with that seed.
+#include <algorithm>
+#include <cstdarg>
+#include <cstdio>
+#include <cstring>
+#include <string>
+#include <vector>
+
+#include "../../include/bromoc_gpu.h"
+#include "batch.cuh"
+#include "ff.cuh"
+#include "launch.h"
+#include "physics.cuh"
+
+namespace bgpu {
+
+constexpr int kRowWarps = 4;
+
+// Energies of one row warp: ecoul, elj, esrpmf, eefpot (ion-ion, each pair
+// half from either side) and the RFPAR cross energy.
+constexpr int kRowTerms = 5;
+
+template <bool RF, bool BD>
+__global__ void __launch_bounds__(32 * kRowWarps)
+    k_batch_rows(const __grid_constant__ KP p, const RepDev *rep, const int2 *work,
+                 int nwork, float4 *pk1n, float4 *pk2n, float *wpart, uint64_t step,
+                 int qforces, double *fout) {
+  __shared__ float4 sh[kRowWarps][32], sl[kRowWarps][32], sq[kRowWarps][RF ? 32 : 1];
+  __shared__ float4 tab[kIonTabTypes * kIonTabTypes];
+  const int nt = p.nion_t;
+  for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
+  __syncthreads();
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int widx = blockIdx.x * kRowWarps + w;
+  if (widx >= nwork) return;  // no block-wide barrier follows
+  const int2 wk = work[widx];
+  const RepDev &R = rep[wk.x];
+  const int off = R.off, n = R.n, I = wk.y, T = (n + 31) >> 5;
+  const int il = I * 32 + lane;
+  const bool iv = il < n;
+  const int i = off + il;
+  float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th, tq = th;
+  if (iv) {
+    th = p.pk1[i];
+    tl = p.pk2[i];
+    if (RF) tq = p.pk3[i];
+  }
+  const int row = ((__float_as_int(th.w) & 0xffff) - p.ndna) * nt;
+  const int tb = __float_as_int(tq.z);
+  const float srt = tl.w, rft = tq.x, ct = p.f.celec * tq.y;
+  float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float e[kRowTerms] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int J = 0; J < T; ++J) {
+    const int jl = J * 32 + lane;
+    __syncwarp();
+    if (jl < n) {
+      sh[w][lane] = p.pk1[off + jl];
+      sl[w][lane] = p.pk2[off + jl];
+      if (RF) sq[w][lane] = p.pk3[off + jl];
+    }
+    __syncwarp();
+    const int cnt = min(32, n - J * 32);
+    float fx = 0.f, fy = 0.f, fz = 0.f, A = 0.f, B = 0.f;
+    if (iv) {
+      for (int k = 0; k < cnt; ++k) {
+        if (J == I && k == lane) continue;
+        const float4 h = sh[w][k], l = sl[w][k];
+        const float dx = (th.x - h.x) + (tl.x - l.x);
+        const float dy = (th.y - h.y) + (tl.y - l.y);
+        const float dz = (th.z - h.z) + (tl.z - l.z);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float4 q = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
+        const float ir = rsqrtf(r2), ir2 = ir * ir;
+        const float cofo = q.x * ir;
+        e[0] = fmaf(0.5f, cofo, e[0]);
+        float d6 = q.z * ir2;
+        d6 = d6 * d6 * d6;
+        const float d12 = d6 * d6;
+        e[1] = fmaf(0.5f * q.y, d12 - d6, e[1]);
+        float de = fmaf(cofo, ir2, (6.0f * q.y) * ir2 * fmaf(2.0f, d12, -d6));
+        const int qf = __float_as_int(q.w);
+        if ((qf & kSrp) && r2 <= p.rthf) de += srpmf32(p, qf >> 4, r2, ir, 0.5f, e);
+        if (RF) {
+          const float4 u = sq[w][k];
+          const int sb = __float_as_int(u.z);
+          const bool t_is_i = il > J * 32 + k;
+          if (t_is_i ? ((tb & 4) && (sb & 8)) : ((sb & 4) && (tb & 8))) {
+            const float rij = u.x * rft, srij = l.w * srt;
+            const float rfdn = rsqrtf(fmaf(rij, rij, r2));
+            const float aux0 = ct * u.y;
+            const float a1 = aux0 * rij * rfdn;
+            if (t_is_i) e[4] = fmaf(a1, srij, e[4]);
+            const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
+            A = fmaf(-a1, l.w, A);
+            B = fmaf(-a2 * fmaf(rij, 0.5f, r2), u.x, B);
+            de = fmaf(a2, rij, de);
+          }
+        }
+        fx = fmaf(de, dx, fx);
+        fy = fmaf(de, dy, fy);
+        fz = fmaf(de, dz, fz);
+      }
+    }
+    acc2(s[0], c[0], fx);
+    acc2(s[1], c[1], fy);
+    acc2(s[2], c[2], fz);
+    acc2(s[3], c[3], A);
+    acc2(s[4], c[4], B);
+  }
+  // row energies -> this work item's slot (fixed shuffle tree)
+#pragma unroll
+  for (int k = 0; k < kRowTerms; ++k) {
+    float v = e[k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) wpart[(size_t)widx * kRowTerms + k] = v;
+  }
+  if (!iv) return;
+  const int cap = p.cap;
+#pragma unroll
+  for (int k = 0; k < 3; ++k) acc2(s[k], c[k], p.ffield_f[k * cap + i]);
+  if (RF) {  // A sd1 + B sd2 of the cross term (rfpar.f90:177-223)
+    const float Av = s[3] + c[3], Bv = s[4] + c[4];
+    const float4 d1 = p.rfd[2 * (size_t)i], d2 = p.rfd[2 * (size_t)i + 1];
+    acc2(s[0], c[0], fmaf(Av, d1.x, Bv * d2.x));
+    acc2(s[1], c[1], fmaf(Av, d1.y, Bv * d2.y));
+    acc2(s[2], c[2], fmaf(Av, d1.z, Bv * d2.z));
+  }
+  const float F[3] = {s[0] + c[0], s[1] + c[1], s[2] + c[2]};
+  if (!qforces) return;
+  if (!BD) {
+    if (fout)
+      for (int k = 0; k < 3; ++k) fout[3 * (size_t)i + k] = F[k];
+    return;
+  }
+  // dynamics0.mono.f90:31-46 on float-float positions
+  const float2 fa = p.fact_f[abs(p.typei[i])];
+  float g[3];
+  bd_noise3_f(R.seed, step, (uint32_t)il, g);
+  float hh[3] = {th.x, th.y, th.z}, ll[3] = {tl.x, tl.y, tl.z};
+#pragma unroll
+  for (int k = 0; k < 3; ++k) {
+    float d = F[k] * fa.x;
+    clamp_f(p.f.bdmax, d);
+    ff_add(hh[k], ll[k], fmaf(fa.y, g[k], d));
+  }
+  fixcoor_ff(R.box, hh, ll);
+  pk1n[i] = make_float4(hh[0], hh[1], hh[2], th.w);
+  pk2n[i] = make_float4(ll[0], ll[1], ll[2], 0.0f);
+}
+
+// Per-replica ENERGY terms (energy.mono.f90 slots) from the field terms of
+// its slots and the pair terms of its work items; one block per replica,
+// fixed-order sums in FP64.
+__global__ void __launch_bounds__(256)
+    k_batch_ereduce(const RepDev *rep, const float4 *pe, const float *wpart, int rfpar_on,
+                    double *eterms) {
+  __shared__ double red[(256 / 32) * 9];
+  __shared__ double tot[9];
+  const RepDev &R = rep[blockIdx.x];
+  double v[9] = {0, 0, 0, 0, 0, 0, 0, 0, 0};
+  for (int k = threadIdx.x; k < R.n; k += blockDim.x) {
+    const float4 q = pe[R.off + k];
+    v[0] += q.x;
+    v[1] += q.y;
+    v[2] += q.z;
+    v[3] += q.w;
+  }
+  for (int k = R.w0 + threadIdx.x; k < R.w1; k += blockDim.x)
+    for (int m = 0; m < kRowTerms; ++m) v[4 + m] += wpart[(size_t)k * kRowTerms + m];
+  block_sum<9>(v, red, tot);
+  if (threadIdx.x == 0) {
+    double o[kNTerms] = {};
+    o[9] = tot[0];              // ememb
+    o[10] = tot[1];             // egsbpa
+    o[12] = tot[2];             // evdwgd
+    o[13] = tot[3] + tot[8];    // erfpar: self + cross
+    o[1] = tot[4];              // eelec
+    o[2] = tot[5];              // evdw
+    o[3] = tot[6];              // esrpmf
+    o[4] = tot[7];              // eefpot
+    o[11] = rfpar_on ? o[13] : 0.0;
+    o[0] = o[9] + o[10] + o[12] + o[13] + o[1] + o[2] + o[3] + o[4];
+    for (int k = 0; k < kNTerms; ++k) eterms[(size_t)blockIdx.x * kNTerms + k] = o[k];
+  }
+}
+
+}  // namespace bgpu
+
+using namespace bgpu;
+
+struct bromoc_batch {
+  bromoc_ctx *proto = nullptr;
+  KP kp{};                     // prototype's parameter block, batch arrays swapped in
+  cudaStream_t stream = nullptr;
+  std::string err;
+  int nrep = 0, nslots = 0, nwork = 0, cur = 0;
+  std::vector<int> cap, off, n;
+  std::vector<RepDev> rep_h;   // host copy of the replica records
+  std::vector<int> nwtype_h;   // [ntype+1] ion type -> combined type
+  std::vector<double> cg_h;    // [ntype+1] charges
+  bool have_sys = false;
+  // device
+  RepDev *rep = nullptr;
+  int *rep_of = nullptr;
+  int2 *work = nullptr;
+  float4 *pk1[2] = {nullptr, nullptr}, *pk2[2] = {nullptr, nullptr};
+  float4 *pe = nullptr;
+  float *wpart = nullptr;
+  double *eterms = nullptr;
+  RepDev *rep_pinned = nullptr;
+  std::vector<void *> allocs;
+  long long launches = 0;
+};
+
+namespace {
+
+int bset(bromoc_batch *b, int code, const char *fmt, ...) {
+  char buf[512];
+  va_list ap;
+  va_start(ap, fmt);
+  vsnprintf(buf, sizeof buf, fmt, ap);
+  va_end(ap);
+  if (b) b->err = buf;
+  return code;
+}
+
+#define BCU(call)                                                              \
+  do {                                                                         \
+    cudaError_t e_ = (call);                                                   \
+    if (e_ != cudaSuccess)                                                     \
+      return bset(b, BROMOC_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_));  \
+  } while (0)
+
+template <class T>
+int balloc(bromoc_batch *b, T **p, size_t count) {
+  *p = nullptr;
+  cudaError_t e = cudaMalloc((void **)p, std::max<size_t>(count, 1) * sizeof(T));
+  if (e != cudaSuccess)
+    return bset(b, BROMOC_E_NOMEM, "cudaMalloc(%zu bytes): %s", count * sizeof(T),
+                cudaGetErrorString(e));
+  b->allocs.push_back((void *)*p);
+  return BROMOC_OK;
+}
+
+void split(double v, float &h, float &l) {
+  h = (float)v;
+  l = (float)(v - (double)h);
+}
+
+// work items (replica, row tile), longest rows first; each replica's items
+// stay contiguous (w0, w1)
+int rebuild_work(bromoc_batch *b) {
+  std::vector<int> order(b->nrep);
+  for (int r = 0; r < b->nrep; ++r) order[r] = r;
+  std::stable_sort(order.begin(), order.end(),
+                   [&](int a, int c) { return b->n[a] > b->n[c]; });
+  std::vector<int2> items;
+  for (int r : order) {
+    const int T = (b->n[r] + 31) / 32;
+    b->rep_h[r].w0 = (int)items.size();
+    for (int I = 0; I < T; ++I) items.push_back(make_int2(r, I));
+    b->rep_h[r].w1 = (int)items.size();
+  }
+  if ((int)items.size() > b->nwork) {
+    if (b->work) cudaFree(b->work);
+    if (b->wpart) cudaFree(b->wpart);
+    b->work = nullptr;
+    b->wpart = nullptr;
+    BCU(cudaMalloc((void **)&b->work, items.size() * sizeof(int2)));
+    BCU(cudaMalloc((void **)&b->wpart, items.size() * kRowTerms * sizeof(float)));
+  }
+  b->nwork = (int)items.size();
+  if (!items.empty())
+    BCU(cudaMemcpy(b->work, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  BCU(cudaMemcpy(b->rep, b->rep_h.data(), b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice));
+  return BROMOC_OK;
+}
+
+// The pair + BD launch of one step.
+void launch_rows(bromoc_batch *b, const KP &p, bool rf, bool bd, float4 *pk1n, float4 *pk2n,
+                 uint64_t step, double *fout) {
+  const int nb = (b->nwork + kRowWarps - 1) / kRowWarps;
+  const dim3 g(nb), blk(32 * kRowWarps);
+  if (rf && bd)
+    k_batch_rows<true, true><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n, pk2n,
+                                                       b->wpart, step, 1, fout);
+  else if (rf)
+    k_batch_rows<true, false><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n,
+                                                        pk2n, b->wpart, step, 1, fout);
+  else if (bd)
+    k_batch_rows<false, true><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n,
+                                                        pk2n, b->wpart, step, 1, fout);
+  else
+    k_batch_rows<false, false><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n,
+                                                         pk2n, b->wpart, step, 1, fout);
+}
+
+}  // namespace
+
+extern "C" {
+
+int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity,
+                        bromoc_batch **out) {
+  if (!proto || !out || nrep < 1 || !capacity) return BROMOC_E_ARG;
+  *out = nullptr;
+  const KP *pk = nullptr;
+  cudaStream_t stream = nullptr;
+  int rc = bromoc_ctx_prepare_f32(proto, &pk, &stream);
+  if (rc) return rc;
+  if (!pk->ipq_ok)
+    return bromoc_ctx_fail(proto, BROMOC_E_STATE,
+                           "batch: needs analytic ion-ion laws (no EFPOT) and <= 16 ion types");
+  if (pk->nsites != 0)
+    return bromoc_ctx_fail(proto, BROMOC_E_STATE, "batch: replicas hold ions only (no sites)");
+  bromoc_batch *b = new bromoc_batch;
+  b->proto = proto;
+  b->kp = *pk;
+  b->stream = stream;
+  b->nrep = nrep;
+  b->cap.resize(nrep);
+  b->off.resize(nrep);
+  b->n.assign(nrep, 0);
+  b->rep_h.assign(nrep, RepDev{});
+  int slots = 0;
+  for (int r = 0; r < nrep; ++r) {
+    if (capacity[r] < 1) {
+      delete b;
+      return bromoc_ctx_fail(proto, BROMOC_E_ARG, "batch: every capacity must be >= 1");
+    }
+    b->off[r] = slots;
+    b->cap[r] = capacity[r];
+    b->rep_h[r].off = slots;
+    b->rep_h[r].cap = capacity[r];
+    slots += (capacity[r] + 31) / 32 * 32;  // replicas start on tile boundaries
+  }
+  b->nslots = slots;
+  KP &p = b->kp;
+  const size_t ns = slots;
+  rc = balloc(b, &b->rep, nrep);
+  if (!rc) rc = balloc(b, &b->rep_of, ns);
+  for (int k = 0; k < 2 && !rc; ++k) {
+    rc = balloc(b, &b->pk1[k], ns);
+    if (!rc) rc = balloc(b, &b->pk2[k], ns);
+  }
+  float4 *pk3 = nullptr, *rfd = nullptr;
+  float *ffield = nullptr;
+  int *typei = nullptr;
+  DevState *st = nullptr;
+  if (!rc) rc = balloc(b, &pk3, ns);
+  if (!rc) rc = balloc(b, &rfd, 2 * ns);
+  if (!rc) rc = balloc(b, &ffield, 3 * ns);
+  if (!rc) rc = balloc(b, &typei, ns);
+  if (!rc) rc = balloc(b, &b->pe, ns);
+  if (!rc) rc = balloc(b, &b->eterms, (size_t)nrep * kNTerms);
+  if (!rc) rc = balloc(b, &st, 1);
+  if (!rc && cudaMallocHost((void **)&b->rep_pinned, nrep * sizeof(RepDev)) != cudaSuccess)
+    rc = bset(b, BROMOC_E_NOMEM, "batch: pinned replica records");
+  if (rc) {
+    const std::string msg = b->err;
+    bromoc_batch_destroy(b);
+    return bromoc_ctx_fail(proto, rc, msg.c_str());
+  }
+  std::vector<int> rep_of(ns, 0);
+  for (int r = 0; r < nrep; ++r)
+    for (int k = b->off[r]; k < (r + 1 < nrep ? b->off[r + 1] : slots); ++k) rep_of[k] = r;
+  cudaMemcpy(b->rep_of, rep_of.data(), ns * sizeof(int), cudaMemcpyHostToDevice);
+  cudaMemset(pk3, 0, ns * sizeof(float4));
+  cudaMemset(b->pk1[0], 0, ns * sizeof(float4));
+  cudaMemset(b->pk2[0], 0, ns * sizeof(float4));
+  cudaMemset(st, 0, sizeof(DevState));
+  // host copies of the type tables
+  b->nwtype_h.resize(p.ntype + 1);
+  b->cg_h.resize(p.ntype + 1);
+  cudaMemcpy(b->nwtype_h.data(), p.nwtype, (p.ntype + 1) * sizeof(int), cudaMemcpyDeviceToHost);
+  cudaMemcpy(b->cg_h.data(), p.cg, (p.ntype + 1) * sizeof(double), cudaMemcpyDeviceToHost);
+  // batch arrays in the parameter block
+  p.cap = slots;
+  p.nsites = 0;
+  p.nfix = 0;
+  p.st = st;
+  p.pk3 = pk3;
+  p.rfd = rfd;
+  p.ffield_f = ffield;
+  p.typei = typei;
+  p.qproxdiff = 0;
+  int *warn = nullptr;
+  if (balloc(b, &warn, p.nttyp + 1) == BROMOC_OK) cudaMemset(warn, 0, (p.nttyp + 1) * sizeof(int));
+  p.warn = warn;
+  if (cudaGetLastError() != cudaSuccess) {
+    bromoc_batch_destroy(b);
+    return bromoc_ctx_fail(proto, BROMOC_E_CUDA, "batch: setup copies failed");
+  }
+  if ((rc = rebuild_work(b))) {
+    const std::string msg = b->err;
+    bromoc_batch_destroy(b);
+    return bromoc_ctx_fail(proto, rc, msg.c_str());
+  }
+  *out = b;
+  return BROMOC_OK;
+}
+
+int bromoc_batch_destroy(bromoc_batch *b) {
+  if (!b) return BROMOC_E_ARG;
+  if (b->stream) cudaStreamSynchronize(b->stream);
+  for (void *a : b->allocs) cudaFree(a);
+  if (b->work) cudaFree(b->work);
+  if (b->wpart) cudaFree(b->wpart);
+  if (b->rep_pinned) cudaFreeHost(b->rep_pinned);
+  delete b;
+  return BROMOC_OK;
+}
+
+const char *bromoc_batch_last_error(const bromoc_batch *b) {
+  return b ? b->err.c_str() : "null batch";
+}
+
+int64_t bromoc_batch_launch_count(const bromoc_batch *b) { return b ? b->launches : -1; }
+
+}  // extern "C"
+
+extern "C" {
+
+int bromoc_batch_set_systems(bromoc_batch *b, const bromoc_system *sys) {
+  if (!b || !sys) return bset(b, BROMOC_E_ARG, "set_systems: null");
+  // the drift and noise factors are shared (prototype tables): every
+  // replica must have the prototype's dt, kbt and bdmax
+  for (int r = 0; r < b->nrep; ++r) {
+    const bromoc_system &q = sys[r];
+    if ((float)q.bdmax != b->kp.f.bdmax || (float)(q.dt / q.kbt) != b->kp.f.kbtdt)
+      return bset(b, BROMOC_E_ARG, "set_systems: replica %d differs in dt, kbt or bdmax", r);
+    BoxF &bx = b->rep_h[r].box;
+    bx = BoxF{};
+    bx.shape = q.shape;
+    bx.rsphe = (float)q.rsphe;
+    bx.rsphe2 = (float)(q.rsphe * q.rsphe);
+    bx.iecx = q.shape == BROMOC_ECYL ? (float)(2.0 / q.lx) : 0.0f;
+    bx.iecy = q.shape == BROMOC_ECYL ? (float)(2.0 / q.ly) : 0.0f;
+    const double bd[6] = {q.cx - 0.5 * q.lx, q.cx + 0.5 * q.lx, q.cy - 0.5 * q.ly,
+                          q.cy + 0.5 * q.ly, q.cz - 0.5 * q.lz, q.cz + 0.5 * q.lz};
+    for (int k = 0; k < 6; ++k) split(bd[k], bx.bh[k], bx.bl[k]);
+    const double c[3] = {q.cx, q.cy, q.cz};
+    for (int k = 0; k < 3; ++k) split(c[k], bx.ch[k], bx.cl[k]);
+  }
+  BCU(cudaStreamSynchronize(b->stream));
+  BCU(cudaMemcpy(b->rep, b->rep_h.data(), b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice));
+  b->have_sys = true;
+  return BROMOC_OK;
+}
+
+int bromoc_batch_set_particles(bromoc_batch *b, int32_t r, int32_t n, const double *x,
+                               const double *y, const double *z, const int32_t *typei) {
+  if (!b || !x || !y || !z || !typei) return bset(b, BROMOC_E_ARG, "set_particles: null");
+  if (r < 0 || r >= b->nrep) return bset(b, BROMOC_E_ARG, "set_particles: no replica %d", r);
+  if (n < 0 || n > b->cap[r])
+    return bset(b, BROMOC_E_CAPACITY, "set_particles: %d ions exceed capacity %d", n, b->cap[r]);
+  const KP &p = b->kp;
+  std::vector<float4> h1(n), h2(n), h3(n);
+  for (int i = 0; i < n; ++i) {
+    const int t = typei[i] < 0 ? -typei[i] : typei[i];
+    if (t <= p.nold || t > p.ntype)
+      return bset(b, BROMOC_E_ARG, "set_particles: typei(%d) = %d is not an ion type", i + 1,
+                  typei[i]);
+    float xh, xl, yh, yl, zh, zl;
+    split(x[i], xh, xl);
+    split(y[i], yh, yl);
+    split(z[i], zh, zl);
+    int code = (b->nwtype_h[t] - 1) | (1 << 16);  // every batch ion is mobile
+    float fcode;
+    std::memcpy(&fcode, &code, sizeof fcode);
+    int fl = 2;
+    float ffl;
+    std::memcpy(&ffl, &fl, sizeof ffl);
+    h1[i] = make_float4(xh, yh, zh, fcode);
+    h2[i] = make_float4(xl, yl, zl, 0.0f);
+    h3[i] = make_float4(0.0f, (float)b->cg_h[t], ffl, 0.0f);
+  }
+  BCU(cudaStreamSynchronize(b->stream));
+  const size_t o = b->off[r];
+  if (n > 0) {
+    BCU(cudaMemcpy(b->pk1[b->cur] + o, h1.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->pk2[b->cur] + o, h2.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->kp.pk3 + o, h3.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
+    BCU(cudaMemcpy(b->kp.typei + o, typei, n * sizeof(int), cudaMemcpyHostToDevice));
+  }
+  b->n[r] = n;
+  b->rep_h[r].n = n;
+  return rebuild_work(b);
+}
+
+int bromoc_batch_get_particles(bromoc_batch *b, int32_t r, int32_t *n, double *x, double *y,
+                               double *z) {
+  if (!b || r < 0 || r >= b->nrep) return bset(b, BROMOC_E_ARG, "get_particles: bad replica");
+  const int m = b->n[r];
+  if (n) *n = m;
+  std::vector<float4> h1(m), h2(m);
+  BCU(cudaStreamSynchronize(b->stream));
+  if (m > 0) {
+    BCU(cudaMemcpy(h1.data(), b->pk1[b->cur] + b->off[r], m * sizeof(float4),
+                   cudaMemcpyDeviceToHost));
+    BCU(cudaMemcpy(h2.data(), b->pk2[b->cur] + b->off[r], m * sizeof(float4),
+                   cudaMemcpyDeviceToHost));
+  }
+  for (int i = 0; i < m; ++i) {
+    if (x) x[i] = (double)h1[i].x + (double)h2[i].x;
+    if (y) y[i] = (double)h1[i].y + (double)h2[i].y;
+    if (z) z[i] = (double)h1[i].z + (double)h2[i].z;
+  }
+  return BROMOC_OK;
+}
+
+// nsteps BD steps (ENERGY + dynamics0) of every replica; eterms, if given,
+// receives nrep x 14 ENERGY terms of the last step's configuration.
+int bromoc_batch_bd_steps(bromoc_batch *b, uint32_t terms, int32_t nsteps, const uint64_t *seeds,
+                          uint64_t step0, double *eterms) {
+  if (!b || !seeds || nsteps < 0) return bset(b, BROMOC_E_ARG, "bd_steps: bad arguments");
+  if (!b->have_sys) return bset(b, BROMOC_E_STATE, "bd_steps: set_systems first");
+  for (int r = 0; r < b->nrep; ++r) b->rep_h[r].seed = seeds[r];
+  BCU(cudaStreamSynchronize(b->stream));  // the pinned records may still be in use
+  std::memcpy(b->rep_pinned, b->rep_h.data(), b->nrep * sizeof(RepDev));
+  BCU(cudaMemcpyAsync(b->rep, b->rep_pinned, b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice,
+                      b->stream));
+  const bool rf = (terms & BROMOC_M_RFPAR) && b->kp.qrfpar;
+  const int nb = (b->nwork + kRowWarps - 1) / kRowWarps;
+  for (int k = 0; k < nsteps; ++k) {
+    KP p = b->kp;
+    p.pk1 = b->pk1[b->cur];
+    p.pk2 = b->pk2[b->cur];
+    const int nx = b->cur ^ 1;
+    launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
+    if (nb > 0) launch_rows(b, p, rf, true, b->pk1[nx], b->pk2[nx], step0 + k, nullptr);
+    b->launches += 1 + (nb > 0);
+    b->cur = nx;
+  }
+  BCU(cudaGetLastError());
+  if (eterms && nsteps > 0) {
+    k_batch_ereduce<<<b->nrep, 256, 0, b->stream>>>(b->rep, b->pe, b->wpart, rf ? 1 : 0,
+                                                    b->eterms);
+    b->launches += 1;
+    BCU(cudaMemcpyAsync(eterms, b->eterms, (size_t)b->nrep * kNTerms * sizeof(double),
+                        cudaMemcpyDeviceToHost, b->stream));
+    BCU(cudaStreamSynchronize(b->stream));
+  }
+  return BROMOC_OK;
+}
+
+// ENERGY of every replica at its current configuration: nrep x 14 terms and,
+// if forces is given, 3 doubles per slot (replica r's ion k at slot off_r + k,
+// off_r from bromoc_batch_offset).
+int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double *eterms) {
+  if (!b) return BROMOC_E_ARG;
+  const bool rf = (terms & BROMOC_M_RFPAR) && b->kp.qrfpar;
+  KP p = b->kp;
+  p.pk1 = b->pk1[b->cur];
+  p.pk2 = b->pk2[b->cur];
+  double *fdev = nullptr;
+  if (forces) BCU(cudaMalloc((void **)&fdev, (size_t)b->nslots * 3 * sizeof(double)));
+  launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
+  const int nb = (b->nwork + kRowWarps - 1) / kRowWarps;
+  if (nb > 0) launch_rows(b, p, rf, false, nullptr, nullptr, 0, fdev);
+  k_batch_ereduce<<<b->nrep, 256, 0, b->stream>>>(b->rep, b->pe, b->wpart, rf ? 1 : 0,
+                                                  b->eterms);
+  b->launches += 2 + (nb > 0);
+  cudaError_t e = cudaGetLastError();
+  if (e == cudaSuccess && eterms)
+    e = cudaMemcpyAsync(eterms, b->eterms, (size_t)b->nrep * kNTerms * sizeof(double),
+                        cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess && forces)
+    e = cudaMemcpyAsync(forces, fdev, (size_t)b->nslots * 3 * sizeof(double),
+                        cudaMemcpyDeviceToHost, b->stream);
+  if (e == cudaSuccess) e = cudaStreamSynchronize(b->stream);
+  if (fdev) cudaFree(fdev);
+  if (e != cudaSuccess) return bset(b, BROMOC_E_CUDA, "batch energy: %s", cudaGetErrorString(e));
+  return BROMOC_OK;
+}
+
+int bromoc_batch_offset(const bromoc_batch *b, int32_t r) {
+  return (b && r >= 0 && r < b->nrep) ? b->off[r] : -1;
+}
+
+int bromoc_batch_slots(const bromoc_batch *b) { return b ? b->nslots : -1; }
+
+}  // extern "C"

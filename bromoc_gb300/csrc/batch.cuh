@@ -1,0 +1,24 @@
+// Replica batches: independent systems that share the prototype context's
+// types, pair tables and grid maps, each with its own box, particles and
+// noise seed, advanced together by one launch per kernel per BD step.
+#pragma once
+#include "kparams.cuh"
+
+namespace bgpu {
+
+// One replica on the device.  Its particles occupy slots [off, off + cap)
+// of the batch arrays (off a multiple of 32), the first n of them live.
+struct RepDev {
+  int off, n, cap;
+  int w0, w1;      // its row-tile work items in the sorted work list
+  int pad;
+  uint64_t seed;   // BD noise key of this replica
+  BoxF box;        // fixcoor constants
+};
+
+// fields.cu: the FP32 field terms of every live slot (one warp each); lane
+// 0 leaves (ememb, egsbpa, evdwgd, erfpar self) of the slot in pe.
+void launch_batch_fields(const KP &p, const int *rep_of, const RepDev *rep, float4 *pe,
+                         int nslots, uint32_t mask, int qforces, cudaStream_t stream);
+
+}  // namespace bgpu

@@ -131,4 +131,53 @@ __device__ __forceinline__ void block_sum_f(const float v[N], float *smem, float
   __syncthreads();
 }
 
+__device__ __forceinline__ void clamp_f(float bdmax, float &d) {
+  if (fabsf(d) > bdmax) d = copysignf(bdmax, d);
+}
+
+// fixcoor.f90:19-68 on float-float coordinates
+__device__ __forceinline__ void fixcoor_ff(const BoxF &c, float h[3], float l[3]) {
+  if (c.shape == 1) {  // sphere: reflect through the wall
+    const float d0 = ff_diff(h[0], l[0], c.ch[0], c.cl[0]);
+    const float d1 = ff_diff(h[1], l[1], c.ch[1], c.cl[1]);
+    const float d2 = ff_diff(h[2], l[2], c.ch[2], c.cl[2]);
+    const float r2 = fmaf(d0, d0, fmaf(d1, d1, d2 * d2));
+    if (r2 > c.rsphe2) {
+      const float lzrad = 2.0f * c.rsphe * rsqrtf(r2) - 1.0f;
+      const float d[3] = {d0, d1, d2};
+      for (int k = 0; k < 3; ++k) {
+        h[k] = c.ch[k];
+        l[k] = c.cl[k];
+        ff_add(h[k], l[k], lzrad * d[k]);
+      }
+    }
+    return;
+  }
+  int k0 = 0;
+  if (c.shape == 2) {  // elliptic cylinder
+    const float ex = ff_diff(h[0], l[0], c.ch[0], c.cl[0]) * c.iecx;
+    const float ey = ff_diff(h[1], l[1], c.ch[1], c.cl[1]) * c.iecy;
+    const float r2 = fmaf(ex, ex, ey * ey);
+    if (r2 > 1.0f) {
+      const float r = 0.99999994f * rsqrtf(r2);
+      for (int k = 0; k < 2; ++k) {
+        const float d = ff_diff(h[k], l[k], c.ch[k], c.cl[k]);
+        h[k] = c.ch[k];
+        l[k] = c.cl[k];
+        ff_add(h[k], l[k], r * d);
+      }
+    }
+    k0 = 2;
+  }
+  for (int k = k0; k < 3; ++k) {  // box clamp (z only for the cylinder)
+    if (ff_diff(h[k], l[k], c.bh[2 * k], c.bl[2 * k]) < 0.0f) {
+      h[k] = c.bh[2 * k];
+      l[k] = c.bl[2 * k];
+    } else if (ff_diff(h[k], l[k], c.bh[2 * k + 1], c.bl[2 * k + 1]) > 0.0f) {
+      h[k] = c.bh[2 * k + 1];
+      l[k] = c.bl[2 * k + 1];
+    }
+  }
+}
+
 }  // namespace bgpu

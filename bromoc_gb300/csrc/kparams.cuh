@@ -25,6 +25,14 @@ struct AxisF {
   int ncl;
 };
 
+// System shape for fixcoor in float-float (fixcoor.f90).
+struct BoxF {
+  int shape;           // 0 box, 1 sphere, 2 elliptic cylinder
+  float rsphe, rsphe2, iecx, iecy;
+  float bh[6], bl[6];  // box bounds x-,x+,y-,y+,z-,z+ (hi, lo)
+  float ch[3], cl[3];  // shape centre (hi, lo)
+};
+
 // Single-precision constants of the FP32 path, filled on the host so that
 // no kernel of that path converts a double.
 struct F32C {
@@ -32,9 +40,7 @@ struct F32C {
   // 9..11: the repulsion grid for the B-spline stencil
   AxisF ax[12];
   float celec, sqrfac, thold8, thold27, kbtdt, bdmax, fact0n1, fact0n2;
-  float rsphe, rsphe2, iecx, iecy;
-  float bh[6], bl[6];  // box bounds x-,x+,y-,y+,z-,z+ (hi, lo)
-  float ch[3], cl[3];  // shape centre (hi, lo)
+  BoxF box;
 };
 
 struct KP {

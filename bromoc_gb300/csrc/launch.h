@@ -88,3 +88,6 @@ struct bromoc_ctx;
 bool bromoc_ctx_pair_view(const bromoc_ctx *ctx, const bgpu::KP **kp,
                           cudaStream_t *stream, int *precision);
 int bromoc_ctx_fail(bromoc_ctx *ctx, int code, const char *msg);
+// FP32 prototype for a replica batch: completes its setup (scratch, FP32
+// constants) and returns its parameter block.
+int bromoc_ctx_prepare_f32(bromoc_ctx *ctx, const bgpu::KP **kp, cudaStream_t *stream);

@@ -236,6 +236,14 @@ class SystemSpec:
             return _lib.efpot_from_knots(r, u, fct, qchr)
         return self._builder(r, u, fct, qchr)
 
+    def system_struct(self) -> "abi.System":
+        """The SYSTEM + SIMUL scalars as the C struct (bromoc_system)."""
+        return abi.System(shape=self.shape, qcountion=int(self.qcountion),
+                          lx=self.lx, ly=self.ly, lz=self.lz, cx=self.cx,
+                          cy=self.cy, cz=self.cz, rsphe=self.rsphe,
+                          temp=self.temp, kbt=self.kbt, cdie=self.cdie,
+                          dt=self.dt, bdmax=self.bdmax)
+
     # ---- push into an engine ------------------------------------------------
     def push(self, eng: "abi.Engine"):
         keep = []
@@ -247,11 +255,7 @@ class SystemSpec:
         nt, ntype = self.nttyp, self.ntype
         eng.nttyp, eng.ntype, eng.nold = nt, ntype, self.nold
         self._builder = eng.efpot_from_knots
-        sysd = abi.System(shape=self.shape, qcountion=int(self.qcountion),
-                          lx=self.lx, ly=self.ly, lz=self.lz, cx=self.cx,
-                          cy=self.cy, cz=self.cz, rsphe=self.rsphe,
-                          temp=self.temp, kbt=self.kbt, cdie=self.cdie,
-                          dt=self.dt, bdmax=self.bdmax)
+        sysd = self.system_struct()
         eng.call("set_system", C.byref(sysd))
         cg = np.zeros(ntype)
         dif = np.zeros(ntype)

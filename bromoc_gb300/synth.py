@@ -82,6 +82,53 @@ def _kcl_types(spec: SystemSpec):
     spec.lj_sigma.update(K=K_PARAMS["sigma"], Cl=CL_PARAMS["sigma"])
 
 
+def jittered_lattice(rng, n, lo, hi, dmin=3.0, ok=None):
+    """n positions in [lo, hi)^3 at least dmin apart, vectorised: a random
+    subset of the sites of a cubic lattice (spacing a >= dmin), each moved
+    uniformly within +-(a - dmin)/2 of its site; ok(points) -> bool mask
+    drops sites (the lattice is refined until n sites remain)."""
+    lo, hi = float(lo), float(hi)
+    m = int(np.ceil(n ** (1.0 / 3.0)))
+    while True:
+        a = (hi - lo) / m
+        if a < dmin:
+            raise ValueError("box too small for n particles at this separation")
+        sites = rng.permutation(m ** 3)
+        ijk = np.stack(np.unravel_index(sites, (m, m, m)), 1).astype(float)
+        p = lo + (ijk + 0.5) * a + (a - dmin) * (rng.random((len(sites), 3)) - 0.5)
+        if ok is not None:
+            p = p[ok(p)]
+        if len(p) >= n:
+            return p[:n]
+        m += 1
+
+
+def outside_pore_slab(p, radius=10.0, slab=30.0, half_xy=59.5):
+    """Mask of points not inside the solid slab of pore_maps' geometry."""
+    rho = np.hypot(p[:, 0], p[:, 1])
+    inside_map = (np.abs(p[:, 0]) <= half_xy) & (np.abs(p[:, 1]) <= half_xy)
+    return ~(inside_map & (np.abs(p[:, 2]) <= 0.5 * slab + 1.0) & (rho >= radius - 1.0))
+
+
+def batch_replicas(seed=4, nrep=256, nmin=200, nmax=8000, conc=1.0):
+    """Replica set of uneven bulk KCl systems at conc (M of salt, so
+    2 conc 6.022e-4 ions per A^3): counts uniform in [nmin, nmax], cube boxes
+    of edge (N / (2 conc 6.022e-4))^(1/3) centred at the origin, positions
+    on a jittered lattice (3 A minimum separation).
+    Returns (counts, edges, list of (x, y, z, typei))."""
+    rng = np.random.default_rng(seed)
+    counts = rng.integers(nmin, nmax + 1, nrep)
+    counts += counts % 2  # equal K+ and Cl-
+    edges = (counts / (2.0 * conc * 6.02214e-4)) ** (1.0 / 3.0)
+    parts = []
+    for n, L in zip(counts, edges):
+        h = 0.5 * L - 0.5
+        p = jittered_lattice(rng, int(n), -h, h, ok=outside_pore_slab)
+        t = np.array([1, 2] * (int(n) // 2), np.int32)
+        parts.append((p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy(), t))
+    return counts.astype(int), edges, parts
+
+
 def bulk_kcl(seed=1, n_per=130, L=60.0, srpmf=False, precision=abi.FP64):
     """Bulk KCl: 2*n_per ions in an L^3 box with hard walls."""
     rng = np.random.default_rng(seed)

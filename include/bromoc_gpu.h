@@ -359,6 +359,38 @@ int bromoc_gpu_efpot_from_knots(int32_t n, const double *xx, const double *yy,
                                 double fct, int32_t qchr, double *ep,
                                 double *sc3, double *dm2o, double *dmio);
 
+/* ---- replica batches (no reference counterpart: the reference runs one
+ * system per process) --------------------------------------------------------
+ * nrep independent ion systems (capacity[r] ions each) that share the FP32
+ * prototype context's types, pair laws and grid maps, each with its own box,
+ * particles and noise seed.  Restrictions: analytic ion-ion laws (no EFPOT),
+ * at most 16 ion types, no sites or fixed ions, dynamics0, every replica
+ * with the prototype's dt, kbt and bdmax.  The prototype must outlive the
+ * batch.  A replica's trajectory with seed s is that of a single context
+ * driven by bromoc_gpu_bd_steps with seed s (up to FP32 summation order). */
+typedef struct bromoc_batch bromoc_batch;
+int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity,
+                        bromoc_batch **out);
+int bromoc_batch_destroy(bromoc_batch *b);
+const char *bromoc_batch_last_error(const bromoc_batch *b);
+/* per-replica SYSTEM blocks: box/shape for fixcoor; dt, kbt, bdmax checked */
+int bromoc_batch_set_systems(bromoc_batch *b, const bromoc_system *sys);
+int bromoc_batch_set_particles(bromoc_batch *b, int32_t r, int32_t n, const double *x,
+                               const double *y, const double *z, const int32_t *typei);
+int bromoc_batch_get_particles(bromoc_batch *b, int32_t r, int32_t *n, double *x,
+                               double *y, double *z);
+/* nsteps x (ENERGY + dynamics0) of every replica; seeds[nrep]; eterms
+ * (nrep x BROMOC_NTERMS, or NULL) receives the last step's energies */
+int bromoc_batch_bd_steps(bromoc_batch *b, uint32_t terms, int32_t nsteps,
+                          const uint64_t *seeds, uint64_t step0, double *eterms);
+/* ENERGY of every replica; forces (3 doubles per slot, or NULL): replica
+ * r's ion k at slot bromoc_batch_offset(b, r) + k.  Allocates a scratch
+ * buffer when forces are requested. */
+int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double *eterms);
+int bromoc_batch_offset(const bromoc_batch *b, int32_t r);
+int bromoc_batch_slots(const bromoc_batch *b);
+int64_t bromoc_batch_launch_count(const bromoc_batch *b);
+
 #ifdef __cplusplus
 }
 #endif

@@ -58,6 +58,20 @@ def load() -> C.CDLL:
             f = getattr(lib, "bromoc_batch_" + name)
             f.argtypes = args
             f.restype = C.c_int
+        u64 = C.c_uint64
+        for name, args in (
+                ("create", [vp, C.c_int32, C.c_int32, C.POINTER(vp)]),
+                ("destroy", [vp]),
+                ("set_particles", [vp, C.c_int32, d, d, d, i32]),
+                ("forward", [vp, C.c_int32, C.c_int32, u64, u64, C.c_int32, C.c_double,
+                             C.c_double, C.c_double, d]),
+                ("backward", [vp, d, d, d]),
+                ("get_particles", [vp, C.c_int32, d, d, d])):
+            f = getattr(lib, "bromoc_adj_" + name)
+            f.argtypes = args
+            f.restype = C.c_int
+        lib.bromoc_adj_last_error.argtypes = [vp]
+        lib.bromoc_adj_last_error.restype = C.c_char_p
         lib.bromoc_batch_last_error.argtypes = [vp]
         lib.bromoc_batch_last_error.restype = C.c_char_p
         lib.bromoc_batch_launch_count.argtypes = [vp]

@@ -161,17 +161,29 @@ class BromocError(RuntimeError):
 # Contexts must be destroyed before the CUDA runtime linked into the library
 # tears itself down at process exit: Python's atexit hooks run first.
 _LIVE = weakref.WeakSet()
+# objects that borrow a context (replica batches, adjoint engines): closed
+# before any context, since their teardown uses the context's stream
+_DEPENDENTS = weakref.WeakSet()
 _SHUTDOWN = False
+
+
+def register_dependent(obj) -> None:
+    _DEPENDENTS.add(obj)
+
+
+def shutting_down() -> bool:
+    return _SHUTDOWN
 
 
 @atexit.register
 def _close_all():
     global _SHUTDOWN
-    for eng in list(_LIVE):
-        try:
-            eng.close()
-        except Exception:
-            pass
+    for group in (_DEPENDENTS, _LIVE):
+        for obj in list(group):
+            try:
+                obj.close()
+            except Exception:
+                pass
     _SHUTDOWN = True
 
 

@@ -22,6 +22,7 @@ class Batch:
         if rc != abi.OK:
             raise abi.BromocError(rc, self.lib.bromoc_gpu_last_error(proto.h).decode())
         self.h = h
+        abi.register_dependent(self)
 
     def _chk(self, rc, what):
         if rc != abi.OK:
@@ -34,6 +35,8 @@ class Batch:
             self.h = None
 
     def __del__(self):
+        if abi.shutting_down():
+            return
         try:
             self.close()
         except Exception:

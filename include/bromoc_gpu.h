@@ -391,6 +391,36 @@ int bromoc_batch_offset(const bromoc_batch *b, int32_t r);
 int bromoc_batch_slots(const bromoc_batch *b);
 int64_t bromoc_batch_launch_count(const bromoc_batch *b);
 
+/* ---- adjoint of a BD segment (no reference counterpart) ----------------------
+ * Gradient of a function of the segment's pair-distance histogram with respect
+ * to the tabulated (EFPOT) ion-ion laws.  The prototype context supplies the
+ * types, the pair tables (every ion-ion law tabulated), the box (BROMOC_BOX,
+ * hard walls) and dt/kbt; ions only, at most 4 ion types, dynamics0 with the
+ * Philox noise of (seed, step).  precision: arithmetic of the pair terms
+ * (BROMOC_FP32 needs an FP32 prototype).  The histogram is the Gaussian-
+ * smoothed pair-distance histogram, H_b = sum over the configurations after
+ * each step and over pairs of K(r0 + b dr - r_ij), K the normal density of
+ * width sigma, per ion-type pair (a <= b): ntp = nt (nt + 1) / 2 rows of
+ * nbins.  backward takes dL/dH and returns dL/d(table parameters)
+ * in the layouts of bromoc_pairs: g_ep[3 cnt] (p1, p2, p3 per piece), g_sc[3 ntc]
+ * (core a/r^12 constant, core offset, tail a/r^6 constant). */
+typedef struct bromoc_adj bromoc_adj;
+int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
+                      bromoc_adj **out);
+int bromoc_adj_destroy(bromoc_adj *a);
+const char *bromoc_adj_last_error(const bromoc_adj *a);
+int bromoc_adj_set_particles(bromoc_adj *a, int32_t n, const double *x, const double *y,
+                             const double *z, const int32_t *typei);
+/* nsteps BD steps from the configuration of set_particles, checkpoints every
+ * ckpt steps; hist[ntp * nbins] receives the histogram */
+int bromoc_adj_forward(bromoc_adj *a, int32_t nsteps, int32_t ckpt, uint64_t seed,
+                       uint64_t step0, int32_t nbins, double r0, double dr, double sigma,
+                       double *hist);
+int bromoc_adj_backward(bromoc_adj *a, const double *dl_dhist, double *g_ep, double *g_sc);
+/* which = 0: the initial configuration, 1: the last forward run's final one */
+int bromoc_adj_get_particles(bromoc_adj *a, int32_t which, double *x, double *y,
+                             double *z);
+
 #ifdef __cplusplus
 }
 #endif

@@ -80,3 +80,15 @@ def make_pair(spec: SystemSpec, gpu_create, oracle_create, cap=4000):
     spec.push(g)
     spec.push(o)
     return g, o
+
+
+def efpot_all(n_per=32, L=30.0, seed=13, precision=abi.FP64, r1=10.0):
+    """Bulk KCl whose three ion-ion laws are all tabulated (the adjoint's
+    system)."""
+    s = pairs(n_per, L, srpmf=False, seed=seed, precision=precision)
+    rng = np.random.default_rng(seed)
+    s.efpot_res = 0.05
+    s.efpot_knots[("K", "K")] = synth.efpot_knots(rng, 3.1, 0.09, r0=2.5, r1=r1)
+    s.efpot_knots[("K", "Cl")] = synth.efpot_knots(rng, 3.6, 0.11, r0=2.5, r1=r1)
+    s.efpot_knots[("Cl", "Cl")] = synth.efpot_knots(rng, 4.0, 0.15, r0=2.5, r1=r1)
+    return s

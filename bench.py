@@ -12,7 +12,9 @@ in FP64.  Synthetic inputs (the reference ships no maps or decks).
 
 The line also carries "batched": 256 bulk KCl replicas of 200-8000 ions
 (1 M, cube boxes, the same maps) advanced by the replica-batch engine, timed
-against the plain path run replica by replica through one context.
+against the plain path run replica by replica through one context; and
+"adjoint": the gradient of a smoothed-RDF loss over a 2000-step segment of
+4096 ions with respect to 3x300 EFPOT knots (forward + adjoint times).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl gb300|reference]
 
@@ -201,6 +203,60 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
             "plain_per_replica": {"value": plain, "ms_per_step": tp / plain_steps,
                                   "steps": plain_steps},
             "speedup_vs_plain": value / plain}
+
+
+ADJ_N, ADJ_STEPS, ADJ_CKPT = 4096, 2000, 100
+
+
+def adjoint_measure(sh):
+    """Adjoint of a frozen-noise BD segment (4096 ions at 1 M KCl, all three
+    ion-ion laws tabulated on 300 knots each, 2000 steps, checkpoints every
+    100): forward (with the smoothed-RDF histogram, 0.05-15 A, sigma 0.1 A)
+    and backward (recomputation + adjoint), FP32 pair arithmetic, FP64
+    gradient accumulators; CUDA events on the shared stream."""
+    import torch
+    from bromoc_gb300 import _lib
+    from bromoc_gb300.adjoint import Adjoint, RdfLoss, knot_gradient, knot_jacobians
+    rng = np.random.default_rng(SEED + 5)
+    L = (ADJ_N / (2 * 6.02214e-4)) ** (1.0 / 3.0)
+    spec = synth.bulk_kcl(seed=SEED, n_per=2, L=L, precision=abi.FP32)
+    h = 0.5 * L - 0.5
+    p = synth.jittered_lattice(rng, ADJ_N, -h, h)
+    spec.x, spec.y, spec.z = p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
+    spec.typei = np.array([1, 2] * (ADJ_N // 2), np.int32)
+    spec.efpot_res = 0.05
+    for key, (sg, ep) in ((("K", "K"), (3.1, 0.09)), (("K", "Cl"), (3.6, 0.11)),
+                          (("Cl", "Cl"), (4.0, 0.15))):
+        spec.efpot_knots[key] = synth.efpot_knots(rng, sg, ep, r0=1.05, r1=16.0, res=0.05)
+    proto = _lib.create(ADJ_N + 64, abi.FP32, sh)
+    spec.push(proto)
+    adj = Adjoint(proto, ADJ_N, abi.FP32)
+    adj.set_particles(spec.x, spec.y, spec.z, spec.typei)
+    nbins, r0, dr, sig = 150, 0.05, 0.1, 0.1
+    rb = r0 + dr * np.arange(nbins)
+    loss = RdfLoss(2, [ADJ_N // 2] * 2, L ** 3, ADJ_STEPS, rb, np.ones((3, nbins)))
+    stream = torch.cuda.current_stream()
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
+    torch.cuda.synchronize()
+    ev[0].record(stream)
+    hist = adj.forward(ADJ_STEPS, ADJ_CKPT, SEED, 0, nbins, r0, dr, sig, 3)
+    ev[1].record(stream)
+    value, dl = loss.loss_grad(hist)
+    pt = spec.pair_tables()
+    g_ep, g_sc = adj.backward(dl, int(pt["cnt"]), int(pt["ntc"]))
+    ev[2].record(stream)
+    torch.cuda.synchronize()
+    t_f, t_b = ev[0].elapsed_time(ev[1]), ev[1].elapsed_time(ev[2])
+    grads = knot_gradient(knot_jacobians(spec, proto.efpot_from_knots), g_ep, g_sc)
+    adj.close()
+    return {"workload": f"{ADJ_N} ions, 1 M KCl, 3x300 EFPOT knots, {ADJ_STEPS}-step "
+                        f"frozen-noise segment, checkpoints every {ADJ_CKPT}, smoothed RDF "
+                        "0.05-15 A (sigma 0.1 A), FP32 pairs, FP64 gradient accumulators",
+            "forward_ms": t_f, "backward_ms": t_b,
+            "value": ADJ_N * ADJ_STEPS / ((t_f + t_b) * 1e-3),
+            "unit": "particle-steps/s (forward + adjoint)",
+            "loss": value,
+            "knot_grad_norm": float(np.sqrt(sum(np.sum(g * g) for g in grads.values())))}
 
 
 def measured_peaks():
@@ -422,8 +478,8 @@ def run_gpu(args, rank, world, local_rank):
         per = PAIR_FLOP + RF_FLOP
         ms, nl = kt[dom]
         achieved = per * pairs / (ms / nl * 1e-3) / 1e12
-        traffic, prof = profile_traffic("k_pairs32")
-        roof = {"kernel": "k_pairs32",
+        traffic, prof = profile_traffic("k_pairs32n")
+        roof = {"kernel": "k_pairs32n",
                 "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
                 "unit": "TFLOP/s", "frac": achieved / peak_fp32,
                 "traffic": traffic,
@@ -442,6 +498,7 @@ def run_gpu(args, rank, world, local_rank):
                 "peak_source": src, "launch_ms": ms / nl,
                 "share": kt[dom][0] / tot_k}
     batched = batch_measure(sh, flush)
+    adjoint = adjoint_measure(sh)
     cpu = oracle_baseline(float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15")))
     clocks = clk.summary()
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s",
@@ -461,6 +518,7 @@ def run_gpu(args, rank, world, local_rank):
                     "path": "bromoc_gpu_simul_cycles_host, pinned host arrays"},
             "gpu_launches": launches,
             "batched": batched,
+            "adjoint": adjoint,
             "wall_s": wall, "clocks": clocks}
     print(json.dumps(line), flush=True)
     if dist:

@@ -201,7 +201,12 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_pairs(KP p, AdjArgs a) {
             for (int b = b0; b <= b1; ++b) {
               const R u = ((R)a.r0 + b * (R)a.dr - r) / sg;
               const R k = ia * exp(-(R)0.5 * u * u);
-              atomicAdd(hb + b, (unsigned long long)((double)k * kHistScale + 0.5));
+              unsigned long long q;
+              if constexpr (sizeof(R) == 8)
+                q = (unsigned long long)(k * kHistScale + 0.5);
+              else  // FP32 run: the fixed-point value formed on the FP32 pipe
+                q = __float2ull_rn(k * (float)kHistScale);
+              atomicAdd(hb + b, q);
             }
           }
           continue;

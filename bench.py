@@ -44,7 +44,7 @@ import numpy as np
 ROOT = Path(__file__).resolve().parent
 sys.path.insert(0, str(ROOT))
 
-from bromoc_gb300 import abi, synth  # noqa: E402
+from bromoc_gb300 import abi, replicas, synth  # noqa: E402
 
 METRIC = ("particle-steps/s, 1 GB300: plain vs batched+adjoint, force rel err "
           "≤1e-5 vs FP64")
@@ -58,7 +58,7 @@ RF_FLOP = 32                # RFPAR cross term, FLOP per unordered pair
 
 def workload(rank: int = 0, precision=abi.FP32):
     maps = synth.pore_maps(seed=102)
-    spec = synth.pore(seed=3 + 1000 * rank, nions=NIONS, maps=maps,
+    spec = synth.pore(seed=replicas.replica_seed(3, rank), nions=NIONS, maps=maps,
                       precision=precision, buffers=True)
     return spec
 
@@ -405,13 +405,7 @@ def run_gpu(args, rank, world, local_rank):
     launches = _lib.launch_count(eng) - l0
     t_ms = sum(a.elapsed_time(b) for a, b in ev)
     ps = NBD * sum(nmob)
-    tmax = t_ms
-    if dist:
-        tt = torch.tensor([t_ms, ps], dtype=torch.float64, device="cuda")
-        tm = tt[:1].clone()
-        dist.all_reduce(tm, op=dist.ReduceOp.MAX)
-        dist.all_reduce(tt[1:], op=dist.ReduceOp.SUM)
-        tmax, ps = float(tm[0]), float(tt[1])
+    tmax, ps = replicas.aggregate(t_ms, ps, device="cuda")
     value = ps / (tmax * 1e-3)
     # per-kernel CUDA-event timing in a separate pass after the timed region
     # (the event records would perturb it), same workload and step sequence

@@ -184,12 +184,12 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
     for r, (x, y, z, t) in enumerate(parts):
         g.call("set_system", C.byref(systems[r]))
         g.set_particles(x, y, z, t)
-        g.bd_steps(1, int(seeds[r]), 0)
+        g.bd_steps(1, int(seeds[r]), 0, energies=False)
         torch.cuda.synchronize()
         flush.zero_()
         a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         a.record(stream)
-        g.bd_steps(plain_steps, int(seeds[r]), 1)
+        g.bd_steps(plain_steps, int(seeds[r]), 1, energies=False)
         e.record(stream)
         torch.cuda.synchronize()
         tp += a.elapsed_time(e)
@@ -377,8 +377,8 @@ def run_gpu(args, rank, world, local_rank):
     nfix = spec.nsites + spec.nfix
 
     def step(cyc):
-        eng.grand(NGCMC, SEED, cyc, )
-        eng.bd_steps(NBD, SEED, (cyc - 1) * NBD)
+        eng.grand(NGCMC, SEED, cyc)
+        eng.bd_steps(NBD, SEED, (cyc - 1) * NBD, energies=False)
 
     for c in range(1, args.warmup + 1):
         step(c)
@@ -409,18 +409,30 @@ def run_gpu(args, rank, world, local_rank):
     value = ps / (tmax * 1e-3)
     # per-kernel CUDA-event timing in a separate pass after the timed region
     # (the event records would perturb it), same workload and step sequence
+    # (a) as timed: the BD steps of a cycle are one fused loop launch;
+    # (b) the same steps one launch per kernel and step, for the per-kernel
+    #     breakdown and the pair kernel's own roofline
     ktsteps = min(args.steps, 10)
     cyc_k = args.warmup + args.steps + 1
-    _lib.kernel_timing(eng, True)
-    for k in range(ktsteps):
-        flush.zero_()
-        step(cyc_k + k)
-    torch.cuda.synchronize()
-    kt = {name: _lib.kernel_time(eng, k) for name, k in
-          (("pairs", _lib.K_PAIRS), ("rfcross", _lib.K_RFCROSS),
-           ("fields", _lib.K_FIELDS), ("assemble", _lib.K_ASSEMBLE))}
-    kt = {k: v for k, v in kt.items() if v[1] > 0}
-    _lib.kernel_timing(eng, False)
+
+    def timed_kernels(cyc0):
+        _lib.kernel_timing(eng, True)
+        for k in range(ktsteps):
+            flush.zero_()
+            step(cyc0 + k)
+        torch.cuda.synchronize()
+        out = {name: _lib.kernel_time(eng, k) for name, k in
+               (("pairs", _lib.K_PAIRS), ("rfcross", _lib.K_RFCROSS),
+                ("fields", _lib.K_FIELDS), ("assemble", _lib.K_ASSEMBLE),
+                ("bd_loop", _lib.K_LOOP))}
+        _lib.kernel_timing(eng, False)
+        return {k: v for k, v in out.items() if v[1] > 0}
+
+    kt = timed_kernels(cyc_k)
+    _lib.set_fused_bd(eng, False)
+    kt_split = timed_kernels(cyc_k + ktsteps)
+    _lib.set_fused_bd(eng, True)
+    ktsteps *= 2
 
     # e2e through the host-array C ABI entry point (pinned host buffers)
     cap = 23000
@@ -466,7 +478,32 @@ def run_gpu(args, rank, world, local_rank):
     dom = max(kt, key=lambda k: kt[k][0])
     n_ion = statistics.mean(nmob) + spec.nfix
     pairs = n_ion * (n_ion - 1) / 2
-    if dom == "pairs":
+    per = PAIR_FLOP + RF_FLOP
+    pair_roof = None
+    if "pairs" in kt_split:
+        ms, nl = kt_split["pairs"]
+        a = per * pairs / (ms / nl * 1e-3) / 1e12
+        pair_roof = {"kernel": "k_pairs32n (one launch per BD step)", "achieved": a,
+                     "unit": "TFLOP/s", "frac": a / peak_fp32, "launch_ms": ms / nl,
+                     "traffic": profile_traffic("k_pairs32n")[0]}
+    if dom == "bd_loop":
+        # one launch runs the NBD steps of a cycle: the pair work of each
+        # step (ion-ion law + RFPAR cross term of every unordered pair) is
+        # the algorithmic FLOP count; maps, assembly and moves ride along
+        ms, nl = kt[dom]
+        achieved = per * pairs * NBD / (ms / nl * 1e-3) / 1e12
+        traffic, prof = profile_traffic("k_bd_loop")
+        roof = {"kernel": "k_bd_loop",
+                "bound": "fp32", "achieved": achieved, "peak": peak_fp32,
+                "unit": "TFLOP/s", "frac": achieved / peak_fp32,
+                "traffic": traffic,
+                "peak_source": "FP32 FMA probe kernel measured in this run "
+                               "(MEASURED_PEAKS.json has no FP32 figure)",
+                "algorithmic": f"{per} FLOP x N(N-1)/2 unordered pairs x {NBD} BD "
+                               f"steps per launch, N = {n_ion:.0f} ions",
+                "launch_ms": ms / nl, "share": kt[dom][0] / tot_k,
+                "pair_kernel_unfused": pair_roof}
+    elif dom == "pairs":
         # the FP32 pair kernel evaluates the ion-ion law and the RFPAR cross
         # term of every pair in one pass
         per = PAIR_FLOP + RF_FLOP
@@ -504,6 +541,8 @@ def run_gpu(args, rank, world, local_rank):
             "roofline": roof,
             "kernel_ms": {k: {"total_ms": v[0], "launches": v[1],
                               "share": v[0] / tot_k} for k, v in kt.items()},
+            "kernel_ms_unfused": {k: {"total_ms": v[0], "launches": v[1]}
+                                  for k, v in kt_split.items()},
             "cpu_baseline": cpu,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": h2d // e2e_steps,

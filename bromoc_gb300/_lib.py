@@ -38,6 +38,8 @@ def load() -> C.CDLL:
         lib.bromoc_gpu_launch_count.restype = C.c_int64
         lib.bromoc_gpu_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
         lib.bromoc_gpu_kernel_timing.restype = C.c_int
+        lib.bromoc_gpu_set_fused_bd.argtypes = [C.c_void_p, C.c_int32]
+        lib.bromoc_gpu_set_fused_bd.restype = C.c_int
         lib.bromoc_gpu_kernel_time.argtypes = [C.c_void_p, C.c_int32, d,
                                                C.POINTER(C.c_int64)]
         lib.bromoc_gpu_kernel_time.restype = C.c_int
@@ -98,7 +100,13 @@ def efpot_from_knots(r, u, fct, qchr):
     return abi.efpot_from_knots(load(), PREFIX, r, u, fct, qchr)
 
 
-K_PAIRS, K_RFCROSS, K_FIELDS, K_ASSEMBLE = 0, 1, 2, 3
+K_PAIRS, K_RFCROSS, K_FIELDS, K_ASSEMBLE, K_LOOP = 0, 1, 2, 3, 4
+
+
+def set_fused_bd(eng: abi.Engine, on: bool) -> None:
+    """FP32 bd_steps as one cooperative launch (on, the default) or one
+    launch per kernel and step (off); the trajectories agree."""
+    eng._chk(load().bromoc_gpu_set_fused_bd(eng.h, int(on)), "set_fused_bd")
 
 
 def kernel_timing(eng: abi.Engine, on: bool) -> None:

@@ -300,11 +300,15 @@ class Engine:
     def dynamics(self, variant, seed, step):
         self._chk(self._fn("dynamics")(self.h, variant, seed, step), "dynamics")
 
-    def bd_steps(self, nsteps, seed, step0=0, variant=DYN0, terms=M_ALL):
+    def bd_steps(self, nsteps, seed, step0=0, variant=DYN0, terms=M_ALL,
+                 energies=True):
+        """nsteps BD steps; with energies, the terms at the last step's
+        starting configuration (else None, and no energy is formed)."""
         e = np.zeros(NTERMS)
         self._chk(self._fn("bd_steps")(self.h, terms, variant, nsteps, seed,
-                                       step0, ptr(e, C.c_double)), "bd_steps")
-        return dict(zip(TERM_NAMES, e.tolist()))
+                                       step0, ptr(e, C.c_double) if energies else None),
+                  "bd_steps")
+        return dict(zip(TERM_NAMES, e.tolist())) if energies else None
 
     def grand(self, ngcmc, seed, cycle, terms=M_ALL):
         d = C.c_double(0.0)

@@ -59,6 +59,7 @@ struct bromoc_ctx {
   long long launches = 0;  // kernels launched by this context
   // diagnostic kernel timing: event pairs per kernel family
   bool timing = false;
+  bool fused_bd = true;  // nsteps BD steps in one cooperative launch where supported
   std::vector<KTimer> tpool[BROMOC_K_NKINDS];
   int tused[BROMOC_K_NKINDS] = {};
 };
@@ -311,7 +312,7 @@ void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
 }
 
 int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
-                AssembleFlags &fl) {
+                AssembleFlags &fl, bool timers = true) {
   KP &p = ctx->kp;
   plan.ntot_ub = ntot_ub(ctx);
   plan.fp32 = ctx->precision == BROMOC_FP32;
@@ -362,9 +363,11 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
     fl.rf = (mask & BROMOC_M_RFPAR) && p.qrfpar && nion > 0 && plan.nchunk_rf > 0;
     fl.nchunk_rf = fl.rf ? plan.nchunk_rf : 0;
   }
-  plan.t_pairs = (fl.ii || fl.ntile) ? next_timer(ctx, BROMOC_K_PAIRS) : nullptr;
-  plan.t_rf = fl.rf ? next_timer(ctx, BROMOC_K_RFCROSS) : nullptr;
-  plan.t_fields = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_FIELDS) : nullptr;
+  if (timers) {
+    plan.t_pairs = (fl.ii || fl.ntile) ? next_timer(ctx, BROMOC_K_PAIRS) : nullptr;
+    plan.t_rf = fl.rf ? next_timer(ctx, BROMOC_K_RFCROSS) : nullptr;
+    plan.t_fields = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_FIELDS) : nullptr;
+  }
   if (energy_slots(p, plan, mask) > ctx->nslot_cap)
     return set_err(ctx, BROMOC_E_ARG, "energy slots exceed scratch");
   return BROMOC_OK;
@@ -1190,7 +1193,24 @@ int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_
   AssembleFlags fl{};
   if ((rc = ensure_ff(ctx))) return rc;
   if (ctx->precision == BROMOC_FP32 && nsteps > 0) ctx->dbl_fresh = false;
-  for (int k = 0; k < nsteps; ++k) {
+  int k = 0;
+  // FP32 Newton-3 systems without sites: the steps whose energy is not
+  // wanted run as one cooperative launch (loop.cu) with the forces, moves
+  // and summation order of the per-kernel steps below.
+  const int nloop = eterms ? nsteps - 1 : nsteps;
+  if (ctx->fused_bd && ctx->precision == BROMOC_FP32 && nloop > 0) {
+    if ((rc = plan_energy(ctx, terms, false, plan, fl, false))) return rc;
+    if (bd_loop_supported(p, fl)) {
+      KTimer *tl = next_timer(ctx, BROMOC_K_LOOP);
+      if (tl) cudaEventRecord(tl->a, ctx->stream);
+      CU(launch_bd_loop(p, fl, plan.ntot_ub, terms, variant, seed, step0, nloop, 1,
+                        ctx->stream));
+      if (tl) cudaEventRecord(tl->b, ctx->stream);
+      ctx->launches += 1;
+      k = nloop;
+    }
+  }
+  for (; k < nsteps; ++k) {
     const bool last = k + 1 == nsteps;
     if ((rc = plan_energy(ctx, terms, last && eterms, plan, fl))) return rc;
     ctx->launches += launch_energy(p, plan, terms, 1, ctx->stream);
@@ -1296,6 +1316,12 @@ int bromoc_gpu_get_countions(bromoc_ctx *ctx, int32_t *nf, int32_t *nb) {
 
 int64_t bromoc_gpu_launch_count(const bromoc_ctx *ctx) {
   return ctx ? (int64_t)ctx->launches : -1;
+}
+
+int bromoc_gpu_set_fused_bd(bromoc_ctx *ctx, int32_t on) {
+  if (!ctx) return BROMOC_E_ARG;
+  ctx->fused_bd = on != 0;
+  return BROMOC_OK;
 }
 
 int bromoc_gpu_kernel_timing(bromoc_ctx *ctx, int32_t on) {

@@ -5,6 +5,7 @@
 #include "ff.cuh"
 #include "launch.h"
 #include "physics.cuh"
+#include "pairs_n3.cuh"
 
 namespace bgpu {
 
@@ -223,20 +224,6 @@ __global__ void __launch_bounds__(kPairThreads)
   }
 }
 
-// ---------------------------------------------------------------------------
-// FP32 pair kernel with Newton's third law: each unordered ion pair once.
-// Ions form tiles of 32; one warp takes tile pair (I, J), I <= J, from a
-// flat row-major list.  Lane l holds row ion i = I*32 + l in registers; the
-// column tile's records and its force accumulators sit in the warp's shared
-// memory.  At step k lane l meets column lane m = (l + k) mod 32, so in one
-// step the 32 lanes touch 32 different column entries and the column forces
-// need no atomics (a __syncwarp orders the steps).  A diagonal tile uses
-// k = 1..16, half of the lanes at k = 16, so each pair inside it appears once.
-// Same laws and rules as k_pairs32 (ion-ion force only on mobile ions, the
-// RFPAR chain on every ion in the map); the energy of a pair is added once.
-// Output: per tile pair and side, per lane, (f, A) and B (tpf, tpb); the
-// assembly kernel sums a particle's row and column entries in fixed order.
-// ---------------------------------------------------------------------------
 constexpr int kN3Warps = 4;
 
 template <bool II, bool RF, bool EFP>
@@ -252,178 +239,13 @@ __global__ void __launch_bounds__(32 * kN3Warps)
   if (II && !EFP)
     for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
-  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int w = threadIdx.x >> 5;
   const int T = p.ntile;
   const int q = blockIdx.x * kN3Warps + w;
-  const int ntot = p.st->ntot;
-  const int m0 = p.nsites + p.nfix;
-  const bool live = q < n3_pairs(T);
   float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
-  float fx = 0.f, fy = 0.f, fz = 0.f, A = 0.f, B = 0.f;
-  bool iv = false;
-  int jl = 0;
-  if (live) {  // warp-uniform
-    // row I of q: the largest I with offset(I) <= q
-    int I = (int)((2.0f * T + 1.0f - sqrtf((2.0f * T + 1.0f) * (2.0f * T + 1.0f) - 8.0f * q)) * 0.5f);
-    I = max(0, min(I, T - 1));
-    while (I > 0 && n3_index(T, I, I) > q) --I;
-    while (I + 1 < T && n3_index(T, I + 1, I + 1) <= q) ++I;
-    const int J = I + (q - n3_index(T, I, I));
-    const bool diag = I == J;
-    const int i = p.nsites + I * 32 + lane;
-    jl = p.nsites + J * 32 + lane;
-    // column tile into shared memory (code -1 marks a slot past ntot)
-    if (jl < ntot) {
-      sh[w][lane] = p.pk1[jl];
-      sl[w][lane] = p.pk2[jl];
-      if (RF) sq[w][lane] = p.pk3[jl];
-    } else {
-      sh[w][lane] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
-      sl[w][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (RF) sq[w][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-    }
-    acc[w][lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-    if (RF) accb[w][lane] = 0.f;
-    iv = i < ntot;
-    float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th, tq = th;
-    if (iv) {
-      th = p.pk1[i];
-      tl = p.pk2[i];
-      if (RF) tq = p.pk3[i];
-    }
-    const int tcode = __float_as_int(th.w);
-    const bool tmob = iv && i >= m0;
-    const int row = EFP ? (tcode & 0xffff) * p.nttyp : ((tcode & 0xffff) - p.ndna) * nt;
-    const int tb = __float_as_int(tq.z);
-    const float srt = tl.w, rft = tq.x, ct = p.f.celec * tq.y;
-    __syncwarp();
-    // Fast path: an off-diagonal tile pair whose 64 ions are all present and
-    // mobile (and, with RFPAR, all qualify for the cross term in both roles):
-    // no per-pair validity, mobility or role test.
-    bool lane_ok = iv && tmob && jl < ntot && jl >= m0;
-    if (RF) lane_ok = lane_ok && (tb & 12) == 12 && (__float_as_int(sq[w][lane].z) & 12) == 12;
-    const bool fast = II && !EFP && !diag && __all_sync(0xffffffffu, lane_ok);
-    if (fast) {
-      for (int k = 0; k < 32; ++k) {
-        const int mm = (lane + k) & 31;
-        float4 *ac = acc[w];
-        float *acb = accb[w];
-        const float4 h = sh[w][mm], l = sl[w][mm];
-        const float dx = (th.x - h.x) + (tl.x - l.x);
-        const float dy = (th.y - h.y) + (tl.y - l.y);
-        const float dz = (th.z - h.z) + (tl.z - l.z);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
-        const float ir = rsqrtf(r2), ir2 = ir * ir;
-        const float cofo = c.x * ir;
-        e[0] += cofo;
-        float d6 = c.z * ir2;
-        d6 = d6 * d6 * d6;
-        const float d12 = d6 * d6;
-        e[1] = fmaf(c.y, d12 - d6, e[1]);
-        float de = fmaf(cofo, ir2, (6.0f * c.y) * ir2 * fmaf(2.0f, d12, -d6));
-        const int cf = __float_as_int(c.w);
-        if ((cf & kSrp) && r2 <= p.rthf) de += srpmf32(p, cf >> 4, r2, ir, 1.0f, e);
-        float4 a = ac[mm];
-        if (RF) {
-          const float4 u = sq[w][mm];
-          const float rij = u.x * rft, srij = l.w * srt;
-          const float rfdn = rsqrtf(fmaf(rij, rij, r2));
-          const float aux0 = ct * u.y;
-          const float a1 = aux0 * rij * rfdn;
-          e[4] = fmaf(a1, srij, e[4]);
-          const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
-          const float aux3 = -a2 * fmaf(rij, 0.5f, r2);
-          A = fmaf(-a1, l.w, A);
-          B = fmaf(aux3, u.x, B);
-          a.w = fmaf(-a1, srt, a.w);
-          acb[mm] = fmaf(aux3, rft, acb[mm]);
-          de = fmaf(a2, rij, de);
-        }
-        fx = fmaf(de, dx, fx);
-        fy = fmaf(de, dy, fy);
-        fz = fmaf(de, dz, fz);
-        a.x = fmaf(-de, dx, a.x);
-        a.y = fmaf(-de, dy, a.y);
-        a.z = fmaf(-de, dz, a.z);
-        ac[mm] = a;
-        __syncwarp();
-      }
-    } else {
-      const int k0 = diag ? 1 : 0, k1 = diag ? 16 : 31;
-      for (int k = k0; k <= k1; ++k) {
-        const int mm = (lane + k) & 31;
-        const float4 h = sh[w][mm];
-        const int scode = __float_as_int(h.w);
-        if (iv && scode >= 0 && !(diag && k == 16 && lane >= 16)) {
-          const float4 l = sl[w][mm];
-          const int j = p.nsites + J * 32 + mm;
-          const bool smob = j >= m0;
-          const float dx = (th.x - h.x) + (tl.x - l.x);
-          const float dy = (th.y - h.y) + (tl.y - l.y);
-          const float dz = (th.z - h.z) + (tl.z - l.z);
-          const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          float dii = 0.0f, drf = 0.0f, dAs = 0.0f, dBs = 0.0f;
-          if (II && (tmob || smob)) {
-            if (EFP) {
-              dii = law32k(p, __ldg(p.pidx + row + (scode & 0xffff)), r2, 1.0f, e);
-            } else {
-              const float4 c = tab[row + (scode & 0xffff) - p.ndna];
-              const float ir = rsqrtf(r2), ir2 = ir * ir;
-              const float cofo = c.x * ir;
-              e[0] += cofo;
-              float d6 = c.z * ir2;
-              d6 = d6 * d6 * d6;
-              const float d12 = d6 * d6;
-              e[1] = fmaf(c.y, d12 - d6, e[1]);
-              dii = fmaf(cofo, ir2, (6.0f * c.y) * ir2 * fmaf(2.0f, d12, -d6));
-              const int cf = __float_as_int(c.w);
-              if ((cf & kSrp) && r2 <= p.rthf) dii += srpmf32(p, cf >> 4, r2, ir, 1.0f, e);
-            }
-          }
-          if (RF) {
-            const float4 sqv = sq[w][mm];
-            const int sb = __float_as_int(sqv.z);
-            if (i > j ? ((tb & 4) && (sb & 8)) : ((sb & 4) && (tb & 8))) {
-              const float rij = sqv.x * rft, srij = l.w * srt;
-              const float rfdn = rsqrtf(fmaf(rij, rij, r2));
-              const float aux0 = ct * sqv.y;
-              const float a1 = aux0 * rij * rfdn;
-              e[4] = fmaf(a1, srij, e[4]);
-              const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
-              const float aux3 = -a2 * fmaf(rij, 0.5f, r2);
-              A = fmaf(-a1, l.w, A);
-              B = fmaf(aux3, sqv.x, B);
-              dAs = -a1 * srt;
-              dBs = aux3 * rft;
-              drf = a2 * rij;
-            }
-          }
-          const float dt = (tmob ? dii : 0.0f) + drf, ds = (smob ? dii : 0.0f) + drf;
-          fx = fmaf(dt, dx, fx);
-          fy = fmaf(dt, dy, fy);
-          fz = fmaf(dt, dz, fz);
-          float4 a = acc[w][mm];
-          a.x = fmaf(-ds, dx, a.x);
-          a.y = fmaf(-ds, dy, a.y);
-          a.z = fmaf(-ds, dz, a.z);
-          a.w += dAs;
-          acc[w][mm] = a;
-          if (RF) accb[w][mm] += dBs;
-        }
-        __syncwarp();
-      }
-    }
-    // row side (lane l = row ion), column side (lane l = column ion)
-    float4 *o = p.tpf + (size_t)q * 64;
-    o[lane] = qforces && iv ? make_float4(fx, fy, fz, A) : make_float4(0.f, 0.f, 0.f, 0.f);
-    o[32 + lane] = qforces && jl < ntot ? acc[w][lane] : make_float4(0.f, 0.f, 0.f, 0.f);
-    if (RF) {
-      float *ob = p.tpb + (size_t)q * 64;
-      ob[lane] = qforces && iv ? B : 0.f;
-      ob[32 + lane] = qforces && jl < ntot ? accb[w][lane] : 0.f;
-    }
-  }
+  if (q < n3_pairs(T))  // warp-uniform
+    n3_tile<II, RF, EFP>(p, q, T, p.st->ntot, qforces, sh[w], sl[w], sq[w], acc[w], accb[w],
+                         tab, e);
   block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;

@@ -4,8 +4,8 @@
 // its attempts in one cooperative launch (k_grand).  The live particle count
 // stays on the device (DevState::ntot).
 #include <algorithm>
-#include <cuda/atomic>
 
+#include "gridsync.cuh"
 #include "launch.h"
 #include "physics.cuh"
 
@@ -281,7 +281,6 @@ void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
 // another block has given up, records kErrBarrier and the launch returns.
 // ---------------------------------------------------------------------------
 constexpr int kGrandThreads = 128;
-constexpr int kWaitSpins = 1 << 23;  // ~0.5-1 s of polling at most
 
 struct GrandState {
   Trial s;                  // current trial
@@ -315,34 +314,6 @@ struct Draws {
     return u01(w[n++ & 3]);
   }
 };
-
-// Bounded polls (thread 0 of a block), acquire ordering.
-__device__ bool wait_at_least(unsigned *ctr, unsigned target, DevState *st) {
-  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
-  volatile int *err = &st->err;
-  for (int spin = 0; a.load(cuda::memory_order_acquire) < target; ++spin) {
-    if (spin > kWaitSpins || ((spin & 1023) == 1023 && (*err & kErrBarrier))) {
-      atomicOr(&st->err, kErrBarrier);
-      return false;
-    }
-    __nanosleep(32);
-  }
-  return true;
-}
-
-__device__ __forceinline__ void release_add(unsigned *ctr, unsigned v) {
-  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
-  a.fetch_add(v, cuda::memory_order_release);
-}
-
-// Block-wide: thread 0 waits, everyone learns the outcome.
-__device__ bool block_wait(unsigned *ctr, unsigned target, DevState *st, int *flag) {
-  if (threadIdx.x == 0) *flag = wait_at_least(ctr, target, st) ? 1 : 0;
-  __syncthreads();
-  const bool ok = *flag != 0;
-  __syncthreads();
-  return ok;
-}
 
 // Proposal of one attempt (grand.f90:42-86): insertion point by rejection
 // sampling inside the buffer (insert.f90) or the rank-th ion of the buffer

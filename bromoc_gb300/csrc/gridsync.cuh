@@ -1,0 +1,62 @@
+// Bounded inter-block synchronisation for cooperative launches.  Every wait
+// gives up after kWaitSpins polls, or as soon as another block has given up;
+// it then records kErrBarrier in the device state and returns false, so the
+// launch ends and the host reads the error instead of a hung context.
+#pragma once
+#include <cuda/atomic>
+#include "common.cuh"
+
+namespace bgpu {
+
+constexpr int kWaitSpins = 1 << 23;  // ~0.5-1 s of polling at most
+
+// Thread 0 of a block: poll until *ctr >= target (acquire ordering).
+__device__ __forceinline__ bool wait_at_least(unsigned *ctr, unsigned target, DevState *st,
+                                              bool sleep = true) {
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
+  volatile int *err = &st->err;
+  for (int spin = 0; a.load(cuda::memory_order_acquire) < target; ++spin) {
+    if (spin > kWaitSpins || ((spin & 1023) == 1023 && (*err & kErrBarrier))) {
+      atomicOr(&st->err, kErrBarrier);
+      return false;
+    }
+    if (sleep) __nanosleep(32);
+  }
+  return true;
+}
+
+__device__ __forceinline__ void release_add(unsigned *ctr, unsigned v) {
+  cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
+  a.fetch_add(v, cuda::memory_order_release);
+}
+
+// Block-wide: thread 0 waits, everyone learns the outcome.
+__device__ __forceinline__ bool block_wait(unsigned *ctr, unsigned target, DevState *st,
+                                           int *flag) {
+  if (threadIdx.x == 0) *flag = wait_at_least(ctr, target, st) ? 1 : 0;
+  __syncthreads();
+  const bool ok = *flag != 0;
+  __syncthreads();
+  return ok;
+}
+
+// Grid-wide barrier number k (1, 2, ...) on a counter that starts the launch
+// at zero: each block arrives once, then waits for k * gridDim.x arrivals.
+// The fences make every write of the block before the barrier visible to
+// every block after it.  *flag: one shared int of the block.
+__device__ __forceinline__ bool grid_barrier(unsigned *ctr, unsigned k, DevState *st,
+                                             int *flag) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    release_add(ctr, 1u);
+    *flag = wait_at_least(ctr, k * gridDim.x, st, false) ? 1 : 0;
+    __threadfence();
+  }
+  __syncthreads();
+  // thread 0 rewrites *flag only after the next barrier's first
+  // __syncthreads, which every thread reaches after this read
+  return *flag != 0;
+}
+
+}  // namespace bgpu

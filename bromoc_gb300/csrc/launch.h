@@ -72,6 +72,13 @@ void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,
                      int do_bd, int variant, uint64_t seed, uint64_t step,
                      cudaStream_t stream);
 
+// loop.cu: nsteps fused BD steps of the FP32 Newton-3 path in one
+// cooperative launch (fields_first: evaluate the single-particle terms first)
+bool bd_loop_supported(const KP &p, const AssembleFlags &fl);
+cudaError_t launch_bd_loop(const KP &p, const AssembleFlags &fl, int ntot_ub, uint32_t mask,
+                           int variant, uint64_t seed, uint64_t step0, int nsteps,
+                           int fields_first, cudaStream_t stream);
+
 // gcmc.cu
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream);

@@ -1,0 +1,141 @@
+// Fused BD loop of the FP32 Newton-3 path: nsteps Brownian-dynamics steps
+// (dynamics0-3.mono.f90 driven by the ENERGY force of energy.mono.f90) in one
+// cooperative launch.  Per step, two phases separated by grid barriers:
+//
+//   P  every tile pair of ions (the Newton-3 pair tile, one warp each, spread
+//      round-robin over the blocks) -> per-tile-pair partial forces;
+//   A  one block per tile of 32 ions: sum the tile's partials in fixed order,
+//      add the single-particle forces, move the 32 ions, then evaluate the
+//      single-particle terms (maps, RFPAR gathers) at the new positions,
+//      which the next step's phase P reads.
+//
+// The force terms, their summation order and the noise are those of the
+// per-kernel step (fields, pair kernel, assembly), so the positions after a
+// call agree with the per-kernel path's.  Energies are not formed here; a
+// step whose energy is wanted runs per kernel.  Every barrier wait is
+// bounded (gridsync.cuh): a stalled launch records kErrBarrier and returns.
+#include <algorithm>
+
+#include "fields32.cuh"
+#include "gridsync.cuh"
+#include "launch.h"
+#include "move32.cuh"
+#include "pairs_n3.cuh"
+
+namespace bgpu {
+
+constexpr int kLoopWarps = 16;
+
+// Phase P's per-warp column arrays and phase A's partial sums share the
+// block's shared memory (the phases never overlap within a block).
+template <bool RF>
+union LoopSmem {
+  struct {
+    float4 sh[kLoopWarps][32], sl[kLoopWarps][32], sq[kLoopWarps][RF ? 32 : 1];
+    float4 acc[kLoopWarps][32];
+    float accb[kLoopWarps][RF ? 32 : 1];
+  } pr;
+  float part[kLoopWarps][10][32];
+};
+
+template <bool II, bool RF, bool EFP>
+__global__ void __launch_bounds__(32 * kLoopWarps, 1)
+    k_bd_loop(const __grid_constant__ KP p, AssembleFlags fl, uint32_t mask, int variant,
+              uint64_t seed, uint64_t step0, int nsteps, int fields_first) {
+  __shared__ LoopSmem<RF> sm;
+  __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
+  __shared__ int flag;
+  const int nt = p.nion_t;
+  if (II && !EFP)
+    for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
+  __syncthreads();
+  const int w = threadIdx.x >> 5;
+  const int G = gridDim.x;
+  // work slot of this warp: consecutive work items go to consecutive blocks
+  const int slot = w * G + blockIdx.x, nslot = G * kLoopWarps;
+  const int ntot = p.st->ntot;  // constant during BD
+  const int T = fl.ntile, npair = n3_pairs(T);
+  const int m0 = p.nsites + p.nfix;
+  unsigned bar = 0;
+  float eo[4];  // single-particle energies: not formed here
+  if (fields_first) {
+    for (int i = p.nsites + slot; i < ntot; i += nslot)
+      fields_one_f32(p, i, false, i < m0, mask, 1, eo);
+    if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
+  }
+  for (int s = 0; s < nsteps; ++s) {
+    float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int q = slot; q < npair; q += nslot)
+      n3_tile<II, RF, EFP>(p, q, T, ntot, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w],
+                           sm.pr.acc[w], sm.pr.accb[w], tab, e);
+    if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
+    for (int t = blockIdx.x; t < T; t += G) {
+      assemble_tile<kLoopWarps>(p, fl, 1, variant, seed, step0 + s, t, 0, sm.part);
+      __syncthreads();  // the tile's new positions; part free again
+      if (s + 1 < nsteps) {
+        const int i = p.nsites + 32 * t + w, i2 = i + kLoopWarps;
+        if (i < ntot) fields_one_f32(p, i, false, i < m0, mask, 1, eo);
+        if (i2 < ntot) fields_one_f32(p, i2, false, i2 < m0, mask, 1, eo);
+      }
+    }
+    if (s + 1 < nsteps && !grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
+  }
+}
+
+template <bool II, bool RF, bool EFP>
+static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t mask,
+                                 int variant, uint64_t seed, uint64_t step0, int nsteps,
+                                 int fields_first, cudaStream_t stream) {
+  static int max_res[64] = {};
+  int dev = 0;
+  cudaError_t e = cudaGetDevice(&dev);
+  if (e != cudaSuccess) return e;
+  if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
+  auto kern = k_bd_loop<II, RF, EFP>;
+  if (max_res[dev] == 0) {
+    int per_sm = 0, nsm = 0;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kLoopWarps, 0)) !=
+        cudaSuccess)
+      return e;
+    if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
+      return e;
+    // one block per SM at most: every block must be resident at once
+    max_res[dev] = per_sm > 0 ? nsm : -1;
+  }
+  if (max_res[dev] < 0) return cudaErrorCooperativeLaunchTooLarge;
+  const int T = fl.ntile;
+  const int grid = std::max(1, std::min(max_res[dev], std::max(n3_pairs(T), T)));
+  if ((e = cudaMemsetAsync(&p.st->bar_count, 0, sizeof(unsigned), stream)) != cudaSuccess)
+    return e;
+  KP pc = p;
+  AssembleFlags fc = fl;
+  void *args[] = {(void *)&pc, (void *)&fc, (void *)&mask, (void *)&variant,
+                  (void *)&seed, (void *)&step0, (void *)&nsteps, (void *)&fields_first};
+  return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(32 * kLoopWarps), args,
+                                     0, stream);
+}
+
+bool bd_loop_supported(const KP &p, const AssembleFlags &fl) {
+  return fl.fp32_partials && fl.ntile > 0 && !fl.use_total && p.nsites == 0 && !fl.is;
+}
+
+cudaError_t launch_bd_loop(const KP &p, const AssembleFlags &fl, int ntot_ub, uint32_t mask,
+                           int variant, uint64_t seed, uint64_t step0, int nsteps,
+                           int fields_first, cudaStream_t stream) {
+  const PairCfg32 pc = pair_cfg32(p, ntot_ub, mask);
+  const bool efp = !p.ipq_ok;
+  if (pc.ii && pc.rf)
+    return efp ? launch_loop_t<true, true, true>(p, fl, mask, variant, seed, step0, nsteps,
+                                                 fields_first, stream)
+               : launch_loop_t<true, true, false>(p, fl, mask, variant, seed, step0, nsteps,
+                                                  fields_first, stream);
+  if (pc.ii)
+    return efp ? launch_loop_t<true, false, true>(p, fl, mask, variant, seed, step0, nsteps,
+                                                  fields_first, stream)
+               : launch_loop_t<true, false, false>(p, fl, mask, variant, seed, step0, nsteps,
+                                                   fields_first, stream);
+  return launch_loop_t<false, true, true>(p, fl, mask, variant, seed, step0, nsteps,
+                                          fields_first, stream);
+}
+
+}  // namespace bgpu

@@ -322,9 +322,14 @@ enum {
   BROMOC_K_RFCROSS = 1,  /* RFPAR cross-term pair kernel                   */
   BROMOC_K_FIELDS = 2,   /* single-particle map/membrane kernel            */
   BROMOC_K_ASSEMBLE = 3, /* force assembly + BD update                     */
-  BROMOC_K_NKINDS = 4
+  BROMOC_K_LOOP = 4,     /* fused BD loop (all of the above, many steps)   */
+  BROMOC_K_NKINDS = 5
 };
 int bromoc_gpu_kernel_timing(bromoc_ctx *ctx, int32_t on);
+/* bd_steps in FP32 mode runs the steps of a system without sites as one
+ * cooperative launch (on = 1, the default) or one launch per kernel and
+ * step (on = 0); the trajectories agree.  No counterpart in the reference. */
+int bromoc_gpu_set_fused_bd(bromoc_ctx *ctx, int32_t on);
 /* total milliseconds and number of timed launches since timing was turned
  * on (synchronises the context's stream) */
 int bromoc_gpu_kernel_time(bromoc_ctx *ctx, int32_t which, double *total_ms,

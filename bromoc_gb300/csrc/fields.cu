@@ -259,12 +259,14 @@ __global__ void __launch_bounds__(32 * kFieldWarps)
     k_fields_warp_f32(const __grid_constant__ KP p, uint32_t mask, int qforces, int slot0) {
   __shared__ float red[kFieldWarps * 4];
   __shared__ float tot[4];
+  __shared__ AxisF ax[12];
+  stage_axes(p, ax);
   const int i = blockIdx.x * kFieldWarps + (threadIdx.x >> 5);
   const int ntot = p.st->ntot;
   float eo[4] = {0.0f, 0.0f, 0.0f, 0.0f};  // lane 0: ememb, egsbpa, evdwgd, erfpar
   if (i < ntot) {  // warp-uniform
     const bool site = i < p.nsites;
-    fields_one_f32(p, i, site, !site && i < p.nsites + p.nfix, mask, qforces, eo);
+    fields_one_f32(p, i, site, !site && i < p.nsites + p.nfix, mask, qforces, eo, ax);
   }
   block_sum_f<4>(eo, red, tot);
   if (threadIdx.x == 0) {
@@ -320,12 +322,14 @@ void launch_pack(const KP &p, int ntot_ub, bool to_records, cudaStream_t stream)
 __global__ void __launch_bounds__(32 * kFieldWarps)
     k_batch_fields(const __grid_constant__ KP p, const int *rep_of, const RepDev *rep,
                    float4 *pe, int nslots, uint32_t mask, int qforces) {
+  __shared__ AxisF ax[12];
+  stage_axes(p, ax);
   const int i = blockIdx.x * kFieldWarps + (threadIdx.x >> 5);
   if (i >= nslots) return;  // warp-uniform from here on
   const RepDev &R = rep[rep_of[i]];
   if (i - R.off >= R.n) return;
   float eo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
-  fields_one_f32(p, i, false, false, mask, qforces, eo);
+  fields_one_f32(p, i, false, false, mask, qforces, eo, ax);
   if ((threadIdx.x & 31) == 0) pe[i] = make_float4(eo[0], eo[1], eo[2], eo[3]);
 }
 

@@ -53,8 +53,18 @@ __device__ __forceinline__ size_t phiv_ifir(const KP &p, int i, int iontype) {
 
 // The FP32 field terms of particle i, one warp (lane 0 holds eo: ememb,
 // egsbpa, evdwgd, erfpar).  site / fixed: the particle's role.
+// The 12 axis records of the cell search, copied from the parameter block
+// into shared memory: every lane reads its own record, and divergent indexing
+// of the parameter block serialises.  Every thread of the block calls it.
+__device__ __forceinline__ void stage_axes(const KP &p, AxisF *ax) {
+  if (threadIdx.x < 12) ax[threadIdx.x] = p.f.ax[threadIdx.x];
+  __syncthreads();
+}
+
+// ax: the block's staged copy of p.f.ax (stage_axes).
 __device__ __forceinline__ void fields_one_f32(const KP &p, int i, bool site, bool fixed,
-                                               uint32_t mask, int qforces, float eo[4]) {
+                                               uint32_t mask, int qforces, float eo[4],
+                                               const AxisF *ax) {
   const int lane = threadIdx.x & 31;
   const float4 h4 = p.pk1[i], l4 = p.pk2[i];
   const float charge = p.pk3[i].y;
@@ -67,7 +77,7 @@ __device__ __forceinline__ void fields_one_f32(const KP &p, int i, bool site, bo
   int cix = 0, cin = 0;
   float cfr = 0.0f;
   if (lane < 12) {
-    const AxisF &A = p.f.ax[lane];
+    const AxisF &A = ax[lane];
     const int a = lane % 3;
     const float ph = a == 0 ? h4.x : (a == 1 ? h4.y : h4.z);
     const float pl = a == 0 ? l4.x : (a == 1 ? l4.y : l4.z);

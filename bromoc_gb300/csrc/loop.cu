@@ -4,10 +4,11 @@
 //
 //   P  every tile pair of ions (the Newton-3 pair tile, one warp each, spread
 //      round-robin over the blocks) -> per-tile-pair partial forces;
-//   A  one block per tile of 32 ions: sum the tile's partials in fixed order,
-//      add the single-particle forces, move the 32 ions, then evaluate the
+//   A  one block per half tile of 16 ions (whole tiles of 32 when the half
+//      tiles outnumber the blocks): sum the tile's partials in fixed order,
+//      add the single-particle forces, move the ions, then evaluate the
 //      single-particle terms (maps, RFPAR gathers) at the new positions,
-//      which the next step's phase P reads.
+//      one warp per ion, which the next step's phase P reads.
 //
 // The force terms, their summation order and the noise are those of the
 // per-kernel step (fields, pair kernel, assembly), so the positions after a
@@ -45,6 +46,8 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   __shared__ LoopSmem<RF> sm;
   __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
   __shared__ int flag;
+  __shared__ AxisF ax[12];
+  stage_axes(p, ax);
   const int nt = p.nion_t;
   if (II && !EFP)
     for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
@@ -58,9 +61,13 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   const int m0 = p.nsites + p.nfix;
   unsigned bar = 0;
   float eo[4];  // single-particle energies: not formed here
+  // phase A in half tiles (16 ions a block, one field evaluation a warp)
+  // while they fit the grid once, else whole tiles
+  const bool halves = 2 * T <= G;
+  const int nitem = halves ? 2 * T : T;
   if (fields_first) {
     for (int i = p.nsites + slot; i < ntot; i += nslot)
-      fields_one_f32(p, i, false, i < m0, mask, 1, eo);
+      fields_one_f32(p, i, false, i < m0, mask, 1, eo, ax);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
   }
   for (int s = 0; s < nsteps; ++s) {
@@ -69,13 +76,16 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
       n3_tile<II, RF, EFP>(p, q, T, ntot, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w],
                            sm.pr.acc[w], sm.pr.accb[w], tab, e);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
-    for (int t = blockIdx.x; t < T; t += G) {
-      assemble_tile<kLoopWarps>(p, fl, 1, variant, seed, step0 + s, t, 0, sm.part);
-      __syncthreads();  // the tile's new positions; part free again
+    for (int it = blockIdx.x; it < nitem; it += G) {
+      const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;
+      assemble_tile<kLoopWarps>(p, fl, 1, variant, seed, step0 + s, t, 0, sm.part, h);
+      __syncthreads();  // the new positions; part free again
       if (s + 1 < nsteps) {
-        const int i = p.nsites + 32 * t + w, i2 = i + kLoopWarps;
-        if (i < ntot) fields_one_f32(p, i, false, i < m0, mask, 1, eo);
-        if (i2 < ntot) fields_one_f32(p, i2, false, i2 < m0, mask, 1, eo);
+        const int base = p.nsites + 32 * t + (halves ? 16 * h : 0);
+        for (int u = w; u < (halves ? 16 : 32); u += kLoopWarps) {
+          const int i = base + u;
+          if (i < ntot) fields_one_f32(p, i, false, i < m0, mask, 1, eo, ax);
+        }
       }
     }
     if (s + 1 < nsteps && !grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;

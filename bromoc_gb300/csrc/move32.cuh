@@ -177,11 +177,14 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
 // compensated sums meet in shared memory in a fixed order; warp 0 then
 // assembles and moves its 32 particles, one lane each.  Inputs that another
 // block may have written in the same launch are read past L1.  blk: the tile
-// (site tiles are 0 .. site_blocks-1).  Every thread of the block calls it.
+// (site tiles are 0 .. site_blocks-1); half: -1 for the whole tile, else only
+// lanes 16 half .. 16 half + 15 assemble and move (two blocks share a tile).
+// Every thread of the block calls it.
 template <int NW>
 __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &fl, int do_bd,
                                               int variant, uint64_t seed, uint64_t step,
-                                              int blk, int site_blocks, float (*part)[10][32]) {
+                                              int blk, int site_blocks, float (*part)[10][32],
+                                              int half = -1) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool ionblk = blk >= site_blocks;
   const int Ti = blk - site_blocks;
@@ -233,7 +236,7 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &
       part[w][5 + k][lane] = c[k];
     }
   __syncthreads();
-  if (w != 0) return;
+  if (w != 0 || (half >= 0 && (lane >> 4) != half)) return;
   for (int ww = 1; ww < NW; ++ww)
 #pragma unroll
     for (int k = 0; k < 5; ++k) acc2p(s[k], c[k], part[ww][k][lane], part[ww][5 + k][lane]);

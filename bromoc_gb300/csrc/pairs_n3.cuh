@@ -5,6 +5,8 @@
 #include "launch.h"
 #include "physics.cuh"
 
+#include <cuda/std/type_traits>
+
 namespace bgpu {
 
 // ---------------------------------------------------------------------------
@@ -47,13 +49,17 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
   const bool diag = I == J;
   const int i = p.nsites + I * 32 + lane;
   jl = p.nsites + J * 32 + lane;
-  // column tile into shared memory (code -1 marks a slot past ntot)
+  // column tile into shared memory; its first ncol slots hold ions.  An
+  // empty slot sits 1e10 A away with zero charge, srfe and reff and the first
+  // ion type, so the branch-free path below can run over it with its law
+  // entry zeroed: every term it adds is then exactly zero.
+  const int ncol = min(32, max(0, ntot - (p.nsites + J * 32)));
   if (jl < ntot) {
     sh[lane] = __ldcg(p.pk1 + jl);
     sl[lane] = __ldcg(p.pk2 + jl);
     if (RF) sq[lane] = __ldcg(p.pk3 + jl);
   } else {
-    sh[lane] = make_float4(0.f, 0.f, 0.f, __int_as_float(-1));
+    sh[lane] = make_float4(1e10f, 1e10f, 1e10f, __int_as_float(EFP ? 0 : p.ndna));
     sl[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
     if (RF) sq[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
@@ -72,13 +78,17 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
   const int tb = __float_as_int(tq.z);
   const float srt = tl.w, rft = tq.x, ct = p.f.celec * tq.y;
   __syncwarp();
-  // Fast path: an off-diagonal tile pair whose 64 ions are all present and
-  // mobile (and, with RFPAR, all qualify for the cross term in both roles):
-  // no per-pair validity, mobility or role test.
-  bool lane_ok = iv && tmob && jl < ntot && jl >= m0;
-  if (RF) lane_ok = lane_ok && (tb & 12) == 12 && (__float_as_int(sq[lane].z) & 12) == 12;
+  // Fast path: an off-diagonal tile pair whose 32 row ions are present and
+  // whose ions are all mobile (and, with RFPAR, all qualify for the cross
+  // term in both roles): no per-pair validity, mobility or role test.  A
+  // column tile with empty slots (RAG) zeroes their law entries instead.
+  bool lane_ok = iv && tmob && (jl >= ntot || jl >= m0);
+  if (RF)
+    lane_ok = lane_ok && (tb & 12) == 12 &&
+              (jl >= ntot || (__float_as_int(sq[lane].z) & 12) == 12);
   const bool fast = II && !EFP && !diag && __all_sync(0xffffffffu, lane_ok);
-  if (fast) {
+  auto fast_loop = [&](auto rag) {
+    constexpr bool RAG = decltype(rag)::value;
     for (int k = 0; k < 32; ++k) {
       const int mm = (lane + k) & 31;
       float4 *ac = acc;
@@ -88,7 +98,8 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
       const float dy = (th.y - h.y) + (tl.y - l.y);
       const float dz = (th.z - h.z) + (tl.z - l.z);
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      const float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
+      float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
+      if (RAG && mm >= ncol) c = make_float4(0.f, 0.f, c.z, 0.f);
       const float ir = rsqrtf(r2), ir2 = ir * ir;
       const float cofo = c.x * ir;
       e[0] += cofo;
@@ -124,13 +135,19 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
       ac[mm] = a;
       __syncwarp();
     }
+  };
+  if (fast) {
+    if (ncol < 32)
+      fast_loop(cuda::std::true_type{});
+    else
+      fast_loop(cuda::std::false_type{});
   } else {
     const int k0 = diag ? 1 : 0, k1 = diag ? 16 : 31;
     for (int k = k0; k <= k1; ++k) {
       const int mm = (lane + k) & 31;
       const float4 h = sh[mm];
       const int scode = __float_as_int(h.w);
-      if (iv && scode >= 0 && !(diag && k == 16 && lane >= 16)) {
+      if (iv && mm < ncol && !(diag && k == 16 && lane >= 16)) {
         const float4 l = sl[mm];
         const int j = p.nsites + J * 32 + mm;
         const bool smob = j >= m0;

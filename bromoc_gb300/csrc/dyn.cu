@@ -213,7 +213,7 @@ __global__ void __launch_bounds__(32 * kAsmWarps)
   if (do_bd) bd_move_f32(p, variant, seed, step, i, F);
 }
 
-constexpr int kTileWarps = 8;
+constexpr int kTileWarps = 16;  // as the fused loop's phase A: the same sums
 
 __global__ void __launch_bounds__(32 * kTileWarps)
     k_assemble_tiles(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,

@@ -47,6 +47,7 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
   __shared__ int flag;
   __shared__ AxisF ax[12];
+  __shared__ float4 npos[32][2];  // phase A: the moved records of the tile
   stage_axes(p, ax);
   const int nt = p.nion_t;
   if (II && !EFP)
@@ -78,13 +79,13 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
     for (int it = blockIdx.x; it < nitem; it += G) {
       const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;
-      assemble_tile<kLoopWarps>(p, fl, 1, variant, seed, step0 + s, t, 0, sm.part, h);
+      assemble_tile<kLoopWarps>(p, fl, 1, variant, seed, step0 + s, t, 0, sm.part, h, npos);
       __syncthreads();  // the new positions; part free again
       if (s + 1 < nsteps) {
-        const int base = p.nsites + 32 * t + (halves ? 16 * h : 0);
-        for (int u = w; u < (halves ? 16 : 32); u += kLoopWarps) {
-          const int i = base + u;
-          if (i < ntot) fields_one_f32(p, i, false, i < m0, mask, 1, eo, ax);
+        const int u0 = halves ? 16 * h : 0;
+        for (int u = u0 + w; u < u0 + (halves ? 16 : 32); u += kLoopWarps) {
+          const int i = p.nsites + 32 * t + u;
+          if (i < ntot) fields_one_f32(p, i, false, i < m0, mask, 1, eo, ax, npos[u]);
         }
       }
     }

@@ -109,14 +109,39 @@ __device__ __forceinline__ void diff_model(const KP &p, int variant, int i, int 
 // their diffusion profile in FP64 (options off the hot path); variant 0 and
 // everything else stay on the FP32 pipe.
 // ---------------------------------------------------------------------------
-__device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t seed,
-                                            uint64_t step, int i, const float F[3]) {
+// What one particle's FP32 move needs besides its force: its position
+// records, ion type, diffusion factors and noise.  None depends on the
+// force, so the assembly gathers them before it sums the force.
+struct MoveIn {
+  float4 h4, l4;  // position hi / lo records
+  float g[3];     // Gaussian noise of this step
+  float2 fa;      // (fact1, fact2) of dynamics0
+  int itype;      // ion type, 0 for a site
+  bool moves;     // false for fixed ions and frozen sites
+};
+
+// The loaded part (the types and factors do not change during BD and come
+// through the read-only path); noise: whether to draw the noise here too.
+__device__ __forceinline__ MoveIn move_in_f32(const KP &p, int variant, uint64_t seed,
+                                              uint64_t step, int i, bool noise = true) {
+  MoveIn m;
   const int m0 = p.nsites + p.nfix;
-  if (i < m0 && (i >= p.nsites || !p.stfree[i])) return;  // fixed ions, frozen sites
-  float4 h4 = p.pk1[i], l4 = p.pk2[i];
-  float h[3] = {h4.x, h4.y, h4.z}, l[3] = {l4.x, l4.y, l4.z};
-  float g[3];
-  bd_noise3_f(seed, step, (uint32_t)i, g);
+  m.moves = !(i < m0 && (i >= p.nsites || !p.stfree[i]));
+  m.h4 = p.pk1[i];
+  m.l4 = p.pk2[i];
+  m.itype = i < p.nsites ? 0 : abs(__ldg(p.typei + i));
+  m.fa = variant == 0 && i >= p.nsites ? __ldg(p.fact_f + m.itype) : make_float2(0.f, 0.f);
+  if (noise) bd_noise3_f(seed, step, (uint32_t)i, m.g);
+  return m;
+}
+
+// The move itself; m.h4 / m.l4 become the new records, also stored to
+// pk1 / pk2.
+__device__ __forceinline__ void bd_move_f32(const KP &p, int variant, int i, const float F[3],
+                                            MoveIn &m) {
+  if (!m.moves) return;
+  float h[3] = {m.h4.x, m.h4.y, m.h4.z}, l[3] = {m.l4.x, m.l4.y, m.l4.z};
+  const float *g = m.g;
   if (i < p.nsites) {  // dynamics0nuc.f90:31-44
     for (int k = 0; k < 3; ++k) {
       float d = F[k] * p.f.fact0n1;
@@ -125,12 +150,11 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
     }
     if (!p.qdnafree) fixcoor_ff(p.f.box, h, l);
   } else {
-    const int itype = abs(p.typei[i]);
+    const int itype = m.itype;
     float fact1, fact2, dD[3] = {0.0f, 0.0f, 0.0f};
     if (variant == 0) {
-      const float2 fa = p.fact_f[itype];
-      fact1 = fa.x;
-      fact2 = fa.y;
+      fact1 = m.fa.x;
+      fact2 = m.fa.y;
     } else {
       double f1, f2, dd[3];
       diff_model(p, variant, i, itype, (double)h[2] + (double)l[2], f1, f2, dd);
@@ -160,14 +184,20 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
     }
     fixcoor_ff(p.f.box, h, l);
   }
-  h4.x = h[0];
-  h4.y = h[1];
-  h4.z = h[2];
-  l4.x = l[0];
-  l4.y = l[1];
-  l4.z = l[2];
-  p.pk1[i] = h4;
-  p.pk2[i] = l4;
+  m.h4.x = h[0];
+  m.h4.y = h[1];
+  m.h4.z = h[2];
+  m.l4.x = l[0];
+  m.l4.y = l[1];
+  m.l4.z = l[2];
+  p.pk1[i] = m.h4;
+  p.pk2[i] = m.l4;
+}
+
+__device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t seed,
+                                            uint64_t step, int i, const float F[3]) {
+  MoveIn m = move_in_f32(p, variant, seed, step, i);
+  bd_move_f32(p, variant, i, F, m);
 }
 
 // FP32 assembly for the Newton-3 partials: one block of NW warps per tile of
@@ -179,18 +209,49 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
 // block may have written in the same launch are read past L1.  blk: the tile
 // (site tiles are 0 .. site_blocks-1); half: -1 for the whole tile, else only
 // lanes 16 half .. 16 half + 15 assemble and move (two blocks share a tile).
-// Every thread of the block calls it.
+// Warp 1 draws their noise while warp 0 gathers their other inputs.
+// npos: when given, warp 0 leaves each of those particles' records there
+// (npos[lane] = {hi, lo}, after the move).  Every thread of the block calls it.
 template <int NW>
 __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &fl, int do_bd,
                                               int variant, uint64_t seed, uint64_t step,
                                               int blk, int site_blocks, float (*part)[10][32],
-                                              int half = -1) {
+                                              int half = -1, float4 (*npos)[2] = nullptr) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool ionblk = blk >= site_blocks;
   const int Ti = blk - site_blocks;
   const int i = ionblk ? p.nsites + 32 * Ti + lane : 32 * blk + lane;
   const int ntot = p.st->ntot;
   float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  // warp 0: the particle's own inputs, loaded while the partials are summed
+  const bool own = w == 0 && (half < 0 || (lane >> 4) == half) && i < ntot &&
+                   (ionblk || i < p.nsites);
+  MoveIn mv{};
+  float fo[3] = {0.f, 0.f, 0.f}, fs[3] = {0.f, 0.f, 0.f};
+  float4 d1 = make_float4(0.f, 0.f, 0.f, 0.f), d2 = d1;
+  // warp 1 draws the noise of warp 0's particles meanwhile, into part[0]
+  // (warp 0 keeps no partials there)
+  if (w == 1 && do_bd && (half < 0 || (lane >> 4) == half) && i < ntot &&
+      (ionblk || i < p.nsites)) {
+    float g[3];
+    bd_noise3_f(seed, step, (uint32_t)i, g);
+    part[0][0][lane] = g[0];
+    part[0][1][lane] = g[1];
+    part[0][2][lane] = g[2];
+  }
+  if (own) {
+    const int cap = p.cap;
+#pragma unroll
+    for (int k = 0; k < 3; ++k) {
+      fo[k] = __ldcg(p.ffield_f + k * cap + i);
+      if (fl.is) fs[k] = __ldcg(p.fis_f + k * cap + i);
+    }
+    if (fl.rf_ab && ionblk) {
+      d1 = __ldcg(p.rfd + 2 * (size_t)i);
+      d2 = __ldcg(p.rfd + 2 * (size_t)i + 1);
+    }
+    if (do_bd) mv = move_in_f32(p, variant, seed, step, i, NW < 2);
+  }
   if (ionblk) {
     const int T = fl.ntile;
     for (int u0 = w; u0 < T; u0 += 4 * NW) {
@@ -236,20 +297,17 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &
       part[w][5 + k][lane] = c[k];
     }
   __syncthreads();
-  if (w != 0 || (half >= 0 && (lane >> 4) != half)) return;
+  if (!own) return;
   for (int ww = 1; ww < NW; ++ww)
 #pragma unroll
     for (int k = 0; k < 5; ++k) acc2p(s[k], c[k], part[ww][k][lane], part[ww][5 + k][lane]);
-  if (i >= ntot || (!ionblk && i >= p.nsites)) return;
-  const int cap = p.cap;
 #pragma unroll
   for (int k = 0; k < 3; ++k) {
-    acc2(s[k], c[k], __ldcg(p.ffield_f + k * cap + i));
-    if (fl.is) acc2(s[k], c[k], __ldcg(p.fis_f + k * cap + i));
+    acc2(s[k], c[k], fo[k]);
+    if (fl.is) acc2(s[k], c[k], fs[k]);
   }
   if (fl.rf_ab && ionblk) {  // A sd1 + B sd2 of the cross term, rfpar.f90:177-223
     const float A = s[3] + c[3], B = s[4] + c[4];
-    const float4 d1 = __ldcg(p.rfd + 2 * (size_t)i), d2 = __ldcg(p.rfd + 2 * (size_t)i + 1);
     acc2(s[0], c[0], fmaf(A, d1.x, B * d2.x));
     acc2(s[1], c[1], fmaf(A, d1.y, B * d2.y));
     acc2(s[2], c[2], fmaf(A, d1.z, B * d2.z));
@@ -263,7 +321,16 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &
     p.fz[i] = F[2];
     return;
   }
-  bd_move_f32(p, variant, seed, step, i, F);
+  if (NW >= 2) {
+    mv.g[0] = part[0][0][lane];
+    mv.g[1] = part[0][1][lane];
+    mv.g[2] = part[0][2][lane];
+  }
+  bd_move_f32(p, variant, i, F, mv);
+  if (npos) {
+    npos[lane][0] = mv.h4;
+    npos[lane][1] = mv.l4;
+  }
 }
 
 }  // namespace bgpu

@@ -377,7 +377,7 @@ def run_gpu(args, rank, world, local_rank):
     nfix = spec.nsites + spec.nfix
 
     def step(cyc):
-        eng.grand(NGCMC, SEED, cyc)
+        eng.grand(NGCMC, SEED, cyc, dener=False)
         eng.bd_steps(NBD, SEED, (cyc - 1) * NBD, energies=False)
 
     for c in range(1, args.warmup + 1):

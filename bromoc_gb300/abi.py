@@ -310,11 +310,13 @@ class Engine:
                   "bd_steps")
         return dict(zip(TERM_NAMES, e.tolist())) if energies else None
 
-    def grand(self, ngcmc, seed, cycle, terms=M_ALL):
+    def grand(self, ngcmc, seed, cycle, terms=M_ALL, dener=True):
+        """ngcmc GCMC attempts; with dener, waits for them and returns the
+        sum of the attempts' energy changes (else returns None at once)."""
         d = C.c_double(0.0)
         self._chk(self._fn("grand")(self.h, terms, ngcmc, seed, cycle,
-                                    C.byref(d)), "grand")
-        return d.value
+                                    C.byref(d) if dener else None), "grand")
+        return d.value if dener else None
 
     def get_buffers(self):
         nb = self.nbuffer

@@ -1,20 +1,21 @@
 // Replica batches on the device (scope-table configuration C4): many
-// independent systems of uneven size advance together, two launches per BD
-// step for the whole batch.
+// independent systems of uneven size advance together, three launches per
+// BD step for the whole batch.
 //
 //   k_batch_fields (fields.cu): the FP32 field terms of every live slot.
-//   k_batch_rows:  one warp owns 32 ions of one replica and sweeps every
-//                  ion of that replica, 32 at a time through shared memory;
-//                  its forces (ion-ion laws + RFPAR cross term) complete in
-//                  registers, so the warp then assembles them and makes the
-//                  BD move (dynamics0) at once, writing the other position
-//                  buffer so that no warp reads a moved source.
+//   k_batch_pairs: every tile pair of every replica, one warp each, through
+//                  the Newton-3 pair tile of the single-system kernels
+//                  (pairs_n3.cuh) on that replica's slots; partial forces
+//                  per tile pair into the replica's stretch of the buffers.
+//   k_batch_asm:   one block per tile of 32 ions of one replica: the tile
+//                  assembly and dynamics0 move of the single-system path
+//                  (move32.cuh) with the replica's box and noise key, in
+//                  place (the pair launch has finished reading positions).
 //
-// Each unordered pair is evaluated by both of its ions (no partial buffers,
-// no reduction pass).  Work items (replica, row tile) are sorted longest
-// first for load balance.  Replica r draws its noise from seed_r with the
-// same counters as a single context, so a batch replica follows the
-// trajectory of bromoc_gpu_bd_steps with that seed.
+// A replica's particles, partial sums and moves are exactly those of a
+// single context holding that replica (same summation order, noise drawn
+// from the replica's seed with the single context's counters), so a batch
+// replica follows the trajectory of bromoc_gpu_bd_steps bit for bit.
 #include <algorithm>
 #include <cstdarg>
 #include <cstdio>
@@ -26,104 +27,39 @@
 #include "batch.cuh"
 #include "ff.cuh"
 #include "launch.h"
+#include "move32.cuh"
+#include "pairs_n3.cuh"
 #include "physics.cuh"
 
 namespace bgpu {
 
-constexpr int kRowWarps = 4;
+constexpr int kPairWarps = 4;   // tile pairs per block of k_batch_pairs
+constexpr int kAsmTileWarps = 16;  // as the single-system tile assembly
 
-// Energies of one row warp: ecoul, elj, esrpmf, eefpot (ion-ion, each pair
-// half from either side) and the RFPAR cross energy.
+// Energies of one tile pair: ecoul, elj, esrpmf, eefpot, RFPAR cross.
 constexpr int kRowTerms = 5;
 
-template <bool RF, bool BD>
-__global__ void __launch_bounds__(32 * kRowWarps)
-    k_batch_rows(const __grid_constant__ KP p, const RepDev *rep, const int2 *work,
-                 int nwork, float4 *pk1n, float4 *pk2n, float *wpart, uint64_t step,
-                 int qforces, double *fout) {
-  __shared__ float4 sh[kRowWarps][32], sl[kRowWarps][32], sq[kRowWarps][RF ? 32 : 1];
+template <bool RF>
+__global__ void __launch_bounds__(32 * kPairWarps)
+    k_batch_pairs(const __grid_constant__ KP p, const RepDev *rep, const int2 *work, int nwork,
+                  float4 *tpf, float *tpb, float *wpart) {
+  __shared__ float4 sh[kPairWarps][32], sl[kPairWarps][32], sq[kPairWarps][RF ? 32 : 1];
+  __shared__ float4 acc[kPairWarps][32];
+  __shared__ float accb[kPairWarps][RF ? 32 : 1];
   __shared__ float4 tab[kIonTabTypes * kIonTabTypes];
   const int nt = p.nion_t;
   for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int widx = blockIdx.x * kRowWarps + w;
+  const int widx = blockIdx.x * kPairWarps + w;
   if (widx >= nwork) return;  // no block-wide barrier follows
   const int2 wk = work[widx];
   const RepDev &R = rep[wk.x];
-  const int off = R.off, n = R.n, I = wk.y, T = (n + 31) >> 5;
-  const int il = I * 32 + lane;
-  const bool iv = il < n;
-  const int i = off + il;
-  float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th, tq = th;
-  if (iv) {
-    th = p.pk1[i];
-    tl = p.pk2[i];
-    if (RF) tq = p.pk3[i];
-  }
-  const int row = ((__float_as_int(th.w) & 0xffff) - p.ndna) * nt;
-  const int tb = __float_as_int(tq.z);
-  const float srt = tl.w, rft = tq.x, ct = p.f.celec * tq.y;
-  float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const PairSys ps{p.pk1 + R.off, p.pk2 + R.off, p.pk3 + R.off, tpf + (size_t)R.poff * 64,
+                   tpb + (size_t)R.poff * 64, 0, 0, R.n, (R.n + 31) >> 5};
   float e[kRowTerms] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  for (int J = 0; J < T; ++J) {
-    const int jl = J * 32 + lane;
-    __syncwarp();
-    if (jl < n) {
-      sh[w][lane] = p.pk1[off + jl];
-      sl[w][lane] = p.pk2[off + jl];
-      if (RF) sq[w][lane] = p.pk3[off + jl];
-    }
-    __syncwarp();
-    const int cnt = min(32, n - J * 32);
-    float fx = 0.f, fy = 0.f, fz = 0.f, A = 0.f, B = 0.f;
-    if (iv) {
-      for (int k = 0; k < cnt; ++k) {
-        if (J == I && k == lane) continue;
-        const float4 h = sh[w][k], l = sl[w][k];
-        const float dx = (th.x - h.x) + (tl.x - l.x);
-        const float dy = (th.y - h.y) + (tl.y - l.y);
-        const float dz = (th.z - h.z) + (tl.z - l.z);
-        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-        const float4 q = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
-        const float ir = rsqrtf(r2), ir2 = ir * ir;
-        const float cofo = q.x * ir;
-        e[0] = fmaf(0.5f, cofo, e[0]);
-        float d6 = q.z * ir2;
-        d6 = d6 * d6 * d6;
-        const float d12 = d6 * d6;
-        e[1] = fmaf(0.5f * q.y, d12 - d6, e[1]);
-        float de = fmaf(cofo, ir2, (6.0f * q.y) * ir2 * fmaf(2.0f, d12, -d6));
-        const int qf = __float_as_int(q.w);
-        if ((qf & kSrp) && r2 <= p.rthf) de += srpmf32(p, qf >> 4, r2, ir, 0.5f, e);
-        if (RF) {
-          const float4 u = sq[w][k];
-          const int sb = __float_as_int(u.z);
-          const bool t_is_i = il > J * 32 + k;
-          if (t_is_i ? ((tb & 4) && (sb & 8)) : ((sb & 4) && (tb & 8))) {
-            const float rij = u.x * rft, srij = l.w * srt;
-            const float rfdn = rsqrtf(fmaf(rij, rij, r2));
-            const float aux0 = ct * u.y;
-            const float a1 = aux0 * rij * rfdn;
-            if (t_is_i) e[4] = fmaf(a1, srij, e[4]);
-            const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
-            A = fmaf(-a1, l.w, A);
-            B = fmaf(-a2 * fmaf(rij, 0.5f, r2), u.x, B);
-            de = fmaf(a2, rij, de);
-          }
-        }
-        fx = fmaf(de, dx, fx);
-        fy = fmaf(de, dy, fy);
-        fz = fmaf(de, dz, fz);
-      }
-    }
-    acc2(s[0], c[0], fx);
-    acc2(s[1], c[1], fy);
-    acc2(s[2], c[2], fz);
-    acc2(s[3], c[3], A);
-    acc2(s[4], c[4], B);
-  }
-  // row energies -> this work item's slot (fixed shuffle tree)
+  n3_tile<true, RF, false>(p, ps, wk.y, 1, sh[w], sl[w], sq[w], acc[w], accb[w], tab, e);
+  // the tile pair's energies -> its slot (fixed shuffle tree)
 #pragma unroll
   for (int k = 0; k < kRowTerms; ++k) {
     float v = e[k];
@@ -131,38 +67,29 @@ __global__ void __launch_bounds__(32 * kRowWarps)
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
     if (lane == 0) wpart[(size_t)widx * kRowTerms + k] = v;
   }
-  if (!iv) return;
-  const int cap = p.cap;
-#pragma unroll
-  for (int k = 0; k < 3; ++k) acc2(s[k], c[k], p.ffield_f[k * cap + i]);
-  if (RF) {  // A sd1 + B sd2 of the cross term (rfpar.f90:177-223)
-    const float Av = s[3] + c[3], Bv = s[4] + c[4];
-    const float4 d1 = p.rfd[2 * (size_t)i], d2 = p.rfd[2 * (size_t)i + 1];
-    acc2(s[0], c[0], fmaf(Av, d1.x, Bv * d2.x));
-    acc2(s[1], c[1], fmaf(Av, d1.y, Bv * d2.y));
-    acc2(s[2], c[2], fmaf(Av, d1.z, Bv * d2.z));
-  }
-  const float F[3] = {s[0] + c[0], s[1] + c[1], s[2] + c[2]};
-  if (!qforces) return;
-  if (!BD) {
-    if (fout)
-      for (int k = 0; k < 3; ++k) fout[3 * (size_t)i + k] = F[k];
-    return;
-  }
-  // dynamics0.mono.f90:31-46 on float-float positions
-  const float2 fa = p.fact_f[abs(p.typei[i])];
-  float g[3];
-  bd_noise3_f(R.seed, step, (uint32_t)il, g);
-  float hh[3] = {th.x, th.y, th.z}, ll[3] = {tl.x, tl.y, tl.z};
-#pragma unroll
-  for (int k = 0; k < 3; ++k) {
-    float d = F[k] * fa.x;
-    clamp_f(p.f.bdmax, d);
-    ff_add(hh[k], ll[k], fmaf(fa.y, g[k], d));
-  }
-  fixcoor_ff(R.box, hh, ll);
-  pk1n[i] = make_float4(hh[0], hh[1], hh[2], th.w);
-  pk2n[i] = make_float4(ll[0], ll[1], ll[2], 0.0f);
+}
+
+// One block per (replica, tile): the tile assembly and move of the single
+// system path on the replica's slots; fout (if not moving): 3 doubles per
+// slot.
+template <bool RF>
+__global__ void __launch_bounds__(32 * kAsmTileWarps)
+    k_batch_asm(const __grid_constant__ KP p, const RepDev *rep, const int2 *tiles,
+                const float4 *tpf, const float *tpb, int do_bd, uint64_t step, double *fout) {
+  __shared__ float part[kAsmTileWarps][10][32];
+  const int2 tk = tiles[blockIdx.x];
+  const RepDev &R = rep[tk.x];
+  const size_t o = R.off;
+  const AsmSys ms{p.pk1 + o, p.pk2 + o, p.typei + o, p.ffield_f + o, nullptr, p.rfd + 2 * o,
+                  tpf + (size_t)R.poff * 64, tpb + (size_t)R.poff * 64, p.cap, 0, 0, R.n,
+                  (R.n + 31) >> 5, R.seed, &R.box,
+                  fout ? fout + 3 * o : nullptr, fout ? fout + 3 * o + 1 : nullptr,
+                  fout ? fout + 3 * o + 2 : nullptr, 3};
+  AssembleFlags fl{};
+  fl.fp32_partials = 1;
+  fl.ntile = ms.T;
+  fl.rf_ab = RF;
+  assemble_tile<kAsmTileWarps>(p, ms, fl, do_bd, 0, step, tk.y, 0, part);
 }
 
 // Per-replica ENERGY terms (energy.mono.f90 slots) from the field terms of
@@ -210,7 +137,7 @@ struct bromoc_batch {
   KP kp{};                     // prototype's parameter block, batch arrays swapped in
   cudaStream_t stream = nullptr;
   std::string err;
-  int nrep = 0, nslots = 0, nwork = 0, cur = 0;
+  int nrep = 0, nslots = 0, nwork = 0, cur = 0;  // cur: always 0 (moves are in place)
   std::vector<int> cap, off, n;
   std::vector<RepDev> rep_h;   // host copy of the replica records
   std::vector<int> nwtype_h;   // [ntype+1] ion type -> combined type
@@ -219,7 +146,11 @@ struct bromoc_batch {
   // device
   RepDev *rep = nullptr;
   int *rep_of = nullptr;
-  int2 *work = nullptr;
+  int2 *work = nullptr;    // (replica, tile pair), replica by replica
+  int2 *tiles = nullptr;   // (replica, tile)
+  int ntiles = 0, ntile_cap = 0;
+  float4 *tpf = nullptr;   // per-tile-pair partials, replica r from poff_r * 64
+  float *tpb = nullptr;
   float4 *pk1[2] = {nullptr, nullptr}, *pk2[2] = {nullptr, nullptr};
   float4 *pe = nullptr;
   float *wpart = nullptr;
@@ -264,19 +195,16 @@ void split(double v, float &h, float &l) {
   l = (float)(v - (double)h);
 }
 
-// work items (replica, row tile), longest rows first; each replica's items
-// stay contiguous (w0, w1)
+// work items: every tile pair (replica, q) and every tile (replica, t) of the
+// live particles, replica by replica; w0, w1 bound each replica's tile pairs
 int rebuild_work(bromoc_batch *b) {
-  std::vector<int> order(b->nrep);
-  for (int r = 0; r < b->nrep; ++r) order[r] = r;
-  std::stable_sort(order.begin(), order.end(),
-                   [&](int a, int c) { return b->n[a] > b->n[c]; });
-  std::vector<int2> items;
-  for (int r : order) {
+  std::vector<int2> items, tiles;
+  for (int r = 0; r < b->nrep; ++r) {
     const int T = (b->n[r] + 31) / 32;
     b->rep_h[r].w0 = (int)items.size();
-    for (int I = 0; I < T; ++I) items.push_back(make_int2(r, I));
+    for (int q = 0; q < n3_pairs(T); ++q) items.push_back(make_int2(r, q));
     b->rep_h[r].w1 = (int)items.size();
+    for (int t = 0; t < T; ++t) tiles.push_back(make_int2(r, t));
   }
   if ((int)items.size() > b->nwork) {
     if (b->work) cudaFree(b->work);
@@ -287,29 +215,44 @@ int rebuild_work(bromoc_batch *b) {
     BCU(cudaMalloc((void **)&b->wpart, items.size() * kRowTerms * sizeof(float)));
   }
   b->nwork = (int)items.size();
+  if ((int)tiles.size() > b->ntile_cap) {
+    if (b->tiles) cudaFree(b->tiles);
+    b->tiles = nullptr;
+    BCU(cudaMalloc((void **)&b->tiles, tiles.size() * sizeof(int2)));
+    b->ntile_cap = (int)tiles.size();
+  }
+  b->ntiles = (int)tiles.size();
   if (!items.empty())
     BCU(cudaMemcpy(b->work, items.data(), items.size() * sizeof(int2), cudaMemcpyHostToDevice));
+  if (!tiles.empty())
+    BCU(cudaMemcpy(b->tiles, tiles.data(), tiles.size() * sizeof(int2), cudaMemcpyHostToDevice));
   BCU(cudaMemcpy(b->rep, b->rep_h.data(), b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice));
   return BROMOC_OK;
 }
 
-// The pair + BD launch of one step.
-void launch_rows(bromoc_batch *b, const KP &p, bool rf, bool bd, float4 *pk1n, float4 *pk2n,
-                 uint64_t step, double *fout) {
-  const int nb = (b->nwork + kRowWarps - 1) / kRowWarps;
-  const dim3 g(nb), blk(32 * kRowWarps);
-  if (rf && bd)
-    k_batch_rows<true, true><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n, pk2n,
-                                                       b->wpart, step, 1, fout);
-  else if (rf)
-    k_batch_rows<true, false><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n,
-                                                        pk2n, b->wpart, step, 1, fout);
-  else if (bd)
-    k_batch_rows<false, true><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n,
-                                                        pk2n, b->wpart, step, 1, fout);
-  else
-    k_batch_rows<false, false><<<g, blk, 0, b->stream>>>(p, b->rep, b->work, b->nwork, pk1n,
-                                                         pk2n, b->wpart, step, 1, fout);
+// The pair and assembly launches of one step (do_bd: move, else forces
+// into fout if given).
+void launch_pairs_asm(bromoc_batch *b, const KP &p, bool rf, int do_bd, uint64_t step,
+                      double *fout) {
+  const int nb = (b->nwork + kPairWarps - 1) / kPairWarps;
+  if (nb > 0) {
+    if (rf)
+      k_batch_pairs<true><<<nb, 32 * kPairWarps, 0, b->stream>>>(p, b->rep, b->work, b->nwork,
+                                                                 b->tpf, b->tpb, b->wpart);
+    else
+      k_batch_pairs<false><<<nb, 32 * kPairWarps, 0, b->stream>>>(p, b->rep, b->work, b->nwork,
+                                                                  b->tpf, b->tpb, b->wpart);
+    b->launches += 1;
+  }
+  if (b->ntiles > 0) {
+    if (rf)
+      k_batch_asm<true><<<b->ntiles, 32 * kAsmTileWarps, 0, b->stream>>>(
+          p, b->rep, b->tiles, b->tpf, b->tpb, do_bd, step, fout);
+    else
+      k_batch_asm<false><<<b->ntiles, 32 * kAsmTileWarps, 0, b->stream>>>(
+          p, b->rep, b->tiles, b->tpf, b->tpb, do_bd, step, fout);
+    b->launches += 1;
+  }
 }
 
 }  // namespace
@@ -339,6 +282,7 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   b->n.assign(nrep, 0);
   b->rep_h.assign(nrep, RepDev{});
   int slots = 0;
+  size_t npair = 0;
   for (int r = 0; r < nrep; ++r) {
     if (capacity[r] < 1) {
       delete b;
@@ -348,17 +292,17 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
     b->cap[r] = capacity[r];
     b->rep_h[r].off = slots;
     b->rep_h[r].cap = capacity[r];
+    b->rep_h[r].poff = (int)npair;
     slots += (capacity[r] + 31) / 32 * 32;  // replicas start on tile boundaries
+    npair += n3_pairs((capacity[r] + 31) / 32);
   }
   b->nslots = slots;
   KP &p = b->kp;
   const size_t ns = slots;
   rc = balloc(b, &b->rep, nrep);
   if (!rc) rc = balloc(b, &b->rep_of, ns);
-  for (int k = 0; k < 2 && !rc; ++k) {
-    rc = balloc(b, &b->pk1[k], ns);
-    if (!rc) rc = balloc(b, &b->pk2[k], ns);
-  }
+  if (!rc) rc = balloc(b, &b->pk1[0], ns);
+  if (!rc) rc = balloc(b, &b->pk2[0], ns);
   float4 *pk3 = nullptr, *rfd = nullptr;
   float *ffield = nullptr;
   int *typei = nullptr;
@@ -369,6 +313,8 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   if (!rc) rc = balloc(b, &typei, ns);
   if (!rc) rc = balloc(b, &b->pe, ns);
   if (!rc) rc = balloc(b, &b->eterms, (size_t)nrep * kNTerms);
+  if (!rc) rc = balloc(b, &b->tpf, npair * 64);
+  if (!rc) rc = balloc(b, &b->tpb, npair * 64);
   if (!rc) rc = balloc(b, &st, 1);
   if (!rc && cudaMallocHost((void **)&b->rep_pinned, nrep * sizeof(RepDev)) != cudaSuccess)
     rc = bset(b, BROMOC_E_NOMEM, "batch: pinned replica records");
@@ -400,6 +346,7 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   p.ffield_f = ffield;
   p.typei = typei;
   p.qproxdiff = 0;
+  p.qcountion = 0;  // no crossing counters in a batch
   int *warn = nullptr;
   if (balloc(b, &warn, p.nttyp + 1) == BROMOC_OK) cudaMemset(warn, 0, (p.nttyp + 1) * sizeof(int));
   p.warn = warn;
@@ -422,6 +369,7 @@ int bromoc_batch_destroy(bromoc_batch *b) {
   for (void *a : b->allocs) cudaFree(a);
   if (b->work) cudaFree(b->work);
   if (b->wpart) cudaFree(b->wpart);
+  if (b->tiles) cudaFree(b->tiles);
   if (b->rep_pinned) cudaFreeHost(b->rep_pinned);
   delete b;
   return BROMOC_OK;
@@ -537,16 +485,13 @@ int bromoc_batch_bd_steps(bromoc_batch *b, uint32_t terms, int32_t nsteps, const
   BCU(cudaMemcpyAsync(b->rep, b->rep_pinned, b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice,
                       b->stream));
   const bool rf = (terms & BROMOC_M_RFPAR) && b->kp.qrfpar;
-  const int nb = (b->nwork + kRowWarps - 1) / kRowWarps;
+  KP p = b->kp;
+  p.pk1 = b->pk1[b->cur];
+  p.pk2 = b->pk2[b->cur];
   for (int k = 0; k < nsteps; ++k) {
-    KP p = b->kp;
-    p.pk1 = b->pk1[b->cur];
-    p.pk2 = b->pk2[b->cur];
-    const int nx = b->cur ^ 1;
     launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
-    if (nb > 0) launch_rows(b, p, rf, true, b->pk1[nx], b->pk2[nx], step0 + k, nullptr);
-    b->launches += 1 + (nb > 0);
-    b->cur = nx;
+    b->launches += 1;
+    launch_pairs_asm(b, p, rf, 1, step0 + k, nullptr);
   }
   BCU(cudaGetLastError());
   if (eterms && nsteps > 0) {
@@ -572,11 +517,10 @@ int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double 
   double *fdev = nullptr;
   if (forces) BCU(cudaMalloc((void **)&fdev, (size_t)b->nslots * 3 * sizeof(double)));
   launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
-  const int nb = (b->nwork + kRowWarps - 1) / kRowWarps;
-  if (nb > 0) launch_rows(b, p, rf, false, nullptr, nullptr, 0, fdev);
+  launch_pairs_asm(b, p, rf, 0, 0, fdev);
   k_batch_ereduce<<<b->nrep, 256, 0, b->stream>>>(b->rep, b->pe, b->wpart, rf ? 1 : 0,
                                                   b->eterms);
-  b->launches += 2 + (nb > 0);
+  b->launches += 2;
   cudaError_t e = cudaGetLastError();
   if (e == cudaSuccess && eterms)
     e = cudaMemcpyAsync(eterms, b->eterms, (size_t)b->nrep * kNTerms * sizeof(double),

@@ -164,8 +164,8 @@ __global__ void __launch_bounds__(32 * kAsmWarps)
 
 
 __global__ void __launch_bounds__(32 * kAsmWarps)
-    k_assemble_f32(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,
-                   uint64_t step) {
+    k_assemble_f32(const __grid_constant__ KP p, AssembleFlags fl, int do_bd, int variant,
+                   uint64_t seed, uint64_t step) {
   const int i = blockIdx.x * kAsmWarps + (threadIdx.x >> 5);
   const int lane = threadIdx.x & 31;
   const int ntot = p.st->ntot;
@@ -216,10 +216,11 @@ __global__ void __launch_bounds__(32 * kAsmWarps)
 constexpr int kTileWarps = 16;  // as the fused loop's phase A: the same sums
 
 __global__ void __launch_bounds__(32 * kTileWarps)
-    k_assemble_tiles(KP p, AssembleFlags fl, int do_bd, int variant, uint64_t seed,
-                     uint64_t step, int site_blocks) {
+    k_assemble_tiles(const __grid_constant__ KP p, AssembleFlags fl, int do_bd, int variant,
+                     uint64_t seed, uint64_t step, int site_blocks) {
   __shared__ float part[kTileWarps][10][32];
-  assemble_tile<kTileWarps>(p, fl, do_bd, variant, seed, step, blockIdx.x, site_blocks, part);
+  assemble_tile<kTileWarps>(p, ctx_asm_sys(p, fl.ntile, seed), fl, do_bd, variant, step,
+                            blockIdx.x, site_blocks, part);
 }
 
 void launch_assemble(const KP &p, int ntot_ub, const AssembleFlags &fl,

@@ -244,8 +244,8 @@ __global__ void __launch_bounds__(32 * kN3Warps)
   const int q = blockIdx.x * kN3Warps + w;
   float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
   if (q < n3_pairs(T))  // warp-uniform
-    n3_tile<II, RF, EFP>(p, q, T, p.st->ntot, qforces, sh[w], sl[w], sq[w], acc[w], accb[w],
-                         tab, e);
+    n3_tile<II, RF, EFP>(p, pair_sys(p, p.st->ntot, T), q, qforces, sh[w], sl[w], sq[w],
+                         acc[w], accb[w], tab, e);
   block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;

@@ -59,6 +59,8 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   const int slot = w * G + blockIdx.x, nslot = G * kLoopWarps;
   const int ntot = p.st->ntot;  // constant during BD
   const int T = fl.ntile, npair = n3_pairs(T);
+  const PairSys ps = pair_sys(p, ntot, T);
+  const AsmSys as = ctx_asm_sys(p, T, seed);
   const int m0 = p.nsites + p.nfix;
   unsigned bar = 0;
   float eo[4];  // single-particle energies: not formed here
@@ -74,12 +76,12 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   for (int s = 0; s < nsteps; ++s) {
     float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int q = slot; q < npair; q += nslot)
-      n3_tile<II, RF, EFP>(p, q, T, ntot, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w],
-                           sm.pr.acc[w], sm.pr.accb[w], tab, e);
+      n3_tile<II, RF, EFP>(p, ps, q, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w], sm.pr.acc[w],
+                           sm.pr.accb[w], tab, e);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
     for (int it = blockIdx.x; it < nitem; it += G) {
       const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;
-      assemble_tile<kLoopWarps>(p, fl, 1, variant, seed, step0 + s, t, 0, sm.part, h, npos);
+      assemble_tile<kLoopWarps>(p, as, fl, 1, variant, step0 + s, t, 0, sm.part, h, npos);
       __syncthreads();  // the new positions; part free again
       if (s + 1 < nsteps) {
         const int u0 = halves ? 16 * h : 0;

@@ -109,6 +109,30 @@ __device__ __forceinline__ void diff_model(const KP &p, int variant, int i, int 
 // their diffusion profile in FP64 (options off the hot path); variant 0 and
 // everything else stay on the FP32 pipe.
 // ---------------------------------------------------------------------------
+// The arrays and sizes the FP32 assembly and move of one system work on: a
+// context's own (ctx_asm_sys), or one replica's slots and partials in a
+// batch.  ffield / fis are component-major with stride cap from the
+// system's first particle; the noise of particle i is drawn from seed with
+// i counted from the system's first particle.
+struct AsmSys {
+  float4 *pk1, *pk2;
+  const int *typei;
+  const float *ffield, *fis;
+  const float4 *rfd;
+  const float4 *tpf;
+  const float *tpb;
+  int cap, nsites, nfix, ntot, T;
+  uint64_t seed;
+  const BoxF *box;
+  double *fx, *fy, *fz;  // forces out when not moving (element i at i * fs)
+  int fs;
+};
+
+__device__ __forceinline__ AsmSys ctx_asm_sys(const KP &p, int T, uint64_t seed) {
+  return AsmSys{p.pk1, p.pk2, p.typei, p.ffield_f, p.fis_f, p.rfd, p.tpf, p.tpb, p.cap,
+                p.nsites, p.nfix, p.st->ntot, T, seed, &p.f.box, p.fx, p.fy, p.fz, 1};
+}
+
 // What one particle's FP32 move needs besides its force: its position
 // records, ion type, diffusion factors and noise.  None depends on the
 // force, so the assembly gathers them before it sums the force.
@@ -122,33 +146,33 @@ struct MoveIn {
 
 // The loaded part (the types and factors do not change during BD and come
 // through the read-only path); noise: whether to draw the noise here too.
-__device__ __forceinline__ MoveIn move_in_f32(const KP &p, int variant, uint64_t seed,
+__device__ __forceinline__ MoveIn move_in_f32(const KP &p, const AsmSys &ms, int variant,
                                               uint64_t step, int i, bool noise = true) {
   MoveIn m;
-  const int m0 = p.nsites + p.nfix;
-  m.moves = !(i < m0 && (i >= p.nsites || !p.stfree[i]));
-  m.h4 = p.pk1[i];
-  m.l4 = p.pk2[i];
-  m.itype = i < p.nsites ? 0 : abs(__ldg(p.typei + i));
-  m.fa = variant == 0 && i >= p.nsites ? __ldg(p.fact_f + m.itype) : make_float2(0.f, 0.f);
-  if (noise) bd_noise3_f(seed, step, (uint32_t)i, m.g);
+  const int m0 = ms.nsites + ms.nfix;
+  m.moves = !(i < m0 && (i >= ms.nsites || !p.stfree[i]));
+  m.h4 = ms.pk1[i];
+  m.l4 = ms.pk2[i];
+  m.itype = i < ms.nsites ? 0 : abs(__ldg(ms.typei + i));
+  m.fa = variant == 0 && i >= ms.nsites ? __ldg(p.fact_f + m.itype) : make_float2(0.f, 0.f);
+  if (noise) bd_noise3_f(ms.seed, step, (uint32_t)i, m.g);
   return m;
 }
 
 // The move itself; m.h4 / m.l4 become the new records, also stored to
 // pk1 / pk2.
-__device__ __forceinline__ void bd_move_f32(const KP &p, int variant, int i, const float F[3],
-                                            MoveIn &m) {
+__device__ __forceinline__ void bd_move_f32(const KP &p, const AsmSys &ms, int variant, int i,
+                                            const float F[3], MoveIn &m) {
   if (!m.moves) return;
   float h[3] = {m.h4.x, m.h4.y, m.h4.z}, l[3] = {m.l4.x, m.l4.y, m.l4.z};
   const float *g = m.g;
-  if (i < p.nsites) {  // dynamics0nuc.f90:31-44
+  if (i < ms.nsites) {  // dynamics0nuc.f90:31-44
     for (int k = 0; k < 3; ++k) {
       float d = F[k] * p.f.fact0n1;
       clamp_f(p.f.bdmax, d);
       ff_add(h[k], l[k], fmaf(p.f.fact0n2, g[k], d));
     }
-    if (!p.qdnafree) fixcoor_ff(p.f.box, h, l);
+    if (!p.qdnafree) fixcoor_ff(*ms.box, h, l);
   } else {
     const int itype = m.itype;
     float fact1, fact2, dD[3] = {0.0f, 0.0f, 0.0f};
@@ -182,7 +206,7 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, int i, con
           atomicAdd(&p.nbackward[it * p.cntpts + j], 1);
       }
     }
-    fixcoor_ff(p.f.box, h, l);
+    fixcoor_ff(*ms.box, h, l);
   }
   m.h4.x = h[0];
   m.h4.y = h[1];
@@ -190,14 +214,15 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, int i, con
   m.l4.x = l[0];
   m.l4.y = l[1];
   m.l4.z = l[2];
-  p.pk1[i] = m.h4;
-  p.pk2[i] = m.l4;
+  ms.pk1[i] = m.h4;
+  ms.pk2[i] = m.l4;
 }
 
 __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t seed,
                                             uint64_t step, int i, const float F[3]) {
-  MoveIn m = move_in_f32(p, variant, seed, step, i);
-  bd_move_f32(p, variant, i, F, m);
+  const AsmSys ms = ctx_asm_sys(p, 0, seed);
+  MoveIn m = move_in_f32(p, ms, variant, step, i);
+  bd_move_f32(p, ms, variant, i, F, m);
 }
 
 // FP32 assembly for the Newton-3 partials: one block of NW warps per tile of
@@ -213,47 +238,48 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
 // npos: when given, warp 0 leaves each of those particles' records there
 // (npos[lane] = {hi, lo}, after the move).  Every thread of the block calls it.
 template <int NW>
-__device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &fl, int do_bd,
-                                              int variant, uint64_t seed, uint64_t step,
-                                              int blk, int site_blocks, float (*part)[10][32],
-                                              int half = -1, float4 (*npos)[2] = nullptr) {
+__device__ __forceinline__ void assemble_tile(const KP &p, const AsmSys &ms,
+                                              const AssembleFlags &fl, int do_bd, int variant,
+                                              uint64_t step, int blk, int site_blocks,
+                                              float (*part)[10][32], int half = -1,
+                                              float4 (*npos)[2] = nullptr) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool ionblk = blk >= site_blocks;
   const int Ti = blk - site_blocks;
-  const int i = ionblk ? p.nsites + 32 * Ti + lane : 32 * blk + lane;
-  const int ntot = p.st->ntot;
+  const int i = ionblk ? ms.nsites + 32 * Ti + lane : 32 * blk + lane;
+  const int ntot = ms.ntot;
   float s[5] = {0.f, 0.f, 0.f, 0.f, 0.f}, c[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   // warp 0: the particle's own inputs, loaded while the partials are summed
   const bool own = w == 0 && (half < 0 || (lane >> 4) == half) && i < ntot &&
-                   (ionblk || i < p.nsites);
+                   (ionblk || i < ms.nsites);
   MoveIn mv{};
   float fo[3] = {0.f, 0.f, 0.f}, fs[3] = {0.f, 0.f, 0.f};
   float4 d1 = make_float4(0.f, 0.f, 0.f, 0.f), d2 = d1;
   // warp 1 draws the noise of warp 0's particles meanwhile, into part[0]
   // (warp 0 keeps no partials there)
   if (w == 1 && do_bd && (half < 0 || (lane >> 4) == half) && i < ntot &&
-      (ionblk || i < p.nsites)) {
+      (ionblk || i < ms.nsites)) {
     float g[3];
-    bd_noise3_f(seed, step, (uint32_t)i, g);
+    bd_noise3_f(ms.seed, step, (uint32_t)i, g);
     part[0][0][lane] = g[0];
     part[0][1][lane] = g[1];
     part[0][2][lane] = g[2];
   }
   if (own) {
-    const int cap = p.cap;
+    const int cap = ms.cap;
 #pragma unroll
     for (int k = 0; k < 3; ++k) {
-      fo[k] = __ldcg(p.ffield_f + k * cap + i);
-      if (fl.is) fs[k] = __ldcg(p.fis_f + k * cap + i);
+      fo[k] = __ldcg(ms.ffield + k * cap + i);
+      if (fl.is) fs[k] = __ldcg(ms.fis + k * cap + i);
     }
     if (fl.rf_ab && ionblk) {
-      d1 = __ldcg(p.rfd + 2 * (size_t)i);
-      d2 = __ldcg(p.rfd + 2 * (size_t)i + 1);
+      d1 = __ldcg(ms.rfd + 2 * (size_t)i);
+      d2 = __ldcg(ms.rfd + 2 * (size_t)i + 1);
     }
-    if (do_bd) mv = move_in_f32(p, variant, seed, step, i, NW < 2);
+    if (do_bd) mv = move_in_f32(p, ms, variant, step, i, NW < 2);
   }
   if (ionblk) {
-    const int T = fl.ntile;
+    const int T = ms.T;
     for (int u0 = w; u0 < T; u0 += 4 * NW) {
       float4 va[4], vb[4];
       float ba[4], bb[4];
@@ -265,11 +291,11 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &
         if (u < T) {
           const int q = u < Ti ? n3_index(T, u, Ti) : n3_index(T, Ti, u);
           const size_t o = (size_t)q * 64 + (u < Ti ? 32 : 0) + lane;
-          va[j] = __ldcg(p.tpf + o);
-          if (fl.rf_ab) ba[j] = __ldcg(p.tpb + o);
+          va[j] = __ldcg(ms.tpf + o);
+          if (fl.rf_ab) ba[j] = __ldcg(ms.tpb + o);
           if (u == Ti) {  // diagonal tile pair: the column side too
-            vb[j] = __ldcg(p.tpf + o + 32);
-            if (fl.rf_ab) bb[j] = __ldcg(p.tpb + o + 32);
+            vb[j] = __ldcg(ms.tpf + o + 32);
+            if (fl.rf_ab) bb[j] = __ldcg(ms.tpb + o + 32);
           }
         }
       }
@@ -316,9 +342,11 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &
 #pragma unroll
   for (int k = 0; k < 3; ++k) F[k] = s[k] + c[k];
   if (!do_bd) {  // forces for the host (energy calls)
-    p.fx[i] = F[0];
-    p.fy[i] = F[1];
-    p.fz[i] = F[2];
+    if (ms.fx) {
+      ms.fx[(size_t)i * ms.fs] = F[0];
+      ms.fy[(size_t)i * ms.fs] = F[1];
+      ms.fz[(size_t)i * ms.fs] = F[2];
+    }
     return;
   }
   if (NW >= 2) {
@@ -326,7 +354,7 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AssembleFlags &
     mv.g[1] = part[0][1][lane];
     mv.g[2] = part[0][2][lane];
   }
-  bd_move_f32(p, variant, i, F, mv);
+  bd_move_f32(p, ms, variant, i, F, mv);
   if (npos) {
     npos[lane][0] = mv.h4;
     npos[lane][1] = mv.l4;

@@ -25,17 +25,33 @@ namespace bgpu {
 // Output: per tile pair and side, per lane, (f, A) and B (tpf, tpb); the
 // assembly kernel sums a particle's row and column entries in fixed order.
 // ---------------------------------------------------------------------------
+// The particle records and partial buffers of one system for the pair tile:
+// a context's own arrays, or one replica's slots and partials in a batch.
+struct PairSys {
+  const float4 *pk1, *pk2, *pk3;
+  float4 *tpf;
+  float *tpb;
+  int nsites, nfix;
+  int ntot;  // live particles
+  int T;     // ion tiles of 32
+};
+
+__device__ __forceinline__ PairSys pair_sys(const KP &p, int ntot, int T) {
+  return PairSys{p.pk1, p.pk2, p.pk3, p.tpf, p.tpb, p.nsites, p.nfix, ntot, T};
+}
+
 // One tile pair q of the Newton-3 pair kernel, run by one warp (all 32
 // lanes).  sh/sl/sq/acc/accb: the warp's own 32-entry shared arrays; tab:
 // the block's dense ion-ion law table; e: the lane's energy sums (ecoul,
-// elj, esrpmf, eefpot, erfpar), added to.  T: ion tiles; ntot: live count.
+// elj, esrpmf, eefpot, erfpar), added to.  p: the laws and constants.
 template <bool II, bool RF, bool EFP>
-__device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int qforces,
+__device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, int qforces,
                                         float4 *sh, float4 *sl, float4 *sq, float4 *acc,
                                         float *accb, const float4 *tab, float e[5]) {
   const int lane = threadIdx.x & 31;
   const int nt = p.nion_t;
-  const int m0 = p.nsites + p.nfix;
+  const int T = ps.T, ntot = ps.ntot;
+  const int m0 = ps.nsites + ps.nfix;
   float fx = 0.f, fy = 0.f, fz = 0.f, A = 0.f, B = 0.f;
   bool iv = false;
   int jl = 0;
@@ -47,17 +63,17 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
   while (I + 1 < T && n3_index(T, I + 1, I + 1) <= q) ++I;
   const int J = I + (q - n3_index(T, I, I));
   const bool diag = I == J;
-  const int i = p.nsites + I * 32 + lane;
-  jl = p.nsites + J * 32 + lane;
+  const int i = ps.nsites + I * 32 + lane;
+  jl = ps.nsites + J * 32 + lane;
   // column tile into shared memory; its first ncol slots hold ions.  An
   // empty slot sits 1e10 A away with zero charge, srfe and reff and the first
   // ion type, so the branch-free path below can run over it with its law
   // entry zeroed: every term it adds is then exactly zero.
-  const int ncol = min(32, max(0, ntot - (p.nsites + J * 32)));
+  const int ncol = min(32, max(0, ntot - (ps.nsites + J * 32)));
   if (jl < ntot) {
-    sh[lane] = __ldcg(p.pk1 + jl);
-    sl[lane] = __ldcg(p.pk2 + jl);
-    if (RF) sq[lane] = __ldcg(p.pk3 + jl);
+    sh[lane] = __ldcg(ps.pk1 + jl);
+    sl[lane] = __ldcg(ps.pk2 + jl);
+    if (RF) sq[lane] = __ldcg(ps.pk3 + jl);
   } else {
     sh[lane] = make_float4(1e10f, 1e10f, 1e10f, __int_as_float(EFP ? 0 : p.ndna));
     sl[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -68,9 +84,9 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
   iv = i < ntot;
   float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th, tq = th;
   if (iv) {
-    th = __ldcg(p.pk1 + i);
-    tl = __ldcg(p.pk2 + i);
-    if (RF) tq = __ldcg(p.pk3 + i);
+    th = __ldcg(ps.pk1 + i);
+    tl = __ldcg(ps.pk2 + i);
+    if (RF) tq = __ldcg(ps.pk3 + i);
   }
   const int tcode = __float_as_int(th.w);
   const bool tmob = iv && i >= m0;
@@ -79,13 +95,18 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
   const float srt = tl.w, rft = tq.x, ct = p.f.celec * tq.y;
   __syncwarp();
   // Fast path: an off-diagonal tile pair whose 32 row ions are present and
-  // whose ions are all mobile (and, with RFPAR, all qualify for the cross
-  // term in both roles): no per-pair validity, mobility or role test.  A
-  // column tile with empty slots (RAG) zeroes their law entries instead.
+  // whose ions are all mobile: no per-pair validity, mobility or role test.
+  // With RFPAR every ion must either qualify for the cross term in both
+  // roles (flags 4 and 8) or lie outside the RFPAR map (flag 1 clear), where
+  // its srfe and reff are zero and every cross-term quantity of its pairs
+  // comes out exactly zero.  A column tile with empty slots (RAG) zeroes
+  // their law entries instead.
   bool lane_ok = iv && tmob && (jl >= ntot || jl >= m0);
-  if (RF)
-    lane_ok = lane_ok && (tb & 12) == 12 &&
-              (jl >= ntot || (__float_as_int(sq[lane].z) & 12) == 12);
+  if (RF) {
+    const int sb0 = __float_as_int(sq[lane].z);
+    lane_ok = lane_ok && ((tb & 12) == 12 || !(tb & 1)) &&
+              (jl >= ntot || (sb0 & 12) == 12 || !(sb0 & 1));
+  }
   const bool fast = II && !EFP && !diag && __all_sync(0xffffffffu, lane_ok);
   auto fast_loop = [&](auto rag) {
     constexpr bool RAG = decltype(rag)::value;
@@ -100,7 +121,7 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
       if (RAG && mm >= ncol) c = make_float4(0.f, 0.f, c.z, 0.f);
-      const float ir = rsqrtf(r2), ir2 = ir * ir;
+      const float ir = rsqrt_nz(r2), ir2 = ir * ir;
       const float cofo = c.x * ir;
       e[0] += cofo;
       float d6 = c.z * ir2;
@@ -114,7 +135,7 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
       if (RF) {
         const float4 u = sq[mm];
         const float rij = u.x * rft, srij = l.w * srt;
-        const float rfdn = rsqrtf(fmaf(rij, rij, r2));
+        const float rfdn = rsqrt_nz(fmaf(rij, rij, r2));
         const float aux0 = ct * u.y;
         const float a1 = aux0 * rij * rfdn;
         e[4] = fmaf(a1, srij, e[4]);
@@ -149,7 +170,7 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
       const int scode = __float_as_int(h.w);
       if (iv && mm < ncol && !(diag && k == 16 && lane >= 16)) {
         const float4 l = sl[mm];
-        const int j = p.nsites + J * 32 + mm;
+        const int j = ps.nsites + J * 32 + mm;
         const bool smob = j >= m0;
         const float dx = (th.x - h.x) + (tl.x - l.x);
         const float dy = (th.y - h.y) + (tl.y - l.y);
@@ -161,7 +182,7 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
             dii = law32k(p, __ldg(p.pidx + row + (scode & 0xffff)), r2, 1.0f, e);
           } else {
             const float4 c = tab[row + (scode & 0xffff) - p.ndna];
-            const float ir = rsqrtf(r2), ir2 = ir * ir;
+            const float ir = rsqrt_nz(r2), ir2 = ir * ir;
             const float cofo = c.x * ir;
             e[0] += cofo;
             float d6 = c.z * ir2;
@@ -178,7 +199,7 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
           const int sb = __float_as_int(sqv.z);
           if (i > j ? ((tb & 4) && (sb & 8)) : ((sb & 4) && (tb & 8))) {
             const float rij = sqv.x * rft, srij = l.w * srt;
-            const float rfdn = rsqrtf(fmaf(rij, rij, r2));
+            const float rfdn = rsqrt_nz(fmaf(rij, rij, r2));
             const float aux0 = ct * sqv.y;
             const float a1 = aux0 * rij * rfdn;
             e[4] = fmaf(a1, srij, e[4]);
@@ -207,11 +228,11 @@ __device__ __forceinline__ void n3_tile(const KP &p, int q, int T, int ntot, int
     }
   }
   // row side (lane l = row ion), column side (lane l = column ion)
-  float4 *o = p.tpf + (size_t)q * 64;
+  float4 *o = ps.tpf + (size_t)q * 64;
   o[lane] = qforces && iv ? make_float4(fx, fy, fz, A) : make_float4(0.f, 0.f, 0.f, 0.f);
   o[32 + lane] = qforces && jl < ntot ? acc[lane] : make_float4(0.f, 0.f, 0.f, 0.f);
   if (RF) {
-    float *ob = p.tpb + (size_t)q * 64;
+    float *ob = ps.tpb + (size_t)q * 64;
     ob[lane] = qforces && iv ? B : 0.f;
     ob[32 + lane] = qforces && jl < ntot ? accb[lane] : 0.f;
   }

@@ -11,6 +11,15 @@ __device__ __forceinline__ double pow6d(double v) {
   double v2 = v * v;
   return v2 * v2 * v2;
 }
+// 1/sqrt(x) for a positive normal float: the hardware approximation (PTX
+// rsqrt.approx.ftz.f32, relative error below 2^-22.9 by the PTX ISA).
+// rsqrtf() wraps the same operation in a denormal-input path that pair
+// distances and RFPAR denominators never take.
+__device__ __forceinline__ float rsqrt_nz(float x) {
+  float y;
+  asm("rsqrt.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
 __device__ __forceinline__ float pow3f(float v) { return v * v * v; }
 __device__ __forceinline__ float pow6f(float v) {
   float v2 = v * v;

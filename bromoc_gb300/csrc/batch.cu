@@ -73,7 +73,7 @@ __global__ void __launch_bounds__(32 * kPairWarps)
 // system path on the replica's slots; fout (if not moving): 3 doubles per
 // slot.
 template <bool RF>
-__global__ void __launch_bounds__(32 * kAsmTileWarps)
+__global__ void __launch_bounds__(32 * kAsmTileWarps, 2)
     k_batch_asm(const __grid_constant__ KP p, const RepDev *rep, const int2 *tiles,
                 const float4 *tpf, const float *tpb, int do_bd, uint64_t step, double *fout) {
   __shared__ float part[kAsmTileWarps][10][32];

@@ -228,7 +228,8 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
 // FP32 assembly for the Newton-3 partials: one block of NW warps per tile of
 // 32 particles (site tiles first, then the ion tiles of the pair kernel).
 // The warps take every NW-th tile pair of the ion tile, four at a time with
-// all loads issued first, each partial one coalesced 512-byte row; their
+// all loads issued first, each partial one coalesced 512-byte row (the
+// diagonal pair's column side last, by the warp that holds it); their
 // compensated sums meet in shared memory in a fixed order; warp 0 then
 // assembles and moves its 32 particles, one lane each.  Inputs that another
 // block may have written in the same launch are read past L1.  blk: the tile
@@ -281,22 +282,18 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AsmSys &ms,
   if (ionblk) {
     const int T = ms.T;
     for (int u0 = w; u0 < T; u0 += 4 * NW) {
-      float4 va[4], vb[4];
-      float ba[4], bb[4];
+      float4 va[4];
+      float ba[4];
 #pragma unroll
       for (int j = 0; j < 4; ++j) {
         const int u = u0 + j * NW;
-        va[j] = vb[j] = make_float4(0.f, 0.f, 0.f, 0.f);
-        ba[j] = bb[j] = 0.f;
+        va[j] = make_float4(0.f, 0.f, 0.f, 0.f);
+        ba[j] = 0.f;
         if (u < T) {
           const int q = u < Ti ? n3_index(T, u, Ti) : n3_index(T, Ti, u);
           const size_t o = (size_t)q * 64 + (u < Ti ? 32 : 0) + lane;
           va[j] = __ldcg(ms.tpf + o);
           if (fl.rf_ab) ba[j] = __ldcg(ms.tpb + o);
-          if (u == Ti) {  // diagonal tile pair: the column side too
-            vb[j] = __ldcg(ms.tpf + o + 32);
-            if (fl.rf_ab) bb[j] = __ldcg(ms.tpb + o + 32);
-          }
         }
       }
 #pragma unroll
@@ -306,14 +303,16 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AsmSys &ms,
         acc2(s[2], c[2], va[j].z);
         acc2(s[3], c[3], va[j].w);
         acc2(s[4], c[4], ba[j]);
-        if (u0 + j * NW == Ti) {
-          acc2(s[0], c[0], vb[j].x);
-          acc2(s[1], c[1], vb[j].y);
-          acc2(s[2], c[2], vb[j].z);
-          acc2(s[3], c[3], vb[j].w);
-          acc2(s[4], c[4], bb[j]);
-        }
       }
+    }
+    if (Ti < T && Ti % NW == w) {  // the diagonal tile pair's column side
+      const size_t o = (size_t)n3_index(T, Ti, Ti) * 64 + 32 + lane;
+      const float4 vb = __ldcg(ms.tpf + o);
+      acc2(s[0], c[0], vb.x);
+      acc2(s[1], c[1], vb.y);
+      acc2(s[2], c[2], vb.z);
+      acc2(s[3], c[3], vb.w);
+      if (fl.rf_ab) acc2(s[4], c[4], __ldcg(ms.tpb + o));
     }
   }
   if (w > 0)

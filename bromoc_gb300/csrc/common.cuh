@@ -75,6 +75,7 @@ struct Trial {
   double srfe, reff;        // RFPAR gathers of the trial (0 outside the map)
   int rf_in;                // trial inside the RFPAR map
   int ntot;                 // live particle count when the trial was made
+  int chg;                  // GRAND: slot the previous accepted move rewrote, -1 none
 };
 
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------

@@ -32,7 +32,10 @@ __device__ __forceinline__ double seg8(double v) {
 // static field (staticf0.f90), repulsion (vdwgd0trln.f90), gsrfen and greff
 // (rfpar.f90:312-344 with its early exit); lanes 0..26 the B-spline nodes
 // (vdwgd0spln.f90).  Fills e_single, srfe, reff, rf_in of tr (lane 0).
-__device__ void trial_single_warp(const KP &p, Trial &tr, uint32_t mask, int qalert) {
+// nalert: when given, the warnings are counted there (lane 0) instead of
+// being added to p.warn.
+__device__ void trial_single_warp(const KP &p, Trial &tr, uint32_t mask, int qalert,
+                                  int *nalert = nullptr) {
   const int lane = threadIdx.x & 31;
   const int j0 = tr.j - 1;
   const bool beion = j0 >= p.nsites;
@@ -114,8 +117,12 @@ __device__ void trial_single_warp(const KP &p, Trial &tr, uint32_t mask, int qal
     double e = 0.0;
     if ((mask & 2u) && p.qmemb) {
       double f[3];
-      if (membrane_one(p, jt2, charge, x, y, z, false, true, e, f) && qalert)
-        atomicAdd(&p.warn[jt2], 1);
+      if (membrane_one(p, jt2, charge, x, y, z, false, true, e, f) && qalert) {
+        if (nalert)
+          ++*nalert;
+        else
+          atomicAdd(&p.warn[jt2], 1);
+      }
     }
     if (do_rf) e += 0.5 * p.celec * p.cg[tr.itype] * p.cg[tr.itype] * sj * sj;
     if (do_phix) e += le;
@@ -124,7 +131,12 @@ __device__ void trial_single_warp(const KP &p, Trial &tr, uint32_t mask, int qal
       const double ps = p.qtrln ? s_v : bsum;
       if (ps >= (p.qtrln ? p.thold8 : p.thold27)) {
         ev = 1.0e10;
-        if (qalert) atomicAdd(&p.warn[jt2], 1);
+        if (qalert) {
+          if (nalert)
+            ++*nalert;
+          else
+            atomicAdd(&p.warn[jt2], 1);
+        }
       }
       e += ev;
     }
@@ -157,16 +169,33 @@ __device__ __forceinline__ Trial load_trial_cg(const Trial *t) {
   return r;
 }
 
+// What interact_one reads of particle i: position, type and its RFPAR
+// (srfe, reff).  Read past L1 (__ldcg): inside the GRAND kernel they change
+// between attempts.
+struct PartRec {
+  double x, y, z;
+  double2 rf;
+  int ti;
+};
+
+__device__ __forceinline__ PartRec load_part(const KP &p, int i, bool rf) {
+  PartRec r;
+  r.ti = __ldcg(p.typei + i);
+  r.x = __ldcg(p.x + i);
+  r.y = __ldcg(p.y + i);
+  r.z = __ldcg(p.z + i);
+  r.rf = rf && i >= p.nsites ? __ldcg(p.gc_rf + i) : make_double2(0.0, 0.0);
+  return r;
+}
+
 // ΔE term of particle i (pair law + RFPAR cross) against the trial, the
-// O(N) part of INTERACT.  Particle data are read past L1 (__ldcg) because
-// inside the GRAND kernel they change between attempts.
-__device__ double interact_one(const KP &p, const Trial &tr, uint32_t mask, int i,
-                               int jt2, bool beion, bool rf, int &err) {
+// O(N) part of INTERACT; q: the particle's record (load_part).
+__device__ double interact_rec(const KP &p, const Trial &tr, uint32_t mask, int i, int jt2,
+                               bool beion, bool rf, const PartRec &q, int &err) {
   const bool ion_i = i >= p.nsites;
-  const int ti = __ldcg(p.typei + i);
+  const int ti = q.ti;
   if (ion_i && guard_bad(p.st, abs(ti) - p.nold - 1, p.ntype - p.nold, 31)) return 0.0;
-  const double dx = __ldcg(p.x + i) - tr.x, dy = __ldcg(p.y + i) - tr.y,
-               dz = __ldcg(p.z + i) - tr.z;
+  const double dx = q.x - tr.x, dy = q.y - tr.y, dz = q.z - tr.z;
   const double d2 = dx * dx + dy * dy + dz * dz;
   double u = 0.0;
   if (mask & 1u) {
@@ -180,7 +209,7 @@ __device__ double interact_one(const KP &p, const Trial &tr, uint32_t mask, int 
     if (is >= 0) u += law_interact64(p, p.pp[is], d2, err);
   }
   if (rf && ion_i) {
-    const double2 g = __ldcg(p.gc_rf + i);
+    const double2 g = q.rf;
     if (g.x != 0.0) {
       const double tau = p.celec * p.cg[tr.itype];
       const double reffij = tr.reff * g.y;
@@ -188,6 +217,11 @@ __device__ double interact_one(const KP &p, const Trial &tr, uint32_t mask, int 
     }
   }
   return u;
+}
+
+__device__ double interact_one(const KP &p, const Trial &tr, uint32_t mask, int i, int jt2,
+                               bool beion, bool rf, int &err) {
+  return interact_rec(p, tr, mask, i, jt2, beion, rf, load_part(p, i, rf), err);
 }
 
 // Combined type of the trial particle, 0 (and a guard record) when invalid.
@@ -266,25 +300,43 @@ void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
 // in one cooperative launch.  Block 0 owns the GCMC state (live count,
 // buffer counters, buffer parameters) in shared memory for the whole launch
 // and writes it back at the end; the other blocks only sum ΔE.  Per attempt:
-//   block 0: proposal + the trial's single-particle terms; publish the
-//            trial (generation flag, release);
+//   block 0: the proposal and the trial's single-particle terms; publish
+//            the trial (generation flag, release);
 //   every block: its share of the O(N) ΔE sum -> ipart[block]; arrive on a
 //            counter (release);
-//   block 0: waits for every arrival (acquire), total ΔE, Im-Roux
-//            acceptance, insertion/deletion, counters; then straight on to
-//            the next proposal.
+//   block 0: while the other blocks sum, the next attempt's random draws
+//            (they do not depend on the outcome) and, for an insertion, the
+//            next trial's single-particle terms (they depend only on its
+//            position); then waits for every arrival (acquire), total ΔE,
+//            Im-Roux acceptance, insertion/deletion, counters, and the part
+//            of the next proposal that depends on the new state (the live
+//            count; for a deletion the rank of its ion, which slot holds it
+//            and its single-particle terms).
 // One synchronisation per attempt.  Each thread owns the same particles in
-// every phase (round-robin over blocks), so the RFPAR prepass of a particle
-// is read only by the thread that wrote it until block 0 edits it.  Data
+// every phase (round-robin over blocks): it reads its particle's record
+// before waiting for the next trial, and re-reads it only if the trial
+// names its slot as the one the last accepted move rewrote.  Block 0
+// proposes the first attempt before its share of the RFPAR prepass.  Data
 // that another block wrote during the launch are read past L1 (__ldcg).
+// With more than one block, block 0 owns no particles.
 // Every wait is bounded: it gives up after kWaitSpins polls, or as soon as
 // another block has given up, records kErrBarrier and the launch returns.
+// The draws, the proposals and their outcomes are those of proposing
+// each attempt after the previous one is settled.
 // ---------------------------------------------------------------------------
 constexpr int kGrandThreads = 128;
 
 struct GrandState {
   Trial s;                  // current trial
   double2 trial_rf;         // RFPAR (srfe, reff) at an insertion trial
+  Trial nx;                 // the next attempt's draws (+ insertion terms)
+  double nx_u;              // the next deletion's rank draw
+  double2 nx_rf;            // RFPAR (srfe, reff) of the next insertion trial
+  int nx_fields;            // nx holds the trial's single-particle terms (an
+                            // insertion's, or a deletion's found in the state
+                            // before the pending acceptance)
+  int nx_alert;             // warnings of that deletion trial, not yet counted
+  int chg;                  // slot the last accepted move rewrote, -1 none
   int ntot;
   int nat[kMaxBuffers], ninsert[kMaxBuffers], nremove[kMaxBuffers], ntotat[kMaxBuffers];
   double dener_sum;
@@ -315,95 +367,180 @@ struct Draws {
   }
 };
 
-// Proposal of one attempt (grand.f90:42-86): insertion point by rejection
-// sampling inside the buffer (insert.f90) or the rank-th ion of the buffer
-// in slot order (find.f90), then the trial's single-particle terms (warp 0)
-// and, for an insertion, its RFPAR (srfe, reff) (warp 1).
-__device__ void propose(const KP &p, uint32_t mask, uint64_t seed, uint64_t cycle,
-                        uint32_t attempt, GrandState &g) {
-  __syncthreads();
-  if (threadIdx.x == 0) {
-    Trial t{};
-    Draws d{seed, cycle, attempt};
-    const int nbuf = p.nbuffer, ntot = g.ntot;
-    if (d.next() < 0.5) {
-      const int ib = (int)((double)nbuf * d.next()) + 1;
-      t.insert = 1;
-      t.ib = ib;
-      if (ib <= nbuf && g.avnum[ib] > 0.0) {
-        t.itype = g.ibfftyp[ib];
-        t.j = ntot + 1;
-        t.valid = 1;
-        bool ok = false;
-        for (int it = 0; it < (1 << 20) && !ok; ++it) {
-          const double u1 = d.next(), u2 = d.next(), u3 = d.next();
-          t.x = p.lx * (u1 - 0.5) + p.cx;
-          t.y = p.ly * (u2 - 0.5) + p.cy;
-          t.z = g.lzmin[ib] + (g.lzmax[ib] - g.lzmin[ib]) * u3;
-          ok = true;
-          if (p.shape == 1) {
-            const double r2 = (t.x - p.cx) * (t.x - p.cx) + (t.y - p.cy) * (t.y - p.cy) +
-                              (t.z - p.cz) * (t.z - p.cz);
-            ok = r2 > g.rmin[ib] * g.rmin[ib] && r2 < g.rmax[ib] * g.rmax[ib];
-          } else if (p.shape == 2) {
-            const double ex = (t.x - p.cx) * p.iecx, ey = (t.y - p.cy) * p.iecy;
-            ok = ex * ex + ey * ey < 1.0;
-          }
-        }
-        if (!ok) {  // rejection sampling did not terminate: give up the attempt
-          t.valid = 0;
-          atomicOr(&p.st->err, kErrFind);
+// The random part of one attempt's proposal (grand.f90:42-86), thread 0 of
+// block 0: insertion or deletion, the buffer, for an insertion its point by
+// rejection sampling inside the buffer (insert.f90), for a deletion the
+// uniform its rank is drawn from (find.f90).  None depends on the state.
+__device__ void propose_draws(const KP &p, uint64_t seed, uint64_t cycle, uint32_t attempt,
+                              GrandState &g) {
+  Trial t{};
+  Draws d{seed, cycle, attempt};
+  const int nbuf = p.nbuffer;
+  double u_rank = 0.0;
+  if (d.next() < 0.5) {
+    const int ib = (int)((double)nbuf * d.next()) + 1;
+    t.insert = 1;
+    t.ib = ib;
+    if (ib <= nbuf && g.avnum[ib] > 0.0) {
+      t.itype = g.ibfftyp[ib];
+      t.valid = 1;
+      bool ok = false;
+      for (int it = 0; it < (1 << 20) && !ok; ++it) {
+        const double u1 = d.next(), u2 = d.next(), u3 = d.next();
+        t.x = p.lx * (u1 - 0.5) + p.cx;
+        t.y = p.ly * (u2 - 0.5) + p.cy;
+        t.z = g.lzmin[ib] + (g.lzmax[ib] - g.lzmin[ib]) * u3;
+        ok = true;
+        if (p.shape == 1) {
+          const double r2 = (t.x - p.cx) * (t.x - p.cx) + (t.y - p.cy) * (t.y - p.cy) +
+                            (t.z - p.cz) * (t.z - p.cz);
+          ok = r2 > g.rmin[ib] * g.rmin[ib] && r2 < g.rmax[ib] * g.rmax[ib];
+        } else if (p.shape == 2) {
+          const double ex = (t.x - p.cx) * p.iecx, ey = (t.y - p.cy) * p.iecy;
+          ok = ex * ex + ey * ey < 1.0;
         }
       }
+      if (!ok) {  // rejection sampling did not terminate: give up the attempt
+        t.valid = 0;
+        atomicOr(&p.st->err, kErrFind);
+      }
+    }
+  } else {
+    t.ib = (int)((double)nbuf * d.next()) + 1;
+    u_rank = d.next();
+    t.insert = 0;
+  }
+  t.draw = (int)d.n;
+  g.nx = t;
+  g.nx_u = u_rank;
+  g.nx_fields = 0;
+}
+
+// find.f90: the slot of the rank-th ion of buffer ib in slot order, -1 if
+// none; block 0, every thread, result in g.found.
+__device__ void find_rank(const KP &p, GrandState &g, int ib, int rank) {
+  __syncthreads();
+  if (threadIdx.x == 0) g.found = -1;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
+  const int lo = p.nsites + p.nfix, ntot = g.ntot;
+  const int per = (ntot - lo + (int)blockDim.x - 1) / (int)blockDim.x;
+  const int a = lo + threadIdx.x * per, b = min(ntot, a + per);
+  int c = 0;
+  for (int k = a; k < b; ++k) c += (p.ibuffer[k] == ib);
+  int incl = c;  // inclusive scan: warp shuffles, then the warp totals
+#pragma unroll
+  for (int o = 1; o < 32; o <<= 1) {
+    const int v = __shfl_up_sync(0xffffffffu, incl, o);
+    if (lane >= o) incl += v;
+  }
+  if (lane == 31) g.scan[wid] = incl;
+  __syncthreads();
+  int before = incl - c;
+  for (int w = 0; w < wid; ++w) before += g.scan[w];
+  if (rank > before && rank <= before + c) {  // exactly one thread
+    int r = before;
+    for (int k = a; k < b; ++k)
+      if (p.ibuffer[k] == ib && ++r == rank) {
+        g.found = k;
+        break;
+      }
+  }
+  __syncthreads();
+}
+
+// The next trial's single-particle terms ahead of the pending acceptance,
+// block 0 (every thread).  An insertion's depend on its point only: warp 0
+// its terms, warp 1 its RFPAR (srfe, reff).  A deletion's are found in the
+// current state (its rank from the current buffer count, the slot, the
+// terms, warnings counted but not yet added): exact if the acceptance
+// changes nothing, else redone by propose_finish.
+__device__ void next_terms(const KP &p, uint32_t mask, GrandState &g) {
+  __syncthreads();
+  Trial t = g.nx;
+  if (t.insert) {
+    if (t.valid) {
+      t.j = p.nsites + 1;  // any ion slot: the terms of an ion at t's point
+      if (threadIdx.x < 32) {
+        trial_single_warp(p, t, mask, 0);
+        if (threadIdx.x == 0) {
+          g.nx.e_single = t.e_single;
+          g.nx.srfe = t.srfe;
+          g.nx.reff = t.reff;
+          g.nx.rf_in = t.rf_in;
+        }
+      } else if (threadIdx.x == 32 && (mask & 16u) && p.qrfpar) {
+        g.nx_rf = rf_single(p, t.x, t.y, t.z, t.itype);
+      }
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) g.nx_fields = t.valid;
+    return;
+  }
+  const int nbuf = p.nbuffer, ib = t.ib;
+  const int natb = ib <= nbuf ? g.nat[ib - 1] : 0;
+  const int ip = (int)((double)natb * g.nx_u) + 1;
+  if (!(ib <= nbuf && ip <= natb)) return;  // block-uniform: nothing to find
+  find_rank(p, g, ib, ip);
+  const int k = g.found;
+  if (k < 0 || k >= g.ntot) return;
+  t.itype = g.ibfftyp[ib];
+  t.valid = 1;
+  t.j = k + 1;
+  t.x = p.x[k];
+  t.y = p.y[k];
+  t.z = p.z[k];
+  if (threadIdx.x == 0) g.nx_alert = 0;
+  __syncthreads();
+  if (threadIdx.x < 32) {
+    trial_single_warp(p, t, mask, 1, &g.nx_alert);
+    if (threadIdx.x == 0) {
+      g.nx = t;
+      g.nx_fields = 1;
+    }
+  }
+  __syncthreads();
+}
+
+// The state-dependent part of the proposal, block 0: the live count, for a
+// deletion the rank-th ion of the buffer in slot order (find.f90) and its
+// single-particle terms (deletion trials raise warnings as INTERACT with
+// Qalert does, insertion trials do not: grand.f90:48,86); g.nx -> g.s.
+// Terms that next_terms found ahead are kept when they still hold: always
+// for an insertion, for a deletion when the acceptance changed nothing.
+__device__ void propose_finish(const KP &p, uint32_t mask, GrandState &g) {
+  __syncthreads();
+  const bool keep = g.nx_fields && (g.nx.insert || g.chg < 0);
+  if (threadIdx.x == 0) {
+    Trial t = g.nx;
+    const int ntot = g.ntot, nbuf = p.nbuffer;
+    if (t.insert) {
+      t.j = ntot + 1;
+    } else if (keep) {
+      if (g.nx_alert > 0) atomicAdd(&p.warn[p.nwtype[t.itype]], g.nx_alert);
     } else {
-      const int ib = (int)((double)nbuf * d.next()) + 1;
+      const int ib = t.ib;
       const int natb = ib <= nbuf ? g.nat[ib - 1] : 0;
-      const int ip = (int)((double)natb * d.next()) + 1;
-      t.insert = 0;
-      t.ib = ib;
+      const int ip = (int)((double)natb * g.nx_u) + 1;
+      t.valid = 0;
       if (ib <= nbuf && ip <= natb) {
         t.itype = g.ibfftyp[ib];
         t.valid = 1;
         t.j = ip;  // rank within the buffer; resolved to a slot below
       }
     }
-    t.draw = (int)d.n;
     t.ntot = ntot;
+    t.chg = g.chg;
     g.s = t;
-    g.found = -1;
+    if (t.insert) g.trial_rf = g.nx_rf;
   }
   __syncthreads();
+  if (keep) return;
   const Trial &s = g.s;
-  if (s.valid && !s.insert) {  // find.f90: the rank-th ion of buffer ib in slot order
-    const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
-    const int lo = p.nsites + p.nfix, ntot = g.ntot;
-    const int per = (ntot - lo + (int)blockDim.x - 1) / (int)blockDim.x;
-    const int a = lo + threadIdx.x * per, b = min(ntot, a + per);
-    int c = 0;
-    for (int k = a; k < b; ++k) c += (p.ibuffer[k] == s.ib);
-    int incl = c;  // inclusive scan: warp shuffles, then the warp totals
-#pragma unroll
-    for (int o = 1; o < 32; o <<= 1) {
-      const int v = __shfl_up_sync(0xffffffffu, incl, o);
-      if (lane >= o) incl += v;
-    }
-    if (lane == 31) g.scan[wid] = incl;
-    __syncthreads();
-    int before = incl - c;
-    for (int w = 0; w < wid; ++w) before += g.scan[w];
-    const int rank = s.j;
-    if (rank > before && rank <= before + c) {  // exactly one thread
-      int r = before;
-      for (int k = a; k < b; ++k)
-        if (p.ibuffer[k] == s.ib && ++r == rank) {
-          g.found = k;
-          break;
-        }
-    }
-    __syncthreads();
+  if (s.valid && !s.insert) {
+    find_rank(p, g, s.ib, s.j);
     if (threadIdx.x == 0) {
       const int k = g.found;
-      if (k < 0 || guard_bad(p.st, k, ntot, 11)) {
+      if (k < 0 || guard_bad(p.st, k, g.ntot, 11)) {
         g.s.valid = 0;
         atomicOr(&p.st->err, kErrFind);
       } else {
@@ -414,27 +551,34 @@ __device__ void propose(const KP &p, uint32_t mask, uint64_t seed, uint64_t cycl
       }
     }
     __syncthreads();
-  }
-  // the trial's single-particle terms (deletion trials raise warnings as
-  // INTERACT with Qalert does, insertion trials do not: grand.f90:48,86)
-  if (threadIdx.x < 32 && g.s.valid) {
-    Trial t = g.s;
-    trial_single_warp(p, t, mask, t.insert ? 0 : 1);
-    if (threadIdx.x == 0) g.s = t;
-  } else if (threadIdx.x == 32 && g.s.valid && g.s.insert && (mask & 16u) && p.qrfpar) {
-    g.trial_rf = rf_single(p, g.s.x, g.s.y, g.s.z, g.s.itype);
+    if (threadIdx.x < 32 && g.s.valid) {
+      Trial t = g.s;
+      trial_single_warp(p, t, mask, 1);
+      if (threadIdx.x == 0) g.s = t;
+    }
+  } else if (s.valid && s.insert) {  // not computed ahead
+    if (threadIdx.x < 32) {
+      Trial t = g.s;
+      trial_single_warp(p, t, mask, 0);
+      if (threadIdx.x == 0) g.s = t;
+    } else if (threadIdx.x == 32 && (mask & 16u) && p.qrfpar) {
+      g.trial_rf = rf_single(p, g.s.x, g.s.y, g.s.z, g.s.itype);
+    }
   }
   __syncthreads();
 }
 
 // Total ΔE, Im-Roux acceptance and the insertion/deletion (grand.f90:48-116)
-// of the current trial; block 0, state in g.
+// of the current trial; block 0, state in g.  g.chg: the slot an accepted
+// move rewrote (the new ion's, or the deleted ion's that the last ion
+// fills), -1 otherwise.
 __device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint64_t cycle,
                        uint32_t attempt, GrandState &g) {
   const Trial &tr = g.s;
   const bool rf_on = (mask & 16u) && p.qrfpar;
   double dener = 0.0;
   if (tr.valid) dener = interact_total(p, tr, nblk, g.red, g.tot);
+  if (threadIdx.x == 0) g.chg = -1;
   if (threadIdx.x == 0 && tr.valid && !guard_bad(p.st, tr.ib - 1, p.nbuffer, 21)) {
     const int ib = tr.ib, b = ib - 1;
     const int nat = g.nat[b];
@@ -473,6 +617,7 @@ __device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint
           if (rf_on) p.gc_rf[ntot] = g.trial_rf;
           g.ntot = ntot + 1;
           g.ninsert[b] += 1;
+          g.chg = ntot;
         }
       } else if (!guard_bad(p.st, tr.j - 1, ntot, 23) &&
                  !guard_bad(p.st, ntot - 1, p.cap, 24)) {
@@ -487,6 +632,7 @@ __device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint
         if (rf_on) p.gc_rf[iat] = __ldcg(p.gc_rf + last);
         g.nat[b] = nat - 1;
         g.ntot = ntot - 1;
+        g.chg = iat;
       }
     }
   }
@@ -502,9 +648,16 @@ __global__ void __launch_bounds__(kGrandThreads)
   __shared__ int flag;
   DevState *st = p.st;
   const bool b0 = blockIdx.x == 0;
-  const int nthr = gridDim.x * blockDim.x;
-  const int gtid = threadIdx.x * gridDim.x + blockIdx.x;  // round-robin over blocks
-  if (b0) {  // GCMC state into shared memory
+  // particles round-robin over the blocks; with more than one block, block 0
+  // only coordinates (its proposals and acceptances stay off the ΔE sums)
+  const int nwb = gridDim.x > 1 ? gridDim.x - 1 : 1;
+  const bool owns = gridDim.x == 1 || !b0;
+  const int nthr = nwb * blockDim.x;
+  const int gtid = owns ? threadIdx.x * nwb + (gridDim.x > 1 ? blockIdx.x - 1 : 0) : nthr;
+  const bool rf_on = (mask & 16u) && p.qrfpar;
+  const int ntot0 = st->ntot;
+  bool ok = true;
+  if (b0) {  // GCMC state into shared memory, then the first proposal
     const int nb = p.nbuffer;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       g.nat[b] = st->nat[b];
@@ -524,33 +677,40 @@ __global__ void __launch_bounds__(kGrandThreads)
       g.qbias[ib] = p.qbufferbias[ib];
     }
     if (threadIdx.x == 0) {
-      g.ntot = st->ntot;
+      g.ntot = ntot0;
       g.dener_sum = st->dener_sum;
+      g.chg = -1;
+    }
+    __syncthreads();
+    if (ngcmc > 0) {
+      if (threadIdx.x == 0) propose_draws(p, seed, cycle, 0u, g);
+      propose_finish(p, mask, g);
+      if (threadIdx.x == 0) {
+        *p.trial = g.s;
+        release_add(&st->bar_gen, 1u);
+      }
     }
   }
-  const int ntot0 = st->ntot;
-  if ((mask & 16u) && p.qrfpar)  // RFPAR prepass, each thread its own particles
+  if (rf_on)  // RFPAR prepass, each thread its own particles
     for (int i = gtid; i < ntot0; i += nthr)
       if (i >= p.nsites) p.gc_rf[i] = rf_single(p, p.x[i], p.y[i], p.z[i], abs(p.typei[i]));
-  bool ok = true;
-  if (b0) {
-    propose(p, mask, seed, cycle, 0u, g);
-    if (threadIdx.x == 0) {
-      *p.trial = g.s;
-      release_add(&st->bar_gen, 1u);
-    }
-  }
+  // this thread's first particle, read ahead of each attempt
+  PartRec pre{};
+  if (gtid < ntot0) pre = load_part(p, gtid, rf_on);
   for (int a = 0; a < ngcmc && ok; ++a) {
     if (!b0 && !(ok = block_wait(&st->bar_gen, (unsigned)(a + 1), st, &flag))) break;
     const Trial tr = b0 ? g.s : load_trial_cg(p.trial);
     const int jt2 = trial_type2(p, tr);
     const bool beion = tr.valid && tr.j - 1 >= p.nsites;
     const bool rf = tr.valid && tr.rf_in && (mask & 16u);
+    if (gtid == tr.chg) pre = load_part(p, gtid, rf_on);  // rewritten by the last move
     double u = 0.0;
     int err = 0;
     if (jt2 > 0)
       for (int i = gtid; i < tr.ntot; i += nthr)
-        if (i != tr.j - 1) u += interact_one(p, tr, mask, i, jt2, beion, rf, err);
+        if (i != tr.j - 1)
+          u += i == gtid ? interact_rec(p, tr, mask, i, jt2, beion, rf, pre, err)
+                         : interact_one(p, tr, mask, i, jt2, beion, rf, err);
     if (err) atomicOr(&st->err, err);
     double *red = g.red, *tot = g.tot;
     block_sum<1>(&u, red, tot);
@@ -559,10 +719,15 @@ __global__ void __launch_bounds__(kGrandThreads)
       release_add(&st->bar_count, 1u);
     }
     if (b0) {
+      const bool more = a + 1 < ngcmc;
+      if (more) {  // the next attempt's draws (and insertion terms) meanwhile
+        if (threadIdx.x == 0) propose_draws(p, seed, cycle, (uint32_t)(a + 1), g);
+        next_terms(p, mask, g);
+      }
       if (!(ok = block_wait(&st->bar_count, (unsigned)(gridDim.x * (a + 1)), st, &flag))) break;
       accept(p, mask, gridDim.x, seed, cycle, (uint32_t)a, g);
-      if (a + 1 < ngcmc) {
-        propose(p, mask, seed, cycle, (uint32_t)(a + 1), g);
+      if (more) {
+        propose_finish(p, mask, g);
         if (threadIdx.x == 0) {
           *p.trial = g.s;
           release_add(&st->bar_gen, 1u);
@@ -602,7 +767,7 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
       return e;
     max_res[dev] = std::max(1, per_sm * nsm);
   }
-  int grid = (ntot_ub + ngcmc + 63) / 64;
+  int grid = (ntot_ub + ngcmc + 63) / 64 + 1;  // + block 0, the coordinator
   grid = std::max(1, std::min(std::min(grid, max_res[dev]), ipart_slots));
   // both launch counters start at zero
   if ((e = cudaMemsetAsync(&p.st->bar_count, 0, 2 * sizeof(unsigned), stream)) != cudaSuccess)

@@ -205,6 +205,35 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
             "speedup_vs_plain": value / plain}
 
 
+def pair_scaling(sh, peak_fp32, sizes=(2000, 4000, 8000), reps=10):
+    """The Newton-3 pair kernel alone on larger pores (the same maps and
+    laws), where the tile pairs outnumber the warps: its FP32 roofline
+    without the latency floor of the 2000-ion step.  CUDA events around
+    each launch (the library's kernel timers), after three warm-up calls."""
+    from bromoc_gb300 import _lib
+    maps = synth.pore_maps(seed=102)
+    out = []
+    for n in sizes:
+        spec = synth.pore(seed=3, nions=n, maps=maps, precision=abi.FP32, buffers=False)
+        g = _lib.create(n + 64, abi.FP32, sh)
+        spec.push(g)
+        for _ in range(3):
+            g.energy(abi.M_ALL, forces=True)
+        _lib.kernel_timing(g, True)
+        for _ in range(reps):
+            g.energy(abi.M_ALL, forces=True)
+        ms, nl = _lib.kernel_time(g, _lib.K_PAIRS)
+        _lib.kernel_timing(g, False)
+        n_ion = g.live_ntot()
+        pairs = n_ion * (n_ion - 1) / 2
+        t = ms / nl * 1e-3
+        a = (PAIR_FLOP + RF_FLOP) * pairs / t / 1e12
+        out.append({"ions": n_ion, "launch_us": t * 1e6, "achieved_tflops": a,
+                    "frac": a / peak_fp32})
+        del g
+    return out
+
+
 ADJ_N, ADJ_STEPS, ADJ_CKPT = 4096, 2000, 100
 
 
@@ -528,6 +557,7 @@ def run_gpu(args, rank, world, local_rank):
                 "frac": achieved / peaks["hbm_gbs"], "traffic": None,
                 "peak_source": src, "launch_ms": ms / nl,
                 "share": kt[dom][0] / tot_k}
+    scaling_pairs = pair_scaling(sh, peak_fp32)
     batched = batch_measure(sh, flush)
     adjoint = adjoint_measure(sh)
     cpu = oracle_baseline(float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15")))
@@ -550,6 +580,7 @@ def run_gpu(args, rank, world, local_rank):
                     "steps": e2e_steps,
                     "path": "bromoc_gpu_simul_cycles_host, pinned host arrays"},
             "gpu_launches": launches,
+            "pair_kernel_scaling": scaling_pairs,
             "batched": batched,
             "adjoint": adjoint,
             "wall_s": wall, "clocks": clocks}

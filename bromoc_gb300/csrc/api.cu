@@ -753,9 +753,11 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
         const PairParamF &f = pf[is];
         if (f.flags & kEfp) ok = false;
         const int fl = f.flags & 15;
+        // (fct, 6 epp4, sgp2, SRPMF cutoff on r^2 or -1): the LJ force takes
+        // 6 epp4; the SRPMF test is one compare
         tab[(size_t)a * nion + b] =
-            make_float4((fl & kChr) ? f.fct : 0.0f, (fl & kLj) ? f.epp4 : 0.0f,
-                        (fl & kLj) ? f.sgp2 : 0.0f, bits((is << 4) | fl));
+            make_float4((fl & kChr) ? f.fct : 0.0f, (fl & kLj) ? 6.0f * f.epp4 : 0.0f,
+                        (fl & kLj) ? f.sgp2 : 0.0f, (fl & kSrp) ? (float)p.rth : -1.0f);
       }
     float4 *dt = const_cast<float4 *>(p.ipq);
     if (!rc) rc = upload(ctx, &dt, tab.data(), std::max<size_t>(tab.size(), 1));

@@ -59,6 +59,7 @@ __global__ void __launch_bounds__(32 * kPairWarps)
                    tpb + (size_t)R.poff * 64, 0, 0, R.n, (R.n + 31) >> 5};
   float e[kRowTerms] = {0.f, 0.f, 0.f, 0.f, 0.f};
   n3_tile<true, RF, false>(p, ps, wk.y, 1, sh[w], sl[w], sq[w], acc[w], accb[w], tab, e);
+  e[1] *= 1.0f / 6.0f;  // the tile sums 6 x elj
   // the tile pair's energies -> its slot (fixed shuffle tree)
 #pragma unroll
   for (int k = 0; k < kRowTerms; ++k) {

@@ -167,9 +167,9 @@ __global__ void __launch_bounds__(kPairThreads)
             d6 = d6 * d6 * d6;
             const float d12 = d6 * d6;
             e[1] = fmaf(w, q.y * (d12 - d6), e[1]);
-            de = fmaf(cofo, ir2, (6.0f * q.y) * ir2 * fmaf(2.0f, d12, -d6));
-            const int qf = __float_as_int(q.w);
-            if ((qf & kSrp) && r2 <= p.rthf) de += srpmf32(p, qf >> 4, r2, ir, w, e);
+            de = ir2 * fmaf(q.y, fmaf(2.0f, d12, -d6), cofo);
+            if (r2 <= q.w)
+              de += srpmf32(p, srp_index(p, __float_as_int(th.w), code), r2, ir, w, e);
           }
         }
         if (RF && trf) {
@@ -217,7 +217,7 @@ __global__ void __launch_bounds__(kPairThreads)
     double *dst = p.epart + (size_t)(slot0 + blockIdx.y * gridDim.x + blockIdx.x) * kNTerms;
     for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
     dst[1] = tot[0];
-    dst[2] = tot[1];
+    dst[2] = EFP ? (double)tot[1] : (double)tot[1] / 6.0;  // dense table: 6 x elj
     dst[3] = tot[2];
     dst[4] = tot[3];
     dst[13] = tot[4];
@@ -251,7 +251,7 @@ __global__ void __launch_bounds__(32 * kN3Warps)
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
     for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
     dst[1] = tot[0];
-    dst[2] = tot[1];
+    dst[2] = EFP ? (double)tot[1] : (double)tot[1] / 6.0;  // dense table: 6 x elj
     dst[3] = tot[2];
     dst[4] = tot[3];
     dst[13] = tot[4];

@@ -68,9 +68,9 @@ struct KP {
   const float4 *ppk;
   const int *pidx;        // [nttyp*nttyp] 0-based pair index, -1 none
   // dense ion-ion law table for the FP32 pair kernel: [nion_t * nion_t] of
-  // (fct, epp4, sgp2, bits(is << 4 | flags)), fct/epp4 zeroed where the pair
-  // has no Coulomb/LJ term; ipq_ok when it applies (no tabulated ion-ion
-  // law, nion_t <= kIonTabTypes)
+  // (fct, 6 epp4, sgp2, rth or -1), fct/epp4 zeroed where the pair has no
+  // Coulomb/LJ term, rth (the SRPMF cutoff on r^2) where it has SRPMF;
+  // ipq_ok when it applies (no tabulated ion-ion law, nion_t <= kIonTabTypes)
   const float4 *ipq;
   int nion_t, ipq_ok;
   const double *ep;       // [3*cnt] reference form (p1,p2,p3)

@@ -25,6 +25,12 @@ namespace bgpu {
 // Output: per tile pair and side, per lane, (f, A) and B (tpf, tpb); the
 // assembly kernel sums a particle's row and column entries in fixed order.
 // ---------------------------------------------------------------------------
+// Pair index of two particles' type codes (only on the rare SRPMF branch:
+// the dense law table keeps the SRPMF cutoff, not the index).
+__device__ __forceinline__ int srp_index(const KP &p, int code_i, int code_j) {
+  return __ldg(p.pidx + (code_i & 0xffff) * p.nttyp + (code_j & 0xffff));
+}
+
 // The particle records and partial buffers of one system for the pair tile:
 // a context's own arrays, or one replica's slots and partials in a batch.
 struct PairSys {
@@ -43,7 +49,9 @@ __device__ __forceinline__ PairSys pair_sys(const KP &p, int ntot, int T) {
 // One tile pair q of the Newton-3 pair kernel, run by one warp (all 32
 // lanes).  sh/sl/sq/acc/accb: the warp's own 32-entry shared arrays; tab:
 // the block's dense ion-ion law table; e: the lane's energy sums (ecoul,
-// elj, esrpmf, eefpot, erfpar), added to.  p: the laws and constants.
+// elj, esrpmf, eefpot, erfpar), added to; without EFP the elj sum holds
+// 6 x elj (the dense table holds 6 epp4).
+// p: the laws and constants.
 template <bool II, bool RF, bool EFP>
 __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, int qforces,
                                         float4 *sh, float4 *sl, float4 *sq, float4 *acc,
@@ -128,9 +136,9 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
       d6 = d6 * d6 * d6;
       const float d12 = d6 * d6;
       e[1] = fmaf(c.y, d12 - d6, e[1]);
-      float de = fmaf(cofo, ir2, (6.0f * c.y) * ir2 * fmaf(2.0f, d12, -d6));
-      const int cf = __float_as_int(c.w);
-      if ((cf & kSrp) && r2 <= p.rthf) de += srpmf32(p, cf >> 4, r2, ir, 1.0f, e);
+      float de = ir2 * fmaf(c.y, fmaf(2.0f, d12, -d6), cofo);
+      if (r2 <= c.w)
+        de += srpmf32(p, srp_index(p, tcode, __float_as_int(h.w)), r2, ir, 1.0f, e);
       float4 a = ac[mm];
       if (RF) {
         const float4 u = sq[mm];
@@ -189,9 +197,8 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
             d6 = d6 * d6 * d6;
             const float d12 = d6 * d6;
             e[1] = fmaf(c.y, d12 - d6, e[1]);
-            dii = fmaf(cofo, ir2, (6.0f * c.y) * ir2 * fmaf(2.0f, d12, -d6));
-            const int cf = __float_as_int(c.w);
-            if ((cf & kSrp) && r2 <= p.rthf) dii += srpmf32(p, cf >> 4, r2, ir, 1.0f, e);
+            dii = ir2 * fmaf(c.y, fmaf(2.0f, d12, -d6), cofo);
+            if (r2 <= c.w) dii += srpmf32(p, srp_index(p, tcode, scode), r2, ir, 1.0f, e);
           }
         }
         if (RF) {

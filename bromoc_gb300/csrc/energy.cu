@@ -230,8 +230,8 @@ template <bool II, bool RF, bool EFP>
 __global__ void __launch_bounds__(32 * kN3Warps)
     k_pairs32n(KP p, int qforces, int slot0) {
   __shared__ float4 sh[kN3Warps][32], sl[kN3Warps][32], sq[kN3Warps][RF ? 32 : 1];
-  __shared__ float4 acc[kN3Warps][32];
-  __shared__ float accb[kN3Warps][RF ? 32 : 1];
+  __shared__ float4 acc[kN3Warps][32], acc1[kN3Warps][32];
+  __shared__ float accb[kN3Warps][RF ? 32 : 1], accb1[kN3Warps][RF ? 32 : 1];
   __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
   __shared__ float red[kN3Warps * 5];
   __shared__ float tot[5];
@@ -245,7 +245,7 @@ __global__ void __launch_bounds__(32 * kN3Warps)
   float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
   if (q < n3_pairs(T))  // warp-uniform
     n3_tile<II, RF, EFP>(p, pair_sys(p, p.st->ntot, T), q, qforces, sh[w], sl[w], sq[w],
-                         acc[w], accb[w], tab, e);
+                         acc[w], accb[w], acc1[w], accb1[w], tab, e);
   block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;

@@ -33,8 +33,8 @@ template <bool RF>
 union LoopSmem {
   struct {
     float4 sh[kLoopWarps][32], sl[kLoopWarps][32], sq[kLoopWarps][RF ? 32 : 1];
-    float4 acc[kLoopWarps][32];
-    float accb[kLoopWarps][RF ? 32 : 1];
+    float4 acc[kLoopWarps][32], acc1[kLoopWarps][32];
+    float accb[kLoopWarps][RF ? 32 : 1], accb1[kLoopWarps][RF ? 32 : 1];
   } pr;
   float part[kLoopWarps][10][32];
 };
@@ -43,7 +43,8 @@ template <bool II, bool RF, bool EFP>
 __global__ void __launch_bounds__(32 * kLoopWarps, 1)
     k_bd_loop(const __grid_constant__ KP p, AssembleFlags fl, uint32_t mask, int variant,
               uint64_t seed, uint64_t step0, int nsteps, int fields_first) {
-  __shared__ LoopSmem<RF> sm;
+  extern __shared__ __align__(16) unsigned char loop_dsm[];  // sizeof(LoopSmem<RF>)
+  LoopSmem<RF> &sm = *reinterpret_cast<LoopSmem<RF> *>(loop_dsm);
   __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
   __shared__ int flag;
   __shared__ AxisF ax[12];
@@ -77,7 +78,7 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
     float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int q = slot; q < npair; q += nslot)
       n3_tile<II, RF, EFP>(p, ps, q, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w], sm.pr.acc[w],
-                           sm.pr.accb[w], tab, e);
+                           sm.pr.accb[w], sm.pr.acc1[w], sm.pr.accb1[w], tab, e);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
     for (int it = blockIdx.x; it < nitem; it += G) {
       const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;
@@ -105,9 +106,14 @@ static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t 
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
   auto kern = k_bd_loop<II, RF, EFP>;
+  const size_t dsm = sizeof(LoopSmem<RF>);
   if (max_res[dev] == 0) {
     int per_sm = 0, nsm = 0;
-    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kLoopWarps, 0)) !=
+    if ((e = cudaFuncSetAttribute((const void *)kern,
+                                  cudaFuncAttributeMaxDynamicSharedMemorySize, (int)dsm)) !=
+        cudaSuccess)
+      return e;
+    if ((e = cudaOccupancyMaxActiveBlocksPerMultiprocessor(&per_sm, kern, 32 * kLoopWarps, dsm)) !=
         cudaSuccess)
       return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
@@ -125,7 +131,7 @@ static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t 
   void *args[] = {(void *)&pc, (void *)&fc, (void *)&mask, (void *)&variant,
                   (void *)&seed, (void *)&step0, (void *)&nsteps, (void *)&fields_first};
   return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(32 * kLoopWarps), args,
-                                     0, stream);
+                                     dsm, stream);
 }
 
 bool bd_loop_supported(const KP &p, const AssembleFlags &fl) {

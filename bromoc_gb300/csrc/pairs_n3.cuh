@@ -25,6 +25,9 @@ namespace bgpu {
 // Output: per tile pair and side, per lane, (f, A) and B (tpf, tpb); the
 // assembly kernel sums a particle's row and column entries in fixed order.
 // ---------------------------------------------------------------------------
+// Systems up to this many ion tiles run the pair tile's two-chain loop.
+constexpr int kN3DualTiles = 96;
+
 // Pair index of two particles' type codes (only on the rare SRPMF branch:
 // the dense law table keeps the SRPMF cutoff, not the index).
 __device__ __forceinline__ int srp_index(const KP &p, int code_i, int code_j) {
@@ -47,7 +50,8 @@ __device__ __forceinline__ PairSys pair_sys(const KP &p, int ntot, int T) {
 }
 
 // One tile pair q of the Newton-3 pair kernel, run by one warp (all 32
-// lanes).  sh/sl/sq/acc/accb: the warp's own 32-entry shared arrays; tab:
+// lanes).  sh/sl/sq/acc/accb/acc1/accb1: the warp's own 32-entry shared
+// arrays; tab:
 // the block's dense ion-ion law table; e: the lane's energy sums (ecoul,
 // elj, esrpmf, eefpot, erfpar), added to; without EFP the elj sum holds
 // 6 x elj (the dense table holds 6 epp4).
@@ -55,7 +59,8 @@ __device__ __forceinline__ PairSys pair_sys(const KP &p, int ntot, int T) {
 template <bool II, bool RF, bool EFP>
 __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, int qforces,
                                         float4 *sh, float4 *sl, float4 *sq, float4 *acc,
-                                        float *accb, const float4 *tab, float e[5]) {
+                                        float *accb, float4 *acc1, float *accb1,
+                                        const float4 *tab, float e[5]) {
   const int lane = threadIdx.x & 31;
   const int nt = p.nion_t;
   const int T = ps.T, ntot = ps.ntot;
@@ -88,7 +93,8 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
     if (RF) sq[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
   }
   acc[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
-  if (RF) accb[lane] = 0.f;
+  acc1[lane] = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (RF) accb[lane] = accb1[lane] = 0.f;
   iv = i < ntot;
   float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th, tq = th;
   if (iv) {
@@ -116,60 +122,96 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
               (jl >= ntot || (sb0 & 12) == 12 || !(sb0 & 1));
   }
   const bool fast = II && !EFP && !diag && __all_sync(0xffffffffu, lane_ok);
-  auto fast_loop = [&](auto rag) {
+  // One pair of the branch-free loop: row lane against column entry mm, its
+  // terms into the row sums (gx, gy, gz, gA, gB, ge) and into the column
+  // sums ac[mm], acb[mm].
+  auto pair_step = [&](auto rag, int mm, float4 *ac, float *acb, float &gx, float &gy,
+                       float &gz, float &gA, float &gB, float *ge) {
     constexpr bool RAG = decltype(rag)::value;
+    const float4 h = sh[mm], l = sl[mm];
+    const float dx = (th.x - h.x) + (tl.x - l.x);
+    const float dy = (th.y - h.y) + (tl.y - l.y);
+    const float dz = (th.z - h.z) + (tl.z - l.z);
+    const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+    float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
+    if (RAG && mm >= ncol) c = make_float4(0.f, 0.f, c.z, 0.f);
+    const float ir = rsqrt_nz(r2), ir2 = ir * ir;
+    const float cofo = c.x * ir;
+    ge[0] += cofo;
+    float d6 = c.z * ir2;
+    d6 = d6 * d6 * d6;
+    const float d12 = d6 * d6;
+    ge[1] = fmaf(c.y, d12 - d6, ge[1]);
+    float de = ir2 * fmaf(c.y, fmaf(2.0f, d12, -d6), cofo);
+    if (r2 <= c.w)
+      de += srpmf32(p, srp_index(p, tcode, __float_as_int(h.w)), r2, ir, 1.0f, ge);
+    float4 a = ac[mm];
+    if (RF) {
+      const float4 u = sq[mm];
+      const float rij = u.x * rft, srij = l.w * srt;
+      const float rfdn = rsqrt_nz(fmaf(rij, rij, r2));
+      const float aux0 = ct * u.y;
+      const float a1 = aux0 * rij * rfdn;
+      ge[4] = fmaf(a1, srij, ge[4]);
+      const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
+      const float aux3 = -a2 * fmaf(rij, 0.5f, r2);
+      gA = fmaf(-a1, l.w, gA);
+      gB = fmaf(aux3, u.x, gB);
+      a.w = fmaf(-a1, srt, a.w);
+      acb[mm] = fmaf(aux3, rft, acb[mm]);
+      de = fmaf(a2, rij, de);
+    }
+    gx = fmaf(de, dx, gx);
+    gy = fmaf(de, dy, gy);
+    gz = fmaf(de, dz, gz);
+    a.x = fmaf(-de, dx, a.x);
+    a.y = fmaf(-de, dy, a.y);
+    a.z = fmaf(-de, dz, a.z);
+    ac[mm] = a;
+  };
+  // Two independent chains per step, k and k + 16, each with its own row
+  // and column sums (acc / acc1): in one step both touch 32 distinct column
+  // entries of their own arrays; the halves meet at the end.  Small systems
+  // (T <= kN3DualTiles: about one tile pair per warp, latency-bound) take
+  // it; larger ones, issue-bound, keep the single chain.  The choice depends
+  // on T alone, so every kernel running a system of T tiles sums alike.
+  auto fast_loop_dual = [&](auto rag) {
+    float fx1 = 0.f, fy1 = 0.f, fz1 = 0.f, A1 = 0.f, B1 = 0.f;
+    float e1[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    for (int k = 0; k < 16; ++k) {
+      pair_step(rag, (lane + k) & 31, acc, accb, fx, fy, fz, A, B, e);
+      pair_step(rag, (lane + k + 16) & 31, acc1, accb1, fx1, fy1, fz1, A1, B1, e1);
+      __syncwarp();
+    }
+    fx += fx1;
+    fy += fy1;
+    fz += fz1;
+    A += A1;
+    B += B1;
+#pragma unroll
+    for (int m = 0; m < 5; ++m) e[m] += e1[m];
+    const float4 a0 = acc[lane], a1 = acc1[lane];  // this lane's column entry
+    acc[lane] = make_float4(a0.x + a1.x, a0.y + a1.y, a0.z + a1.z, a0.w + a1.w);
+    if (RF) accb[lane] += accb1[lane];
+  };
+  auto fast_loop = [&](auto rag) {
     for (int k = 0; k < 32; ++k) {
-      const int mm = (lane + k) & 31;
-      float4 *ac = acc;
-      float *acb = accb;
-      const float4 h = sh[mm], l = sl[mm];
-      const float dx = (th.x - h.x) + (tl.x - l.x);
-      const float dy = (th.y - h.y) + (tl.y - l.y);
-      const float dz = (th.z - h.z) + (tl.z - l.z);
-      const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
-      if (RAG && mm >= ncol) c = make_float4(0.f, 0.f, c.z, 0.f);
-      const float ir = rsqrt_nz(r2), ir2 = ir * ir;
-      const float cofo = c.x * ir;
-      e[0] += cofo;
-      float d6 = c.z * ir2;
-      d6 = d6 * d6 * d6;
-      const float d12 = d6 * d6;
-      e[1] = fmaf(c.y, d12 - d6, e[1]);
-      float de = ir2 * fmaf(c.y, fmaf(2.0f, d12, -d6), cofo);
-      if (r2 <= c.w)
-        de += srpmf32(p, srp_index(p, tcode, __float_as_int(h.w)), r2, ir, 1.0f, e);
-      float4 a = ac[mm];
-      if (RF) {
-        const float4 u = sq[mm];
-        const float rij = u.x * rft, srij = l.w * srt;
-        const float rfdn = rsqrt_nz(fmaf(rij, rij, r2));
-        const float aux0 = ct * u.y;
-        const float a1 = aux0 * rij * rfdn;
-        e[4] = fmaf(a1, srij, e[4]);
-        const float a2 = aux0 * srij * rfdn * rfdn * rfdn;
-        const float aux3 = -a2 * fmaf(rij, 0.5f, r2);
-        A = fmaf(-a1, l.w, A);
-        B = fmaf(aux3, u.x, B);
-        a.w = fmaf(-a1, srt, a.w);
-        acb[mm] = fmaf(aux3, rft, acb[mm]);
-        de = fmaf(a2, rij, de);
-      }
-      fx = fmaf(de, dx, fx);
-      fy = fmaf(de, dy, fy);
-      fz = fmaf(de, dz, fz);
-      a.x = fmaf(-de, dx, a.x);
-      a.y = fmaf(-de, dy, a.y);
-      a.z = fmaf(-de, dz, a.z);
-      ac[mm] = a;
+      pair_step(rag, (lane + k) & 31, acc, accb, fx, fy, fz, A, B, e);
       __syncwarp();
     }
   };
   if (fast) {
-    if (ncol < 32)
-      fast_loop(cuda::std::true_type{});
-    else
-      fast_loop(cuda::std::false_type{});
+    if (T <= kN3DualTiles) {
+      if (ncol < 32)
+        fast_loop_dual(cuda::std::true_type{});
+      else
+        fast_loop_dual(cuda::std::false_type{});
+    } else {
+      if (ncol < 32)
+        fast_loop(cuda::std::true_type{});
+      else
+        fast_loop(cuda::std::false_type{});
+    }
   } else {
     const int k0 = diag ? 1 : 0, k1 = diag ? 16 : 31;
     for (int k = k0; k <= k1; ++k) {

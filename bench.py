@@ -412,11 +412,11 @@ def run_gpu(args, rank, world, local_rank):
     for c in range(1, args.warmup + 1):
         step(c)
     torch.cuda.synchronize()
-    # particle counts per step (GCMC changes ntot): read before each step
-    # outside the events
     ev = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True))
           for _ in range(args.steps)]
-    nmob = []
+    # the mobile count of each cycle (after its GRAND) is copied to pinned
+    # memory on the stream, so the host never waits inside the loop
+    counts = torch.zeros(args.steps, dtype=torch.int32, pin_memory=True)
     l0 = _lib.launch_count(eng)
     if dist:
         dist.barrier()
@@ -424,13 +424,16 @@ def run_gpu(args, rank, world, local_rank):
     with ClockSampler(local_rank) as clk:
         w0 = time.perf_counter()
         for k in range(args.steps):
-            nmob.append(eng.live_ntot() - nfix)
+            cyc = args.warmup + 1 + k
             flush.zero_()
             ev[k][0].record(stream)
-            step(args.warmup + 1 + k)
+            eng.grand(NGCMC, SEED, cyc, dener=False)
+            _lib.live_count_async(eng, counts.data_ptr() + 4 * k)
+            eng.bd_steps(NBD, SEED, (cyc - 1) * NBD, energies=False)
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0
+    nmob = [int(c) - nfix for c in counts.tolist()]
     launches = _lib.launch_count(eng) - l0
     t_ms = sum(a.elapsed_time(b) for a, b in ev)
     ps = NBD * sum(nmob)

@@ -38,6 +38,8 @@ def load() -> C.CDLL:
         lib.bromoc_gpu_launch_count.restype = C.c_int64
         lib.bromoc_gpu_kernel_timing.argtypes = [C.c_void_p, C.c_int32]
         lib.bromoc_gpu_kernel_timing.restype = C.c_int
+        lib.bromoc_gpu_live_count_async.argtypes = [C.c_void_p, C.c_void_p]
+        lib.bromoc_gpu_live_count_async.restype = C.c_int
         lib.bromoc_gpu_set_fused_bd.argtypes = [C.c_void_p, C.c_int32]
         lib.bromoc_gpu_set_fused_bd.restype = C.c_int
         lib.bromoc_gpu_kernel_time.argtypes = [C.c_void_p, C.c_int32, d,
@@ -101,6 +103,13 @@ def efpot_from_knots(r, u, fct, qchr):
 
 
 K_PAIRS, K_RFCROSS, K_FIELDS, K_ASSEMBLE, K_LOOP = 0, 1, 2, 3, 4
+
+
+def live_count_async(eng: abi.Engine, dst_ptr: int) -> None:
+    """Enqueue a copy of the live particle count to the pinned int32 at
+    dst_ptr; it holds the value once the context's stream has synchronised."""
+    eng._chk(load().bromoc_gpu_live_count_async(eng.h, C.c_void_p(dst_ptr)),
+             "live_count_async")
 
 
 def set_fused_bd(eng: abi.Engine, on: bool) -> None:

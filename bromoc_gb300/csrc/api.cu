@@ -1320,6 +1320,13 @@ int64_t bromoc_gpu_launch_count(const bromoc_ctx *ctx) {
   return ctx ? (int64_t)ctx->launches : -1;
 }
 
+int bromoc_gpu_live_count_async(bromoc_ctx *ctx, int32_t *dst) {
+  if (!ctx || !dst) return BROMOC_E_ARG;
+  CU(cudaMemcpyAsync(dst, &ctx->kp.st->ntot, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  return BROMOC_OK;
+}
+
 int bromoc_gpu_set_fused_bd(bromoc_ctx *ctx, int32_t on) {
   if (!ctx) return BROMOC_E_ARG;
   ctx->fused_bd = on != 0;

@@ -313,6 +313,11 @@ int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t nfix,
 
 /* Number of kernels this context has launched so far. */
 int64_t bromoc_gpu_launch_count(const bromoc_ctx *ctx);
+/* The live particle count as the context's stream reaches this call, copied
+ * to *dst (pinned host memory) without waiting: valid once the stream has
+ * synchronised.  A driver that records the count every cycle need not stop
+ * the GPU.  No counterpart in the reference (its count is a host global). */
+int bromoc_gpu_live_count_async(bromoc_ctx *ctx, int32_t *dst);
 
 /* ---- diagnostics (no counterpart in the reference) ----------------------
  * Per-kernel timing with CUDA events recorded on the launching stream around

@@ -132,3 +132,19 @@ def test_loop_pore_sizes(gpu_lib, nions):
     ta, _, _ = a.energy(abi.M_ALL, forces=False)
     tb, _, _ = b.energy(abi.M_ALL, forces=False)
     assert ta == tb
+
+
+def test_live_count_async(gpu_lib):
+    """The count copied on the stream without a wait equals the synchronous
+    read, cycle by cycle through GRAND."""
+    import ctypes as C
+    spec = systems.gcmc(precision=abi.FP32)
+    g = _engine(gpu_lib, spec, True)
+    got = (C.c_int32 * 8)()
+    want = []
+    for cyc in range(1, 9):
+        g.grand(6, 99, cyc, dener=False)
+        _lib.live_count_async(g, C.addressof(got) + 4 * (cyc - 1))
+        g.bd_steps(2, seed=5, step0=2 * cyc, energies=False)
+        want.append(g.live_ntot())
+    assert list(got) == want

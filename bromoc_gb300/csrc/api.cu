@@ -1259,11 +1259,19 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   KP &p = ctx->kp;
   if (ngcmc < 0 || cycle < 1) return set_err(ctx, BROMOC_E_ARG, "grand: bad ngcmc or cycle");
   if (p.nbuffer < 1) return set_err(ctx, BROMOC_E_STATE, "grand: no buffers");
-  if ((rc = ensure_dbl(ctx))) return rc;
-  if (ngcmc > 0) ctx->ff_fresh = false;  // GCMC edits the FP64 arrays
+  // FP32 mode: GRAND works on the float-float records (the current
+  // positions while BD runs), FP64 mode on the FP64 arrays
+  const bool ff = ctx->precision == BROMOC_FP32;
+  if ((rc = ff ? ensure_ff(ctx) : ensure_dbl(ctx))) return rc;
+  if (ngcmc > 0) {
+    if (ff)
+      ctx->dbl_fresh = false;
+    else
+      ctx->ff_fresh = false;
+  }
   CU(cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), ctx->stream));
   if (ngcmc > 0) {
-    CU(launch_grand(p, ntot_ub(ctx), ctx->ipart_slots, terms, seed, cycle, ngcmc,
+    CU(launch_grand(p, ntot_ub(ctx), ctx->ipart_slots, terms, seed, cycle, ngcmc, ff ? 1 : 0,
                     ctx->stream));
     ctx->launches += 1;
     ctx->attempts_total += ngcmc;

@@ -82,7 +82,8 @@ __global__ void __launch_bounds__(32 * kAsmTileWarps, 2)
   const int2 tk = tiles[blockIdx.x];
   const RepDev &R = rep[tk.x];
   const size_t o = R.off;
-  const AsmSys ms{p.pk1 + o, p.pk2 + o, p.typei + o, p.ffield_f + o, nullptr, p.rfd + 2 * o,
+  const AsmSys ms{p.pk1 + o, p.pk2 + o, p.pk3 + o, p.typei + o, p.ffield_f + o, nullptr,
+                  p.rfd + 2 * o,
                   tpf + (size_t)R.poff * 64, tpb + (size_t)R.poff * 64, p.cap, 0, 0, R.n,
                   (R.n + 31) >> 5, R.seed, &R.box,
                   fout ? fout + 3 * o : nullptr, fout ? fout + 3 * o + 1 : nullptr,

@@ -62,17 +62,18 @@ __device__ __forceinline__ void stage_axes(const KP &p, AxisF *ax) {
 }
 
 // ax: the block's staged copy of p.f.ax (stage_axes); pos: when given, the
-// particle's position records {hi, lo} (else read from pk1 / pk2).
+// particle's position records {hi, lo} and {charge, ion type bits} (else
+// read from pk1 / pk2 / pk3 / typei).
 __device__ __forceinline__ void fields_one_f32(const KP &p, int i, bool site, bool fixed,
                                                uint32_t mask, int qforces, float eo[4],
                                                const AxisF *ax, const float4 *pos = nullptr) {
   const int lane = threadIdx.x & 31;
   const float4 h4 = pos ? pos[0] : p.pk1[i], l4 = pos ? pos[1] : p.pk2[i];
-  const float charge = p.pk3[i].y;
+  const float charge = pos ? pos[2].x : p.pk3[i].y;
   const int code = __float_as_int(h4.w);
   const int itype2 = (code & 0xffff) + 1;
   const int mobile = (code >> 16) & 1;
-  const int iontype = site ? 0 : abs(p.typei[i]);
+  const int iontype = site ? 0 : (pos ? __float_as_int(pos[2].y) : abs(p.typei[i]));
   const bool qf = qforces != 0;
   // ---- per-(grid, axis) cells, float-float, lanes 0..11 -----------------
   int cix = 0, cin = 0;

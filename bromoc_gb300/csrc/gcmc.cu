@@ -178,12 +178,25 @@ struct PartRec {
   int ti;
 };
 
-__device__ __forceinline__ PartRec load_part(const KP &p, int i, bool rf) {
+// Position of particle i: the FP64 arrays, or (ff, FP32 mode) the
+// float-float records as hi + lo in FP64, the value the records stand for.
+// Read past L1.
+__device__ __forceinline__ double3 pos_of(const KP &p, bool ff, int i) {
+  if (ff) {
+    const float4 h = __ldcg(p.pk1 + i), l = __ldcg(p.pk2 + i);
+    return make_double3((double)h.x + (double)l.x, (double)h.y + (double)l.y,
+                        (double)h.z + (double)l.z);
+  }
+  return make_double3(__ldcg(p.x + i), __ldcg(p.y + i), __ldcg(p.z + i));
+}
+
+__device__ __forceinline__ PartRec load_part(const KP &p, int i, bool rf, bool ff = false) {
   PartRec r;
   r.ti = __ldcg(p.typei + i);
-  r.x = __ldcg(p.x + i);
-  r.y = __ldcg(p.y + i);
-  r.z = __ldcg(p.z + i);
+  const double3 q = pos_of(p, ff, i);
+  r.x = q.x;
+  r.y = q.y;
+  r.z = q.z;
   r.rf = rf && i >= p.nsites ? __ldcg(p.gc_rf + i) : make_double2(0.0, 0.0);
   return r;
 }
@@ -220,8 +233,8 @@ __device__ double interact_rec(const KP &p, const Trial &tr, uint32_t mask, int 
 }
 
 __device__ double interact_one(const KP &p, const Trial &tr, uint32_t mask, int i, int jt2,
-                               bool beion, bool rf, int &err) {
-  return interact_rec(p, tr, mask, i, jt2, beion, rf, load_part(p, i, rf), err);
+                               bool beion, bool rf, int &err, bool ff = false) {
+  return interact_rec(p, tr, mask, i, jt2, beion, rf, load_part(p, i, rf, ff), err);
 }
 
 // Combined type of the trial particle, 0 (and a guard record) when invalid.
@@ -318,7 +331,9 @@ void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
 // names its slot as the one the last accepted move rewrote.  Block 0
 // proposes the first attempt before its share of the RFPAR prepass.  Data
 // that another block wrote during the launch are read past L1 (__ldcg).
-// With more than one block, block 0 owns no particles.
+// With more than one block, block 0 owns no particles.  In FP32 mode
+// (ffpos) the positions are read from and written to the float-float
+// records, so no conversion kernel runs around the call.
 // Every wait is bounded: it gives up after kWaitSpins polls, or as soon as
 // another block has given up, records kErrBarrier and the launch returns.
 // The draws, the proposals and their outcomes are those of proposing
@@ -337,6 +352,7 @@ struct GrandState {
                             // before the pending acceptance)
   int nx_alert;             // warnings of that deletion trial, not yet counted
   int chg;                  // slot the last accepted move rewrote, -1 none
+  int ff;                   // FP32 mode: positions live in the float-float records
   int ntot;
   int nat[kMaxBuffers], ninsert[kMaxBuffers], nremove[kMaxBuffers], ntotat[kMaxBuffers];
   double dener_sum;
@@ -486,9 +502,10 @@ __device__ void next_terms(const KP &p, uint32_t mask, GrandState &g) {
   t.itype = g.ibfftyp[ib];
   t.valid = 1;
   t.j = k + 1;
-  t.x = p.x[k];
-  t.y = p.y[k];
-  t.z = p.z[k];
+  const double3 q = pos_of(p, g.ff, k);
+  t.x = q.x;
+  t.y = q.y;
+  t.z = q.z;
   if (threadIdx.x == 0) g.nx_alert = 0;
   __syncthreads();
   if (threadIdx.x < 32) {
@@ -545,9 +562,10 @@ __device__ void propose_finish(const KP &p, uint32_t mask, GrandState &g) {
         atomicOr(&p.st->err, kErrFind);
       } else {
         g.s.j = k + 1;
-        g.s.x = p.x[k];
-        g.s.y = p.y[k];
-        g.s.z = p.z[k];
+        const double3 q = pos_of(p, g.ff, k);
+        g.s.x = q.x;
+        g.s.y = q.y;
+        g.s.z = q.z;
       }
     }
     __syncthreads();
@@ -609,9 +627,18 @@ __device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint
         } else if (!guard_bad(p.st, ntot, p.cap, 22)) {
           g.dener_sum += dener;
           g.nat[b] = nat + 1;
-          p.x[ntot] = tr.x;
-          p.y[ntot] = tr.y;
-          p.z[ntot] = tr.z;
+          if (g.ff) {  // the records as k_pack forms them (a mobile ion)
+            const float xh = (float)tr.x, yh = (float)tr.y, zh = (float)tr.z;
+            const int code = (p.nwtype[tr.itype] - 1) | (1 << 16);
+            p.pk1[ntot] = make_float4(xh, yh, zh, __int_as_float(code));
+            p.pk2[ntot] = make_float4((float)(tr.x - (double)xh), (float)(tr.y - (double)yh),
+                                      (float)(tr.z - (double)zh), 0.0f);
+            p.pk3[ntot] = make_float4(0.0f, (float)p.cg[tr.itype], __int_as_float(1 << 1), 0.0f);
+          } else {
+            p.x[ntot] = tr.x;
+            p.y[ntot] = tr.y;
+            p.z[ntot] = tr.z;
+          }
           p.typei[ntot] = tr.z < p.cz ? -tr.itype : tr.itype;
           p.ibuffer[ntot] = ib;
           if (rf_on) p.gc_rf[ntot] = g.trial_rf;
@@ -624,9 +651,15 @@ __device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint
         const int iat = tr.j - 1, last = ntot - 1;
         g.dener_sum -= dener;
         g.nremove[b] += 1;
-        p.x[iat] = p.x[last];
-        p.y[iat] = p.y[last];
-        p.z[iat] = p.z[last];
+        if (g.ff) {
+          p.pk1[iat] = __ldcg(p.pk1 + last);
+          p.pk2[iat] = __ldcg(p.pk2 + last);
+          p.pk3[iat] = __ldcg(p.pk3 + last);
+        } else {
+          p.x[iat] = p.x[last];
+          p.y[iat] = p.y[last];
+          p.z[iat] = p.z[last];
+        }
         p.typei[iat] = p.typei[last];
         p.ibuffer[iat] = p.ibuffer[last];
         if (rf_on) p.gc_rf[iat] = __ldcg(p.gc_rf + last);
@@ -643,7 +676,7 @@ __device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint
 }
 
 __global__ void __launch_bounds__(kGrandThreads)
-    k_grand(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, int ngcmc) {
+    k_grand(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, int ngcmc, int ffpos) {
   __shared__ GrandState g;
   __shared__ int flag;
   DevState *st = p.st;
@@ -680,6 +713,7 @@ __global__ void __launch_bounds__(kGrandThreads)
       g.ntot = ntot0;
       g.dener_sum = st->dener_sum;
       g.chg = -1;
+      g.ff = ffpos;
     }
     __syncthreads();
     if (ngcmc > 0) {
@@ -693,24 +727,27 @@ __global__ void __launch_bounds__(kGrandThreads)
   }
   if (rf_on)  // RFPAR prepass, each thread its own particles
     for (int i = gtid; i < ntot0; i += nthr)
-      if (i >= p.nsites) p.gc_rf[i] = rf_single(p, p.x[i], p.y[i], p.z[i], abs(p.typei[i]));
+      if (i >= p.nsites) {
+        const double3 q = pos_of(p, ffpos, i);
+        p.gc_rf[i] = rf_single(p, q.x, q.y, q.z, abs(p.typei[i]));
+      }
   // this thread's first particle, read ahead of each attempt
   PartRec pre{};
-  if (gtid < ntot0) pre = load_part(p, gtid, rf_on);
+  if (gtid < ntot0) pre = load_part(p, gtid, rf_on, ffpos);
   for (int a = 0; a < ngcmc && ok; ++a) {
     if (!b0 && !(ok = block_wait(&st->bar_gen, (unsigned)(a + 1), st, &flag))) break;
     const Trial tr = b0 ? g.s : load_trial_cg(p.trial);
     const int jt2 = trial_type2(p, tr);
     const bool beion = tr.valid && tr.j - 1 >= p.nsites;
     const bool rf = tr.valid && tr.rf_in && (mask & 16u);
-    if (gtid == tr.chg) pre = load_part(p, gtid, rf_on);  // rewritten by the last move
+    if (gtid == tr.chg) pre = load_part(p, gtid, rf_on, ffpos);  // rewritten by the last move
     double u = 0.0;
     int err = 0;
     if (jt2 > 0)
       for (int i = gtid; i < tr.ntot; i += nthr)
         if (i != tr.j - 1)
           u += i == gtid ? interact_rec(p, tr, mask, i, jt2, beion, rf, pre, err)
-                         : interact_one(p, tr, mask, i, jt2, beion, rf, err);
+                         : interact_one(p, tr, mask, i, jt2, beion, rf, err, ffpos);
     if (err) atomicOr(&st->err, err);
     double *red = g.red, *tot = g.tot;
     block_sum<1>(&u, red, tot);
@@ -752,7 +789,8 @@ __global__ void __launch_bounds__(kGrandThreads)
 // Blocks of the GRAND launch: about one per 64 particles, all co-resident,
 // at most the ipart slots the context holds (ipart_slots).
 cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
-                         uint64_t seed, uint64_t cycle, int ngcmc, cudaStream_t stream) {
+                         uint64_t seed, uint64_t cycle, int ngcmc, int ffpos,
+                         cudaStream_t stream) {
   static int max_res[64] = {};
   int dev = 0;
   cudaError_t e = cudaGetDevice(&dev);
@@ -773,7 +811,8 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
   if ((e = cudaMemsetAsync(&p.st->bar_count, 0, 2 * sizeof(unsigned), stream)) != cudaSuccess)
     return e;
   KP pc = p;
-  void *args[] = {(void *)&pc, (void *)&mask, (void *)&seed, (void *)&cycle, (void *)&ngcmc};
+  void *args[] = {(void *)&pc, (void *)&mask, (void *)&seed, (void *)&cycle, (void *)&ngcmc,
+                  (void *)&ffpos};
   return cudaLaunchCooperativeKernel((const void *)k_grand, dim3(grid), dim3(kGrandThreads),
                                      args, 0, stream);
 }

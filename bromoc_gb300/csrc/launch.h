@@ -83,8 +83,10 @@ cudaError_t launch_bd_loop(const KP &p, const AssembleFlags &fl, int ntot_ub, ui
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream);
 // GRAND: ngcmc attempts in one cooperative launch (gcmc.cu)
+// ffpos: FP32 mode, positions in the float-float records (pk1, pk2)
 cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
-                         uint64_t seed, uint64_t cycle, int ngcmc, cudaStream_t stream);
+                         uint64_t seed, uint64_t cycle, int ngcmc, int ffpos,
+                         cudaStream_t stream);
 int interact_slots(int ntot_ub);
 
 }  // namespace bgpu

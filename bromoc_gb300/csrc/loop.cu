@@ -48,7 +48,7 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
   __shared__ int flag;
   __shared__ AxisF ax[12];
-  __shared__ float4 npos[32][2];  // phase A: the moved records of the tile
+  __shared__ float4 npos[32][3];  // phase A: the moved records of the tile
   stage_axes(p, ax);
   const int nt = p.nion_t;
   if (II && !EFP)

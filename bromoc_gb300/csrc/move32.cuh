@@ -116,6 +116,7 @@ __device__ __forceinline__ void diff_model(const KP &p, int variant, int i, int 
 // i counted from the system's first particle.
 struct AsmSys {
   float4 *pk1, *pk2;
+  const float4 *pk3;
   const int *typei;
   const float *ffield, *fis;
   const float4 *rfd;
@@ -129,7 +130,7 @@ struct AsmSys {
 };
 
 __device__ __forceinline__ AsmSys ctx_asm_sys(const KP &p, int T, uint64_t seed) {
-  return AsmSys{p.pk1, p.pk2, p.typei, p.ffield_f, p.fis_f, p.rfd, p.tpf, p.tpb, p.cap,
+  return AsmSys{p.pk1, p.pk2, p.pk3, p.typei, p.ffield_f, p.fis_f, p.rfd, p.tpf, p.tpb, p.cap,
                 p.nsites, p.nfix, p.st->ntot, T, seed, &p.f.box, p.fx, p.fy, p.fz, 1};
 }
 
@@ -140,6 +141,7 @@ struct MoveIn {
   float4 h4, l4;  // position hi / lo records
   float g[3];     // Gaussian noise of this step
   float2 fa;      // (fact1, fact2) of dynamics0
+  float charge;   // from the pk3 record
   int itype;      // ion type, 0 for a site
   bool moves;     // false for fixed ions and frozen sites
 };
@@ -154,6 +156,7 @@ __device__ __forceinline__ MoveIn move_in_f32(const KP &p, const AsmSys &ms, int
   m.h4 = ms.pk1[i];
   m.l4 = ms.pk2[i];
   m.itype = i < ms.nsites ? 0 : abs(__ldg(ms.typei + i));
+  m.charge = __ldcg(&ms.pk3[i].y);
   m.fa = variant == 0 && i >= ms.nsites ? __ldg(p.fact_f + m.itype) : make_float2(0.f, 0.f);
   if (noise) bd_noise3_f(ms.seed, step, (uint32_t)i, m.g);
   return m;
@@ -237,13 +240,13 @@ __device__ __forceinline__ void bd_move_f32(const KP &p, int variant, uint64_t s
 // lanes 16 half .. 16 half + 15 assemble and move (two blocks share a tile).
 // Warp 1 draws their noise while warp 0 gathers their other inputs.
 // npos: when given, warp 0 leaves each of those particles' records there
-// (npos[lane] = {hi, lo}, after the move).  Every thread of the block calls it.
+// (npos[lane] = {hi, lo} after the move, {charge, ion type bits, 0, 0}).  Every thread of the block calls it.
 template <int NW>
 __device__ __forceinline__ void assemble_tile(const KP &p, const AsmSys &ms,
                                               const AssembleFlags &fl, int do_bd, int variant,
                                               uint64_t step, int blk, int site_blocks,
                                               float (*part)[10][32], int half = -1,
-                                              float4 (*npos)[2] = nullptr) {
+                                              float4 (*npos)[3] = nullptr) {
   const int w = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const bool ionblk = blk >= site_blocks;
   const int Ti = blk - site_blocks;
@@ -357,6 +360,7 @@ __device__ __forceinline__ void assemble_tile(const KP &p, const AsmSys &ms,
   if (npos) {
     npos[lane][0] = mv.h4;
     npos[lane][1] = mv.l4;
+    npos[lane][2] = make_float4(mv.charge, __int_as_float(mv.itype), 0.f, 0.f);
   }
 }
 

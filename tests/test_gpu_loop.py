@@ -148,3 +148,31 @@ def test_live_count_async(gpu_lib):
         g.bd_steps(2, seed=5, step0=2 * cyc, energies=False)
         want.append(g.live_ntot())
     assert list(got) == want
+
+
+def test_fp32_grand_on_records_matches_oracle(gpu_lib, oracle_mod):
+    """FP32 mode runs GRAND on the float-float records (no conversion
+    kernels): the same insertions and deletions as the FP64 oracle, counter
+    for counter, with energy sums and positions equal to within the records'
+    ~48-bit precision; interleaved BD steps keep the records authoritative."""
+    spec = systems.gcmc(precision=abi.FP32)
+    g = _engine(gpu_lib, spec, True)
+    o = oracle_mod.create(CAP)
+    spec.push(o)
+    for cyc in range(1, 13):
+        dg = g.grand(6, 4242, cyc)
+        do = o.grand(6, 4242, cyc)
+        assert abs(dg - do) <= 1e-8 * max(1.0, abs(do)), (cyc, dg, do)
+    for x, y in zip(g.get_buffers(), o.get_buffers()):
+        np.testing.assert_array_equal(x, y)
+    xg, yg, zg, tg, ibg = g.get_particles()
+    xo, yo, zo, to, ibo = o.get_particles()
+    np.testing.assert_array_equal(tg, to)
+    np.testing.assert_array_equal(ibg, ibo)
+    np.testing.assert_allclose(np.stack([xg, yg, zg]), np.stack([xo, yo, zo]), atol=1e-10)
+    # records stay current through a BD run and a further GRAND call
+    g.bd_steps(3, seed=8, step0=0, energies=False)
+    n0 = g.live_ntot()
+    g.grand(6, 4242, 13)
+    p = _state(g)[0]
+    assert np.isfinite(p).all() and abs(g.live_ntot() - n0) <= 6

@@ -125,6 +125,7 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         "set_membrane": [vp, C.POINTER(Membrane)],
         "set_diffusion": [vp, C.POINTER(Diffusion)],
         "set_countions": [vp, C.c_int32, _d],
+        "set_periodic": [vp, C.c_int32, C.c_double],
         "set_buffers": [vp, C.POINTER(Buffers)],
         "set_particles": [vp, C.c_int32, C.c_int32, C.c_int32, _d, _d, _d, _i,
                           _i],

@@ -580,6 +580,8 @@ int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
     return bromoc_ctx_fail(proto, BROMOC_E_STATE,
                            "adjoint: FP32 arithmetic needs an FP32 prototype");
   }
+  if (pk->periodic)
+    return bromoc_ctx_fail(proto, BROMOC_E_STATE, "adjoint: the periodic mode is not supported");
   if (pk->nsites != 0 || pk->shape != BROMOC_BOX)
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "adjoint: ions only, in a box");
   if (pk->nion_t > kAdjMaxIonTypes)

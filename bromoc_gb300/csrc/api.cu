@@ -204,6 +204,8 @@ void fill_box(const bromoc_system &q, BoxF &b) {
   for (int k = 0; k < 6; ++k) split_ff(bd[k], b.bh[k], b.bl[k]);
   const double c[3] = {q.cx, q.cy, q.cz};
   for (int k = 0; k < 3; ++k) split_ff(c[k], b.ch[k], b.cl[k]);
+  const double L[3] = {q.lx, q.ly, q.lz};
+  for (int k = 0; k < 3; ++k) split_ff(L[k], b.Lh[k], b.Ll[k]);
 }
 
 // Single-precision constants of the FP32 kernels (KP::f) from the FP64 state.
@@ -238,6 +240,13 @@ void fill_f32(bromoc_ctx *ctx) {
   f.fact0n1 = (float)p.fact0n1;
   f.fact0n2 = (float)p.fact0n2;
   fill_box(ctx->sys, f.box);
+  f.box.periodic = p.periodic;
+  const double L[3] = {p.lx, p.ly, p.lz};
+  for (int k = 0; k < 3; ++k) {
+    f.L[k] = (float)L[k];
+    f.iL[k] = (float)(1.0 / L[k]);
+  }
+  f.rc2 = (float)p.rc2;
 }
 
 int ensure_scratch(bromoc_ctx *ctx) {
@@ -344,6 +353,9 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
     plan.nchunk_ii = plan.nchunk_rf = p.nchunk_ii = p.nchunk_rf = 0;
     fl.ntile = T;
     fl.rf_ab = pair_cfg32(p, plan.ntot_ub, mask).rf;
+  } else if (plan.fp32 && p.periodic && pair_cfg32(p, plan.ntot_ub, mask).ntg > 0) {
+    return set_err(ctx, BROMOC_E_CAPACITY, "periodic mode: up to %d ions in FP32",
+                   32 * kN3MaxTiles);
   } else if (plan.fp32) {  // one fused pair kernel (ion-ion + RFPAR cross)
     const PairCfg32 pc = pair_cfg32(p, plan.ntot_ub, mask);
     chunking(pc.ntg, nion, plan.nchunk_ii, p.chunk_ii);
@@ -377,6 +389,8 @@ int check_ready(bromoc_ctx *ctx) {
   if (!ctx->have_sys || !ctx->have_types || !ctx->have_pairs)
     return set_err(ctx, BROMOC_E_STATE,
                    "set_system, set_types and set_pairs are required");
+  if (ctx->kp.periodic && (ctx->kp.nsites > 0 || ctx->kp.qrfpar))
+    return set_err(ctx, BROMOC_E_STATE, "periodic mode: ions only, without RFPAR");
   if (ctx->precision == BROMOC_FP32) fill_f32(ctx);
   return ensure_scratch(ctx);
 }
@@ -1332,6 +1346,17 @@ int bromoc_gpu_live_count_async(bromoc_ctx *ctx, int32_t *dst) {
   if (!ctx || !dst) return BROMOC_E_ARG;
   CU(cudaMemcpyAsync(dst, &ctx->kp.st->ntot, sizeof(int32_t), cudaMemcpyDeviceToHost,
                      ctx->stream));
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_set_periodic(bromoc_ctx *ctx, int32_t on, double rcut) {
+  if (!ctx) return BROMOC_E_ARG;
+  if (on && (!ctx->have_sys || ctx->sys.shape != BROMOC_BOX))
+    return set_err(ctx, BROMOC_E_STATE, "set_periodic: needs set_system with a box");
+  if (on && !(rcut > 0.0)) return set_err(ctx, BROMOC_E_ARG, "set_periodic: rcut must be > 0");
+  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->kp.periodic = on != 0;
+  ctx->kp.rc2 = on ? rcut * rcut : 0.0;
   return BROMOC_OK;
 }
 

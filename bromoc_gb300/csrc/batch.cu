@@ -273,6 +273,8 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   if (!pk->ipq_ok)
     return bromoc_ctx_fail(proto, BROMOC_E_STATE,
                            "batch: needs analytic ion-ion laws (no EFPOT) and <= 16 ion types");
+  if (pk->periodic)
+    return bromoc_ctx_fail(proto, BROMOC_E_STATE, "batch: the periodic mode is not supported");
   if (pk->nsites != 0)
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "batch: replicas hold ions only (no sites)");
   bromoc_batch *b = new bromoc_batch;

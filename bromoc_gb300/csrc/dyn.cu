@@ -16,9 +16,23 @@ __device__ __forceinline__ void clamp_bd(double bdmax, double &d) {
   if (fabs(d) > bdmax) d = fsign(bdmax, d);
 }
 
-// fixcoor.f90:19-68
+__device__ __forceinline__ void wrap1(double lo, double L, double &v) {
+  if (v < lo)
+    v += L;
+  else if (v >= lo + L)
+    v -= L;
+}
+
+// fixcoor.f90:19-68; in the extension mode (periodic box) one wrap into the
+// box per axis instead of the clamp (BD moves are far shorter than a box).
 __device__ __forceinline__ void fixcoor(const KP &p, double &x, double &y,
                                         double &z) {
+  if (p.periodic) {
+    wrap1(p.lx2m, p.lx, x);
+    wrap1(p.ly2m, p.ly, y);
+    wrap1(p.lz2m, p.lz, z);
+    return;
+  }
   if (p.shape == 1) {  // sphere: reflect through the wall
     const double r2 = (x - p.cx) * (x - p.cx) + (y - p.cy) * (y - p.cy) +
                       (z - p.cz) * (z - p.cz);

@@ -53,8 +53,14 @@ __global__ void __launch_bounds__(kPairThreads)
         if (base + k == t) continue;
         const int code = sc[k];
         const PairParam &q = p.pp[p.pidx[row + (code & 0xffff)]];
-        const double dx = xt - sx[k], dy = yt - sy[k], dz = zt - sz[k];
+        double dx = xt - sx[k], dy = yt - sy[k], dz = zt - sz[k];
+        if (p.periodic) {  // extension mode: nearest image, plain cutoff
+          dx -= p.lx * rint(dx / p.lx);
+          dy -= p.ly * rint(dy / p.ly);
+          dz -= p.lz * rint(dz / p.lz);
+        }
         const double d2 = dx * dx + dy * dy + dz * dz;
+        if (p.periodic && d2 >= p.rc2) continue;
         const double w = (code >> 16) ? 0.5 : 1.0;
         double dist;
         const double de = law64(p, q, d2, w, e, dist, err);
@@ -226,7 +232,7 @@ __global__ void __launch_bounds__(kPairThreads)
 
 constexpr int kN3Warps = 4;
 
-template <bool II, bool RF, bool EFP>
+template <bool II, bool RF, bool EFP, bool PBC = false>
 __global__ void __launch_bounds__(32 * kN3Warps)
     k_pairs32n(KP p, int qforces, int slot0) {
   __shared__ float4 sh[kN3Warps][32], sl[kN3Warps][32], sq[kN3Warps][RF ? 32 : 1];
@@ -244,8 +250,8 @@ __global__ void __launch_bounds__(32 * kN3Warps)
   const int q = blockIdx.x * kN3Warps + w;
   float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
   if (q < n3_pairs(T))  // warp-uniform
-    n3_tile<II, RF, EFP>(p, pair_sys(p, p.st->ntot, T), q, qforces, sh[w], sl[w], sq[w],
-                         acc[w], accb[w], acc1[w], accb1[w], tab, e);
+    n3_tile<II, RF, EFP, PBC>(p, pair_sys(p, p.st->ntot, T), q, qforces, sh[w], sl[w], sq[w],
+                              acc[w], accb[w], acc1[w], accb1[w], tab, e);
   block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
@@ -514,8 +520,14 @@ __global__ void __launch_bounds__(kPairThreads)
         const bool i_mobile = t_is_i ? tmob : ((fl >> 1) & 1);
         const double srj = t_is_i ? ss[k] : srt;
         if (!i_mobile || srj == 0.0) continue;
-        const double dx = xt - sx[k], dy = yt - sy[k], dz = zt - sz[k];
+        double dx = xt - sx[k], dy = yt - sy[k], dz = zt - sz[k];
+        if (p.periodic) {  // extension mode: nearest image, plain cutoff
+          dx -= p.lx * rint(dx / p.lx);
+          dy -= p.ly * rint(dy / p.ly);
+          dz -= p.lz * rint(dz / p.lz);
+        }
         const double d2 = dx * dx + dy * dy + dz * dz;
+        if (p.periodic && d2 >= p.rc2) continue;
         const double rij = sr[k] * rft;
         const double srij = ss[k] * srt;
         const double rfdn = 1.0 / sqrt(rij * rij + d2);
@@ -603,7 +615,10 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
     const int nb = n3_blocks(plan.ntile);
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
     const bool efp = !p.ipq_ok;
-    if (pc.ii && pc.rf)
+    if (p.periodic)  // extension mode: ion-ion only (no RFPAR)
+      (efp ? k_pairs32n<true, false, true, true> : k_pairs32n<true, false, false, true>)
+          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot);
+    else if (pc.ii && pc.rf)
       (efp ? k_pairs32n<true, true, true> : k_pairs32n<true, true, false>)
           <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot);
     else if (pc.ii)

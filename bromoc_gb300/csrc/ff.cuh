@@ -135,8 +135,26 @@ __device__ __forceinline__ void clamp_f(float bdmax, float &d) {
   if (fabsf(d) > bdmax) d = copysignf(bdmax, d);
 }
 
-// fixcoor.f90:19-68 on float-float coordinates
+// (h, l) += (ah, al), renormalised
+__device__ __forceinline__ void ff_add2(float &h, float &l, float ah, float al) {
+  float s, e;
+  two_sum(h, ah, s, e);
+  e = __fadd_rn(e, __fadd_rn(l, al));
+  fast_two_sum(s, e, h, l);
+}
+
+// fixcoor.f90:19-68 on float-float coordinates; in the extension mode
+// (periodic box) one wrap into [lower bound, lower bound + L) per axis.
 __device__ __forceinline__ void fixcoor_ff(const BoxF &c, float h[3], float l[3]) {
+  if (c.periodic) {
+    for (int k = 0; k < 3; ++k) {
+      if (ff_diff(h[k], l[k], c.bh[2 * k], c.bl[2 * k]) < 0.0f)
+        ff_add2(h[k], l[k], c.Lh[k], c.Ll[k]);
+      else if (ff_diff(h[k], l[k], c.bh[2 * k + 1], c.bl[2 * k + 1]) >= 0.0f)
+        ff_add2(h[k], l[k], -c.Lh[k], -c.Ll[k]);
+    }
+    return;
+  }
   if (c.shape == 1) {  // sphere: reflect through the wall
     const float d0 = ff_diff(h[0], l[0], c.ch[0], c.cl[0]);
     const float d1 = ff_diff(h[1], l[1], c.ch[1], c.cl[1]);

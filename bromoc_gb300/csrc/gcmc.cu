@@ -208,8 +208,14 @@ __device__ double interact_rec(const KP &p, const Trial &tr, uint32_t mask, int 
   const bool ion_i = i >= p.nsites;
   const int ti = q.ti;
   if (ion_i && guard_bad(p.st, abs(ti) - p.nold - 1, p.ntype - p.nold, 31)) return 0.0;
-  const double dx = q.x - tr.x, dy = q.y - tr.y, dz = q.z - tr.z;
+  double dx = q.x - tr.x, dy = q.y - tr.y, dz = q.z - tr.z;
+  if (p.periodic) {  // extension mode: nearest image, plain cutoff
+    dx -= p.lx * rint(dx / p.lx);
+    dy -= p.ly * rint(dy / p.ly);
+    dz -= p.lz * rint(dz / p.lz);
+  }
   const double d2 = dx * dx + dy * dy + dz * dz;
+  if (p.periodic && d2 >= p.rc2) return 0.0;
   double u = 0.0;
   if (mask & 1u) {
     int is = -1;

@@ -31,6 +31,8 @@ struct BoxF {
   float rsphe, rsphe2, iecx, iecy;
   float bh[6], bl[6];  // box bounds x-,x+,y-,y+,z-,z+ (hi, lo)
   float ch[3], cl[3];  // shape centre (hi, lo)
+  int periodic;        // extension mode: wrap instead of clamp (box only)
+  float Lh[3], Ll[3];  // box lengths (hi, lo)
 };
 
 // Single-precision constants of the FP32 path, filled on the host so that
@@ -41,6 +43,7 @@ struct F32C {
   AxisF ax[12];
   float celec, sqrfac, thold8, thold27, kbtdt, bdmax, fact0n1, fact0n2;
   BoxF box;
+  float L[3], iL[3], rc2;  // extension mode: box lengths, their inverses, cutoff^2
 };
 
 struct KP {
@@ -49,6 +52,10 @@ struct KP {
   DevState *st;   // live ntot, buffer counters, error flags
   // ---- system ----
   int shape, qcountion;
+  // extension mode (no counterpart in the reference): minimum-image periodic
+  // box and a plain cutoff rc2 (on r^2) for ion pairs; moves wrap
+  int periodic;
+  double rc2;
   double lx, ly, lz, cx, cy, cz, rsphe, rsphe2, iecx, iecy;
   double lx2m, lx2p, ly2m, ly2p, lz2m, lz2p;
   double kbtdt, ikbt, dt, bdmax;

@@ -39,7 +39,7 @@ union LoopSmem {
   float part[kLoopWarps][10][32];
 };
 
-template <bool II, bool RF, bool EFP>
+template <bool II, bool RF, bool EFP, bool PBC>
 __global__ void __launch_bounds__(32 * kLoopWarps, 1)
     k_bd_loop(const __grid_constant__ KP p, AssembleFlags fl, uint32_t mask, int variant,
               uint64_t seed, uint64_t step0, int nsteps, int fields_first) {
@@ -77,7 +77,7 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   for (int s = 0; s < nsteps; ++s) {
     float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int q = slot; q < npair; q += nslot)
-      n3_tile<II, RF, EFP>(p, ps, q, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w], sm.pr.acc[w],
+      n3_tile<II, RF, EFP, PBC>(p, ps, q, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w], sm.pr.acc[w],
                            sm.pr.accb[w], sm.pr.acc1[w], sm.pr.accb1[w], tab, e);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
     for (int it = blockIdx.x; it < nitem; it += G) {
@@ -96,7 +96,7 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   }
 }
 
-template <bool II, bool RF, bool EFP>
+template <bool II, bool RF, bool EFP, bool PBC = false>
 static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t mask,
                                  int variant, uint64_t seed, uint64_t step0, int nsteps,
                                  int fields_first, cudaStream_t stream) {
@@ -105,7 +105,7 @@ static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t 
   cudaError_t e = cudaGetDevice(&dev);
   if (e != cudaSuccess) return e;
   if (dev < 0 || dev >= 64) return cudaErrorInvalidDevice;
-  auto kern = k_bd_loop<II, RF, EFP>;
+  auto kern = k_bd_loop<II, RF, EFP, PBC>;
   const size_t dsm = sizeof(LoopSmem<RF>);
   if (max_res[dev] == 0) {
     int per_sm = 0, nsm = 0;
@@ -143,6 +143,11 @@ cudaError_t launch_bd_loop(const KP &p, const AssembleFlags &fl, int ntot_ub, ui
                            int fields_first, cudaStream_t stream) {
   const PairCfg32 pc = pair_cfg32(p, ntot_ub, mask);
   const bool efp = !p.ipq_ok;
+  if (p.periodic)  // extension mode: ion-ion only (no RFPAR)
+    return efp ? launch_loop_t<true, false, true, true>(p, fl, mask, variant, seed, step0,
+                                                        nsteps, fields_first, stream)
+               : launch_loop_t<true, false, false, true>(p, fl, mask, variant, seed, step0,
+                                                         nsteps, fields_first, stream);
   if (pc.ii && pc.rf)
     return efp ? launch_loop_t<true, true, true>(p, fl, mask, variant, seed, step0, nsteps,
                                                  fields_first, stream)

@@ -212,6 +212,9 @@ extern "C" int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t
   if (!bromoc_ctx_pair_view(ctx, &kp, &stream, &precision))
     return bromoc_ctx_fail(ctx, BROMOC_E_STATE,
                            "pair_energy_static: set_system, set_types and set_pairs first");
+  if (kp->periodic)
+    return bromoc_ctx_fail(ctx, BROMOC_E_STATE,
+                           "pair_energy_static: the periodic mode is not supported");
   if (!x || !y || !z || !typei || !fx || !fy || !fz || !eterms4)
     return bromoc_ctx_fail(ctx, BROMOC_E_ARG, "pair_energy_static: null device buffer");
   if (n > kMaxIons)

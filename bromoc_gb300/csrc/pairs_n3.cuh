@@ -25,6 +25,15 @@ namespace bgpu {
 // Output: per tile pair and side, per lane, (f, A) and B (tpf, tpb); the
 // assembly kernel sums a particle's row and column entries in fixed order.
 // ---------------------------------------------------------------------------
+// Extension mode (periodic box): the nearest image of a separation whose
+// components are at most one box length; rintf rounds half to even, as the
+// FP64 path's rint.
+__device__ __forceinline__ void min_image_f(const KP &p, float &dx, float &dy, float &dz) {
+  dx = fmaf(-p.f.L[0], rintf(dx * p.f.iL[0]), dx);
+  dy = fmaf(-p.f.L[1], rintf(dy * p.f.iL[1]), dy);
+  dz = fmaf(-p.f.L[2], rintf(dz * p.f.iL[2]), dz);
+}
+
 // Systems up to this many ion tiles run the pair tile's two-chain loop.
 constexpr int kN3DualTiles = 96;
 
@@ -56,7 +65,7 @@ __device__ __forceinline__ PairSys pair_sys(const KP &p, int ntot, int T) {
 // elj, esrpmf, eefpot, erfpar), added to; without EFP the elj sum holds
 // 6 x elj (the dense table holds 6 epp4).
 // p: the laws and constants.
-template <bool II, bool RF, bool EFP>
+template <bool II, bool RF, bool EFP, bool PBC = false>
 __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, int qforces,
                                         float4 *sh, float4 *sl, float4 *sq, float4 *acc,
                                         float *accb, float4 *acc1, float *accb1,
@@ -129,12 +138,13 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
                        float &gz, float &gA, float &gB, float *ge) {
     constexpr bool RAG = decltype(rag)::value;
     const float4 h = sh[mm], l = sl[mm];
-    const float dx = (th.x - h.x) + (tl.x - l.x);
-    const float dy = (th.y - h.y) + (tl.y - l.y);
-    const float dz = (th.z - h.z) + (tl.z - l.z);
+    float dx = (th.x - h.x) + (tl.x - l.x);
+    float dy = (th.y - h.y) + (tl.y - l.y);
+    float dz = (th.z - h.z) + (tl.z - l.z);
+    if (PBC) min_image_f(p, dx, dy, dz);
     const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
     float4 c = tab[row + (__float_as_int(h.w) & 0xffff) - p.ndna];
-    if (RAG && mm >= ncol) c = make_float4(0.f, 0.f, c.z, 0.f);
+    if ((RAG && mm >= ncol) || (PBC && r2 >= p.f.rc2)) c = make_float4(0.f, 0.f, c.z, 0.f);
     const float ir = rsqrt_nz(r2), ir2 = ir * ir;
     const float cofo = c.x * ir;
     ge[0] += cofo;
@@ -222,12 +232,13 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
         const float4 l = sl[mm];
         const int j = ps.nsites + J * 32 + mm;
         const bool smob = j >= m0;
-        const float dx = (th.x - h.x) + (tl.x - l.x);
-        const float dy = (th.y - h.y) + (tl.y - l.y);
-        const float dz = (th.z - h.z) + (tl.z - l.z);
+        float dx = (th.x - h.x) + (tl.x - l.x);
+        float dy = (th.y - h.y) + (tl.y - l.y);
+        float dz = (th.z - h.z) + (tl.z - l.z);
+        if (PBC) min_image_f(p, dx, dy, dz);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         float dii = 0.0f, drf = 0.0f, dAs = 0.0f, dBs = 0.0f;
-        if (II && (tmob || smob)) {
+        if (II && (tmob || smob) && !(PBC && r2 >= p.f.rc2)) {
           if (EFP) {
             dii = law32k(p, __ldg(p.pidx + row + (scode & 0xffff)), r2, 1.0f, e);
           } else {

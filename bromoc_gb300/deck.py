@@ -71,6 +71,9 @@ class SystemSpec:
     lj_pair: dict = field(default_factory=dict)   # (a, b) -> (eps, sigma)
     srpmf: dict = field(default_factory=dict)     # (a, b) -> (c0..c4)
     srpmf_rth: float | None = None
+    # extension mode (no counterpart in the reference): minimum-image periodic
+    # box with a plain cutoff on ion pairs (Angstrom); None = hard walls
+    periodic_rcut: float | None = None
     efpot_knots: dict = field(default_factory=dict)  # (a, b) -> (r[], U[])
     efpot_res: float = 0.1
     # sites
@@ -257,6 +260,8 @@ class SystemSpec:
         self._builder = eng.efpot_from_knots
         sysd = self.system_struct()
         eng.call("set_system", C.byref(sysd))
+        if self.periodic_rcut is not None:
+            eng.call("set_periodic", 1, float(self.periodic_rcut))
         cg = np.zeros(ntype)
         dif = np.zeros(ntype)
         for i in range(self.nion):

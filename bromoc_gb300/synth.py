@@ -129,8 +129,10 @@ def batch_replicas(seed=4, nrep=256, nmin=200, nmax=8000, conc=1.0):
     return counts.astype(int), edges, parts
 
 
-def bulk_kcl(seed=1, n_per=130, L=60.0, srpmf=False, precision=abi.FP64):
-    """Bulk KCl: 2*n_per ions in an L^3 box with hard walls."""
+def bulk_kcl(seed=1, n_per=130, L=60.0, srpmf=False, precision=abi.FP64, periodic_rcut=None):
+    """Bulk KCl: 2*n_per ions in an L^3 box with hard walls, or (periodic_rcut,
+    the extension mode) periodic with that pair cutoff; the ions then keep
+    1.5 A from the faces, so no two images start closer than 3 A."""
     rng = np.random.default_rng(seed)
     s = SystemSpec(shape=abi.BOX, lx=L, ly=L, lz=L, temp=300.0, cdie=80.0,
                    dt=0.02, bdmax=1.0, precision=precision)
@@ -138,7 +140,8 @@ def bulk_kcl(seed=1, n_per=130, L=60.0, srpmf=False, precision=abi.FP64):
     if srpmf:
         s.srpmf.update(SRPMF_KCL)
         s.srpmf_rth = 8.0
-    h = 0.5 * L - 0.5
+    s.periodic_rcut = periodic_rcut
+    h = 0.5 * L - (1.5 if periodic_rcut is not None else 0.5)
     p = place(rng, 2 * n_per, [-h] * 3, [h] * 3)
     s.x, s.y, s.z = p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
     s.typei = np.array([1] * n_per + [2] * n_per, np.int32)

@@ -335,6 +335,13 @@ int bromoc_gpu_kernel_timing(bromoc_ctx *ctx, int32_t on);
  * cooperative launch (on = 1, the default) or one launch per kernel and
  * step (on = 0); the trajectories agree.  No counterpart in the reference. */
 int bromoc_gpu_set_fused_bd(bromoc_ctx *ctx, int32_t on);
+/* Extension mode, no counterpart in the reference: a periodic box system
+ * (after set_system with BROMOC_BOX) whose ion pairs interact through the
+ * nearest periodic image when closer than rcut (Angstrom; plain cutoff, no
+ * shift), with every move wrapped into the box instead of clamped.  Ions
+ * only (no sites), without RFPAR; in FP32 mode up to 8192 ions.  on = 0
+ * returns to the reference's hard walls without cutoff. */
+int bromoc_gpu_set_periodic(bromoc_ctx *ctx, int32_t on, double rcut);
 /* total milliseconds and number of timed launches since timing was turned
  * on (synchronises the context's stream) */
 int bromoc_gpu_kernel_time(bromoc_ctx *ctx, int32_t which, double *total_ms,

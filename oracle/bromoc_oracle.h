@@ -25,6 +25,7 @@ int bromoc_ref_set_rfpar(bromoc_ref *r, const bromoc_grid *g, int32_t nmaps,
                          double reffac, const int32_t *map_of_type);
 int bromoc_ref_set_membrane(bromoc_ref *r, const bromoc_membrane *m);
 int bromoc_ref_set_diffusion(bromoc_ref *r, const bromoc_diffusion *d);
+int bromoc_ref_set_periodic(bromoc_ref *r, int32_t on, double rcut);
 int bromoc_ref_set_countions(bromoc_ref *r, int32_t cntpts,
                              const double *zcont);
 int bromoc_ref_set_buffers(bromoc_ref *r, const bromoc_buffers *b);

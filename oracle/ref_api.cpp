@@ -241,6 +241,17 @@ int bromoc_ref_set_diffusion(bromoc_ref *r, const bromoc_diffusion *d) {
   return BROMOC_OK;
 }
 
+int bromoc_ref_set_periodic(bromoc_ref *r, int32_t on, double rcut) {
+  if (!r) return BROMOC_E_ARG;
+  State &s = r->s;
+  if (on && (!s.have_sys || s.sys.shape != BROMOC_BOX))
+    return fail(r, "set_periodic: needs set_system with a box");
+  if (on && !(rcut > 0.0)) return fail(r, "set_periodic: rcut must be > 0");
+  s.periodic = on != 0;
+  s.rcut2 = on ? rcut * rcut : 0.0;
+  return BROMOC_OK;
+}
+
 int bromoc_ref_set_countions(bromoc_ref *r, int32_t cntpts, const double *zcont) {
   if (!r || cntpts < 0 || (cntpts > 0 && !zcont)) return fail(r, "set_countions");
   State &s = r->s;
@@ -331,6 +342,10 @@ static bool ready(bromoc_ref *r) {
   State &s = r->s;
   if (!s.have_sys || !s.have_types || !s.have_pairs) {
     s.err = "set_system, set_types and set_pairs are required";
+    return false;
+  }
+  if (s.periodic && (s.nsites > 0 || s.qrfpar)) {  // the extension mode's scope
+    s.err = "periodic mode: ions only, without RFPAR";
     return false;
   }
   return true;

@@ -10,8 +10,23 @@ static inline double fsign(double a, double b) {
   return b >= 0.0 ? std::fabs(a) : -std::fabs(a);
 }
 
-// fixcoor.f90:19-68
+// One periodic wrap into [lo, lo + L): BD moves are far shorter than a box.
+static inline void wrap1(double lo, double L, double &v) {
+  if (v < lo)
+    v += L;
+  else if (v >= lo + L)
+    v -= L;
+}
+
+// fixcoor.f90:19-68; in the extension mode (periodic box) the position is
+// wrapped into the box instead of clamped.
 void fixcoor(const State &s, double &xi, double &yi, double &zi) {
+  if (s.periodic) {
+    wrap1(s.lx2m, s.sys.lx, xi);
+    wrap1(s.ly2m, s.sys.ly, yi);
+    wrap1(s.lz2m, s.sys.lz, zi);
+    return;
+  }
   const bromoc_system &q = s.sys;
   if (q.shape == BROMOC_SPHERE) {
     double r2 = (xi - q.cx) * (xi - q.cx) + (yi - q.cy) * (yi - q.cy) +

@@ -755,9 +755,10 @@ void interact(State &s, uint32_t mask, double &dener, double xj, double yj,
       if (i == j) continue;
       int itype2 = s.nwtype[std::abs(s.typei[i])];
       int is = nindex(s, itype2, jtype2);
-      double dist2 = (s.x[i] - xj) * (s.x[i] - xj) +
-                     (s.y[i] - yj) * (s.y[i] - yj) +
-                     (s.z[i] - zj) * (s.z[i] - zj);
+      double ddx = s.x[i] - xj, ddy = s.y[i] - yj, ddz = s.z[i] - zj;
+      s.min_image(ddx, ddy, ddz);  // extension mode only
+      double dist2 = ddx * ddx + ddy * ddy + ddz * ddz;
+      if (s.periodic && dist2 >= s.rcut2) continue;
       if (s.qefpot[is]) {
         double eefp, dist;
         gety(s, is, dist2, eefp, dist);

@@ -302,7 +302,9 @@ static void ionion_range(const State &s, int jlo, int jhi, bool qforces,
       int is = nindex(s, itype2, jtype2);
       double dxx = s.x[i] - s.x[j], dyy = s.y[i] - s.y[j],
              dzz = s.z[i] - s.z[j];
+      s.min_image(dxx, dyy, dzz);  // extension mode only
       double dist2 = dxx * dxx + dyy * dyy + dzz * dzz;
+      if (s.periodic && dist2 >= s.rcut2) continue;
       double de = 0.0, dist = 0.0, idist = 0.0, idist2 = 0.0, cofo = 0.0,
              dist6 = 0.0, dist12 = 0.0, esrpmf1 = 0.0, esrpmf2 = 0.0,
              esrpmf3 = 0.0, fdf = 0.0, fdv = 0.0, eefp = 0.0;

@@ -14,6 +14,7 @@
 // State mirrors the Fortran modules (grandmod, gsbpmod, efpmod, extramod,
 // nucleotmod); particle arrays are 1-based like the Fortran.
 #pragma once
+#include <cmath>
 #include <cstdint>
 #include <string>
 #include <vector>
@@ -61,6 +62,10 @@ struct State {
   double ikbt = 0, kbtdt = 0;
   double lx2m = 0, lx2p = 0, ly2m = 0, ly2p = 0, lz2m = 0, lz2p = 0;
   double rsphe2 = 0, iecx = 0, iecy = 0;
+  // extension mode (no counterpart in the reference): minimum-image periodic
+  // box and a plain cutoff on ion pairs, positions wrapped after each move
+  bool periodic = false;
+  double rcut2 = 0;
   // types (1-based)
   int ntype = 0, nold = 0, nttyp = 0, ndna = 0, nion = 0, ndnaxnion = 0;
   std::vector<int> nwtype;
@@ -130,6 +135,13 @@ struct State {
   std::vector<int> warn;  // 1-based by combined type
 
   bool qpar() const { return have_types && ntype > nold; }  // PARTICLES given
+  // extension mode: nearest periodic image of a separation
+  void min_image(double &dx, double &dy, double &dz) const {
+    if (!periodic) return;
+    dx -= sys.lx * std::rint(dx / sys.lx);
+    dy -= sys.ly * std::rint(dy / sys.ly);
+    dz -= sys.lz * std::rint(dz / sys.lz);
+  }
   bool qnucl() const { return nsites > 0; }
   void resize_particles(int cap);
 };

@@ -23,6 +23,12 @@ def pairs(n_per=24, L=32.0, srpmf=True, seed=5, precision=abi.FP64):
                           precision=precision)
 
 
+def periodic_kcl(n_per=40, L=36.0, seed=11, precision=abi.FP64, rcut=15.0):
+    """Bulk KCl in the extension mode: periodic box, 15 A pair cutoff."""
+    return synth.bulk_kcl(seed=seed, n_per=n_per, L=L, srpmf=True, precision=precision,
+                          periodic_rcut=rcut)
+
+
 def efpot_ions(n_per=24, L=32.0, seed=6, precision=abi.FP64):
     """Bulk KCl whose K-Cl and Cl-Cl pairs use tabulated potentials."""
     s = pairs(n_per, L, srpmf=True, seed=seed, precision=precision)

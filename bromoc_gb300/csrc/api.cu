@@ -41,7 +41,9 @@ struct bromoc_ctx {
   // live ntot bookkeeping (see ntot_ub)
   int ntot_known = 0;
   long long attempts_total = 0, attempts_at_known = 0;
-  int *h_ntot = nullptr;  // pinned
+  // pinned words: [0] ntot read back, [1] error word, [2..3] dener_sum,
+  // [4] ntot uploaded (never a target of a pending read-back)
+  int *h_ntot = nullptr;
   cudaEvent_t ev_ntot = nullptr;
   bool rb_pending = false;
   long long rb_attempts = 0;
@@ -416,12 +418,9 @@ int ensure_dbl(bromoc_ctx *ctx) {
   return BROMOC_OK;
 }
 
-int check_device_err(bromoc_ctx *ctx) {
-  int e = 0;
-  CU(cudaMemcpyAsync(ctx->h_ntot + 1, &ctx->kp.st->err, sizeof(int),
-                     cudaMemcpyDeviceToHost, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
-  e = ctx->h_ntot[1];
+// Turns a nonzero device error word (read back with the stream idle) into
+// the API error, clearing the word and the guard record.
+int device_err_result(bromoc_ctx *ctx, int e) {
   if (e) {
     int bad[3] = {0, 0, 0};
     CU(cudaMemcpy(bad, &ctx->kp.st->bad_site, sizeof bad, cudaMemcpyDeviceToHost));
@@ -437,6 +436,13 @@ int check_device_err(bromoc_ctx *ctx) {
                    bad[0], bad[1], bad[2]);
   }
   return BROMOC_OK;
+}
+
+int check_device_err(bromoc_ctx *ctx) {
+  CU(cudaMemcpyAsync(ctx->h_ntot + 1, &ctx->kp.st->err, sizeof(int),
+                     cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return device_err_result(ctx, ctx->h_ntot[1]);
 }
 
 }  // namespace
@@ -495,7 +501,7 @@ int bromoc_gpu_create(int32_t capacity, int32_t precision, void *stream,
       rc = BROMOC_E_CUDA;
     ctx->own_stream = true;
   }
-  if (!rc && cudaMallocHost((void **)&ctx->h_ntot, 4 * sizeof(int)) != cudaSuccess)
+  if (!rc && cudaMallocHost((void **)&ctx->h_ntot, 8 * sizeof(int)) != cudaSuccess)
     rc = BROMOC_E_CUDA;
   if (!rc && cudaEventCreateWithFlags(&ctx->ev_ntot, cudaEventDisableTiming) != cudaSuccess)
     rc = BROMOC_E_CUDA;
@@ -1042,10 +1048,15 @@ int bromoc_gpu_set_buffers(bromoc_ctx *ctx, const bromoc_buffers *b) {
   return BROMOC_OK;
 }
 
-int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
-                             int32_t nfix, const double *x, const double *y,
-                             const double *z, const int32_t *typei,
-                             const int32_t *ibuffer) {
+}  // extern "C"
+
+namespace {
+
+// Host arrays -> device.  Stream-ordered after earlier work; with wait the
+// call returns once the copies are done (the caller may reuse its buffers).
+int upload_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites, int32_t nfix,
+                     const double *x, const double *y, const double *z, const int32_t *typei,
+                     const int32_t *ibuffer, bool wait) {
   if (!ctx || !x || !y || !z || !typei) return set_err(ctx, BROMOC_E_ARG, "set_particles: null");
   KP &p = ctx->kp;
   if (ntot < 0 || ntot > p.cap)
@@ -1062,7 +1073,9 @@ int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
       return set_err(ctx, BROMOC_E_ARG, "set_particles: typei(%d) = %d is not an ion type",
                      i + 1, typei[i]);
   }
-  CU(cudaStreamSynchronize(ctx->stream));
+  // the count goes up from its own pinned word: a read-back still pending on
+  // the stream targets word 0 and would overwrite it before the upload
+  if (wait) CU(cudaStreamSynchronize(ctx->stream));
   p.nfix = nfix;
   const size_t n = (size_t)std::max(ntot, 1);
   CU(cudaMemcpyAsync(p.x, x, ntot * sizeof(double), cudaMemcpyHostToDevice, ctx->stream));
@@ -1073,9 +1086,10 @@ int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
     CU(cudaMemcpyAsync(p.ibuffer, ibuffer, ntot * sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
   else
     CU(cudaMemsetAsync(p.ibuffer, 0, n * sizeof(int), ctx->stream));
-  *ctx->h_ntot = ntot;
-  CU(cudaMemcpyAsync(&p.st->ntot, ctx->h_ntot, sizeof(int), cudaMemcpyHostToDevice, ctx->stream));
-  CU(cudaStreamSynchronize(ctx->stream));
+  ctx->h_ntot[4] = ntot;
+  CU(cudaMemcpyAsync(&p.st->ntot, ctx->h_ntot + 4, sizeof(int), cudaMemcpyHostToDevice,
+                     ctx->stream));
+  if (wait) CU(cudaStreamSynchronize(ctx->stream));
   ctx->ntot_known = ntot;
   ctx->attempts_at_known = ctx->attempts_total;
   ctx->rb_pending = false;
@@ -1083,6 +1097,56 @@ int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
   ctx->ff_fresh = false;
   ctx->dbl_fresh = true;
   return BROMOC_OK;
+}
+
+// Device -> host arrays with one wait: the count, the error word and, for
+// each array, the entries up to the count's host-side upper bound (the
+// buffers are capacity-sized) travel together.  *err receives the word.
+int download_particles(bromoc_ctx *ctx, int32_t *ntot, double *x, double *y, double *z,
+                       int32_t *typei, int32_t *ibuffer, int *err) {
+  int rc = ensure_dbl(ctx);
+  if (rc) return rc;
+  KP &p = ctx->kp;
+  const int ub = ntot_ub(ctx);
+  CU(cudaMemcpyAsync(ctx->h_ntot, &p.st->ntot, 2 * sizeof(int), cudaMemcpyDeviceToHost,
+                     ctx->stream));
+  int lo = 0, hi = ub;
+  for (int pass = 0; pass < 2; ++pass) {
+    const size_t m = (size_t)(hi - lo);
+    if (m) {
+      if (x) CU(cudaMemcpyAsync(x + lo, p.x + lo, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      if (y) CU(cudaMemcpyAsync(y + lo, p.y + lo, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      if (z) CU(cudaMemcpyAsync(z + lo, p.z + lo, m * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
+      if (typei)
+        CU(cudaMemcpyAsync(typei + lo, p.typei + lo, m * sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+      if (ibuffer)
+        CU(cudaMemcpyAsync(ibuffer + lo, p.ibuffer + lo, m * sizeof(int), cudaMemcpyDeviceToHost,
+                           ctx->stream));
+    }
+    CU(cudaStreamSynchronize(ctx->stream));
+    const int n = ctx->h_ntot[0];
+    if (n <= hi) break;
+    lo = hi;  // the bound is exact by construction; this pass never runs
+    hi = std::min(n, p.cap);
+  }
+  ctx->ntot_known = ctx->h_ntot[0];
+  ctx->attempts_at_known = ctx->attempts_total;
+  ctx->rb_pending = false;
+  if (ntot) *ntot = ctx->ntot_known;
+  if (err) *err = ctx->h_ntot[1];
+  return BROMOC_OK;
+}
+
+}  // namespace
+
+extern "C" {
+
+int bromoc_gpu_set_particles(bromoc_ctx *ctx, int32_t ntot, int32_t nsites,
+                             int32_t nfix, const double *x, const double *y,
+                             const double *z, const int32_t *typei,
+                             const int32_t *ibuffer) {
+  return upload_particles(ctx, ntot, nsites, nfix, x, y, z, typei, ibuffer, true);
 }
 
 int bromoc_gpu_get_particles(bromoc_ctx *ctx, int32_t *ntot, double *x, double *y,
@@ -1252,7 +1316,8 @@ int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant, i
                              int32_t nfix, double *x, double *y, double *z,
                              const int32_t *typei, double *eterms) {
   if (!ctx || !x || !y || !z || !typei) return set_err(ctx, BROMOC_E_ARG, "bd_steps_host: null");
-  int rc = bromoc_gpu_set_particles(ctx, ntot, nsites, nfix, x, y, z, typei, nullptr);
+  // the host arrays are read and rewritten in stream order: one wait, at the end
+  int rc = upload_particles(ctx, ntot, nsites, nfix, x, y, z, typei, nullptr, false);
   if (!rc) rc = bromoc_gpu_bd_steps(ctx, terms, variant, nsteps, seed, step0, eterms);
   if (!rc) rc = ensure_dbl(ctx);
   if (!rc) {
@@ -1260,8 +1325,11 @@ int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant, i
     CU(cudaMemcpyAsync(x, p.x, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaMemcpyAsync(y, p.y, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
     CU(cudaMemcpyAsync(z, p.z, ntot * sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
-    CU(cudaStreamSynchronize(ctx->stream));
+    CU(cudaMemcpyAsync(ctx->h_ntot + 1, &p.st->err, sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
   }
+  cudaStreamSynchronize(ctx->stream);  // also on an error: no copy outlives the call
+  if (!rc) rc = device_err_result(ctx, ctx->h_ntot[1]);
   return rc;
 }
 
@@ -1399,7 +1467,8 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms, int32_t varian
     return set_err(ctx, BROMOC_E_ARG, "simul_cycles_host: null");
   if (ncycle < 0 || ngcmc < 0 || nbd < 0 || cycle0 < 1)
     return set_err(ctx, BROMOC_E_ARG, "simul_cycles_host: bad counts");
-  int rc = bromoc_gpu_set_particles(ctx, *ntot, nsites, nfix, x, y, z, typei, ibuffer);
+  // the host arrays are read and rewritten in stream order: one wait, at the end
+  int rc = upload_particles(ctx, *ntot, nsites, nfix, x, y, z, typei, ibuffer, false);
   for (int c = 0; !rc && c < ncycle; ++c) {
     const uint64_t cyc = cycle0 + c;
     if (ngcmc > 0) rc = bromoc_gpu_grand(ctx, terms, ngcmc, seed, cyc, nullptr);
@@ -1407,8 +1476,10 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms, int32_t varian
       rc = bromoc_gpu_bd_steps(ctx, terms, variant, nbd, seed, (cyc - 1) * nbd,
                                c + 1 == ncycle ? eterms : nullptr);
   }
-  if (!rc) rc = bromoc_gpu_get_particles(ctx, ntot, x, y, z, typei, ibuffer);
-  if (!rc) rc = check_device_err(ctx);
+  int e = 0;
+  if (!rc) rc = download_particles(ctx, ntot, x, y, z, typei, ibuffer, &e);
+  if (!rc) rc = device_err_result(ctx, e);
+  if (rc) cudaStreamSynchronize(ctx->stream);  // no copy outlives the call
   return rc;
 }
 

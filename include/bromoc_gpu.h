@@ -277,8 +277,11 @@ int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant,
 /* Drop-in for one or more cycles of simul1.f90:351-390 over HOST arrays:
  * per cycle GRAND(ngcmc) then nbd x (ENERGY with forces + DYNAMICSn).  The
  * particle arrays (capacity-sized buffers) are uploaded, advanced on the
- * device and written back with the new *ntot (GCMC changes it).  Cycles are
- * numbered cycle0, cycle0+1, ...; BD steps (cycle-1)*nbd + istep - 1. */
+ * device and written back with the new *ntot (GCMC changes it); entries
+ * past the new *ntot may be overwritten too (up to *ntot + ncycle*ngcmc).
+ * Cycles are numbered cycle0, cycle0+1, ...; BD steps
+ * (cycle-1)*nbd + istep - 1.  The work is queued in stream order with one
+ * wait at the end: the call returns when the arrays hold the result. */
 int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms,
                                  int32_t variant, int32_t ncycle,
                                  int32_t ngcmc, int32_t nbd, uint64_t seed,

@@ -275,7 +275,8 @@ int ensure_scratch(bromoc_ctx *ctx) {
   // + ion-site (tiles)
   ctx->nslot_cap = fields_blocks((int)cap) + tiles * (2 * kMaxChunks + 4) + 8;
   if ((rc = dalloc(ctx, &p.epart, (size_t)ctx->nslot_cap * kNTerms))) return rc;
-  if ((rc = dalloc(ctx, &p.ipart, (size_t)tiles + 2))) return rc;
+  if ((rc = dalloc(ctx, &p.ipart, ((size_t)tiles + 2) * kSpec))) return rc;
+  if ((rc = dalloc(ctx, &p.ierr, ((size_t)tiles + 2) * kSpec))) return rc;
   ctx->ipart_slots = tiles + 2;
   if ((rc = dalloc(ctx, &p.gc_rf, cap))) return rc;
   if ((rc = dalloc(ctx, &p.rf_srfe, cap))) return rc;
@@ -286,7 +287,8 @@ int ensure_scratch(bromoc_ctx *ctx) {
   if ((rc = dalloc(ctx, &p.dids, 5 * cap))) return rc;
   CU(cudaMemset(p.dids, 0, 5 * cap * sizeof(double)));
   if ((rc = dalloc(ctx, &p.eterms, kNTerms))) return rc;
-  if ((rc = dalloc(ctx, &p.trial, 1))) return rc;
+  if ((rc = dalloc(ctx, &p.trial, kSpec))) return rc;
+  if ((rc = dalloc(ctx, &p.ground, 1))) return rc;
   if ((rc = dalloc(ctx, &ctx->d_dener, 1))) return rc;
   ctx->have_scratch = true;
   return BROMOC_OK;

@@ -78,6 +78,18 @@ struct Trial {
   int chg;                  // GRAND: slot the previous accepted move rewrote, -1 none
 };
 
+// GRAND attempts evaluated together in one round of the GRAND kernel.
+constexpr int kSpec = 8;
+
+// Header of one GRAND round, written by the coordinating block before it
+// publishes the round's trials (Trial[kSpec]).
+struct GrandRound {
+  int a0, na;               // first attempt of the round, attempts (0: the launch ends)
+  int ntot;                 // live particle count the trials were made against
+  int nchg;                 // slots the previous round rewrote
+  int chg[kSpec];
+};
+
 // ---- Philox4x32-10 (Salmon, Moraes, Dror, Shaw, SC'11) -------------------
 __host__ __device__ inline void philox4x32_10(uint32_t c0, uint32_t c1,
                                               uint32_t c2, uint32_t c3,

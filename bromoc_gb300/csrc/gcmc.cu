@@ -316,50 +316,87 @@ void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
 
 // ---------------------------------------------------------------------------
 // GRAND (grand.f90:19-121, insert.f90, find.f90): every attempt of one call
-// in one cooperative launch.  Block 0 owns the GCMC state (live count,
-// buffer counters, buffer parameters) in shared memory for the whole launch
-// and writes it back at the end; the other blocks only sum ΔE.  Per attempt:
-//   block 0: the proposal and the trial's single-particle terms; publish
-//            the trial (generation flag, release);
-//   every block: its share of the O(N) ΔE sum -> ipart[block]; arrive on a
-//            counter (release);
-//   block 0: while the other blocks sum, the next attempt's random draws
-//            (they do not depend on the outcome) and, for an insertion, the
-//            next trial's single-particle terms (they depend only on its
-//            position); then waits for every arrival (acquire), total ΔE,
-//            Im-Roux acceptance, insertion/deletion, counters, and the part
-//            of the next proposal that depends on the new state (the live
-//            count; for a deletion the rank of its ion, which slot holds it
-//            and its single-particle terms).
-// One synchronisation per attempt.  Each thread owns the same particles in
-// every phase (round-robin over blocks): it reads its particle's record
-// before waiting for the next trial, and re-reads it only if the trial
-// names its slot as the one the last accepted move rewrote.  Block 0
-// proposes the first attempt before its share of the RFPAR prepass.  Data
-// that another block wrote during the launch are read past L1 (__ldcg).
-// With more than one block, block 0 owns no particles.  In FP32 mode
-// (ffpos) the positions are read from and written to the float-float
-// records, so no conversion kernel runs around the call.
+// in one cooperative launch, settled in order, evaluated in rounds.
+//
+// On this part a warp issues one FP64 instruction per ~64 clocks however
+// many of its lanes are active, so an attempt's O(N) ΔE sum costs the FP64
+// chain of one pair term whatever the lanes do.  A round therefore
+// evaluates the pair terms of every particle against up to kSpec attempts
+// at once (lane = particle x attempt), all in the state at the start of
+// the round, and block 0 then settles the attempts in order:
+//   - up to the round's first acceptance the state is the round's, and the
+//     round's sums are those of the sequential algorithm;
+//   - after an acceptance, an insertion trial's ΔE is its sum plus its pair
+//     terms with the ions the round inserted, minus those with the ions the
+//     round deleted (trial-trial terms, formed while the other blocks sum);
+//   - a deletion trial keeps its target and sum when the rank drawn from
+//     the buffer's current count is the rank the target was found at and
+//     no deletion of the round touched the buffer (neither the deleted ion
+//     nor the last ion moved into the freed slot belongs to it): ranks of a
+//     buffer's ions change only then, an insertion appends its ion last.
+//     Otherwise the round ends before that attempt and the next round
+//     proposes from the current state.
+// The draws, the proposals and their outcomes are those of proposing each
+// attempt after the previous one is settled; ΔE agrees to FP64 rounding (a
+// correction adds a pair term outside the block partial sums).  Error flags
+// of the pair terms and a deletion trial's warnings count only for the
+// attempts settled with them.
+//
+// Per round:
+//   block 0: the trials: draws (a thread per attempt), deletion targets in
+//            the current state (one block scan for all), single-particle
+//            terms (a warp per trial); publish the round (release bar_gen);
+//   blocks 1..: pair terms, lane = (particle, attempt) -> per-block partial
+//            of each attempt (ipart) and its error flags (ierr); arrive on
+//            bar_count (release);
+//   block 0, meanwhile: each trial's particle as an ion record holds it
+//            (with its RFPAR srfe, reff) and the trial-trial pair terms; after
+//            every arrival (acquire) the totals, the acceptances of all
+//            attempts as if none before them were accepted (in parallel),
+//            then the settling in order.
+// A round with no attempts ends the launch.  Each thread owns the same
+// particles in every round and keeps its first particle's record across
+// rounds, re-read only when the round header names the slot as rewritten.
+// Data another block wrote during the launch are read past L1 (__ldcg).
 // Every wait is bounded: it gives up after kWaitSpins polls, or as soon as
 // another block has given up, records kErrBarrier and the launch returns.
-// The draws, the proposals and their outcomes are those of proposing
-// each attempt after the previous one is settled.
 // ---------------------------------------------------------------------------
 constexpr int kGrandThreads = 128;
+constexpr int kGrandWarps = kGrandThreads / 32;
+
+// Lanes per particle in the pair phase: the attempts of a round rounded up
+// to a power of two (lane = particle * lanes + attempt).
+__host__ __device__ inline int grand_lanes(int ngcmc) {
+  const int a = ngcmc < 1 ? 1 : (ngcmc < kSpec ? ngcmc : kSpec);
+  int ap = 1;
+  while (ap < a) ap <<= 1;
+  return ap;
+}
 
 struct GrandState {
-  Trial s;                  // current trial
-  double2 trial_rf;         // RFPAR (srfe, reff) at an insertion trial
-  Trial nx;                 // the next attempt's draws (+ insertion terms)
-  double nx_u;              // the next deletion's rank draw
-  double2 nx_rf;            // RFPAR (srfe, reff) of the next insertion trial
-  int nx_fields;            // nx holds the trial's single-particle terms (an
-                            // insertion's, or a deletion's found in the state
-                            // before the pending acceptance)
-  int nx_alert;             // warnings of that deletion trial, not yet counted
-  int chg;                  // slot the last accepted move rewrote, -1 none
-  int ff;                   // FP32 mode: positions live in the float-float records
-  int ntot;
+  Trial tr[kSpec];          // the round's trials
+  double u_rank[kSpec];     // deletion: the rank draw
+  double u_acc[kSpec];      // the acceptance draw
+  int ip0[kSpec];           // deletion: the rank its target was found at, 0 none
+  int need[kSpec], found[kSpec];
+  int nalert[kSpec];        // deletion: warnings of its single-particle terms
+  // each trial's particle as an ion record holds it: position (float-float
+  // rounded in FP32 mode), signed type, RFPAR (srfe, reff) at that position
+  double px[kSpec], py[kSpec], pz[kSpec];
+  double2 rf[kSpec];
+  int ti[kSpec];
+  double tt[kSpec][kSpec];  // tt[k][a], k < a: trial a's pair term with k's particle
+  int terr[kSpec][kSpec];
+  double base[kSpec];       // the round's sums, totalled over the blocks
+  int aerr[kSpec];
+  double de0[kSpec];        // ΔE and acceptance with no acceptance earlier
+  int acc0[kSpec];          // in the round
+  int pbuf[kSpec], pdel[kSpec];  // buffer (0-based) whose count the attempt changed, by
+  int nat0[kMaxBuffers];    // the buffer counts at the start of the round
+  int scan[kGrandWarps][kSpec];
+  int nchg, chg[kSpec];     // slots the last round rewrote
+  int done;                 // attempts the round settled
+  int ntot, ff, nbuf;
   int nat[kMaxBuffers], ninsert[kMaxBuffers], nremove[kMaxBuffers], ntotat[kMaxBuffers];
   double dener_sum;
   // buffer parameters, 1-based as in KP
@@ -367,9 +404,6 @@ struct GrandState {
   double lzmin[kMaxBuffers + 1], lzmax[kMaxBuffers + 1];
   double rmin[kMaxBuffers + 1], rmax[kMaxBuffers + 1];
   int ibfftyp[kMaxBuffers + 1], qbias[kMaxBuffers + 1];
-  int scan[kGrandThreads / 32];
-  int found;
-  double red[kGrandThreads / 32], tot[1];
 };
 
 // The attempt's uniform draws, gcmc_uniform(seed, cycle, attempt, n) for
@@ -389,16 +423,16 @@ struct Draws {
   }
 };
 
-// The random part of one attempt's proposal (grand.f90:42-86), thread 0 of
-// block 0: insertion or deletion, the buffer, for an insertion its point by
-// rejection sampling inside the buffer (insert.f90), for a deletion the
-// uniform its rank is drawn from (find.f90).  None depends on the state.
+// The random part of one attempt's proposal (grand.f90:42-86): insertion
+// or deletion, the buffer, for an insertion its point by rejection sampling
+// inside the buffer (insert.f90), for a deletion the uniform its rank is
+// drawn from (find.f90).  None depends on the state.
 __device__ void propose_draws(const KP &p, uint64_t seed, uint64_t cycle, uint32_t attempt,
-                              GrandState &g) {
-  Trial t{};
+                              const GrandState &g, Trial &t, double &u_rank) {
+  t = Trial{};
   Draws d{seed, cycle, attempt};
-  const int nbuf = p.nbuffer;
-  double u_rank = 0.0;
+  const int nbuf = g.nbuf;
+  u_rank = 0.0;
   if (d.next() < 0.5) {
     const int ib = (int)((double)nbuf * d.next()) + 1;
     t.insert = 1;
@@ -433,270 +467,391 @@ __device__ void propose_draws(const KP &p, uint64_t seed, uint64_t cycle, uint32
     t.insert = 0;
   }
   t.draw = (int)d.n;
-  g.nx = t;
-  g.nx_u = u_rank;
-  g.nx_fields = 0;
 }
 
-// find.f90: the slot of the rank-th ion of buffer ib in slot order, -1 if
-// none; block 0, every thread, result in g.found.
-__device__ void find_rank(const KP &p, GrandState &g, int ib, int rank) {
-  __syncthreads();
-  if (threadIdx.x == 0) g.found = -1;
+// find.f90 for every deletion trial k of the round with need[k]: the slot
+// of the ip0[k]-th ion of buffer tr[k].ib in slot order into found[k] (left
+// at -1 if none).  Block 0, every thread; one pass over the buffer tags.
+__device__ void find_ranks(const KP &p, GrandState &g, int na) {
   const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5;
   const int lo = p.nsites + p.nfix, ntot = g.ntot;
   const int per = (ntot - lo + (int)blockDim.x - 1) / (int)blockDim.x;
   const int a = lo + threadIdx.x * per, b = min(ntot, a + per);
-  int c = 0;
-  for (int k = a; k < b; ++k) c += (p.ibuffer[k] == ib);
-  int incl = c;  // inclusive scan: warp shuffles, then the warp totals
+  int ib[kSpec], c[kSpec];
 #pragma unroll
-  for (int o = 1; o < 32; o <<= 1) {
-    const int v = __shfl_up_sync(0xffffffffu, incl, o);
-    if (lane >= o) incl += v;
+  for (int k = 0; k < kSpec; ++k) {
+    ib[k] = k < na && g.need[k] ? g.tr[k].ib : -1;
+    c[k] = 0;
   }
-  if (lane == 31) g.scan[wid] = incl;
-  __syncthreads();
-  int before = incl - c;
-  for (int w = 0; w < wid; ++w) before += g.scan[w];
-  if (rank > before && rank <= before + c) {  // exactly one thread
-    int r = before;
-    for (int k = a; k < b; ++k)
-      if (p.ibuffer[k] == ib && ++r == rank) {
-        g.found = k;
-        break;
-      }
+  for (int s = a; s < b; ++s) {
+    const int v = p.ibuffer[s];
+#pragma unroll
+    for (int k = 0; k < kSpec; ++k) c[k] += v == ib[k];
+  }
+  int before[kSpec];
+#pragma unroll
+  for (int k = 0; k < kSpec; ++k) {  // inclusive scans: warp shuffles, then warp totals
+    int incl = c[k];
+#pragma unroll
+    for (int o = 1; o < 32; o <<= 1) {
+      const int v = __shfl_up_sync(0xffffffffu, incl, o);
+      if (lane >= o) incl += v;
+    }
+    if (lane == 31) g.scan[wid][k] = incl;
+    before[k] = incl - c[k];
   }
   __syncthreads();
-}
-
-// The next trial's single-particle terms ahead of the pending acceptance,
-// block 0 (every thread).  An insertion's depend on its point only: warp 0
-// its terms, warp 1 its RFPAR (srfe, reff).  A deletion's are found in the
-// current state (its rank from the current buffer count, the slot, the
-// terms, warnings counted but not yet added): exact if the acceptance
-// changes nothing, else redone by propose_finish.
-__device__ void next_terms(const KP &p, uint32_t mask, GrandState &g) {
-  __syncthreads();
-  Trial t = g.nx;
-  if (t.insert) {
-    if (t.valid) {
-      t.j = p.nsites + 1;  // any ion slot: the terms of an ion at t's point
-      if (threadIdx.x < 32) {
-        trial_single_warp(p, t, mask, 0);
-        if (threadIdx.x == 0) {
-          g.nx.e_single = t.e_single;
-          g.nx.srfe = t.srfe;
-          g.nx.reff = t.reff;
-          g.nx.rf_in = t.rf_in;
+#pragma unroll
+  for (int k = 0; k < kSpec; ++k) {
+    if (ib[k] < 0) continue;
+    for (int w = 0; w < wid; ++w) before[k] += g.scan[w][k];
+    const int rank = g.ip0[k];
+    if (rank > before[k] && rank <= before[k] + c[k]) {  // exactly one thread
+      int r = before[k];
+      for (int s = a; s < b; ++s)
+        if (p.ibuffer[s] == ib[k] && ++r == rank) {
+          g.found[k] = s;
+          break;
         }
-      } else if (threadIdx.x == 32 && (mask & 16u) && p.qrfpar) {
-        g.nx_rf = rf_single(p, t.x, t.y, t.z, t.itype);
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x == 0) g.nx_fields = t.valid;
-    return;
-  }
-  const int nbuf = p.nbuffer, ib = t.ib;
-  const int natb = ib <= nbuf ? g.nat[ib - 1] : 0;
-  const int ip = (int)((double)natb * g.nx_u) + 1;
-  if (!(ib <= nbuf && ip <= natb)) return;  // block-uniform: nothing to find
-  find_rank(p, g, ib, ip);
-  const int k = g.found;
-  if (k < 0 || k >= g.ntot) return;
-  t.itype = g.ibfftyp[ib];
-  t.valid = 1;
-  t.j = k + 1;
-  const double3 q = pos_of(p, g.ff, k);
-  t.x = q.x;
-  t.y = q.y;
-  t.z = q.z;
-  if (threadIdx.x == 0) g.nx_alert = 0;
-  __syncthreads();
-  if (threadIdx.x < 32) {
-    trial_single_warp(p, t, mask, 1, &g.nx_alert);
-    if (threadIdx.x == 0) {
-      g.nx = t;
-      g.nx_fields = 1;
     }
   }
   __syncthreads();
 }
 
-// The state-dependent part of the proposal, block 0: the live count, for a
-// deletion the rank-th ion of the buffer in slot order (find.f90) and its
-// single-particle terms (deletion trials raise warnings as INTERACT with
-// Qalert does, insertion trials do not: grand.f90:48,86); g.nx -> g.s.
-// Terms that next_terms found ahead are kept when they still hold: always
-// for an insertion, for a deletion when the acceptance changed nothing.
-__device__ void propose_finish(const KP &p, uint32_t mask, GrandState &g) {
-  __syncthreads();
-  const bool keep = g.nx_fields && (g.nx.insert || g.chg < 0);
-  if (threadIdx.x == 0) {
-    Trial t = g.nx;
-    const int ntot = g.ntot, nbuf = p.nbuffer;
-    if (t.insert) {
-      t.j = ntot + 1;
-    } else if (keep) {
-      if (g.nx_alert > 0) atomicAdd(&p.warn[p.nwtype[t.itype]], g.nx_alert);
-    } else {
-      const int ib = t.ib;
-      const int natb = ib <= nbuf ? g.nat[ib - 1] : 0;
-      const int ip = (int)((double)natb * g.nx_u) + 1;
-      t.valid = 0;
-      if (ib <= nbuf && ip <= natb) {
-        t.itype = g.ibfftyp[ib];
-        t.valid = 1;
-        t.j = ip;  // rank within the buffer; resolved to a slot below
-      }
-    }
-    t.ntot = ntot;
-    t.chg = g.chg;
-    g.s = t;
-    if (t.insert) g.trial_rf = g.nx_rf;
-  }
-  __syncthreads();
-  if (keep) return;
-  const Trial &s = g.s;
-  if (s.valid && !s.insert) {
-    find_rank(p, g, s.ib, s.j);
-    if (threadIdx.x == 0) {
-      const int k = g.found;
-      if (k < 0 || guard_bad(p.st, k, g.ntot, 11)) {
-        g.s.valid = 0;
-        atomicOr(&p.st->err, kErrFind);
-      } else {
-        g.s.j = k + 1;
-        const double3 q = pos_of(p, g.ff, k);
-        g.s.x = q.x;
-        g.s.y = q.y;
-        g.s.z = q.z;
-      }
-    }
-    __syncthreads();
-    if (threadIdx.x < 32 && g.s.valid) {
-      Trial t = g.s;
-      trial_single_warp(p, t, mask, 1);
-      if (threadIdx.x == 0) g.s = t;
-    }
-  } else if (s.valid && s.insert) {  // not computed ahead
-    if (threadIdx.x < 32) {
-      Trial t = g.s;
-      trial_single_warp(p, t, mask, 0);
-      if (threadIdx.x == 0) g.s = t;
-    } else if (threadIdx.x == 32 && (mask & 16u) && p.qrfpar) {
-      g.trial_rf = rf_single(p, g.s.x, g.s.y, g.s.z, g.s.itype);
-    }
-  }
-  __syncthreads();
-}
-
-// Total ΔE, Im-Roux acceptance and the insertion/deletion (grand.f90:48-116)
-// of the current trial; block 0, state in g.  g.chg: the slot an accepted
-// move rewrote (the new ion's, or the deleted ion's that the last ion
-// fills), -1 otherwise.
-__device__ void accept(const KP &p, uint32_t mask, int nblk, uint64_t seed, uint64_t cycle,
-                       uint32_t attempt, GrandState &g) {
-  const Trial &tr = g.s;
-  const bool rf_on = (mask & 16u) && p.qrfpar;
-  double dener = 0.0;
-  if (tr.valid) dener = interact_total(p, tr, nblk, g.red, g.tot);
-  if (threadIdx.x == 0) g.chg = -1;
-  if (threadIdx.x == 0 && tr.valid && !guard_bad(p.st, tr.ib - 1, p.nbuffer, 21)) {
-    const int ib = tr.ib, b = ib - 1;
-    const int nat = g.nat[b];
-    const double boltz = exp(-(dener - g.mu[ib]) * p.ikbt);
-    double rate;
+// The round's trials (block 0, every thread): attempts a0 .. a0+na-1
+// proposed in the current state, with their single-particle terms
+// (deletion trials count their warnings in nalert, insertion trials raise
+// none: grand.f90:48,86) and acceptance draws.
+__device__ void build_round(const KP &p, uint32_t mask, uint64_t seed, uint64_t cycle, int a0,
+                            int na, GrandState &g) {
+  const int t = threadIdx.x;
+  if (t < na) {
+    Trial tr;
+    double u = 0.0;
+    propose_draws(p, seed, cycle, (uint32_t)(a0 + t), g, tr, u);
+    tr.ntot = g.ntot;
+    tr.chg = -1;
+    g.need[t] = 0;
+    g.found[t] = -1;
+    g.nalert[t] = 0;
+    g.ip0[t] = 0;
     if (tr.insert) {
-      if (g.qbias[ib]) {
-        rate = g.avnum[ib] + g.kbb[ib] * (g.avnum[ib] - (double)(g.ntotat[b] / (long long)cycle));
-        rate = rate * boltz / (double)(nat + 1);
-      } else {
-        rate = (g.avnum[ib] / (nat + 1)) * boltz;
-      }
-      rate = rate / (1.0 + rate);
+      tr.j = g.ntot + 1;
     } else {
-      if (g.qbias[ib]) {
-        rate = g.avnum[ib] + g.kbb[ib] * (g.avnum[ib] - (double)(g.ntotat[b] / (long long)cycle));
-        rate = rate * boltz / (double)nat;
-      } else {
-        rate = (g.avnum[ib] / nat) * boltz;
+      const int ib = tr.ib;
+      const int natb = ib <= g.nbuf ? g.nat[ib - 1] : 0;
+      const int ip = (int)((double)natb * u) + 1;
+      tr.valid = 0;
+      if (ib <= g.nbuf && ip <= natb) {
+        tr.itype = g.ibfftyp[ib];
+        tr.valid = 1;
+        g.need[t] = 1;
+        g.ip0[t] = ip;
       }
-      rate = 1.0 / (1.0 + rate);
     }
-    if (gcmc_uniform(seed, cycle, attempt, (uint32_t)tr.draw) <= rate) {
-      const int ntot = g.ntot;
-      if (tr.insert) {
-        if (ntot + 1 > p.cap) {
-          atomicOr(&p.st->err, kErrCapacity);
-        } else if (!guard_bad(p.st, ntot, p.cap, 22)) {
-          g.dener_sum += dener;
-          g.nat[b] = nat + 1;
-          if (g.ff) {  // the records as k_pack forms them (a mobile ion)
-            const float xh = (float)tr.x, yh = (float)tr.y, zh = (float)tr.z;
-            const int code = (p.nwtype[tr.itype] - 1) | (1 << 16);
-            p.pk1[ntot] = make_float4(xh, yh, zh, __int_as_float(code));
-            p.pk2[ntot] = make_float4((float)(tr.x - (double)xh), (float)(tr.y - (double)yh),
-                                      (float)(tr.z - (double)zh), 0.0f);
-            p.pk3[ntot] = make_float4(0.0f, (float)p.cg[tr.itype], __int_as_float(1 << 1), 0.0f);
-          } else {
-            p.x[ntot] = tr.x;
-            p.y[ntot] = tr.y;
-            p.z[ntot] = tr.z;
-          }
-          p.typei[ntot] = tr.z < p.cz ? -tr.itype : tr.itype;
-          p.ibuffer[ntot] = ib;
-          if (rf_on) p.gc_rf[ntot] = g.trial_rf;
-          g.ntot = ntot + 1;
-          g.ninsert[b] += 1;
-          g.chg = ntot;
-        }
-      } else if (!guard_bad(p.st, tr.j - 1, ntot, 23) &&
-                 !guard_bad(p.st, ntot - 1, p.cap, 24)) {
-        const int iat = tr.j - 1, last = ntot - 1;
-        g.dener_sum -= dener;
-        g.nremove[b] += 1;
-        if (g.ff) {
-          p.pk1[iat] = __ldcg(p.pk1 + last);
-          p.pk2[iat] = __ldcg(p.pk2 + last);
-          p.pk3[iat] = __ldcg(p.pk3 + last);
-        } else {
-          p.x[iat] = p.x[last];
-          p.y[iat] = p.y[last];
-          p.z[iat] = p.z[last];
-        }
-        p.typei[iat] = p.typei[last];
-        p.ibuffer[iat] = p.ibuffer[last];
-        if (rf_on) p.gc_rf[iat] = __ldcg(p.gc_rf + last);
-        g.nat[b] = nat - 1;
-        g.ntot = ntot - 1;
-        g.chg = iat;
+    g.tr[t] = tr;
+    g.u_rank[t] = u;
+    g.u_acc[t] = gcmc_uniform(seed, cycle, (uint32_t)(a0 + t), (uint32_t)tr.draw);
+  }
+  __syncthreads();
+  find_ranks(p, g, na);
+  if (t < na && g.need[t]) {
+    Trial &tr = g.tr[t];
+    const int k = g.found[t];
+    if (k < 0 || guard_bad(p.st, k, g.ntot, 11)) {
+      tr.valid = 0;
+      g.ip0[t] = 0;
+      atomicOr(&p.st->err, kErrFind);
+    } else {
+      tr.j = k + 1;
+      const double3 q = pos_of(p, g.ff, k);
+      tr.x = q.x;
+      tr.y = q.y;
+      tr.z = q.z;
+    }
+  }
+  __syncthreads();
+  for (int k = t >> 5; k < na; k += kGrandWarps) {
+    Trial tr = g.tr[k];
+    if (tr.valid) {
+      trial_single_warp(p, tr, mask, tr.insert ? 0 : 1, &g.nalert[k]);
+      if ((t & 31) == 0) {
+        g.tr[k].e_single = tr.e_single;
+        g.tr[k].srfe = tr.srfe;
+        g.tr[k].reff = tr.reff;
+        g.tr[k].rf_in = tr.rf_in;
       }
     }
   }
   __syncthreads();
-  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x)  // prob(ib, nat(ib)) += 1
-    if (!guard_bad(p.st, g.nat[b], p.cap + 1, 25))
-      atomicAdd(&p.prob[(size_t)b * (p.cap + 1) + g.nat[b]], 1);
+}
+
+// A coordinate as its float-float record stores it (hi = fl(x), lo =
+// fl(x - hi)), read back as hi + lo.
+__device__ __forceinline__ double ff_rounded(double x) {
+  const float h = (float)x;
+  return (double)h + (double)(float)(x - (double)h);
+}
+
+// Each trial's particle as an ion record holds it (block 0, a thread per
+// trial): an insertion's what its acceptance writes (the point, rounded to
+// the float-float record in FP32 mode; the signed type; RFPAR at the
+// record's point), a deletion's its target's record.
+__device__ void trial_ions(const KP &p, uint32_t mask, int na, GrandState &g) {
+  const int t = threadIdx.x;
+  const bool rf_on = (mask & 16u) && p.qrfpar;
+  if (t < na) {
+    const Trial &tr = g.tr[t];
+    double x = tr.x, y = tr.y, z = tr.z;
+    int ti = 0;
+    double2 rf = make_double2(0.0, 0.0);
+    if (tr.valid) {
+      if (tr.insert) {
+        if (g.ff) {
+          x = ff_rounded(x);
+          y = ff_rounded(y);
+          z = ff_rounded(z);
+        }
+        ti = tr.z < p.cz ? -tr.itype : tr.itype;
+      } else {
+        ti = p.typei[tr.j - 1];
+      }
+      if (rf_on) rf = rf_single(p, x, y, z, abs(ti));
+    }
+    g.px[t] = x;
+    g.py[t] = y;
+    g.pz[t] = z;
+    g.ti[t] = ti;
+    g.rf[t] = rf;
+  }
+}
+
+// Trial-trial pair terms (block 0, a thread per pair k < a): trial a's
+// INTERACT term with trial k's particle as an ion record holds it.
+__device__ void trial_pairs(const KP &p, uint32_t mask, int na, GrandState &g) {
+  for (int idx = threadIdx.x; idx < na * na; idx += blockDim.x) {
+    const int k = idx / na, a = idx - k * na;
+    if (k >= a) continue;
+    const Trial &ta = g.tr[a], &tk = g.tr[k];
+    double v = 0.0;
+    int err = 0;
+    // two deletions of one ion are never both settled (the first touches
+    // the buffer of the second)
+    if (ta.valid && tk.valid && (ta.insert || tk.insert || ta.j != tk.j)) {
+      const int jt2 = trial_type2(p, ta);
+      if (jt2 > 0) {
+        PartRec q;
+        q.x = g.px[k];
+        q.y = g.py[k];
+        q.z = g.pz[k];
+        q.rf = g.rf[k];
+        q.ti = g.ti[k];
+        v = interact_rec(p, ta, mask, p.nsites, jt2, true, ta.rf_in && (mask & 16u), q, err);
+      }
+    }
+    g.tt[k][a] = v;
+    g.terr[k][a] = err;
+  }
+}
+
+// Totals of the round's block partials (block 0): warp w for attempts w,
+// w + kGrandWarps, ...; a fixed summation order.
+__device__ void round_sums(const KP &p, int na, GrandState &g) {
+  const int lane = threadIdx.x & 31, nblk = gridDim.x;
+  for (int a = threadIdx.x >> 5; a < na; a += kGrandWarps) {
+    double v = 0.0;
+    int e = 0;
+    for (int b = 1 + lane; b < nblk; b += 32) {
+      v += __ldcg(p.ipart + (size_t)b * kSpec + a);
+      e |= __ldcg(p.ierr + (size_t)b * kSpec + a);
+    }
+    v = wsum(v);
+    e = __reduce_or_sync(0xffffffffu, e);
+    if (lane == 0) {
+      g.base[a] = v;
+      g.aerr[a] = e;
+    }
+  }
+}
+
+// Im-Roux acceptance probability of trial tr with total ΔE de in the
+// current state (grand.f90:88-116).
+__device__ double accept_rate(const KP &p, const GrandState &g, const Trial &tr, double de,
+                              uint64_t cycle) {
+  const int ib = tr.ib, b = ib - 1;
+  const int nat = g.nat[b];
+  const double boltz = exp(-(de - g.mu[ib]) * p.ikbt);
+  double rate;
+  if (tr.insert) {
+    if (g.qbias[ib]) {
+      rate = g.avnum[ib] + g.kbb[ib] * (g.avnum[ib] - (double)(g.ntotat[b] / (long long)cycle));
+      rate = rate * boltz / (double)(nat + 1);
+    } else {
+      rate = (g.avnum[ib] / (nat + 1)) * boltz;
+    }
+    return rate / (1.0 + rate);
+  }
+  if (g.qbias[ib]) {
+    rate = g.avnum[ib] + g.kbb[ib] * (g.avnum[ib] - (double)(g.ntotat[b] / (long long)cycle));
+    rate = rate * boltz / (double)nat;
+  } else {
+    rate = (g.avnum[ib] / nat) * boltz;
+  }
+  return 1.0 / (1.0 + rate);
+}
+
+// ΔE and acceptance of every attempt as if no attempt before it in the
+// round were accepted (block 0, a thread per attempt): exact up to the
+// round's first acceptance.
+__device__ void first_acceptances(const KP &p, uint64_t cycle, int na, GrandState &g) {
+  const int a = threadIdx.x;
+  if (a >= na) return;
+  const Trial &tr = g.tr[a];
+  g.de0[a] = 0.0;
+  g.acc0[a] = 0;
+  if (tr.valid && tr.ib >= 1 && tr.ib <= g.nbuf) {
+    const double de = tr.e_single + g.base[a];
+    g.de0[a] = de;
+    g.acc0[a] = g.u_acc[a] <= accept_rate(p, g, tr, de, cycle);
+  }
+}
+
+// The round's attempts in order (block 0, thread 0): ΔE, acceptance and the
+// insertion or deletion (grand.f90:48-116), until an attempt whose trial no
+// longer holds.  g.done: the attempts settled; g.chg: the slots rewritten.
+__device__ void settle(const KP &p, uint32_t mask, uint64_t cycle, int na, GrandState &g) {
+  const bool rf_on = (mask & 16u) && p.qrfpar;
+  bool changed = false;
+  unsigned long long touched = 0;  // bit b: an accepted deletion touched buffer b + 1
+  int nacc = 0, acc_k[kSpec];
+  double acc_s[kSpec];
+  int done = 0;
+  g.nchg = 0;
+  for (int a = 0; a < na; ++a) {
+    Trial tr = g.tr[a];
+    if (changed && !tr.insert) {  // the deletion trial in the current state
+      const int ib = tr.ib;
+      const int natb = ib <= g.nbuf ? g.nat[ib - 1] : 0;
+      const int ip = (int)((double)natb * g.u_rank[a]) + 1;
+      if (!(ib <= g.nbuf && ip <= natb))
+        tr.valid = 0;  // no ion left to delete: the attempt does nothing
+      else if (g.ip0[a] == 0 || ip != g.ip0[a] || ((touched >> (ib - 1)) & 1ull))
+        break;  // another target: propose it again in the next round
+    }
+    g.pbuf[a] = -1;
+    g.pdel[a] = 0;
+    int err = 0;
+    if (tr.valid && !guard_bad(p.st, tr.ib - 1, p.nbuffer, 21)) {
+      const int ib = tr.ib, b = ib - 1;
+      double de;
+      bool yes;
+      err = g.aerr[a];
+      if (!changed) {
+        de = g.de0[a];
+        yes = g.acc0[a] != 0;
+      } else {
+        double c = 0.0;
+        for (int m = 0; m < nacc; ++m) {
+          c += acc_s[m] * g.tt[acc_k[m]][a];
+          err |= g.terr[acc_k[m]][a];
+        }
+        de = tr.e_single + g.base[a] + c;
+        yes = g.u_acc[a] <= accept_rate(p, g, tr, de, cycle);
+      }
+      if (!tr.insert && g.nalert[a] > 0) atomicAdd(&p.warn[p.nwtype[tr.itype]], g.nalert[a]);
+      if (yes) {
+        const int ntot = g.ntot, nat = g.nat[b];
+        if (tr.insert) {
+          if (ntot + 1 > p.cap) {
+            atomicOr(&p.st->err, kErrCapacity);
+          } else if (!guard_bad(p.st, ntot, p.cap, 22)) {
+            g.dener_sum += de;
+            g.nat[b] = nat + 1;
+            if (g.ff) {  // the records as k_pack forms them (a mobile ion)
+              const float xh = (float)tr.x, yh = (float)tr.y, zh = (float)tr.z;
+              const int code = (p.nwtype[tr.itype] - 1) | (1 << 16);
+              p.pk1[ntot] = make_float4(xh, yh, zh, __int_as_float(code));
+              p.pk2[ntot] = make_float4((float)(tr.x - (double)xh), (float)(tr.y - (double)yh),
+                                        (float)(tr.z - (double)zh), 0.0f);
+              p.pk3[ntot] =
+                  make_float4(0.0f, (float)p.cg[tr.itype], __int_as_float(1 << 1), 0.0f);
+            } else {
+              p.x[ntot] = tr.x;
+              p.y[ntot] = tr.y;
+              p.z[ntot] = tr.z;
+            }
+            p.typei[ntot] = g.ti[a];
+            p.ibuffer[ntot] = ib;
+            if (rf_on) p.gc_rf[ntot] = g.rf[a];
+            g.ntot = ntot + 1;
+            g.ninsert[b] += 1;
+            g.chg[g.nchg++] = ntot;
+            g.pbuf[a] = b;
+            g.pdel[a] = 1;
+            acc_k[nacc] = a;
+            acc_s[nacc++] = 1.0;
+            changed = true;
+          }
+        } else if (!guard_bad(p.st, tr.j - 1, ntot, 23) &&
+                   !guard_bad(p.st, ntot - 1, p.cap, 24)) {
+          const int iat = tr.j - 1, last = ntot - 1;
+          const int bz = p.ibuffer[last];  // the ion the freed slot receives
+          g.dener_sum -= de;
+          g.nremove[b] += 1;
+          if (g.ff) {
+            p.pk1[iat] = __ldcg(p.pk1 + last);
+            p.pk2[iat] = __ldcg(p.pk2 + last);
+            p.pk3[iat] = __ldcg(p.pk3 + last);
+          } else {
+            p.x[iat] = p.x[last];
+            p.y[iat] = p.y[last];
+            p.z[iat] = p.z[last];
+          }
+          p.typei[iat] = p.typei[last];
+          p.ibuffer[iat] = bz;
+          if (rf_on) p.gc_rf[iat] = __ldcg(p.gc_rf + last);
+          g.nat[b] = nat - 1;
+          g.ntot = ntot - 1;
+          g.chg[g.nchg++] = iat;
+          g.pbuf[a] = b;
+          g.pdel[a] = -1;
+          touched |= 1ull << b;
+          if (bz >= 1 && bz <= kMaxBuffers) touched |= 1ull << (bz - 1);
+          acc_k[nacc] = a;
+          acc_s[nacc++] = -1.0;
+          changed = true;
+        }
+      }
+    }
+    if (err) atomicOr(&p.st->err, err);
+    done = a + 1;
+  }
+  g.done = done;
+}
+
+// prob(ib, nat(ib)) += 1 after each settled attempt (grand.f90:117-119),
+// a thread per buffer replaying the round's count changes.
+__device__ void round_histogram(const KP &p, GrandState &g) {
+  for (int b = threadIdx.x; b < g.nbuf; b += blockDim.x) {
+    int n = g.nat0[b];
+    for (int a = 0; a < g.done; ++a) {
+      if (g.pbuf[a] == b) n += g.pdel[a];
+      if (!guard_bad(p.st, n, p.cap + 1, 25)) atomicAdd(&p.prob[(size_t)b * (p.cap + 1) + n], 1);
+    }
+  }
 }
 
 __global__ void __launch_bounds__(kGrandThreads)
     k_grand(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, int ngcmc, int ffpos) {
   __shared__ GrandState g;
+  __shared__ double red[kGrandWarps * kSpec];
+  __shared__ int ered[kGrandWarps * kSpec];
   __shared__ int flag;
   DevState *st = p.st;
-  const bool b0 = blockIdx.x == 0;
-  // particles round-robin over the blocks; with more than one block, block 0
-  // only coordinates (its proposals and acceptances stay off the ΔE sums)
-  const int nwb = gridDim.x > 1 ? gridDim.x - 1 : 1;
-  const bool owns = gridDim.x == 1 || !b0;
-  const int nthr = nwb * blockDim.x;
-  const int gtid = owns ? threadIdx.x * nwb + (gridDim.x > 1 ? blockIdx.x - 1 : 0) : nthr;
   const bool rf_on = (mask & 16u) && p.qrfpar;
   const int ntot0 = st->ntot;
   bool ok = true;
-  if (b0) {  // GCMC state into shared memory, then the first proposal
+  if (blockIdx.x == 0) {  // the coordinator: GCMC state into shared memory
     const int nb = p.nbuffer;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       g.nat[b] = st->nat[b];
@@ -718,69 +873,45 @@ __global__ void __launch_bounds__(kGrandThreads)
     if (threadIdx.x == 0) {
       g.ntot = ntot0;
       g.dener_sum = st->dener_sum;
-      g.chg = -1;
       g.ff = ffpos;
+      g.nbuf = nb;
+      g.nchg = 0;
     }
     __syncthreads();
-    if (ngcmc > 0) {
-      if (threadIdx.x == 0) propose_draws(p, seed, cycle, 0u, g);
-      propose_finish(p, mask, g);
-      if (threadIdx.x == 0) {
-        *p.trial = g.s;
+    int a0 = 0;
+    for (unsigned r = 1; ok; ++r) {
+      const int na = min(ngcmc - a0, kSpec);
+      if (na > 0) build_round(p, mask, seed, cycle, a0, na, g);
+      if (threadIdx.x == 0) {  // publish the round
+        GrandRound *hd = p.ground;
+        hd->a0 = a0;
+        hd->na = na;
+        hd->ntot = g.ntot;
+        hd->nchg = g.nchg;
+        for (int c = 0; c < g.nchg; ++c) hd->chg[c] = g.chg[c];
+        for (int k = 0; k < na; ++k) p.trial[k] = g.tr[k];
+        __threadfence();
         release_add(&st->bar_gen, 1u);
       }
+      if (na <= 0) break;
+      trial_ions(p, mask, na, g);
+      for (int b = threadIdx.x; b < nb; b += blockDim.x) g.nat0[b] = g.nat[b];
+      __syncthreads();
+      trial_pairs(p, mask, na, g);
+      if (!(ok = block_wait(&st->bar_count, (unsigned)(gridDim.x - 1) * r, st, &flag))) break;
+      round_sums(p, na, g);
+      __syncthreads();
+      first_acceptances(p, cycle, na, g);
+      __syncthreads();
+      if (threadIdx.x == 0) settle(p, mask, cycle, na, g);
+      __syncthreads();
+      round_histogram(p, g);
+      a0 += g.done;
+      __syncthreads();
     }
-  }
-  if (rf_on)  // RFPAR prepass, each thread its own particles
-    for (int i = gtid; i < ntot0; i += nthr)
-      if (i >= p.nsites) {
-        const double3 q = pos_of(p, ffpos, i);
-        p.gc_rf[i] = rf_single(p, q.x, q.y, q.z, abs(p.typei[i]));
-      }
-  // this thread's first particle, read ahead of each attempt
-  PartRec pre{};
-  if (gtid < ntot0) pre = load_part(p, gtid, rf_on, ffpos);
-  for (int a = 0; a < ngcmc && ok; ++a) {
-    if (!b0 && !(ok = block_wait(&st->bar_gen, (unsigned)(a + 1), st, &flag))) break;
-    const Trial tr = b0 ? g.s : load_trial_cg(p.trial);
-    const int jt2 = trial_type2(p, tr);
-    const bool beion = tr.valid && tr.j - 1 >= p.nsites;
-    const bool rf = tr.valid && tr.rf_in && (mask & 16u);
-    if (gtid == tr.chg) pre = load_part(p, gtid, rf_on, ffpos);  // rewritten by the last move
-    double u = 0.0;
-    int err = 0;
-    if (jt2 > 0)
-      for (int i = gtid; i < tr.ntot; i += nthr)
-        if (i != tr.j - 1)
-          u += i == gtid ? interact_rec(p, tr, mask, i, jt2, beion, rf, pre, err)
-                         : interact_one(p, tr, mask, i, jt2, beion, rf, err, ffpos);
-    if (err) atomicOr(&st->err, err);
-    double *red = g.red, *tot = g.tot;
-    block_sum<1>(&u, red, tot);
-    if (threadIdx.x == 0) {
-      p.ipart[blockIdx.x] = tot[0];
-      release_add(&st->bar_count, 1u);
-    }
-    if (b0) {
-      const bool more = a + 1 < ngcmc;
-      if (more) {  // the next attempt's draws (and insertion terms) meanwhile
-        if (threadIdx.x == 0) propose_draws(p, seed, cycle, (uint32_t)(a + 1), g);
-        next_terms(p, mask, g);
-      }
-      if (!(ok = block_wait(&st->bar_count, (unsigned)(gridDim.x * (a + 1)), st, &flag))) break;
-      accept(p, mask, gridDim.x, seed, cycle, (uint32_t)a, g);
-      if (more) {
-        propose_finish(p, mask, g);
-        if (threadIdx.x == 0) {
-          *p.trial = g.s;
-          release_add(&st->bar_gen, 1u);
-        }
-      }
-    }
-  }
-  if (b0) {  // GCMC state back to the device record (also after a failed wait)
+    // GCMC state back to the device record (also after a failed wait)
     __syncthreads();
-    for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) {
+    for (int b = threadIdx.x; b < nb; b += blockDim.x) {
       st->nat[b] = g.nat[b];
       st->ninsert[b] = g.ninsert[b];
       st->nremove[b] = g.nremove[b];
@@ -789,11 +920,83 @@ __global__ void __launch_bounds__(kGrandThreads)
       st->ntot = g.ntot;
       st->dener_sum = g.dener_sum;
     }
+    return;
+  }
+  // blocks 1..: the pair terms.  Warp wg of the pair phase holds particles
+  // wg * per_warp + lane / ap, then + stride, ...; lane & (ap - 1) is the
+  // lane's attempt within the round.
+  const int ap = grand_lanes(ngcmc), per_warp = 32 / ap;
+  const int lane = threadIdx.x & 31, wid = threadIdx.x >> 5, la = lane & (ap - 1);
+  const int stride = (gridDim.x - 1) * kGrandWarps * per_warp;
+  const int i0 = ((blockIdx.x - 1) * kGrandWarps + wid) * per_warp + lane / ap;
+  // RFPAR prepass: one lane per particle, at its position; the first
+  // particle's record (its RFPAR from that lane) is kept across rounds
+  double2 rf0 = make_double2(0.0, 0.0);
+  if (rf_on && la == 0)
+    for (int i = i0; i < ntot0; i += stride)
+      if (i >= p.nsites) {
+        const double3 q = pos_of(p, ffpos, i);
+        const double2 v = rf_single(p, q.x, q.y, q.z, abs(p.typei[i]));
+        p.gc_rf[i] = v;
+        if (i == i0) rf0 = v;
+      }
+  PartRec pre{};
+  if (i0 < ntot0) pre = load_part(p, i0, false, ffpos);
+  pre.rf.x = __shfl_sync(0xffffffffu, rf0.x, lane & ~(ap - 1));
+  pre.rf.y = __shfl_sync(0xffffffffu, rf0.y, lane & ~(ap - 1));
+  for (unsigned r = 1; ok; ++r) {
+    if (!(ok = block_wait(&st->bar_gen, r, st, &flag))) break;
+    const GrandRound *hd = p.ground;
+    const int na = __ldcg(&hd->na);
+    if (na <= 0) break;
+    const int ntot = __ldcg(&hd->ntot), nchg = __ldcg(&hd->nchg);
+    for (int c = 0; c < nchg; ++c)  // the previous round rewrote this slot
+      if (__ldcg(&hd->chg[c]) == i0 && i0 < ntot) pre = load_part(p, i0, rf_on, ffpos);
+    Trial tr{};
+    if (la < na) tr = load_trial_cg(p.trial + la);
+    const int jt2 = trial_type2(p, tr);
+    const bool beion = tr.valid && tr.j - 1 >= p.nsites;
+    const bool rf = tr.valid && tr.rf_in && (mask & 16u);
+    double u = 0.0;
+    int err = 0;
+    if (jt2 > 0)
+      for (int i = i0; i < ntot; i += stride)
+        if (i != tr.j - 1)
+          u += i == i0 ? interact_rec(p, tr, mask, i, jt2, beion, rf, pre, err)
+                       : interact_one(p, tr, mask, i, jt2, beion, rf, err, ffpos);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      if (o >= ap) {  // lanes of one attempt
+        u += __shfl_xor_sync(0xffffffffu, u, o);
+        err |= __shfl_xor_sync(0xffffffffu, err, o);
+      }
+    if (lane < ap) {
+      red[wid * kSpec + lane] = u;
+      ered[wid * kSpec + lane] = err;
+    }
+    __syncthreads();
+    if (threadIdx.x < na) {
+      double s = 0.0;
+      int e = 0;
+      for (int w = 0; w < kGrandWarps; ++w) {
+        s += red[w * kSpec + threadIdx.x];
+        e |= ered[w * kSpec + threadIdx.x];
+      }
+      p.ipart[(size_t)blockIdx.x * kSpec + threadIdx.x] = s;
+      p.ierr[(size_t)blockIdx.x * kSpec + threadIdx.x] = e;
+    }
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      __threadfence();
+      release_add(&st->bar_count, 1u);
+    }
   }
 }
 
-// Blocks of the GRAND launch: about one per 64 particles, all co-resident,
-// at most the ipart slots the context holds (ipart_slots).
+// Blocks of the GRAND launch: the coordinator and enough blocks for a lane
+// per (particle, attempt of a round), all co-resident, at most the partial
+// slots the context holds (ipart_slots); with fewer, a lane takes several
+// particles.
 cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
                          uint64_t seed, uint64_t cycle, int ngcmc, int ffpos,
                          cudaStream_t stream) {
@@ -809,10 +1012,12 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
       return e;
     if ((e = cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev)) != cudaSuccess)
       return e;
-    max_res[dev] = std::max(1, per_sm * nsm);
+    max_res[dev] = std::max(2, per_sm * nsm);
   }
-  int grid = (ntot_ub + ngcmc + 63) / 64 + 1;  // + block 0, the coordinator
-  grid = std::max(1, std::min(std::min(grid, max_res[dev]), ipart_slots));
+  const int per_warp = 32 / grand_lanes(ngcmc);
+  const int warps = (ntot_ub + ngcmc + per_warp - 1) / per_warp;
+  int grid = (warps + kGrandWarps - 1) / kGrandWarps + 1;  // + block 0, the coordinator
+  grid = std::max(2, std::min(std::min(grid, max_res[dev]), ipart_slots));
   // both launch counters start at zero
   if ((e = cudaMemsetAsync(&p.st->bar_count, 0, 2 * sizeof(unsigned), stream)) != cudaSuccess)
     return e;

@@ -132,7 +132,8 @@ struct KP {
   const double *avnum, *mu, *kbb, *lzmin, *lzmax, *rmin, *rmax;
   const uint8_t *qbufferbias;
   int *prob;                    // [nbuffer*(cap+1)]
-  Trial *trial;
+  Trial *trial;                 // [kSpec] INTERACT's trial; GRAND's round trials
+  GrandRound *ground;           // GRAND's round header
   double2 *gc_rf;               // [cap] RFPAR (srfe, reff) of each ion for
                                 // INTERACT's cross term, (0,0) off the map
   // ---- scratch ----
@@ -163,7 +164,9 @@ struct KP {
   double *epart;                // [nslot*kNTerms] block partial energies
   double *eterms;               // [kNTerms] reduced energies
   int *warn;                    // [nttyp+1]
-  double *ipart;                // [nslot] INTERACT block partials
+  double *ipart;                // [nslot*kSpec] INTERACT (per block) and GRAND
+                                // (per block and attempt) partial sums
+  int *ierr;                    // [nslot*kSpec] GRAND: error flags of the partials
 };
 
 }  // namespace bgpu

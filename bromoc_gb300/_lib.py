@@ -102,7 +102,7 @@ def efpot_from_knots(r, u, fct, qchr):
     return abi.efpot_from_knots(load(), PREFIX, r, u, fct, qchr)
 
 
-K_PAIRS, K_RFCROSS, K_FIELDS, K_ASSEMBLE, K_LOOP = 0, 1, 2, 3, 4
+K_PAIRS, K_RFCROSS, K_FIELDS, K_ASSEMBLE, K_LOOP, K_GRAND = 0, 1, 2, 3, 4, 5
 
 
 def live_count_async(eng: abi.Engine, dst_ptr: int) -> None:

@@ -85,6 +85,12 @@ int set_err(bromoc_ctx *c, int code, const char *fmt, ...) {
       return set_err(ctx, BROMOC_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
+// A double as the nearest float plus the nearest float of the remainder.
+float2 ffsplit(double v) {
+  const float h = (float)v;
+  return make_float2(h, (float)(v - (double)h));
+}
+
 template <class T>
 int dalloc(bromoc_ctx *ctx, T **p, size_t n) {
   *p = nullptr;
@@ -279,6 +285,8 @@ int ensure_scratch(bromoc_ctx *ctx) {
   if ((rc = dalloc(ctx, &p.ierr, ((size_t)tiles + 2) * kSpec))) return rc;
   ctx->ipart_slots = tiles + 2;
   if ((rc = dalloc(ctx, &p.gc_rf, cap))) return rc;
+  if ((rc = dalloc(ctx, &p.gc_rff, cap))) return rc;
+  if ((rc = dalloc(ctx, &p.tff, kSpec))) return rc;
   if ((rc = dalloc(ctx, &p.rf_srfe, cap))) return rc;
   if ((rc = dalloc(ctx, &p.rf_reff, cap))) return rc;
   if ((rc = dalloc(ctx, &p.rf_d1, 3 * cap))) return rc;
@@ -427,6 +435,8 @@ int device_err_result(bromoc_ctx *ctx, int e) {
     int bad[3] = {0, 0, 0};
     CU(cudaMemcpy(bad, &ctx->kp.st->bad_site, sizeof bad, cudaMemcpyDeviceToHost));
     CU(cudaMemsetAsync(&ctx->kp.st->err, 0, 4 * sizeof(int), ctx->stream));
+    if (e & kErrBarrier)  // every block passes launch_exit; clear the counters all the same
+      CU(cudaMemsetAsync(&ctx->kp.st->bar_count, 0, 3 * sizeof(unsigned), ctx->stream));
     CU(cudaStreamSynchronize(ctx->stream));
     if (e == kErrCapacity)
       return set_err(ctx, BROMOC_E_CAPACITY, "grand: ntot is greater than capacity");
@@ -612,6 +622,15 @@ int bromoc_gpu_set_types(bromoc_ctx *ctx, const bromoc_types *t) {
   int rc = upload1(ctx, &p.nwtype, t->nwtype, t->ntype);
   if (!rc) rc = upload1(ctx, &p.cg, t->cg, t->ntype);
   if (!rc) rc = upload1(ctx, &p.diffusion, t->diffusion, t->ntype);
+  if (!rc) {  // float-float charges of GRAND
+    std::vector<float2> c(t->ntype), qc(t->ntype);
+    for (int i = 0; i < t->ntype; ++i) {
+      c[i] = ffsplit(t->cg[i]);
+      qc[i] = ffsplit(p.celec * t->cg[i]);
+    }
+    rc = upload1(ctx, &p.cgff, c.data(), t->ntype);
+    if (!rc) rc = upload1(ctx, &p.qcff, qc.data(), t->ntype);
+  }
   if (rc) return rc;
   int *w = nullptr;
   if ((rc = dalloc(ctx, &w, t->nttyp + 1))) return rc;
@@ -749,6 +768,41 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
   float4 *dpk = const_cast<float4 *>(p.ppk);
   if (int rc2 = upload(ctx, &dpk, pk.data(), pk.size())) return rc2;
   p.ppk = dpk;
+  {  // float-float twins for GRAND
+    std::vector<PairFF> pff(ntc);
+    for (int k = 0; k < ntc; ++k) {
+      const PairParam &a = pp[k];
+      PairFF &f = pff[k];
+      f.fct = ffsplit(a.fct);
+      f.epp4 = ffsplit(a.epp4);
+      f.sgp2 = ffsplit(a.sgp2);
+      f.c0 = ffsplit(a.c0);
+      f.c1 = ffsplit(a.c1);
+      f.c2 = ffsplit(a.c2);
+      f.c3pi = ffsplit(a.c3 * kPi);
+      f.c4 = ffsplit(a.c4);
+      f.sc0 = ffsplit(a.sc0);
+      f.sc1 = ffsplit(a.sc1);
+      f.sc2 = ffsplit(a.sc2);
+      f.dm2lo = ffsplit(a.dm2lo);
+      f.dm2hi = ffsplit(a.dm2hi);
+      f.dmi = ffsplit(a.dmi);
+      f.flags = a.flags;
+      f.nxi = a.nxi;
+      f.npieces = a.npieces;
+      f.pad = 0;
+    }
+    std::vector<float2> eff(anyef ? 3 * (size_t)q->cnt : 3, make_float2(0.f, 0.f));
+    if (anyef)
+      for (size_t g = 0; g < 3 * (size_t)q->cnt; ++g) eff[g] = ffsplit(q->ep[g]);
+    PairFF *dff = const_cast<PairFF *>(p.ppff);
+    float2 *deff = const_cast<float2 *>(p.epff);
+    int rc1 = upload(ctx, &dff, pff.data(), pff.size());
+    if (!rc1) rc1 = upload(ctx, &deff, eff.data(), eff.size());
+    p.ppff = dff;
+    p.epff = deff;
+    if (rc1) return rc1;
+  }
   PairParam *dpp = const_cast<PairParam *>(p.pp);
   PairParamF *dpf = const_cast<PairParamF *>(p.ppf);
   int *dpi = const_cast<int *>(p.pidx);
@@ -888,6 +942,13 @@ int bromoc_gpu_set_phiv(bromoc_ctx *ctx, const bromoc_grid *g, const int8_t *phi
     float *d = const_cast<float *>(p.esvdw_f);
     rc = upload(ctx, &d, es.data(), es.size());
     p.esvdw_f = d;
+    if (rc) return rc;
+    std::vector<float2> ef(ctx->nttyp + 1, ffsplit(o->svdw));  // float-float, for GRAND
+    if (!o->nmcden && o->scal)
+      for (int t = 1; t <= ctx->nttyp; ++t) ef[t] = ffsplit(o->svdw * o->scal[t - 1]);
+    float2 *df = const_cast<float2 *>(p.esvff);
+    rc = upload(ctx, &df, ef.data(), ef.size());
+    p.esvff = df;
     if (rc) return rc;
   }
   ctx->phiv_nmaps = o->nmaps;
@@ -1030,6 +1091,17 @@ int bromoc_gpu_set_buffers(bromoc_ctx *ctx, const bromoc_buffers *b) {
   if (!rc) rc = upload1(ctx, &p.avnum, b->avnum, n);
   if (!rc) rc = upload1(ctx, &p.mu, b->mu, n);
   if (!rc) rc = upload1(ctx, &p.kbb, b->kb, n);
+  if (!rc) {  // float-float (avnum, mu, kb) per buffer for GRAND's acceptance, 1-based
+    std::vector<float2> v(3 * (size_t)(n + 1), make_float2(0.f, 0.f));
+    for (int i = 0; i < n; ++i) {
+      v[3 * (i + 1)] = ffsplit(b->avnum[i]);
+      v[3 * (i + 1) + 1] = ffsplit(b->mu[i]);
+      v[3 * (i + 1) + 2] = ffsplit(b->kb[i]);
+    }
+    float2 *d = const_cast<float2 *>(p.bufff);
+    rc = upload(ctx, &d, v.data(), v.size());
+    p.bufff = d;
+  }
   if (!rc) rc = upload1(ctx, &p.lzmin, b->lzmin, n);
   if (!rc) rc = upload1(ctx, &p.lzmax, b->lzmax, n);
   if (!rc) rc = upload1(ctx, &p.rmin, b->rmin, n);
@@ -1353,10 +1425,48 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
     else
       ctx->ff_fresh = false;
   }
-  CU(cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), ctx->stream));
+  // the kernel starts its energy sum at zero; without a launch, zero it here
+  if (ngcmc == 0) CU(cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), ctx->stream));
+  {  // float-float constants of the GRAND kernel's ΔE
+    FFC &f = p.ffc;
+    const Grid3 *gs[3] = {&p.g1, &p.g2, &p.g3};
+    for (int m = 0; m < 3; ++m) {
+      const Grid3 &g = *gs[m];
+      const double tr[3] = {g.tranx, g.trany, g.tranz}, bc[3] = {g.xbcen, g.ybcen, g.zbcen};
+      const int ncl[3] = {g.nclx, g.ncly, g.nclz};
+      for (int a = 0; a < 3; ++a) {
+        f.g[m].ub[a] = ffsplit(bc[a] + tr[a]);
+        f.g[m].lb[a] = ffsplit(bc[a] - tr[a]);
+        f.g[m].o[a] = ffsplit(tr[a] - bc[a]);
+        f.g[m].ncl[a] = ncl[a];
+      }
+      f.g[m].dcel = ffsplit(g.dcel);
+      f.g[m].idcel = ffsplit(g.idcel);
+    }
+    f.sqrfac = ffsplit(p.sqrfac);
+    f.thold8 = ffsplit(p.thold8);
+    f.thold27 = ffsplit(p.thold27);
+    f.vzmin = ffsplit(p.vzmin);
+    f.vzmax = ffsplit(p.vzmax);
+    f.rth = ffsplit(p.rth);
+    f.srpx = ffsplit(p.srpx);
+    f.srpk = ffsplit(p.srpk);
+    f.srpy = ffsplit(p.srpy);
+    f.ires = ffsplit(p.ires);
+    f.ikbt = ffsplit(p.ikbt);
+    const double L[3] = {p.lx, p.ly, p.lz};
+    for (int a = 0; a < 3; ++a) {
+      f.L[a] = ffsplit(L[a]);
+      f.iL[a] = L[a] > 0.0 ? (float)(1.0 / L[a]) : 0.0f;
+    }
+    f.rc2 = ffsplit(p.rc2);
+  }
   if (ngcmc > 0) {
+    KTimer *tg = next_timer(ctx, BROMOC_K_GRAND);
+    if (tg) cudaEventRecord(tg->a, ctx->stream);
     CU(launch_grand(p, ntot_ub(ctx), ctx->ipart_slots, terms, seed, cycle, ngcmc, ff ? 1 : 0,
                     ctx->stream));
+    if (tg) cudaEventRecord(tg->b, ctx->stream);
     ctx->launches += 1;
     ctx->attempts_total += ngcmc;
   }

@@ -56,8 +56,10 @@ struct DevState {
   int nremove[kMaxBuffers];
   int ntotat[kMaxBuffers];
   double dener_sum;         // accumulated GCMC energy change
-  unsigned bar_count;       // grid barrier of the GRAND kernel: arrivals,
-  unsigned bar_gen;         // and generation (zeroed count before each launch)
+  unsigned bar_count;       // grid barriers of the cooperative kernels: arrivals,
+  unsigned bar_gen;         // a generation flag and the blocks that have
+  unsigned bar_exit;        // finished; all zero between launches (the last
+                            // block out of a launch clears them)
 };
 
 // GCMC trial of one attempt (written by the proposal kernel).
@@ -164,13 +166,19 @@ __device__ inline void bd_noise3_f(uint64_t seed, uint64_t step, uint32_t slot,
 }
 
 // GCMC uniform draw `draw` of attempt `attempt` of cycle `cycle`.
-__host__ __device__ inline double gcmc_uniform(uint64_t seed, uint64_t cycle,
-                                               uint32_t attempt, uint32_t draw) {
+// The 32-bit word behind gcmc_uniform (the uniform is word * 2^-32).
+__host__ __device__ inline uint32_t gcmc_word(uint64_t seed, uint64_t cycle, uint32_t attempt,
+                                              uint32_t draw) {
   uint32_t w[4];
   philox4x32_10(attempt, draw >> 2, (uint32_t)cycle,
                 ((uint32_t)(cycle >> 32) & 0x00FFFFFFu) | (2u << 24),
                 (uint32_t)seed, (uint32_t)(seed >> 32), w);
-  return u01(w[draw & 3]);
+  return w[draw & 3];
+}
+
+__host__ __device__ inline double gcmc_uniform(uint64_t seed, uint64_t cycle,
+                                               uint32_t attempt, uint32_t draw) {
+  return u01(gcmc_word(seed, cycle, attempt, draw));
 }
 
 __host__ __device__ inline double fsign(double a, double b) {

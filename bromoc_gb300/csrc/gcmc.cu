@@ -5,6 +5,7 @@
 // stays on the device (DevState::ntot).
 #include <algorithm>
 
+#include "ffmath.cuh"
 #include "gridsync.cuh"
 #include "launch.h"
 #include "physics.cuh"
@@ -364,6 +365,464 @@ void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
 constexpr int kGrandThreads = 128;
 constexpr int kGrandWarps = kGrandThreads / 32;
 
+// ---- tables of the GRAND kernel ---------------------------------------------
+// The type and pair-law tables its serial paths read, copied into shared
+// memory when they fit (a lookup then costs an SM round trip, not an L2
+// one); otherwise the refs point at the global arrays.
+constexpr int kShTypes = kMaxTypes + 1, kShPidx = 1024, kShPairs = 48;
+struct TypeRefs {
+  const int *nwtype, *rfmap, *vmap;
+  const float2 *qc, *cg, *esv;
+};
+struct PairRefs {
+  const int *pidx, *nwtype;
+  const PairFF *ppff;
+};
+struct GrandTabs {
+  int nwtype[kShTypes], rfmap[kShTypes], vmap[kShTypes];
+  float2 qc[kShTypes], cg[kShTypes], esv[kShTypes];
+  int pidx[kShPidx];
+  PairFF ppff[kShPairs];
+};
+
+// Every thread of the block; the caller synchronises before use.
+__device__ void load_tabs(const KP &p, GrandTabs &t, TypeRefs &tr, PairRefs &pr) {
+  const bool types = p.ntype + 1 <= kShTypes && p.nttyp + 1 <= kShTypes;
+  const bool pairs = types && p.nttyp * p.nttyp <= kShPidx && p.ntc <= kShPairs;
+  if (types) {
+    for (int i = threadIdx.x; i <= p.ntype; i += blockDim.x) {
+      t.nwtype[i] = p.nwtype[i];
+      t.qc[i] = p.qcff[i];
+      t.cg[i] = p.cgff[i];
+      t.rfmap[i] = p.rfpar_map_of_type ? p.rfpar_map_of_type[i] : 0;
+      t.vmap[i] = p.phiv_map_of_type ? p.phiv_map_of_type[i] : 0;
+    }
+    for (int i = threadIdx.x; i <= p.nttyp; i += blockDim.x)
+      t.esv[i] = p.esvff ? p.esvff[i] : make_float2(0.f, 0.f);
+  }
+  if (pairs) {
+    for (int i = threadIdx.x; i < p.nttyp * p.nttyp; i += blockDim.x) t.pidx[i] = p.pidx[i];
+    const int *src = reinterpret_cast<const int *>(p.ppff);
+    int *dst = reinterpret_cast<int *>(t.ppff);
+    for (int i = threadIdx.x; i < p.ntc * (int)(sizeof(PairFF) / sizeof(int)); i += blockDim.x)
+      dst[i] = src[i];
+  }
+  tr = types ? TypeRefs{t.nwtype, t.rfmap, t.vmap, t.qc, t.cg, t.esv}
+             : TypeRefs{p.nwtype, p.rfpar_map_of_type, p.phiv_map_of_type, p.qcff, p.cgff, p.esvff};
+  pr = pairs ? PairRefs{t.pidx, tr.nwtype, t.ppff} : PairRefs{p.pidx, p.nwtype, p.ppff};
+}
+
+// rfpar_ifir through the refs
+__device__ __forceinline__ size_t rf_ifir(const KP &p, const TypeRefs &tr, int itype) {
+  return p.qrfpsin ? 0 : (size_t)tr.rfmap[itype] * ((size_t)p.g3.nclx * p.g3.ncly * p.g3.nclz);
+}
+
+// ---- ΔE terms in float-float (ffmath.cuh) -----------------------------------
+// GRAND evaluates INTERACT's O(N) terms, the trial-trial terms and their sums
+// in float-float; a pair closer than kFFMinD2 falls back to the FP64 law.
+
+constexpr float kFFMinD2 = 0.01f;  // A^2: below, LJ and SRPMF may leave float's range
+
+// Float-float exp and cos stay out of line (one copy each): GRAND's chains
+// run once per launch, and inlined copies at every call site stall its
+// warps on instruction fetch.  (Routines that read the parameter block stay
+// inline: a call would take its address and move it to local memory.)
+__device__ __noinline__ f2 exp_ff(f2 a) { return f2_exp(a); }
+__device__ __noinline__ f2 cos_ff(f2 a) { return f2_cos(a); }
+
+__device__ __forceinline__ f2 f2_ld(float2 v) { return {v.x, v.y}; }
+__device__ __forceinline__ float2 f2_st(f2 a) { return make_float2(a.h, a.l); }
+__device__ __forceinline__ bool f2_lt(f2 a, f2 b) { return a.h < b.h || (a.h == b.h && a.l < b.l); }
+__device__ __forceinline__ bool f2_le(f2 a, f2 b) { return a.h < b.h || (a.h == b.h && a.l <= b.l); }
+__device__ __forceinline__ f2 f2_pow3(f2 v) { return f2_mul(f2_sqr(v), v); }
+__device__ __forceinline__ f2 f2_pow6(f2 v) {
+  const f2 s = f2_sqr(v);
+  return f2_mul(f2_sqr(s), s);
+}
+// (int) of the value h + l, truncating toward zero as the FP64 code does
+__device__ __forceinline__ int f2_trunc(f2 a) {
+  int i = (int)a.h;
+  if ((float)i == a.h) {
+    if (a.h > 0.0f && a.l < 0.0f) --i;
+    else if (a.h < 0.0f && a.l > 0.0f) ++i;
+  }
+  return i;
+}
+// d - L rint(d / L): the nearest image (the quotient's rounding at an exact
+// half box is where the two images are equally near)
+__device__ __forceinline__ f2 min_image_ff(f2 d, float2 L, float iL) {
+  const float k = rintf(__fmul_rn(d.h, iL));
+  return f2_sub(d, f2_mulf(f2_ld(L), k));
+}
+
+// efp64 in float-float (polynom.f90:197-230)
+__device__ f2 efp_ff(const KP &p, const PairFF &q, f2 x2, int &err) {
+  if (f2_lt(x2, f2_ld(q.dm2lo))) {
+    const f2 ix2 = f2_rcp(x2);
+    return f2_add(f2_mul(f2_ld(q.sc0), f2_pow6(ix2)), f2_ld(q.sc1));
+  }
+  if (f2_lt(f2_ld(q.dm2hi), x2)) {
+    const f2 ix2 = f2_rcp(x2);
+    const f2 c = f2_mul(f2_ld(q.sc2), f2_pow3(ix2));
+    return (q.flags & kChr) ? f2_add(c, f2_mul(f2_ld(q.fct), f2_sqrt(ix2))) : c;
+  }
+  const f2 x = f2_sqrt(x2);
+  int i = f2_trunc(f2_mul(f2_sub(x, f2_ld(q.dmi)), f2_ld(p.ffc.ires))) + q.nxi;
+  if (i < q.nxi || i >= q.nxi + q.npieces) {
+    err |= kErrTableIndex;
+    i = min(max(i, q.nxi), q.nxi + q.npieces - 1);
+  }
+  const f2 p1 = f2_ld(p.epff[3 * i]), p2 = f2_ld(p.epff[3 * i + 1]),
+           p3 = f2_ld(p.epff[3 * i + 2]);
+  return f2_add(p1, f2_mul(x, f2_add(p2, f2_mul(x, p3))));
+}
+
+// law_interact64 in float-float: U of a pair at squared distance d2
+// (interact.f90's pair terms: Coulomb, LJ, SRPMF, or the tabulated law)
+__device__ f2 law_ff(const KP &p, const PairFF &q, f2 d2, int &err) {
+  if (q.flags & kEfp) return efp_ff(p, q, d2, err);
+  const f2 idist = f2_rsqrt(d2), idist2 = f2_sqr(idist);
+  f2 u = f2_f(0.0f);
+  if (q.flags & kChr) u = f2_mul(f2_ld(q.fct), idist);
+  if (q.flags & kLj) {
+    const f2 d6 = f2_pow3(f2_mul(f2_ld(q.sgp2), idist2));
+    u = f2_add(u, f2_mul(f2_mul(f2_ld(q.epp4), d6), f2_addf(d6, -1.0f)));
+  }
+  if ((q.flags & kSrp) && f2_le(d2, f2_ld(p.ffc.rth))) {
+    const f2 r = f2_mul(d2, idist);
+    const f2 t = f2_sub(f2_ld(q.c1), r);
+    f2 es = f2_mul(f2_mul(f2_ld(q.c0), exp_ff(f2_mul(t, f2_ld(q.c2)))),
+                   cos_ff(f2_mul(f2_ld(q.c3pi), t)));
+    es = f2_add(es, f2_mul(f2_ld(q.c4), f2_pow6(f2_mul(f2_ld(q.c1), idist))));
+    const f2 srpx = f2_ld(p.ffc.srpx);
+    if (!f2_lt(r, srpx))
+      es = f2_sub(f2_mul(es, exp_ff(f2_neg(f2_mul(f2_ld(p.ffc.srpk), f2_sub(r, srpx))))),
+                  f2_ld(p.ffc.srpy));
+    u = f2_add(u, es);
+  }
+  return u;
+}
+
+// What a GRAND pair term reads of a particle, in float-float: position,
+// signed type, RFPAR record (q srfe reff, reff^2).
+struct PartFF {
+  f2 x, y, z;
+  int ti;
+  float4 rf;
+};
+
+__device__ __forceinline__ PartFF load_partff(const KP &p, int i, bool rf, bool ff) {
+  PartFF r;
+  r.ti = __ldcg(p.typei + i);
+  if (ff) {
+    const float4 h = __ldcg(p.pk1 + i), l = __ldcg(p.pk2 + i);
+    r.x = {h.x, l.x};
+    r.y = {h.y, l.y};
+    r.z = {h.z, l.z};
+  } else {
+    r.x = f2_of(__ldcg(p.x + i));
+    r.y = f2_of(__ldcg(p.y + i));
+    r.z = f2_of(__ldcg(p.z + i));
+  }
+  r.rf = rf && i >= p.nsites ? __ldcg(p.gc_rff + i) : make_float4(0.f, 0.f, 0.f, 0.f);
+  return r;
+}
+
+// The FP64 term of a pair closer than float-float's range (rare)
+__device__ double near_pair64(const KP &p, const Trial &tr, uint32_t mask, int i,
+                                           int jt2, bool rf, const PartRec &q, int &err) {
+  return interact_rec(p, tr, mask, i, jt2, tr.j - 1 >= p.nsites, rf, q, err);
+}
+
+// interact_rec in float-float: particle i's ΔE term with trial t.  False
+// when the pair is closer than kFFMinD2 (the caller takes the FP64 law).
+__device__ __forceinline__ bool pair_ff(const KP &p, const PairRefs &P, const TrialFF &t,
+                                        uint32_t mask, int i, const PartFF &q, f2 &u, int &err) {
+  u = f2_f(0.0f);
+  const bool ion_i = i >= p.nsites;
+  const int ti = q.ti;
+  if (ion_i && guard_bad(p.st, abs(ti) - p.nold - 1, p.ntype - p.nold, 31)) return true;
+  f2 dx = f2_sub(q.x, f2_ld(t.x)), dy = f2_sub(q.y, f2_ld(t.y)), dz = f2_sub(q.z, f2_ld(t.z));
+  if (p.periodic) {  // extension mode: nearest image, plain cutoff
+    dx = min_image_ff(dx, p.ffc.L[0], p.ffc.iL[0]);
+    dy = min_image_ff(dy, p.ffc.L[1], p.ffc.iL[1]);
+    dz = min_image_ff(dz, p.ffc.L[2], p.ffc.iL[2]);
+  }
+  const f2 d2 = f2_add(f2_add(f2_sqr(dx), f2_sqr(dy)), f2_sqr(dz));
+  if (p.periodic && !f2_lt(d2, f2_ld(p.ffc.rc2))) return true;
+  if (d2.h < kFFMinD2) return false;
+  const bool beion = t.j - 1 >= p.nsites;
+  if (mask & 1u) {
+    int is = -1;
+    if (beion && ion_i)  // interact.f90:173-210
+      is = P.pidx[(P.nwtype[abs(ti)] - 1) * p.nttyp + t.jt2 - 1];
+    else if (beion && !ion_i)  // interact.f90:351-381
+      is = P.pidx[(p.typtyp[i] - 1) * p.nttyp + t.jt2 - 1];
+    else if (!beion && ion_i)  // interact.f90:383-413
+      is = P.pidx[(P.nwtype[abs(ti)] - 1) * p.nttyp + t.jt2 - 1];
+    if (is >= 0) u = law_ff(p, P.ppff[is], d2, err);
+  }
+  if (t.rf && ion_i && q.rf.x != 0.0f) {  // RFPAR cross term
+    const f2 c = {q.rf.x, q.rf.y}, rr = {q.rf.z, q.rf.w};
+    u = f2_add(u, f2_mul(f2_mul(f2_ld(t.a), c), f2_rsqrt(f2_add(f2_mul(f2_ld(t.b), rr), d2))));
+  }
+  return true;
+}
+
+// ---- single-particle terms in float-float ----------------------------------
+__device__ __forceinline__ f2 f2_abs(f2 a) { return a.h < 0.0f ? f2_neg(a) : a; }
+
+__device__ __forceinline__ bool in_grid_ff(const GridFF &g, f2 x, f2 y, f2 z) {
+  return f2_le(x, f2_ld(g.ub[0])) && f2_le(f2_ld(g.lb[0]), x) && f2_le(y, f2_ld(g.ub[1])) &&
+         f2_le(f2_ld(g.lb[1]), y) && f2_le(z, f2_ld(g.ub[2])) && f2_le(f2_ld(g.lb[2]), z);
+}
+
+// cell_of: the cell of grid coordinate xi (truncated), clamped below the
+// last node
+__device__ __forceinline__ int cell_ff(const GridFF &g, f2 xi, int a) {
+  const int i = f2_trunc(f2_mul(xi, f2_ld(g.idcel)));
+  return i == g.ncl[a] - 1 ? g.ncl[a] - 2 : i;
+}
+
+// spln_cell: the nearest node (half away from zero), clamped to the interior
+__device__ __forceinline__ int spln_node_ff(const GridFF &g, f2 xi, int a) {
+  const f2 u = f2_mul(xi, f2_ld(g.idcel));
+  int n = (int)floorf(u.h);
+  f2 r = f2_addf(u, -(float)n);  // u - n, exact
+  if (r.h < 0.0f) {
+    --n;
+    r = f2_addf(r, 1.0f);
+  }
+  const f2 half = f2_f(0.5f);
+  if (f2_lt(half, r) || (r.h == 0.5f && r.l == 0.0f && n >= 0)) ++n;
+  if (n == 0) n = 1;
+  if (n == g.ncl[a] - 1) n = g.ncl[a] - 2;
+  return n;
+}
+
+// 1 - |xi - node dcel| / dcel: the trilinear weight of a node along one axis
+__device__ __forceinline__ f2 tri_w(const GridFF &g, f2 xi, int node) {
+  const f2 d = f2_abs(f2_sub(xi, f2_mulf(f2_ld(g.dcel), (float)node)));
+  return f2_sub(f2_f(1.0f), f2_mul(d, f2_ld(g.idcel)));
+}
+
+// quadratic B-spline m3 (m3.f90)
+__device__ __forceinline__ f2 m3_ff(f2 x) {
+  const f2 zero = f2_f(0.0f);
+  const bool in02 = f2_le(zero, x) && f2_le(x, f2_f(2.0f));
+  const bool in13 = f2_le(f2_f(1.0f), x) && f2_le(x, f2_f(3.0f));
+  const f2 m2m = in02 ? f2_sub(f2_f(1.0f), f2_abs(f2_addf(x, -1.0f))) : zero;
+  const f2 m2 = in13 ? f2_sub(f2_f(1.0f), f2_abs(f2_addf(x, -2.0f))) : zero;
+  if (!(f2_le(zero, x) && f2_le(x, f2_f(3.0f)))) return zero;
+  return f2_add(f2_mul(f2_mulf(x, 0.5f), m2m), f2_mul(f2_mulf(f2_sub(f2_f(3.0f), x), 0.5f), m2));
+}
+
+__device__ __forceinline__ f2 shfl_xor_ff(f2 v, int o) {
+  return {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)};
+}
+__device__ __forceinline__ f2 seg8_ff(f2 v) {
+  v = f2_add(v, shfl_xor_ff(v, 4));
+  v = f2_add(v, shfl_xor_ff(v, 2));
+  return f2_add(v, shfl_xor_ff(v, 1));
+}
+__device__ __forceinline__ f2 wsum_ff(f2 v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = f2_add(v, shfl_xor_ff(v, o));
+  return v;
+}
+
+// rfpar_gather (rfpar.f90:94-150, no gradients, the same early exit) in
+// float-float: (srfe, reff) of an ion of the map ifir at (x, y, z); (0, 0)
+// off the map, as rf_single.
+__device__ void rf_gather_ff(const KP &p, f2 x, f2 y, f2 z, size_t ifir, f2 &srfe, f2 &reff) {
+  const GridFF &g = p.ffc.g[2];
+  srfe = reff = f2_f(0.0f);
+  if (!in_grid_ff(g, x, y, z)) return;
+  const f2 xi = f2_add(x, f2_ld(g.o[0])), yi = f2_add(y, f2_ld(g.o[1])),
+           zi = f2_add(z, f2_ld(g.o[2]));
+  const int ix = cell_ff(g, xi, 0), iy = cell_ff(g, yi, 1), iz = cell_ff(g, zi, 2);
+  const size_t ncyz = (size_t)g.ncl[1] * g.ncl[2];
+  const f2 sq = f2_ld(p.ffc.sqrfac);
+  float gs[8], gr[8];  // the eight nodes' values, loaded together
+#pragma unroll
+  for (int n = 0; n < 8; ++n) {
+    const size_t node = ifir + (size_t)(ix + (n >> 2)) * ncyz +
+                        (size_t)(iy + ((n >> 1) & 1)) * g.ncl[2] + iz + (n & 1);
+    gs[n] = __ldg(p.gsrfen + node);
+    gr[n] = __ldg(p.greff + node);
+  }
+#pragma unroll
+  for (int a = 0; a < 2; ++a) {
+    const f2 ai = tri_w(g, xi, ix + a);
+#pragma unroll
+    for (int b = 0; b < 2; ++b) {
+      const f2 ab = f2_mul(ai, tri_w(g, yi, iy + b));
+#pragma unroll
+      for (int c = 0; c < 2; ++c) {
+        const int n = 4 * a + 2 * b + c;
+        if (gs[n] == 0.0f) break;  // the reference's exit of the innermost loop
+        const f2 fi = f2_mul(ab, tri_w(g, zi, iz + c));
+        srfe = f2_add(srfe, f2_mulf(fi, gs[n]));
+        reff = f2_add(reff, f2_mul(fi, f2_mulf(sq, gr[n])));
+      }
+    }
+  }
+}
+
+// RFPAR record (q srfe reff, reff^2) of an ion of type |ti|
+__device__ __forceinline__ float4 rf_record_ff(const TypeRefs &tr, f2 srfe, f2 reff, int ti) {
+  const f2 c = f2_mul(f2_mul(f2_ld(tr.cg[abs(ti)]), srfe), reff), d = f2_sqr(reff);
+  return make_float4(c.h, c.l, d.h, d.l);
+}
+
+// trial_single_warp in float-float for an ion trial at (x, y, z) (one full
+// warp, the same lane layout: lanes 8g + corner the trilinear nodes of the
+// static field, the repulsion map, gsrfen and greff; lanes 0..26 the
+// B-spline nodes); the membrane term stays FP64 (lane 0).  Lane 0 fills
+// tr.e_single, srfe, reff, rf_in and returns srfe, reff in float-float.
+__device__ void trial_single_ff(const KP &p, const TypeRefs &T, Trial &tr, f2 x, f2 y, f2 z,
+                                uint32_t mask, int qalert, int *nalert, f2 &srfe_o, f2 &reff_o,
+                                f2 &e_o) {
+  const int lane = threadIdx.x & 31;
+  const FFC &c = p.ffc;
+  const int j0 = tr.j - 1, it = tr.itype;
+  const int jt2 = T.nwtype[it];
+  const int g = lane >> 3, cn = lane & 7;
+  const int ca = (cn >> 2) & 1, cb = (cn >> 1) & 1, cc = cn & 1;
+  const bool do_phix = (mask & 4u) && p.qphix && in_grid_ff(c.g[0], x, y, z);
+  const GridFF &g2 = c.g[1];
+  const bool do_phiv = (mask & 8u) && p.qphiv && f2_le(x, f2_ld(g2.ub[0])) &&
+                       f2_le(f2_ld(g2.lb[0]), x) && f2_le(y, f2_ld(g2.ub[1])) &&
+                       f2_le(f2_ld(g2.lb[1]), y) && f2_le(z, f2_ld(c.vzmax)) &&
+                       f2_le(f2_ld(c.vzmin), z);
+  const bool do_rf = (mask & 16u) && p.qrfpar && in_grid_ff(c.g[2], x, y, z);
+  // repulsion map and scale (phiv_select for an ion slot)
+  size_t vifir = 0;
+  if (p.qnmcden && j0 >= p.nsites + p.nfix)
+    vifir = (size_t)T.vmap[it] * ((size_t)p.g2.nclx * p.g2.ncly * p.g2.nclz);
+  const f2 esv = do_phiv ? f2_ld(T.esv[jt2]) : f2_f(0.0f);
+  const f2 qc = f2_ld(T.qc[it]);
+  const size_t rfifir = do_rf ? rf_ifir(p, T, it) : 0;
+  f2 v = f2_f(0.0f), w = f2_f(0.0f);
+  float psum = 0.0f, gs_own = 0.0f;
+  bool active = false;
+  if ((g == 0 && do_phix) || (g == 1 && do_phiv && p.qtrln) || (g >= 2 && do_rf)) {
+    const GridFF &gg = c.g[g == 0 ? 0 : (g == 1 ? 1 : 2)];
+    const f2 xi = f2_add(x, f2_ld(gg.o[0])), yi = f2_add(y, f2_ld(gg.o[1])),
+             zi = f2_add(z, f2_ld(gg.o[2]));
+    const int ix = cell_ff(gg, xi, 0), iy = cell_ff(gg, yi, 1), iz = cell_ff(gg, zi, 2);
+    w = f2_mul(f2_mul(tri_w(gg, xi, ix + ca), tri_w(gg, yi, iy + cb)), tri_w(gg, zi, iz + cc));
+    const size_t node = (size_t)(ix + ca) * gg.ncl[1] * gg.ncl[2] +
+                        (size_t)(iy + cb) * gg.ncl[2] + iz + cc;
+    if (g == 0) {
+      v = f2_mulf(qc, __ldg(p.phix + node));
+    } else if (g == 1) {
+      psum = (float)__ldg(p.phiv + vifir + node);
+      v = f2_mulf(esv, psum);
+    } else {
+      const size_t n3 = rfifir + node;
+      gs_own = __ldg(p.gsrfen + n3);
+      v = g == 2 ? f2_f(gs_own) : f2_mulf(f2_ld(c.sqrfac), __ldg(p.greff + n3));
+    }
+    active = true;
+  }
+  const float gs_c0 = __shfl_sync(0xffffffffu, gs_own, lane & ~1);
+  if (g >= 2 && active && !(gs_c0 != 0.0f && (cc == 0 || gs_own != 0.0f))) active = false;
+  f2 le = active ? f2_mul(w, v) : f2_f(0.0f);
+  le = seg8_ff(le);
+  psum += __shfl_xor_sync(0xffffffffu, psum, 4);  // at most 8 small integers: exact
+  psum += __shfl_xor_sync(0xffffffffu, psum, 2);
+  psum += __shfl_xor_sync(0xffffffffu, psum, 1);
+  f2 be = f2_f(0.0f);
+  float bsum = 0.0f;
+  if (do_phiv && !p.qtrln) {  // warp-uniform
+    f2 e1 = f2_f(0.0f);
+    float s1 = 0.0f;
+    if (lane < 27) {
+      const f2 xi = f2_add(x, f2_ld(g2.o[0])), yi = f2_add(y, f2_ld(g2.o[1])),
+               zi = f2_add(z, f2_ld(g2.o[2]));
+      const int ix = spln_node_ff(g2, xi, 0), iy = spln_node_ff(g2, yi, 1),
+                iz = spln_node_ff(g2, zi, 2);
+      const int k = ix - 1 + lane / 9, l = iy - 1 + (lane / 3) % 3, m = iz - 1 + lane % 3;
+      const f2 dc = f2_ld(g2.dcel), id = f2_ld(g2.idcel);
+      auto arg = [&](f2 q, int n) {
+        return f2_sub(f2_f(1.5f), f2_mul(f2_sub(q, f2_mulf(dc, (float)n)), id));
+      };
+      const f2 fi = f2_mul(f2_mul(m3_ff(arg(xi, k)), m3_ff(arg(yi, l))), m3_ff(arg(zi, m)));
+      if (fi.h != 0.0f) {
+        const float phis = (float)__ldg(p.phiv + vifir + (size_t)k * g2.ncl[1] * g2.ncl[2] +
+                                        (size_t)l * g2.ncl[2] + m);
+        s1 = phis;
+        e1 = f2_mulf(f2_mul(fi, esv), phis);
+      }
+    }
+    be = wsum_ff(e1);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) s1 += __shfl_xor_sync(0xffffffffu, s1, o);  // exact
+    bsum = s1;
+  }
+  const f2 e_v = {__shfl_sync(0xffffffffu, le.h, 8), __shfl_sync(0xffffffffu, le.l, 8)};
+  const float s_v = __shfl_sync(0xffffffffu, psum, 8);
+  const f2 sj = {__shfl_sync(0xffffffffu, le.h, 16), __shfl_sync(0xffffffffu, le.l, 16)};
+  const f2 rj = {__shfl_sync(0xffffffffu, le.h, 24), __shfl_sync(0xffffffffu, le.l, 24)};
+  if (lane == 0) {
+    f2 e = f2_f(0.0f);
+    if ((mask & 2u) && p.qmemb) {  // FP64
+      double em = 0.0, f[3];
+      if (membrane_one(p, jt2, p.cg[it], tr.x, tr.y, tr.z, false, true, em, f) && qalert) {
+        if (nalert)
+          ++*nalert;
+        else
+          atomicAdd(&p.warn[jt2], 1);
+      }
+      e = f2_of(em);
+    }
+    if (do_rf)
+      e = f2_add(e, f2_mulf(f2_mul(f2_mul(qc, f2_ld(T.cg[it])), f2_sqr(sj)), 0.5f));
+    if (do_phix) e = f2_add(e, le);
+    if (do_phiv) {
+      f2 ev = p.qtrln ? e_v : be;
+      const float ps = p.qtrln ? s_v : bsum;
+      if (f2_le(f2_ld(p.qtrln ? c.thold8 : c.thold27), f2_f(ps))) {
+        ev = f2_f(1.0e10f);  // exact in float
+        if (qalert) {
+          if (nalert)
+            ++*nalert;
+          else
+            atomicAdd(&p.warn[jt2], 1);
+        }
+      }
+      e = f2_add(e, ev);
+    }
+    tr.e_single = f2_dbl(e);
+    e_o = e;
+    srfe_o = do_rf ? sj : f2_f(0.0f);
+    reff_o = do_rf ? rj : f2_f(0.0f);
+    tr.srfe = f2_dbl(srfe_o);
+    tr.reff = f2_dbl(reff_o);
+    tr.rf_in = do_rf ? 1 : 0;
+  }
+}
+
+// A trial as the pair terms read it (block 0, once per trial), from its
+// float-float position and RFPAR gathers.
+__device__ TrialFF trial_ff(const KP &p, const TypeRefs &T, const Trial &t, uint32_t mask, f2 x,
+                            f2 y, f2 z, f2 srfe, f2 reff) {
+  TrialFF f{};
+  f.valid = t.valid;
+  f.j = t.j;
+  f.jt2 = trial_type2(p, t);
+  f.rf = t.valid && t.rf_in && (mask & 16u);
+  f.x = f2_st(x);
+  f.y = f2_st(y);
+  f.z = f2_st(z);
+  if (f.rf) {
+    f.a = f2_st(f2_mul(f2_mul(f2_ld(T.qc[t.itype]), srfe), reff));
+    f.b = f2_st(f2_sqr(reff));
+  }
+  return f;
+}
+
 // Lanes per particle in the pair phase: the attempts of a round rounded up
 // to a power of two (lane = particle * lanes + attempt).
 __host__ __device__ inline int grand_lanes(int ngcmc) {
@@ -380,17 +839,29 @@ struct GrandState {
   int ip0[kSpec];           // deletion: the rank its target was found at, 0 none
   int need[kSpec], found[kSpec];
   int nalert[kSpec];        // deletion: warnings of its single-particle terms
-  // each trial's particle as an ion record holds it: position (float-float
-  // rounded in FP32 mode), signed type, RFPAR (srfe, reff) at that position
-  double px[kSpec], py[kSpec], pz[kSpec];
-  double2 rf[kSpec];
+  f2 fx[kSpec], fy[kSpec], fz[kSpec];  // the trials' positions in float-float
+  f2 fsr[kSpec], fre[kSpec];            // and their RFPAR gathers (srfe, reff)
+  TrialFF tf[kSpec];        // the trials as the pair terms read them
+  // each trial's particle as an ion record holds it: position (that of the
+  // float-float record in FP32 mode), signed type, RFPAR record, and the
+  // RFPAR gathers behind it
+  PartFF pff[kSpec];
+  f2 psr[kSpec], pre_[kSpec];
   int ti[kSpec];
-  double tt[kSpec][kSpec];  // tt[k][a], k < a: trial a's pair term with k's particle
+  f2 es[kSpec];             // the trials' single-particle terms
+  f2 tt[kSpec][kSpec];      // tt[k][a], k < a: trial a's pair term with k's particle
   int terr[kSpec][kSpec];
-  double base[kSpec];       // the round's sums, totalled over the blocks
+  f2 base[kSpec];           // the round's sums, totalled over the blocks
   int aerr[kSpec];
-  double de0[kSpec];        // ΔE and acceptance with no acceptance earlier
-  int acc0[kSpec];          // in the round
+  f2 uacc[kSpec];           // the acceptance draws (exact in float-float)
+  int dti[kSpec];           // a deletion target's signed type
+  // settling in waves: per attempt its outcome in the current state, its ΔE
+  // and error flags; the moves accepted so far in the round
+  int wst[kSpec], werr[kSpec];
+  f2 wde[kSpec];
+  int cur, stop, nacc, acck[kSpec], accs[kSpec];
+  unsigned long long touched;  // bit b: an accepted deletion touched buffer b + 1
+  f2 avf[kMaxBuffers + 1], muf[kMaxBuffers + 1], kbbf[kMaxBuffers + 1];
   int pbuf[kSpec], pdel[kSpec];  // buffer (0-based) whose count the attempt changed, by
   int nat0[kMaxBuffers];    // the buffer counts at the start of the round
   int scan[kGrandWarps][kSpec];
@@ -522,8 +993,8 @@ __device__ void find_ranks(const KP &p, GrandState &g, int na) {
 // proposed in the current state, with their single-particle terms
 // (deletion trials count their warnings in nalert, insertion trials raise
 // none: grand.f90:48,86) and acceptance draws.
-__device__ void build_round(const KP &p, uint32_t mask, uint64_t seed, uint64_t cycle, int a0,
-                            int na, GrandState &g) {
+__device__ void build_round(const KP &p, const TypeRefs &T, uint32_t mask, uint64_t seed,
+                            uint64_t cycle, int a0, int na, GrandState &g) {
   const int t = threadIdx.x;
   if (t < na) {
     Trial tr;
@@ -552,6 +1023,12 @@ __device__ void build_round(const KP &p, uint32_t mask, uint64_t seed, uint64_t 
     g.tr[t] = tr;
     g.u_rank[t] = u;
     g.u_acc[t] = gcmc_uniform(seed, cycle, (uint32_t)(a0 + t), (uint32_t)tr.draw);
+    {  // the same draw in float-float: word * 2^-32 split at bit 8, exact
+      const uint32_t w = gcmc_word(seed, cycle, (uint32_t)(a0 + t), (uint32_t)tr.draw);
+      float h, l;
+      two_sum((float)(w & 0xFFFFFF00u) * 0x1p-32f, (float)(w & 0xFFu) * 0x1p-32f, h, l);
+      g.uacc[t] = {h, l};
+    }
   }
   __syncthreads();
   find_ranks(p, g, na);
@@ -570,19 +1047,43 @@ __device__ void build_round(const KP &p, uint32_t mask, uint64_t seed, uint64_t 
       tr.z = q.z;
     }
   }
+  if (t < na) {  // positions in float-float: a deletion's from its records
+    const Trial &tr = g.tr[t];
+    g.dti[t] = tr.valid && !tr.insert ? __ldcg(p.typei + tr.j - 1) : 0;
+    if (tr.valid && !tr.insert && g.ff) {
+      const int k = tr.j - 1;
+      const float4 h = __ldcg(p.pk1 + k), l = __ldcg(p.pk2 + k);
+      g.fx[t] = {h.x, l.x};
+      g.fy[t] = {h.y, l.y};
+      g.fz[t] = {h.z, l.z};
+    } else {
+      g.fx[t] = f2_of(tr.x);
+      g.fy[t] = f2_of(tr.y);
+      g.fz[t] = f2_of(tr.z);
+    }
+    g.fsr[t] = g.fre[t] = f2_f(0.0f);
+  }
   __syncthreads();
   for (int k = t >> 5; k < na; k += kGrandWarps) {
     Trial tr = g.tr[k];
     if (tr.valid) {
-      trial_single_warp(p, tr, mask, tr.insert ? 0 : 1, &g.nalert[k]);
+      f2 sr, re, es;
+      trial_single_ff(p, T, tr, g.fx[k], g.fy[k], g.fz[k], mask, tr.insert ? 0 : 1, &g.nalert[k],
+                      sr, re, es);
       if ((t & 31) == 0) {
+        g.es[k] = es;
         g.tr[k].e_single = tr.e_single;
         g.tr[k].srfe = tr.srfe;
         g.tr[k].reff = tr.reff;
         g.tr[k].rf_in = tr.rf_in;
+        g.fsr[k] = sr;
+        g.fre[k] = re;
       }
     }
   }
+  __syncthreads();
+  if (t < na)
+    g.tf[t] = trial_ff(p, T, g.tr[t], mask, g.fx[t], g.fy[t], g.fz[t], g.fsr[t], g.fre[t]);
   __syncthreads();
 }
 
@@ -594,59 +1095,54 @@ __device__ __forceinline__ double ff_rounded(double x) {
 }
 
 // Each trial's particle as an ion record holds it (block 0, a thread per
-// trial): an insertion's what its acceptance writes (the point, rounded to
-// the float-float record in FP32 mode; the signed type; RFPAR at the
-// record's point), a deletion's its target's record.
-__device__ void trial_ions(const KP &p, uint32_t mask, int na, GrandState &g) {
+// trial): an insertion's what its acceptance writes (the point as its
+// record holds it, the signed type, the RFPAR record at that point), a
+// deletion's its target's record.  The RFPAR gathers at that point are the
+// trial's own (trial_single_ff, the same map nodes and early exit).
+__device__ void trial_ions(const KP &p, const TypeRefs &T, uint32_t mask, int na,
+                           GrandState &g) {
   const int t = threadIdx.x;
   const bool rf_on = (mask & 16u) && p.qrfpar;
   if (t < na) {
     const Trial &tr = g.tr[t];
-    double x = tr.x, y = tr.y, z = tr.z;
-    int ti = 0;
-    double2 rf = make_double2(0.0, 0.0);
-    if (tr.valid) {
-      if (tr.insert) {
-        if (g.ff) {
-          x = ff_rounded(x);
-          y = ff_rounded(y);
-          z = ff_rounded(z);
-        }
-        ti = tr.z < p.cz ? -tr.itype : tr.itype;
-      } else {
-        ti = p.typei[tr.j - 1];
-      }
-      if (rf_on) rf = rf_single(p, x, y, z, abs(ti));
-    }
-    g.px[t] = x;
-    g.py[t] = y;
-    g.pz[t] = z;
+    const int ti = !tr.valid ? 0 : (tr.insert ? (tr.z < p.cz ? -tr.itype : tr.itype) : g.dti[t]);
     g.ti[t] = ti;
-    g.rf[t] = rf;
+    g.psr[t] = g.fsr[t];
+    g.pre_[t] = g.fre[t];
+    PartFF &q = g.pff[t];
+    q.x = g.fx[t];
+    q.y = g.fy[t];
+    q.z = g.fz[t];
+    q.ti = ti;
+    q.rf = tr.valid && rf_on ? rf_record_ff(T, g.fsr[t], g.fre[t], ti)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
   }
 }
 
 // Trial-trial pair terms (block 0, a thread per pair k < a): trial a's
 // INTERACT term with trial k's particle as an ion record holds it.
-__device__ void trial_pairs(const KP &p, uint32_t mask, int na, GrandState &g) {
+__device__ void trial_pairs(const KP &p, const PairRefs &P, uint32_t mask, int na,
+                            GrandState &g) {
   for (int idx = threadIdx.x; idx < na * na; idx += blockDim.x) {
     const int k = idx / na, a = idx - k * na;
     if (k >= a) continue;
     const Trial &ta = g.tr[a], &tk = g.tr[k];
-    double v = 0.0;
+    f2 v = f2_f(0.0f);
     int err = 0;
     // two deletions of one ion are never both settled (the first touches
     // the buffer of the second)
     if (ta.valid && tk.valid && (ta.insert || tk.insert || ta.j != tk.j)) {
-      const int jt2 = trial_type2(p, ta);
-      if (jt2 > 0) {
-        PartRec q;
-        q.x = g.px[k];
-        q.y = g.py[k];
-        q.z = g.pz[k];
-        q.rf = g.rf[k];
-        q.ti = g.ti[k];
-        v = interact_rec(p, ta, mask, p.nsites, jt2, true, ta.rf_in && (mask & 16u), q, err);
+      const TrialFF &fa = g.tf[a];
+      if (fa.jt2 > 0) {
+        if (!pair_ff(p, P, fa, mask, p.nsites, g.pff[k], v, err)) {  // closer than float-float's range: the FP64 law
+          PartRec q;
+          q.x = f2_dbl(g.pff[k].x);
+          q.y = f2_dbl(g.pff[k].y);
+          q.z = f2_dbl(g.pff[k].z);
+          q.rf = make_double2(f2_dbl(g.psr[k]), f2_dbl(g.pre_[k]));
+          q.ti = g.ti[k];
+          v = f2_of(near_pair64(p, ta, mask, p.nsites, fa.jt2, fa.rf != 0, q, err));
+        }
       }
     }
     g.tt[k][a] = v;
@@ -658,14 +1154,17 @@ __device__ void trial_pairs(const KP &p, uint32_t mask, int na, GrandState &g) {
 // w + kGrandWarps, ...; a fixed summation order.
 __device__ void round_sums(const KP &p, int na, GrandState &g) {
   const int lane = threadIdx.x & 31, nblk = gridDim.x;
+  const float2 *ipf = reinterpret_cast<const float2 *>(p.ipart);
   for (int a = threadIdx.x >> 5; a < na; a += kGrandWarps) {
-    double v = 0.0;
+    f2 v = f2_f(0.0f);
     int e = 0;
     for (int b = 1 + lane; b < nblk; b += 32) {
-      v += __ldcg(p.ipart + (size_t)b * kSpec + a);
+      v = f2_add(v, f2_ld(__ldcg(ipf + (size_t)b * kSpec + a)));
       e |= __ldcg(p.ierr + (size_t)b * kSpec + a);
     }
-    v = wsum(v);
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1)
+      v = f2_add(v, {__shfl_xor_sync(0xffffffffu, v.h, o), __shfl_xor_sync(0xffffffffu, v.l, o)});
     e = __reduce_or_sync(0xffffffffu, e);
     if (lane == 0) {
       g.base[a] = v;
@@ -700,133 +1199,179 @@ __device__ double accept_rate(const KP &p, const GrandState &g, const Trial &tr,
   return 1.0 / (1.0 + rate);
 }
 
-// ΔE and acceptance of every attempt as if no attempt before it in the
-// round were accepted (block 0, a thread per attempt): exact up to the
-// round's first acceptance.
-__device__ void first_acceptances(const KP &p, uint64_t cycle, int na, GrandState &g) {
-  const int a = threadIdx.x;
-  if (a >= na) return;
-  const Trial &tr = g.tr[a];
-  g.de0[a] = 0.0;
-  g.acc0[a] = 0;
-  if (tr.valid && tr.ib >= 1 && tr.ib <= g.nbuf) {
-    const double de = tr.e_single + g.base[a];
-    g.de0[a] = de;
-    g.acc0[a] = g.u_acc[a] <= accept_rate(p, g, tr, de, cycle);
+// accept_rate's decision in float-float: 1 accept, 0 reject, -1 when the
+// Boltzmann factor's exponent leaves float's range (decide in FP64).  The
+// draw u is exact; the rate agrees with the FP64 one to ~2^-46, so the two
+// decisions differ only for draws that close to the rate.
+__device__ int accept_ff(const KP &p, const GrandState &g, const Trial &tr, f2 de, f2 u,
+                         uint64_t cycle) {
+  const int ib = tr.ib, b = ib - 1;
+  const int nat = g.nat[b];
+  const f2 x = f2_neg(f2_mul(f2_sub(de, g.muf[ib]), f2_ld(p.ffc.ikbt)));
+  if (!(fabsf(x.h) <= 80.0f)) return -1;  // also NaN
+  const f2 boltz = exp_ff(x);
+  f2 a = g.avf[ib];
+  if (g.qbias[ib])
+    a = f2_add(a, f2_mul(g.kbbf[ib], f2_addf(a, -(float)(g.ntotat[b] / (long long)cycle))));
+  f2 rate;
+  if (tr.insert) {
+    rate = f2_div(f2_mul(a, boltz), f2_f((float)(nat + 1)));
+    rate = f2_div(rate, f2_addf(rate, 1.0f));
+  } else {
+    rate = f2_div(f2_mul(a, boltz), f2_f((float)nat));
+    rate = f2_rcp(f2_addf(rate, 1.0f));
   }
+  return f2_le(u, rate) ? 1 : 0;
 }
 
-// The round's attempts in order (block 0, thread 0): ΔE, acceptance and the
-// insertion or deletion (grand.f90:48-116), until an attempt whose trial no
-// longer holds.  g.done: the attempts settled; g.chg: the slots rewritten.
-__device__ void settle(const KP &p, uint32_t mask, uint64_t cycle, int na, GrandState &g) {
-  const bool rf_on = (mask & 16u) && p.qrfpar;
-  bool changed = false;
-  unsigned long long touched = 0;  // bit b: an accepted deletion touched buffer b + 1
-  int nacc = 0, acc_k[kSpec];
-  double acc_s[kSpec];
-  int done = 0;
-  g.nchg = 0;
-  for (int a = 0; a < na; ++a) {
-    Trial tr = g.tr[a];
-    if (changed && !tr.insert) {  // the deletion trial in the current state
-      const int ib = tr.ib;
-      const int natb = ib <= g.nbuf ? g.nat[ib - 1] : 0;
-      const int ip = (int)((double)natb * g.u_rank[a]) + 1;
-      if (!(ib <= g.nbuf && ip <= natb))
-        tr.valid = 0;  // no ion left to delete: the attempt does nothing
-      else if (g.ip0[a] == 0 || ip != g.ip0[a] || ((touched >> (ib - 1)) & 1ull))
-        break;  // another target: propose it again in the next round
-    }
-    g.pbuf[a] = -1;
-    g.pdel[a] = 0;
-    int err = 0;
-    if (tr.valid && !guard_bad(p.st, tr.ib - 1, p.nbuffer, 21)) {
-      const int ib = tr.ib, b = ib - 1;
-      double de;
-      bool yes;
-      err = g.aerr[a];
-      if (!changed) {
-        de = g.de0[a];
-        yes = g.acc0[a] != 0;
-      } else {
-        double c = 0.0;
-        for (int m = 0; m < nacc; ++m) {
-          c += acc_s[m] * g.tt[acc_k[m]][a];
-          err |= g.terr[acc_k[m]][a];
-        }
-        de = tr.e_single + g.base[a] + c;
-        yes = g.u_acc[a] <= accept_rate(p, g, tr, de, cycle);
-      }
-      if (!tr.insert && g.nalert[a] > 0) atomicAdd(&p.warn[p.nwtype[tr.itype]], g.nalert[a]);
-      if (yes) {
-        const int ntot = g.ntot, nat = g.nat[b];
-        if (tr.insert) {
-          if (ntot + 1 > p.cap) {
-            atomicOr(&p.st->err, kErrCapacity);
-          } else if (!guard_bad(p.st, ntot, p.cap, 22)) {
-            g.dener_sum += de;
-            g.nat[b] = nat + 1;
-            if (g.ff) {  // the records as k_pack forms them (a mobile ion)
-              const float xh = (float)tr.x, yh = (float)tr.y, zh = (float)tr.z;
-              const int code = (p.nwtype[tr.itype] - 1) | (1 << 16);
-              p.pk1[ntot] = make_float4(xh, yh, zh, __int_as_float(code));
-              p.pk2[ntot] = make_float4((float)(tr.x - (double)xh), (float)(tr.y - (double)yh),
-                                        (float)(tr.z - (double)zh), 0.0f);
-              p.pk3[ntot] =
-                  make_float4(0.0f, (float)p.cg[tr.itype], __int_as_float(1 << 1), 0.0f);
-            } else {
-              p.x[ntot] = tr.x;
-              p.y[ntot] = tr.y;
-              p.z[ntot] = tr.z;
-            }
-            p.typei[ntot] = g.ti[a];
-            p.ibuffer[ntot] = ib;
-            if (rf_on) p.gc_rf[ntot] = g.rf[a];
-            g.ntot = ntot + 1;
-            g.ninsert[b] += 1;
-            g.chg[g.nchg++] = ntot;
-            g.pbuf[a] = b;
-            g.pdel[a] = 1;
-            acc_k[nacc] = a;
-            acc_s[nacc++] = 1.0;
-            changed = true;
-          }
-        } else if (!guard_bad(p.st, tr.j - 1, ntot, 23) &&
-                   !guard_bad(p.st, ntot - 1, p.cap, 24)) {
-          const int iat = tr.j - 1, last = ntot - 1;
-          const int bz = p.ibuffer[last];  // the ion the freed slot receives
-          g.dener_sum -= de;
-          g.nremove[b] += 1;
-          if (g.ff) {
-            p.pk1[iat] = __ldcg(p.pk1 + last);
-            p.pk2[iat] = __ldcg(p.pk2 + last);
-            p.pk3[iat] = __ldcg(p.pk3 + last);
-          } else {
-            p.x[iat] = p.x[last];
-            p.y[iat] = p.y[last];
-            p.z[iat] = p.z[last];
-          }
-          p.typei[iat] = p.typei[last];
-          p.ibuffer[iat] = bz;
-          if (rf_on) p.gc_rf[iat] = __ldcg(p.gc_rf + last);
-          g.nat[b] = nat - 1;
-          g.ntot = ntot - 1;
-          g.chg[g.nchg++] = iat;
-          g.pbuf[a] = b;
-          g.pdel[a] = -1;
-          touched |= 1ull << b;
-          if (bz >= 1 && bz <= kMaxBuffers) touched |= 1ull << (bz - 1);
-          acc_k[nacc] = a;
-          acc_s[nacc++] = -1.0;
-          changed = true;
-        }
-      }
-    }
-    if (err) atomicOr(&p.st->err, err);
-    done = a + 1;
+__device__ __forceinline__ bool accepts(const KP &p, const GrandState &g, const Trial &tr, f2 de,
+                                        int a, uint64_t cycle) {
+  const int r = accept_ff(p, g, tr, de, g.uacc[a], cycle);
+  return r >= 0 ? r != 0 : g.u_acc[a] <= accept_rate(p, g, tr, f2_dbl(de), cycle);
+}
+
+// Outcomes of an attempt in the current state.
+enum : int { kNoop = 0, kReject = 1, kAccept = 2, kStop = 3 };
+
+// One attempt in the current state (block 0, the attempt's thread): kStop
+// when its deletion trial may no longer name its target (a new round
+// proposes it), kNoop when there is nothing to do, else its acceptance,
+// with ΔE -- the round's sum plus the trial-trial terms of the moves
+// accepted so far -- and the error flags of the terms it used.
+__device__ int evaluate(const KP &p, uint64_t cycle, int a, GrandState &g, f2 &de, int &err) {
+  const Trial &tr = g.tr[a];
+  de = f2_f(0.0f);
+  err = 0;
+  bool valid = tr.valid;
+  if (g.nacc > 0 && !tr.insert) {  // the deletion trial in the current state
+    const int ib = tr.ib;
+    const int natb = ib <= g.nbuf ? g.nat[ib - 1] : 0;
+    const int ip = (int)((double)natb * g.u_rank[a]) + 1;
+    if (!(ib <= g.nbuf && ip <= natb))
+      valid = false;  // no ion left to delete
+    else if (g.ip0[a] == 0 || ip != g.ip0[a] || ((g.touched >> (ib - 1)) & 1ull))
+      return kStop;
   }
-  g.done = done;
+  if (!valid || guard_bad(p.st, tr.ib - 1, p.nbuffer, 21)) return kNoop;
+  err = g.aerr[a];
+  de = f2_add(g.es[a], g.base[a]);
+  for (int m = 0; m < g.nacc; ++m) {
+    const f2 t = g.tt[g.acck[m]][a];
+    de = f2_add(de, g.accs[m] > 0 ? t : f2_neg(t));
+    err |= g.terr[g.acck[m]][a];
+  }
+  return accepts(p, g, tr, de, a, cycle) ? kAccept : kReject;
+}
+
+// The insertion or deletion of accepted attempt a (grand.f90:63-110; block
+// 0, thread 0).  False when nothing changed (capacity or a guard).
+__device__ bool apply_move(const KP &p, bool rf_on, int a, GrandState &g) {
+  const Trial &tr = g.tr[a];
+  const f2 de = g.wde[a];
+  const int ib = tr.ib, b = ib - 1;
+  const int ntot = g.ntot, nat = g.nat[b];
+  if (tr.insert) {
+    if (ntot + 1 > p.cap) {
+      atomicOr(&p.st->err, kErrCapacity);
+      return false;
+    }
+    if (guard_bad(p.st, ntot, p.cap, 22)) return false;
+    g.dener_sum += f2_dbl(de);
+    g.nat[b] = nat + 1;
+    if (g.ff) {  // the records as k_pack forms them (a mobile ion)
+      const f2 x = g.fx[a], y = g.fy[a], z = g.fz[a];
+      const int code = (p.nwtype[tr.itype] - 1) | (1 << 16);
+      p.pk1[ntot] = make_float4(x.h, y.h, z.h, __int_as_float(code));
+      p.pk2[ntot] = make_float4(x.l, y.l, z.l, 0.0f);
+      p.pk3[ntot] = make_float4(0.0f, (float)p.cg[tr.itype], __int_as_float(1 << 1), 0.0f);
+    } else {
+      p.x[ntot] = tr.x;
+      p.y[ntot] = tr.y;
+      p.z[ntot] = tr.z;
+    }
+    p.typei[ntot] = g.ti[a];
+    p.ibuffer[ntot] = ib;
+    if (rf_on) p.gc_rff[ntot] = g.pff[a].rf;
+    g.ntot = ntot + 1;
+    g.ninsert[b] += 1;
+    g.chg[g.nchg++] = ntot;
+    g.pdel[a] = 1;
+  } else {
+    if (guard_bad(p.st, tr.j - 1, ntot, 23) || guard_bad(p.st, ntot - 1, p.cap, 24)) return false;
+    const int iat = tr.j - 1, last = ntot - 1;
+    const int bz = p.ibuffer[last];  // the ion the freed slot receives
+    g.dener_sum -= f2_dbl(de);
+    g.nremove[b] += 1;
+    if (g.ff) {
+      p.pk1[iat] = __ldcg(p.pk1 + last);
+      p.pk2[iat] = __ldcg(p.pk2 + last);
+      p.pk3[iat] = __ldcg(p.pk3 + last);
+    } else {
+      p.x[iat] = p.x[last];
+      p.y[iat] = p.y[last];
+      p.z[iat] = p.z[last];
+    }
+    p.typei[iat] = p.typei[last];
+    p.ibuffer[iat] = bz;
+    if (rf_on) p.gc_rff[iat] = __ldcg(p.gc_rff + last);
+    g.nat[b] = nat - 1;
+    g.ntot = ntot - 1;
+    g.chg[g.nchg++] = iat;
+    g.pdel[a] = -1;
+    g.touched |= 1ull << b;
+    if (bz >= 1 && bz <= kMaxBuffers) g.touched |= 1ull << (bz - 1);
+  }
+  g.pbuf[a] = b;
+  g.acck[g.nacc] = a;
+  g.accs[g.nacc++] = tr.insert ? 1 : -1;
+  return true;
+}
+
+// The round's attempts in order (block 0, every thread), in waves: each
+// wave evaluates every attempt not yet settled, in parallel, in the current
+// state; thread 0 then settles them in order up to the first move made
+// (the rest are evaluated again in the new state) or the first trial that
+// no longer holds (the round ends there).  A wave per accepted move, plus
+// one.  g.done: the attempts settled; g.chg: the slots rewritten.
+__device__ void settle(const KP &p, uint32_t mask, uint64_t cycle, int na, GrandState &g) {
+  const int t = threadIdx.x;
+  const bool rf_on = (mask & 16u) && p.qrfpar;
+  if (t == 0) {
+    g.cur = 0;
+    g.stop = 0;
+    g.nacc = 0;
+    g.touched = 0;
+    g.nchg = 0;
+  }
+  __syncthreads();
+  for (;;) {
+    const int a0 = g.cur;
+    if (a0 >= na || g.stop) break;
+    if (t >= a0 && t < na) g.wst[t] = evaluate(p, cycle, t, g, g.wde[t], g.werr[t]);
+    __syncthreads();
+    if (t == 0) {
+      int k = a0;
+      while (k < na) {
+        const int st = g.wst[k];
+        if (st == kStop) {
+          g.stop = 1;
+          break;
+        }
+        const Trial &tr = g.tr[k];
+        g.pbuf[k] = -1;
+        g.pdel[k] = 0;
+        if (g.werr[k]) atomicOr(&p.st->err, g.werr[k]);
+        if (st != kNoop && !tr.insert && g.nalert[k] > 0)
+          atomicAdd(&p.warn[p.nwtype[tr.itype]], g.nalert[k]);
+        const bool moved = st == kAccept && apply_move(p, rf_on, k, g);
+        ++k;
+        if (moved) break;
+      }
+      g.cur = k;
+    }
+    __syncthreads();
+  }
+  if (t == 0) g.done = g.cur;
 }
 
 // prob(ib, nat(ib)) += 1 after each settled attempt (grand.f90:117-119),
@@ -844,13 +1389,17 @@ __device__ void round_histogram(const KP &p, GrandState &g) {
 __global__ void __launch_bounds__(kGrandThreads)
     k_grand(KP p, uint32_t mask, uint64_t seed, uint64_t cycle, int ngcmc, int ffpos) {
   __shared__ GrandState g;
-  __shared__ double red[kGrandWarps * kSpec];
+  __shared__ GrandTabs tabs;
+  __shared__ float2 red[kGrandWarps * kSpec];
   __shared__ int ered[kGrandWarps * kSpec];
   __shared__ int flag;
   DevState *st = p.st;
   const bool rf_on = (mask & 16u) && p.qrfpar;
   const int ntot0 = st->ntot;
   bool ok = true;
+  TypeRefs T;
+  PairRefs P;
+  load_tabs(p, tabs, T, P);
   if (blockIdx.x == 0) {  // the coordinator: GCMC state into shared memory
     const int nb = p.nbuffer;
     for (int b = threadIdx.x; b < nb; b += blockDim.x) {
@@ -869,10 +1418,13 @@ __global__ void __launch_bounds__(kGrandThreads)
       g.rmax[ib] = p.rmax[ib];
       g.ibfftyp[ib] = p.ibfftyp[ib];
       g.qbias[ib] = p.qbufferbias[ib];
+      g.avf[ib] = f2_ld(p.bufff[3 * ib]);
+      g.muf[ib] = f2_ld(p.bufff[3 * ib + 1]);
+      g.kbbf[ib] = f2_ld(p.bufff[3 * ib + 2]);
     }
     if (threadIdx.x == 0) {
       g.ntot = ntot0;
-      g.dener_sum = st->dener_sum;
+      g.dener_sum = 0.0;  // the call's sum
       g.ff = ffpos;
       g.nbuf = nb;
       g.nchg = 0;
@@ -881,29 +1433,30 @@ __global__ void __launch_bounds__(kGrandThreads)
     int a0 = 0;
     for (unsigned r = 1; ok; ++r) {
       const int na = min(ngcmc - a0, kSpec);
-      if (na > 0) build_round(p, mask, seed, cycle, a0, na, g);
-      if (threadIdx.x == 0) {  // publish the round
+      if (na > 0) build_round(p, T, mask, seed, cycle, a0, na, g);
+      if (threadIdx.x == kGrandThreads - 32) {  // publish the round (warp 0 goes on)
         GrandRound *hd = p.ground;
         hd->a0 = a0;
         hd->na = na;
         hd->ntot = g.ntot;
         hd->nchg = g.nchg;
         for (int c = 0; c < g.nchg; ++c) hd->chg[c] = g.chg[c];
-        for (int k = 0; k < na; ++k) p.trial[k] = g.tr[k];
+        for (int k = 0; k < na; ++k) {
+          p.trial[k] = g.tr[k];
+          p.tff[k] = g.tf[k];
+        }
         __threadfence();
         release_add(&st->bar_gen, 1u);
       }
       if (na <= 0) break;
-      trial_ions(p, mask, na, g);
+      trial_ions(p, T, mask, na, g);
       for (int b = threadIdx.x; b < nb; b += blockDim.x) g.nat0[b] = g.nat[b];
       __syncthreads();
-      trial_pairs(p, mask, na, g);
+      trial_pairs(p, P, mask, na, g);
       if (!(ok = block_wait(&st->bar_count, (unsigned)(gridDim.x - 1) * r, st, &flag))) break;
       round_sums(p, na, g);
       __syncthreads();
-      first_acceptances(p, cycle, na, g);
-      __syncthreads();
-      if (threadIdx.x == 0) settle(p, mask, cycle, na, g);
+      settle(p, mask, cycle, na, g);
       __syncthreads();
       round_histogram(p, g);
       a0 += g.done;
@@ -920,6 +1473,7 @@ __global__ void __launch_bounds__(kGrandThreads)
       st->ntot = g.ntot;
       st->dener_sum = g.dener_sum;
     }
+    launch_exit(st);
     return;
   }
   // blocks 1..: the pair terms.  Warp wg of the pair phase holds particles
@@ -931,58 +1485,74 @@ __global__ void __launch_bounds__(kGrandThreads)
   const int i0 = ((blockIdx.x - 1) * kGrandWarps + wid) * per_warp + lane / ap;
   // RFPAR prepass: one lane per particle, at its position; the first
   // particle's record (its RFPAR from that lane) is kept across rounds
-  double2 rf0 = make_double2(0.0, 0.0);
+  float4 rf0 = make_float4(0.f, 0.f, 0.f, 0.f);
   if (rf_on && la == 0)
     for (int i = i0; i < ntot0; i += stride)
       if (i >= p.nsites) {
-        const double3 q = pos_of(p, ffpos, i);
-        const double2 v = rf_single(p, q.x, q.y, q.z, abs(p.typei[i]));
-        p.gc_rf[i] = v;
-        if (i == i0) rf0 = v;
+        const PartFF q = load_partff(p, i, false, ffpos);
+        f2 sr, re;
+        rf_gather_ff(p, q.x, q.y, q.z, rf_ifir(p, T, abs(q.ti)), sr, re);
+        const float4 c = rf_record_ff(T, sr, re, q.ti);
+        p.gc_rff[i] = c;
+        if (i == i0) rf0 = c;
       }
-  PartRec pre{};
-  if (i0 < ntot0) pre = load_part(p, i0, false, ffpos);
-  pre.rf.x = __shfl_sync(0xffffffffu, rf0.x, lane & ~(ap - 1));
-  pre.rf.y = __shfl_sync(0xffffffffu, rf0.y, lane & ~(ap - 1));
+  PartFF pre{};
+  if (i0 < ntot0) pre = load_partff(p, i0, false, ffpos);
+  const int src = lane & ~(ap - 1);
+  pre.rf = make_float4(__shfl_sync(0xffffffffu, rf0.x, src), __shfl_sync(0xffffffffu, rf0.y, src),
+                       __shfl_sync(0xffffffffu, rf0.z, src), __shfl_sync(0xffffffffu, rf0.w, src));
   for (unsigned r = 1; ok; ++r) {
     if (!(ok = block_wait(&st->bar_gen, r, st, &flag))) break;
+    // the round header and the lane's trial, loaded together (a trial slot
+    // past the round's attempts holds stale data and is not used)
     const GrandRound *hd = p.ground;
-    const int na = __ldcg(&hd->na);
+    const int na = __ldcg(&hd->na), ntot = __ldcg(&hd->ntot), nchg = __ldcg(&hd->nchg);
+    TrialFF tf;
+    {
+      const uint2 *src2 = reinterpret_cast<const uint2 *>(p.tff + la);
+      uint2 *dst2 = reinterpret_cast<uint2 *>(&tf);
+#pragma unroll
+      for (int k = 0; k < (int)(sizeof(TrialFF) / sizeof(uint2)); ++k) dst2[k] = __ldcg(src2 + k);
+    }
     if (na <= 0) break;
-    const int ntot = __ldcg(&hd->ntot), nchg = __ldcg(&hd->nchg);
+    if (la >= na) tf.valid = 0;
     for (int c = 0; c < nchg; ++c)  // the previous round rewrote this slot
-      if (__ldcg(&hd->chg[c]) == i0 && i0 < ntot) pre = load_part(p, i0, rf_on, ffpos);
-    Trial tr{};
-    if (la < na) tr = load_trial_cg(p.trial + la);
-    const int jt2 = trial_type2(p, tr);
-    const bool beion = tr.valid && tr.j - 1 >= p.nsites;
-    const bool rf = tr.valid && tr.rf_in && (mask & 16u);
-    double u = 0.0;
+      if (__ldcg(&hd->chg[c]) == i0 && i0 < ntot) pre = load_partff(p, i0, rf_on, ffpos);
+    f2 u = f2_f(0.0f);
     int err = 0;
-    if (jt2 > 0)
+    if (tf.valid && tf.jt2 > 0)
       for (int i = i0; i < ntot; i += stride)
-        if (i != tr.j - 1)
-          u += i == i0 ? interact_rec(p, tr, mask, i, jt2, beion, rf, pre, err)
-                       : interact_one(p, tr, mask, i, jt2, beion, rf, err, ffpos);
+        if (i != tf.j - 1) {
+          f2 v;
+          if (!pair_ff(p, P, tf, mask, i, i == i0 ? pre : load_partff(p, i, rf_on, ffpos), v,
+                       err)) {
+            // closer than float-float's range: the FP64 law (RFPAR gathered in FP64)
+            const Trial tr = load_trial_cg(p.trial + la);
+            PartRec q = load_part(p, i, false, ffpos);
+            if (rf_on && i >= p.nsites) q.rf = rf_single(p, q.x, q.y, q.z, abs(q.ti));
+            v = f2_of(near_pair64(p, tr, mask, i, tf.jt2, tf.rf != 0, q, err));
+          }
+          u = f2_add(u, v);
+        }
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1)
       if (o >= ap) {  // lanes of one attempt
-        u += __shfl_xor_sync(0xffffffffu, u, o);
+        u = f2_add(u, {__shfl_xor_sync(0xffffffffu, u.h, o), __shfl_xor_sync(0xffffffffu, u.l, o)});
         err |= __shfl_xor_sync(0xffffffffu, err, o);
       }
     if (lane < ap) {
-      red[wid * kSpec + lane] = u;
+      red[wid * kSpec + lane] = f2_st(u);
       ered[wid * kSpec + lane] = err;
     }
     __syncthreads();
     if (threadIdx.x < na) {
-      double s = 0.0;
+      f2 s2 = f2_f(0.0f);
       int e = 0;
       for (int w = 0; w < kGrandWarps; ++w) {
-        s += red[w * kSpec + threadIdx.x];
+        s2 = f2_add(s2, f2_ld(red[w * kSpec + threadIdx.x]));
         e |= ered[w * kSpec + threadIdx.x];
       }
-      p.ipart[(size_t)blockIdx.x * kSpec + threadIdx.x] = s;
+      reinterpret_cast<float2 *>(p.ipart)[(size_t)blockIdx.x * kSpec + threadIdx.x] = f2_st(s2);
       p.ierr[(size_t)blockIdx.x * kSpec + threadIdx.x] = e;
     }
     __syncthreads();
@@ -991,6 +1561,7 @@ __global__ void __launch_bounds__(kGrandThreads)
       release_add(&st->bar_count, 1u);
     }
   }
+  launch_exit(st);
 }
 
 // Blocks of the GRAND launch: the coordinator and enough blocks for a lane
@@ -1018,10 +1589,7 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
   const int warps = (ntot_ub + ngcmc + per_warp - 1) / per_warp;
   int grid = (warps + kGrandWarps - 1) / kGrandWarps + 1;  // + block 0, the coordinator
   grid = std::max(2, std::min(std::min(grid, max_res[dev]), ipart_slots));
-  // both launch counters start at zero
-  if ((e = cudaMemsetAsync(&p.st->bar_count, 0, 2 * sizeof(unsigned), stream)) != cudaSuccess)
-    return e;
-  KP pc = p;
+  KP pc = p;  // the barrier counters are zero between launches (launch_exit)
   void *args[] = {(void *)&pc, (void *)&mask, (void *)&seed, (void *)&cycle, (void *)&ngcmc,
                   (void *)&ffpos};
   return cudaLaunchCooperativeKernel((const void *)k_grand, dim3(grid), dim3(kGrandThreads),

@@ -59,4 +59,23 @@ __device__ __forceinline__ bool grid_barrier(unsigned *ctr, unsigned k, DevState
   return *flag != 0;
 }
 
+// End of a cooperative launch that used the counters (every block, every
+// thread; also after a wait that gave up): the last block out clears them
+// for the next launch on the stream, so no reset runs between launches.
+// By then every other block has passed its last wait.
+__device__ __forceinline__ void launch_exit(DevState *st) {
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    __threadfence();
+    cuda::atomic_ref<unsigned, cuda::thread_scope_device> x(st->bar_exit);
+    if (x.fetch_add(1u, cuda::memory_order_acq_rel) == gridDim.x - 1) {
+      cuda::atomic_ref<unsigned, cuda::thread_scope_device>(st->bar_count)
+          .store(0u, cuda::memory_order_relaxed);
+      cuda::atomic_ref<unsigned, cuda::thread_scope_device>(st->bar_gen)
+          .store(0u, cuda::memory_order_relaxed);
+      x.store(0u, cuda::memory_order_relaxed);
+    }
+  }
+}
+
 }  // namespace bgpu

@@ -46,6 +46,34 @@ struct F32C {
   float L[3], iL[3], rc2;  // extension mode: box lengths, their inverses, cutoff^2
 };
 
+// Float-float twins (value = x + y) of what GRAND's ΔE reads, filled on the
+// host so that the GRAND kernel converts no constant.
+struct PairFF {  // PairParam; c3pi = c3 * pi as the FP64 law forms it
+  float2 fct, epp4, sgp2, c0, c1, c2, c3pi, c4, sc0, sc1, sc2, dm2lo, dm2hi, dmi;
+  int flags, nxi, npieces, pad;
+};
+struct GridFF {  // Grid3: in-map bounds bcen -+ tran, offsets tran - bcen, cell size
+  float2 ub[3], lb[3], o[3];
+  float2 dcel, idcel;
+  int ncl[3];
+};
+struct FFC {
+  GridFF g[3];    // static field, repulsion, RFPAR
+  float2 sqrfac, thold8, thold27, vzmin, vzmax;
+  float2 rth, srpx, srpk, srpy, ires, ikbt;
+  float2 L[3];    // extension mode: box lengths
+  float iL[3];    //   their inverses (nearest float)
+  float2 rc2;     //   cutoff on r^2
+};
+// A GRAND trial as its pair terms read it, in float-float.
+struct TrialFF {
+  float2 x, y, z;
+  float2 a;       // celec q_trial srfe reff: factor of the RFPAR cross term
+  float2 b;       // reff^2 of the trial
+  int valid, j, jt2, rf;  // rf: the cross term is on
+};
+static_assert(sizeof(TrialFF) % 8 == 0 && alignof(TrialFF) == 8, "TrialFF is read as uint2");
+
 struct KP {
   // ---- sizes (host-known) ----
   int cap, nsites, nfix, ntype, nold, nttyp, ndna, ntc;
@@ -164,6 +192,15 @@ struct KP {
   double *epart;                // [nslot*kNTerms] block partial energies
   double *eterms;               // [kNTerms] reduced energies
   int *warn;                    // [nttyp+1]
+  // ---- GRAND in float-float ----
+  FFC ffc;
+  const PairFF *ppff;           // [ntc]
+  const float2 *cgff, *qcff;    // [ntype+1] charge, celec * charge
+  const float2 *esvff;          // [nttyp+1] repulsion scale per combined type
+  const float2 *bufff;          // [3*(nbuffer+1)] (avnum, mu, kb) per buffer, 1-based
+  const float2 *epff;           // [3*cnt] effective-potential pieces (p1, p2, p3)
+  float4 *gc_rff;               // [cap] per ion: (q srfe reff, reff^2), each hi, lo
+  TrialFF *tff;                 // [kSpec] the round's trials
   double *ipart;                // [nslot*kSpec] INTERACT (per block) and GRAND
                                 // (per block and attempt) partial sums
   int *ierr;                    // [nslot*kSpec] GRAND: error flags of the partials

@@ -72,14 +72,14 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   if (fields_first) {
     for (int i = p.nsites + slot; i < ntot; i += nslot)
       fields_one_f32(p, i, false, i < m0, mask, 1, eo, ax);
-    if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
+    if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) goto done;
   }
   for (int s = 0; s < nsteps; ++s) {
     float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int q = slot; q < npair; q += nslot)
       n3_tile<II, RF, EFP, PBC>(p, ps, q, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w], sm.pr.acc[w],
                            sm.pr.accb[w], sm.pr.acc1[w], sm.pr.accb1[w], tab, e);
-    if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
+    if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) goto done;
     for (int it = blockIdx.x; it < nitem; it += G) {
       const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;
       assemble_tile<kLoopWarps>(p, as, fl, 1, variant, step0 + s, t, 0, sm.part, h, npos);
@@ -92,8 +92,10 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
         }
       }
     }
-    if (s + 1 < nsteps && !grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) return;
+    if (s + 1 < nsteps && !grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) goto done;
   }
+done:
+  launch_exit(p.st);
 }
 
 template <bool II, bool RF, bool EFP, bool PBC = false>
@@ -124,9 +126,7 @@ static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t 
   if (max_res[dev] < 0) return cudaErrorCooperativeLaunchTooLarge;
   const int T = fl.ntile;
   const int grid = std::max(1, std::min(max_res[dev], std::max(n3_pairs(T), T)));
-  if ((e = cudaMemsetAsync(&p.st->bar_count, 0, sizeof(unsigned), stream)) != cudaSuccess)
-    return e;
-  KP pc = p;
+  KP pc = p;  // the barrier counters are zero between launches (launch_exit)
   AssembleFlags fc = fl;
   void *args[] = {(void *)&pc, (void *)&fc, (void *)&mask, (void *)&variant,
                   (void *)&seed, (void *)&step0, (void *)&nsteps, (void *)&fields_first};

@@ -2,13 +2,38 @@
 // (the pair laws run on the FP32 pipe, not on tensor cores).  Eight
 // independent FMA chains per thread, two waves of 8 blocks x 256 threads per
 // SM, timed with CUDA events on the caller's stream.
+//
+// Also the accuracy check of the float-float functions (ffmath.cuh): each
+// input is rounded to float-float, the function applied, the result widened
+// back to FP64 for the caller to compare with an FP64 reference.
 #include <algorithm>
 
 #include <cuda_runtime.h>
 
 #include "../../include/bromoc_gpu.h"
+#include "ffmath.cuh"
 
 namespace {
+
+__global__ void k_ff_check(int fn, int n, const double *x, double *out) {
+  using namespace bgpu;
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= n) return;
+  const f2 a = f2_of(x[i]), b = f2_of(x[i + 1 < n ? i + 1 : 0]);
+  f2 r = a;
+  switch (fn) {
+    case BROMOC_FF_EXP: r = f2_exp(a); break;
+    case BROMOC_FF_COS: r = f2_cos(a); break;
+    case BROMOC_FF_SQRT: r = f2_sqrt(a); break;
+    case BROMOC_FF_RCP: r = f2_rcp(a); break;
+    case BROMOC_FF_MUL: r = f2_mul(a, b); break;
+    case BROMOC_FF_DIV: r = f2_div(a, b); break;
+    case BROMOC_FF_ADD: r = f2_add(a, b); break;
+    case BROMOC_FF_RSQRT: r = f2_rsqrt(a); break;
+    default: break;
+  }
+  out[i] = f2_dbl(r);
+}
 
 __global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters,
                                                   float b, float c) {
@@ -65,4 +90,21 @@ extern "C" int bromoc_gpu_fp32_peak(void *stream, double *tflops) {
   if (err != cudaSuccess) return BROMOC_E_CUDA;
   *tflops = best;
   return BROMOC_OK;
+}
+
+extern "C" int bromoc_gpu_ff_check(int32_t fn, int32_t n, const double *x, double *out) {
+  if (!x || !out || n < 1 || fn < BROMOC_FF_EXP || fn > BROMOC_FF_RSQRT) return BROMOC_E_ARG;
+  double *d = nullptr;
+  if (cudaMalloc(&d, 2 * (size_t)n * sizeof(double)) != cudaSuccess) return BROMOC_E_NOMEM;
+  int rc = BROMOC_OK;
+  if (cudaMemcpy(d, x, (size_t)n * sizeof(double), cudaMemcpyHostToDevice) != cudaSuccess)
+    rc = BROMOC_E_CUDA;
+  if (!rc) {
+    k_ff_check<<<(n + 127) / 128, 128>>>(fn, n, d, d + n);
+    if (cudaMemcpy(out, d + n, (size_t)n * sizeof(double), cudaMemcpyDeviceToHost) !=
+        cudaSuccess)
+      rc = BROMOC_E_CUDA;
+  }
+  cudaFree(d);
+  return rc;
 }

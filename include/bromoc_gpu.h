@@ -331,7 +331,8 @@ enum {
   BROMOC_K_FIELDS = 2,   /* single-particle map/membrane kernel            */
   BROMOC_K_ASSEMBLE = 3, /* force assembly + BD update                     */
   BROMOC_K_LOOP = 4,     /* fused BD loop (all of the above, many steps)   */
-  BROMOC_K_NKINDS = 5
+  BROMOC_K_GRAND = 5,    /* GRAND (all attempts of a call)                 */
+  BROMOC_K_NKINDS = 6
 };
 int bromoc_gpu_kernel_timing(bromoc_ctx *ctx, int32_t on);
 /* bd_steps in FP32 mode runs the steps of a system without sites as one
@@ -352,6 +353,21 @@ int bromoc_gpu_kernel_time(bromoc_ctx *ctx, int32_t which, double *total_ms,
 /* Measured FP32 FMA throughput of the current device (TFLOP/s), the
  * denominator of the pair kernels' roofline. */
 int bromoc_gpu_fp32_peak(void *stream, double *tflops);
+/* Accuracy check of the float-float arithmetic GRAND evaluates its ΔE in
+ * (no counterpart in the reference): out[i] = f(x[i]) for the function
+ * fn below (binary ones take x[i] and x[(i+1) mod n]), each input first
+ * rounded to float-float, on the current device (synchronous). */
+enum {
+  BROMOC_FF_EXP = 0,
+  BROMOC_FF_COS = 1,
+  BROMOC_FF_SQRT = 2,
+  BROMOC_FF_RCP = 3,
+  BROMOC_FF_MUL = 4,
+  BROMOC_FF_DIV = 5,
+  BROMOC_FF_ADD = 6,
+  BROMOC_FF_RSQRT = 7
+};
+int bromoc_gpu_ff_check(int32_t fn, int32_t n, const double *x, double *out);
 
 /* GRAND (grand.f90:19-121): ngcmc grand-canonical insertion/deletion
  * attempts of cycle `cycle` (1-based icycle), device resident.  Uniforms are

@@ -159,6 +159,31 @@ class TestGpuPeriodic:
             b = o.interact(*p, 1, n + 1)
             assert abs(a - b) <= 1e-10 * max(1.0, abs(b)), (p, a, b)
 
+    @pytest.mark.parametrize("precision", [abi.FP64, abi.FP32])
+    def test_grand_nearest_image(self, gpu_lib, oracle_mod, precision):
+        """GRAND in the extension mode: ΔE through the nearest image within
+        the cutoff (float-float in the GPU kernel), the same attempts and
+        outcomes as the oracle."""
+        spec = _spec(precision=precision, n_per=60)
+        spec.buffers = [dict(ion="K", conc=1.5, lzmin=-0.5 * L, lzmax=0.5 * L),
+                        dict(ion="Cl", conc=0.5, lzmin=-0.5 * L, lzmax=0.5 * L)]
+        spec.count()
+        g = gpu_lib.create(CAP, precision)
+        spec.push(g)
+        o = oracle_mod.create(CAP)
+        spec.push(o)
+        for cyc in range(1, 7):
+            dg, do = g.grand(8, 31, cyc), o.grand(8, 31, cyc)
+            assert abs(dg - do) <= 1e-8 * max(1.0, abs(do)), (cyc, dg, do)
+        for x, y in zip(g.get_buffers(), o.get_buffers()):
+            np.testing.assert_array_equal(x, y)
+        _, nins, nrem, _ = o.get_buffers()
+        assert nins.sum() + nrem.sum() > 0
+        pg, po = g.get_particles(), o.get_particles()
+        np.testing.assert_array_equal(pg[3], po[3])
+        np.testing.assert_array_equal(pg[4], po[4])
+        np.testing.assert_allclose(np.stack(pg[:3]), np.stack(po[:3]), atol=1e-9)
+
     def test_refusals(self, gpu_lib):
         sph = synth.bulk_kcl(n_per=4, L=30.0)
         sph.shape = abi.SPHERE

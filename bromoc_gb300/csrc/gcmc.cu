@@ -1445,8 +1445,7 @@ __global__ void __launch_bounds__(kGrandThreads)
           p.trial[k] = g.tr[k];
           p.tff[k] = g.tf[k];
         }
-        __threadfence();
-        release_add(&st->bar_gen, 1u);
+        release_add(&st->bar_gen, 1u);  // orders this thread's stores before it
       }
       if (na <= 0) break;
       trial_ions(p, T, mask, na, g);
@@ -1555,11 +1554,8 @@ __global__ void __launch_bounds__(kGrandThreads)
       reinterpret_cast<float2 *>(p.ipart)[(size_t)blockIdx.x * kSpec + threadIdx.x] = f2_st(s2);
       p.ierr[(size_t)blockIdx.x * kSpec + threadIdx.x] = e;
     }
-    __syncthreads();
-    if (threadIdx.x == 0) {
-      __threadfence();
-      release_add(&st->bar_count, 1u);
-    }
+    __syncthreads();  // the partials, then the release of the arrival
+    if (threadIdx.x == 0) release_add(&st->bar_count, 1u);
   }
   launch_exit(st);
 }

@@ -1,6 +1,7 @@
 // ORACLE -- test infrastructure only.  A CPU (FP64, sequential) restatement of
 // the cg-gcmc-bd hot-path routines of the BROMOC reference, used by tests/,
-// __graft_entry__.smoke() and the CPU-baseline leg of bench.py as the checker.
+// __graft_entry__.smoke() and the CPU-baseline leg of bench.py as the
+// reference the GPU results are compared with.
 // Nothing in the product links or calls this code.
 //
 // Parity status: the reference (Fortran 90) cannot be compiled in this

@@ -3,7 +3,7 @@
 Tolerances: FP64 mode reproduces the oracle to summation-order rounding
 (1e-10 relative); FP32 pair arithmetic must give forces within 1e-5 relative
 of the FP64 oracle (||dF|| / ||F|| and per particle with a floor of 1e-3 of
-the median force) -- the bar the benchmark spec sets for single-precision pairs.
+the median force) -- the accuracy required of single-precision pairs.
 Integer outputs (warning counters, GCMC counters, crossing counts, particle
 counts) must match exactly.
 """

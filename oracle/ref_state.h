@@ -4,8 +4,8 @@
 // reference the GPU results are compared with.
 // Nothing in the product links or calls this code.
 //
-// Parity status: the reference (Fortran 90) cannot be compiled in this
-// container or on the GPU host (no Fortran compiler), and it ships no golden
+// Parity status: the reference (Fortran 90) cannot be compiled with the
+// toolchains at hand (C, C++ and CUDA only), and it ships no golden
 // vectors.  This restatement is pinned only by the reference's own built-in
 // known-answer procedures -- TEST (central finite-difference forces,
 // testfirst.f90:35-85) and ENERGY == 1/2 sum INTERACT

@@ -456,7 +456,7 @@ def run_gpu(args, rank, world, local_rank):
         out = {name: _lib.kernel_time(eng, k) for name, k in
                (("pairs", _lib.K_PAIRS), ("rfcross", _lib.K_RFCROSS),
                 ("fields", _lib.K_FIELDS), ("assemble", _lib.K_ASSEMBLE),
-                ("bd_loop", _lib.K_LOOP))}
+                ("bd_loop", _lib.K_LOOP), ("grand", _lib.K_GRAND))}
         _lib.kernel_timing(eng, False)
         return {k: v for k, v in out.items() if v[1] > 0}
 

@@ -70,3 +70,26 @@ def test_rounds_match_sequential_oracle(gpu_lib, oracle_mod, kind, precision):
     np.testing.assert_array_equal(ibg, ibo)
     tol = 1e-7 if precision == abi.FP32 else 1e-9
     np.testing.assert_allclose(np.stack([xg, yg, zg]), np.stack([xo, yo, zo]), atol=tol)
+
+
+@pytest.mark.parametrize("precision", [abi.FP64, abi.FP32])
+def test_rounds_with_sites(gpu_lib, oracle_mod, precision):
+    """Fixed DNA sites among the particles: the O(N) sums take the ion-site
+    laws (tabulated) for them; buffers at both ends of the box."""
+    spec = systems.dna(precision=precision)
+    spec.buffers = [dict(ion="K", conc=1.0, lzmin=-0.5 * spec.lz, lzmax=-0.5 * spec.lz + 10.0),
+                    dict(ion="Cl", conc=1.0, lzmin=0.5 * spec.lz - 10.0, lzmax=0.5 * spec.lz)]
+    spec.count()
+    g = gpu_lib.create(CAP, precision)
+    spec.push(g)
+    o = oracle_mod.create(CAP)
+    spec.push(o)
+    for cyc in range(1, 7):
+        dg, do = g.grand(6, 17, cyc), o.grand(6, 17, cyc)
+        assert abs(dg - do) <= 1e-8 * max(1.0, abs(do)), (cyc, dg, do)
+    for x, y in zip(g.get_buffers(), o.get_buffers()):
+        np.testing.assert_array_equal(x, y)
+    pg, po = g.get_particles(), o.get_particles()
+    np.testing.assert_array_equal(pg[3], po[3])
+    np.testing.assert_array_equal(pg[4], po[4])
+    np.testing.assert_allclose(np.stack(pg[:3]), np.stack(po[:3]), atol=1e-9)

@@ -747,6 +747,10 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
   p.ires = q->res > 0 ? 1.0 / q->res : 0.0;
   p.rthf = (float)p.rth;
   p.srpxf = (float)p.srpx;
+  p.srpx2lo = (float)(p.srpx * p.srpx * (1.0 - kSrpWin));
+  p.srpx2hi = (float)(p.srpx * p.srpx * (1.0 + kSrpWin));
+  p.rthlo = (float)(p.rth * (1.0 - kSrpWin));
+  p.rthhi = (float)(p.rth * (1.0 + kSrpWin));
   p.srpkf = (float)p.srpk;
   p.srpyf = (float)p.srpy;
   p.iresf = (float)p.ires;
@@ -830,10 +834,11 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
         if (f.flags & kEfp) ok = false;
         const int fl = f.flags & 15;
         // (fct, 6 epp4, sgp2, SRPMF cutoff on r^2 or -1): the LJ force takes
-        // 6 epp4; the SRPMF test is one compare
-        tab[(size_t)a * nion + b] =
-            make_float4((fl & kChr) ? f.fct : 0.0f, (fl & kLj) ? 6.0f * f.epp4 : 0.0f,
-                        (fl & kLj) ? f.sgp2 : 0.0f, (fl & kSrp) ? (float)p.rth : -1.0f);
+        // 6 epp4; the SRPMF test is one compare, against rth widened by the
+        // window in which srp_branch decides in FP64
+        tab[(size_t)a * nion + b] = make_float4(
+            (fl & kChr) ? f.fct : 0.0f, (fl & kLj) ? 6.0f * f.epp4 : 0.0f,
+            (fl & kLj) ? f.sgp2 : 0.0f, (fl & kSrp) ? p.rthhi : -1.0f);
       }
     float4 *dt = const_cast<float4 *>(p.ipq);
     if (!rc) rc = upload(ctx, &dt, tab.data(), std::max<size_t>(tab.size(), 1));

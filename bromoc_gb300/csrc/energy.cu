@@ -163,7 +163,8 @@ __global__ void __launch_bounds__(kPairThreads)
           const int code = __float_as_int(h.w);
           const float w = (code >> 16) ? 0.5f : 1.0f;
           if (EFP) {
-            de = law32k(p, __ldg(p.pidx + row + (code & 0xffff)), r2, w, e);
+            de = law32k(p, __ldg(p.pidx + row + (code & 0xffff)), r2, w, e,
+                        [&] { return r2_ff64(th, tl, h, l); });
           } else {
             const float4 q = tab[row + (code & 0xffff) - p.ndna];
             const float ir = rsqrtf(r2), ir2 = ir * ir;
@@ -175,7 +176,8 @@ __global__ void __launch_bounds__(kPairThreads)
             e[1] = fmaf(w, q.y * (d12 - d6), e[1]);
             de = ir2 * fmaf(q.y, fmaf(2.0f, d12, -d6), cofo);
             if (r2 <= q.w)
-              de += srpmf32(p, srp_index(p, __float_as_int(th.w), code), r2, ir, w, e);
+              de += srpmf32(p, srp_index(p, __float_as_int(th.w), code), r2, ir, w, e,
+                            srp_branch(p, r2, [&] { return r2_ff64(th, tl, h, l); }));
           }
         }
         if (RF && trf) {
@@ -398,7 +400,7 @@ __global__ void __launch_bounds__(kPairThreads)
       const float dx = ff_diff(th.x, tl.x, h.x, l.x), dy = ff_diff(th.y, tl.y, h.y, l.y),
                   dz = ff_diff(th.z, tl.z, h.z, l.z);
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-      const float de = law32(p, q, r2, 1.0f, e, err);
+      const float de = law32(p, q, r2, 1.0f, e, err, [&] { return r2_ff64(th, tl, h, l); });
       if (p.qproxdiff && (q.flags & kEfp) && r2 >= q.dm2lo && r2 <= q.dm2hi) {
         const float dist = sqrtf(r2);
         const float dm = dist - q.dmi;
@@ -451,7 +453,8 @@ __global__ void __launch_bounds__(kPairThreads) k_siteforce32(KP p) {
                   dz = ff_diff(h.z, l.z, sh.z, sl.z);
       const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
       float ef[4];
-      const float de = law32(p, p.ppf[is], r2, 0.0f, ef, err);
+      const float de =
+          law32(p, p.ppf[is], r2, 0.0f, ef, err, [&] { return r2_ff64(h, l, sh, sl); });
       f[0] = fmaf(-de, dx, f[0]);
       f[1] = fmaf(-de, dy, f[1]);
       f[2] = fmaf(-de, dz, f[2]);

@@ -5,6 +5,10 @@
 
 namespace bgpu {
 
+// Relative window around the SRPMF boundaries on r^2 within which the FP32
+// pair path takes its branch from the pair's FP64 r^2 (srp_branch).
+constexpr double kSrpWin = 4e-6;
+
 struct Grid3 {
   int nclx, ncly, nclz;
   double dcel, idcel, tranx, trany, tranz, xbcen, ybcen, zbcen;
@@ -104,7 +108,8 @@ struct KP {
   const int *pidx;        // [nttyp*nttyp] 0-based pair index, -1 none
   // dense ion-ion law table for the FP32 pair kernel: [nion_t * nion_t] of
   // (fct, 6 epp4, sgp2, rth or -1), fct/epp4 zeroed where the pair has no
-  // Coulomb/LJ term, rth (the SRPMF cutoff on r^2) where it has SRPMF;
+  // Coulomb/LJ term, rth (the SRPMF cutoff on r^2, widened by srp_branch's
+  // FP64 decision window) where it has SRPMF;
   // ipq_ok when it applies (no tabulated ion-ion law, nion_t <= kIonTabTypes)
   const float4 *ipq;
   int nion_t, ipq_ok;
@@ -113,6 +118,9 @@ struct KP {
   int cnt;
   double rth, srpx, srpk, srpy, res, ires;
   float rthf, srpxf, srpkf, srpyf, iresf;  // FP32 copies for the fast path
+  // the SRPMF boundaries on r^2 (taper start srpx^2, cutoff rth) with the
+  // window around each in which srp_branch decides in FP64: below, above
+  float srpx2lo, srpx2hi, rthlo, rthhi;
   // ---- sites ----
   const int *typtyp;      // [nsites] 1-based combined type
   const double *sitecharge;

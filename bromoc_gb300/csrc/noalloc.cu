@@ -22,8 +22,13 @@
 //     every slot it later reads (nothing relies on zeroed memory) and clears
 //     its error flag itself;
 //   - the first call on a device looks up the scratch's device address with
-//     cudaGetSymbolAddress (with that device current); make that first call
-//     before any stream capture begins.
+//     cudaGetSymbolAddress (with that device current) and keeps it for the
+//     life of the process; make that first call before any stream capture
+//     begins.  A device reset (cudaDeviceReset) ends every context of this
+//     library and leaves that address stale: the library is not used again
+//     in a process after a reset;
+//   - each call waits on its stream before it returns (it reads back the
+//     error word), so its results are ready when it returns.
 #include <cstdio>
 #include <mutex>
 
@@ -67,6 +72,8 @@ __global__ void __launch_bounds__(kTile)
                    const double *__restrict__ y, const double *__restrict__ z,
                    const int *__restrict__ typei, StaticScratch *s) {
   __shared__ double sx[kTile], sy[kTile], sz[kTile];
+  // FP32: each source's coordinates split once into hi + lo floats
+  __shared__ float4 shi[FP32 ? kTile : 1], slo[FP32 ? kTile : 1];
   __shared__ int sc[kTile];
   __shared__ double red[(kTile / 32) * 4];
   __shared__ double tot[4];
@@ -106,6 +113,15 @@ __global__ void __launch_bounds__(kTile)
       sx[threadIdx.x] = x[src];
       sy[threadIdx.x] = y[src];
       sz[threadIdx.x] = z[src];
+      if (FP32) {
+        float4 h, l;
+        hi_lo(sx[threadIdx.x], h.x, l.x);
+        hi_lo(sy[threadIdx.x], h.y, l.y);
+        hi_lo(sz[threadIdx.x], h.z, l.z);
+        h.w = l.w = 0.f;
+        shi[threadIdx.x] = h;
+        slo[threadIdx.x] = l;
+      }
       sc[threadIdx.x] = good ? ((p.nwtype[it] - 1) | ((src >= nfix) << 16)) : -1;
     }
     __syncthreads();
@@ -117,14 +133,15 @@ __global__ void __launch_bounds__(kTile)
         if (base + k == t || code < 0) continue;
         const int is = p.pidx[row + (code & 0xffff)];
         if (FP32) {
-          float sxh, sxl, syh, syl, szh, szl;
-          hi_lo(sx[k], sxh, sxl);
-          hi_lo(sy[k], syh, syl);
-          hi_lo(sz[k], szh, szl);
-          const float dx = (xh - sxh) + (xl - sxl), dy = (yh - syh) + (yl - syl),
-                      dz = (zh - szh) + (zl - szl);
+          const float4 sh = shi[k], sl = slo[k];
+          const float dx = (xh - sh.x) + (xl - sl.x), dy = (yh - sh.y) + (yl - sl.y),
+                      dz = (zh - sh.z) + (zl - sl.z);
           const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
-          const float de = law32(p, p.ppf[is], r2, (code >> 16) ? 0.5f : 1.0f, ef, terr);
+          const float de =
+              law32(p, p.ppf[is], r2, (code >> 16) ? 0.5f : 1.0f, ef, terr, [&] {
+                return r2_ff64(make_float4(xh, yh, zh, 0.f), make_float4(xl, yl, zl, 0.f),
+                               sh, sl);
+              });
           ff[0] = fmaf(de, dx, ff[0]);
           ff[1] = fmaf(de, dy, ff[1]);
           ff[2] = fmaf(de, dz, ff[2]);
@@ -215,7 +232,7 @@ extern "C" int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t
   if (kp->periodic)
     return bromoc_ctx_fail(ctx, BROMOC_E_STATE,
                            "pair_energy_static: the periodic mode is not supported");
-  if (!x || !y || !z || !typei || !fx || !fy || !fz || !eterms4)
+  if (!eterms4 || (n > 0 && (!x || !y || !z || !typei || !fx || !fy || !fz)))
     return bromoc_ctx_fail(ctx, BROMOC_E_ARG, "pair_energy_static: null device buffer");
   if (n > kMaxIons)
     return bromoc_ctx_fail(ctx, BROMOC_E_CAPACITY,
@@ -226,12 +243,12 @@ extern "C" int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t
   StaticScratch *s = nullptr;
   int rc = scratch_address(ctx, &s);
   if (rc) return rc;
-  if (n == 0) return BROMOC_OK;
-  // source chunks of a multiple of the tile, at most kMaxChunks
+  // source chunks of a multiple of the tile, at most kMaxChunks (none for
+  // n == 0, where the output kernel still writes zero energies)
   const int stiles = (n + kTile - 1) / kTile;
   const int per = (stiles + kMaxChunks - 1) / kMaxChunks;
   const int chunk = per * kTile;
-  const int nchunk = (n + chunk - 1) / chunk;
+  const int nchunk = n > 0 ? (n + chunk - 1) / chunk : 0;
   const int ttiles = (n - nfix + kTile - 1) / kTile;
   if (cudaMemsetAsync(&s->err, 0, sizeof(int), stream) != cudaSuccess)
     return bromoc_ctx_fail(ctx, BROMOC_E_CUDA, "pair_energy_static: clearing the flag");
@@ -244,7 +261,7 @@ extern "C" int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t
       k_pairs_static<false><<<g, kTile, 0, stream>>>(*kp, n, nfix, chunk, x, y, z, typei, s);
     nslots = ttiles * nchunk;
   }
-  k_pairs_static_out<<<(n + 255) / 256, 256, 0, stream>>>(n, nfix, ttiles > 0 ? nchunk : 0,
+  k_pairs_static_out<<<max(1, (n + 255) / 256), 256, 0, stream>>>(n, nfix, ttiles > 0 ? nchunk : 0,
                                                           nslots, fx, fy, fz, eterms4, s);
   int err = 0;
   if (cudaGetLastError() != cudaSuccess ||

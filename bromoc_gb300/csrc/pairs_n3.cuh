@@ -34,6 +34,25 @@ __device__ __forceinline__ void min_image_f(const KP &p, float &dx, float &dy, f
   dz = fmaf(-p.f.L[2], rintf(dz * p.f.iL[2]), dz);
 }
 
+// FP64 r^2 of a pair for srp_branch (the SRPMF boundary decision), with the
+// nearest image in the periodic extension mode: the same whole-box shifts as
+// min_image_f, in FP64 lengths as the FP64 path takes them.  The source's
+// records are read again from the warp's shared arrays (entry mm): volatile
+// reads, so that the pair loop need not keep them live for this rare path.
+template <bool PBC>
+__device__ __forceinline__ double pair_r2_64(const KP &p, const float4 &th, const float4 &tl,
+                                             int mm, const float4 *sh, const float4 *sl) {
+  const volatile float *vh = reinterpret_cast<const volatile float *>(sh + mm);
+  const volatile float *vl = reinterpret_cast<const volatile float *>(sl + mm);
+  const float4 h = make_float4(vh[0], vh[1], vh[2], 0.f);
+  const float4 l = make_float4(vl[0], vl[1], vl[2], 0.f);
+  if (!PBC) return r2_ff64(th, tl, h, l);
+  const float dx = (th.x - h.x) + (tl.x - l.x), dy = (th.y - h.y) + (tl.y - l.y),
+              dz = (th.z - h.z) + (tl.z - l.z);
+  return r2_ff64(th, tl, h, l, p.lx * (double)rintf(dx * p.f.iL[0]),
+                 p.ly * (double)rintf(dy * p.f.iL[1]), p.lz * (double)rintf(dz * p.f.iL[2]));
+}
+
 // Systems up to this many ion tiles run the pair tile's two-chain loop.
 constexpr int kN3DualTiles = 96;
 
@@ -154,7 +173,8 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
     ge[1] = fmaf(c.y, d12 - d6, ge[1]);
     float de = ir2 * fmaf(c.y, fmaf(2.0f, d12, -d6), cofo);
     if (r2 <= c.w)
-      de += srpmf32(p, srp_index(p, tcode, __float_as_int(h.w)), r2, ir, 1.0f, ge);
+      de += srpmf32(p, srp_index(p, tcode, __float_as_int(h.w)), r2, ir, 1.0f, ge,
+                    srp_branch(p, r2, [&] { return pair_r2_64<PBC>(p, th, tl, mm, sh, sl); }));
     float4 a = ac[mm];
     if (RF) {
       const float4 u = sq[mm];
@@ -240,7 +260,8 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
         float dii = 0.0f, drf = 0.0f, dAs = 0.0f, dBs = 0.0f;
         if (II && (tmob || smob) && !(PBC && r2 >= p.f.rc2)) {
           if (EFP) {
-            dii = law32k(p, __ldg(p.pidx + row + (scode & 0xffff)), r2, 1.0f, e);
+            dii = law32k(p, __ldg(p.pidx + row + (scode & 0xffff)), r2, 1.0f, e,
+                         [&] { return pair_r2_64<PBC>(p, th, tl, mm, sh, sl); });
           } else {
             const float4 c = tab[row + (scode & 0xffff) - p.ndna];
             const float ir = rsqrt_nz(r2), ir2 = ir * ir;
@@ -251,7 +272,9 @@ __device__ __forceinline__ void n3_tile(const KP &p, const PairSys &ps, int q, i
             const float d12 = d6 * d6;
             e[1] = fmaf(c.y, d12 - d6, e[1]);
             dii = ir2 * fmaf(c.y, fmaf(2.0f, d12, -d6), cofo);
-            if (r2 <= c.w) dii += srpmf32(p, srp_index(p, tcode, scode), r2, ir, 1.0f, e);
+            if (r2 <= c.w)
+              dii += srpmf32(p, srp_index(p, tcode, scode), r2, ir, 1.0f, e,
+                             srp_branch(p, r2, [&] { return pair_r2_64<PBC>(p, th, tl, mm, sh, sl); }));
           }
         }
         if (RF) {

@@ -139,10 +139,47 @@ __device__ __forceinline__ double law64(const KP &p, const PairParam &q,
   return de;
 }
 
+// ---- which SRPMF branch a pair takes, FP32 path --------------------------
+// The reference's SRPMF law (energy.mono.f90:147-175) is not continuous at
+// its two boundaries: energy and force jump where the taper starts (r =
+// srpx), and the force where the law ends (r^2 = rth).  An FP32 r^2 carries a
+// relative error of a few 1e-7, so a pair that close to a boundary could take
+// the other branch than in FP64 and be off by the whole jump.  Outside a
+// window of kSrpWin (relative) around either boundary the FP32 r^2 decides;
+// inside it r2d() -- the pair's r^2 in FP64 from its float-float position
+// records -- decides, as the FP64 path would.
+// Returns 0 beyond rth, 1 inside rth before the taper, 2 in the taper.
+// The window's bounds are kernel-parameter constants (srpx2lo/hi, rthlo/hi),
+// which the comparisons read directly.
+template <class R2D>
+__device__ __forceinline__ int srp_branch(const KP &p, float r2, R2D r2d) {
+  if (r2 > p.rthhi) return 0;
+  if (r2 < p.rthlo) {
+    if (r2 >= p.srpx2hi) return 2;
+    if (r2 <= p.srpx2lo) return 1;
+  }
+  const double d = r2d();
+  return d > p.rth ? 0 : (d >= p.srpx * p.srpx ? 2 : 1);
+}
+
+// r^2 in FP64 of a pair from its float-float records (hi, lo) of the target
+// (th, tl) and the source (h, l): every difference of two floats is exact in
+// FP64.  s: whole box lengths to take off each component (the periodic
+// extension mode's nearest image), zero otherwise.
+__device__ __forceinline__ double r2_ff64(const float4 &th, const float4 &tl, const float4 &h,
+                                          const float4 &l, double sx = 0.0, double sy = 0.0,
+                                          double sz = 0.0) {
+  const double dx = ((double)th.x - (double)h.x) + ((double)tl.x - (double)l.x) - sx;
+  const double dy = ((double)th.y - (double)h.y) + ((double)tl.y - (double)l.y) - sy;
+  const double dz = ((double)th.z - (double)h.z) + ((double)tl.z - (double)l.z) - sz;
+  return dx * dx + dy * dy + dz * dz;
+}
+
 // ---- analytic pair law, FP32 ---------------------------------------------
+template <class R2D>
 __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
                                        float r2, float w, float e[4],
-                                       int &err) {
+                                       int &err, R2D r2d) {
   if (q.flags & kEfp) {
     float yp;
     e[3] += w * efp32(p, q, r2, yp, err);
@@ -162,7 +199,8 @@ __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
     e[1] += w * q.epp4 * (d12 - d6);
     de += q.epp4 * 6.0f * ir2 * (2.0f * d12 - d6);
   }
-  if ((q.flags & kSrp) && r2 <= p.rthf) {
+  const int branch = (q.flags & kSrp) && r2 <= p.rthhi ? srp_branch(p, r2, r2d) : 0;
+  if (branch) {
     float r = r2 * ir;
     float s, c;
     sincospif(q.c3 * (q.c1 - r), &s, &c);  // cos(c3 pi (c1 - r))
@@ -170,7 +208,7 @@ __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
     float e3 = pow6f(q.c1 * ir);
     float e0 = q.c0 * e1 * c + q.c4 * e3;
     float dc = (-q.c2 * c + q.c3 * (float)kPi * s) * q.c0 * e1 - 6.0f * q.c4 * e3 * ir;
-    if (r >= p.srpxf) {
+    if (branch == 2) {
       float fdf = expf(-p.srpkf * (r - p.srpxf)) - p.srpyf;
       dc = dc * fdf - e0 * p.srpkf * (fdf + p.srpyf);
       e0 = e0 * fdf;
@@ -181,11 +219,13 @@ __device__ __forceinline__ float law32(const KP &p, const PairParamF &q,
   return de;
 }
 
-// ---- SRPMF of pair type is inside rth, FP32 (energy.mono.f90:147-175):
-// c0 exp((c1 - r) c2) cos(c3 pi (c1 - r)) + c4 (c1 / r)^6 with the taper
-// beyond srpx; adds w E to e[2] and returns its -(dE/dr)/r term.
+// ---- SRPMF of a pair inside rth, FP32 (energy.mono.f90:147-175):
+// c0 exp((c1 - r) c2) cos(c3 pi (c1 - r)) + c4 (c1 / r)^6, tapered when
+// branch == 2 (srp_branch), nothing when branch == 0; adds w E to e[2] and
+// returns its -(dE/dr)/r term.
 __device__ __forceinline__ float srpmf32(const KP &p, int is, float r2, float ir, float w,
-                                         float e[4]) {
+                                         float e[4], int branch) {
+  if (branch == 0) return 0.0f;
   const float4 *q = p.ppk + 4 * is;
   const float4 q1 = __ldg(q + 1);
   const float c4 = __ldg(q + 2).x;
@@ -196,7 +236,7 @@ __device__ __forceinline__ float srpmf32(const KP &p, int is, float r2, float ir
   const float e3 = pow6f(q1.y * ir);
   float e0 = q1.x * e1 * c + c4 * e3;
   float dc = (-q1.z * c + q1.w * (float)kPi * s) * q1.x * e1 - 6.0f * c4 * e3 * ir;
-  if (r >= p.srpxf) {
+  if (branch == 2) {
     const float fdf = expf(-p.srpkf * (r - p.srpxf)) - p.srpyf;
     dc = dc * fdf - e0 * p.srpkf * (fdf + p.srpyf);
     e0 = e0 * fdf;
@@ -208,8 +248,9 @@ __device__ __forceinline__ float srpmf32(const KP &p, int is, float r2, float ir
 // ---- analytic pair law, FP32, packed table (p.ppk) ----------------------
 // The common Coulomb + LJ path needs one 16-byte load per pair; SRPMF
 // coefficients and the table constants are fetched only when used.
+template <class R2D>
 __device__ __forceinline__ float law32k(const KP &p, int is, float r2, float w,
-                                        float e[4]) {
+                                        float e[4], R2D r2d) {
   const float4 *q = p.ppk + 4 * is;
   const float4 q0 = __ldg(q);
   const int fl = __float_as_int(q0.w);
@@ -257,7 +298,8 @@ __device__ __forceinline__ float law32k(const KP &p, int is, float r2, float w,
     e[1] = fmaf(w, q0.y * (d12 - d6), e[1]);
     de = fmaf(q0.y * 6.0f * ir2, 2.0f * d12 - d6, de);
   }
-  if ((fl & kSrp) && r2 <= p.rthf) de += srpmf32(p, is, r2, ir, w, e);
+  if ((fl & kSrp) && r2 <= p.rthhi)
+    de += srpmf32(p, is, r2, ir, w, e, srp_branch(p, r2, r2d));
   return de;
 }
 

@@ -306,8 +306,12 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms,
  * n > 4096 returns BROMOC_E_CAPACITY.  No allocation or free happens in the
  * call.  All calls on a device share that scratch: calls that overlap on
  * the GPU race.  The first call on a device resolves the scratch address
- * (cudaGetSymbolAddress with that device current) -- make it before any
- * stream capture.  The call returns after the results are written. */
+ * (cudaGetSymbolAddress with that device current) and keeps it for the life
+ * of the process -- make that first call before any stream capture; after a
+ * device reset the library is not used again in the process.  Each call waits
+ * on its stream before it returns (it reads back an error word), so the
+ * results are written when it returns; n == 0 writes zero energies (the
+ * per-ion arrays may then be null). */
 int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t nfix,
                                   const double *x, const double *y,
                                   const double *z, const int32_t *typei,

@@ -50,7 +50,7 @@ def test_batch_energy_forces(setup, oracle_mod):
         off = b.offset(r)
         fb = f[off:off + len(s.x)]
         glob, worst = force_err(fb, fo)
-        assert glob <= FP32_TOL and worst <= 10 * FP32_TOL, (r, glob, worst)
+        assert glob <= FP32_TOL and worst <= FP32_TOL, (r, glob, worst)
         tb = {k: et[r, i] for i, k in enumerate(abi.TERM_NAMES)}
         assert energy_err(tb, to) <= 1e-5, (r, tb, to)
 

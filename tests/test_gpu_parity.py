@@ -2,8 +2,11 @@
 
 Tolerances: FP64 mode reproduces the oracle to summation-order rounding
 (1e-10 relative); FP32 pair arithmetic must give forces within 1e-5 relative
-of the FP64 oracle (||dF|| / ||F|| and per particle with a floor of 1e-3 of
-the median force) -- the accuracy required of single-precision pairs.
+of the FP64 oracle, as a whole (||dF|| / ||F||) and particle by particle
+against max(|F_i|, RMS |F|).  The floor is there because an FP32 r^2 rounds
+at a few 1e-7, which the contact pairs' r^-14 law turns into ~1e-6 of their
+force: a particle whose contact forces nearly cancel cannot reach 1e-5 of
+its own small net force.
 Integer outputs (warning counters, GCMC counters, crossing counts, particle
 counts) must match exactly.
 """
@@ -29,11 +32,13 @@ def _engines(spec, gpu_lib, oracle_mod, cap=CAP):
 
 
 def force_err(fg, fo):
+    """(global relative error, worst per-particle error against
+    max(|F_i|, RMS |F|))."""
     d = np.linalg.norm(fg - fo, axis=1)
     n = np.linalg.norm(fo, axis=1)
-    floor = 1e-3 * max(np.median(n), 1e-12)
+    floor = max(np.sqrt(np.mean(n * n)), 1e-300)
     glob = np.linalg.norm(fg - fo) / max(np.linalg.norm(fo), 1e-300)
-    return glob, (d / np.maximum(n, floor)).max()
+    return glob, float((d / np.maximum(n, floor)).max())
 
 
 def energy_err(tg, to):
@@ -50,7 +55,7 @@ def test_energy_forces(gpu_lib, oracle_mod, family, prec):
     to, fo, wo = o.energy(abi.M_ALL, forces=True)
     tol = FP64_TOL if prec == abi.FP64 else FP32_TOL
     glob, worst = force_err(fg, fo)
-    assert glob <= tol and worst <= 10 * tol, (family, glob, worst)
+    assert glob <= tol and worst <= tol, (family, glob, worst)
     etol = FP64_TOL if prec == abi.FP64 else 1e-5
     assert energy_err(tg, to) <= etol, (tg, to)
     np.testing.assert_array_equal(wg, wo)

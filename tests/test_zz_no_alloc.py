@@ -76,6 +76,35 @@ def test_static_scratch_matches_context_path(gpu_lib, prec):
     _check(lib, b, eng)
 
 
+@pytest.mark.parametrize("prec", [abi.FP64, abi.FP32])
+def test_static_scratch_chunk_packing(gpu_lib, prec):
+    """Sizes that pack several source tiles into one chunk: about 2100 ions
+    (two tiles per chunk, a ragged last chunk) and the 4096-ion limit (all
+    16 chunks of the scratch), both with fixed ions."""
+    from bromoc_gb300 import synth
+    lib = gpu_lib.load()
+    _declare(lib)
+    eng = gpu_lib.create(4200, prec)
+    for n_per, L, nfix in ((1050, 72.0, 7), (2048, 84.0, 33)):
+        s = synth.bulk_kcl(seed=40 + n_per, n_per=n_per, L=L, srpmf=True,
+                           precision=prec)
+        s.nfix = nfix
+        _check(lib, s, eng)
+
+
+def test_static_scratch_empty(gpu_lib):
+    """No ions: the energies come back as zeros, whatever the output
+    buffer held before."""
+    lib = gpu_lib.load()
+    _declare(lib)
+    eng = gpu_lib.create(64, abi.FP64)
+    systems.pairs(n_per=10).push(eng)
+    rc, _, e = _static_call(lib, eng, np.zeros(0), np.zeros(0), np.zeros(0),
+                            np.zeros(0, np.int32), 0)
+    assert rc == abi.OK
+    np.testing.assert_array_equal(e, np.zeros(4))
+
+
 def test_static_scratch_rejects_oversize(gpu_lib):
     lib = gpu_lib.load()
     _declare(lib)

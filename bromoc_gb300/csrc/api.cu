@@ -825,7 +825,8 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
   if (rc) return rc;
   {  // dense ion-ion table of the FP32 pair kernel
     const int nion = nt - ndna;
-    std::vector<float4> tab((size_t)nion * nion);
+    std::vector<float4> tab((size_t)nion * ipq_stride(nion),
+                            make_float4(0.0f, 0.0f, 0.0f, -1.0f));
     bool ok = nion <= kIonTabTypes;
     for (int a = 0; a < nion && ok; ++a)
       for (int b = 0; b < nion; ++b) {
@@ -836,7 +837,7 @@ int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *q) {
         // (fct, 6 epp4, sgp2, SRPMF cutoff on r^2 or -1): the LJ force takes
         // 6 epp4; the SRPMF test is one compare, against rth widened by the
         // window in which srp_branch decides in FP64
-        tab[(size_t)a * nion + b] = make_float4(
+        tab[(size_t)a * ipq_stride(nion) + b] = make_float4(
             (fl & kChr) ? f.fct : 0.0f, (fl & kLj) ? 6.0f * f.epp4 : 0.0f,
             (fl & kLj) ? f.sgp2 : 0.0f, (fl & kSrp) ? p.rthhi : -1.0f);
       }

@@ -43,12 +43,10 @@ template <bool RF>
 __global__ void __launch_bounds__(32 * kPairWarps)
     k_batch_pairs(const __grid_constant__ KP p, const RepDev *rep, const int2 *work, int nwork,
                   float4 *tpf, float *tpb, float *wpart) {
-  __shared__ float4 sh[kPairWarps][32], sl[kPairWarps][32], sq[kPairWarps][RF ? 32 : 1];
-  __shared__ float4 acc[kPairWarps][32], acc1[kPairWarps][32];
-  __shared__ float accb[kPairWarps][RF ? 32 : 1], accb1[kPairWarps][RF ? 32 : 1];
-  __shared__ float4 tab[kIonTabTypes * kIonTabTypes];
+  __shared__ N3Warp<RF> nw[kPairWarps];
+  __shared__ float4 tab[kIpqMax];
   const int nt = p.nion_t;
-  for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
+  for (int k = threadIdx.x; k < nt * ipq_stride(nt); k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
   const int widx = blockIdx.x * kPairWarps + w;
@@ -58,8 +56,7 @@ __global__ void __launch_bounds__(32 * kPairWarps)
   const PairSys ps{p.pk1 + R.off, p.pk2 + R.off, p.pk3 + R.off, tpf + (size_t)R.poff * 64,
                    tpb + (size_t)R.poff * 64, 0, 0, R.n, (R.n + 31) >> 5};
   float e[kRowTerms] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  n3_tile<true, RF, false>(p, ps, wk.y, 1, sh[w], sl[w], sq[w], acc[w], accb[w], acc1[w],
-                           accb1[w], tab, e);
+  n3_tile<true, RF, false>(p, ps, wk.y, 1, nw[w], tab, e);
   e[1] *= 1.0f / 6.0f;  // the tile sums 6 x elj
   // the tile pair's energies -> its slot (fixed shuffle tree)
 #pragma unroll

@@ -22,6 +22,29 @@ constexpr int kNTerms = 14;       // BROMOC_NTERMS
 constexpr int kMaxBuffers = 64;
 constexpr int kMaxTypes = 64;
 constexpr int kIonTabTypes = 16;  // ion types of the shared-memory pair table
+// Row stride of that table: each row of ion type a holds its nt laws (a, b)
+// and, at column nt, a zero law that empty column slots of a pair tile use.
+__host__ __device__ constexpr int ipq_stride(int nt) { return nt + 1; }
+constexpr int kIpqMax = kIonTabTypes * (kIonTabTypes + 1);
+
+// ---- packed FP32 pairs (f32x2, sm_100 and later) ---------------------------
+// One instruction applies the operation to both halves; each half rounds as
+// the scalar operation would.
+__device__ __forceinline__ float2 v2add(float2 a, float2 b) { return __fadd2_rn(a, b); }
+__device__ __forceinline__ float2 v2mul(float2 a, float2 b) { return __fmul2_rn(a, b); }
+__device__ __forceinline__ float2 v2fma(float2 a, float2 b, float2 c) {
+  return __ffma2_rn(a, b, c);
+}
+__device__ __forceinline__ float2 v2sub(float2 a, float2 b) {
+  float2 d;
+  asm("{\n\t.reg .b64 ra, rb, rd;\n\tmov.b64 ra, {%2, %3};\n\tmov.b64 rb, {%4, %5};\n\t"
+      "sub.rn.f32x2 rd, ra, rb;\n\tmov.b64 {%0, %1}, rd;\n\t}"
+      : "=f"(d.x), "=f"(d.y)
+      : "f"(a.x), "f"(a.y), "f"(b.x), "f"(b.y));
+  return d;
+}
+__device__ __forceinline__ float2 v2(float a, float b) { return make_float2(a, b); }
+__device__ __forceinline__ float2 v2(float a) { return make_float2(a, a); }
 
 // error flags raised by kernels (bit mask in DevState::err)
 enum : int {

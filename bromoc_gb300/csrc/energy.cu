@@ -112,12 +112,12 @@ template <bool II, bool RF, bool EFP>
 __global__ void __launch_bounds__(kPairThreads)
     k_pairs32(KP p, int qforces, int slot0, int t0) {
   __shared__ float4 sh[kPairThreads], sl[kPairThreads], sq[RF ? kPairThreads : 1];
-  __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
+  __shared__ float4 tab[EFP ? 1 : kIpqMax];
   __shared__ float red[(kPairThreads / 32) * 5];
   __shared__ float tot[5];
   const int nt = p.nion_t;
   if (II && !EFP)
-    for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
+    for (int k = threadIdx.x; k < nt * ipq_stride(nt); k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   const int ntot = p.st->ntot;
   const int m0 = p.nsites + p.nfix;
   const int t = t0 + blockIdx.x * kPairThreads + threadIdx.x;
@@ -129,7 +129,7 @@ __global__ void __launch_bounds__(kPairThreads)
     if (RF) tq = p.pk3[t];
     tb = __float_as_int(tq.z);
     const int code = __float_as_int(th.w) & 0xffff;
-    row = EFP ? code * p.nttyp : (code - p.ndna) * nt;
+    row = EFP ? code * p.nttyp : (code - p.ndna) * ipq_stride(nt);
   }
   const bool tmob = II && t < ntot && t >= m0;
   const bool trf = RF && t < ntot && (tb & 1);
@@ -237,23 +237,20 @@ constexpr int kN3Warps = 4;
 template <bool II, bool RF, bool EFP, bool PBC = false>
 __global__ void __launch_bounds__(32 * kN3Warps)
     k_pairs32n(KP p, int qforces, int slot0) {
-  __shared__ float4 sh[kN3Warps][32], sl[kN3Warps][32], sq[kN3Warps][RF ? 32 : 1];
-  __shared__ float4 acc[kN3Warps][32], acc1[kN3Warps][32];
-  __shared__ float accb[kN3Warps][RF ? 32 : 1], accb1[kN3Warps][RF ? 32 : 1];
-  __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
+  __shared__ N3Warp<RF> nw[kN3Warps];
+  __shared__ float4 tab[EFP ? 1 : kIpqMax];
   __shared__ float red[kN3Warps * 5];
   __shared__ float tot[5];
   const int nt = p.nion_t;
   if (II && !EFP)
-    for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
+    for (int k = threadIdx.x; k < nt * ipq_stride(nt); k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
   const int w = threadIdx.x >> 5;
   const int T = p.ntile;
   const int q = blockIdx.x * kN3Warps + w;
   float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
   if (q < n3_pairs(T))  // warp-uniform
-    n3_tile<II, RF, EFP, PBC>(p, pair_sys(p, p.st->ntot, T), q, qforces, sh[w], sl[w], sq[w],
-                              acc[w], accb[w], acc1[w], accb1[w], tab, e);
+    n3_tile<II, RF, EFP, PBC>(p, pair_sys(p, p.st->ntot, T), q, qforces, nw[w], tab, e);
   block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;

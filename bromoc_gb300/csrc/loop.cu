@@ -31,11 +31,7 @@ constexpr int kLoopWarps = 16;
 // block's shared memory (the phases never overlap within a block).
 template <bool RF>
 union LoopSmem {
-  struct {
-    float4 sh[kLoopWarps][32], sl[kLoopWarps][32], sq[kLoopWarps][RF ? 32 : 1];
-    float4 acc[kLoopWarps][32], acc1[kLoopWarps][32];
-    float accb[kLoopWarps][RF ? 32 : 1], accb1[kLoopWarps][RF ? 32 : 1];
-  } pr;
+  N3Warp<RF> nw[kLoopWarps];
   float part[kLoopWarps][10][32];
 };
 
@@ -45,14 +41,14 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
               uint64_t seed, uint64_t step0, int nsteps, int fields_first) {
   extern __shared__ __align__(16) unsigned char loop_dsm[];  // sizeof(LoopSmem<RF>)
   LoopSmem<RF> &sm = *reinterpret_cast<LoopSmem<RF> *>(loop_dsm);
-  __shared__ float4 tab[EFP ? 1 : kIonTabTypes * kIonTabTypes];
+  __shared__ float4 tab[EFP ? 1 : kIpqMax];
   __shared__ int flag;
   __shared__ AxisF ax[12];
   __shared__ float4 npos[32][3];  // phase A: the moved records of the tile
   stage_axes(p, ax);
   const int nt = p.nion_t;
   if (II && !EFP)
-    for (int k = threadIdx.x; k < nt * nt; k += blockDim.x) tab[k] = __ldg(p.ipq + k);
+    for (int k = threadIdx.x; k < nt * ipq_stride(nt); k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
   const int w = threadIdx.x >> 5;
   const int G = gridDim.x;
@@ -77,8 +73,7 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   for (int s = 0; s < nsteps; ++s) {
     float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     for (int q = slot; q < npair; q += nslot)
-      n3_tile<II, RF, EFP, PBC>(p, ps, q, 1, sm.pr.sh[w], sm.pr.sl[w], sm.pr.sq[w], sm.pr.acc[w],
-                           sm.pr.accb[w], sm.pr.acc1[w], sm.pr.accb1[w], tab, e);
+      n3_tile<II, RF, EFP, PBC>(p, ps, q, 1, sm.nw[w], tab, e);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) goto done;
     for (int it = blockIdx.x; it < nitem; it += G) {
       const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;

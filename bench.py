@@ -6,9 +6,13 @@ Workload (the nanopore system with grid maps): 120x120x180 maps at 1 A
 repulsion slab with a 10 A pore, repwalls layers), ~2000 K+/Cl- ions with
 Coulomb/cdie 80 + LJ + SRPMF pairs, four GCMC buffers (1 M) at both ends.
 One bench step = one simul1 cycle: GRAND with 4 attempts, then 10 BD steps
-(ENERGY with forces + dynamics0).  ENERGY and the BD update in FP32
-(float-float positions, compensated force sums, FP64 energy totals); GCMC ΔE
-in FP64.  Synthetic inputs (the reference ships no maps or decks).
+(ENERGY forces + dynamics0).  GPU arm: pair laws and the BD update in FP32
+(float-float positions, compensated force sums); the GCMC acceptance ΔE in
+float-float on the FP32 pipe (about 48 bits; the FP64 formula where float's
+range does not hold), not FP64.  The CPU arm is FP64 throughout.  Energy
+totals are not formed in the timed BD steps (forces only), as simul1 forms
+them only at its print steps.  Synthetic inputs (the reference ships no maps
+or decks).
 
 The line also carries "batched": 256 bulk KCl replicas of 200-8000 ions
 (1 M, cube boxes, the same maps) advanced by the replica-batch engine, timed
@@ -68,9 +72,17 @@ def config_dict():
                         "rfpar), K+/Cl- Coulomb+LJ+SRPMF, 4 GCMC buffers",
             "step": f"one cycle = GRAND({NGCMC} attempts) + {NBD} BD steps",
             "nions": NIONS, "grid": [120, 120, 180], "ngcmc": NGCMC, "nbd": NBD,
-            "pairs": "FP32 arithmetic, compensated FP32 force sums, FP64 energy "
-                     "totals; no cutoff (all pairs)",
+            "pairs": "all pairs (no cutoff); arithmetic per arm under 'precision'",
+            "energy_totals": "not formed in the timed BD steps (forces only)",
             "l2": "flushed between timed steps (256 MB write outside the events)"}
+
+
+PRECISION_GPU = {"pairs": "FP32 arithmetic, float-float positions, compensated FP32 "
+                          "force sums",
+                 "gcmc_dE": "float-float on the FP32 pipe (~2^-47 per operation); "
+                            "FP64 formula where float's range does not hold",
+                 "energy_totals": "FP64 sums of FP32 block partials"}
+PRECISION_CPU = {"pairs": "FP64", "gcmc_dE": "FP64", "energy_totals": "FP64"}
 
 
 # ---------------------------------------------------------------------------
@@ -308,14 +320,15 @@ def profile_traffic(kernel: str):
 
 def oracle_baseline(steps_budget_s: float, nthreads: int | None = None):
     """The CPU restatement (OpenMP build) on the same workload for a bounded
-    sample: whole cycles until the time budget is spent."""
+    sample: whole cycles until the time budget is spent; nthreads: OpenMP
+    threads (default: all the host's)."""
     from oracle import oracle
-    if nthreads:
-        os.environ["OMP_NUM_THREADS"] = str(nthreads)
+    lib = oracle.load(omp=True)
+    lib.bromoc_ref_set_threads(int(nthreads or os.cpu_count() or 1))
     spec = workload(0, precision=abi.FP64)
     eng = oracle.create(23000, omp=True)
     spec.push(eng)
-    cores = oracle.load(omp=True).bromoc_ref_threads()
+    cores = lib.bromoc_ref_threads()
     done_ps, cyc, t0 = 0, 0, time.perf_counter()
     while True:
         cyc += 1
@@ -326,10 +339,95 @@ def oracle_baseline(steps_budget_s: float, nthreads: int | None = None):
         if time.perf_counter() - t0 >= steps_budget_s:
             break
     dt = time.perf_counter() - t0
+    lib.bromoc_ref_set_threads(int(os.cpu_count() or 1))
     return {"value": done_ps / dt, "unit": "particle-steps/s", "cores": cores,
             "kind": "port",
             "sample": f"{cyc} cycles ({cyc * NBD} BD steps, {cyc * NGCMC} GCMC "
                       f"attempts) of the same workload, FP64, {dt:.1f} s"}
+
+
+def _force_errs(fg, fo):
+    d = np.linalg.norm(fg - fo, axis=1)
+    n = np.linalg.norm(fo, axis=1)
+    floor = max(float(np.sqrt(np.mean(n * n))), 1e-300)
+    return (float(np.linalg.norm(fg - fo) / max(np.linalg.norm(fo), 1e-300)),
+            float((d / np.maximum(n, floor)).max()))
+
+
+def _energy_err(tg, to):
+    scale = max(1.0, sum(abs(v) for k, v in to.items() if k != "ener"))
+    return float(max(abs(tg[k] - to[k]) for k in to) / scale)
+
+
+def oracle_checks(sh, batch_parts):
+    """The FP64 oracle as the checker of each timed form, on the timed
+    workloads' own inputs (untimed):
+      plain   : ENERGY of the nanopore workload, FP32 GPU against the oracle;
+      grand   : four GRAND(4) calls from the workload's state: the float-float
+                ΔE against the oracle's FP64 ΔE, and whether every counter
+                and particle type agrees;
+      batched : three replicas of the batch (smallest, median, largest).
+    Force errors: ||dF|| / ||F|| and the worst particle against
+    max(|F_i|, RMS |F|); energy: the worst term relative to the sum of the
+    terms' magnitudes."""
+    from bromoc_gb300 import _lib
+    from bromoc_gb300.batch import Batch
+    from oracle import oracle
+    out = {}
+    spec = workload(0, precision=abi.FP32)
+    g = _lib.create(23000, abi.FP32, sh)
+    o = oracle.create(23000)
+    spec.push(g)
+    spec.push(o)
+    tg, fg, _ = g.energy(abi.M_ALL, forces=True)
+    to, fo, _ = o.energy(abi.M_ALL, forces=True)
+    fgl, fwo = _force_errs(fg, fo)
+    out["plain"] = {"force_rel_err": fgl, "force_worst_particle": fwo,
+                    "energy_rel_err": _energy_err(tg, to), "ions": len(fo)}
+    derr = 0.0
+    for cyc in range(1, 5):
+        dg, do = g.grand(NGCMC, SEED, cyc), o.grand(NGCMC, SEED, cyc)
+        derr = max(derr, abs(dg - do) / max(1.0, abs(do)))
+    same = all((a == b).all() for a, b in zip(g.get_buffers(), o.get_buffers()))
+    same = same and bool((g.get_particles()[3] == o.get_particles()[3]).all())
+    out["grand"] = {"dE_rel_err": derr, "counters_equal": same, "calls": 4}
+    del g, o
+    counts, edges, parts = batch_parts
+    pick = [int(np.argmin(counts)), int(np.argsort(counts)[len(counts) // 2]),
+            int(np.argmax(counts))]
+    proto_spec = synth.pore(seed=3, nions=NIONS, maps=synth.pore_maps(seed=102),
+                            precision=abi.FP32, buffers=False)
+    proto = _lib.create(NIONS + 64, abi.FP32, sh)
+    proto_spec.push(proto)
+    sub = [int(counts[r]) for r in pick]
+    b = Batch(proto, sub)
+    reps = []
+    for r in pick:
+        s = synth.pore(seed=3, nions=NIONS, maps=synth.pore_maps(seed=102),
+                       precision=abi.FP32, buffers=False)
+        s.lx = s.ly = s.lz = float(edges[r])
+        x, y, z, t = parts[r]
+        s.x, s.y, s.z, s.typei = x, y, z, t
+        reps.append(s)
+    b.set_systems([s.system_struct() for s in reps])
+    for k, s in enumerate(reps):
+        b.set_particles(k, s.x, s.y, s.z, s.typei)
+    et, f = b.energy(abi.M_ALL, forces=True)
+    worst = {"force_rel_err": 0.0, "force_worst_particle": 0.0, "energy_rel_err": 0.0}
+    for k, s in enumerate(reps):
+        o = oracle.create(len(s.x) + 16)
+        s.push(o)
+        to, fo, _ = o.energy(abi.M_ALL, forces=True)
+        off = b.offset(k)
+        fgl, fwo = _force_errs(f[off:off + len(s.x)], fo)
+        tb = {kk: et[k, i] for i, kk in enumerate(abi.TERM_NAMES)}
+        worst["force_rel_err"] = max(worst["force_rel_err"], fgl)
+        worst["force_worst_particle"] = max(worst["force_worst_particle"], fwo)
+        worst["energy_rel_err"] = max(worst["energy_rel_err"], _energy_err(tb, to))
+    worst["replicas"] = sub
+    out["batched"] = worst
+    b.close()
+    return out
 
 
 # ---------------------------------------------------------------------------
@@ -362,6 +460,7 @@ def run_reference(args, rank, world):
             "ms_per_step": 1e3 * dt / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f64",
             "data": "synthetic", "config": config_dict(), "impl": "reference",
+            "precision": PRECISION_CPU,
             "cpu_baseline": {"value": v, "unit": "particle-steps/s",
                              "cores": cores, "kind": "port",
                              "sample": f"{args.steps} full cycles of the workload "
@@ -386,18 +485,6 @@ def run_gpu(args, rank, world, local_rank):
     stream = torch.cuda.Stream()
     torch.cuda.set_stream(stream)
     sh = stream.cuda_stream
-
-    # accuracy of the FP32 pair path against the FP64 path (validated
-    # against the FP64 oracle by the parity tests) on this workload
-    spec64 = workload(rank, precision=abi.FP64)
-    g64 = _lib.create(23000, abi.FP64, sh)
-    spec64.push(g64)
-    _, f64, _ = g64.energy(abi.M_ALL, forces=True)
-    g32a = _lib.create(23000, abi.FP32, sh)
-    spec64.push(g32a)
-    _, f32, _ = g32a.energy(abi.M_ALL, forces=True)
-    force_rel = float(np.linalg.norm(f32 - f64) / np.linalg.norm(f64))
-    del g64, g32a
 
     spec = workload(rank, precision=abi.FP32)
     eng = _lib.create(23000, abi.FP32, sh)
@@ -563,20 +650,26 @@ def run_gpu(args, rank, world, local_rank):
     scaling_pairs = pair_scaling(sh, peak_fp32)
     batched = batch_measure(sh, flush)
     adjoint = adjoint_measure(sh)
-    cpu = oracle_baseline(float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15")))
+    # the oracle leg: CPU baselines, then the oracle as the checker
+    budget = float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15"))
+    cpu = oracle_baseline(budget)
+    cpu_mono = oracle_baseline(max(1.0, budget / 2), nthreads=1)
+    checks = oracle_checks(sh, synth.batch_replicas(nrep=BATCH_NREP))
     clocks = clk.summary()
     line = {"metric": METRIC, "value": value, "unit": "particle-steps/s",
             "n_gpus": world, "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": tmax / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic", "config": config_dict(),
-            "force_rel_err_fp32_vs_fp64": force_rel,
+            "precision": PRECISION_GPU,
+            "oracle_error": checks,
             "roofline": roof,
             "kernel_ms": {k: {"total_ms": v[0], "launches": v[1],
                               "share": v[0] / tot_k} for k, v in kt.items()},
             "kernel_ms_unfused": {k: {"total_ms": v[0], "launches": v[1]}
                                   for k, v in kt_split.items()},
             "cpu_baseline": cpu,
+            "cpu_baseline_mono": cpu_mono,
             "e2e": {"value": e2e_val, "unit": "particle-steps/s",
                     "h2d_bytes_per_step": h2d // e2e_steps,
                     "d2h_bytes_per_step": d2h // e2e_steps,

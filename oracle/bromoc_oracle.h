@@ -13,6 +13,8 @@ int bromoc_ref_create(int32_t capacity, bromoc_ref **out);
 int bromoc_ref_destroy(bromoc_ref *r);
 const char *bromoc_ref_last_error(const bromoc_ref *r);
 int bromoc_ref_threads(void);
+/* OpenMP threads of the timed build (no effect on the sequential one). */
+int bromoc_ref_set_threads(int32_t n);
 int bromoc_ref_set_system(bromoc_ref *r, const bromoc_system *sys);
 int bromoc_ref_set_types(bromoc_ref *r, const bromoc_types *t);
 int bromoc_ref_set_pairs(bromoc_ref *r, const bromoc_pairs *p);

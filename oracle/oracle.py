@@ -33,6 +33,8 @@ def load(omp: bool = False) -> C.CDLL:
         abi.declare(lib, PREFIX)
         lib.bromoc_ref_create.argtypes = [C.c_int32, C.POINTER(C.c_void_p)]
         lib.bromoc_ref_threads.restype = C.c_int
+        lib.bromoc_ref_set_threads.argtypes = [C.c_int32]
+        lib.bromoc_ref_set_threads.restype = C.c_int
         lib.bromoc_ref_philox.argtypes = [C.POINTER(C.c_uint32)] * 3
         lib.bromoc_ref_philox.restype = None
         lib.bromoc_ref_bd_gauss.argtypes = [C.c_uint64, C.c_uint64, C.c_uint32,

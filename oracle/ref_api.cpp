@@ -56,6 +56,16 @@ int bromoc_ref_threads(void) {
 #endif
 }
 
+int bromoc_ref_set_threads(int32_t n) {
+#ifdef _OPENMP
+  if (n < 1) return BROMOC_E_ARG;
+  omp_set_num_threads(n);
+#else
+  (void)n;
+#endif
+  return BROMOC_OK;
+}
+
 int bromoc_ref_set_system(bromoc_ref *r, const bromoc_system *q) {
   if (!r || !q) return fail(r, "set_system: null");
   State &s = r->s;

@@ -10,13 +10,14 @@ namespace bgpu {
 
 constexpr int kWaitSpins = 1 << 23;  // ~0.5-1 s of polling at most
 
-// Thread 0 of a block: poll until *ctr >= target (acquire ordering).
+// Thread 0 of a block: poll until *ctr >= target (acquire ordering), at
+// most `limit` polls.
 __device__ __forceinline__ bool wait_at_least(unsigned *ctr, unsigned target, DevState *st,
-                                              bool sleep = true) {
+                                              bool sleep = true, int limit = kWaitSpins) {
   cuda::atomic_ref<unsigned, cuda::thread_scope_device> a(*ctr);
   volatile int *err = &st->err;
   for (int spin = 0; a.load(cuda::memory_order_acquire) < target; ++spin) {
-    if (spin > kWaitSpins || ((spin & 1023) == 1023 && (*err & kErrBarrier))) {
+    if (spin > limit || ((spin & 1023) == 1023 && (*err & kErrBarrier))) {
       atomicOr(&st->err, kErrBarrier);
       return false;
     }

@@ -12,6 +12,7 @@
 
 #include "../../include/bromoc_gpu.h"
 #include "ffmath.cuh"
+#include "gridsync.cuh"
 
 namespace {
 
@@ -56,7 +57,43 @@ __global__ void __launch_bounds__(256) k_fma_peak(float *out, int iters,
   if (s == 1234.5f) out[blockIdx.x * blockDim.x + threadIdx.x] = s;
 }
 
+// Bounded-wait self-test: block 0 waits (the grid barrier's own wait, at
+// most `spins` polls) for an arrival on *ctr; block 1 makes it only when
+// `arrive` is set.  Without it the wait runs out, records kErrBarrier in
+// st->err and the kernel returns.  An ordinary launch of two blocks: block 1
+// needs nothing from block 0, so both end either way.
+__global__ void k_wait_selftest(unsigned *ctr, bgpu::DevState *st, int spins, int arrive) {
+  using namespace bgpu;
+  if (threadIdx.x != 0) return;
+  if (blockIdx.x == 1) {
+    if (arrive) release_add(ctr, 1u);
+    return;
+  }
+  wait_at_least(ctr, 1u, st, true, spins);
+}
+
 }  // namespace
+
+extern "C" int bromoc_gpu_wait_selftest(int32_t spins, int32_t arrive, int32_t *err_word) {
+  if (!err_word || spins < 1) return BROMOC_E_ARG;
+  struct Buf {
+    unsigned ctr;
+    bgpu::DevState st;
+  } *d = nullptr;
+  if (cudaMalloc(&d, sizeof(Buf)) != cudaSuccess) return BROMOC_E_NOMEM;
+  int rc = BROMOC_OK;
+  if (cudaMemset(d, 0, sizeof(Buf)) != cudaSuccess) rc = BROMOC_E_CUDA;
+  if (!rc) {
+    k_wait_selftest<<<2, 32>>>(&d->ctr, &d->st, spins, arrive ? 1 : 0);
+    int err = 0;
+    if (cudaGetLastError() != cudaSuccess ||
+        cudaMemcpy(&err, &d->st.err, sizeof(int), cudaMemcpyDeviceToHost) != cudaSuccess)
+      rc = BROMOC_E_CUDA;
+    *err_word = err;
+  }
+  cudaFree(d);
+  return rc;
+}
 
 extern "C" int bromoc_gpu_fp32_peak(void *stream, double *tflops) {
   if (!tflops) return BROMOC_E_ARG;

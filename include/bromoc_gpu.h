@@ -76,7 +76,10 @@ enum { BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2 };
 /* FP64 mirrors the reference's -fdefault-real-8 build.  FP32 runs ENERGY and
  * the BD update in single precision: positions as float-float pairs, pair
  * laws and map gathers in FP32, compensated force sums, energy totals
- * accumulated in FP64 across blocks.  GCMC (INTERACT, GRAND) stays FP64. */
+ * accumulated in FP64 across blocks.  INTERACT stays FP64.  GRAND evaluates
+ * its ΔE and acceptance in float-float arithmetic on the FP32 pipe (about
+ * 48 bits), with the FP64 law for pairs closer than 0.1 A and the FP64
+ * acceptance formula where an exponent leaves float's range. */
 enum { BROMOC_FP64 = 0, BROMOC_FP32 = 1 };
 
 /* BD update variants: dynamics0 (uniform D), dynamics1 (z-switch D,
@@ -354,6 +357,13 @@ int bromoc_gpu_set_periodic(bromoc_ctx *ctx, int32_t on, double rcut);
  * on (synchronises the context's stream) */
 int bromoc_gpu_kernel_time(bromoc_ctx *ctx, int32_t which, double *total_ms,
                            int64_t *launches);
+/* Self-test of the bounded waits of the cooperative kernels (no counterpart
+ * in the reference): one block waits, through the grid barrier's own wait
+ * limited to `spins` polls, for an arrival that a second block makes only
+ * when `arrive` is nonzero.  *err_word receives the device error word: 16
+ * (the barrier flag) when the wait ran out, 0 when the arrival came.  The
+ * kernel returns either way; synchronous, on the current device. */
+int bromoc_gpu_wait_selftest(int32_t spins, int32_t arrive, int32_t *err_word);
 /* Measured FP32 FMA throughput of the current device (TFLOP/s), the
  * denominator of the pair kernels' roofline. */
 int bromoc_gpu_fp32_peak(void *stream, double *tflops);

@@ -188,11 +188,14 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
     launches = b.launch_count() - l0
     nions = int(counts.sum())
     value = nions * steps / (tb * 1e-3)
+    tw, tn, tms = b.tuning()
+    graph_calls = b.graph_launches()
     b.close()
     # plain path, replica by replica
     g = _lib.create(int(counts.max()) + 64, abi.FP32, sh)
     spec.push(g)
     tp = 0.0
+    tp_rep = np.zeros(len(parts))
     for r, (x, y, z, t) in enumerate(parts):
         g.call("set_system", C.byref(systems[r]))
         g.set_particles(x, y, z, t)
@@ -204,9 +207,41 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
         g.bd_steps(plain_steps, int(seeds[r]), 1, energies=False)
         e.record(stream)
         torch.cuda.synchronize()
-        tp += a.elapsed_time(e)
+        tp_rep[r] = a.elapsed_time(e)
+        tp += tp_rep[r]
     plain = nions * plain_steps / (tp * 1e-3)
-    del g, proto
+    del g
+    # per size bucket: the bucket's replicas as a batch of their own against
+    # the same replicas on the plain path (times above)
+    buckets = []
+    for k, (lo, hi) in enumerate(((0, 999), (1000, 4000), (4001, 1 << 30))):
+        sel = [r for r in range(len(counts)) if lo <= counts[r] <= hi]
+        if not sel:
+            continue
+        sb = Batch(proto, [int(counts[r]) for r in sel])
+        sb.set_systems([systems[r] for r in sel])
+        for j, r in enumerate(sel):
+            sb.set_particles(j, *parts[r])
+        sseeds = seeds[sel]
+        sb.bd_steps(warm, sseeds, 0)
+        torch.cuda.synchronize()
+        ts = 0.0
+        for kk in range(steps):
+            flush.zero_()
+            a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            a.record(stream)
+            sb.bd_steps(1, sseeds, warm + kk)
+            e.record(stream)
+            torch.cuda.synchronize()
+            ts += a.elapsed_time(e)
+        nb_ions = int(counts[sel].sum())
+        bv = nb_ions * steps / (ts * 1e-3)
+        pv = nb_ions * plain_steps / (tp_rep[sel].sum() * 1e-3)
+        buckets.append({"ions_range": [lo, min(hi, 8000)], "replicas": len(sel),
+                        "ions": nb_ions, "batch": bv, "plain_per_replica": pv,
+                        "speedup": bv / pv, "pair_warps_chosen": int(sb.tuning()[0][k])})
+        sb.close()
+    del proto
     return {"workload": f"{BATCH_NREP} bulk KCl replicas, N uniform in [200, 8000] "
                         f"({nions} ions), 1 M, cube boxes, shared 120x120x180 maps, "
                         "ENERGY (Coulomb+LJ+SRPMF, fields, RFPAR) + dynamics0, FP32",
@@ -214,7 +249,16 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
             "steps": steps, "gpu_launches": launches,
             "plain_per_replica": {"value": plain, "ms_per_step": tp / plain_steps,
                                   "steps": plain_steps},
-            "speedup_vs_plain": value / plain}
+            "speedup_vs_plain": value / plain,
+            "graph": {"calls_replayed": graph_calls,
+                      "note": "each bd_steps call: one CUDA-graph launch (seed and step "
+                              "uploads, then per step the field pass and, per size bucket, "
+                              "the pair and assembly launches)"},
+            "autotuner": {"buckets": ["<1000", "1000-4000", ">4000"],
+                          "pair_warps_per_block": [int(v) for v in tw],
+                          "tile_pairs": [int(v) for v in tn],
+                          "pair_pass_ms_by_warps_2_4_8": [[float(x) for x in row] for row in tms]},
+            "per_bucket": buckets}
 
 
 def pair_scaling(sh, peak_fp32, sizes=(2000, 4000, 8000), reps=10):
@@ -242,6 +286,52 @@ def pair_scaling(sh, peak_fp32, sizes=(2000, 4000, 8000), reps=10):
         a = (PAIR_FLOP + RF_FLOP) * pairs / t / 1e12
         out.append({"ions": n_ion, "launch_us": t * 1e6, "achieved_tflops": a,
                     "frac": a / peak_fp32})
+        del g
+    return out
+
+
+C1_STEPS = 2000
+
+
+def c1_measure(sh, steps=C1_STEPS):
+    """The bulk configuration: 130 K+ and 130 Cl- in a 60 A cube, FP64,
+    dt 0.02 ps; reference semantics (hard walls, all pairs) and the
+    extension mode (periodic, 20 A cutoff).  GPU: `steps` BD steps per call
+    (ENERGY forces + dynamics0), CUDA events on the shared stream after
+    warm-up.  CPU: the oracle restatement, one thread, a bounded sample of
+    the same steps."""
+    import torch
+    from bromoc_gb300 import _lib
+    from oracle import oracle
+    out = {"workload": "bulk KCl: 130 K+ / 130 Cl- (1 M), 60 A cube, FP64, dt 0.02 ps"}
+    stream = torch.cuda.current_stream()
+    for mode, rc in (("hard_walls", None), ("periodic_rc20", 20.0)):
+        spec = synth.bulk_kcl(seed=SEED, n_per=130, L=60.0, srpmf=True, precision=abi.FP64,
+                              periodic_rcut=rc)
+        g = _lib.create(300, abi.FP64, sh)
+        spec.push(g)
+        g.bd_steps(50, SEED, 0, energies=False)
+        a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        torch.cuda.synchronize()
+        a.record(stream)
+        g.bd_steps(steps, SEED, 50, energies=False)
+        e.record(stream)
+        torch.cuda.synchronize()
+        ms = a.elapsed_time(e)
+        lib = oracle.load(omp=True)
+        lib.bromoc_ref_set_threads(1)
+        o = oracle.create(300, omp=True)
+        spec.push(o)
+        ncpu, t0 = 0, time.perf_counter()
+        while time.perf_counter() - t0 < 2.0:
+            o.bd_steps(20, SEED, ncpu, energies=False)
+            ncpu += 20
+        dt = time.perf_counter() - t0
+        lib.bromoc_ref_set_threads(int(os.cpu_count() or 1))
+        out[mode] = {"value": 260 * steps / (ms * 1e-3), "unit": "particle-steps/s",
+                     "ms_per_bd_step": ms / steps, "steps": steps,
+                     "cpu_one_thread": {"value": 260 * ncpu / dt, "steps": ncpu,
+                                        "kind": "port"}}
         del g
     return out
 
@@ -276,6 +366,7 @@ def adjoint_measure(sh):
     nbins, r0, dr, sig = 150, 0.05, 0.1, 0.1
     rb = r0 + dr * np.arange(nbins)
     loss = RdfLoss(2, [ADJ_N // 2] * 2, L ** 3, ADJ_STEPS, rb, np.ones((3, nbins)))
+    fd = adjoint_fd_check(sh, spec, loss, (nbins, r0, dr, sig))
     stream = torch.cuda.current_stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     torch.cuda.synchronize()
@@ -297,7 +388,61 @@ def adjoint_measure(sh):
             "value": ADJ_N * ADJ_STEPS / ((t_f + t_b) * 1e-3),
             "unit": "particle-steps/s (forward + adjoint)",
             "loss": value,
-            "knot_grad_norm": float(np.sqrt(sum(np.sum(g * g) for g in grads.values())))}
+            "knot_grad_norm": float(np.sqrt(sum(np.sum(g * g) for g in grads.values()))),
+            "fd_check": fd}
+
+
+def adjoint_fd_check(sh, spec, loss, hist_args, h=1e-4):
+    """The C5 segment's knot gradients against central differences of the
+    same frozen-noise loss, untimed: for the K-K and K-Cl knot the loss
+    feels most, the FP64 adjoint, the FP32 adjoint, and the difference
+    quotient with h = 1e-4 kcal/mol of FP64 forward runs."""
+    import copy
+    from bromoc_gb300 import _lib
+    from bromoc_gb300.adjoint import Adjoint, knot_gradient, knot_jacobians
+    nbins, r0, dr, sig = hist_args
+    grads, runs = {}, {}
+    for prec in (abi.FP64, abi.FP32):
+        s = copy.copy(spec)
+        s.efpot_knots = dict(spec.efpot_knots)
+        s.precision = prec
+        proto = _lib.create(ADJ_N + 64, prec, sh)
+        s.push(proto)
+        adj = Adjoint(proto, ADJ_N, prec)
+
+        def run(s=s, proto=proto, adj=adj):
+            s.push(proto)
+            adj.set_particles(s.x, s.y, s.z, s.typei)
+            return adj.forward(ADJ_STEPS, ADJ_CKPT, SEED, 0, nbins, r0, dr, sig, 3)
+
+        _, dl = loss.loss_grad(run())
+        pt = s.pair_tables()
+        g_ep, g_sc = adj.backward(dl, int(pt["cnt"]), int(pt["ntc"]))
+        grads[prec] = knot_gradient(knot_jacobians(s, proto.efpot_from_knots), g_ep, g_sc)
+        runs[prec] = (s, run, adj, proto)
+    s64, run64, _, _ = runs[abi.FP64]
+    out = []
+    for key in (("K", "K"), ("K", "Cl")):
+        g64 = grads[abi.FP64][key]
+        m = int(np.argmax(np.abs(g64)))
+        r, u0 = s64.efpot_knots[key]
+        u0 = np.asarray(u0, float)
+        vals = []
+        for sgn in (1, -1):
+            u = u0.copy()
+            u[m] += sgn * h
+            s64.efpot_knots[key] = (r, u)
+            vals.append(loss.loss_grad(run64())[0])
+        s64.efpot_knots[key] = (r, u0)
+        fdv = (vals[0] - vals[1]) / (2 * h)
+        g32 = float(grads[abi.FP32][key][m])
+        out.append({"pair": "-".join(key), "knot_r": float(r[m]), "adjoint_fp64": float(g64[m]),
+                    "adjoint_fp32": g32, "central_difference": fdv, "h": h,
+                    "rel_err_fp64_vs_fd": abs(float(g64[m]) - fdv) / abs(fdv),
+                    "rel_err_fp32_vs_fd": abs(g32 - fdv) / abs(fdv)})
+    for _, _, adj, _ in runs.values():
+        adj.close()
+    return out
 
 
 def measured_peaks():
@@ -650,6 +795,7 @@ def run_gpu(args, rank, world, local_rank):
     scaling_pairs = pair_scaling(sh, peak_fp32)
     batched = batch_measure(sh, flush)
     adjoint = adjoint_measure(sh)
+    bulk_c1 = c1_measure(sh)
     # the oracle leg: CPU baselines, then the oracle as the checker
     budget = float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15"))
     cpu = oracle_baseline(budget)
@@ -679,6 +825,7 @@ def run_gpu(args, rank, world, local_rank):
             "pair_kernel_scaling": scaling_pairs,
             "batched": batched,
             "adjoint": adjoint,
+            "bulk_c1": bulk_c1,
             "wall_s": wall, "clocks": clocks}
     print(json.dumps(line), flush=True)
     if dist:

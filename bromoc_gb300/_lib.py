@@ -80,6 +80,12 @@ def load() -> C.CDLL:
         lib.bromoc_batch_last_error.restype = C.c_char_p
         lib.bromoc_batch_launch_count.argtypes = [vp]
         lib.bromoc_batch_launch_count.restype = C.c_int64
+        lib.bromoc_batch_graph_launches.argtypes = [vp]
+        lib.bromoc_batch_graph_launches.restype = C.c_int64
+        lib.bromoc_batch_set_graph.argtypes = [vp, C.c_int32]
+        lib.bromoc_batch_set_graph.restype = C.c_int
+        lib.bromoc_batch_tuning.argtypes = [vp, i32, i32, d]
+        lib.bromoc_batch_tuning.restype = C.c_int
         _lib = lib
     return _lib
 

@@ -137,6 +137,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         "bd_steps": [vp, C.c_uint32, C.c_int32, C.c_int32, C.c_uint64,
                      C.c_uint64, _d],
         "grand": [vp, C.c_uint32, C.c_int32, C.c_uint64, C.c_uint64, _d],
+        "metropolis": [vp, C.c_uint32, C.c_int32, C.c_double, C.c_uint64, C.c_uint64, _i,
+                       _d],
         "get_buffers": [vp, _i, _i, _i, _i],
         "get_countions": [vp, _i, _i],
         "get_dids": [vp, _d],
@@ -168,8 +170,20 @@ _DEPENDENTS = weakref.WeakSet()
 _SHUTDOWN = False
 
 
-def register_dependent(obj) -> None:
+def register_dependent(obj, owner=None) -> None:
+    """obj borrows owner's context (its stream and tables).  The owner holds
+    it strongly and closes it before destroying the context: a garbage
+    collection may finalize the two in either order (and clears weak
+    references first), so the order cannot rest on weak references.  obj
+    removes itself from the owner when it closes (unregister_dependent)."""
     _DEPENDENTS.add(obj)
+    if owner is not None:
+        owner._dependents.add(obj)
+
+
+def unregister_dependent(obj, owner) -> None:
+    if owner is not None:
+        owner._dependents.discard(obj)
 
 
 def shutting_down() -> bool:
@@ -207,6 +221,7 @@ class Engine:
         self.nold = 0
         self.nbuffer = 0
         self.cntpts = 0
+        self._dependents = set()
         _LIVE.add(self)
 
     def _fn(self, name):
@@ -220,6 +235,8 @@ class Engine:
 
     def close(self):
         if self.h:
+            for dep in list(getattr(self, "_dependents", ())):
+                dep.close()
             self._fn("destroy")(self.h)
             self.h = None
 
@@ -318,6 +335,14 @@ class Engine:
         self._chk(self._fn("grand")(self.h, terms, ngcmc, seed, cycle,
                                     C.byref(d) if dener else None), "grand")
         return d.value if dener else None
+
+    def metropolis(self, nmcm, mcmax, seed, cycle, terms=M_ALL):
+        """METROPOLIS: nmcm moves -> (accepted moves, summed energy change)."""
+        na = C.c_int32(0)
+        d = C.c_double(0.0)
+        self._chk(self._fn("metropolis")(self.h, terms, nmcm, mcmax, seed, cycle,
+                                         C.byref(na), C.byref(d)), "metropolis")
+        return na.value, d.value
 
     def get_buffers(self):
         nb = self.nbuffer

@@ -30,7 +30,7 @@ class Adjoint:
             raise abi.BromocError(rc, self.lib.bromoc_gpu_last_error(proto.h).decode())
         self.h = h
         self.n = 0
-        abi.register_dependent(self)
+        abi.register_dependent(self, proto)
 
     def _chk(self, rc, what):
         if rc != abi.OK:
@@ -40,6 +40,7 @@ class Adjoint:
         if getattr(self, "h", None):
             self.lib.bromoc_adj_destroy(self.h)
             self.h = None
+            abi.unregister_dependent(self, self.proto)
 
     def __del__(self):
         if abi.shutting_down():

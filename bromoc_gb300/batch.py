@@ -22,7 +22,7 @@ class Batch:
         if rc != abi.OK:
             raise abi.BromocError(rc, self.lib.bromoc_gpu_last_error(proto.h).decode())
         self.h = h
-        abi.register_dependent(self)
+        abi.register_dependent(self, proto)
 
     def _chk(self, rc, what):
         if rc != abi.OK:
@@ -33,6 +33,7 @@ class Batch:
         if getattr(self, "h", None):
             self.lib.bromoc_batch_destroy(self.h)
             self.h = None
+            abi.unregister_dependent(self, self.proto)
 
     def __del__(self):
         if abi.shutting_down():
@@ -82,6 +83,28 @@ class Batch:
             self.h, terms, f.ctypes.data_as(dp) if f is not None else None,
             et.ctypes.data_as(dp)), "energy")
         return et, f
+
+    def set_graph(self, on: bool):
+        """Replay runs of BD steps from a captured CUDA graph (on, the
+        default) or launch them one by one; the trajectories agree."""
+        self._chk(self.lib.bromoc_batch_set_graph(self.h, int(on)), "set_graph")
+
+    def tuning(self):
+        """The autotuner's state per size bucket (< 1000, 1000-4000, > 4000
+        ions): chosen pair-kernel warps per block (0: not tuned or empty),
+        tile pairs, and the measured ms of a pair pass per candidate
+        (2, 4, 8 warps)."""
+        w = np.zeros(3, np.int32)
+        n = np.zeros(3, np.int32)
+        ms = np.zeros(9)
+        self._chk(self.lib.bromoc_batch_tuning(self.h, w.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               n.ctypes.data_as(C.POINTER(C.c_int32)),
+                                               ms.ctypes.data_as(C.POINTER(C.c_double))),
+                  "tuning")
+        return w, n, ms.reshape(3, 3)
+
+    def graph_launches(self):
+        return int(self.lib.bromoc_batch_graph_launches(self.h))
 
     def offset(self, r):
         return self.lib.bromoc_batch_offset(self.h, r)

@@ -383,6 +383,7 @@ using namespace bgpu;
 struct bromoc_adj {
   bromoc_ctx *proto = nullptr;
   cudaStream_t stream = nullptr;
+  int orphaned = 0;  // set when the prototype context is destroyed first
   int precision = BROMOC_FP32;
   std::string err;
   int cap = 0, n = 0, nt = 0, ntp = 0;
@@ -589,6 +590,7 @@ int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
   bromoc_adj *ad = new bromoc_adj;
   ad->proto = proto;
   ad->stream = s;
+  bromoc_ctx_attach(proto, &ad->orphaned);
   ad->precision = precision;
   ad->cap = capacity;
   ad->nt = pk->nion_t;
@@ -620,9 +622,13 @@ int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
 
 int bromoc_adj_destroy(bromoc_adj *ad) {
   if (!ad) return BROMOC_E_ARG;
-  if (ad->stream) cudaStreamSynchronize(ad->stream);
+  if (!ad->orphaned) {
+    if (ad->stream) cudaStreamSynchronize(ad->stream);
+    bromoc_ctx_detach(ad->proto, &ad->orphaned);
+  }
   for (void *p : ad->allocs) cudaFree(p);
   delete ad;
+  cudaGetLastError();  // leave no non-sticky error behind for the next call
   return BROMOC_OK;
 }
 
@@ -636,6 +642,7 @@ extern "C" {
 
 int bromoc_adj_set_particles(bromoc_adj *ad, int32_t n, const double *x, const double *y,
                              const double *z, const int32_t *typei) {
+  if (ad && ad->orphaned) return aset(ad, BROMOC_E_STATE, "the prototype context was destroyed");
   if (!ad || !x || !y || !z || !typei) return aset(ad, BROMOC_E_ARG, "set_particles: null");
   if (n < 2 || n > ad->cap)
     return aset(ad, BROMOC_E_CAPACITY, "set_particles: n = %d outside [2, %d]", n, ad->cap);
@@ -680,6 +687,7 @@ int bromoc_adj_set_particles(bromoc_adj *ad, int32_t n, const double *x, const d
 int bromoc_adj_forward(bromoc_adj *ad, int32_t nsteps, int32_t ckpt, uint64_t seed,
                        uint64_t step0, int32_t nbins, double r0, double dr, double sigma,
                        double *hist) {
+  if (ad && ad->orphaned) return aset(ad, BROMOC_E_STATE, "the prototype context was destroyed");
   if (!ad || !hist || nsteps < 1 || ckpt < 1 || nbins < 1 || !(dr > 0.0) || !(sigma > 0.0) ||
       r0 < 0.0)
     return aset(ad, BROMOC_E_ARG, "forward: bad arguments");
@@ -737,6 +745,7 @@ int bromoc_adj_forward(bromoc_adj *ad, int32_t nsteps, int32_t ckpt, uint64_t se
 }
 
 int bromoc_adj_backward(bromoc_adj *ad, const double *dl_dhist, double *g_ep, double *g_sc) {
+  if (ad && ad->orphaned) return aset(ad, BROMOC_E_STATE, "the prototype context was destroyed");
   if (!ad || !dl_dhist || !g_ep || !g_sc) return aset(ad, BROMOC_E_ARG, "backward: null");
   if (!ad->have_forward) return aset(ad, BROMOC_E_STATE, "backward: run forward first");
   KP p;
@@ -757,6 +766,7 @@ int bromoc_adj_backward(bromoc_adj *ad, const double *dl_dhist, double *g_ep, do
 
 // which = 0: the initial configuration, 1: the last forward run's final one
 int bromoc_adj_get_particles(bromoc_adj *ad, int32_t which, double *x, double *y, double *z) {
+  if (ad && ad->orphaned) return aset(ad, BROMOC_E_STATE, "the prototype context was destroyed");
   if (!ad || !x || !y || !z) return aset(ad, BROMOC_E_ARG, "get_particles: null");
   const int n = ad->n;
   std::vector<float4> h(n), l(n);

@@ -5,6 +5,7 @@
 // set_* calls corresponds to what the reference's deck interpreter leaves in
 // its Fortran modules; the particle arrays stay device-resident between
 // calls, and GCMC edits them in place on the device.
+#include <algorithm>
 #include <cmath>
 #include <cstdarg>
 #include <cstdio>
@@ -52,6 +53,9 @@ struct bromoc_ctx {
   int nslot_cap = 0;
   int ipart_slots = 0;
   int tp_tiles = 0;  // tiles the Newton-3 partial buffers hold
+  int cell_cap = 0;  // cells the cell-list arrays hold
+  McState *mc = nullptr;  // Metropolis chain record (device)
+  std::vector<int *> dependents;  // orphan flags of batches and adjoint engines
   double *d_dener = nullptr;
   // last energy plan (for dynamics())
   AssembleFlags last_fl{};
@@ -332,6 +336,46 @@ void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
   nchunk = (nsources + chunk - 1) / chunk;
 }
 
+// Cells of the FP32 extension mode's cell list: the most cubes of edge at
+// least rc (1 + 1e-4) along each box edge; false (no cell list) unless
+// every axis holds four or more, where the 27 neighbour cells are a strict
+// part of the box.
+bool cell_grid(KP &p) {
+  p.ncells = 0;
+  if (!p.periodic || !(p.rc2 > 0.0)) return false;
+  const double rc = std::sqrt(p.rc2) * (1.0 + 1e-4);
+  const double L[3] = {p.lx, p.ly, p.lz};
+  int n = 1;
+  for (int a = 0; a < 3; ++a) {
+    p.nc[a] = (int)std::floor(L[a] / rc);
+    if (p.nc[a] < 4) return false;
+    p.cinv[a] = (float)(p.nc[a] / L[a]);
+    n *= p.nc[a];
+  }
+  p.ncells = n;
+  return true;
+}
+
+int ensure_cells(bromoc_ctx *ctx) {
+  KP &p = ctx->kp;
+  int rc;
+  if (!p.cell_ion) {
+    if ((rc = dalloc(ctx, &p.cell_ion, (size_t)p.cap))) return rc;
+    if ((rc = dalloc(ctx, &p.ion_cell, (size_t)p.cap))) return rc;
+  }
+  if (p.ncells > ctx->cell_cap) {
+    CU(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx, p.cell_n);
+    dfree(ctx, p.cell_start);
+    p.cell_n = p.cell_start = nullptr;
+    ctx->cell_cap = 0;
+    if ((rc = dalloc(ctx, &p.cell_n, (size_t)p.ncells + 1))) return rc;
+    if ((rc = dalloc(ctx, &p.cell_start, (size_t)p.ncells + 1))) return rc;
+    ctx->cell_cap = p.ncells;
+  }
+  return BROMOC_OK;
+}
+
 int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
                 AssembleFlags &fl, bool timers = true) {
   KP &p = ctx->kp;
@@ -345,7 +389,18 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   fl.fp32_partials = plan.fp32;
   fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
   plan.ntile = p.ntile = 0;
-  if (plan.fp32 && nion > 0 && (nion + 31) / 32 <= kN3MaxTiles &&
+  plan.cells = false;
+  if (plan.fp32 && p.periodic && nion > 0 && pair_cfg32(p, plan.ntot_ub, mask).ntg > 0 &&
+      cell_grid(p)) {  // extension mode: the cell-list pair kernel
+    const int rc = ensure_cells(ctx);
+    if (rc) return rc;
+    plan.cells = true;
+    plan.nchunk_ii = p.nchunk_ii = 1;
+    plan.nchunk_rf = p.nchunk_rf = 0;
+    fl.ii = 1;
+    fl.ii_from = p.nsites + p.nfix;
+    fl.nchunk_ii = 1;
+  } else if (plan.fp32 && nion > 0 && (nion + 31) / 32 <= kN3MaxTiles &&
       pair_cfg32(p, plan.ntot_ub, mask).ntg > 0) {  // Newton-3 pair kernel
     const int T = (nion + 31) / 32;
     if (T > ctx->tp_tiles) {  // grow the tile-pair partials (rare)
@@ -366,7 +421,9 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
     fl.ntile = T;
     fl.rf_ab = pair_cfg32(p, plan.ntot_ub, mask).rf;
   } else if (plan.fp32 && p.periodic && pair_cfg32(p, plan.ntot_ub, mask).ntg > 0) {
-    return set_err(ctx, BROMOC_E_CAPACITY, "periodic mode: up to %d ions in FP32",
+    return set_err(ctx, BROMOC_E_CAPACITY,
+                   "periodic mode in FP32: more than %d ions need at least four cells of "
+                   "the cutoff along every box edge",
                    32 * kN3MaxTiles);
   } else if (plan.fp32) {  // one fused pair kernel (ion-ion + RFPAR cross)
     const PairCfg32 pc = pair_cfg32(p, plan.ntot_ub, mask);
@@ -398,6 +455,10 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
 }
 
 int check_ready(bromoc_ctx *ctx) {
+  // a non-sticky error of an earlier, unrelated runtime call would otherwise
+  // be reported by this call's launch checks (faults stay sticky and are
+  // still reported)
+  cudaGetLastError();
   if (!ctx->have_sys || !ctx->have_types || !ctx->have_pairs)
     return set_err(ctx, BROMOC_E_STATE,
                    "set_system, set_types and set_pairs are required");
@@ -479,6 +540,16 @@ int bromoc_ctx_prepare_f32(bromoc_ctx *ctx, const KP **kp, cudaStream_t *stream)
   return BROMOC_OK;
 }
 
+void bromoc_ctx_attach(bromoc_ctx *ctx, int *orphaned) {
+  if (ctx && orphaned) ctx->dependents.push_back(orphaned);
+}
+
+void bromoc_ctx_detach(bromoc_ctx *ctx, int *orphaned) {
+  if (!ctx) return;
+  auto &d = ctx->dependents;
+  d.erase(std::remove(d.begin(), d.end(), orphaned), d.end());
+}
+
 int bromoc_ctx_fail(bromoc_ctx *ctx, int code, const char *msg) {
   return set_err(ctx, code, "%s", msg);
 }
@@ -538,6 +609,7 @@ int bromoc_gpu_create(int32_t capacity, int32_t precision, void *stream,
 
 int bromoc_gpu_destroy(bromoc_ctx *ctx) {
   if (!ctx) return BROMOC_OK;
+  for (int *f : ctx->dependents) *f = 1;  // their stream and tables go now
   if (ctx->stream) cudaStreamSynchronize(ctx->stream);
   for (void *a : ctx->allocs)
     if (a) cudaFree(a);
@@ -1310,6 +1382,35 @@ int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj, d
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(dener, ctx->d_dener, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
+  return check_device_err(ctx);
+}
+
+int bromoc_gpu_metropolis(bromoc_ctx *ctx, uint32_t terms, int32_t nmcm, double mcmax,
+                          uint64_t seed, uint64_t cycle, int32_t *naccept,
+                          double *dener_sum) {
+  if (!ctx || nmcm < 0 || !(mcmax > 0.0)) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if ((rc = ensure_dbl(ctx))) return rc;
+  if ((rc = sync_ntot(ctx))) return rc;
+  KP &p = ctx->kp;
+  if (p.nfix > 0)
+    return set_err(ctx, BROMOC_E_STATE,
+                   "metropolis: systems with fixed ions are not supported (move.f90 draws "
+                   "the ion over ntot - nsites slots)");
+  const int ntot = ctx->ntot_known;
+  if (ntot - p.nsites < 1) return set_err(ctx, BROMOC_E_STATE, "metropolis: no mobile ion");
+  if (!ctx->mc && (rc = dalloc(ctx, &ctx->mc, 1))) return rc;
+  CU(cudaMemsetAsync(ctx->mc, 0, sizeof(McState), ctx->stream));
+  ctx->launches += launch_metropolis(p, ntot, terms, nmcm, mcmax, seed, cycle, ctx->mc,
+                                     ctx->stream);
+  CU(cudaGetLastError());
+  McState h{};
+  CU(cudaMemcpyAsync(&h, ctx->mc, sizeof h, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  if (naccept) *naccept = h.naccept;
+  if (dener_sum) *dener_sum = h.dener;
+  if (ctx->precision == BROMOC_FP32) ctx->ff_fresh = false;  // the FP64 arrays moved
   return check_device_err(ctx);
 }
 

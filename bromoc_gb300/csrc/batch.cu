@@ -1,6 +1,5 @@
 // Replica batches on the device (scope-table configuration C4): many
-// independent systems of uneven size advance together, three launches per
-// BD step for the whole batch.
+// independent systems of uneven size advance together.
 //
 //   k_batch_fields (fields.cu): the FP32 field terms of every live slot.
 //   k_batch_pairs: every tile pair of every replica, one warp each, through
@@ -11,6 +10,16 @@
 //                  assembly and dynamics0 move of the single-system path
 //                  (move32.cuh) with the replica's box and noise key, in
 //                  place (the pair launch has finished reading positions).
+//
+// Replicas fall into size buckets (fewer than 1000 ions, up to 4000, more);
+// each bucket's tile pairs and tiles are launched separately, with the pair
+// kernel's warps per block chosen for that bucket by an autotuner (timed
+// pair passes, which change no state, at the first BD step after the
+// replicas change).  A run of BD steps -- the upload of the seeds and of
+// the step index, then every step's launches -- is captured once into a
+// CUDA graph and replayed for later calls with the same step count: one
+// graph launch per call.  The kernels read the step index from device
+// memory, so one graph serves every step0.
 //
 // A replica's particles, partial sums and moves are exactly those of a
 // single context holding that replica (same summation order, noise drawn
@@ -33,23 +42,28 @@
 
 namespace bgpu {
 
-constexpr int kPairWarps = 4;   // tile pairs per block of k_batch_pairs
-constexpr int kAsmTileWarps = 16;  // as the single-system tile assembly
+constexpr int kAsmTileWarps = 16;  // as the single-system tile assembly (same sums)
+// replica size buckets: [0, 1000), [1000, 4000], above
+constexpr int kBuckets = 3;
+inline int size_bucket(int n) { return n < 1000 ? 0 : (n <= 4000 ? 1 : 2); }
+// the autotuner's candidates for the pair kernel's warps per block
+constexpr int kPairWarpChoices[3] = {2, 4, 8};
 
 // Energies of one tile pair: ecoul, elj, esrpmf, eefpot, RFPAR cross.
 constexpr int kRowTerms = 5;
 
-template <bool RF>
-__global__ void __launch_bounds__(32 * kPairWarps)
+// work / wpart: one bucket's stretch of the work list and its energy slots
+template <bool RF, int W>
+__global__ void __launch_bounds__(32 * W)
     k_batch_pairs(const __grid_constant__ KP p, const RepDev *rep, const int2 *work, int nwork,
                   float4 *tpf, float *tpb, float *wpart) {
-  __shared__ N3Warp<RF> nw[kPairWarps];
+  __shared__ N3Warp<RF> nw[W];
   __shared__ float4 tab[kIpqMax];
   const int nt = p.nion_t;
   for (int k = threadIdx.x; k < nt * ipq_stride(nt); k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int widx = blockIdx.x * kPairWarps + w;
+  const int widx = blockIdx.x * W + w;
   if (widx >= nwork) return;  // no block-wide barrier follows
   const int2 wk = work[widx];
   const RepDev &R = rep[wk.x];
@@ -71,11 +85,14 @@ __global__ void __launch_bounds__(32 * kPairWarps)
 // One block per (replica, tile): the tile assembly and move of the single
 // system path on the replica's slots; fout (if not moving): 3 doubles per
 // slot.
+// step: *step0 + k (the step index lives in device memory for graph replay)
 template <bool RF>
 __global__ void __launch_bounds__(32 * kAsmTileWarps, 2)
     k_batch_asm(const __grid_constant__ KP p, const RepDev *rep, const int2 *tiles,
-                const float4 *tpf, const float *tpb, int do_bd, uint64_t step, double *fout) {
+                const float4 *tpf, const float *tpb, int do_bd, const uint64_t *step0, int k,
+                double *fout) {
   __shared__ float part[kAsmTileWarps][10][32];
+  const uint64_t step = *step0 + (uint64_t)k;
   const int2 tk = tiles[blockIdx.x];
   const RepDev &R = rep[tk.x];
   const size_t o = R.off;
@@ -138,11 +155,24 @@ struct bromoc_batch {
   cudaStream_t stream = nullptr;
   std::string err;
   int nrep = 0, nslots = 0, nwork = 0, cur = 0;  // cur: always 0 (moves are in place)
+  // buckets: work items [wb[k], wb[k+1]) and tiles [tb[k], tb[k+1]) of bucket k
+  int wb[kBuckets + 1] = {}, tb[kBuckets + 1] = {};
+  int pair_warps[kBuckets] = {4, 4, 4};  // the autotuner's choice per bucket
+  float tune_ms[kBuckets][3] = {};       // its measured pair pass per candidate
+  bool tuned = false;
+  // graph of a run of BD steps: replayed while nsteps and rf match
+  bool use_graph = true;
+  cudaGraphExec_t gexec = nullptr;
+  int g_nsteps = -1, g_rf = -1, g_terms = -1;
+  long long g_launches = 0;      // kernels in the graph
+  long long graph_launches = 0;  // graph launches so far
+  uint64_t *step_pinned = nullptr, *d_step0 = nullptr;
   std::vector<int> cap, off, n;
   std::vector<RepDev> rep_h;   // host copy of the replica records
   std::vector<int> nwtype_h;   // [ntype+1] ion type -> combined type
   std::vector<double> cg_h;    // [ntype+1] charges
   bool have_sys = false;
+  int orphaned = 0;  // set when the prototype context is destroyed first
   // device
   RepDev *rep = nullptr;
   int *rep_of = nullptr;
@@ -195,17 +225,33 @@ void split(double v, float &h, float &l) {
   l = (float)(v - (double)h);
 }
 
+void drop_graph(bromoc_batch *b) {
+  if (b->gexec) cudaGraphExecDestroy(b->gexec);
+  b->gexec = nullptr;
+  b->g_nsteps = b->g_rf = -1;
+}
+
 // work items: every tile pair (replica, q) and every tile (replica, t) of the
-// live particles, replica by replica; w0, w1 bound each replica's tile pairs
+// live particles, bucket by bucket and replica by replica within a bucket;
+// w0, w1 bound each replica's tile pairs
 int rebuild_work(bromoc_batch *b) {
   std::vector<int2> items, tiles;
-  for (int r = 0; r < b->nrep; ++r) {
-    const int T = (b->n[r] + 31) / 32;
-    b->rep_h[r].w0 = (int)items.size();
-    for (int q = 0; q < n3_pairs(T); ++q) items.push_back(make_int2(r, q));
-    b->rep_h[r].w1 = (int)items.size();
-    for (int t = 0; t < T; ++t) tiles.push_back(make_int2(r, t));
+  for (int k = 0; k < kBuckets; ++k) {
+    b->wb[k] = (int)items.size();
+    b->tb[k] = (int)tiles.size();
+    for (int r = 0; r < b->nrep; ++r) {
+      if (size_bucket(b->n[r]) != k) continue;
+      const int T = (b->n[r] + 31) / 32;
+      b->rep_h[r].w0 = (int)items.size();
+      for (int q = 0; q < n3_pairs(T); ++q) items.push_back(make_int2(r, q));
+      b->rep_h[r].w1 = (int)items.size();
+      for (int t = 0; t < T; ++t) tiles.push_back(make_int2(r, t));
+    }
   }
+  b->wb[kBuckets] = (int)items.size();
+  b->tb[kBuckets] = (int)tiles.size();
+  b->tuned = false;
+  drop_graph(b);
   if ((int)items.size() > b->nwork) {
     if (b->work) cudaFree(b->work);
     if (b->wpart) cudaFree(b->wpart);
@@ -230,28 +276,99 @@ int rebuild_work(bromoc_batch *b) {
   return BROMOC_OK;
 }
 
-// The pair and assembly launches of one step (do_bd: move, else forces
-// into fout if given).
-void launch_pairs_asm(bromoc_batch *b, const KP &p, bool rf, int do_bd, uint64_t step,
+template <bool RF>
+void launch_pairs_w(int w, int nb, cudaStream_t s, const KP &p, const RepDev *rep,
+                    const int2 *work, int nwork, float4 *tpf, float *tpb, float *wpart) {
+  if (w == 2)
+    k_batch_pairs<RF, 2><<<nb, 64, 0, s>>>(p, rep, work, nwork, tpf, tpb, wpart);
+  else if (w == 8)
+    k_batch_pairs<RF, 8><<<nb, 256, 0, s>>>(p, rep, work, nwork, tpf, tpb, wpart);
+  else
+    k_batch_pairs<RF, 4><<<nb, 128, 0, s>>>(p, rep, work, nwork, tpf, tpb, wpart);
+}
+
+// The pair launch of bucket k with w warps per block.
+void launch_bucket_pairs(bromoc_batch *b, const KP &p, bool rf, int k, int w) {
+  const int n = b->wb[k + 1] - b->wb[k];
+  if (n <= 0) return;
+  const int nb = (n + w - 1) / w;
+  const int2 *work = b->work + b->wb[k];
+  float *wpart = b->wpart + (size_t)b->wb[k] * kRowTerms;
+  if (rf)
+    launch_pairs_w<true>(w, nb, b->stream, p, b->rep, work, n, b->tpf, b->tpb, wpart);
+  else
+    launch_pairs_w<false>(w, nb, b->stream, p, b->rep, work, n, b->tpf, b->tpb, wpart);
+  b->launches += 1;
+}
+
+// The pair and assembly launches of one step, bucket by bucket (do_bd:
+// move, else forces into fout if given); kstep: the step's offset from the
+// device-resident step index.
+void launch_pairs_asm(bromoc_batch *b, const KP &p, bool rf, int do_bd, int kstep,
                       double *fout) {
-  const int nb = (b->nwork + kPairWarps - 1) / kPairWarps;
-  if (nb > 0) {
+  for (int k = 0; k < kBuckets; ++k) launch_bucket_pairs(b, p, rf, k, b->pair_warps[k]);
+  for (int k = 0; k < kBuckets; ++k) {
+    const int nt = b->tb[k + 1] - b->tb[k];
+    if (nt <= 0) continue;
+    const int2 *tiles = b->tiles + b->tb[k];
     if (rf)
-      k_batch_pairs<true><<<nb, 32 * kPairWarps, 0, b->stream>>>(p, b->rep, b->work, b->nwork,
-                                                                 b->tpf, b->tpb, b->wpart);
+      k_batch_asm<true><<<nt, 32 * kAsmTileWarps, 0, b->stream>>>(
+          p, b->rep, tiles, b->tpf, b->tpb, do_bd, b->d_step0, kstep, fout);
     else
-      k_batch_pairs<false><<<nb, 32 * kPairWarps, 0, b->stream>>>(p, b->rep, b->work, b->nwork,
-                                                                  b->tpf, b->tpb, b->wpart);
+      k_batch_asm<false><<<nt, 32 * kAsmTileWarps, 0, b->stream>>>(
+          p, b->rep, tiles, b->tpf, b->tpb, do_bd, b->d_step0, kstep, fout);
     b->launches += 1;
   }
-  if (b->ntiles > 0) {
-    if (rf)
-      k_batch_asm<true><<<b->ntiles, 32 * kAsmTileWarps, 0, b->stream>>>(
-          p, b->rep, b->tiles, b->tpf, b->tpb, do_bd, step, fout);
-    else
-      k_batch_asm<false><<<b->ntiles, 32 * kAsmTileWarps, 0, b->stream>>>(
-          p, b->rep, b->tiles, b->tpf, b->tpb, do_bd, step, fout);
+}
+
+// The autotuner: per bucket, every candidate warps-per-block of the pair
+// kernel timed over three pair passes (after one untimed pass) with CUDA
+// events on the batch's stream; the fastest is kept.  A pair pass only
+// writes the partial buffers, which the next step rewrites, so tuning moves
+// no particle.
+int autotune(bromoc_batch *b, const KP &p, bool rf) {
+  cudaEvent_t e0, e1;
+  BCU(cudaEventCreate(&e0));
+  BCU(cudaEventCreate(&e1));
+  const long long l0 = b->launches;
+  for (int k = 0; k < kBuckets; ++k) {
+    if (b->wb[k + 1] == b->wb[k]) continue;
+    float best = 0.0f;
+    for (int c = 0; c < 3; ++c) {
+      const int w = kPairWarpChoices[c];
+      launch_bucket_pairs(b, p, rf, k, w);
+      cudaEventRecord(e0, b->stream);
+      for (int rep = 0; rep < 3; ++rep) launch_bucket_pairs(b, p, rf, k, w);
+      cudaEventRecord(e1, b->stream);
+      cudaEventSynchronize(e1);
+      float ms = 0.0f;
+      cudaEventElapsedTime(&ms, e0, e1);
+      b->tune_ms[k][c] = ms / 3.0f;
+      if (c == 0 || ms < best) {
+        best = ms;
+        b->pair_warps[k] = w;
+      }
+    }
+  }
+  b->launches = l0;  // tuning passes are not steps
+  cudaEventDestroy(e0);
+  cudaEventDestroy(e1);
+  BCU(cudaGetLastError());
+  b->tuned = true;
+  return BROMOC_OK;
+}
+
+// The launches of nsteps BD steps with their uploads (seeds in the replica
+// records, the step index), in stream order.
+void enqueue_steps(bromoc_batch *b, const KP &p, bool rf, uint32_t terms, int nsteps) {
+  cudaMemcpyAsync(b->rep, b->rep_pinned, b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice,
+                  b->stream);
+  cudaMemcpyAsync(b->d_step0, b->step_pinned, sizeof(uint64_t), cudaMemcpyHostToDevice,
+                  b->stream);
+  for (int k = 0; k < nsteps; ++k) {
+    launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
     b->launches += 1;
+    launch_pairs_asm(b, p, rf, 1, k, nullptr);
   }
 }
 
@@ -278,6 +395,7 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   b->proto = proto;
   b->kp = *pk;
   b->stream = stream;
+  bromoc_ctx_attach(proto, &b->orphaned);
   b->nrep = nrep;
   b->cap.resize(nrep);
   b->off.resize(nrep);
@@ -318,8 +436,11 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   if (!rc) rc = balloc(b, &b->tpf, npair * 64);
   if (!rc) rc = balloc(b, &b->tpb, npair * 64);
   if (!rc) rc = balloc(b, &st, 1);
+  if (!rc) rc = balloc(b, &b->d_step0, 1);
   if (!rc && cudaMallocHost((void **)&b->rep_pinned, nrep * sizeof(RepDev)) != cudaSuccess)
     rc = bset(b, BROMOC_E_NOMEM, "batch: pinned replica records");
+  if (!rc && cudaMallocHost((void **)&b->step_pinned, sizeof(uint64_t)) != cudaSuccess)
+    rc = bset(b, BROMOC_E_NOMEM, "batch: pinned step index");
   if (rc) {
     const std::string msg = b->err;
     bromoc_batch_destroy(b);
@@ -367,13 +488,19 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
 
 int bromoc_batch_destroy(bromoc_batch *b) {
   if (!b) return BROMOC_E_ARG;
-  if (b->stream) cudaStreamSynchronize(b->stream);
+  if (!b->orphaned) {
+    if (b->stream) cudaStreamSynchronize(b->stream);
+    bromoc_ctx_detach(b->proto, &b->orphaned);
+  }
   for (void *a : b->allocs) cudaFree(a);
   if (b->work) cudaFree(b->work);
   if (b->wpart) cudaFree(b->wpart);
   if (b->tiles) cudaFree(b->tiles);
   if (b->rep_pinned) cudaFreeHost(b->rep_pinned);
+  if (b->step_pinned) cudaFreeHost(b->step_pinned);
+  drop_graph(b);
   delete b;
+  cudaGetLastError();  // leave no non-sticky error behind for the next call
   return BROMOC_OK;
 }
 
@@ -389,6 +516,7 @@ extern "C" {
 
 int bromoc_batch_set_systems(bromoc_batch *b, const bromoc_system *sys) {
   if (!b || !sys) return bset(b, BROMOC_E_ARG, "set_systems: null");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
   // the drift and noise factors are shared (prototype tables): every
   // replica must have the prototype's dt, kbt and bdmax
   for (int r = 0; r < b->nrep; ++r) {
@@ -417,6 +545,7 @@ int bromoc_batch_set_systems(bromoc_batch *b, const bromoc_system *sys) {
 int bromoc_batch_set_particles(bromoc_batch *b, int32_t r, int32_t n, const double *x,
                                const double *y, const double *z, const int32_t *typei) {
   if (!b || !x || !y || !z || !typei) return bset(b, BROMOC_E_ARG, "set_particles: null");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
   if (r < 0 || r >= b->nrep) return bset(b, BROMOC_E_ARG, "set_particles: no replica %d", r);
   if (n < 0 || n > b->cap[r])
     return bset(b, BROMOC_E_CAPACITY, "set_particles: %d ions exceed capacity %d", n, b->cap[r]);
@@ -457,6 +586,7 @@ int bromoc_batch_set_particles(bromoc_batch *b, int32_t r, int32_t n, const doub
 int bromoc_batch_get_particles(bromoc_batch *b, int32_t r, int32_t *n, double *x, double *y,
                                double *z) {
   if (!b || r < 0 || r >= b->nrep) return bset(b, BROMOC_E_ARG, "get_particles: bad replica");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
   const int m = b->n[r];
   if (n) *n = m;
   std::vector<float4> h1(m), h2(m);
@@ -480,20 +610,53 @@ int bromoc_batch_get_particles(bromoc_batch *b, int32_t r, int32_t *n, double *x
 int bromoc_batch_bd_steps(bromoc_batch *b, uint32_t terms, int32_t nsteps, const uint64_t *seeds,
                           uint64_t step0, double *eterms) {
   if (!b || !seeds || nsteps < 0) return bset(b, BROMOC_E_ARG, "bd_steps: bad arguments");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  cudaGetLastError();  // a stale non-sticky error of an unrelated call
   if (!b->have_sys) return bset(b, BROMOC_E_STATE, "bd_steps: set_systems first");
   for (int r = 0; r < b->nrep; ++r) b->rep_h[r].seed = seeds[r];
   BCU(cudaStreamSynchronize(b->stream));  // the pinned records may still be in use
   std::memcpy(b->rep_pinned, b->rep_h.data(), b->nrep * sizeof(RepDev));
-  BCU(cudaMemcpyAsync(b->rep, b->rep_pinned, b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice,
-                      b->stream));
+  *b->step_pinned = step0;
   const bool rf = (terms & BROMOC_M_RFPAR) && b->kp.qrfpar;
   KP p = b->kp;
   p.pk1 = b->pk1[b->cur];
   p.pk2 = b->pk2[b->cur];
-  for (int k = 0; k < nsteps; ++k) {
-    launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
-    b->launches += 1;
-    launch_pairs_asm(b, p, rf, 1, step0 + k, nullptr);
+  if (nsteps > 0 && !b->tuned) {
+    BCU(cudaMemcpyAsync(b->rep, b->rep_pinned, b->nrep * sizeof(RepDev),
+                        cudaMemcpyHostToDevice, b->stream));
+    int rc = autotune(b, p, rf);
+    if (rc) return rc;
+  }
+  if (nsteps > 0 && b->use_graph) {
+    if (!b->gexec || b->g_nsteps != nsteps || b->g_rf != (int)rf ||
+        (uint32_t)b->g_terms != terms) {
+      drop_graph(b);
+      cudaGraph_t g = nullptr;
+      const long long l0 = b->launches;
+      BCU(cudaStreamBeginCapture(b->stream, cudaStreamCaptureModeThreadLocal));
+      enqueue_steps(b, p, rf, terms, nsteps);
+      const cudaError_t ec = cudaStreamEndCapture(b->stream, &g);
+      if (ec != cudaSuccess) {
+        if (g) cudaGraphDestroy(g);
+        return bset(b, BROMOC_E_CUDA, "bd_steps: graph capture: %s", cudaGetErrorString(ec));
+      }
+      const cudaError_t ei = cudaGraphInstantiate(&b->gexec, g, 0);
+      cudaGraphDestroy(g);
+      if (ei != cudaSuccess) {
+        b->gexec = nullptr;
+        return bset(b, BROMOC_E_CUDA, "bd_steps: graph instantiate: %s", cudaGetErrorString(ei));
+      }
+      b->g_launches = b->launches - l0;
+      b->launches = l0;
+      b->g_nsteps = nsteps;
+      b->g_rf = (int)rf;
+      b->g_terms = (int)terms;
+    }
+    BCU(cudaGraphLaunch(b->gexec, b->stream));
+    b->launches += b->g_launches;
+    b->graph_launches += 1;
+  } else if (nsteps > 0) {
+    enqueue_steps(b, p, rf, terms, nsteps);
   }
   BCU(cudaGetLastError());
   if (eterms && nsteps > 0) {
@@ -512,6 +675,8 @@ int bromoc_batch_bd_steps(bromoc_batch *b, uint32_t terms, int32_t nsteps, const
 // off_r from bromoc_batch_offset).
 int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double *eterms) {
   if (!b) return BROMOC_E_ARG;
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  cudaGetLastError();  // a stale non-sticky error of an unrelated call
   const bool rf = (terms & BROMOC_M_RFPAR) && b->kp.qrfpar;
   KP p = b->kp;
   p.pk1 = b->pk1[b->cur];
@@ -519,7 +684,7 @@ int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double 
   double *fdev = nullptr;
   if (forces) BCU(cudaMalloc((void **)&fdev, (size_t)b->nslots * 3 * sizeof(double)));
   launch_batch_fields(p, b->rep_of, b->rep, b->pe, b->nslots, terms, 1, b->stream);
-  launch_pairs_asm(b, p, rf, 0, 0, fdev);
+  launch_pairs_asm(b, p, rf, 0, 0, fdev);  // no move: the step index is not read
   k_batch_ereduce<<<b->nrep, 256, 0, b->stream>>>(b->rep, b->pe, b->wpart, rf ? 1 : 0,
                                                   b->eterms);
   b->launches += 2;
@@ -534,6 +699,30 @@ int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double 
   if (fdev) cudaFree(fdev);
   if (e != cudaSuccess) return bset(b, BROMOC_E_CUDA, "batch energy: %s", cudaGetErrorString(e));
   return BROMOC_OK;
+}
+
+int bromoc_batch_set_graph(bromoc_batch *b, int32_t on) {
+  if (!b) return BROMOC_E_ARG;
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  BCU(cudaStreamSynchronize(b->stream));
+  b->use_graph = on != 0;
+  if (!b->use_graph) drop_graph(b);
+  return BROMOC_OK;
+}
+
+int bromoc_batch_tuning(const bromoc_batch *b, int32_t *warps, int32_t *items, double *ms) {
+  if (!b) return BROMOC_E_ARG;
+  for (int k = 0; k < kBuckets; ++k) {
+    if (warps) warps[k] = b->tuned && b->wb[k + 1] > b->wb[k] ? b->pair_warps[k] : 0;
+    if (items) items[k] = b->wb[k + 1] - b->wb[k];
+    for (int c = 0; c < 3; ++c)
+      if (ms) ms[3 * k + c] = b->tuned ? (double)b->tune_ms[k][c] : 0.0;
+  }
+  return BROMOC_OK;
+}
+
+int64_t bromoc_batch_graph_launches(const bromoc_batch *b) {
+  return b ? b->graph_launches : -1;
 }
 
 int bromoc_batch_offset(const bromoc_batch *b, int32_t r) {

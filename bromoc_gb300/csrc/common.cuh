@@ -204,6 +204,17 @@ __host__ __device__ inline double gcmc_uniform(uint64_t seed, uint64_t cycle,
   return u01(gcmc_word(seed, cycle, attempt, draw));
 }
 
+// The uniforms of Metropolis moves: the GCMC stream's layout under its own
+// tag (3), so the two streams never share a counter.
+__host__ __device__ inline double mc_uniform(uint64_t seed, uint64_t cycle, uint32_t move,
+                                             uint32_t draw) {
+  uint32_t w[4];
+  philox4x32_10(move, draw >> 2, (uint32_t)cycle,
+                ((uint32_t)(cycle >> 32) & 0x00FFFFFFu) | (3u << 24), (uint32_t)seed,
+                (uint32_t)(seed >> 32), w);
+  return u01(w[draw & 3]);
+}
+
 __host__ __device__ inline double fsign(double a, double b) {
   return b >= 0.0 ? fabs(a) : -fabs(a);
 }

@@ -611,7 +611,12 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
   const bool nonbond = (mask & 1u) != 0;
   const int nmob_ub = nub - p.nsites - p.nfix;
   const PairCfg32 pc = pair_cfg32(p, nub, mask);
-  if (plan.fp32 && plan.ntile > 0 && (pc.ii || pc.rf)) {
+  if (plan.fp32 && plan.cells) {
+    if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
+    nk += launch_cells(p, nub, qforces, slot, stream);
+    if (plan.t_pairs) cudaEventRecord(plan.t_pairs->b, stream);
+    slot += cell_pair_blocks(p, nub);
+  } else if (plan.fp32 && plan.ntile > 0 && (pc.ii || pc.rf)) {
     const int nb = n3_blocks(plan.ntile);
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
     const bool efp = !p.ipq_ok;
@@ -689,7 +694,9 @@ int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {
   const int nmob_ub = nub - p.nsites - p.nfix;
   if (plan.fp32) {
     const PairCfg32 pc = pair_cfg32(p, nub, mask);
-    if (plan.ntile > 0 && (pc.ii || pc.rf))
+    if (plan.cells)
+      slot += cell_pair_blocks(p, nub);
+    else if (plan.ntile > 0 && (pc.ii || pc.rf))
       slot += n3_blocks(plan.ntile);
     else if (pc.ntg > 0 && plan.nchunk_ii > 0)
       slot += ((pc.ntg + kPairThreads - 1) / kPairThreads) * plan.nchunk_ii;

@@ -194,6 +194,12 @@ struct KP {
   float4 *tpf;                  // [npairs][2][32]
   float *tpb;                   // [npairs][2][32]
   int ntile;                    // ion tiles of 32 (0: chunked pair kernel)
+  // extension mode, FP32: cell list of the ions (cells of edge >= the cutoff,
+  // so every pair within it lies in the same or a neighbouring cell)
+  int nc[3], ncells;            // cells per axis, total (0: no cell list)
+  float cinv[3];                // cells per Angstrom along each axis
+  int *cell_n, *cell_start;     // [ncells + 1]: counts (then cursors), first slot
+  int *cell_ion, *ion_cell;     // [cap]: ions by cell (ascending within a cell); an ion's cell
   const float2 *fact_f;         // [ntype+1] (fact1a, fact2a)
   const float2 *zcont_ff;       // [cntpts] crossing planes (hi, lo)
   const float *esvdw_f;         // [nttyp+1] repulsion scale per combined type

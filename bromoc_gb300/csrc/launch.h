@@ -15,6 +15,7 @@ struct EnergyPlan {
   int nchunk_rf;      // source chunks of the RFPAR cross kernel
   int ntile;          // FP32: ion tiles of the Newton-3 pair kernel (0: chunked)
   bool fp32;
+  bool cells = false; // FP32 extension mode: the cell-list pair kernel
   bool reduce_energy; // launch the final energy reduction
   KTimer *t_pairs = nullptr, *t_rf = nullptr, *t_fields = nullptr;
 };
@@ -65,6 +66,10 @@ void launch_pack(const KP &p, int ntot_ub, bool to_records, cudaStream_t stream)
 int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
                   int qforces, cudaStream_t stream);
 int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask);
+// cells.cu: the cell list of the FP32 extension mode and its pair kernel
+// (block partial energies from `slot`); returns the kernels launched
+int launch_cells(const KP &p, int ntot_ub, int qforces, int slot, cudaStream_t stream);
+int cell_pair_blocks(const KP &p, int ntot_ub);
 int n3_blocks(int ntile);  // blocks (energy slots) of the Newton-3 pair kernel
 
 // dyn.cu: force assembly, optionally fused with the BD update
@@ -80,6 +85,16 @@ cudaError_t launch_bd_loop(const KP &p, const AssembleFlags &fl, int ntot_ub, ui
                            int fields_first, cudaStream_t stream);
 
 // gcmc.cu
+// Metropolis moves (mc.cu): the chain's device record, reset per call.
+struct McState {
+  int iat, skip, draw, naccept;  // the move's ion (0-based), no position found, next draw
+  double xn, yn, zn;             // its proposed position
+  double e[2];                   // INTERACT at the old and the new position
+  double dener;                  // accepted energy change of the call
+};
+int launch_metropolis(const KP &p, int ntot, uint32_t mask, int nmcm, double mcmax,
+                      uint64_t seed, uint64_t cycle, McState *mc, cudaStream_t stream);
+
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream);
 // GRAND: ngcmc attempts in one cooperative launch (gcmc.cu)
@@ -100,3 +115,8 @@ int bromoc_ctx_fail(bromoc_ctx *ctx, int code, const char *msg);
 // FP32 prototype for a replica batch: completes its setup (scratch, FP32
 // constants) and returns its parameter block.
 int bromoc_ctx_prepare_f32(bromoc_ctx *ctx, const bgpu::KP **kp, cudaStream_t *stream);
+// Replica batches and adjoint engines borrow their prototype context's
+// stream and tables.  They attach a flag to it; a context destroyed before
+// them sets the flag, and they then neither touch its stream nor run.
+void bromoc_ctx_attach(bromoc_ctx *ctx, int *orphaned);
+void bromoc_ctx_detach(bromoc_ctx *ctx, int *orphaned);

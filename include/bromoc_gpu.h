@@ -391,6 +391,18 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc,
                      uint64_t seed, uint64_t cycle, double *dener_sum);
 /* Buffer counters after GRAND: nat, ninsert, nremove [nbuffer] and the
  * occupancy histogram prob[nbuffer*(capacity+1)] (prob(ib,n) of simul1). */
+/* METROPOLIS (metropolis.f90:31-55, move.f90:19-45): nmcm Monte Carlo moves
+ * of cycle `cycle`, device resident.  Each picks a mobile ion and a
+ * displacement of up to mcmax/2 per axis (drawn again while the position
+ * lies outside the system, at most 1000 times; then the move is skipped),
+ * evaluates INTERACT at the old and the new position, and accepts downhill
+ * moves and uphill ones with probability exp(-(enew - eold)/kT).  Uniforms:
+ * Philox4x32-10 keyed by (seed, cycle, move, draw) under their own stream
+ * tag.  naccept, dener_sum (may be NULL): accepted moves and their summed
+ * energy change (ener += dener).  Systems with fixed ions are refused. */
+int bromoc_gpu_metropolis(bromoc_ctx *ctx, uint32_t terms, int32_t nmcm, double mcmax,
+                          uint64_t seed, uint64_t cycle, int32_t *naccept,
+                          double *dener_sum);
 int bromoc_gpu_get_buffers(bromoc_ctx *ctx, int32_t *nat, int32_t *ninsert,
                            int32_t *nremove, int32_t *prob);
 /* countions crossing counters [(ntype-nold)*cntpts], type-major */
@@ -440,6 +452,21 @@ int bromoc_batch_energy(bromoc_batch *b, uint32_t terms, double *forces, double 
 int bromoc_batch_offset(const bromoc_batch *b, int32_t r);
 int bromoc_batch_slots(const bromoc_batch *b);
 int64_t bromoc_batch_launch_count(const bromoc_batch *b);
+/* Runs of BD steps replayed from a CUDA graph (on, the default: the seeds'
+ * and step index's uploads and every step's launches captured once per
+ * step count and replayed, one graph launch per call) or launched one by
+ * one (off); the trajectories agree bit for bit.  No counterpart in the
+ * reference, which has no batch. */
+int bromoc_batch_set_graph(bromoc_batch *b, int32_t on);
+/* The autotuner's state per replica size bucket (fewer than 1000 ions,
+ * 1000-4000, more): warps[3] the pair kernel's chosen warps per block (0
+ * when the bucket is empty or not tuned yet), items[3] its tile pairs,
+ * ms[9] the measured time of one pair pass of bucket k with 2, 4, 8 warps
+ * per block at ms[3k..3k+2].  Tuning runs at the first BD step after the
+ * replicas' particles change.  No counterpart in the reference. */
+int bromoc_batch_tuning(const bromoc_batch *b, int32_t *warps, int32_t *items, double *ms);
+/* Graph launches so far (one per bd_steps call on the graph path). */
+int64_t bromoc_batch_graph_launches(const bromoc_batch *b);
 
 /* ---- adjoint of a BD segment (no reference counterpart) ----------------------
  * Gradient of a function of the segment's pair-distance histogram with respect

@@ -15,6 +15,9 @@ const char *bromoc_ref_last_error(const bromoc_ref *r);
 int bromoc_ref_threads(void);
 /* OpenMP threads of the timed build (no effect on the sequential one). */
 int bromoc_ref_set_threads(int32_t n);
+int bromoc_ref_metropolis(bromoc_ref *r, uint32_t terms, int32_t nmcm, double mcmax,
+                          uint64_t seed, uint64_t cycle, int32_t *naccept,
+                          double *dener_sum);
 int bromoc_ref_set_system(bromoc_ref *r, const bromoc_system *sys);
 int bromoc_ref_set_types(bromoc_ref *r, const bromoc_types *t);
 int bromoc_ref_set_pairs(bromoc_ref *r, const bromoc_pairs *p);

@@ -426,6 +426,22 @@ int bromoc_ref_grand(bromoc_ref *r, uint32_t terms, int32_t ngcmc, uint64_t seed
   return r->s.err.empty() ? BROMOC_OK : BROMOC_E_CAPACITY;
 }
 
+int bromoc_ref_metropolis(bromoc_ref *r, uint32_t terms, int32_t nmcm, double mcmax,
+                          uint64_t seed, uint64_t cycle, int32_t *naccept,
+                          double *dener_sum) {
+  if (!r || nmcm < 0 || !(mcmax > 0.0)) return BROMOC_E_ARG;
+  if (!ready(r)) return BROMOC_E_STATE;
+  if (r->s.nfix > 0) return fail(r, "metropolis: systems with fixed ions are not supported",
+                                 BROMOC_E_STATE);
+  if (r->s.ntot - r->s.nsites < 1) return fail(r, "metropolis: no mobile ion", BROMOC_E_STATE);
+  double d = 0.0;
+  int na = 0;
+  bref::metropolis(r->s, terms, nmcm, mcmax, seed, cycle, d, na);
+  if (naccept) *naccept = na;
+  if (dener_sum) *dener_sum = d;
+  return BROMOC_OK;
+}
+
 int bromoc_ref_get_buffers(bromoc_ref *r, int32_t *nat, int32_t *ninsert,
                            int32_t *nremove, int32_t *prob) {
   if (!r) return BROMOC_E_ARG;

@@ -328,4 +328,58 @@ void grand(State &s, uint32_t mask, int ngcmc, uint64_t seed, uint64_t icycle,
   }
 }
 
+// move.f90:19-45: a mobile ion and a displacement of up to mcmax/2 per
+// axis, drawn again while the new position lies outside the system.
+static bool mc_move(const State &s, double mcmax, uint64_t seed, uint64_t cycle, uint32_t m,
+                    uint32_t &draw, int &iat, double &xn, double &yn, double &zn) {
+  const bromoc_system &q = s.sys;
+  const double natom2 = (double)(s.ntot - s.nsites);
+  for (int t = 0; t < kMcTries; ++t) {
+    iat = s.nsites + s.nfix + (int)(natom2 * mc_uniform(seed, cycle, m, draw++)) + 1;
+    xn = s.x[iat] + mcmax * (mc_uniform(seed, cycle, m, draw++) - 0.5);
+    yn = s.y[iat] + mcmax * (mc_uniform(seed, cycle, m, draw++) - 0.5);
+    zn = s.z[iat] + mcmax * (mc_uniform(seed, cycle, m, draw++) - 0.5);
+    bool out;
+    if (q.shape == BROMOC_SPHERE) {
+      const double r2 = (xn - q.cx) * (xn - q.cx) + (yn - q.cy) * (yn - q.cy) +
+                        (zn - q.cz) * (zn - q.cz);
+      out = r2 > s.rsphe2;
+    } else if (q.shape == BROMOC_ECYL) {
+      const double ex = (xn - q.cx) * s.iecx, ey = (yn - q.cy) * s.iecy;
+      out = ex * ex + ey * ey > 1.0 || zn < s.lz2m || zn > s.lz2p;
+    } else {
+      out = xn < s.lx2m || xn > s.lx2p || yn < s.ly2m || yn > s.ly2p || zn < s.lz2m ||
+            zn > s.lz2p;
+    }
+    if (!out) return true;
+  }
+  return false;
+}
+
+// metropolis.f90:31-55: INTERACT of the ion at its old (with alerts) and new
+// position; downhill moves are taken, uphill ones with probability
+// exp(-(enew - eold)/kT).
+void metropolis(State &s, uint32_t mask, int nmcm, double mcmax, uint64_t seed,
+                uint64_t cycle, double &dener_sum, int &naccept) {
+  for (int m = 0; m < nmcm; ++m) {
+    uint32_t draw = 0;
+    int iat = 0;
+    double xn, yn, zn;
+    if (!mc_move(s, mcmax, seed, cycle, (uint32_t)m, draw, iat, xn, yn, zn)) continue;
+    const int it = std::abs(s.typei[iat]);
+    double eold, enew;
+    interact(s, mask, eold, s.x[iat], s.y[iat], s.z[iat], it, iat, true);
+    interact(s, mask, enew, xn, yn, zn, it, iat, false);
+    bool acc = enew <= eold;
+    if (!acc) acc = mc_uniform(seed, cycle, (uint32_t)m, draw++) < std::exp(-(enew - eold) * s.ikbt);
+    if (acc) {
+      s.x[iat] = xn;
+      s.y[iat] = yn;
+      s.z[iat] = zn;
+      dener_sum += enew - eold;
+      ++naccept;
+    }
+  }
+}
+
 }  // namespace bref

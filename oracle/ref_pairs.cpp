@@ -280,6 +280,17 @@ double bd_gauss(uint64_t seed, uint64_t step, uint32_t slot, int comp) {
   return (comp & 1) ? box_muller(w[2], w[3]) : box_muller(w[0], w[1]);
 }
 
+// The uniforms of Metropolis moves: the GCMC stream's layout under its own
+// tag, so the two never share a counter.
+double mc_uniform(uint64_t seed, uint64_t cycle, uint32_t move, uint32_t draw) {
+  uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};
+  uint32_t ctr[4] = {move, draw >> 2, (uint32_t)cycle,
+                     ((uint32_t)(cycle >> 32) & 0x00FFFFFFu) | (3u << 24)};
+  uint32_t w[4];
+  philox4x32_10(ctr, key, w);
+  return u01(w[draw & 3]);
+}
+
 double gcmc_uniform(uint64_t seed, uint64_t cycle, uint32_t attempt,
                     uint32_t draw) {
   uint32_t key[2] = {(uint32_t)seed, (uint32_t)(seed >> 32)};

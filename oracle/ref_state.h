@@ -189,5 +189,11 @@ void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],
 double bd_gauss(uint64_t seed, uint64_t step, uint32_t slot, int comp);
 double gcmc_uniform(uint64_t seed, uint64_t cycle, uint32_t attempt,
                     uint32_t draw);
+double mc_uniform(uint64_t seed, uint64_t cycle, uint32_t move, uint32_t draw);
+// metropolis.f90:31-55 with move.f90:19-45; at most kMcTries draws of a
+// position inside the system per move (the reference draws until one is)
+constexpr int kMcTries = 1000;
+void metropolis(State &s, uint32_t mask, int nmcm, double mcmax, uint64_t seed,
+                uint64_t cycle, double &dener_sum, int &naccept);
 
 }  // namespace bref

@@ -78,3 +78,63 @@ def test_batch_rejects_bad_input(setup):
     with pytest.raises(abi.BromocError):
         b.set_particles(len(SIZES), np.zeros(1), np.zeros(1), np.zeros(1),
                         np.ones(1, np.int32))
+
+
+def _uneven_batch(gpu_lib, sizes, seed=300):
+    proto_spec = _replica(99, 20)
+    proto = gpu_lib.create(CAP, abi.FP32)
+    proto_spec.push(proto)
+    reps = []
+    for r, n in enumerate(sizes):
+        if n < 500:
+            reps.append(_replica(seed + r, n))
+            continue
+        # a bulk cube at 1 M for the larger replicas
+        s = _replica(seed + r, 20)
+        L = (n / (2.0 * 6.02214e-4)) ** (1.0 / 3.0)
+        p = synth.jittered_lattice(np.random.default_rng(seed + r), n, -0.5 * L + 0.5,
+                                   0.5 * L - 0.5)
+        s.lx = s.ly = s.lz = float(L)
+        s.x, s.y, s.z = p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
+        s.typei = np.array([1, 2] * (n // 2), np.int32)
+        reps.append(s)
+    b = Batch(proto, sizes)
+    b.set_systems([s.system_struct() for s in reps])
+    for r, s in enumerate(reps):
+        b.set_particles(r, s.x, s.y, s.z, s.typei)
+    return proto, reps, b
+
+
+def test_graph_replay_matches_launches(gpu_lib):
+    """Runs replayed from the captured graph (several calls, changing step0
+    and seeds) and the same runs launched one by one agree bit for bit;
+    the graph is captured once per step count and replayed."""
+    sizes = [40, 150, 1100, 70]
+    out = []
+    for graph in (True, False):
+        _, reps, b = _uneven_batch(gpu_lib, sizes)
+        b.set_graph(graph)
+        for call in range(3):
+            seeds = [500 + 13 * r + call for r in range(len(sizes))]
+            b.bd_steps(2, seeds, step0=10 * call)
+        if graph:
+            assert b.graph_launches() == 3
+        out.append([np.stack(b.get_particles(r, sizes[r])) for r in range(len(sizes))])
+    for a, c in zip(*out):
+        np.testing.assert_array_equal(a, c)
+
+
+def test_autotuner_chooses_per_bucket(gpu_lib):
+    sizes = [40, 1100, 60]
+    _, _, b = _uneven_batch(gpu_lib, sizes)
+    w, n, ms = b.tuning()
+    assert (w == 0).all()  # nothing tuned before the first step
+    b.bd_steps(1, [1, 2, 3], step0=0)
+    w, n, ms = b.tuning()
+    assert n[0] > 0 and n[1] > 0 and n[2] == 0
+    for k in range(3):
+        if n[k]:
+            assert w[k] in (2, 4, 8) and (ms[k] > 0).all()
+            assert ms[k][[2, 4, 8].index(w[k])] == ms[k].min()
+        else:
+            assert w[k] == 0

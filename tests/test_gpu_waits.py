@@ -54,3 +54,37 @@ def test_device_usable_after_expired_wait(gpu_lib, oracle_mod):
     to, fo, _ = o.energy(abi.M_ALL, forces=True)
     assert np.linalg.norm(fg - fo) <= 1e-10 * np.linalg.norm(fo)
     assert abs(tg["ener"] - to["ener"]) <= 1e-10 * max(1.0, abs(to["ener"]))
+
+
+def test_context_destroyed_before_its_dependents(gpu_lib):
+    """A context destroyed while a replica batch and an adjoint engine still
+    borrow it: they are flagged, refuse further work with an error, and
+    their own destroy touches nothing of the gone context."""
+    import ctypes as C
+    from bromoc_gb300.adjoint import Adjoint
+    from bromoc_gb300.batch import Batch
+    lib = gpu_lib.load()
+    spec = systems.pairs(precision=abi.FP32)
+    proto = gpu_lib.create(256, abi.FP32)
+    spec.push(proto)
+    b = Batch(proto, [len(spec.x)])
+    adj_spec = systems.efpot_all(precision=abi.FP32)
+    proto2 = gpu_lib.create(256, abi.FP32)
+    adj_spec.push(proto2)
+    adj = Adjoint(proto2, 256, abi.FP32)
+    # destroy the contexts behind the dependents' backs (the C ABI)
+    lib.bromoc_gpu_destroy(proto.h)
+    proto.h = None
+    lib.bromoc_gpu_destroy(proto2.h)
+    proto2.h = None
+    with pytest.raises(abi.BromocError) as e:
+        b.set_particles(0, spec.x, spec.y, spec.z, spec.typei)
+    assert e.value.code == abi.E_STATE
+    with pytest.raises(abi.BromocError):
+        adj.set_particles(adj_spec.x, adj_spec.y, adj_spec.z, adj_spec.typei)
+    b.close()
+    adj.close()
+    # the device is still fine
+    g = gpu_lib.create(256, abi.FP64)
+    spec.push(g)
+    g.energy()

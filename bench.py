@@ -750,6 +750,19 @@ def run_gpu(args, rank, world, local_rank):
         pair_roof = {"kernel": "k_pairs32n (one launch per BD step)", "achieved": a,
                      "unit": "TFLOP/s", "frac": a / peak_fp32, "launch_ms": ms / nl,
                      "traffic": profile_traffic("k_pairs32n")[0]}
+    gathers = None
+    if "fields" in kt_split:
+        # single-particle terms: 8 static-field corners (32 B), 8 repulsion
+        # corners (8 B), 2 x 8 RFPAR corners (64 B) and the records (48 B)
+        ms, nl = kt_split["fields"]
+        nbytes = n_ion * (32 + 8 + 64 + 48)
+        a = nbytes / (ms / nl * 1e-3) / 1e9
+        gathers = {"kernel": "k_fields_warp_f32 (grid gathers, one launch per BD step)",
+                   "achieved": a, "unit": "GB/s", "peak": peaks["hbm_gbs"],
+                   "peak_source": src + " HBM copy bandwidth (the maps are L2-resident)",
+                   "frac": a / peaks["hbm_gbs"], "launch_ms": ms / nl,
+                   "algorithmic": f"152 B per particle x {n_ion:.0f} particles",
+                   "bound": "latency (cell search, then one round of gathers per particle)"}
     if dom == "bd_loop":
         # one launch runs the NBD steps of a cycle: the pair work of each
         # step (ion-ion law + RFPAR cross term of every unordered pair) is
@@ -766,7 +779,7 @@ def run_gpu(args, rank, world, local_rank):
                 "algorithmic": f"{per} FLOP x N(N-1)/2 unordered pairs x {NBD} BD "
                                f"steps per launch, N = {n_ion:.0f} ions",
                 "launch_ms": ms / nl, "share": kt[dom][0] / tot_k,
-                "pair_kernel_unfused": pair_roof}
+                "pair_kernel_unfused": pair_roof, "gathers": gathers}
     elif dom == "pairs":
         # the FP32 pair kernel evaluates the ion-ion law and the RFPAR cross
         # term of every pair in one pass

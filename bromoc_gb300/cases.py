@@ -1,0 +1,74 @@
+"""Named small workloads of the hot path, each a few calls on cuda:0, for
+kernel captures with ncu (the summaries under profiles/ give the exact
+command lines):
+
+  python -m bromoc_gb300.cases pairs N     FP32 ENERGY (forces) of an N-ion
+                                           pore with the 120x120x180 maps,
+                                           3 calls: k_fields_warp_f32,
+                                           k_pairs32n, k_assemble_tiles
+  python -m bromoc_gb300.cases loop        the nanopore workload (2000 ions,
+                                           4 GCMC buffers): 4 cycles of
+                                           GRAND(4) + a 10-step k_bd_loop
+  python -m bromoc_gb300.cases cells N     FP32 BD steps of N ions of 1 M KCl
+                                           in a periodic cube, 20 A cutoff
+                                           (the cell-list kernels), 3 steps
+"""
+from __future__ import annotations
+
+import sys
+
+import numpy as np
+
+from . import _lib, abi, synth
+
+
+def pairs(n: int):
+    s = synth.pore(seed=3, nions=n, maps=synth.pore_maps(seed=103), precision=abi.FP32,
+                   buffers=False)
+    g = _lib.create(n + 16, abi.FP32)
+    s.push(g)
+    for _ in range(3):
+        g.energy(abi.M_ALL, forces=True)
+
+
+def loop():
+    s = synth.pore(seed=3, nions=2000, maps=synth.pore_maps(seed=102), precision=abi.FP32,
+                   buffers=True)
+    g = _lib.create(2400, abi.FP32)
+    s.push(g)
+    for c in range(4):
+        g.grand(4, 1234, c + 1, dener=False)
+        g.bd_steps(10, seed=1234, step0=10 * c, energies=False)
+    g.live_ntot()
+
+
+def cells(n: int):
+    L = (n / 1.2044e-3) ** (1.0 / 3.0)
+    rng = np.random.default_rng(5)
+    s = synth.bulk_kcl(seed=5, n_per=1, L=L, srpmf=True, precision=abi.FP32,
+                       periodic_rcut=20.0)
+    p = synth.jittered_lattice(rng, n, -0.5 * L + 1.5, 0.5 * L - 1.5)
+    s.x, s.y, s.z = p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
+    s.typei = np.array([1, 2] * (n // 2), np.int32)
+    g = _lib.create(n + 16, abi.FP32)
+    s.push(g)
+    for k in range(3):
+        g.bd_steps(1, seed=7, step0=k, energies=False)
+    g.live_ntot()
+
+
+def main(argv):
+    what = argv[1] if len(argv) > 1 else "loop"
+    if what == "pairs":
+        pairs(int(argv[2]) if len(argv) > 2 else 8000)
+    elif what == "cells":
+        cells(int(argv[2]) if len(argv) > 2 else 20000)
+    elif what == "loop":
+        loop()
+    else:
+        raise SystemExit(f"unknown case {what!r}: pairs N | loop | cells N")
+    print("ok")
+
+
+if __name__ == "__main__":
+    main(sys.argv)

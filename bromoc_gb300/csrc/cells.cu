@@ -12,9 +12,11 @@
 //   fill   : ions into their cell's stretch (atomic cursor per cell);
 //   sort   : each cell's stretch in ascending ion order (one thread per
 //            cell), so a run always sums a particle's pairs in one order.
-// Pair kernel: one thread per ion, in cell order (the lanes of a warp mostly
-// share their 27 neighbour cells, so the source records they read coincide);
-// each pair is evaluated by both of its ions, weight 1/2 per mobile source,
+// Pair kernel: kCellLanes lanes per ion, in cell order (the lanes of a
+// warp mostly share their 27 neighbour cells, so the source records they
+// read coincide); lane u of an ion takes every kCellLanes-th candidate of
+// each neighbour cell, and the lanes' sums meet in a fixed shuffle tree.
+// Each pair is evaluated by both of its ions, weight 1/2 per mobile source,
 // the conventions of the chunked kernel k_pairs32 (FP32 partials fii_f,
 // chunk 0; block partial energies).  Used when every axis holds at least four
 // cells; smaller boxes keep the all-pairs Newton-3 tile.
@@ -26,6 +28,7 @@
 namespace bgpu {
 
 constexpr int kCellThreads = 256;
+constexpr int kCellLanes = 4;  // lanes per ion in the pair kernel
 
 __device__ __forceinline__ int cell_of(const KP &p, const float4 &h, const float4 &l) {
   const float hh[3] = {h.x, h.y, h.z}, ll[3] = {l.x, l.y, l.z};
@@ -106,7 +109,8 @@ __global__ void __launch_bounds__(kCellThreads) k_pairs_cell(KP p, int qforces, 
     for (int k = threadIdx.x; k < nt * ipq_stride(nt); k += blockDim.x) tab[k] = __ldg(p.ipq + k);
   __syncthreads();
   const int ntot = p.st->ntot, m0 = p.nsites + p.nfix;
-  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int k = t / kCellLanes, u = t % kCellLanes;
   const int i = k < ntot - p.nsites ? p.cell_ion[k] : -1;
   float fx = 0.f, fy = 0.f, fz = 0.f;
   float e[4] = {0.f, 0.f, 0.f, 0.f};  // ecoul, elj (6 x elj with the dense table), esrpmf, eefpot
@@ -132,7 +136,7 @@ __global__ void __launch_bounds__(kCellThreads) k_pairs_cell(KP p, int qforces, 
           az -= az >= n2 ? n2 : 0;
           const int cc = (ax * n1 + ay) * n2 + az;
           const int s1 = p.cell_start[cc + 1];
-          for (int s = p.cell_start[cc]; s < s1; ++s) {
+          for (int s = p.cell_start[cc] + u; s < s1; s += kCellLanes) {
             const int j = p.cell_ion[s];
             if (j == i) continue;
             const float4 h = p.pk1[j], l = p.pk2[j];
@@ -170,7 +174,13 @@ __global__ void __launch_bounds__(kCellThreads) k_pairs_cell(KP p, int qforces, 
       }
     }
   }
-  if (i >= 0) {
+#pragma unroll
+  for (int o = 1; o < kCellLanes; o <<= 1) {  // the ion's lanes, fixed order
+    fx += __shfl_xor_sync(0xffffffffu, fx, o);
+    fy += __shfl_xor_sync(0xffffffffu, fy, o);
+    fz += __shfl_xor_sync(0xffffffffu, fz, o);
+  }
+  if (i >= 0 && u == 0) {
     float *f = p.fii_f;  // chunk 0
     f[i] = qforces ? fx : 0.f;
     f[p.cap + i] = qforces ? fy : 0.f;
@@ -188,7 +198,7 @@ __global__ void __launch_bounds__(kCellThreads) k_pairs_cell(KP p, int qforces, 
 }
 
 int cell_pair_blocks(const KP &p, int ntot_ub) {
-  return (std::max(0, ntot_ub - p.nsites) + kCellThreads - 1) / kCellThreads;
+  return (std::max(0, ntot_ub - p.nsites) * kCellLanes + kCellThreads - 1) / kCellThreads;
 }
 
 int launch_cells(const KP &p, int ntot_ub, int qforces, int slot, cudaStream_t stream) {
@@ -200,10 +210,11 @@ int launch_cells(const KP &p, int ntot_ub, int qforces, int slot, cudaStream_t s
   k_cell_scan<<<1, 1024, 0, stream>>>(p);
   k_cell_fill<<<nb, kCellThreads, 0, stream>>>(p);
   k_cell_sort<<<(p.ncells + kCellThreads - 1) / kCellThreads, kCellThreads, 0, stream>>>(p);
+  const int npb = cell_pair_blocks(p, ntot_ub);
   if (p.ipq_ok)
-    k_pairs_cell<false><<<nb, kCellThreads, 0, stream>>>(p, qforces, slot);
+    k_pairs_cell<false><<<npb, kCellThreads, 0, stream>>>(p, qforces, slot);
   else
-    k_pairs_cell<true><<<nb, kCellThreads, 0, stream>>>(p, qforces, slot);
+    k_pairs_cell<true><<<npb, kCellThreads, 0, stream>>>(p, qforces, slot);
   return 5;
 }
 

@@ -47,6 +47,18 @@ def load() -> C.CDLL:
         lib.bromoc_gpu_kernel_time.restype = C.c_int
         lib.bromoc_gpu_fp32_peak.argtypes = [C.c_void_p, d]
         lib.bromoc_gpu_fp32_peak.restype = C.c_int
+        i64p = C.POINTER(C.c_int64)
+        for name, args in (
+                ("set_profiles", [C.c_void_p, C.c_int32, C.c_int32, C.c_int32, C.c_int32,
+                                  C.c_double, C.c_int32]),
+                ("accum_profiles", [C.c_void_p]),
+                ("get_profiles", [C.c_void_p, d, d, d, i32, i32]),
+                ("traj_header", [C.c_int32, C.c_int32, C.c_char_p, C.c_void_p, C.c_int64,
+                                 i64p]),
+                ("traj_frame", [C.c_void_p, C.c_double, C.c_void_p, C.c_int64, i64p])):
+            f = getattr(lib, "bromoc_gpu_" + name)
+            f.argtypes = args
+            f.restype = C.c_int
         vp = C.c_void_p
         for name, args in (
                 ("create", [vp, C.c_int32, i32, C.POINTER(vp)]),

@@ -17,11 +17,12 @@ E_ARG, E_STATE, E_CUDA, E_CAPACITY, E_NOMEM, E_DEVICE = 1, 2, 3, 4, 5, 6
 
 TERM_NAMES = ("ener", "eelec", "evdw", "esrpmf", "eefpot", "eqqmx", "evdwmx",
               "esrpmfmx", "eefpotmx", "ememb", "egsbpa", "egsbpb", "evdwgd",
-              "erfpar")
+              "erfpar", "ebond", "eang", "edihe", "estack", "ebp", "eex", "eqq",
+              "esolv", "econ")
 NTERMS = len(TERM_NAMES)
 
-M_NONBOND, M_MEMB, M_PHIX, M_PHIV, M_RFPAR = 1, 2, 4, 8, 16
-M_ALL = 0x1F
+M_NONBOND, M_MEMB, M_PHIX, M_PHIV, M_RFPAR, M_BOND = 1, 2, 4, 8, 16, 32
+M_ALL = 0x3F
 BOX, SPHERE, ECYL = 0, 1, 2
 FP64, FP32 = 0, 1
 DYN0, DYN1, DYN2, DYN3 = 0, 1, 2, 3
@@ -62,6 +63,25 @@ class Pairs(C.Structure):
 class Sites(C.Structure):
     _fields_ = [("nsites", C.c_int32), ("typtyp", _i), ("charge", _d),
                 ("stfree", _u8), ("phiv_map", _i)]
+
+
+class Nucleotides(C.Structure):
+    _fields_ = [("epsnuc", C.c_double), ("scalepairing", C.c_double),
+                ("fctn", C.c_double), ("kappa", C.c_double),
+                ("qdeby", C.c_int32), ("qsolv", C.c_int32), ("epsolv", C.c_double),
+                ("nbond", C.c_int32), ("sitebond", _i), ("distbond", _d),
+                ("nangle", C.c_int32), ("siteangle", _i), ("valangle", _d),
+                ("ndihe", C.c_int32), ("sitedihe", _i), ("valdihe", _d),
+                ("nstack", C.c_int32), ("sitestack", _i), ("sgstack", _d),
+                ("nbp", C.c_int32), ("sitebp", _i), ("sgbp", _d), ("bpgc", _u8),
+                ("nex", C.c_int32), ("siteex", _i), ("sgex", _d),
+                ("nqq", C.c_int32), ("siteqq", _i),
+                ("nsolv", C.c_int32), ("siteslv", _i),
+                ("afn", C.c_int32), ("sn", _i), ("af", _d),
+                ("ctn", C.c_int32), ("csn", _i),
+                ("kx", _d), ("ky", _d), ("kz", _d),
+                ("contrx", _d), ("contry", _d), ("contrz", _d),
+                ("qunsplit", C.c_int32), ("nsites1st", C.c_int32)]
 
 
 class Grid(C.Structure):
@@ -119,6 +139,7 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         "set_types": [vp, C.POINTER(Types)],
         "set_pairs": [vp, C.POINTER(Pairs)],
         "set_sites": [vp, C.POINTER(Sites)],
+        "set_nucleotides": [vp, C.POINTER(Nucleotides)],
         "set_phix": [vp, C.POINTER(Grid), _f],
         "set_phiv": [vp, C.POINTER(Grid), _i8, C.POINTER(PhivOpts)],
         "set_rfpar": [vp, C.POINTER(Grid), C.c_int32, _f, _f, C.c_double, _i],
@@ -219,6 +240,7 @@ class Engine:
         self.nttyp = 0
         self.ntype = 0
         self.nold = 0
+        self.ndna = 0
         self.nbuffer = 0
         self.cntpts = 0
         self._dependents = set()
@@ -256,6 +278,17 @@ class Engine:
 
     def call(self, name, *args):
         self._chk(self._fn(name)(self.h, *args), name)
+
+    def set_nucleotides(self, topo) -> None:
+        """DNA bonded and Go-like term lists (a bromoc_gb300.nucleotides.Topology,
+        or None to clear them)."""
+        if topo is None:
+            self._chk(self._fn("set_nucleotides")(self.h, None), "set_nucleotides")
+            return
+        st, keep = topo.struct()
+        self._keep = keep
+        self._chk(self._fn("set_nucleotides")(self.h, C.byref(st)), "set_nucleotides")
+        self._keep = []
 
     # -- particles ------------------------------------------------------------
     def set_particles(self, x, y, z, typei, nsites=0, nfix=0, ibuffer=None):

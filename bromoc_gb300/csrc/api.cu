@@ -55,6 +55,12 @@ struct bromoc_ctx {
   int tp_tiles = 0;  // tiles the Newton-3 partial buffers hold
   int cell_cap = 0;  // cells the cell-list arrays hold
   McState *mc = nullptr;  // Metropolis chain record (device)
+  bool nuc_on = false;    // DNA bonded/Go term lists are set
+  // per-cycle profiles (simul1.f90:476-509) and the .btr frame staging buffer
+  bool prof_on = false;
+  ProfArgs prof{};
+  uint32_t *traj_w = nullptr;
+  long long traj_cap = 0;
   std::vector<int *> dependents;  // orphan flags of batches and adjoint engines
   double *d_dener = nullptr;
   // last energy plan (for dynamics())
@@ -136,6 +142,18 @@ int upload1(bromoc_ctx *ctx, const T **dst, const T *src, int n, T fill = T()) {
   int rc = upload(ctx, &d, v.data(), v.size());
   *dst = d;
   return rc;
+}
+
+// Drops the DNA bonded/Go term lists (set_sites renumbers the sites).
+void clear_nucl(bromoc_ctx *ctx) {
+  NucDev &n = ctx->kp.nuc;
+  for (const void *a : {(const void *)n.site, (const void *)n.par, (const void *)n.af,
+                        (const void *)n.te, (const void *)n.tf, (const void *)n.csr_start,
+                        (const void *)n.csr_ent, (const void *)n.csn, (const void *)n.ck,
+                        (const void *)n.cc, (const void *)n.cf})
+    dfree(ctx, const_cast<void *>(a));
+  n = NucDev{};
+  ctx->nuc_on = false;
 }
 
 Grid3 make_grid(const bromoc_grid &g) {
@@ -387,7 +405,8 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   fl = AssembleFlags{};
   fl.fp32_noise = plan.fp32;
   fl.fp32_partials = plan.fp32;
-  fl.is = (mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0;
+  plan.nuc = ctx->nuc_on && p.nsites > 0;
+  fl.is = ((mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0) || plan.nuc;
   plan.ntile = p.ntile = 0;
   plan.cells = false;
   if (plan.fp32 && p.periodic && nion > 0 && pair_cfg32(p, plan.ntot_ub, mask).ntg > 0 &&
@@ -930,6 +949,7 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
     return set_err(ctx, BROMOC_E_ARG, "set_sites: nsites must be in [0, 1024]");
   KP &p = ctx->kp;
   p.nsites = s->nsites;
+  clear_nucl(ctx);  // the term lists name sites of the previous set
   if (s->nsites == 0) return BROMOC_OK;
   if (!s->typtyp || !s->charge || !s->stfree)
     return set_err(ctx, BROMOC_E_ARG, "set_sites: null");
@@ -961,6 +981,126 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
     return set_err(ctx, BROMOC_E_ARG, "set_sites: nmcden needs per-site maps");
   }
   return rc;
+}
+
+int bromoc_gpu_set_nucleotides(bromoc_ctx *ctx, const bromoc_nucleotides *q) {
+  if (!ctx) return BROMOC_E_ARG;
+  CU(cudaStreamSynchronize(ctx->stream));
+  clear_nucl(ctx);
+  if (!q) return BROMOC_OK;
+  const int ns = ctx->kp.nsites;
+  if (ns <= 0) return set_err(ctx, BROMOC_E_STATE, "set_nucleotides: set_sites first");
+  // term list in kind order: bond, angle, torsion, stack, base pair,
+  // excluded volume, qq, solvent, APFOR
+  const int cnt[kNucKinds] = {q->nbond, q->nangle, q->ndihe, q->nstack, q->nbp,
+                              q->nex,   q->nqq,    q->nsolv, q->afn};
+  const int per[kNucKinds] = {2, 3, 4, 2, 2, 2, 2, 2, 1};
+  const int32_t *lst[kNucKinds] = {q->sitebond, q->siteangle, q->sitedihe, q->sitestack,
+                                   q->sitebp,   q->siteex,    q->siteqq,   q->siteslv,
+                                   q->sn};
+  const double *val[kNucKinds] = {q->distbond, q->valangle, q->valdihe, q->sgstack, q->sgbp,
+                                  q->sgex,     nullptr,     nullptr,    nullptr};
+  NucDev &n = ctx->kp.nuc;
+  std::vector<int4> site;
+  std::vector<double> par;
+  int total = 0;
+  for (int k = 0; k < kNucKinds; ++k) {
+    if (cnt[k] < 0 || cnt[k] > (1 << 24))
+      return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: count out of range");
+    if (cnt[k] > 0 && (!lst[k] || (k < 6 && !val[k])))
+      return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: null list");
+    n.off[k] = total;
+    total += cnt[k];
+  }
+  n.off[kNucKinds] = total;
+  if (q->nbp > 0 && !q->bpgc) return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: null bpgc");
+  if (q->afn > 0 && !q->af) return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: null af");
+  site.reserve(total);
+  par.reserve(total);
+  std::vector<std::vector<int>> ent(ns);  // per site: 4t+m, ascending t
+  for (int k = 0; k < kNucKinds; ++k)
+    for (int i = 0; i < cnt[k]; ++i) {
+      int v[4] = {-1, -1, -1, -1};
+      for (int m = 0; m < per[k]; ++m) {
+        const int sj = lst[k][per[k] * i + m];
+        if (sj < 1 || sj > ns)
+          return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: site %d out of [1, %d]", sj, ns);
+        v[m] = sj - 1;
+        ent[sj - 1].push_back(4 * (int)site.size() + m);
+      }
+      if (k == 4) v[2] = q->bpgc[i] ? 1 : 0;
+      site.push_back(make_int4(v[0], v[1], v[2], v[3]));
+      par.push_back(val[k] ? val[k][i] : 0.0);
+    }
+  std::vector<int> start(ns + 1, 0), flat;
+  for (int j = 0; j < ns; ++j) {
+    start[j] = (int)flat.size();
+    flat.insert(flat.end(), ent[j].begin(), ent[j].end());
+  }
+  start[ns] = (int)flat.size();
+  const int ctn = q->ctn;
+  if (ctn < 0 || (ctn > 0 && (!q->csn || !q->kx || !q->ky || !q->kz || !q->contrx ||
+                              !q->contry || !q->contrz)))
+    return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: CONTRANS lists");
+  std::vector<double> ck(3 * (size_t)std::max(ctn, 1), 0.0), cc(3 * (size_t)(ctn + 1), 0.0);
+  for (int i = 0; i < ctn; ++i) {
+    if (q->csn[i] < 0 || q->csn[i] > ns)
+      return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: csn out of [0, nsites]");
+    ck[3 * i] = q->kx[i];
+    ck[3 * i + 1] = q->ky[i];
+    ck[3 * i + 2] = q->kz[i];
+  }
+  for (int i = 0; i <= ctn && ctn > 0; ++i) {
+    cc[3 * i] = q->contrx[i];
+    cc[3 * i + 1] = q->contry[i];
+    cc[3 * i + 2] = q->contrz[i];
+  }
+  if (q->qunsplit && (q->nsites1st < 1 || q->nsites1st >= ns))
+    return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: nsites1st out of [1, nsites)");
+  if (q->qdeby && !(q->kappa > 0.0))
+    return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: Debye length must be positive");
+  if (q->qdeby < 0 || q->qdeby > 2)
+    return set_err(ctx, BROMOC_E_ARG, "set_nucleotides: qdeby must be 0, 1 or 2");
+  int4 *dsite = nullptr;
+  double *dpar = nullptr, *daf = nullptr, *dck = nullptr, *dcc = nullptr;
+  int *dstart = nullptr, *dflat = nullptr, *dcsn = nullptr;
+  int rc = upload(ctx, &dsite, site.data(), site.size());
+  if (!rc) rc = upload(ctx, &dpar, par.data(), par.size());
+  if (!rc) rc = upload(ctx, &daf, q->af, 3 * (size_t)q->afn);
+  if (!rc) rc = upload(ctx, &dstart, start.data(), start.size());
+  if (!rc) rc = upload(ctx, &dflat, flat.data(), flat.size());
+  if (!rc) rc = upload(ctx, &dcsn, q->csn, (size_t)ctn);
+  if (!rc) rc = upload(ctx, &dck, ck.data(), ck.size());
+  if (!rc) rc = upload(ctx, &dcc, cc.data(), cc.size());
+  if (!rc) rc = dalloc(ctx, &n.te, (size_t)total);
+  if (!rc) rc = dalloc(ctx, &n.tf, (size_t)total * 12);
+  if (!rc) rc = dalloc(ctx, &n.cf, 8);
+  n.site = dsite;
+  n.par = dpar;
+  n.af = daf;
+  n.csr_start = dstart;
+  n.csr_ent = dflat;
+  n.csn = dcsn;
+  n.ck = dck;
+  n.cc = dcc;
+  if (rc) {
+    clear_nucl(ctx);
+    return rc;
+  }
+  n.nterm = total;
+  n.epsnuc = q->epsnuc;
+  n.scalepairing = q->scalepairing;
+  n.fctn = q->fctn;
+  n.kappa = q->kappa;
+  n.ikappa = q->qdeby ? 1.0 / q->kappa : 0.0;
+  n.epsolv = q->epsolv;
+  n.qdeby = q->qdeby;
+  n.qsolv = q->qsolv != 0;
+  n.ctn = ctn;
+  n.qunsplit = q->qunsplit != 0;
+  n.nsites1st = q->nsites1st;
+  ctx->nuc_on = true;
+  return BROMOC_OK;
 }
 
 int bromoc_gpu_set_phix(bromoc_ctx *ctx, const bromoc_grid *g, const float *phix) {
@@ -1379,6 +1519,10 @@ int bromoc_gpu_interact(bromoc_ctx *ctx, uint32_t terms, double xj, double yj, d
   CU(cudaMemcpyAsync(p.trial, &t, sizeof t, cudaMemcpyHostToDevice, ctx->stream));
   launch_interact(p, ntot, terms, 1, ctx->d_dener, ctx->stream);
   ctx->launches += 3;
+  if (!beion && ctx->nuc_on) {  // the site's bonded/Go terms (interact.f90:211-334)
+    launch_nucl_interact(p, terms, j - 1, ctx->d_dener, ctx->stream);
+    ++ctx->launches;
+  }
   CU(cudaGetLastError());
   CU(cudaMemcpyAsync(dener, ctx->d_dener, sizeof(double), cudaMemcpyDeviceToHost, ctx->stream));
   CU(cudaStreamSynchronize(ctx->stream));
@@ -1694,12 +1838,134 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms, int32_t varian
     if (!rc && nbd > 0)
       rc = bromoc_gpu_bd_steps(ctx, terms, variant, nbd, seed, (cyc - 1) * nbd,
                                c + 1 == ncycle ? eterms : nullptr);
+    if (!rc && ctx->prof_on) rc = bromoc_gpu_accum_profiles(ctx);  // simul1.f90:476-509
   }
   int e = 0;
   if (!rc) rc = download_particles(ctx, ntot, x, y, z, typei, ibuffer, &e);
   if (!rc) rc = device_err_result(ctx, e);
   if (rc) cudaStreamSynchronize(ctx->stream);  // no copy outlives the call
   return rc;
+}
+
+int bromoc_gpu_set_profiles(bromoc_ctx *ctx, int32_t qrho, int32_t qrdna, int32_t qgr,
+                            int32_t igr, double dr, int32_t npoints) {
+  if (!ctx) return BROMOC_E_ARG;
+  if (!ctx->have_sys || !ctx->have_types)
+    return set_err(ctx, BROMOC_E_STATE, "set_profiles: set_system and set_types first");
+  if (npoints < 1 || (qgr && (!(dr > 0.0) || igr < 1 || igr > ctx->kp.cap)))
+    return set_err(ctx, BROMOC_E_ARG, "set_profiles: npoints, dr or igr out of range");
+  CU(cudaStreamSynchronize(ctx->stream));
+  ProfArgs &a = ctx->prof;
+  for (void *q : {(void *)a.rho_n, (void *)a.rdna_n, (void *)a.gr_n, (void *)a.irmax})
+    dfree(ctx, q);
+  a = ProfArgs{};
+  ctx->prof_on = false;
+  if (!qrho && !qrdna && !qgr) return BROMOC_OK;
+  const KP &p = ctx->kp;
+  // simul1.f90:179-188
+  a.zmini = p.lz2m;
+  a.idelz = 2.0;
+  a.nzmax = std::min((int)(p.lz * a.idelz), (int)npoints);
+  a.rho = qrho != 0;
+  a.rdna = qrdna != 0 && p.nsites > 0;
+  a.gr = qgr != 0;
+  a.igr = igr - 1;
+  a.dr = dr;
+  a.npoints = npoints;
+  const int nion_t = ctx->ntype - ctx->nold;
+  int rc = dalloc(ctx, &a.rho_n, (size_t)std::max(nion_t, 1) * std::max(a.nzmax, 1));
+  if (!rc) rc = dalloc(ctx, &a.rdna_n, (size_t)std::max(ctx->ndna, 1) * std::max(a.nzmax, 1));
+  if (!rc) rc = dalloc(ctx, &a.gr_n, (size_t)std::max(nion_t, 1) * npoints);
+  if (!rc) rc = dalloc(ctx, &a.irmax, 1);
+  if (rc) return rc;
+  CU(cudaMemset(a.rho_n, 0, (size_t)std::max(nion_t, 1) * std::max(a.nzmax, 1) * 8));
+  CU(cudaMemset(a.rdna_n, 0, (size_t)std::max(ctx->ndna, 1) * std::max(a.nzmax, 1) * 8));
+  CU(cudaMemset(a.gr_n, 0, (size_t)std::max(nion_t, 1) * npoints * 8));
+  CU(cudaMemset(a.irmax, 0, sizeof(int)));
+  ctx->prof_on = true;
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_accum_profiles(bromoc_ctx *ctx) {
+  if (!ctx) return BROMOC_E_ARG;
+  if (!ctx->prof_on) return set_err(ctx, BROMOC_E_STATE, "accum_profiles: set_profiles first");
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  launch_profiles(ctx->kp, ctx->precision == BROMOC_FP32, ntot_ub(ctx), ctx->prof, ctx->stream);
+  ++ctx->launches;
+  CU(cudaGetLastError());
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_get_profiles(bromoc_ctx *ctx, double *rho, double *rdna, double *gr,
+                            int32_t *nzmax, int32_t *irmax) {
+  if (!ctx) return BROMOC_E_ARG;
+  if (!ctx->prof_on) return set_err(ctx, BROMOC_E_STATE, "get_profiles: set_profiles first");
+  const ProfArgs &a = ctx->prof;
+  const int nion_t = ctx->ntype - ctx->nold;
+  auto fetch = [&](const unsigned long long *src, size_t n, double *dst) -> int {
+    if (!dst || !src || n == 0) return BROMOC_OK;
+    std::vector<unsigned long long> h(n);
+    CU(cudaMemcpyAsync(h.data(), src, n * 8, cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+    for (size_t k = 0; k < n; ++k) dst[k] = (double)h[k];
+    return BROMOC_OK;
+  };
+  int rc = fetch(a.rho_n, a.rho ? (size_t)nion_t * a.nzmax : 0, rho);
+  if (!rc) rc = fetch(a.rdna_n, a.rdna ? (size_t)ctx->ndna * a.nzmax : 0, rdna);
+  if (!rc) rc = fetch(a.gr_n, a.gr ? (size_t)nion_t * a.npoints : 0, gr);
+  if (rc) return rc;
+  if (nzmax) *nzmax = a.nzmax;
+  if (irmax) {
+    CU(cudaMemcpyAsync(irmax, a.irmax, sizeof(int), cudaMemcpyDeviceToHost, ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_traj_header(int32_t nframe, int32_t nttyp, const char *atnam, void *buf,
+                           int64_t cap, int64_t *nbytes) {
+  if (nttyp < 0 || (nttyp > 0 && !atnam) || !nbytes) return BROMOC_E_ARG;
+  const int64_t n = 12 + 12 + 8 + 4 * (int64_t)nttyp;
+  *nbytes = n;
+  if (!buf) return BROMOC_OK;  // size query
+  if (cap < n) return BROMOC_E_ARG;
+  uint8_t *b = (uint8_t *)buf;
+  const int32_t w[6] = {4, nframe, 4, 4, nttyp, 4};
+  std::memcpy(b, w, 24);
+  const int32_t L = 4 * nttyp;
+  std::memcpy(b + 24, &L, 4);
+  if (nttyp) std::memcpy(b + 28, atnam, 4 * (size_t)nttyp);
+  std::memcpy(b + 28 + 4 * (size_t)nttyp, &L, 4);
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_traj_frame(bromoc_ctx *ctx, double runtime, void *buf, int64_t cap,
+                          int64_t *nbytes) {
+  if (!ctx || !nbytes) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if ((rc = sync_ntot(ctx))) return rc;
+  const int n = ctx->ntot_known;
+  const long long nb = 60 + 16 * (long long)n;
+  *nbytes = nb;
+  if (!buf) return BROMOC_OK;  // size query
+  if (cap < nb) return set_err(ctx, BROMOC_E_ARG, "traj_frame: buffer holds %lld of %lld bytes",
+                               (long long)cap, nb);
+  if (nb > ctx->traj_cap) {
+    dfree(ctx, ctx->traj_w);
+    ctx->traj_w = nullptr;
+    ctx->traj_cap = 0;
+    if ((rc = dalloc(ctx, &ctx->traj_w, (size_t)(nb / 4)))) return rc;
+    ctx->traj_cap = nb;
+  }
+  launch_traj_pack(ctx->kp, ctx->precision == BROMOC_FP32, n, runtime, ctx->traj_w,
+                   ctx->stream);
+  ++ctx->launches;
+  CU(cudaGetLastError());
+  CU(cudaMemcpyAsync(buf, ctx->traj_w, (size_t)nb, cudaMemcpyDeviceToHost, ctx->stream));
+  CU(cudaStreamSynchronize(ctx->stream));
+  return check_device_err(ctx);
 }
 
 int bromoc_gpu_get_dids(bromoc_ctx *ctx, double *dids) {

@@ -18,7 +18,7 @@ namespace bgpu {
 constexpr double kPi = 3.14159265358979323846264338327950288419716939937510;
 constexpr double kTwoPi = 2.0 * kPi;
 constexpr double kRsmall = 1E-3;  // constamod.f90:83
-constexpr int kNTerms = 14;       // BROMOC_NTERMS
+constexpr int kNTerms = 23;       // BROMOC_NTERMS
 constexpr int kMaxBuffers = 64;
 constexpr int kMaxTypes = 64;
 constexpr int kIonTabTypes = 16;  // ion types of the shared-memory pair table

@@ -587,8 +587,10 @@ __global__ void __launch_bounds__(256) k_ereduce(KP p, int nslot, int rfpar_on) 
     double o[kNTerms];
     for (int k = 0; k < kNTerms; ++k) o[k] = tot[k];
     o[11] = rfpar_on ? o[13] : 0.0;  // egsbpb = erfpar
-    o[0] = o[9] + o[10] + o[12] + o[13] + o[1] + o[2] + o[3] + o[7] + o[5] +
-           o[6] + o[4] + o[8];
+    // energy.mono.f90:689: ..., esrpmfmx, ebond .. esolv, eqqmx, evdwmx,
+    // eefpot, eefpotmx, econ
+    o[0] = o[9] + o[10] + o[12] + o[13] + o[1] + o[2] + o[3] + o[7] + o[14] + o[15] +
+           o[16] + o[17] + o[18] + o[19] + o[20] + o[21] + o[5] + o[6] + o[4] + o[8] + o[22];
     for (int k = 0; k < kNTerms; ++k) p.eterms[k] = o[k];
   }
 }
@@ -673,6 +675,20 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
     slot += nb;
     nk += qforces ? 2 : 1;
   }
+  if (plan.nuc) {  // DNA bonded and Go-like terms, after the ion-site forces
+    const bool is_ran = nonbond && p.nsites > 0 && nub > p.nsites;
+    if (qforces && !is_ran && nub > p.nsites)  // fis holds the site terms alone
+      for (int k = 0; k < 3; ++k) {
+        if (plan.fp32)
+          cudaMemsetAsync(p.fis_f + (size_t)k * p.cap + p.nsites, 0,
+                          (size_t)(nub - p.nsites) * sizeof(float), stream);
+        else
+          cudaMemsetAsync(p.fis + (size_t)k * p.cap + p.nsites, 0,
+                          (size_t)(nub - p.nsites) * sizeof(double), stream);
+      }
+    nk += launch_nucl(p, plan.fp32, mask, qforces, is_ran ? 1 : 0, slot, stream);
+    ++slot;
+  }
   if (!plan.fp32 && (mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0) {
     dim3 g((nub - p.nsites + kPairThreads - 1) / kPairThreads, plan.nchunk_rf);
     if (plan.t_rf) cudaEventRecord(plan.t_rf->a, stream);
@@ -705,6 +721,7 @@ int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {
   }
   if ((mask & 1u) && p.nsites > 0 && nub > p.nsites)
     slot += (nub - p.nsites + kPairThreads - 1) / kPairThreads;
+  if (plan.nuc) ++slot;
   if (!plan.fp32 && (mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0)
     slot += ((nub - p.nsites + kPairThreads - 1) / kPairThreads) * plan.nchunk_rf;
   return slot;

@@ -78,6 +78,29 @@ struct TrialFF {
 };
 static_assert(sizeof(TrialFF) % 8 == 0 && alignof(TrialFF) == 8, "TrialFF is read as uint2");
 
+// DNA bonded and Go-like terms between sites (nucleotmod.f90), as one term
+// list in kind order: bond, angle, torsion, stack, base pair, excluded
+// volume, P-P electrostatics, solvent, applied force (APFOR).
+constexpr int kNucKinds = 9;
+struct NucDev {
+  int nterm;                    // 0: none
+  int off[kNucKinds + 1];       // first term of each kind
+  const int4 *site;             // [nterm] 0-based sites (-1 unused); base pair: .z = G-C
+  const double *par;            // [nterm] d0, theta0, phi0 or sigma
+  const double *af;             // [3*afn] applied forces
+  double *te;                   // [nterm] term energies
+  double *tf;                   // [nterm*4*3] force of term t on its site m at (4t+m)*3
+  const int *csr_start;         // [nsites+1] each site's entries in csr_ent
+  const int *csr_ent;           // entries 4t+m in ascending t
+  double epsnuc, scalepairing, fctn, kappa, ikappa, epsolv;
+  int qdeby, qsolv;
+  int ctn, qunsplit, nsites1st;
+  const int *csn;               // [ctn] CONTRANS site (1-based) or 0 for the centre
+  const double *ck;             // [3*ctn] (kx, ky, kz) per entry
+  const double *cc;             // [3*(ctn+1)] anchors (x, y, z) per entry
+  double *cf;                   // [8] centre force per strand and axis, econ
+};
+
 struct KP {
   // ---- sizes (host-known) ----
   int cap, nsites, nfix, ntype, nold, nttyp, ndna, ntc;
@@ -126,6 +149,7 @@ struct KP {
   const double *sitecharge;
   const uint8_t *stfree;
   const int *site_map;    // [nsites] nmcden map or nullptr
+  NucDev nuc;
   // ---- static field ----
   int qphix;
   Grid3 g1;

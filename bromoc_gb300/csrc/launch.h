@@ -17,6 +17,7 @@ struct EnergyPlan {
   bool fp32;
   bool cells = false; // FP32 extension mode: the cell-list pair kernel
   bool reduce_energy; // launch the final energy reduction
+  bool nuc = false;   // DNA bonded/Go terms (nucl.cu)
   KTimer *t_pairs = nullptr, *t_rf = nullptr, *t_fields = nullptr;
 };
 
@@ -54,6 +55,29 @@ struct AssembleFlags {
   int ntile;          // FP32: partials are per tile pair (Newton-3 kernel)
   int rf_ab;          // FP32 Newton-3: add A sd1 + B sd2 of the RFPAR chain
 };
+
+// analysis.cu: per-cycle profiles (counts) and .btr frames
+struct ProfArgs {
+  int rho, rdna, gr;        // which profiles accumulate
+  double zmini, idelz;      // z bins: iz = int((z - zmini) idelz) + 1
+  int nzmax;
+  int igr, npoints;         // RDF centre (0-based) and shells
+  double dr;
+  unsigned long long *rho_n, *rdna_n, *gr_n;  // [(ntype-nold)*nzmax], [ndna*nzmax], [(ntype-nold)*npoints]
+  int *irmax;
+};
+void launch_profiles(const KP &p, bool fp32, int ntot_ub, const ProfArgs &a,
+                     cudaStream_t stream);
+void launch_traj_pack(const KP &p, bool fp32, int n, double runtime, uint32_t *w,
+                      cudaStream_t stream);
+
+// nucl.cu: DNA bonded and Go-like terms; forces into fis / fis_f of the
+// sites (added when accum, else written), energies into one slot
+int launch_nucl(const KP &p, bool fp32, uint32_t mask, int qforces, int accum, int slot,
+                cudaStream_t stream);
+// INTERACT of site j (0-based): adds its bonded/Go terms to *dener
+void launch_nucl_interact(const KP &p, uint32_t mask, int j, double *dener,
+                          cudaStream_t stream);
 
 // fields.cu: single-particle terms, one warp per particle
 int fields_blocks(int ntot_ub);

@@ -79,6 +79,7 @@ class SystemSpec:
     # sites
     site_types: np.ndarray | None = None    # [nsites] combined type 1..ndna
     site_free: np.ndarray | None = None
+    nucl: object = None           # nucleotides.Topology: bonded and Go-like terms
     # maps
     phix: tuple | None = None     # (grid dict, float32[n])
     phiv: tuple | None = None     # (grid dict, int8[nmaps*n], opts dict)
@@ -257,6 +258,7 @@ class SystemSpec:
 
         nt, ntype = self.nttyp, self.ntype
         eng.nttyp, eng.ntype, eng.nold = nt, ntype, self.nold
+        eng.ndna = self.ndna
         self._builder = eng.efpot_from_knots
         sysd = self.system_struct()
         eng.call("set_system", C.byref(sysd))
@@ -307,6 +309,8 @@ class SystemSpec:
                           charge=ptr(sq, C.c_double), stfree=ptr(sf, C.c_uint8),
                           phiv_map=None)
         eng.call("set_sites", C.byref(sites))
+        if ns and self.nucl is not None:
+            eng.set_nucleotides(self.nucl)
         if self.phix is not None:
             g, data = self.phix
             data = k(np.ascontiguousarray(data, np.float32))

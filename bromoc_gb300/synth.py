@@ -7,7 +7,7 @@ each workload is generated from a seed with the stated shapes and sizes:
   pore     : 120x120x180 maps at 1 A (static field = 1 V drop + Gaussians,
              RFPAR Born-like wall penalty, repulsion slab with a 10 A pore),
              ~2000 ions, GCMC buffers at both ends
-  ssdna    : 40 nt x 3 sites (P, S, base) along the pore axis plus ~5000 ions
+  ssdna    : 40 nt x 3 sites (base, S, P) along the pore axis plus ~5000 ions
              with tabulated ion-site effective potentials
 """
 from __future__ import annotations
@@ -16,7 +16,7 @@ import math
 
 import numpy as np
 
-from . import abi
+from . import abi, nucleotides
 from .deck import CELEC, SystemSpec
 
 # KCl parameters of the bulk workload
@@ -272,9 +272,13 @@ def efpot_knots(rng, sigma, eps, r0=2.0, r1=20.0, res=0.05):
     return r, u
 
 
-def ssdna(seed=4, nions=5000, nnuc=40, maps=None, precision=abi.FP32, **kw):
-    """Single-stranded DNA (P, S, base per nucleotide) held along the pore
-    axis, immersed in KCl; ion-site pairs use tabulated potentials."""
+def ssdna(seed=4, nions=5000, nnuc=40, maps=None, precision=abi.FP32, bonded=False,
+          free=False, **kw):
+    """Single-stranded DNA (base, S, P per nucleotide, the site order of
+    bonds.f90) along the pore axis, immersed in KCl; ion-site pairs use
+    tabulated potentials.  bonded: the bonded and Go-like terms of the strand
+    (nucleotides.build_topology on the initial coordinates as the native
+    structure); free: the sites move (else FIXSITE)."""
     rng = np.random.default_rng(seed)
     s = pore(seed=seed + 7, nions=nions, maps=maps, precision=precision,
              buffers=False, **kw)
@@ -287,13 +291,18 @@ def ssdna(seed=4, nions=5000, nnuc=40, maps=None, precision=abi.FP32, **kw):
     for k in range(nnuc):
         z = z0 + 3.4 * k
         ang = 0.6 * k
-        types += [2, 1, int(bases[k])]
-        pos += [(8.0 * math.cos(ang), 8.0 * math.sin(ang), z),
+        types += [int(bases[k]), 1, 2]
+        pos += [(2.0 * math.cos(ang + 0.5), 2.0 * math.sin(ang + 0.5), z + 1.2),
                 (5.5 * math.cos(ang + 0.3), 5.5 * math.sin(ang + 0.3), z + 1.0),
-                (2.0 * math.cos(ang + 0.5), 2.0 * math.sin(ang + 0.5), z + 1.2)]
+                (8.0 * math.cos(ang), 8.0 * math.sin(ang), z)]
     pos = np.array(pos)
     s.site_types = np.array(types, np.int32)
-    s.site_free = np.zeros(len(types), np.uint8)  # held in place (FIXSITE)
+    s.site_free = np.full(len(types), 1 if free else 0, np.uint8)
+    if bonded:
+        names = [s.site_type_names[t - 1] for t in types]
+        s.nucl = nucleotides.build_topology(
+            names, np.ones(len(types), np.int32), pos,
+            fctn=CELEC * s.cgnuc ** 2 / s.cdie)
     # drop ions overlapping the strand
     ions = np.stack([s.x, s.y, s.z], 1)
     d2 = ((ions[:, None, :] - pos[None, :, :]) ** 2).sum(-1).min(1)

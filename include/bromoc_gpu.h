@@ -28,7 +28,7 @@
 extern "C" {
 #endif
 
-#define BROMOC_ABI_VERSION 1
+#define BROMOC_ABI_VERSION 2
 
 /* ---- status codes ------------------------------------------------------ */
 enum {
@@ -57,6 +57,16 @@ enum {
   BROMOC_EGSBPB,       /* reaction field (rfpar.f90 copies erfpar here)    */
   BROMOC_EVDWGD,       /* grid repulsion (vdwgd1trln/spln.f90)             */
   BROMOC_ERFPAR,       /* reaction-field parameters (rfpar.f90)            */
+  /* DNA bonded and Go-like terms (nucleotmod.f90:40-48) */
+  BROMOC_EBOND,        /* bond stretch                                     */
+  BROMOC_EANG,         /* bond angle                                       */
+  BROMOC_EDIHE,        /* torsion                                          */
+  BROMOC_ESTACK,       /* native contacts (stacking)                       */
+  BROMOC_EBP,          /* base-pair hydrogen bonds                         */
+  BROMOC_EEX,          /* excluded volume                                  */
+  BROMOC_EQQ,          /* phosphate-phosphate Coulomb / Debye-Hueckel      */
+  BROMOC_ESOLV,        /* solvent-induced                                  */
+  BROMOC_ECON,         /* harmonic position constraints (CONTRANS)         */
   BROMOC_NTERMS
 };
 
@@ -68,7 +78,8 @@ enum {
   BROMOC_M_PHIX = 1u << 2,    /* Qphix                                     */
   BROMOC_M_PHIV = 1u << 3,    /* Qphiv                                     */
   BROMOC_M_RFPAR = 1u << 4,   /* Qrfpar                                    */
-  BROMOC_M_ALL = 0x1fu
+  BROMOC_M_BOND = 1u << 5,    /* Qnobond: DNA bond, angle and torsion terms */
+  BROMOC_M_ALL = 0x3fu
 };
 
 enum { BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2 };
@@ -144,6 +155,52 @@ typedef struct bromoc_sites {
   const int32_t *phiv_map;   /* [nsites] nmcden repulsion map, or NULL       */
 } bromoc_sites;
 
+/* DNA bonded and Go-like terms between sites (nucleotmod.f90; the lists of
+ * bonds.f90, angles.f90, dihedral.f90 and go_qq.f90, the forms of
+ * energy.mono.f90:196-582).  Site numbers are 1-based; a term's sites are
+ * consecutive (sitebond[2k], sitebond[2k+1] are term k's two sites: the
+ * Fortran sitebond(k,1), sitebond(k,2)).  A count of 0 allows a NULL list.
+ *   bond      eps (d-d0)^2 (1 + 100 (d-d0)^2)
+ *   angle     700 eps (theta-theta0)^2
+ *   torsion   28 eps (1 - cos(phi-phi0))
+ *   stack     4 eps ((sg/d)^12 - (sg/d)^6)
+ *   base pair eps_bp (sg/d)^10 (20 (sg/d)^2 - 24), eps_bp = 2.532 eps s
+ *             for G-C (bpgc != 0) and 2 eps s otherwise, s = scalepairing
+ *   excluded  4 eps ((sg/d)^12 - (sg/d)^6) + eps for d < sg
+ *   qq        fctn/d, or fctn e^{-d/kappa}/d (qdeby 1, or qdeby 2 with both
+ *             sites outside the system, grandmod.f90:74-98)
+ *   solvent   epsolv (1 - e^{0.1875 (13.38-d)})^2 - epsolv
+ * Constant applied forces (APFOR) act on free sites; CONTRANS adds
+ * harmonic springs on single sites or on the sites' centre (csn 0). */
+typedef struct bromoc_nucleotides {
+  double epsnuc;             /* energy scale eps (kcal/mol)                  */
+  double scalepairing;       /* base-pair scale s                            */
+  double fctn;               /* celec cgnuc^2 / cdie                         */
+  double kappa;              /* Debye length (A), qdeby != 0                 */
+  int32_t qdeby;             /* 0 Coulomb, 1 Debye-Hueckel, 2 hybrid         */
+  int32_t qsolv;             /* solvent-induced S-S terms                    */
+  double epsolv;
+  int32_t nbond;   const int32_t *sitebond;  const double *distbond; /* d0 */
+  int32_t nangle;  const int32_t *siteangle; const double *valangle; /* rad, */
+                                             /* middle site is the vertex  */
+  int32_t ndihe;   const int32_t *sitedihe;  const double *valdihe;  /* rad */
+  int32_t nstack;  const int32_t *sitestack; const double *sgstack;
+  int32_t nbp;     const int32_t *sitebp;    const double *sgbp;
+  const uint8_t *bpgc;       /* [nbp] first site is a G or C base            */
+  int32_t nex;     const int32_t *siteex;    const double *sgex;
+  int32_t nqq;     const int32_t *siteqq;
+  int32_t nsolv;   const int32_t *siteslv;
+  int32_t afn;     const int32_t *sn;        /* APFOR sites                  */
+  const double *af;          /* [3*afn] force on site sn[k] (kcal/mol/A)     */
+  int32_t ctn;               /* CONTRANS entries                             */
+  const int32_t *csn;        /* [ctn] site, or 0 for the sites' centre       */
+  const double *kx, *ky, *kz;          /* [ctn] spring constants             */
+  const double *contrx, *contry, *contrz; /* [ctn+1] anchors; entry ctn is  */
+                                       /* the second strand's centre (unsplit) */
+  int32_t qunsplit;          /* centre springs per strand (two strands)      */
+  int32_t nsites1st;         /* sites of the first strand                    */
+} bromoc_nucleotides;
+
 /* Grid header of a PB map file: readphi.f90:43-52 (z fastest, x slowest). */
 typedef struct bromoc_grid {
   int32_t nclx, ncly, nclz;
@@ -212,6 +269,11 @@ int bromoc_gpu_set_system(bromoc_ctx *ctx, const bromoc_system *sys);
 int bromoc_gpu_set_types(bromoc_ctx *ctx, const bromoc_types *types);
 int bromoc_gpu_set_pairs(bromoc_ctx *ctx, const bromoc_pairs *pairs);
 int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *sites);
+/* DNA bonded and Go-like term lists (after set_sites; NULL clears them).
+ * ENERGY adds them to the site forces and to ener; INTERACT of a site adds
+ * the terms that involve it (interact.f90:211-334, with its base-pair
+ * scale of 1). */
+int bromoc_gpu_set_nucleotides(bromoc_ctx *ctx, const bromoc_nucleotides *nuc);
 /* static field phix (readphi PHIX, gsbpmod phix) -- staticf1/staticf0 */
 int bromoc_gpu_set_phix(bromoc_ctx *ctx, const bromoc_grid *g,
                         const float *phix);
@@ -412,6 +474,38 @@ int bromoc_gpu_get_countions(bromoc_ctx *ctx, int32_t *nforward,
 /* Per-particle PROXDIFF nearest-site record dids(5,ntot) of the last
  * ENERGY call (energy.mono.f90:603-621), 5 doubles per particle. */
 int bromoc_gpu_get_dids(bromoc_ctx *ctx, double *dids);
+
+/* ---- per-cycle analysis (simul1.f90:176-188, 476-509) ---------------------
+ * Switch the z-density profile of the mobile ions (qrho, RHO), of the DNA
+ * sites (qrdna, RHDNA) and the radial distribution of the mobile ions
+ * around particle igr (1-based; qgr, RDF, shells of dr, npoints of them),
+ * and clear their counts.  z bins as the reference: from the system's lower
+ * z face, 0.5 A wide, nzmax = min(int(2 lz), npoints).  A particle below
+ * the first bin is not counted (the reference writes outside its array). */
+int bromoc_gpu_set_profiles(bromoc_ctx *ctx, int32_t qrho, int32_t qrdna,
+                            int32_t qgr, int32_t igr, double dr,
+                            int32_t npoints);
+/* One sample from the current state, queued without a wait
+ * (bromoc_gpu_simul_cycles_host takes one per cycle itself). */
+int bromoc_gpu_accum_profiles(bromoc_ctx *ctx);
+/* The sums so far (counts, as the reference's sums of 1.0); any output may
+ * be NULL: rho[(itype-nold-1)*nzmax + iz-1], rdna[(typtyp-1)*nzmax + iz-1],
+ * gr[(itype-nold-1)*npoints + ir-1], the bin count and the RDF's irmax. */
+int bromoc_gpu_get_profiles(bromoc_ctx *ctx, double *rho, double *rdna,
+                            double *gr, int32_t *nzmax, int32_t *irmax);
+
+/* ---- trajectory (.btr: simul1.f90:283-287, wrttraj.f90:33-38) -------------
+ * The bytes of gfortran unformatted sequential records, each framed by
+ * 4-byte length markers, for the caller to append to the file.  With
+ * buf == NULL only *nbytes is set (the size needed).
+ * Header: nframe, nttyp, atnam2(1:nttyp) (character*4 each). */
+int bromoc_gpu_traj_header(int32_t nframe, int32_t nttyp, const char *atnam,
+                           void *buf, int64_t cap, int64_t *nbytes);
+/* One frame of the current state, packed on the device: runtime (real*8),
+ * ntot, typtyp(1:ntot) (ions: nwtype(|typei|)), then x, y and z rounded to
+ * single precision (sng).  60 + 16 ntot bytes. */
+int bromoc_gpu_traj_frame(bromoc_ctx *ctx, double runtime, void *buf,
+                          int64_t cap, int64_t *nbytes);
 
 /* ---- effective-potential table build (setup; polynom.f90, splinepot.f90,
  * discretize.f90).  Host-side C++; writes the quadratic pieces of one pair

@@ -24,15 +24,17 @@ module bromoc_gpu
        BROMOC_E_STATE = 2, BROMOC_E_CUDA = 3, BROMOC_E_CAPACITY = 4, &
        BROMOC_E_NOMEM = 5, BROMOC_E_DEVICE = 6
   integer(c_int32_t), parameter :: BROMOC_M_NONBOND = 1, BROMOC_M_MEMB = 2, &
-       BROMOC_M_PHIX = 4, BROMOC_M_PHIV = 8, BROMOC_M_RFPAR = 16, BROMOC_M_ALL = 31
+       BROMOC_M_PHIX = 4, BROMOC_M_PHIV = 8, BROMOC_M_RFPAR = 16, BROMOC_M_BOND = 32, &
+       BROMOC_M_ALL = 63
   integer(c_int32_t), parameter :: BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2
   integer(c_int32_t), parameter :: BROMOC_FP64 = 0, BROMOC_FP32 = 1
   integer(c_int32_t), parameter :: BROMOC_DYN0 = 0, BROMOC_DYN1 = 1, &
        BROMOC_DYN2 = 2, BROMOC_DYN3 = 3
   ! energy term slots of eterms(1:BROMOC_NTERMS): ener, eelec, evdw, esrpmf,
   ! eefpot, eqqmx, evdwmx, esrpmfmx, eefpotmx, ememb, egsbpa, egsbpb, evdwgd,
-  ! erfpar (1-based here: slot k of the header is eterms(k+1))
-  integer(c_int32_t), parameter :: BROMOC_NTERMS = 14
+  ! erfpar, ebond, eang, edihe, estack, ebp, eex, eqq, esolv, econ
+  ! (1-based here: slot k of the header is eterms(k+1))
+  integer(c_int32_t), parameter :: BROMOC_NTERMS = 23
 
   type, bind(C) :: bromoc_system
     integer(c_int32_t) :: shape
@@ -82,6 +84,54 @@ module bromoc_gpu
     type(c_ptr) :: stfree
     type(c_ptr) :: phiv_map
   end type bromoc_sites
+
+  ! nucleotmod's term lists; site lists are term-major (sitebond(2,nbond) on
+  ! the Fortran side, i.e. transpose(sitebond(1:nbond,1:2)))
+  type, bind(C) :: bromoc_nucleotides
+    real(c_double) :: epsnuc
+    real(c_double) :: scalepairing
+    real(c_double) :: fctn
+    real(c_double) :: kappa
+    integer(c_int32_t) :: qdeby
+    integer(c_int32_t) :: qsolv
+    real(c_double) :: epsolv
+    integer(c_int32_t) :: nbond
+    type(c_ptr) :: sitebond
+    type(c_ptr) :: distbond
+    integer(c_int32_t) :: nangle
+    type(c_ptr) :: siteangle
+    type(c_ptr) :: valangle
+    integer(c_int32_t) :: ndihe
+    type(c_ptr) :: sitedihe
+    type(c_ptr) :: valdihe
+    integer(c_int32_t) :: nstack
+    type(c_ptr) :: sitestack
+    type(c_ptr) :: sgstack
+    integer(c_int32_t) :: nbp
+    type(c_ptr) :: sitebp
+    type(c_ptr) :: sgbp
+    type(c_ptr) :: bpgc
+    integer(c_int32_t) :: nex
+    type(c_ptr) :: siteex
+    type(c_ptr) :: sgex
+    integer(c_int32_t) :: nqq
+    type(c_ptr) :: siteqq
+    integer(c_int32_t) :: nsolv
+    type(c_ptr) :: siteslv
+    integer(c_int32_t) :: afn
+    type(c_ptr) :: sn
+    type(c_ptr) :: af
+    integer(c_int32_t) :: ctn
+    type(c_ptr) :: csn
+    type(c_ptr) :: kx
+    type(c_ptr) :: ky
+    type(c_ptr) :: kz
+    type(c_ptr) :: contrx
+    type(c_ptr) :: contry
+    type(c_ptr) :: contrz
+    integer(c_int32_t) :: qunsplit
+    integer(c_int32_t) :: nsites1st
+  end type bromoc_nucleotides
 
   type, bind(C) :: bromoc_grid
     integer(c_int32_t) :: nclx, ncly, nclz
@@ -177,6 +227,13 @@ module bromoc_gpu
       import :: c_int, c_ptr, bromoc_sites
       type(c_ptr), value :: ctx
       type(bromoc_sites), intent(in) :: s
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_set_nucleotides(ctx, nuc) bind(C, name="bromoc_gpu_set_nucleotides") &
+         result(rc)
+      import :: c_int, c_ptr, bromoc_nucleotides
+      type(c_ptr), value :: ctx
+      type(bromoc_nucleotides), intent(in) :: nuc
       integer(c_int) :: rc
     end function
     function bromoc_gpu_set_phix(ctx, g, phix) bind(C, name="bromoc_gpu_set_phix") result(rc)
@@ -350,6 +407,48 @@ module bromoc_gpu
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: dids(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_set_profiles(ctx, qrho, qrdna, qgr, igr, dr, npoints) &
+         bind(C, name="bromoc_gpu_set_profiles") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: qrho, qrdna, qgr, igr
+      real(c_double), value :: dr
+      integer(c_int32_t), value :: npoints
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_accum_profiles(ctx) bind(C, name="bromoc_gpu_accum_profiles") result(rc)
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_get_profiles(ctx, rho, rdna, gr, nzmax, irmax) &
+         bind(C, name="bromoc_gpu_get_profiles") result(rc)
+      import :: c_int, c_ptr, c_double, c_int32_t
+      type(c_ptr), value :: ctx
+      real(c_double), intent(out) :: rho(*), rdna(*), gr(*)
+      integer(c_int32_t), intent(out) :: nzmax, irmax
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_traj_header(nframe, nttyp, atnam, buf, cap, nbytes) &
+         bind(C, name="bromoc_gpu_traj_header") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_int64_t, c_char
+      integer(c_int32_t), value :: nframe, nttyp
+      character(kind=c_char), intent(in) :: atnam(*)
+      type(c_ptr), value :: buf
+      integer(c_int64_t), value :: cap
+      integer(c_int64_t), intent(out) :: nbytes
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_traj_frame(ctx, runtime, buf, cap, nbytes) &
+         bind(C, name="bromoc_gpu_traj_frame") result(rc)
+      import :: c_int, c_ptr, c_double, c_int64_t
+      type(c_ptr), value :: ctx
+      real(c_double), value :: runtime
+      type(c_ptr), value :: buf
+      integer(c_int64_t), value :: cap
+      integer(c_int64_t), intent(out) :: nbytes
       integer(c_int) :: rc
     end function
     function bromoc_gpu_efpot_from_knots(n, xx, yy, fct, qchr, ep, sc3, dm2o, dmio) &

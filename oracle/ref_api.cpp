@@ -155,10 +155,83 @@ int bromoc_ref_set_sites(bromoc_ref *r, const bromoc_sites *q) {
   if (!r || !q) return fail(r, "set_sites: null");
   State &s = r->s;
   s.nsites = q->nsites;
+  s.nuc = bref::Nucl{};  // the term lists name sites of the previous set
   s.typtyp = one_based(q->typtyp, q->nsites);
   s.sitecharge = one_based(q->charge, q->nsites);
   s.stfree = one_based(q->stfree, q->nsites);
   s.site_phiv_map = one_based(q->phiv_map, q->nsites);
+  return BROMOC_OK;
+}
+
+int bromoc_ref_set_nucleotides(bromoc_ref *r, const bromoc_nucleotides *q) {
+  if (!r) return BROMOC_E_ARG;
+  State &s = r->s;
+  s.nuc = bref::Nucl{};
+  if (!q) return BROMOC_OK;
+  const int ns = s.nsites;
+  bool bad = false;
+  auto list = [&](int n, const int32_t *v, int per, std::vector<int> &out) {
+    if (n < 0 || (n > 0 && !v)) bad = true;
+    if (bad || n <= 0) return;
+    out.assign(v, v + (size_t)n * per);
+    for (int k : out)
+      if (k < 1 || k > ns) bad = true;
+  };
+  auto vals = [&](int n, const double *v, std::vector<double> &out) {
+    if (n > 0 && !v) bad = true;
+    if (!bad && n > 0) out.assign(v, v + n);
+  };
+  bref::Nucl &n = s.nuc;
+  list(q->nbond, q->sitebond, 2, n.bond);
+  vals(q->nbond, q->distbond, n.distbond);
+  list(q->nangle, q->siteangle, 3, n.angle);
+  vals(q->nangle, q->valangle, n.valangle);
+  list(q->ndihe, q->sitedihe, 4, n.dihe);
+  vals(q->ndihe, q->valdihe, n.valdihe);
+  list(q->nstack, q->sitestack, 2, n.stack);
+  vals(q->nstack, q->sgstack, n.sgstack);
+  list(q->nbp, q->sitebp, 2, n.bp);
+  vals(q->nbp, q->sgbp, n.sgbp);
+  if (q->nbp > 0 && !q->bpgc) bad = true;
+  if (!bad && q->nbp > 0) n.bpgc.assign(q->bpgc, q->bpgc + q->nbp);
+  list(q->nex, q->siteex, 2, n.ex);
+  vals(q->nex, q->sgex, n.sgex);
+  list(q->nqq, q->siteqq, 2, n.qq);
+  list(q->nsolv, q->siteslv, 2, n.slv);
+  list(q->afn, q->sn, 1, n.sn);
+  if (q->afn > 0 && !q->af) bad = true;
+  if (!bad && q->afn > 0) n.af.assign(q->af, q->af + 3 * (size_t)q->afn);
+  if (q->ctn < 0 || (q->ctn > 0 && (!q->csn || !q->kx || !q->ky || !q->kz || !q->contrx ||
+                                     !q->contry || !q->contrz)))
+    bad = true;
+  if (!bad && q->ctn > 0) {
+    n.csn.assign(q->csn, q->csn + q->ctn);
+    for (int k : n.csn)
+      if (k < 0 || k > ns) bad = true;
+    n.kx.assign(q->kx, q->kx + q->ctn);
+    n.ky.assign(q->ky, q->ky + q->ctn);
+    n.kz.assign(q->kz, q->kz + q->ctn);
+    n.contrx.assign(q->contrx, q->contrx + q->ctn + 1);
+    n.contry.assign(q->contry, q->contry + q->ctn + 1);
+    n.contrz.assign(q->contrz, q->contrz + q->ctn + 1);
+  }
+  if (q->qunsplit && (q->nsites1st < 1 || q->nsites1st >= ns)) bad = true;
+  if (q->qdeby && !(q->kappa > 0.0)) bad = true;
+  if (bad || ns <= 0) {
+    s.nuc = bref::Nucl{};
+    return fail(r, "set_nucleotides: bad list, site number or count");
+  }
+  n.epsnuc = q->epsnuc;
+  n.scalepairing = q->scalepairing;
+  n.fctn = q->fctn;
+  n.kappa = q->kappa;
+  n.ikappa = q->qdeby ? 1.0 / q->kappa : 0.0;
+  n.qdeby = q->qdeby;
+  n.qsolv = q->qsolv != 0;
+  n.epsolv = q->epsolv;
+  n.qunsplit = q->qunsplit != 0;
+  n.nsites1st = q->nsites1st;
+  n.on = true;
   return BROMOC_OK;
 }
 
@@ -346,6 +419,15 @@ static void terms_out(const State &s, double *e) {
   e[BROMOC_EGSBPB] = s.egsbpb;
   e[BROMOC_EVDWGD] = s.evdwgd;
   e[BROMOC_ERFPAR] = s.erfpar;
+  e[BROMOC_EBOND] = s.ebond;
+  e[BROMOC_EANG] = s.eang;
+  e[BROMOC_EDIHE] = s.edihe;
+  e[BROMOC_ESTACK] = s.estack;
+  e[BROMOC_EBP] = s.ebp;
+  e[BROMOC_EEX] = s.eex;
+  e[BROMOC_EQQ] = s.eqq;
+  e[BROMOC_ESOLV] = s.esolv;
+  e[BROMOC_ECON] = s.econ;
 }
 
 static bool ready(bromoc_ref *r) {

@@ -665,7 +665,7 @@ void rfparionj(State &s, double xj, double yj, double zj, int j, int jtype) {
   }
 }
 
-// interact.f90:19-419 (DNA bonded/Go terms excluded)
+// interact.f90:19-419
 void interact(State &s, uint32_t mask, double &dener, double xj, double yj,
               double zj, int jtype, int j, bool qalert) {
   dener = 0.0;
@@ -784,6 +784,8 @@ void interact(State &s, uint32_t mask, double &dener, double xj, double yj,
       }
     }
   }
+  // DNA bonded and Go-like terms of site j: interact.f90:211-334
+  if (s.qnucl() && !beion) nucl_interact(s, mask, j, dener);
   if (s.qpar() && s.qnucl() && Qnonbond) {
     auto pairlaw = [&](int is, double dist2) {
       if (s.qefpot[is]) {

@@ -382,7 +382,7 @@ static void ionion_range(const State &s, int jlo, int jhi, bool qforces,
   }
 }
 
-// ---- ENERGY: energy.mono.f90:19-692 (DNA bonded/Go terms excluded) -------
+// ---- ENERGY: energy.mono.f90:19-692 ---------------------------------------
 void energy(State &s, uint32_t mask, bool qforces) {
   s.ener = s.eelec = s.eefpot = s.eefpotmx = s.evdw = s.esrpmf = s.esrpmfmx =
       s.ememb = s.egsbpa = s.egsbpb = s.evdwgd = s.eqqmx = s.evdwmx = 0.0;
@@ -461,6 +461,8 @@ void energy(State &s, uint32_t mask, bool qforces) {
     s.eefpot = el[3];
 #endif
   }
+  // DNA bonded and Go-like terms: energy.mono.f90:196-582
+  nucl_energy(s, mask, qforces);
 
   // dids(1:5, nsites+1:ntot) = 0 (energy.mono.f90:583)
   for (int i = nsites + 1; i <= ntot; ++i)
@@ -563,8 +565,10 @@ void energy(State &s, uint32_t mask, bool qforces) {
       }
     }
   }
-  s.ener += s.eelec + s.evdw + s.esrpmf + s.esrpmfmx + s.eqqmx + s.evdwmx +
-            s.eefpot + s.eefpotmx;
+  // energy.mono.f90:689
+  s.ener += s.eelec + s.evdw + s.esrpmf + s.esrpmfmx + s.ebond + s.eang + s.edihe +
+            s.estack + s.ebp + s.eex + s.eqq + s.esolv + s.eqqmx + s.evdwmx + s.eefpot +
+            s.eefpotmx + s.econ;
 }
 
 }  // namespace bref

@@ -53,6 +53,21 @@ struct Grid {
   void set(const bromoc_grid &g);
 };
 
+// DNA bonded and Go-like term lists (nucleotmod.f90), 1-based sites; a
+// term's sites are consecutive in its list
+struct Nucl {
+  bool on = false;
+  double epsnuc = 0, scalepairing = 1, fctn = 0, kappa = 0, ikappa = 0, epsolv = 0;
+  int qdeby = 0;
+  bool qsolv = false, qunsplit = false;
+  int nsites1st = 0;
+  std::vector<int> bond, angle, dihe, stack, bp, ex, qq, slv;
+  std::vector<double> distbond, valangle, valdihe, sgstack, sgbp, sgex;
+  std::vector<uint8_t> bpgc;
+  std::vector<int> sn, csn;
+  std::vector<double> af, kx, ky, kz, contrx, contry, contrz;
+};
+
 struct State {
   std::string err;
   double celec = celec_value();
@@ -134,6 +149,10 @@ struct State {
          eefpotmx = 0, ememb = 0, egsbpa = 0, egsbpb = 0, evdwgd = 0,
          erfpar = 0, eqqmx = 0, evdwmx = 0;
   std::vector<int> warn;  // 1-based by combined type
+  // DNA bonded / Go-like terms (nucleotmod)
+  Nucl nuc;
+  double ebond = 0, eang = 0, edihe = 0, estack = 0, ebp = 0, eex = 0, eqq = 0,
+         esolv = 0, econ = 0;
 
   bool qpar() const { return have_types && ntype > nold; }  // PARTICLES given
   // extension mode: nearest periodic image of a separation
@@ -161,6 +180,11 @@ void splinepot(int nn, const double *xx, const double *yy, double fct,
                bool qchr, double *p, double *sc3, double *dm2o, double *dmio);
 
 void energy(State &s, uint32_t mask, bool qforces);
+// grandmod.f90:74-98
+bool outbox(const State &s, double xi, double yi, double zi);
+// energy.mono.f90:196-582 and interact.f90:211-334 (ref_nucl.cpp)
+void nucl_energy(State &s, uint32_t mask, bool qforces);
+void nucl_interact(const State &s, uint32_t mask, int j, double &dener);
 void membrane(State &s, bool qforces);
 void staticf1(State &s, bool qforces);
 void vdwgd1trln(State &s, bool qforces);

@@ -3,7 +3,7 @@
 The reference (Fortran) cannot be built or imported here and ships no golden
 vectors, so these come from the FP64 CPU restatement in oracle/ on the seeded
 systems of tests/systems.py (the last of them in the periodic extension mode):
-for each term family the 14 ENERGY terms and the forces, the positions after
+for each term family the ENERGY terms (BROMOC_NTERMS of them) and the forces, the positions after
 two BD steps with the injected Philox noise, and
 for the GCMC system the buffer counters and particle count after five GRAND
 calls.  They pin the restatement (and, through the GPU tests, the FP64 GPU
@@ -34,6 +34,7 @@ def families():
         "maps_trln": systems.maps(),
         "maps_spln": systems.maps(trilinear=False),
         "dna": systems.dna(),
+        "dna_duplex": systems.dna_duplex(),
         "periodic": systems.periodic_kcl(),
     }
 

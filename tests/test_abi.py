@@ -27,7 +27,7 @@ def test_library_exports_every_symbol(gpu_lib):
     lib = gpu_lib.load()
     missing = [n for n in declared() if not hasattr(lib, n)]
     assert not missing, missing
-    assert lib.bromoc_gpu_abi_version() == 1
+    assert lib.bromoc_gpu_abi_version() == 2
 
 
 def test_null_arguments_rejected(gpu_lib):

@@ -18,9 +18,11 @@ F90 = (ROOT / "include" / "bromoc_gpu_mod.f90").read_text()
 
 # C scalar type -> kind class
 C_SCALAR = {"int32_t": "i32", "uint32_t": "i32", "int64_t": "i64", "uint64_t": "i64",
-            "double": "f64", "float": "f32", "int8_t": "i8", "uint8_t": "u8", "int": "i32"}
+            "double": "f64", "float": "f32", "int8_t": "i8", "uint8_t": "u8", "int": "i32",
+            "char": "i8"}
 F_KIND = {"integer(c_int32_t)": "i32", "integer(c_int)": "i32", "integer(c_int64_t)": "i64",
-          "real(c_double)": "f64", "real(c_float)": "f32", "integer(c_int8_t)": "i8"}
+          "real(c_double)": "f64", "real(c_float)": "f32", "integer(c_int8_t)": "i8",
+          "character(kind=c_char)": "i8"}
 OPAQUE = {"bromoc_ctx", "bromoc_batch", "bromoc_adj", "void"}
 
 

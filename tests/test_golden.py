@@ -12,7 +12,7 @@ from bromoc_gb300 import abi
 from .golden import make_golden as mg
 
 GOLD = np.load(Path(__file__).parent / "golden" / "golden.npz")
-FAMILIES = ["pairs", "efpot", "maps_trln", "maps_spln", "dna", "periodic"]
+FAMILIES = ["pairs", "efpot", "maps_trln", "maps_spln", "dna", "dna_duplex", "periodic"]
 
 
 def _scale(a):

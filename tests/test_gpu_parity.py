@@ -114,7 +114,7 @@ def test_interact(gpu_lib, oracle_mod, family):
         assert abs(a - b) <= FP64_TOL * max(1.0, abs(b)), (p, a, b)
 
 
-@pytest.mark.parametrize("family", ["pairs", "maps_trln", "maps_spln", "dna"])
+@pytest.mark.parametrize("family", ["pairs", "maps_trln", "maps_spln", "dna", "dna_duplex"])
 def test_bd_steps(gpu_lib, oracle_mod, family):
     """ENERGY + DYNAMICS: identical Philox noise on both sides, so positions
     agree to rounding after one step and stay close over ten."""

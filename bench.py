@@ -336,6 +336,59 @@ def c1_measure(sh, steps=C1_STEPS):
     return out
 
 
+C3_STEPS = 200
+
+
+def c3_measure(sh, steps=C3_STEPS):
+    """The ssDNA configuration: 40 nt x 3 sites (free, with their bonded and
+    Go-like terms) in the 120x120x180 pore maps with ~5000 K+/Cl-, FP32
+    pairs, dynamics0 / dynamics0nuc.  GPU: `steps` BD steps (ENERGY forces +
+    move, one launch per kernel and step: the fused loop takes systems
+    without sites), CUDA events after warm-up.  Error: forces of one ENERGY
+    against the FP64 oracle.  CPU: the oracle on all host threads, a bounded
+    sample of the same steps."""
+    import torch
+    from bromoc_gb300 import _lib
+    from oracle import oracle
+    spec = synth.ssdna(seed=4, nions=5000, nnuc=40, maps=synth.pore_maps(seed=102),
+                       precision=abi.FP32, bonded=True, free=True)
+    n = len(spec.x)
+    g = _lib.create(n + 16, abi.FP32, sh)
+    spec.push(g)
+    o = oracle.create(n + 16)
+    spec.push(o)
+    tg, fg, _ = g.energy(abi.M_ALL, forces=True)
+    to, fo, _ = o.energy(abi.M_ALL, forces=True)
+    fe, fw = _force_errs(np.asarray(fg)[:n], np.asarray(fo)[:n])
+    err = {"force_rel_err": fe, "force_worst_particle": fw,
+           "energy_rel_err": _energy_err(tg, to)}
+    del o
+    stream = torch.cuda.current_stream()
+    g.bd_steps(10, SEED, 0, energies=False)
+    a, e = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    torch.cuda.synchronize()
+    a.record(stream)
+    g.bd_steps(steps, SEED, 10, energies=False)
+    e.record(stream)
+    torch.cuda.synchronize()
+    ms = a.elapsed_time(e)
+    oc = oracle.create(n + 16, omp=True)
+    spec.push(oc)
+    ncpu, t0 = 0, time.perf_counter()
+    while time.perf_counter() - t0 < 3.0:
+        oc.bd_steps(2, SEED, ncpu, energies=False)
+        ncpu += 2
+    dt = time.perf_counter() - t0
+    return {"workload": f"ssDNA: 40 nt x 3 free sites (bonded + Go-like terms) in the "
+                        f"120x120x180 pore maps, {n - spec.nsites} K+/Cl-, FP32 pairs",
+            "particles": n, "sites": spec.nsites, "terms": spec.nucl.counts(),
+            "value": n * steps / (ms * 1e-3), "unit": "particle-steps/s",
+            "ms_per_bd_step": ms / steps, "steps": steps,
+            "oracle_error": err,
+            "cpu": {"value": n * ncpu / dt, "steps": ncpu, "cores": int(os.cpu_count() or 1),
+                    "kind": "port"}}
+
+
 ADJ_N, ADJ_STEPS, ADJ_CKPT = 4096, 2000, 100
 
 
@@ -809,6 +862,7 @@ def run_gpu(args, rank, world, local_rank):
     batched = batch_measure(sh, flush)
     adjoint = adjoint_measure(sh)
     bulk_c1 = c1_measure(sh)
+    ssdna_c3 = c3_measure(sh)
     # the oracle leg: CPU baselines, then the oracle as the checker
     budget = float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15"))
     cpu = oracle_baseline(budget)
@@ -839,6 +893,7 @@ def run_gpu(args, rank, world, local_rank):
             "batched": batched,
             "adjoint": adjoint,
             "bulk_c1": bulk_c1,
+            "ssdna_c3": ssdna_c3,
             "wall_s": wall, "clocks": clocks}
     print(json.dumps(line), flush=True)
     if dist:

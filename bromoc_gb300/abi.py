@@ -21,8 +21,8 @@ TERM_NAMES = ("ener", "eelec", "evdw", "esrpmf", "eefpot", "eqqmx", "evdwmx",
               "esolv", "econ")
 NTERMS = len(TERM_NAMES)
 
-M_NONBOND, M_MEMB, M_PHIX, M_PHIV, M_RFPAR, M_BOND = 1, 2, 4, 8, 16, 32
-M_ALL = 0x3F
+M_NONBOND, M_MEMB, M_PHIX, M_PHIV, M_RFPAR, M_BOND, M_MMIJ = 1, 2, 4, 8, 16, 32, 64
+M_ALL = 0x7F
 BOX, SPHERE, ECYL = 0, 1, 2
 FP64, FP32 = 0, 1
 DYN0, DYN1, DYN2, DYN3 = 0, 1, 2, 3
@@ -84,6 +84,15 @@ class Nucleotides(C.Structure):
                 ("qunsplit", C.c_int32), ("nsites1st", C.c_int32)]
 
 
+class Mmij(C.Structure):
+    _fields_ = [("shape", C.c_int32), ("xnpol", C.c_int32), ("ynpol", C.c_int32),
+                ("znpol", C.c_int32), ("lstpx", _i), ("lstpy", _i), ("lstpz", _i),
+                ("rbxmin", C.c_double), ("rbxmax", C.c_double), ("rbymin", C.c_double),
+                ("rbymax", C.c_double), ("rbzmin", C.c_double), ("rbzmax", C.c_double),
+                ("rfscal", C.c_double), ("nmpol", C.c_int32), ("srdist", C.c_double),
+                ("mmij", _d)]
+
+
 class Grid(C.Structure):
     _fields_ = [("nclx", C.c_int32), ("ncly", C.c_int32), ("nclz", C.c_int32),
                 ("dcel", C.c_double), ("xbcen", C.c_double),
@@ -140,6 +149,7 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         "set_pairs": [vp, C.POINTER(Pairs)],
         "set_sites": [vp, C.POINTER(Sites)],
         "set_nucleotides": [vp, C.POINTER(Nucleotides)],
+        "set_mmij": [vp, C.POINTER(Mmij)],
         "set_phix": [vp, C.POINTER(Grid), _f],
         "set_phiv": [vp, C.POINTER(Grid), _i8, C.POINTER(PhivOpts)],
         "set_rfpar": [vp, C.POINTER(Grid), C.c_int32, _f, _f, C.c_double, _i],
@@ -289,6 +299,30 @@ class Engine:
         self._keep = keep
         self._chk(self._fn("set_nucleotides")(self.h, C.byref(st)), "set_nucleotides")
         self._keep = []
+
+    def set_mmij(self, mm) -> None:
+        """MMIJ reaction field from a dict (shape, npol + lstp + region + rfscal
+        for RECTBOX, or nmpol + srdist for SPHERE, and mmij), or None."""
+        if mm is None:
+            self._chk(self._fn("set_mmij")(self.h, None), "set_mmij")
+            return
+        keep = []
+
+        def arr(v, dt):
+            a = np.ascontiguousarray(v, dt)
+            keep.append(a)
+            return a
+
+        m = arr(np.asarray(mm["mmij"], np.float64).reshape(-1), np.float64)
+        st = Mmij(shape=mm["shape"], mmij=ptr(m, C.c_double), rfscal=mm.get("rfscal", 1.0))
+        if mm["shape"] == BOX:
+            st.xnpol, st.ynpol, st.znpol = mm["npol"]
+            lx, ly, lz = (arr(v, np.int32) for v in mm["lstp"])
+            st.lstpx, st.lstpy, st.lstpz = (ptr(v, C.c_int32) for v in (lx, ly, lz))
+            (st.rbxmin, st.rbxmax), (st.rbymin, st.rbymax), (st.rbzmin, st.rbzmax) = mm["region"]
+        else:
+            st.nmpol, st.srdist = mm["nmpol"], mm["srdist"]
+        self._chk(self._fn("set_mmij")(self.h, C.byref(st)), "set_mmij")
 
     # -- particles ------------------------------------------------------------
     def set_particles(self, x, y, z, typei, nsites=0, nfix=0, ibuffer=None):

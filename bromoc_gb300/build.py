@@ -17,7 +17,7 @@ SRC = PKG / "csrc"
 OBJ = PKG / "_build"
 LIB = PKG / "libbromoc_gpu.so"
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
-UNITS = ["api.cu", "energy.cu", "fields.cu", "dyn.cu", "gcmc.cu", "probe.cu", "noalloc.cu", "batch.cu", "adjoint.cu", "loop.cu", "cells.cu", "mc.cu", "nucl.cu", "analysis.cu", "tables.cpp"]
+UNITS = ["api.cu", "energy.cu", "fields.cu", "dyn.cu", "gcmc.cu", "probe.cu", "noalloc.cu", "batch.cu", "adjoint.cu", "loop.cu", "cells.cu", "mc.cu", "nucl.cu", "analysis.cu", "mmij.cu", "tables.cpp"]
 
 
 def nvcc() -> str:

@@ -585,6 +585,8 @@ int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "adjoint: the periodic mode is not supported");
   if (pk->nsites != 0 || pk->shape != BROMOC_BOX)
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "adjoint: ions only, in a box");
+  if (pk->mm.on)
+    return bromoc_ctx_fail(proto, BROMOC_E_STATE, "adjoint: the MMIJ reaction field is not supported");
   if (pk->nion_t > kAdjMaxIonTypes)
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "adjoint: at most 4 ion types");
   bromoc_adj *ad = new bromoc_adj;

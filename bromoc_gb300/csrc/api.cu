@@ -156,6 +156,17 @@ void clear_nucl(bromoc_ctx *ctx) {
   ctx->nuc_on = false;
 }
 
+// Drops the MMIJ reaction field.
+void clear_mmij(bromoc_ctx *ctx) {
+  MmijDev &m = ctx->kp.mm;
+  for (const void *a : {(const void *)m.lst, (const void *)m.bnorm, (const void *)m.m,
+                        (const void *)m.tab, (const void *)m.in, (const void *)m.ist,
+                        (const void *)m.coefp, (const void *)m.coef, (const void *)m.coef2,
+                        (const void *)m.mq, (const void *)m.rowe})
+    dfree(ctx, const_cast<void *>(a));
+  m = MmijDev{};
+}
+
 Grid3 make_grid(const bromoc_grid &g) {
   Grid3 r{};
   r.nclx = g.nclx;
@@ -339,7 +350,13 @@ KTimer *next_timer(bromoc_ctx *c, int kind) {
 
 // Source chunking of the pair kernels: enough blocks for ~2 waves of the
 // 152 SMs, chunks a multiple of the 128-particle tile.
-void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
+// Source chunks of a target-tiled pair kernel: about eight two-warp blocks
+// per SM.  fine: chunks of any length down to kMinChunk sources (the FP64
+// kernels, where a pair costs ~100 FP64 operations on GB300's narrow FP64
+// pipe and a small system would otherwise occupy a few SMs); else whole
+// source tiles.
+constexpr int kMinChunk = 4;
+void chunking(int ntargets, int nsources, int &nchunk, int &chunk, bool fine = false) {
   if (ntargets <= 0 || nsources <= 0) {
     nchunk = 0;
     chunk = kPairTile;
@@ -348,9 +365,13 @@ void chunking(int ntargets, int nsources, int &nchunk, int &chunk) {
   const int tiles = (ntargets + kPairTile - 1) / kPairTile;
   const int stiles = (nsources + kPairTile - 1) / kPairTile;
   int want = (8 * kSMs + tiles - 1) / tiles;  // ~8 two-warp blocks per SM
-  want = std::max(1, std::min(std::min(want, stiles), kMaxChunks));
-  int per = (stiles + want - 1) / want;  // source tiles per chunk
-  chunk = per * kPairTile;
+  if (fine) {
+    want = std::max(1, std::min(want, kMaxChunks));
+    chunk = std::max(kMinChunk, (nsources + want - 1) / want);
+  } else {
+    want = std::max(1, std::min(std::min(want, stiles), kMaxChunks));
+    chunk = ((stiles + want - 1) / want) * kPairTile;  // source tiles per chunk
+  }
   nchunk = (nsources + chunk - 1) / chunk;
 }
 
@@ -406,6 +427,7 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
   fl.fp32_noise = plan.fp32;
   fl.fp32_partials = plan.fp32;
   plan.nuc = ctx->nuc_on && p.nsites > 0;
+  plan.mmij = p.mm.on && (mask & BROMOC_M_MMIJ);
   fl.is = ((mask & BROMOC_M_NONBOND) && p.nsites > 0 && nion > 0) || plan.nuc;
   plan.ntile = p.ntile = 0;
   plan.cells = false;
@@ -453,9 +475,9 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
     fl.ii_from = pc.t0;
     fl.nchunk_ii = fl.ii ? plan.nchunk_ii : 0;
   } else {
-    chunking(nmob, nion, plan.nchunk_ii, p.chunk_ii);
+    chunking(nmob, nion, plan.nchunk_ii, p.chunk_ii, true);
     p.nchunk_ii = plan.nchunk_ii;
-    chunking(nion, nion, plan.nchunk_rf, p.chunk_rf);
+    chunking(nion, nion, plan.nchunk_rf, p.chunk_rf, true);
     p.nchunk_rf = plan.nchunk_rf;
     fl.ii = (mask & BROMOC_M_NONBOND) && nmob > 0 && plan.nchunk_ii > 0;
     fl.ii_from = p.nsites + p.nfix;
@@ -981,6 +1003,110 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
     return set_err(ctx, BROMOC_E_ARG, "set_sites: nmcden needs per-site maps");
   }
   return rc;
+}
+
+int bromoc_gpu_set_mmij(bromoc_ctx *ctx, const bromoc_mmij *q) {
+  if (!ctx) return BROMOC_E_ARG;
+  CU(cudaStreamSynchronize(ctx->stream));
+  clear_mmij(ctx);
+  if (!q) return BROMOC_OK;
+  KP &p = ctx->kp;
+  MmijDev &m = p.mm;
+  std::vector<int3> lst;
+  std::vector<double> bn;
+  if (q->shape == BROMOC_BOX) {
+    if (q->xnpol < 1 || q->ynpol < 1 || q->znpol < 1 || q->xnpol > 64 || q->ynpol > 64 ||
+        q->znpol > 64 || !q->lstpx || !q->lstpy || !q->lstpz || !q->mmij ||
+        !(q->rbxmax - q->rbxmin > 0.0) || !(q->rbymax - q->rbymin > 0.0) ||
+        !(q->rbzmax - q->rbzmin > 0.0))
+      return set_err(ctx, BROMOC_E_ARG, "set_mmij: RECTBOX orders (1..64), region or matrix");
+    const int nt = q->xnpol * q->ynpol * q->znpol;
+    m.rect = 1;
+    m.nx = q->xnpol;
+    m.ny = q->ynpol;
+    m.nz = q->znpol;
+    m.ntpol = nt;
+    // shell_simul.f90:2792-2802, rect_norm.f90
+    m.xscal = 2.0 / (q->rbxmax - q->rbxmin);
+    m.yscal = 2.0 / (q->rbymax - q->rbymin);
+    m.zscal = 2.0 / (q->rbzmax - q->rbzmin);
+    m.xmax = 1.0 / m.xscal;
+    m.ymax = 1.0 / m.yscal;
+    m.zmax = 1.0 / m.zscal;
+    m.rfscal = q->rfscal;
+    const double ilxyz = m.xscal * m.yscal * m.zscal * 0.125;
+    for (int n = 0; n < nt; ++n) {
+      const int a = q->lstpx[n], b = q->lstpy[n], c = q->lstpz[n];
+      if (a < 0 || a >= m.nx || b < 0 || b >= m.ny || c < 0 || c >= m.nz)
+        return set_err(ctx, BROMOC_E_ARG, "set_mmij: basis order out of range");
+      lst.push_back(make_int3(a, b, c));
+      bn.push_back(std::sqrt((2.0 * a + 1.0) * (2.0 * b + 1.0) * (2.0 * c + 1.0) * ilxyz));
+    }
+  } else if (q->shape == BROMOC_SPHERE) {
+    if (q->nmpol < 1 || q->nmpol > 25 || !(q->srdist > 0.0) || !q->mmij)
+      return set_err(ctx, BROMOC_E_ARG, "set_mmij: SPHERE nmpol (1..25), srdist or matrix");
+    m.rect = 0;
+    m.nmpol = q->nmpol;
+    m.ntpol = q->nmpol * q->nmpol;
+    m.srdist2 = q->srdist * q->srdist;
+    // sphe_svpol.f90, sphe_norm.f90 (factori.f90)
+    auto fact = [](int n) {
+      double f = 1.0;
+      for (int i = 2; i <= n; ++i) f = f * i;
+      return f;
+    };
+    const double sr2 = q->srdist * q->srdist, itwopi = 1.0 / (2.0 * 3.14159265358979323846);
+    double rpart = sr2 * q->srdist, lpart = 1.5 * itwopi;
+    const double ipi = 0.5 * itwopi;
+    lst.push_back(make_int3(0, 0, 0));
+    bn.push_back(std::sqrt(lpart / rpart));
+    for (int l = 1; l < q->nmpol; ++l) {
+      lpart = (2.0 * l + 1.0) * (2.0 * l + 3.0) * ipi;
+      rpart = rpart * sr2;
+      lst.push_back(make_int3(l, 0, 0));
+      bn.push_back(std::sqrt(lpart / rpart));
+      lpart = (2.0 * l + 1.0) * (2.0 * l + 3.0) * itwopi;
+      for (int mm = 1; mm <= l; ++mm) {
+        const double v = std::sqrt(lpart * fact(l - mm) / (rpart * fact(l + mm)));
+        lst.push_back(make_int3(l, mm, 0));
+        bn.push_back(v);
+        lst.push_back(make_int3(l, -mm, 0));
+        bn.push_back(v);
+      }
+    }
+  } else {
+    return set_err(ctx, BROMOC_E_ARG, "set_mmij: shape must be BROMOC_BOX or BROMOC_SPHERE");
+  }
+  const int nt = m.ntpol;
+  std::vector<double> mat(q->mmij, q->mmij + (size_t)nt * nt);
+  for (int i = 0; i < nt; ++i)  // readmmij.f90: the lower triangle from the upper
+    for (int j = 0; j < i; ++j) mat[(size_t)i * nt + j] = mat[(size_t)j * nt + i];
+  m.tabw = mmij_table_width(m.rect, m.nx, m.ny, m.nz, m.nmpol);
+  const size_t cap = p.cap;
+  const int nch = std::max(1, (int)((cap + 1 + 255) / 256));
+  int3 *dl = nullptr;
+  double *db = nullptr, *dm = nullptr;
+  int rc = upload(ctx, &dl, lst.data(), lst.size());
+  if (!rc) rc = upload(ctx, &db, bn.data(), bn.size());
+  if (!rc) rc = upload(ctx, &dm, mat.data(), mat.size());
+  if (!rc) rc = dalloc(ctx, &m.tab, (cap + 1) * (size_t)m.tabw);
+  if (!rc) rc = dalloc(ctx, &m.in, cap + 1);
+  if (!rc) rc = dalloc(ctx, &m.ist, cap + 2);
+  if (!rc) rc = dalloc(ctx, &m.coefp, (size_t)nch * nt);
+  if (!rc) rc = dalloc(ctx, &m.coef, (size_t)nt);
+  if (!rc) rc = dalloc(ctx, &m.coef2, (size_t)nt);
+  if (!rc) rc = dalloc(ctx, &m.mq, (size_t)nt);
+  if (!rc) rc = dalloc(ctx, &m.rowe, (size_t)nt);
+  m.lst = dl;
+  m.bnorm = db;
+  m.m = dm;
+  if (!rc) rc = cudaMemset(m.in, 0, cap + 1) == cudaSuccess ? 0 : BROMOC_E_CUDA;
+  if (rc) {
+    clear_mmij(ctx);
+    return rc ? rc : set_err(ctx, BROMOC_E_CUDA, "set_mmij: device memory");
+  }
+  m.on = 1;
+  return BROMOC_OK;
 }
 
 int bromoc_gpu_set_nucleotides(bromoc_ctx *ctx, const bromoc_nucleotides *q) {
@@ -1605,7 +1731,7 @@ int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_
   const int nloop = eterms ? nsteps - 1 : nsteps;
   if (ctx->fused_bd && ctx->precision == BROMOC_FP32 && nloop > 0) {
     if ((rc = plan_energy(ctx, terms, false, plan, fl, false))) return rc;
-    if (bd_loop_supported(p, fl)) {
+    if (bd_loop_supported(p, fl) && !plan.mmij) {
       KTimer *tl = next_timer(ctx, BROMOC_K_LOOP);
       if (tl) cudaEventRecord(tl->a, ctx->stream);
       CU(launch_bd_loop(p, fl, plan.ntot_ub, terms, variant, seed, step0, nloop, 1,
@@ -1666,6 +1792,10 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   KP &p = ctx->kp;
   if (ngcmc < 0 || cycle < 1) return set_err(ctx, BROMOC_E_ARG, "grand: bad ngcmc or cycle");
   if (p.nbuffer < 1) return set_err(ctx, BROMOC_E_STATE, "grand: no buffers");
+  if (p.mm.on && (terms & BROMOC_M_MMIJ))
+    return set_err(ctx, BROMOC_E_STATE,
+                   "grand: the MMIJ reaction field is not built into GRAND (INTERACT and "
+                   "METROPOLIS have it)");
   // FP32 mode: GRAND works on the float-float records (the current
   // positions while BD runs), FP64 mode on the FP64 arrays
   const bool ff = ctx->precision == BROMOC_FP32;

@@ -391,6 +391,8 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "batch: the periodic mode is not supported");
   if (pk->nsites != 0)
     return bromoc_ctx_fail(proto, BROMOC_E_STATE, "batch: replicas hold ions only (no sites)");
+  if (pk->mm.on)
+    return bromoc_ctx_fail(proto, BROMOC_E_STATE, "batch: the MMIJ reaction field is not supported");
   bromoc_batch *b = new bromoc_batch;
   b->proto = proto;
   b->kp = *pk;

@@ -586,11 +586,13 @@ __global__ void __launch_bounds__(256) k_ereduce(KP p, int nslot, int rfpar_on) 
   if (threadIdx.x == 0) {
     double o[kNTerms];
     for (int k = 0; k < kNTerms; ++k) o[k] = tot[k];
-    o[11] = rfpar_on ? o[13] : 0.0;  // egsbpb = erfpar
-    // energy.mono.f90:689: ..., esrpmfmx, ebond .. esolv, eqqmx, evdwmx,
-    // eefpot, eefpotmx, econ
-    o[0] = o[9] + o[10] + o[12] + o[13] + o[1] + o[2] + o[3] + o[7] + o[14] + o[15] +
+    // energy.mono.f90:65-115, 689: ememb, the MMIJ egsbpb (slot 11 of the
+    // partials), egsbpa, evdwgd, erfpar, then ..., esrpmfmx, ebond .. esolv,
+    // eqqmx, evdwmx, eefpot, eefpotmx, econ; RFPAR then reports
+    // egsbpb = erfpar
+    o[0] = o[9] + o[11] + o[10] + o[12] + o[13] + o[1] + o[2] + o[3] + o[7] + o[14] + o[15] +
            o[16] + o[17] + o[18] + o[19] + o[20] + o[21] + o[5] + o[6] + o[4] + o[8] + o[22];
+    if (rfpar_on) o[11] = o[13];
     for (int k = 0; k < kNTerms; ++k) p.eterms[k] = o[k];
   }
 }
@@ -609,6 +611,10 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
     if (plan.t_fields) cudaEventRecord(plan.t_fields->b, stream);
     slot += nfb;
     ++nk;
+  }
+  if (plan.mmij) {  // energy.mono.f90:71-79; forces added to the field forces
+    nk += launch_mmij(p, plan.fp32, nub, qforces, slot, stream);
+    ++slot;
   }
   const bool nonbond = (mask & 1u) != 0;
   const int nmob_ub = nub - p.nsites - p.nfix;
@@ -707,6 +713,7 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
 int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {
   const int nub = plan.ntot_ub;
   int slot = fields_blocks(nub);
+  if (plan.mmij) ++slot;
   const int nmob_ub = nub - p.nsites - p.nfix;
   if (plan.fp32) {
     const PairCfg32 pc = pair_cfg32(p, nub, mask);

@@ -313,6 +313,8 @@ void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
   k_interact_prep<<<1, 32, 0, stream>>>(p, mask, qalert);
   k_interact_part<<<nb, kIaThreads, 0, stream>>>(p, mask);
   k_interact_final<<<1, kIaThreads, 0, stream>>>(p, nb, dener_dev);
+  if ((mask & 64u) && p.mm.on)  // interact.f90:121-141
+    launch_mmij_interact(p, ntot_ub, dener_dev, stream);
 }
 
 // ---------------------------------------------------------------------------

@@ -101,6 +101,24 @@ struct NucDev {
   double *cf;                   // [8] centre force per strand and axis, econ
 };
 
+// Reaction field of the MMIJ basis (gsbpmod): RECTBOX Legendre products or
+// SPHERE multipoles, FP64; per-particle basis tables (row cap: INTERACT's
+// trial), the coefficient vector and M coef.
+struct MmijDev {
+  int on, rect;
+  int nx, ny, nz, nmpol, ntpol;  // RECTBOX orders per axis; SPHERE nmpol
+  int tabw;                      // doubles per table row
+  const int3 *lst;               // [ntpol] (lx, ly, lz) or (l, m, 0)
+  const double *bnorm;           // [ntpol]
+  const double *m;               // [ntpol*ntpol] symmetric
+  double xscal, yscal, zscal, xmax, ymax, zmax, rfscal, srdist2;
+  double *tab;                   // [(cap+1)*tabw]
+  unsigned char *in;             // [cap+1] in the region
+  double *ist;                   // [cap+2] SPHERE 10/sin(theta); [cap+1]: the last ion's
+  double *coefp;                 // [nchunk*ntpol] per-chunk partial sums
+  double *coef, *coef2, *mq, *rowe;  // [ntpol]
+};
+
 struct KP {
   // ---- sizes (host-known) ----
   int cap, nsites, nfix, ntype, nold, nttyp, ndna, ntc;
@@ -150,6 +168,7 @@ struct KP {
   const uint8_t *stfree;
   const int *site_map;    // [nsites] nmcden map or nullptr
   NucDev nuc;
+  MmijDev mm;
   // ---- static field ----
   int qphix;
   Grid3 g1;

@@ -18,6 +18,7 @@ struct EnergyPlan {
   bool cells = false; // FP32 extension mode: the cell-list pair kernel
   bool reduce_energy; // launch the final energy reduction
   bool nuc = false;   // DNA bonded/Go terms (nucl.cu)
+  bool mmij = false;  // MMIJ reaction field (mmij.cu)
   KTimer *t_pairs = nullptr, *t_rf = nullptr, *t_fields = nullptr;
 };
 
@@ -55,6 +56,14 @@ struct AssembleFlags {
   int ntile;          // FP32: partials are per tile pair (Newton-3 kernel)
   int rf_ab;          // FP32 Newton-3: add A sd1 + B sd2 of the RFPAR chain
 };
+
+// mmij.cu: MMIJ reaction field (energy into slot `slot`, forces added to
+// ffield / ffield_f); INTERACT's term of p.trial added to *dener
+int mmij_chunks(const KP &p, int ntot_ub);
+int mmij_table_width(int rect, int nx, int ny, int nz, int nmpol);
+int launch_mmij(const KP &p, bool fp32, int ntot_ub, int qforces, int slot,
+                cudaStream_t stream);
+void launch_mmij_interact(const KP &p, int ntot_ub, double *dener, cudaStream_t stream);
 
 // analysis.cu: per-cycle profiles (counts) and .btr frames
 struct ProfArgs {

@@ -80,6 +80,7 @@ class SystemSpec:
     site_types: np.ndarray | None = None    # [nsites] combined type 1..ndna
     site_free: np.ndarray | None = None
     nucl: object = None           # nucleotides.Topology: bonded and Go-like terms
+    mmij: dict | None = None      # MMIJ reaction field (abi.Engine.set_mmij)
     # maps
     phix: tuple | None = None     # (grid dict, float32[n])
     phiv: tuple | None = None     # (grid dict, int8[nmaps*n], opts dict)
@@ -311,6 +312,8 @@ class SystemSpec:
         eng.call("set_sites", C.byref(sites))
         if ns and self.nucl is not None:
             eng.set_nucleotides(self.nucl)
+        if self.mmij is not None:
+            eng.set_mmij(self.mmij)
         if self.phix is not None:
             g, data = self.phix
             data = k(np.ascontiguousarray(data, np.float32))

@@ -320,3 +320,28 @@ def ssdna(seed=4, nions=5000, nnuc=40, maps=None, precision=abi.FP32, bonded=Fal
             sig = 0.5 * (4.0 + prm["sigma"])
             s.efpot_knots[(site, ion)] = efpot_knots(rng, sig, math.sqrt(0.2 * prm["eps"]))
     return s
+
+
+def mmij_rect(seed=12, npol=(4, 4, 5), half=(9.0, 9.0, 14.0), rfscal=1.0, scale=2e-3):
+    """A RECTBOX MMIJ reaction field: every basis order up to npol - 1 along
+    each axis (the order pnpio.f writes, z fastest), a symmetric matrix with
+    a negative diagonal (a reaction field lowers the self energy), over the
+    region |x| <= half[0], ..."""
+    rng = np.random.default_rng(seed)
+    lx, ly, lz = np.meshgrid(*(np.arange(n) for n in npol), indexing="ij")
+    nt = int(np.prod(npol))
+    a = rng.normal(0.0, scale, (nt, nt))
+    m = 0.5 * (a + a.T) - np.diag(np.abs(rng.normal(4 * scale, scale, nt)))
+    return dict(shape=abi.BOX, npol=tuple(npol), lstp=(lx.ravel(), ly.ravel(), lz.ravel()),
+                region=((-half[0], half[0]), (-half[1], half[1]), (-half[2], half[2])),
+                rfscal=rfscal, mmij=m)
+
+
+def mmij_sphere(seed=13, nmpol=5, srdist=12.0, scale=2e-3):
+    """A SPHERE MMIJ reaction field of nmpol multipole orders inside radius
+    srdist (symmetric matrix, negative diagonal)."""
+    rng = np.random.default_rng(seed)
+    nt = nmpol * nmpol
+    a = rng.normal(0.0, scale, (nt, nt))
+    m = 0.5 * (a + a.T) - np.diag(np.abs(rng.normal(4 * scale, scale, nt)))
+    return dict(shape=abi.SPHERE, nmpol=nmpol, srdist=srdist, mmij=m)

@@ -79,7 +79,8 @@ enum {
   BROMOC_M_PHIV = 1u << 3,    /* Qphiv                                     */
   BROMOC_M_RFPAR = 1u << 4,   /* Qrfpar                                    */
   BROMOC_M_BOND = 1u << 5,    /* Qnobond: DNA bond, angle and torsion terms */
-  BROMOC_M_ALL = 0x3fu
+  BROMOC_M_MMIJ = 1u << 6,    /* Qmmij: reaction field of the MMIJ basis    */
+  BROMOC_M_ALL = 0x7fu
 };
 
 enum { BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2 };
@@ -201,6 +202,26 @@ typedef struct bromoc_nucleotides {
   int32_t nsites1st;         /* sites of the first strand                    */
 } bromoc_nucleotides;
 
+/* Reaction field of the MMIJ basis (GSBP mmij keywords,
+ * shell_simul.f90:2780-2830, and the file readmmij.f90 reads).  RECTBOX:
+ * Legendre products P_a(2x/wx) P_b(2y/wy) P_c(2z/wz) over the region
+ * |x| <= wx/2, |y| <= wy/2, |z| <= wz/2 (the widths wx = rbxmax - rbxmin
+ * ...; the region is centred at the origin as in the reference), basis
+ * orders lstpx/lstpy/lstpz, energy scale rfscal.  SPHERE: the multipoles
+ * r^l P_l^m(cos theta) {cos, sin}(m phi), l < nmpol <= 25, inside radius
+ * srdist.  mmij: ntpol x ntpol, row-major as in the file; the lower
+ * triangle is taken from the upper one (readmmij.f90). */
+typedef struct bromoc_mmij {
+  int32_t shape;             /* BROMOC_BOX (RECTBOX) or BROMOC_SPHERE        */
+  int32_t xnpol, ynpol, znpol;                  /* RECTBOX                   */
+  const int32_t *lstpx, *lstpy, *lstpz;         /* [ntpol] orders            */
+  double rbxmin, rbxmax, rbymin, rbymax, rbzmin, rbzmax;
+  double rfscal;
+  int32_t nmpol;             /* SPHERE: ntpol = nmpol^2                     */
+  double srdist;
+  const double *mmij;        /* [ntpol*ntpol]                                */
+} bromoc_mmij;
+
 /* Grid header of a PB map file: readphi.f90:43-52 (z fastest, x slowest). */
 typedef struct bromoc_grid {
   int32_t nclx, ncly, nclz;
@@ -274,6 +295,12 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *sites);
  * the terms that involve it (interact.f90:211-334, with its base-pair
  * scale of 1). */
 int bromoc_gpu_set_nucleotides(bromoc_ctx *ctx, const bromoc_nucleotides *nuc);
+/* MMIJ reaction field (NULL switches it off).  ENERGY adds egsbpb
+ * (rect_rf1.f90 / sphe_rf1.f90) to ener and its forces to the mobile ions
+ * in the region; INTERACT of a mobile ion adds E(coef) - E(coef without it)
+ * (rect_rf0.f90 / sphe_rf0.f90).  GRAND refuses a system with it on
+ * (BROMOC_E_STATE). */
+int bromoc_gpu_set_mmij(bromoc_ctx *ctx, const bromoc_mmij *m);
 /* static field phix (readphi PHIX, gsbpmod phix) -- staticf1/staticf0 */
 int bromoc_gpu_set_phix(bromoc_ctx *ctx, const bromoc_grid *g,
                         const float *phix);

@@ -25,7 +25,7 @@ module bromoc_gpu
        BROMOC_E_NOMEM = 5, BROMOC_E_DEVICE = 6
   integer(c_int32_t), parameter :: BROMOC_M_NONBOND = 1, BROMOC_M_MEMB = 2, &
        BROMOC_M_PHIX = 4, BROMOC_M_PHIV = 8, BROMOC_M_RFPAR = 16, BROMOC_M_BOND = 32, &
-       BROMOC_M_ALL = 63
+       BROMOC_M_MMIJ = 64, BROMOC_M_ALL = 127
   integer(c_int32_t), parameter :: BROMOC_BOX = 0, BROMOC_SPHERE = 1, BROMOC_ECYL = 2
   integer(c_int32_t), parameter :: BROMOC_FP64 = 0, BROMOC_FP32 = 1
   integer(c_int32_t), parameter :: BROMOC_DYN0 = 0, BROMOC_DYN1 = 1, &
@@ -133,6 +133,18 @@ module bromoc_gpu
     integer(c_int32_t) :: nsites1st
   end type bromoc_nucleotides
 
+  ! gsbpmod's MMIJ basis: RECTBOX orders and region, or SPHERE nmpol/srdist
+  type, bind(C) :: bromoc_mmij
+    integer(c_int32_t) :: shape
+    integer(c_int32_t) :: xnpol, ynpol, znpol
+    type(c_ptr) :: lstpx, lstpy, lstpz
+    real(c_double) :: rbxmin, rbxmax, rbymin, rbymax, rbzmin, rbzmax
+    real(c_double) :: rfscal
+    integer(c_int32_t) :: nmpol
+    real(c_double) :: srdist
+    type(c_ptr) :: mmij
+  end type bromoc_mmij
+
   type, bind(C) :: bromoc_grid
     integer(c_int32_t) :: nclx, ncly, nclz
     real(c_double) :: dcel
@@ -234,6 +246,12 @@ module bromoc_gpu
       import :: c_int, c_ptr, bromoc_nucleotides
       type(c_ptr), value :: ctx
       type(bromoc_nucleotides), intent(in) :: nuc
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_set_mmij(ctx, m) bind(C, name="bromoc_gpu_set_mmij") result(rc)
+      import :: c_int, c_ptr, bromoc_mmij
+      type(c_ptr), value :: ctx
+      type(bromoc_mmij), intent(in) :: m
       integer(c_int) :: rc
     end function
     function bromoc_gpu_set_phix(ctx, g, phix) bind(C, name="bromoc_gpu_set_phix") result(rc)

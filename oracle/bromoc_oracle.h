@@ -23,6 +23,7 @@ int bromoc_ref_set_types(bromoc_ref *r, const bromoc_types *t);
 int bromoc_ref_set_pairs(bromoc_ref *r, const bromoc_pairs *p);
 int bromoc_ref_set_sites(bromoc_ref *r, const bromoc_sites *s);
 int bromoc_ref_set_nucleotides(bromoc_ref *r, const bromoc_nucleotides *n);
+int bromoc_ref_set_mmij(bromoc_ref *r, const bromoc_mmij *m);
 int bromoc_ref_set_phix(bromoc_ref *r, const bromoc_grid *g, const float *phix);
 int bromoc_ref_set_phiv(bromoc_ref *r, const bromoc_grid *g,
                         const int8_t *phiv, const bromoc_phiv_opts *o);

@@ -235,6 +235,61 @@ int bromoc_ref_set_nucleotides(bromoc_ref *r, const bromoc_nucleotides *q) {
   return BROMOC_OK;
 }
 
+int bromoc_ref_set_mmij(bromoc_ref *r, const bromoc_mmij *q) {
+  if (!r) return BROMOC_E_ARG;
+  State &s = r->s;
+  s.mm = bref::Mmij{};
+  if (!q) return BROMOC_OK;
+  bref::Mmij &m = s.mm;
+  if (q->shape == BROMOC_BOX) {
+    if (q->xnpol < 1 || q->ynpol < 1 || q->znpol < 1 || !q->lstpx || !q->lstpy || !q->lstpz ||
+        !q->mmij || !(q->rbxmax - q->rbxmin > 0.0) || !(q->rbymax - q->rbymin > 0.0) ||
+        !(q->rbzmax - q->rbzmin > 0.0))
+      return fail(r, "set_mmij: RECTBOX orders, region or matrix");
+    m.rect = true;
+    m.xnpol = q->xnpol;
+    m.ynpol = q->ynpol;
+    m.znpol = q->znpol;
+    m.ntpol = q->xnpol * q->ynpol * q->znpol;
+    m.lstpx.assign(q->lstpx, q->lstpx + m.ntpol);
+    m.lstpy.assign(q->lstpy, q->lstpy + m.ntpol);
+    m.lstpz.assign(q->lstpz, q->lstpz + m.ntpol);
+    for (int n = 0; n < m.ntpol; ++n)
+      if (m.lstpx[n] < 0 || m.lstpx[n] >= m.xnpol || m.lstpy[n] < 0 || m.lstpy[n] >= m.ynpol ||
+          m.lstpz[n] < 0 || m.lstpz[n] >= m.znpol) {
+        s.mm = bref::Mmij{};
+        return fail(r, "set_mmij: order out of range");
+      }
+    // shell_simul.f90:2792-2802
+    m.xscal = 2.0 / (q->rbxmax - q->rbxmin);
+    m.yscal = 2.0 / (q->rbymax - q->rbymin);
+    m.zscal = 2.0 / (q->rbzmax - q->rbzmin);
+    m.xmin = -1.0 / m.xscal;
+    m.xmax = 1.0 / m.xscal;
+    m.ymin = -1.0 / m.yscal;
+    m.ymax = 1.0 / m.yscal;
+    m.zmin = -1.0 / m.zscal;
+    m.zmax = 1.0 / m.zscal;
+    m.rfscal = q->rfscal;
+  } else if (q->shape == BROMOC_SPHERE) {
+    if (q->nmpol < 1 || q->nmpol > 25 || !(q->srdist > 0.0) || !q->mmij)
+      return fail(r, "set_mmij: SPHERE nmpol, srdist or matrix");
+    m.rect = false;
+    m.nmpol = q->nmpol;
+    m.ntpol = q->nmpol * q->nmpol;
+    m.srdist = q->srdist;
+  } else {
+    return fail(r, "set_mmij: shape must be RECTBOX or SPHERE");
+  }
+  const int nt = m.ntpol;
+  m.mmij.assign(q->mmij, q->mmij + (size_t)nt * nt);
+  for (int i = 0; i < nt; ++i)  // readmmij.f90: mmij(ij) = mmij(ji) for i > j
+    for (int j = 0; j < i; ++j) m.mmij[(size_t)i * nt + j] = m.mmij[(size_t)j * nt + i];
+  bref::mmij_basis(m);
+  m.on = true;
+  return BROMOC_OK;
+}
+
 int bromoc_ref_set_phix(bromoc_ref *r, const bromoc_grid *g, const float *phix) {
   if (!r || !g || !phix) return fail(r, "set_phix: null");
   State &s = r->s;

@@ -728,6 +728,12 @@ void interact(State &s, uint32_t mask, double &dener, double xj, double yj,
     }
     dener = s.ememb;
   }
+  // interact.f90:121-141 (the ntot bump of an insertion trial is the
+  // j == ntot + 1 case of mmij_interact)
+  if ((mask & BROMOC_M_MMIJ) && s.mm.on) {
+    s.egsbpb = mmij_interact(s, xj, yj, zj, j, jtype);
+    dener += s.egsbpb;
+  }
   if (Qrfpar) {
     if (j == s.ntot + 1) {
       s.ntot += 1;

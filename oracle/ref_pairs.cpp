@@ -398,6 +398,11 @@ void energy(State &s, uint32_t mask, bool qforces) {
 
   if (Qmemb) membrane(s, qforces);
   s.ener = s.ememb;
+  // energy.mono.f90:71-79
+  if ((mask & BROMOC_M_MMIJ) && s.mm.on) {
+    mmij_energy(s, qforces);
+    s.ener += s.egsbpb;
+  }
   if (Qphix) {
     staticf1(s, qforces);
     s.ener += s.egsbpa;

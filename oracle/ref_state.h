@@ -68,6 +68,18 @@ struct Nucl {
   std::vector<double> af, kx, ky, kz, contrx, contry, contrz;
 };
 
+// Reaction field of the MMIJ basis (gsbpmod): RECTBOX Legendre products or
+// SPHERE multipoles; basis vectors 0-based, mmij row-major ntpol x ntpol
+struct Mmij {
+  bool on = false, rect = true;
+  int xnpol = 0, ynpol = 0, znpol = 0, nmpol = 0, ntpol = 0;
+  std::vector<int> lstpx, lstpy, lstpz, lstpl, lstpm;
+  std::vector<double> bnorm, mmij;
+  double xscal = 0, yscal = 0, zscal = 0, xmin = 0, xmax = 0, ymin = 0, ymax = 0, zmin = 0,
+         zmax = 0, rfscal = 1, srdist = 0;
+};
+void mmij_basis(Mmij &m);
+
 struct State {
   std::string err;
   double celec = celec_value();
@@ -151,6 +163,8 @@ struct State {
   std::vector<int> warn;  // 1-based by combined type
   // DNA bonded / Go-like terms (nucleotmod)
   Nucl nuc;
+  // MMIJ reaction field (gsbpmod)
+  Mmij mm;
   double ebond = 0, eang = 0, edihe = 0, estack = 0, ebp = 0, eex = 0, eqq = 0,
          esolv = 0, econ = 0;
 
@@ -185,6 +199,9 @@ bool outbox(const State &s, double xi, double yi, double zi);
 // energy.mono.f90:196-582 and interact.f90:211-334 (ref_nucl.cpp)
 void nucl_energy(State &s, uint32_t mask, bool qforces);
 void nucl_interact(const State &s, uint32_t mask, int j, double &dener);
+// rect_rf1/sphe_rf1 (egsbpb, forces) and rect_rf0/sphe_rf0 (ref_mmij.cpp)
+void mmij_energy(State &s, bool qforces);
+double mmij_interact(const State &s, double xj, double yj, double zj, int j, int jtype);
 void membrane(State &s, bool qforces);
 void staticf1(State &s, bool qforces);
 void vdwgd1trln(State &s, bool qforces);

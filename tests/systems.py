@@ -125,6 +125,18 @@ def dna_duplex(nions=60, nbp=6, seed=21, precision=abi.FP64, qdeby=2):
     return s
 
 
+def mmij(shape="rect", nions=80, seed=14, precision=abi.FP64, buffers=False):
+    """The small pore (fields, RFPAR off) with an MMIJ reaction field over a
+    region that holds part of the ions."""
+    s = synth.pore(seed=seed, nions=nions, maps=small_maps(), radius=6.0, slab=10.0,
+                   precision=precision, buffers=buffers, rfpar=False)
+    if buffers:
+        s.count()
+    s.mmij = (synth.mmij_rect(seed=seed, half=(9.0, 9.0, 12.0), rfscal=1.5) if shape == "rect"
+              else synth.mmij_sphere(seed=seed, nmpol=5, srdist=11.0))
+    return s
+
+
 def gcmc(nions=60, seed=9, precision=abi.FP64):
     s = maps(nions=nions, seed=seed, buffers=True, precision=precision,
              membrane=False)
@@ -142,6 +154,8 @@ def all_families():
         "maps_fixed": lambda **k: maps(nfix=6, **k),
         "dna": lambda **k: dna(**k),
         "dna_duplex": lambda **k: dna_duplex(**k),
+        "mmij_rect": lambda **k: mmij("rect", **k),
+        "mmij_sphere": lambda **k: mmij("sphere", **k),
     }
 
 

@@ -56,6 +56,6 @@ def test_traj_frames_round_trip(gpu_lib, tmp_path):
     f = frames[-1]
     assert f.runtime == pytest.approx(12 * spec.dt)
     np.testing.assert_array_equal(f.xyz, last[0].astype(np.float32))
-    nw = spec.nwtype
+    nw = spec.nwtype()
     expect = np.concatenate([spec.site_types, nw[np.abs(last[1][spec.nsites:]) - 1]])
     np.testing.assert_array_equal(f.types, expect)

@@ -70,7 +70,7 @@ def workload(rank: int = 0, precision=abi.FP32):
 def config_dict():
     return {"workload": f"nanopore-{NIONS}: 120x120x180 maps (phix, phiv+repwalls, "
                         "rfpar), K+/Cl- Coulomb+LJ+SRPMF, 4 GCMC buffers",
-            "step": f"one cycle = GRAND({NGCMC} attempts) + {NBD} BD steps",
+            "step": f"one cycle = GRAND({NGCMC} attempts) + {NBD} BD steps + COUNT",
             "nions": NIONS, "grid": [120, 120, 180], "ngcmc": NGCMC, "nbd": NBD,
             "pairs": "all pairs (no cutoff); arithmetic per arm under 'precision'",
             "energy_totals": "not formed in the timed BD steps (forces only)",
@@ -533,6 +533,7 @@ def oracle_baseline(steps_budget_s: float, nthreads: int | None = None):
         eng.grand(NGCMC, SEED, cyc)
         n = eng.live_ntot()
         eng.bd_steps(NBD, SEED, (cyc - 1) * NBD)
+        eng.count()
         done_ps += NBD * (n - spec.nsites - spec.nfix)
         if time.perf_counter() - t0 >= steps_budget_s:
             break
@@ -644,6 +645,7 @@ def run_reference(args, rank, world):
         eng.grand(NGCMC, SEED, cyc)
         n = eng.live_ntot()
         eng.bd_steps(NBD, SEED, (cyc - 1) * NBD)
+        eng.count()
         return NBD * (n - spec.nsites - spec.nfix)
 
     for c in range(1, args.warmup + 1):
@@ -693,6 +695,7 @@ def run_gpu(args, rank, world, local_rank):
     def step(cyc):
         eng.grand(NGCMC, SEED, cyc, dener=False)
         eng.bd_steps(NBD, SEED, (cyc - 1) * NBD, energies=False)
+        eng.count()
 
     for c in range(1, args.warmup + 1):
         step(c)
@@ -715,6 +718,7 @@ def run_gpu(args, rank, world, local_rank):
             eng.grand(NGCMC, SEED, cyc, dener=False)
             _lib.live_count_async(eng, counts.data_ptr() + 4 * k)
             eng.bd_steps(NBD, SEED, (cyc - 1) * NBD, energies=False)
+            eng.count()
             ev[k][1].record(stream)
         torch.cuda.synchronize()
         wall = time.perf_counter() - w0

@@ -70,7 +70,11 @@ def load() -> C.CDLL:
                               C.c_uint64, d]),
                 ("energy", [vp, C.c_uint32, d, d]),
                 ("offset", [vp, C.c_int32]),
-                ("slots", [vp])):
+                ("slots", [vp]),
+                ("set_buffers", [vp, C.c_int32, C.POINTER(abi.Buffers), i32]),
+                ("grand", [vp, C.c_uint32, C.c_int32, C.POINTER(C.c_uint64), C.c_uint64, d]),
+                ("count", [vp]),
+                ("get_buffers", [vp, C.c_int32, i32, i32, i32, i32, i32])):
             f = getattr(lib, "bromoc_batch_" + name)
             f.argtypes = args
             f.restype = C.c_int

@@ -81,7 +81,8 @@ class Nucleotides(C.Structure):
                 ("ctn", C.c_int32), ("csn", _i),
                 ("kx", _d), ("ky", _d), ("kz", _d),
                 ("contrx", _d), ("contry", _d), ("contrz", _d),
-                ("qunsplit", C.c_int32), ("nsites1st", C.c_int32)]
+                ("qunsplit", C.c_int32), ("nsites1st", C.c_int32),
+                ("qnotr", C.c_int32 * 3), ("notr", C.c_double * 3)]
 
 
 class Mmij(C.Structure):
@@ -173,6 +174,8 @@ def declare(lib: C.CDLL, prefix: str) -> None:
         "get_buffers": [vp, _i, _i, _i, _i],
         "get_countions": [vp, _i, _i],
         "get_dids": [vp, _d],
+        "count": [vp],
+        "get_ntotat": [vp, _i],
         "efpot_from_knots": [C.c_int32, _d, _d, C.c_double, C.c_int32, _d, _d,
                              _d, _d],
     }
@@ -402,6 +405,15 @@ class Engine:
         self._chk(self._fn("grand")(self.h, terms, ngcmc, seed, cycle,
                                     C.byref(d) if dener else None), "grand")
         return d.value if dener else None
+
+    def count(self) -> None:
+        """COUNT (count.f90): buffer membership, nat, ntotat from positions."""
+        self._chk(self._fn("count")(self.h), "count")
+
+    def ntotat(self):
+        v = np.zeros(max(self.nbuffer, 1), np.int32)
+        self._chk(self._fn("get_ntotat")(self.h, ptr(v, C.c_int32)), "get_ntotat")
+        return v[:self.nbuffer]
 
     def metropolis(self, nmcm, mcmax, seed, cycle, terms=M_ALL):
         """METROPOLIS: nmcm moves -> (accepted moves, summed energy change)."""

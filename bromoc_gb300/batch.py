@@ -84,6 +84,54 @@ class Batch:
             et.ctypes.data_as(dp)), "energy")
         return et, f
 
+    def set_buffers(self, r, buffers: dict, ibuffer):
+        """GCMC buffers of replica r (keys of bromoc_buffers, per buffer:
+        ibfftyp, avnum, mu, kb, lzmin, lzmax, rmin, rmax, qbufferbias, nat,
+        ntotat) and the buffer of each of its ions (0 none)."""
+        keep = []
+
+        def arr(k, dt):
+            a = np.ascontiguousarray(buffers[k], dt)
+            keep.append(a)
+            return a.ctypes.data_as(C.POINTER(C.c_int32 if dt == np.int32 else
+                                              (C.c_uint8 if dt == np.uint8 else C.c_double)))
+
+        nb = len(buffers["ibfftyp"])
+        st = abi.Buffers(nbuffer=nb, ibfftyp=arr("ibfftyp", np.int32), avnum=arr("avnum", np.float64),
+                         mu=arr("mu", np.float64), kb=arr("kb", np.float64),
+                         lzmin=arr("lzmin", np.float64), lzmax=arr("lzmax", np.float64),
+                         rmin=arr("rmin", np.float64), rmax=arr("rmax", np.float64),
+                         qbufferbias=arr("qbufferbias", np.uint8), nat=arr("nat", np.int32),
+                         ntotat=arr("ntotat", np.int32))
+        ib = np.ascontiguousarray(ibuffer, np.int32)
+        self._chk(self.lib.bromoc_batch_set_buffers(
+            self.h, r, C.byref(st), ib.ctypes.data_as(C.POINTER(C.c_int32))), "set_buffers")
+
+    def grand(self, ngcmc, seeds, cycle, terms=abi.M_ALL):
+        """ngcmc GCMC attempts on every replica; returns each replica's summed
+        energy change of its accepted moves."""
+        s = np.ascontiguousarray(seeds, np.uint64)
+        d = np.zeros(self.nrep)
+        self._chk(self.lib.bromoc_batch_grand(
+            self.h, terms, ngcmc, s.ctypes.data_as(C.POINTER(C.c_uint64)), cycle,
+            d.ctypes.data_as(C.POINTER(C.c_double))), "grand")
+        return d
+
+    def count(self):
+        self._chk(self.lib.bromoc_batch_count(self.h), "count")
+
+    def get_buffers(self, r, nbuffer, nmax):
+        """(nat, ninsert, nremove, typei[n], ibuffer[n]) of replica r."""
+        ip = C.POINTER(C.c_int32)
+        nat, nin, nrm = (np.zeros(nbuffer, np.int32) for _ in range(3))
+        t = np.zeros(nmax, np.int32)
+        ib = np.zeros(nmax, np.int32)
+        self._chk(self.lib.bromoc_batch_get_buffers(
+            self.h, r, nat.ctypes.data_as(ip), nin.ctypes.data_as(ip), nrm.ctypes.data_as(ip),
+            t.ctypes.data_as(ip), ib.ctypes.data_as(ip)), "get_buffers")
+        n = len(self.get_particles(r, nmax)[0])
+        return nat, nin, nrm, t[:n], ib[:n]
+
     def set_graph(self, on: bool):
         """Replay runs of BD steps from a captured CUDA graph (on, the
         default) or launch them one by one; the trajectories agree."""

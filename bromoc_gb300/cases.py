@@ -12,6 +12,10 @@ command lines):
   python -m bromoc_gb300.cases cells N     FP32 BD steps of N ions of 1 M KCl
                                            in a periodic cube, 20 A cutoff
                                            (the cell-list kernels), 3 steps
+  python -m bromoc_gb300.cases ssdna       FP32 BD steps of 40 nt x 3 free sites
+                                           with their bonded terms and ~5000
+                                           ions in the 120x120x180 pore maps,
+                                           3 steps (per-kernel path)
 """
 from __future__ import annotations
 
@@ -57,6 +61,16 @@ def cells(n: int):
     g.live_ntot()
 
 
+def ssdna():
+    s = synth.ssdna(seed=4, nions=5000, nnuc=40, maps=synth.pore_maps(seed=102),
+                    precision=abi.FP32, bonded=True, free=True)
+    g = _lib.create(len(s.x) + 16, abi.FP32)
+    s.push(g)
+    for k in range(3):
+        g.bd_steps(1, seed=7, step0=k, energies=False)
+    g.live_ntot()
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "loop"
     if what == "pairs":
@@ -65,8 +79,10 @@ def main(argv):
         cells(int(argv[2]) if len(argv) > 2 else 20000)
     elif what == "loop":
         loop()
+    elif what == "ssdna":
+        ssdna()
     else:
-        raise SystemExit(f"unknown case {what!r}: pairs N | loop | cells N")
+        raise SystemExit(f"unknown case {what!r}: pairs N | loop | cells N | ssdna")
     print("ok")
 
 

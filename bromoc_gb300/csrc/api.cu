@@ -1225,6 +1225,10 @@ int bromoc_gpu_set_nucleotides(bromoc_ctx *ctx, const bromoc_nucleotides *q) {
   n.ctn = ctn;
   n.qunsplit = q->qunsplit != 0;
   n.nsites1st = q->nsites1st;
+  for (int a = 0; a < 3; ++a) {
+    n.qnotr[a] = q->qnotr[a] != 0;
+    n.notr[a] = q->notr[a];
+  }
   ctx->nuc_on = true;
   return BROMOC_OK;
 }
@@ -1748,6 +1752,7 @@ int bromoc_gpu_bd_steps(bromoc_ctx *ctx, uint32_t terms, int32_t variant, int32_
     KTimer *ta = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_ASSEMBLE) : nullptr;
     if (ta) cudaEventRecord(ta->a, ctx->stream);
     launch_assemble(p, plan.ntot_ub, fl, 1, variant, seed, step0 + k, ctx->stream);
+    if (plan.nuc) ctx->launches += launch_notrans(p, plan.fp32, ctx->stream);  // simul1.f90:380
     if (ta) cudaEventRecord(ta->b, ctx->stream);
     ctx->launches += plan.ntot_ub > 0;
   }
@@ -1968,6 +1973,7 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms, int32_t varian
     if (!rc && nbd > 0)
       rc = bromoc_gpu_bd_steps(ctx, terms, variant, nbd, seed, (cyc - 1) * nbd,
                                c + 1 == ncycle ? eterms : nullptr);
+    if (!rc) rc = bromoc_gpu_count(ctx);  // simul1.f90:462 (nothing without buffers)
     if (!rc && ctx->prof_on) rc = bromoc_gpu_accum_profiles(ctx);  // simul1.f90:476-509
   }
   int e = 0;
@@ -1975,6 +1981,30 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms, int32_t varian
   if (!rc) rc = device_err_result(ctx, e);
   if (rc) cudaStreamSynchronize(ctx->stream);  // no copy outlives the call
   return rc;
+}
+
+int bromoc_gpu_count(bromoc_ctx *ctx) {
+  if (!ctx) return BROMOC_E_ARG;
+  int rc = check_ready(ctx);
+  if (rc) return rc;
+  if (ctx->kp.nbuffer < 1) return BROMOC_OK;
+  const bool ff = ctx->precision == BROMOC_FP32;
+  if ((rc = ff ? ensure_ff(ctx) : ensure_dbl(ctx))) return rc;
+  launch_count(ctx->kp, ff, ntot_ub(ctx), ctx->stream);
+  ctx->launches += 3;
+  CU(cudaGetLastError());
+  return BROMOC_OK;
+}
+
+int bromoc_gpu_get_ntotat(bromoc_ctx *ctx, int32_t *ntotat) {
+  if (!ctx || !ntotat) return BROMOC_E_ARG;
+  const int nb = ctx->kp.nbuffer;
+  if (nb > 0) {
+    CU(cudaMemcpyAsync(ntotat, ctx->kp.st->ntotat, nb * sizeof(int), cudaMemcpyDeviceToHost,
+                       ctx->stream));
+    CU(cudaStreamSynchronize(ctx->stream));
+  }
+  return BROMOC_OK;
 }
 
 int bromoc_gpu_set_profiles(bromoc_ctx *ctx, int32_t qrho, int32_t qrdna, int32_t qgr,

@@ -186,6 +186,12 @@ struct bromoc_batch {
   float *wpart = nullptr;
   double *eterms = nullptr;
   RepDev *rep_pinned = nullptr;
+  // GCMC of the replicas (bromoc_batch_grand)
+  std::vector<RepGc> gc_h;
+  RepGc *gc = nullptr;
+  int *ibuf = nullptr;         // [nslots] buffer of each slot (0 none)
+  uint64_t *d_seeds = nullptr; // [nrep]
+  bool have_buffers = false;
   std::vector<void *> allocs;
   long long launches = 0;
 };
@@ -234,7 +240,7 @@ void drop_graph(bromoc_batch *b) {
 // work items: every tile pair (replica, q) and every tile (replica, t) of the
 // live particles, bucket by bucket and replica by replica within a bucket;
 // w0, w1 bound each replica's tile pairs
-int rebuild_work(bromoc_batch *b) {
+int rebuild_work(bromoc_batch *b, bool retune = true) {
   std::vector<int2> items, tiles;
   for (int k = 0; k < kBuckets; ++k) {
     b->wb[k] = (int)items.size();
@@ -250,7 +256,7 @@ int rebuild_work(bromoc_batch *b) {
   }
   b->wb[kBuckets] = (int)items.size();
   b->tb[kBuckets] = (int)tiles.size();
-  b->tuned = false;
+  if (retune) b->tuned = false;
   drop_graph(b);
   if ((int)items.size() > b->nwork) {
     if (b->work) cudaFree(b->work);
@@ -439,6 +445,11 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   if (!rc) rc = balloc(b, &b->tpb, npair * 64);
   if (!rc) rc = balloc(b, &st, 1);
   if (!rc) rc = balloc(b, &b->d_step0, 1);
+  double2 *gcrf = nullptr;
+  if (!rc) rc = balloc(b, &b->gc, nrep);
+  if (!rc) rc = balloc(b, &b->ibuf, ns);
+  if (!rc) rc = balloc(b, &b->d_seeds, nrep);
+  if (!rc) rc = balloc(b, &gcrf, ns);
   if (!rc && cudaMallocHost((void **)&b->rep_pinned, nrep * sizeof(RepDev)) != cudaSuccess)
     rc = bset(b, BROMOC_E_NOMEM, "batch: pinned replica records");
   if (!rc && cudaMallocHost((void **)&b->step_pinned, sizeof(uint64_t)) != cudaSuccess)
@@ -456,6 +467,9 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   cudaMemset(b->pk1[0], 0, ns * sizeof(float4));
   cudaMemset(b->pk2[0], 0, ns * sizeof(float4));
   cudaMemset(st, 0, sizeof(DevState));
+  cudaMemset(b->ibuf, 0, ns * sizeof(int));
+  cudaMemset(gcrf, 0, ns * sizeof(double2));
+  b->gc_h.assign(nrep, RepGc{});
   // host copies of the type tables
   b->nwtype_h.resize(p.ntype + 1);
   b->cg_h.resize(p.ntype + 1);
@@ -470,6 +484,7 @@ int bromoc_batch_create(bromoc_ctx *proto, int32_t nrep, const int32_t *capacity
   p.rfd = rfd;
   p.ffield_f = ffield;
   p.typei = typei;
+  p.gc_rf = gcrf;
   p.qproxdiff = 0;
   p.qcountion = 0;  // no crossing counters in a batch
   int *warn = nullptr;
@@ -537,6 +552,17 @@ int bromoc_batch_set_systems(bromoc_batch *b, const bromoc_system *sys) {
     for (int k = 0; k < 6; ++k) split(bd[k], bx.bh[k], bx.bl[k]);
     const double c[3] = {q.cx, q.cy, q.cz};
     for (int k = 0; k < 3; ++k) split(c[k], bx.ch[k], bx.cl[k]);
+    RepGc &g = b->gc_h[r];  // insert.f90 draws in FP64
+    g.shape = q.shape;
+    g.lx = q.lx;
+    g.ly = q.ly;
+    g.lz = q.lz;
+    g.cx = q.cx;
+    g.cy = q.cy;
+    g.cz = q.cz;
+    g.rsphe2 = q.rsphe * q.rsphe;
+    g.iecx = q.shape == BROMOC_ECYL ? 2.0 / q.lx : 0.0;
+    g.iecy = q.shape == BROMOC_ECYL ? 2.0 / q.ly : 0.0;
   }
   BCU(cudaStreamSynchronize(b->stream));
   BCU(cudaMemcpy(b->rep, b->rep_h.data(), b->nrep * sizeof(RepDev), cudaMemcpyHostToDevice));
@@ -580,9 +606,141 @@ int bromoc_batch_set_particles(bromoc_batch *b, int32_t r, int32_t n, const doub
     BCU(cudaMemcpy(b->kp.pk3 + o, h3.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
     BCU(cudaMemcpy(b->kp.typei + o, typei, n * sizeof(int), cudaMemcpyHostToDevice));
   }
+  BCU(cudaMemset(b->ibuf + o, 0, (size_t)b->cap[r] * sizeof(int)));
   b->n[r] = n;
   b->rep_h[r].n = n;
   return rebuild_work(b);
+}
+
+int bromoc_batch_set_buffers(bromoc_batch *b, int32_t r, const bromoc_buffers *bu,
+                             const int32_t *ibuffer) {
+  if (!b || !bu) return bset(b, BROMOC_E_ARG, "set_buffers: null");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  if (r < 0 || r >= b->nrep) return bset(b, BROMOC_E_ARG, "set_buffers: no replica %d", r);
+  const int nb = bu->nbuffer, n = b->n[r];
+  if (nb < 1 || nb > kBatchMaxBuf)
+    return bset(b, BROMOC_E_ARG, "set_buffers: 1..%d buffers per replica", kBatchMaxBuf);
+  if (!bu->ibfftyp || !bu->avnum || !bu->mu || !bu->kb || !bu->lzmin || !bu->lzmax ||
+      !bu->rmin || !bu->rmax || !bu->qbufferbias || !bu->nat || !bu->ntotat ||
+      (n > 0 && !ibuffer))
+    return bset(b, BROMOC_E_ARG, "set_buffers: null");
+  RepGc &g = b->gc_h[r];
+  g.nb = nb;
+  for (int k = 0; k < nb; ++k) {
+    const int t = bu->ibfftyp[k];
+    if (t <= b->kp.nold || t > b->kp.ntype)
+      return bset(b, BROMOC_E_ARG, "set_buffers: buffer %d holds no ion type", k + 1);
+    RepBuf &q = g.buf[k];
+    q = RepBuf{};
+    q.ibfftyp = t;
+    q.qbias = bu->qbufferbias[k] ? 1 : 0;
+    q.nat = bu->nat[k];
+    q.ntotat = bu->ntotat[k];
+    q.avnum = bu->avnum[k];
+    q.mu = bu->mu[k];
+    q.kb = bu->kb[k];
+    q.lzmin = bu->lzmin[k];
+    q.lzmax = bu->lzmax[k];
+    q.rmin = bu->rmin[k];
+    q.rmax = bu->rmax[k];
+  }
+  for (int i = 0; i < n; ++i)
+    if (ibuffer[i] < 0 || ibuffer[i] > nb)
+      return bset(b, BROMOC_E_ARG, "set_buffers: ibuffer(%d) = %d out of range", i + 1,
+                  ibuffer[i]);
+  BCU(cudaStreamSynchronize(b->stream));
+  if (n > 0)
+    BCU(cudaMemcpy(b->ibuf + b->off[r], ibuffer, n * sizeof(int), cudaMemcpyHostToDevice));
+  b->have_buffers = true;
+  return BROMOC_OK;
+}
+
+int bromoc_batch_grand(bromoc_batch *b, uint32_t terms, int32_t ngcmc, const uint64_t *seeds,
+                       uint64_t cycle, double *dener) {
+  if (!b || !seeds) return bset(b, BROMOC_E_ARG, "grand: null");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  if (ngcmc < 0 || cycle < 1) return bset(b, BROMOC_E_ARG, "grand: bad ngcmc or cycle");
+  if (!b->have_sys) return bset(b, BROMOC_E_STATE, "grand: set_systems first");
+  for (int r = 0; r < b->nrep; ++r)
+    if (b->gc_h[r].nb < 1)
+      return bset(b, BROMOC_E_STATE, "grand: replica %d has no buffers (set_buffers)", r);
+  if (ngcmc == 0) {
+    if (dener)
+      for (int r = 0; r < b->nrep; ++r) dener[r] = 0.0;
+    return BROMOC_OK;
+  }
+  for (int r = 0; r < b->nrep; ++r) b->gc_h[r].n = b->n[r];
+  BCU(cudaMemcpyAsync(b->gc, b->gc_h.data(), b->nrep * sizeof(RepGc), cudaMemcpyHostToDevice,
+                      b->stream));
+  BCU(cudaMemcpyAsync(b->d_seeds, seeds, b->nrep * sizeof(uint64_t), cudaMemcpyHostToDevice,
+                      b->stream));
+  launch_batch_grand(b->kp, b->rep, b->gc, b->ibuf, b->nrep, terms, b->d_seeds, cycle, ngcmc,
+                     b->stream);
+  ++b->launches;
+  BCU(cudaGetLastError());
+  BCU(cudaMemcpyAsync(b->gc_h.data(), b->gc, b->nrep * sizeof(RepGc), cudaMemcpyDeviceToHost,
+                      b->stream));
+  BCU(cudaStreamSynchronize(b->stream));
+  bool changed = false;
+  int err = 0;
+  for (int r = 0; r < b->nrep; ++r) {
+    err |= b->gc_h[r].err;
+    if (b->gc_h[r].n != b->n[r]) {
+      b->n[r] = b->gc_h[r].n;
+      b->rep_h[r].n = b->n[r];
+      changed = true;
+    }
+    if (dener) dener[r] = b->gc_h[r].dener;
+  }
+  if (changed) {
+    const int rc = rebuild_work(b, false);  // new counts; the per-bucket tuning stands
+    if (rc) return rc;
+  }
+  if (err & kErrCapacity)
+    return bset(b, BROMOC_E_CAPACITY, "grand: an insertion would exceed a replica's capacity");
+  if (err) return bset(b, BROMOC_E_DEVICE, "grand: device error flags 0x%x", err);
+  return BROMOC_OK;
+}
+
+int bromoc_batch_count(bromoc_batch *b) {
+  if (!b) return BROMOC_E_ARG;
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  if (!b->have_buffers) return BROMOC_OK;
+  for (int r = 0; r < b->nrep; ++r) {
+    b->gc_h[r].n = b->n[r];
+    b->gc_h[r].err = 0;
+  }
+  BCU(cudaMemcpyAsync(b->gc, b->gc_h.data(), b->nrep * sizeof(RepGc), cudaMemcpyHostToDevice,
+                      b->stream));
+  launch_batch_count(b->kp, b->rep, b->gc, b->ibuf, b->nrep, b->stream);
+  ++b->launches;
+  BCU(cudaGetLastError());
+  BCU(cudaMemcpyAsync(b->gc_h.data(), b->gc, b->nrep * sizeof(RepGc), cudaMemcpyDeviceToHost,
+                      b->stream));
+  BCU(cudaStreamSynchronize(b->stream));
+  for (int r = 0; r < b->nrep; ++r)
+    if (b->gc_h[r].err & kErrOutside)
+      return bset(b, BROMOC_E_DEVICE, "count: replica %d has a buffer ion outside its system", r);
+  return BROMOC_OK;
+}
+
+int bromoc_batch_get_buffers(bromoc_batch *b, int32_t r, int32_t *nat, int32_t *ninsert,
+                             int32_t *nremove, int32_t *typei, int32_t *ibuffer) {
+  if (!b || r < 0 || r >= b->nrep) return bset(b, BROMOC_E_ARG, "get_buffers: bad replica");
+  if (b->orphaned) return bset(b, BROMOC_E_STATE, "the prototype context was destroyed");
+  const RepGc &g = b->gc_h[r];
+  for (int k = 0; k < g.nb; ++k) {
+    if (nat) nat[k] = g.buf[k].nat;
+    if (ninsert) ninsert[k] = g.buf[k].ninsert;
+    if (nremove) nremove[k] = g.buf[k].nremove;
+  }
+  const int m = b->n[r];
+  BCU(cudaStreamSynchronize(b->stream));
+  if (typei && m > 0)
+    BCU(cudaMemcpy(typei, b->kp.typei + b->off[r], m * sizeof(int), cudaMemcpyDeviceToHost));
+  if (ibuffer && m > 0)
+    BCU(cudaMemcpy(ibuffer, b->ibuf + b->off[r], m * sizeof(int), cudaMemcpyDeviceToHost));
+  return BROMOC_OK;
 }
 
 int bromoc_batch_get_particles(bromoc_batch *b, int32_t r, int32_t *n, double *x, double *y,

@@ -53,6 +53,7 @@ enum : int {
   kErrFind = 4,         // GCMC deletion could not find the particle
   kErrBounds = 8,       // a guarded index was out of range (access skipped)
   kErrBarrier = 16,     // a grid barrier gave up waiting (the kernel returned)
+  kErrOutside = 32,     // COUNT found a buffer ion outside the system
 };
 
 // packed pair-law switches

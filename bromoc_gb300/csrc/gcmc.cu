@@ -7,6 +7,7 @@
 
 #include "ffmath.cuh"
 #include "gridsync.cuh"
+#include "batch.cuh"
 #include "launch.h"
 #include "physics.cuh"
 
@@ -1592,6 +1593,335 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
                   (void *)&ffpos};
   return cudaLaunchCooperativeKernel((const void *)k_grand, dim3(grid), dim3(kGrandThreads),
                                      args, 0, stream);
+}
+
+// ---------------------------------------------------------------------------
+// COUNT (count.f90:19-95), once per cycle after the BD steps: each mobile
+// ion's buffer -- the first whose ion type and z range (for a sphere also the
+// radial shell) hold it --, nat by integer atomics (order-free, so exact), the
+// sign of a buffer ion's type by its side of cz, then ntotat += nat.  A
+// buffer ion outside the system (the reference's fatal error) raises
+// kErrOutside.
+// ---------------------------------------------------------------------------
+__global__ void k_count_zero(KP p) {
+  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) p.st->nat[b] = 0;
+}
+
+template <bool FF>
+__global__ void __launch_bounds__(256) k_count(KP p) {
+  const int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.st->ntot) return;
+  int ib = 0;
+  if (i >= p.nsites + p.nfix) {
+    const double3 q = pos_of(p, FF, i);
+    const int itype = abs(p.typei[i]);
+    for (int b = 1; b <= p.nbuffer && !ib; ++b) {
+      if (itype != p.ibfftyp[b] || !(q.z >= p.lzmin[b] && q.z <= p.lzmax[b])) continue;
+      bool out = false, in = true;
+      if (p.shape == 1) {
+        const double r2 = (q.x - p.cx) * (q.x - p.cx) + (q.y - p.cy) * (q.y - p.cy) +
+                          (q.z - p.cz) * (q.z - p.cz);
+        out = r2 > p.rsphe2;
+        in = r2 >= p.rmin[b] * p.rmin[b] && r2 <= p.rmax[b] * p.rmax[b];
+      } else {
+        if (p.shape == 2) {
+          const double ex = (q.x - p.cx) * p.iecx, ey = (q.y - p.cy) * p.iecy;
+          out = ex * ex + ey * ey > 1.0;
+        } else {
+          out = q.x < p.lx2m || q.x > p.lx2p || q.y < p.ly2m || q.y > p.ly2p;
+        }
+        out = out || q.z < p.lz2m || q.z > p.lz2p;
+      }
+      if (out) atomicOr(&p.st->err, kErrOutside);
+      if (!in) continue;
+      ib = b;
+      atomicAdd(&p.st->nat[b - 1], 1);
+      p.typei[i] = q.z < p.cz ? -itype : itype;
+    }
+  }
+  p.ibuffer[i] = ib;
+}
+
+__global__ void k_count_fin(KP p) {
+  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) p.st->ntotat[b] += p.st->nat[b];
+}
+
+void launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream) {
+  if (p.nbuffer < 1) return;
+  k_count_zero<<<1, 64, 0, stream>>>(p);
+  const int n = ntot_ub - p.nsites;
+  if (n > 0)
+    (ff ? k_count<true> : k_count<false>)<<<(n + 255) / 256, 256, 0, stream>>>(p);
+  k_count_fin<<<1, 64, 0, stream>>>(p);
+}
+
+// ---------------------------------------------------------------------------
+// GRAND on every replica of a batch (grand.f90:19-121, insert.f90, find.f90):
+// one block per replica, the attempts one after another as the reference
+// makes them, each ΔE the FP64 INTERACT of the single context
+// (trial_single_warp, interact_rec) over the replica's slots, positions read
+// from the float-float records.  The draws are the single context's (the
+// replica's seed, the cycle, the attempt), so a replica makes the moves
+// bromoc_gpu_grand makes on a context holding it.  An accepted move rewrites
+// the records in place: an insertion appends (records, type, buffer, RFPAR
+// gathers), a deletion copies the last ion into the hole.
+// ---------------------------------------------------------------------------
+constexpr int kBgThreads = 256;
+
+__global__ void __launch_bounds__(kBgThreads)
+    k_batch_grand(KP p, const RepDev *rep, RepGc *gcs, int *ibuf, uint32_t mask,
+                  const uint64_t *seeds, uint64_t cycle, int ngcmc) {
+  __shared__ Trial tr;
+  __shared__ int s_n, s_iat, s_acc, s_cnt[kBgThreads / 32];
+  __shared__ double red[kBgThreads / 32], tot[1];
+  const int r = blockIdx.x, tid = threadIdx.x;
+  const RepDev R = rep[r];
+  RepGc &G = gcs[r];
+  const int off = R.off;
+  const uint64_t seed = seeds[r];
+  const bool rf_on = (mask & 16u) && p.qrfpar;
+  if (tid == 0) {
+    s_n = G.n;
+    G.err = 0;
+    G.dener = 0.0;
+  }
+  __syncthreads();
+  // RFPAR gathers of the replica's ions at their positions (interact's cross term)
+  if (rf_on)
+    for (int i = tid; i < s_n; i += blockDim.x) {
+      const double3 q = pos_of(p, true, off + i);
+      p.gc_rf[off + i] = rf_single(p, q.x, q.y, q.z, abs(p.typei[off + i]));
+    }
+  __syncthreads();
+  const int nb = G.nb;
+  for (int a = 0; a < ngcmc; ++a) {
+    const int n = s_n;
+    if (tid == 0) {  // the draws: propose_draws with the replica's box and buffers
+      Trial t{};
+      Draws d{seed, cycle, (uint32_t)a};
+      if (d.next() < 0.5) {
+        const int ib = (int)((double)nb * d.next()) + 1;
+        t.insert = 1;
+        t.ib = ib;
+        if (ib <= nb && G.buf[ib - 1].avnum > 0.0) {
+          const RepBuf &B = G.buf[ib - 1];
+          t.itype = B.ibfftyp;
+          t.valid = 1;
+          bool ok = false;
+          for (int it = 0; it < (1 << 20) && !ok; ++it) {
+            const double u1 = d.next(), u2 = d.next(), u3 = d.next();
+            t.x = G.lx * (u1 - 0.5) + G.cx;
+            t.y = G.ly * (u2 - 0.5) + G.cy;
+            t.z = B.lzmin + (B.lzmax - B.lzmin) * u3;
+            ok = true;
+            if (G.shape == 1) {
+              const double r2 = (t.x - G.cx) * (t.x - G.cx) + (t.y - G.cy) * (t.y - G.cy) +
+                                (t.z - G.cz) * (t.z - G.cz);
+              ok = r2 > B.rmin * B.rmin && r2 < B.rmax * B.rmax;
+            } else if (G.shape == 2) {
+              const double ex = (t.x - G.cx) * G.iecx, ey = (t.y - G.cy) * G.iecy;
+              ok = ex * ex + ey * ey < 1.0;
+            }
+          }
+          if (!ok) {
+            t.valid = 0;
+            G.err |= kErrFind;
+          }
+          t.j = off + n + 1;  // 1-based slot of the newcomer
+          if (t.valid && n + 1 > R.cap) {
+            t.valid = 0;
+            G.err |= kErrCapacity;
+          }
+        }
+      } else {
+        t.ib = (int)((double)nb * d.next()) + 1;
+        const double u_rank = d.next();
+        t.insert = 0;
+        const int natb = t.ib <= nb ? G.buf[t.ib - 1].nat : 0;
+        const int ip = (int)((double)natb * u_rank) + 1;
+        t.valid = t.ib <= nb && ip <= natb;
+        s_iat = ip;  // the rank to find
+      }
+      t.draw = (int)d.n;
+      tr = t;
+    }
+    __syncthreads();
+    if (tr.valid && !tr.insert) {  // find.f90: the ip-th ion of the buffer in slot order
+      const int ib = tr.ib, rank = s_iat;
+      int before = 0, found = -1;
+      for (int c0 = 0; c0 < n && found < 0; c0 += blockDim.x) {
+        const int i = c0 + tid;
+        const bool m = i < n && ibuf[off + i] == ib;
+        const unsigned bal = __ballot_sync(0xffffffffu, m);
+        if ((tid & 31) == 0) s_cnt[tid >> 5] = __popc(bal);
+        __syncthreads();
+        int wb = 0;
+        for (int w = 0; w < (tid >> 5); ++w) wb += s_cnt[w];
+        const int mine = before + wb + __popc(bal & ((1u << (tid & 31)) - 1u)) + 1;
+        if (m && mine == rank) s_acc = i;
+        int all = 0;
+        for (int w = 0; w < kBgThreads / 32; ++w) all += s_cnt[w];
+        __syncthreads();
+        if (before < rank && rank <= before + all) found = s_acc;
+        before += all;
+      }
+      if (tid == 0) {
+        if (found < 0) {
+          tr.valid = 0;
+          G.err |= kErrFind;
+        } else {
+          const double3 q = pos_of(p, true, off + found);
+          tr.j = off + found + 1;
+          tr.itype = G.buf[ib - 1].ibfftyp;
+          tr.x = q.x;
+          tr.y = q.y;
+          tr.z = q.z;
+        }
+      }
+      __syncthreads();
+    }
+    if (!tr.valid) {  // block-uniform; every thread has read tr before it changes
+      __syncthreads();
+      continue;
+    }
+    if (tid < 32) {  // the single-particle terms (warnings not counted in a batch)
+      Trial t = tr;
+      int nalert = 0;
+      trial_single_warp(p, t, mask, tr.insert ? 0 : 1, &nalert);
+      __syncwarp();
+      if (tid == 0) {
+        tr.e_single = t.e_single;
+        tr.srfe = t.srfe;
+        tr.reff = t.reff;
+        tr.rf_in = t.rf_in;
+      }
+    }
+    __syncthreads();
+    const Trial t = tr;
+    const int jt2 = p.nwtype[t.itype];
+    const bool rf = t.rf_in && rf_on;
+    double u = 0.0;
+    int err = 0;
+    for (int i = tid; i < n; i += blockDim.x)
+      if (off + i != t.j - 1) u += interact_rec(p, t, mask, off + i, jt2, true, rf,
+                                                load_part(p, off + i, rf, true), err);
+    if (err) atomicOr(&G.err, err);
+    block_sum<1>(&u, red, tot);
+    if (tid == 0) {  // acceptance (grand.f90:65-116) and the move
+      const double de = t.e_single + tot[0];
+      const RepBuf &B = G.buf[t.ib - 1];
+      const double boltz = exp(-(de - B.mu) * p.ikbt);
+      double rate;
+      const int nat = B.nat;
+      const double bias = B.avnum + B.kb * (B.avnum - (double)(B.ntotat / (long long)cycle));
+      if (t.insert) {
+        rate = B.qbias ? bias * boltz / (double)(nat + 1) : (B.avnum / (nat + 1)) * boltz;
+        rate = rate / (1.0 + rate);
+      } else {
+        rate = B.qbias ? bias * boltz / (double)nat : (B.avnum / nat) * boltz;
+        rate = 1.0 / (1.0 + rate);
+      }
+      Draws d{seed, cycle, (uint32_t)a};
+      d.n = (uint32_t)t.draw;
+      const bool acc = d.next() <= rate;
+      RepBuf &W = G.buf[t.ib - 1];
+      if (acc && t.insert) {
+        const int s = off + n;
+        const float xh = __double2float_rn(t.x), yh = __double2float_rn(t.y),
+                    zh = __double2float_rn(t.z);
+        const int code = (p.nwtype[t.itype] - 1) | (1 << 16);
+        p.pk1[s] = make_float4(xh, yh, zh, __int_as_float(code));
+        p.pk2[s] = make_float4(__double2float_rn(t.x - (double)xh),
+                               __double2float_rn(t.y - (double)yh),
+                               __double2float_rn(t.z - (double)zh), 0.0f);
+        p.pk3[s] = make_float4(0.0f, (float)p.cg[t.itype], __int_as_float(2), 0.0f);
+        p.typei[s] = t.z < G.cz ? -t.itype : t.itype;
+        ibuf[s] = t.ib;
+        if (rf_on) p.gc_rf[s] = rf ? make_double2(t.srfe, t.reff) : make_double2(0.0, 0.0);
+        s_n = n + 1;
+        W.nat += 1;
+        W.ninsert += 1;
+        G.dener += de;
+      } else if (acc) {
+        const int s = t.j - 1, l = off + n - 1;
+        p.pk1[s] = p.pk1[l];
+        p.pk2[s] = p.pk2[l];
+        p.pk3[s] = p.pk3[l];
+        p.typei[s] = p.typei[l];
+        ibuf[s] = ibuf[l];
+        if (rf_on) p.gc_rf[s] = p.gc_rf[l];
+        s_n = n - 1;
+        W.nat -= 1;
+        W.nremove += 1;
+        G.dener -= de;
+      }
+    }
+    __syncthreads();
+  }
+  if (tid == 0) G.n = s_n;
+}
+
+// COUNT of every replica (count.f90 with the replica's box and buffers):
+// one block per replica, nat by shared-memory integer atomics.
+__global__ void __launch_bounds__(kBgThreads)
+    k_batch_count(KP p, const RepDev *rep, RepGc *gcs, int *ibuf) {
+  __shared__ int nat[kBatchMaxBuf], bad;
+  const RepDev R = rep[blockIdx.x];
+  RepGc &G = gcs[blockIdx.x];
+  const int nb = G.nb;
+  if (threadIdx.x < kBatchMaxBuf) nat[threadIdx.x] = 0;
+  if (threadIdx.x == 0) bad = 0;
+  __syncthreads();
+  for (int i = threadIdx.x; i < G.n; i += blockDim.x) {
+    const int s = R.off + i;
+    const double3 q = pos_of(p, true, s);
+    const int itype = abs(p.typei[s]);
+    int ib = 0;
+    for (int b = 1; b <= nb && !ib; ++b) {
+      const RepBuf &B = G.buf[b - 1];
+      if (itype != B.ibfftyp || !(q.z >= B.lzmin && q.z <= B.lzmax)) continue;
+      bool out = false, in = true;
+      if (G.shape == 1) {
+        const double r2 = (q.x - G.cx) * (q.x - G.cx) + (q.y - G.cy) * (q.y - G.cy) +
+                          (q.z - G.cz) * (q.z - G.cz);
+        out = r2 > G.rsphe2;
+        in = r2 >= B.rmin * B.rmin && r2 <= B.rmax * B.rmax;
+      } else {
+        if (G.shape == 2) {
+          const double ex = (q.x - G.cx) * G.iecx, ey = (q.y - G.cy) * G.iecy;
+          out = ex * ex + ey * ey > 1.0;
+        } else {
+          out = q.x < G.cx - 0.5 * G.lx || q.x > G.cx + 0.5 * G.lx ||
+                q.y < G.cy - 0.5 * G.ly || q.y > G.cy + 0.5 * G.ly;
+        }
+        out = out || q.z < G.cz - 0.5 * G.lz || q.z > G.cz + 0.5 * G.lz;
+      }
+      if (out) bad = 1;
+      if (!in) continue;
+      ib = b;
+      atomicAdd(&nat[b - 1], 1);
+      p.typei[s] = q.z < G.cz ? -itype : itype;
+    }
+    ibuf[s] = ib;
+  }
+  __syncthreads();
+  if (threadIdx.x < nb) {
+    G.buf[threadIdx.x].nat = nat[threadIdx.x];
+    G.buf[threadIdx.x].ntotat += nat[threadIdx.x];
+  }
+  if (threadIdx.x == 0 && bad) G.err |= kErrOutside;
+}
+
+void launch_batch_count(const KP &p, const RepDev *rep, RepGc *gc, int *ibuf, int nrep,
+                        cudaStream_t stream) {
+  if (nrep > 0) k_batch_count<<<nrep, kBgThreads, 0, stream>>>(p, rep, gc, ibuf);
+}
+
+void launch_batch_grand(const KP &p, const RepDev *rep, RepGc *gc, int *ibuf, int nrep,
+                        uint32_t mask, const uint64_t *seeds, uint64_t cycle, int ngcmc,
+                        cudaStream_t stream) {
+  if (nrep <= 0 || ngcmc <= 0) return;
+  k_batch_grand<<<nrep, kBgThreads, 0, stream>>>(p, rep, gc, ibuf, mask, seeds, cycle, ngcmc);
 }
 
 }  // namespace bgpu

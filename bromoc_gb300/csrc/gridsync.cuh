@@ -31,10 +31,12 @@ __device__ __forceinline__ void release_add(unsigned *ctr, unsigned v) {
   a.fetch_add(v, cuda::memory_order_release);
 }
 
-// Block-wide: thread 0 waits, everyone learns the outcome.
+// Block-wide: thread 0 waits (polling without sleeps: the waits of GRAND's
+// rounds are a few microseconds, and a sleep's wake-up adds to each),
+// everyone learns the outcome.
 __device__ __forceinline__ bool block_wait(unsigned *ctr, unsigned target, DevState *st,
                                            int *flag) {
-  if (threadIdx.x == 0) *flag = wait_at_least(ctr, target, st) ? 1 : 0;
+  if (threadIdx.x == 0) *flag = wait_at_least(ctr, target, st, false) ? 1 : 0;
   __syncthreads();
   const bool ok = *flag != 0;
   __syncthreads();

@@ -99,6 +99,8 @@ struct NucDev {
   const double *ck;             // [3*ctn] (kx, ky, kz) per entry
   const double *cc;             // [3*(ctn+1)] anchors (x, y, z) per entry
   double *cf;                   // [8] centre force per strand and axis, econ
+  int qnotr[3];                 // NOTRAN: recentre the sites along these axes
+  double notr[3];
 };
 
 // Reaction field of the MMIJ basis (gsbpmod): RECTBOX Legendre products or

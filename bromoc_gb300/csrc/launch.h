@@ -65,6 +65,10 @@ int launch_mmij(const KP &p, bool fp32, int ntot_ub, int qforces, int slot,
                 cudaStream_t stream);
 void launch_mmij_interact(const KP &p, int ntot_ub, double *dener, cudaStream_t stream);
 
+// gcmc.cu: COUNT (count.f90) on the device; ff: positions from the
+// float-float records
+void launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream);
+
 // analysis.cu: per-cycle profiles (counts) and .btr frames
 struct ProfArgs {
   int rho, rdna, gr;        // which profiles accumulate
@@ -84,6 +88,9 @@ void launch_traj_pack(const KP &p, bool fp32, int n, double runtime, uint32_t *w
 // sites (added when accum, else written), energies into one slot
 int launch_nucl(const KP &p, bool fp32, uint32_t mask, int qforces, int accum, int slot,
                 cudaStream_t stream);
+// NOTRAN after a BD step: the sites' centre back to notr along the flagged
+// axes (one block); returns the launches (0 when off)
+int launch_notrans(const KP &p, bool fp32, cudaStream_t stream);
 // INTERACT of site j (0-based): adds its bonded/Go terms to *dener
 void launch_nucl_interact(const KP &p, uint32_t mask, int j, double *dener,
                           cudaStream_t stream);

@@ -402,6 +402,55 @@ __global__ void __launch_bounds__(kNucReduceThreads)
   if (threadIdx.x == 0) *dener += tot[0];
 }
 
+// NOTRAN (simul1.f90:380-385): x(1:nsites) = x(1:nsites) - sum(x)*insites
+// + notrx per flagged axis, after the move; the sum as a fixed tree in FP64.
+template <bool F32>
+__global__ void __launch_bounds__(kNucReduceThreads) k_notrans(KP p) {
+  const NucDev &n = p.nuc;
+  __shared__ double red[(kNucReduceThreads / 32) * 3];
+  __shared__ double tot[3];
+  const int ns = p.nsites;
+  double v[3] = {0.0, 0.0, 0.0};
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    double r[3];
+    site_pos<F32>(p, j, r);
+#pragma unroll
+    for (int c = 0; c < 3; ++c) v[c] += r[c];
+  }
+  block_sum<3>(v, red, tot);
+  const double insites = 1.0 / ns;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    double r[3];
+    site_pos<F32>(p, j, r);
+#pragma unroll
+    for (int c = 0; c < 3; ++c)
+      if (n.qnotr[c]) r[c] = r[c] - tot[c] * insites + n.notr[c];
+    if (F32) {
+      float4 h = p.pk1[j], l = p.pk2[j];
+      float *hc[3] = {&h.x, &h.y, &h.z}, *lc[3] = {&l.x, &l.y, &l.z};
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {
+        if (!n.qnotr[c]) continue;
+        *hc[c] = __double2float_rn(r[c]);
+        *lc[c] = __double2float_rn(r[c] - (double)*hc[c]);
+      }
+      p.pk1[j] = h;
+      p.pk2[j] = l;
+    } else {
+      if (n.qnotr[0]) p.x[j] = r[0];
+      if (n.qnotr[1]) p.y[j] = r[1];
+      if (n.qnotr[2]) p.z[j] = r[2];
+    }
+  }
+}
+
+int launch_notrans(const KP &p, bool fp32, cudaStream_t stream) {
+  const NucDev &n = p.nuc;
+  if (p.nsites <= 0 || !(n.qnotr[0] || n.qnotr[1] || n.qnotr[2])) return 0;
+  (fp32 ? k_notrans<true> : k_notrans<false>)<<<1, kNucReduceThreads, 0, stream>>>(p);
+  return 1;
+}
+
 int launch_nucl(const KP &p, bool fp32, uint32_t mask, int qforces, int accum, int slot,
                 cudaStream_t stream) {
   const NucDev &n = p.nuc;

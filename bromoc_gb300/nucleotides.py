@@ -69,6 +69,7 @@ class Topology:
     contr_second: tuple = (0.0, 0.0, 0.0)        # anchor of the second strand's centre
     qunsplit: bool = False
     nsites1st: int = 0
+    notrans: tuple = (None, None, None)          # NOTRAN centre per axis, None = off
 
     def counts(self) -> dict:
         return {"bond": len(self.bonds), "angle": len(self.angles), "dihe": len(self.dihes),
@@ -126,6 +127,9 @@ class Topology:
             contrx=ptr(anchors[0], C.c_double), contry=ptr(anchors[1], C.c_double),
             contrz=ptr(anchors[2], C.c_double),
             qunsplit=int(self.qunsplit), nsites1st=self.nsites1st)
+        for a in range(3):
+            s.qnotr[a] = int(self.notrans[a] is not None)
+            s.notr[a] = float(self.notrans[a] or 0.0)
         return s, keep
 
 

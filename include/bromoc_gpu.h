@@ -200,6 +200,10 @@ typedef struct bromoc_nucleotides {
                                        /* the second strand's centre (unsplit) */
   int32_t qunsplit;          /* centre springs per strand (two strands)      */
   int32_t nsites1st;         /* sites of the first strand                    */
+  /* NOTRAN (simul1.f90:380-385): after every BD step the sites' centre
+   * along each flagged axis is put back to notr (x - sum(x)/nsites + notr) */
+  int32_t qnotr[3];
+  double notr[3];
 } bromoc_nucleotides;
 
 /* Reaction field of the MMIJ basis (GSBP mmij keywords,
@@ -372,8 +376,10 @@ int bromoc_gpu_bd_steps_host(bromoc_ctx *ctx, uint32_t terms, int32_t variant,
  * device and written back with the new *ntot (GCMC changes it); entries
  * past the new *ntot may be overwritten too (up to *ntot + ncycle*ngcmc).
  * Cycles are numbered cycle0, cycle0+1, ...; BD steps
- * (cycle-1)*nbd + istep - 1.  The work is queued in stream order with one
- * wait at the end: the call returns when the arrays hold the result. */
+ * (cycle-1)*nbd + istep - 1.  Each cycle ends with COUNT (and, when
+ * switched on, a profile sample), as simul1.f90 does.  The work is queued in
+ * stream order with one wait at the end: the call returns when the arrays
+ * hold the result. */
 int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms,
                                  int32_t variant, int32_t ncycle,
                                  int32_t ngcmc, int32_t nbd, uint64_t seed,
@@ -502,6 +508,16 @@ int bromoc_gpu_get_countions(bromoc_ctx *ctx, int32_t *nforward,
  * ENERGY call (energy.mono.f90:603-621), 5 doubles per particle. */
 int bromoc_gpu_get_dids(bromoc_ctx *ctx, double *dids);
 
+/* COUNT (count.f90:19-95; simul1.f90:462 calls it once a cycle, after the
+ * BD steps): each mobile ion's buffer from its position, nat, the sign of a
+ * buffer ion's type by its side of cz, then ntotat += nat.  Queued without
+ * a wait; a buffer ion outside the system is reported as BROMOC_E_DEVICE by
+ * the next call that reads the device flags.  No-op without buffers.
+ * bromoc_gpu_simul_cycles_host runs it every cycle. */
+int bromoc_gpu_count(bromoc_ctx *ctx);
+/* ntotat of every buffer (the running sum of nat that the kb bias uses). */
+int bromoc_gpu_get_ntotat(bromoc_ctx *ctx, int32_t *ntotat);
+
 /* ---- per-cycle analysis (simul1.f90:176-188, 476-509) ---------------------
  * Switch the z-density profile of the mobile ions (qrho, RHO), of the DNA
  * sites (qrdna, RHDNA) and the radial distribution of the mobile ions
@@ -558,6 +574,29 @@ int bromoc_batch_destroy(bromoc_batch *b);
 const char *bromoc_batch_last_error(const bromoc_batch *b);
 /* per-replica SYSTEM blocks: box/shape for fixcoor; dt, kbt, bdmax checked */
 int bromoc_batch_set_systems(bromoc_batch *b, const bromoc_system *sys);
+/* GCMC buffers of replica r (grand.f90 with the prototype's ion types):
+ * 1..8 buffers, the geometry in the replica's own coordinates, their
+ * counts, and ibuffer[n] the buffer of each of its ions (0 none).  A later
+ * set_particles of r clears its ibuffer. */
+int bromoc_batch_set_buffers(bromoc_batch *b, int32_t r, const bromoc_buffers *buf,
+                             const int32_t *ibuffer);
+/* ngcmc GCMC attempts on every replica (grand.f90:19-121): one launch, a
+ * block per replica, the attempts in order with FP64 ΔE (INTERACT on the
+ * replica's records).  Replica r draws from seeds[r] with the single
+ * context's counters, so it makes the moves bromoc_gpu_grand would make on
+ * a context holding it.  dener[r] (optional): the summed ΔE of its accepted
+ * moves.  Waits for the result; the replicas' counts then drive the next
+ * bd_steps (the work lists follow them; the pair-kernel tuning stands).
+ * Deletion warnings are not counted in a batch; ntotat stays as set. */
+int bromoc_batch_grand(bromoc_batch *b, uint32_t terms, int32_t ngcmc,
+                       const uint64_t *seeds, uint64_t cycle, double *dener);
+/* COUNT (count.f90) on every replica with buffers: buffer tags, nat, type
+ * signs, ntotat += nat (one launch; waits). */
+int bromoc_batch_count(bromoc_batch *b);
+/* Replica r's buffer counters and its ions' signed types and buffers
+ * (typei/ibuffer: its current count of entries; NULL skips). */
+int bromoc_batch_get_buffers(bromoc_batch *b, int32_t r, int32_t *nat, int32_t *ninsert,
+                             int32_t *nremove, int32_t *typei, int32_t *ibuffer);
 int bromoc_batch_set_particles(bromoc_batch *b, int32_t r, int32_t n, const double *x,
                                const double *y, const double *z, const int32_t *typei);
 int bromoc_batch_get_particles(bromoc_batch *b, int32_t r, int32_t *n, double *x,

@@ -131,6 +131,8 @@ module bromoc_gpu
     type(c_ptr) :: contrz
     integer(c_int32_t) :: qunsplit
     integer(c_int32_t) :: nsites1st
+    integer(c_int32_t) :: qnotr(3)
+    real(c_double) :: notr(3)
   end type bromoc_nucleotides
 
   ! gsbpmod's MMIJ basis: RECTBOX orders and region, or SPHERE nmpol/srdist
@@ -425,6 +427,17 @@ module bromoc_gpu
       import :: c_int, c_ptr, c_double
       type(c_ptr), value :: ctx
       real(c_double), intent(out) :: dids(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_count(ctx) bind(C, name="bromoc_gpu_count") result(rc)
+      import :: c_int, c_ptr
+      type(c_ptr), value :: ctx
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_get_ntotat(ctx, ntotat) bind(C, name="bromoc_gpu_get_ntotat") result(rc)
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), intent(out) :: ntotat(*)
       integer(c_int) :: rc
     end function
     function bromoc_gpu_set_profiles(ctx, qrho, qrdna, qgr, igr, dr, npoints) &

@@ -55,6 +55,9 @@ int bromoc_ref_bd_steps(bromoc_ref *r, uint32_t terms, int32_t variant,
                         double *eterms);
 int bromoc_ref_grand(bromoc_ref *r, uint32_t terms, int32_t ngcmc,
                      uint64_t seed, uint64_t cycle, double *dener_sum);
+/* count.f90 (buffer membership, nat, ntotat) */
+int bromoc_ref_count(bromoc_ref *r);
+int bromoc_ref_get_ntotat(bromoc_ref *r, int32_t *ntotat);
 int bromoc_ref_get_buffers(bromoc_ref *r, int32_t *nat, int32_t *ninsert,
                            int32_t *nremove, int32_t *prob);
 int bromoc_ref_get_countions(bromoc_ref *r, int32_t *nforward,

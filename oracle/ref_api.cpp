@@ -231,6 +231,10 @@ int bromoc_ref_set_nucleotides(bromoc_ref *r, const bromoc_nucleotides *q) {
   n.epsolv = q->epsolv;
   n.qunsplit = q->qunsplit != 0;
   n.nsites1st = q->nsites1st;
+  for (int a = 0; a < 3; ++a) {
+    n.qnotr[a] = q->qnotr[a] != 0;
+    n.notr[a] = q->notr[a];
+  }
   n.on = true;
   return BROMOC_OK;
 }
@@ -576,6 +580,20 @@ int bromoc_ref_metropolis(bromoc_ref *r, uint32_t terms, int32_t nmcm, double mc
   bref::metropolis(r->s, terms, nmcm, mcmax, seed, cycle, d, na);
   if (naccept) *naccept = na;
   if (dener_sum) *dener_sum = d;
+  return BROMOC_OK;
+}
+
+int bromoc_ref_count(bromoc_ref *r) {
+  if (!r) return BROMOC_E_ARG;
+  State &s = r->s;
+  if (s.nbuffer < 1) return BROMOC_OK;
+  if (!bref::count(s)) return fail(r, "count: particles outside main system", BROMOC_E_DEVICE);
+  return BROMOC_OK;
+}
+
+int bromoc_ref_get_ntotat(bromoc_ref *r, int32_t *ntotat) {
+  if (!r || !ntotat) return BROMOC_E_ARG;
+  for (int i = 0; i < r->s.nbuffer; ++i) ntotat[i] = r->s.ntotat[i + 1];
   return BROMOC_OK;
 }
 

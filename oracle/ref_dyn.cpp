@@ -215,6 +215,20 @@ void dynamics(State &s, int variant, uint64_t seed, uint64_t step) {
     if (q.qcountion) countions(s, zold, s.z[i], itype - s.nold);
     fixcoor(s, s.x[i], s.y[i], s.z[i]);
   }
+  // NOTRAN (simul1.f90:380-385): x(1:nsites) = x(1:nsites) -
+  // sum(x(1:nsites))*insites + notrx along each flagged axis
+  const Nucl &n = s.nuc;
+  if (n.on && s.nsites > 0) {
+    const double insites = 1.0 / s.nsites;
+    std::vector<double> *pos[3] = {&s.x, &s.y, &s.z};
+    for (int a = 0; a < 3; ++a) {
+      if (!n.qnotr[a]) continue;
+      std::vector<double> &v = *pos[a];
+      double sm = 0.0;
+      for (int i = 1; i <= s.nsites; ++i) sm = sm + v[i];
+      for (int i = 1; i <= s.nsites; ++i) v[i] = v[i] - sm * insites + n.notr[a];
+    }
+  }
 }
 
 // insert.f90:19-44.  Uniform draws come from the attempt's stream.
@@ -250,6 +264,45 @@ static int find(const State &s, int ib, int nini, int ip) {
     }
   }
   return iat;  // the Fortran do-variable after loop exhaustion
+}
+
+// count.f90:19-95: each mobile ion's buffer (the first whose ion type and
+// z range -- and for a sphere the radial shell -- hold it), nat, the sign of
+// a buffer ion's type by its side of cz, then ntotat += nat.  A particle
+// outside the system is the reference's fatal error: false.
+bool count(State &s) {
+  const bromoc_system &q = s.sys;
+  for (int ib = 1; ib <= s.nbuffer; ++ib) s.nat[ib] = 0;
+  bool ok = true;
+  for (int i = s.nsites + 1; i <= s.ntot; ++i) {
+    s.ibuffer[i] = 0;
+    if (i <= s.nsites + s.nfix) continue;
+    const int itype = std::abs(s.typei[i]);
+    bool endlog = false;
+    for (int ib = 1; ib <= s.nbuffer && !endlog; ++ib) {
+      if (itype != s.ibfftyp[ib] || !(s.z[i] >= s.lzmin[ib] && s.z[i] <= s.lzmax[ib])) continue;
+      if (q.shape == BROMOC_SPHERE) {
+        const double r2 = (s.x[i] - q.cx) * (s.x[i] - q.cx) + (s.y[i] - q.cy) * (s.y[i] - q.cy) +
+                          (s.z[i] - q.cz) * (s.z[i] - q.cz);
+        if (r2 > s.rsphe2) ok = false;
+        if (!(r2 >= s.rmin[ib] * s.rmin[ib] && r2 <= s.rmax[ib] * s.rmax[ib])) continue;
+      } else {
+        if (q.shape == BROMOC_ECYL) {
+          const double ex = (s.x[i] - q.cx) * s.iecx, ey = (s.y[i] - q.cy) * s.iecy;
+          if (ex * ex + ey * ey > 1.0) ok = false;
+        } else if (s.x[i] < s.lx2m || s.x[i] > s.lx2p || s.y[i] < s.ly2m || s.y[i] > s.ly2p) {
+          ok = false;
+        }
+        if (s.z[i] < s.lz2m || s.z[i] > s.lz2p) ok = false;
+      }
+      s.ibuffer[i] = ib;
+      s.nat[ib] += 1;
+      s.typei[i] = s.z[i] < q.cz ? -itype : itype;
+      endlog = true;
+    }
+  }
+  for (int ib = 1; ib <= s.nbuffer; ++ib) s.ntotat[ib] += s.nat[ib];
+  return ok;
 }
 
 // grand.f90:19-121

@@ -66,6 +66,8 @@ struct Nucl {
   std::vector<uint8_t> bpgc;
   std::vector<int> sn, csn;
   std::vector<double> af, kx, ky, kz, contrx, contry, contrz;
+  int qnotr[3] = {0, 0, 0};  // NOTRAN axes and centres
+  double notr[3] = {0, 0, 0};
 };
 
 // Reaction field of the MMIJ basis (gsbpmod): RECTBOX Legendre products or
@@ -223,6 +225,8 @@ void fixcoor(const State &s, double &xi, double &yi, double &zi);
 void dynamics(State &s, int variant, uint64_t seed, uint64_t step);
 void grand(State &s, uint32_t mask, int ngcmc, uint64_t seed, uint64_t icycle,
            double &dener_sum);
+// count.f90:19-95 (false: a particle lies outside the system)
+bool count(State &s);
 
 // noise: Philox4x32-10 (Salmon et al., SC'11) + Box-Muller cos branch
 void philox4x32_10(const uint32_t ctr[4], const uint32_t key[2],

@@ -69,7 +69,11 @@ def c_structs():
             for part in names.split(","):
                 part = part.strip()
                 kind = "ptr" if part.startswith("*") else C_SCALAR[base]
-                fl.append((part.lstrip("*").strip(), kind))
+                field = part.lstrip("*").strip()
+                if "[" in field:  # a fixed array: name[n] -> (name, kind x n)
+                    field, n = field[:-1].split("[")
+                    kind = f"{kind}x{int(n)}"
+                fl.append((field, kind))
         out[name] = fl
     return out
 
@@ -86,7 +90,13 @@ def f_types():
             decl, names = line.split("::")
             decl = decl.strip()
             kind = "ptr" if decl == "type(c_ptr)" else F_KIND[decl]
-            fl.extend((n.strip(), kind) for n in names.split(","))
+            for n in names.split(","):
+                n = n.strip()
+                if "(" in n:  # a fixed array: name(n) -> (name, kind x n)
+                    n, dim = n[:-1].split("(")
+                    fl.append((n, f"{kind}x{int(dim)}"))
+                else:
+                    fl.append((n, kind))
         out[name] = fl
     return out
 

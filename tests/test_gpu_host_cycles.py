@@ -55,6 +55,7 @@ def _stepwise(g, ncycle, cycle0):
         cyc = cycle0 + c
         g.grand(NGCMC, SEED, cyc, dener=False)
         e = g.bd_steps(NBD, seed=SEED, step0=(cyc - 1) * NBD, energies=c + 1 == ncycle)
+        g.count()  # simul1.f90:462
     return e
 
 

@@ -106,3 +106,22 @@ def test_bad_lists_are_refused(gpu_lib):
         g.set_nucleotides(bad)
     # the context still works and has no lists
     assert g.energy(abi.M_ALL)[0]["ebond"] == 0.0
+
+
+@pytest.mark.parametrize("prec", [abi.FP64, abi.FP32])
+def test_notrans_recentres_the_sites(gpu_lib, oracle_mod, prec):
+    """NOTRAN (simul1.f90:380-385): after every BD step the sites' centre
+    along x and z is back at the given values; positions match the oracle."""
+    spec = systems.dna_duplex(precision=prec)
+    spec.nucl.notrans = (0.5, None, -1.25)
+    g, o = _engines(spec, gpu_lib, oracle_mod)
+    g.bd_steps(3, seed=12, step0=0, energies=False)
+    o.bd_steps(3, seed=12, step0=0)
+    pg = np.stack(g.get_particles()[:3], 1)
+    po = np.stack(o.get_particles()[:3], 1)
+    tol = 1e-9 if prec == abi.FP64 else 1e-5
+    assert np.abs(pg - po).max() <= tol
+    ns = spec.nsites
+    c = pg[:ns].mean(0)
+    assert abs(c[0] - 0.5) <= 1e-6 and abs(c[2] + 1.25) <= 1e-6
+    assert abs(c[1] - np.asarray(spec.y[:ns]).mean()) > 1e-6  # y is left free

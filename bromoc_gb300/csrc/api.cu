@@ -490,8 +490,19 @@ int plan_energy(bromoc_ctx *ctx, uint32_t mask, bool reduce, EnergyPlan &plan,
     plan.t_rf = fl.rf ? next_timer(ctx, BROMOC_K_RFCROSS) : nullptr;
     plan.t_fields = plan.ntot_ub > 0 ? next_timer(ctx, BROMOC_K_FIELDS) : nullptr;
   }
-  if (energy_slots(p, plan, mask) > ctx->nslot_cap)
-    return set_err(ctx, BROMOC_E_ARG, "energy slots exceed scratch");
+  const int need = energy_slots(p, plan, mask);
+  if (need > ctx->nslot_cap) {  // e.g. many DNA terms: grow the block partials
+    CU(cudaStreamSynchronize(ctx->stream));
+    dfree(ctx, p.epart);
+    p.epart = nullptr;
+    const int ncap = need + 64;
+    int rc = dalloc(ctx, &p.epart, (size_t)ncap * kNTerms);
+    if (rc) {
+      ctx->nslot_cap = 0;
+      return rc;
+    }
+    ctx->nslot_cap = ncap;
+  }
   return BROMOC_OK;
 }
 
@@ -987,6 +998,20 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
   p.typtyp = t;
   p.sitecharge = c;
   p.stfree = f;
+  if (!rc && ctx->precision == BROMOC_FP32) {  // partials of the FP32 ion-site tiles
+    for (void *a : {(void *)p.isp_ion, (void *)p.isp_site, (void *)p.isp_dids,
+                    (void *)p.isp_seed})
+      dfree(ctx, a);
+    p.isp_ion = p.isp_site = p.isp_dids = p.isp_seed = nullptr;
+    p.isp_tcap = 0;
+    const size_t S = (s->nsites + 31) / 32, cap = p.cap;
+    const int T = (int)((cap + 31) / 32);
+    rc = dalloc(ctx, &p.isp_ion, S * 3 * cap);
+    if (!rc) rc = dalloc(ctx, &p.isp_dids, S * 6 * cap);
+    if (!rc) rc = dalloc(ctx, &p.isp_seed, 5 * cap);
+    if (!rc) rc = dalloc(ctx, &p.isp_site, (size_t)T * 3 * s->nsites);
+    if (!rc) p.isp_tcap = T;
+  }
   ctx->site_map.clear();
   if (!rc && s->phiv_map) {
     if (p.qphiv && p.qnmcden) {
@@ -1990,8 +2015,7 @@ int bromoc_gpu_count(bromoc_ctx *ctx) {
   if (ctx->kp.nbuffer < 1) return BROMOC_OK;
   const bool ff = ctx->precision == BROMOC_FP32;
   if ((rc = ff ? ensure_ff(ctx) : ensure_dbl(ctx))) return rc;
-  launch_count(ctx->kp, ff, ntot_ub(ctx), ctx->stream);
-  ctx->launches += 3;
+  ctx->launches += launch_count(ctx->kp, ff, ntot_ub(ctx), ctx->stream);
   CU(cudaGetLastError());
   return BROMOC_OK;
 }

@@ -674,7 +674,10 @@ int bromoc_batch_grand(bromoc_batch *b, uint32_t terms, int32_t ngcmc, const uin
                       b->stream));
   BCU(cudaMemcpyAsync(b->d_seeds, seeds, b->nrep * sizeof(uint64_t), cudaMemcpyHostToDevice,
                       b->stream));
-  launch_batch_grand(b->kp, b->rep, b->gc, b->ibuf, b->nrep, terms, b->d_seeds, cycle, ngcmc,
+  KP p = b->kp;  // the batch's own records (the block keeps the prototype's)
+  p.pk1 = b->pk1[b->cur];
+  p.pk2 = b->pk2[b->cur];
+  launch_batch_grand(p, b->rep, b->gc, b->ibuf, b->nrep, terms, b->d_seeds, cycle, ngcmc,
                      b->stream);
   ++b->launches;
   BCU(cudaGetLastError());
@@ -712,7 +715,10 @@ int bromoc_batch_count(bromoc_batch *b) {
   }
   BCU(cudaMemcpyAsync(b->gc, b->gc_h.data(), b->nrep * sizeof(RepGc), cudaMemcpyHostToDevice,
                       b->stream));
-  launch_batch_count(b->kp, b->rep, b->gc, b->ibuf, b->nrep, b->stream);
+  KP p = b->kp;
+  p.pk1 = b->pk1[b->cur];
+  p.pk2 = b->pk2[b->cur];
+  launch_batch_count(p, b->rep, b->gc, b->ibuf, b->nrep, b->stream);
   ++b->launches;
   BCU(cudaGetLastError());
   BCU(cudaMemcpyAsync(b->gc_h.data(), b->gc, b->nrep * sizeof(RepGc), cudaMemcpyDeviceToHost,

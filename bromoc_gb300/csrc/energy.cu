@@ -433,6 +433,204 @@ __global__ void __launch_bounds__(kPairThreads)
   }
 }
 
+// Ion-site pairs as tiles: one warp per (ion tile of 32, site tile of 32),
+// lane l holds ion 32 t + l and meets site (l + k) mod 32 at step k, so in
+// each step the lanes touch distinct site slots and the site sums need no
+// atomics.  The same per-pair law, energies and forces as k_ionsite32 /
+// k_siteforce32 (the pair's r^2 and de are the same numbers on both sides);
+// the PROXDIFF record keeps, per site tile, the smallest dist - mindist over
+// sites j >= 1 (ties: the smaller j), and the first site's own record, which
+// k_ionsite_sum combines in the reference's site order (energy.mono.f90:
+// 603-621: site 1 seeds it, a later site replaces it only when smaller).
+constexpr int kIsWarps = 4;
+
+__global__ void __launch_bounds__(32 * kIsWarps)
+    k_ionsite_tiles(KP p, int qforces, int slot0, int S, int nwork) {
+  __shared__ float4 sh[kIsWarps][32], sl[kIsWarps][32];
+  __shared__ float sf[kIsWarps][3][32];
+  __shared__ float red[kIsWarps * 4];
+  __shared__ float tot[4];
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int wi = blockIdx.x * kIsWarps + w;
+  const int ntot = p.st->ntot, ns = p.nsites;
+  float e[4] = {0.f, 0.f, 0.f, 0.f};
+  int err = 0;
+  if (wi < nwork) {  // warp-uniform
+    const int t = wi / S, s = wi - t * S;
+    const int j0 = 32 * s, jl = j0 + lane;
+    const bool jv = jl < ns;
+    sh[w][lane] = jv ? p.pk1[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sl[w][lane] = jv ? p.pk2[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
+    sf[w][0][lane] = sf[w][1][lane] = sf[w][2][lane] = 0.f;
+    const int i = ns + 32 * t + lane;
+    const bool iv = i < ntot;
+    const bool mobile = i >= ns + p.nfix;
+    float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
+    if (iv) {
+      th = p.pk1[i];
+      tl = p.pk2[i];
+    }
+    const int row = (__float_as_int(th.w) & 0xffff) * p.nttyp;
+    const int nj = min(32, ns - j0);
+    float f[3] = {0.f, 0.f, 0.f};
+    float bv = 3.4e38f, bd = 0.f, bx = 0.f, by = 0.f, bz = 0.f;  // best j >= 1
+    int bj = 1 << 30;
+    float seed[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+    __syncwarp();
+    for (int k = 0; k < 32; ++k) {
+      const int m = (lane + k) & 31;
+      float g0 = 0.f, g1 = 0.f, g2 = 0.f;
+      if (iv && m < nj) {
+        const float4 h = sh[w][m], l = sl[w][m];
+        const int is = p.pidx[row + (__float_as_int(h.w) & 0xffff)];
+        const PairParamF &q = p.ppf[is];
+        const float dx = ff_diff(th.x, tl.x, h.x, l.x), dy = ff_diff(th.y, tl.y, h.y, l.y),
+                    dz = ff_diff(th.z, tl.z, h.z, l.z);
+        const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
+        const float de = law32(p, q, r2, 1.0f, e, err, [&] { return r2_ff64(th, tl, h, l); });
+        const int j = j0 + m;
+        if (p.qproxdiff && (q.flags & kEfp) && r2 >= q.dm2lo && r2 <= q.dm2hi) {
+          const float dist = sqrtf(r2);
+          const float dm = dist - q.dmi;
+          if (dist > 0.0f) {
+            if (j == 0) {
+              seed[0] = dm;
+              seed[1] = dist;
+              seed[2] = dx;
+              seed[3] = dy;
+              seed[4] = dz;
+            } else if (dm < bv || (dm == bv && j < bj)) {
+              bv = dm;
+              bj = j;
+              bd = dist;
+              bx = dx;
+              by = dy;
+              bz = dz;
+            }
+          }
+        }
+        if (qforces && mobile) {
+          f[0] = fmaf(de, dx, f[0]);
+          f[1] = fmaf(de, dy, f[1]);
+          f[2] = fmaf(de, dz, f[2]);
+        }
+        if (qforces && p.stfree[j]) {
+          g0 = -de * dx;
+          g1 = -de * dy;
+          g2 = -de * dz;
+        }
+      }
+      // slot m is this lane's alone in this step
+      sf[w][0][m] += g0;
+      sf[w][1][m] += g1;
+      sf[w][2][m] += g2;
+      __syncwarp();
+    }
+    if (iv) {
+      const size_t cap = p.cap;
+      float *o = p.isp_ion + (size_t)s * 3 * cap;
+      o[i] = f[0];
+      o[cap + i] = f[1];
+      o[2 * cap + i] = f[2];
+      if (p.qproxdiff) {
+        float *d = p.isp_dids + (size_t)s * 6 * cap;
+        d[i] = bv;
+        d[cap + i] = __int_as_float(bj);
+        d[2 * cap + i] = bd;
+        d[3 * cap + i] = bx;
+        d[4 * cap + i] = by;
+        d[5 * cap + i] = bz;
+        if (s == 0)
+          for (int c = 0; c < 5; ++c) p.isp_seed[c * cap + i] = seed[c];
+      }
+    }
+    if (jl < ns) {
+      float *o = p.isp_site + (size_t)t * 3 * ns;
+      o[jl] = sf[w][0][lane];
+      o[ns + jl] = sf[w][1][lane];
+      o[2 * ns + jl] = sf[w][2][lane];
+    }
+  }
+  if (err) atomicOr(&p.st->err, err);
+  block_sum_f<4>(e, red, tot);
+  if (threadIdx.x == 0) {
+    double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
+    for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
+    dst[5] = tot[0];
+    dst[6] = tot[1];
+    dst[7] = tot[2];
+    dst[8] = tot[3];
+  }
+}
+
+// Ion forces: the site tiles' partials in tile order; PROXDIFF: the first
+// site's record, replaced by the smallest later one (smaller j on ties) only
+// when it is below; site forces: the ion tiles' partials in tile order.
+__global__ void __launch_bounds__(256) k_ionsite_sum(KP p, int qforces, int S, int T) {
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  const int ntot = p.st->ntot, ns = p.nsites;
+  const size_t cap = p.cap;
+  const int nion = ntot - ns;
+  if (k < nion) {
+    const int i = ns + k;
+    float f[3] = {0.f, 0.f, 0.f};
+    for (int s = 0; s < S; ++s) {
+      const float *o = p.isp_ion + (size_t)s * 3 * cap;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] += o[c * cap + i];
+    }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p.fis_f[c * cap + i] = qforces ? f[c] : 0.f;
+    if (p.qproxdiff) {
+      float d[5];
+      for (int c = 0; c < 5; ++c) d[c] = p.isp_seed[c * cap + i];
+      float bv = 3.4e38f;
+      int bj = 1 << 30, bs = -1;
+      for (int s = 0; s < S; ++s) {
+        const float *o = p.isp_dids + (size_t)s * 6 * cap;
+        const float v = o[i];
+        const int j = __float_as_int(o[cap + i]);
+        if (v < bv || (v == bv && j < bj)) {
+          bv = v;
+          bj = j;
+          bs = s;
+        }
+      }
+      if (bs >= 0 && bv < d[0]) {
+        const float *o = p.isp_dids + (size_t)bs * 6 * cap;
+        d[0] = bv;
+        d[1] = o[2 * cap + i];
+        d[2] = o[3 * cap + i];
+        d[3] = o[4 * cap + i];
+        d[4] = o[5 * cap + i];
+      }
+      for (int c = 0; c < 5; ++c) p.dids[5 * (size_t)i + c] = (double)d[c];
+    }
+  } else if (k < nion + ns) {
+    const int j = k - nion;
+    float f[3] = {0.f, 0.f, 0.f};
+    if (qforces && p.stfree[j])
+      for (int t = 0; t < T; ++t) {
+        const float *o = p.isp_site + (size_t)t * 3 * ns;
+#pragma unroll
+        for (int c = 0; c < 3; ++c) f[c] += o[c * ns + j];
+      }
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p.fis_f[c * cap + j] = f[c];
+  }
+}
+
+int ionsite_tile_blocks(const KP &p, int nub) {
+  const int S = (p.nsites + 31) / 32, T = (std::max(0, nub - p.nsites) + 31) / 32;
+  return (S * T + kIsWarps - 1) / kIsWarps;
+}
+
+// The FP32 ion-site pairs run as tiles when the context holds their partial
+// buffers for this many ions.
+bool ionsite_tiled(const KP &p, bool fp32, int nub) {
+  return fp32 && p.isp_ion && (std::max(0, nub - p.nsites) + 31) / 32 <= p.isp_tcap;
+}
+
 __global__ void __launch_bounds__(kPairThreads) k_siteforce32(KP p) {
   __shared__ float red[(kPairThreads / 32) * 3];
   __shared__ float tot[3];
@@ -669,17 +867,26 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
   if (nonbond && p.nsites > 0 && nub > p.nsites) {
     const int nion_ub = nub - p.nsites;
     const int nb = (nion_ub + kPairThreads - 1) / kPairThreads;
-    if (plan.fp32) {
-      const size_t smem = (size_t)p.nsites * 2 * sizeof(float4);
-      k_ionsite32<<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
-      if (qforces) k_siteforce32<<<p.nsites, kPairThreads, 0, stream>>>(p);
+    if (ionsite_tiled(p, plan.fp32, nub)) {  // FP32: 32 x 32 tiles
+      const int S = (p.nsites + 31) / 32, T = (nion_ub + 31) / 32;
+      const int tb = ionsite_tile_blocks(p, nub);
+      k_ionsite_tiles<<<tb, 32 * kIsWarps, 0, stream>>>(p, qforces, slot, S, S * T);
+      k_ionsite_sum<<<(nion_ub + p.nsites + 255) / 256, 256, 0, stream>>>(p, qforces, S, T);
+      slot += tb;
+      nk += 2;
     } else {
-      const size_t smem = (size_t)p.nsites * (3 * sizeof(double) + sizeof(int));
-      k_ionsite<<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
-      if (qforces) k_siteforce<<<p.nsites, kPairThreads, 0, stream>>>(p);
+      if (plan.fp32) {
+        const size_t smem = (size_t)p.nsites * 2 * sizeof(float4);
+        k_ionsite32<<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
+        if (qforces) k_siteforce32<<<p.nsites, kPairThreads, 0, stream>>>(p);
+      } else {
+        const size_t smem = (size_t)p.nsites * (3 * sizeof(double) + sizeof(int));
+        k_ionsite<<<nb, kPairThreads, smem, stream>>>(p, qforces, slot);
+        if (qforces) k_siteforce<<<p.nsites, kPairThreads, 0, stream>>>(p);
+      }
+      slot += nb;
+      nk += qforces ? 2 : 1;
     }
-    slot += nb;
-    nk += qforces ? 2 : 1;
   }
   if (plan.nuc) {  // DNA bonded and Go-like terms, after the ion-site forces
     const bool is_ran = nonbond && p.nsites > 0 && nub > p.nsites;
@@ -693,7 +900,7 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
                           (size_t)(nub - p.nsites) * sizeof(double), stream);
       }
     nk += launch_nucl(p, plan.fp32, mask, qforces, is_ran ? 1 : 0, slot, stream);
-    ++slot;
+    slot += nucl_slots(p);
   }
   if (!plan.fp32 && (mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0) {
     dim3 g((nub - p.nsites + kPairThreads - 1) / kPairThreads, plan.nchunk_rf);
@@ -727,8 +934,9 @@ int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask) {
     slot += ((nmob_ub + kPairThreads - 1) / kPairThreads) * plan.nchunk_ii;
   }
   if ((mask & 1u) && p.nsites > 0 && nub > p.nsites)
-    slot += (nub - p.nsites + kPairThreads - 1) / kPairThreads;
-  if (plan.nuc) ++slot;
+    slot += ionsite_tiled(p, plan.fp32, nub) ? ionsite_tile_blocks(p, nub)
+                                              : (nub - p.nsites + kPairThreads - 1) / kPairThreads;
+  if (plan.nuc) slot += nucl_slots(p);
   if (!plan.fp32 && (mask & 16u) && p.qrfpar && nub > p.nsites && plan.nchunk_rf > 0)
     slot += ((nub - p.nsites + kPairThreads - 1) / kPairThreads) * plan.nchunk_rf;
   return slot;

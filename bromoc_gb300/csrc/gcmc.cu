@@ -1607,10 +1607,10 @@ __global__ void k_count_zero(KP p) {
   for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) p.st->nat[b] = 0;
 }
 
+// One particle's COUNT: its buffer (0 none); adds to nat[b - 1] and fixes
+// the sign of its type.
 template <bool FF>
-__global__ void __launch_bounds__(256) k_count(KP p) {
-  const int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.st->ntot) return;
+__device__ __forceinline__ int count_one(const KP &p, int i, int *nat) {
   int ib = 0;
   if (i >= p.nsites + p.nfix) {
     const double3 q = pos_of(p, FF, i);
@@ -1635,24 +1635,53 @@ __global__ void __launch_bounds__(256) k_count(KP p) {
       if (out) atomicOr(&p.st->err, kErrOutside);
       if (!in) continue;
       ib = b;
-      atomicAdd(&p.st->nat[b - 1], 1);
+      atomicAdd(&nat[b - 1], 1);
       p.typei[i] = q.z < p.cz ? -itype : itype;
     }
   }
-  p.ibuffer[i] = ib;
+  return ib;
+}
+
+template <bool FF>
+__global__ void __launch_bounds__(256) k_count(KP p) {
+  const int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= p.st->ntot) return;
+  p.ibuffer[i] = count_one<FF>(p, i, p.st->nat);
+}
+
+// The whole COUNT in one block (systems up to kCountOne ions): nat in shared
+// memory, then nat and ntotat in the device record.
+constexpr int kCountOne = 16384;
+template <bool FF>
+__global__ void __launch_bounds__(1024) k_count_block(KP p) {
+  __shared__ int nat[kMaxBuffers];
+  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) nat[b] = 0;
+  __syncthreads();
+  const int ntot = p.st->ntot;
+  for (int i = p.nsites + threadIdx.x; i < ntot; i += blockDim.x)
+    p.ibuffer[i] = count_one<FF>(p, i, nat);
+  __syncthreads();
+  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) {
+    p.st->nat[b] = nat[b];
+    p.st->ntotat[b] += nat[b];
+  }
 }
 
 __global__ void k_count_fin(KP p) {
   for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) p.st->ntotat[b] += p.st->nat[b];
 }
 
-void launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream) {
-  if (p.nbuffer < 1) return;
-  k_count_zero<<<1, 64, 0, stream>>>(p);
+int launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream) {
+  if (p.nbuffer < 1) return 0;
   const int n = ntot_ub - p.nsites;
-  if (n > 0)
-    (ff ? k_count<true> : k_count<false>)<<<(n + 255) / 256, 256, 0, stream>>>(p);
+  if (n <= kCountOne) {
+    (ff ? k_count_block<true> : k_count_block<false>)<<<1, 1024, 0, stream>>>(p);
+    return 1;
+  }
+  k_count_zero<<<1, 64, 0, stream>>>(p);
+  (ff ? k_count<true> : k_count<false>)<<<(n + 255) / 256, 256, 0, stream>>>(p);
   k_count_fin<<<1, 64, 0, stream>>>(p);
+  return 3;
 }
 
 // ---------------------------------------------------------------------------

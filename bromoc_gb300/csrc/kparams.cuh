@@ -233,6 +233,12 @@ struct KP {
   float4 *pk3;                  // [cap] (reff, q, bits(rf flags), 0), flags in fields.cu
   float4 *rfd;                  // [2*cap] srfe and reff gradients (xyz, 0)
   float *ffield_f, *fis_f;      // [3*cap] single-particle / ion-site forces
+  // FP32 ion-site tiles (32 ions x 32 sites a warp): ion partials per site
+  // tile [S][3][cap], site partials per ion tile [T][3][nsites], the PROXDIFF
+  // nearest-site candidates per site tile [S][6][cap] (value, site, dist,
+  // dx, dy, dz) and the first site's record [5][cap]
+  float *isp_ion, *isp_site, *isp_dids, *isp_seed;
+  int isp_tcap;                 // ion tiles the site partials hold
   float *fii_f, *frf_f;         // [nchunk*3*cap] partial forces
   // Newton's-third-law pair kernel: per tile pair q and side (0 = row tile,
   // 1 = column tile), per lane: (fx, fy, fz, A) and B of the RFPAR chain

@@ -67,7 +67,7 @@ void launch_mmij_interact(const KP &p, int ntot_ub, double *dener, cudaStream_t 
 
 // gcmc.cu: COUNT (count.f90) on the device; ff: positions from the
 // float-float records
-void launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream);
+int launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream);  // launches
 
 // analysis.cu: per-cycle profiles (counts) and .btr frames
 struct ProfArgs {
@@ -88,6 +88,7 @@ void launch_traj_pack(const KP &p, bool fp32, int n, double runtime, uint32_t *w
 // sites (added when accum, else written), energies into one slot
 int launch_nucl(const KP &p, bool fp32, uint32_t mask, int qforces, int accum, int slot,
                 cudaStream_t stream);
+int nucl_slots(const KP &p);  // energy slots launch_nucl writes
 // NOTRAN after a BD step: the sites' centre back to notr along the flagged
 // axes (one block); returns the launches (0 when off)
 int launch_notrans(const KP &p, bool fp32, cudaStream_t stream);

@@ -195,46 +195,56 @@ __device__ void nucl_term(const KP &p, uint32_t mask, int t, int kind, double &e
   }
 }
 
+// One thread per term; the block's energies per kind (a fixed tree) into
+// energy slot slot0 + block.
 template <bool F32>
-__global__ void __launch_bounds__(kNucThreads) k_nucl_terms(KP p, uint32_t mask, int qforces) {
+__global__ void __launch_bounds__(kNucThreads)
+    k_nucl_terms(KP p, uint32_t mask, int qforces, int slot0) {
   const NucDev &n = p.nuc;
+  __shared__ double red[(kNucThreads / 32) * 8];
+  __shared__ double tot[8];
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= n.nterm) return;
-  double e, f[4][3];
-  nucl_term<F32>(p, mask, t, nuc_kind(n, t), e, f);
-  n.te[t] = e;
-  if (qforces) {
-    double *o = n.tf + (size_t)t * 12;
+  double v[8] = {0, 0, 0, 0, 0, 0, 0, 0};
+  if (t < n.nterm) {
+    double e, f[4][3];
+    const int kind = nuc_kind(n, t);
+    nucl_term<F32>(p, mask, t, kind, e, f);
 #pragma unroll
-    for (int m = 0; m < 4; ++m)
+    for (int k = 0; k < 8; ++k) v[k] = kind == k ? e : 0.0;
+    if (qforces) {
+      double *o = n.tf + (size_t)t * 12;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) o[3 * m + c] = f[m][c];
+      for (int m = 0; m < 4; ++m)
+#pragma unroll
+        for (int c = 0; c < 3; ++c) o[3 * m + c] = f[m][c];
+    }
+  }
+  block_sum<8>(v, red, tot);
+  if (threadIdx.x == 0) {
+    double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
+    for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
+    for (int k = 0; k < 8; ++k) dst[14 + k] = tot[k];
   }
 }
 
-// Per-kind energies, CONTRANS (energy.mono.f90:516-581): centre sums of the
-// site coordinates (per strand when unsplit), the centre springs' force per
-// strand and axis into n.cf[0..5], econ; one energy slot row.
+// CONTRANS (energy.mono.f90:516-581): centre sums of the site coordinates
+// (per strand when unsplit), the centre springs' force per strand and axis
+// into n.cf[0..5], econ into one energy slot.
 template <bool F32>
 __global__ void __launch_bounds__(kNucReduceThreads) k_nucl_reduce(KP p, int slot) {
   const NucDev &n = p.nuc;
-  __shared__ double red[(kNucReduceThreads / 32) * 14];
-  __shared__ double tot[14];
-  double v[14];
-#pragma unroll
-  for (int k = 0; k < 14; ++k) v[k] = 0.0;
-  for (int k = 0; k < 8; ++k)
-    for (int t = n.off[k] + threadIdx.x; t < n.off[k + 1]; t += blockDim.x) v[k] += n.te[t];
+  __shared__ double red[(kNucReduceThreads / 32) * 6];
+  __shared__ double tot6[6];
+  double v[6] = {0, 0, 0, 0, 0, 0};
   const int ns = p.nsites, n1 = n.qunsplit ? n.nsites1st : ns;
-  if (n.ctn > 0)
-    for (int j = threadIdx.x; j < ns; j += blockDim.x) {
-      double r[3];
-      site_pos<F32>(p, j, r);
-      const int b = j < n1 ? 8 : 11;
+  for (int j = threadIdx.x; j < ns; j += blockDim.x) {
+    double r[3];
+    site_pos<F32>(p, j, r);
+    const int b = j < n1 ? 0 : 3;
 #pragma unroll
-      for (int c = 0; c < 3; ++c) v[b + c] += r[c];
-    }
-  block_sum<14>(v, red, tot);
+    for (int c = 0; c < 3; ++c) v[b + c] += r[c];
+  }
+  block_sum<6>(v, red, tot6);  // first strand (or all sites) xyz, second strand xyz
   if (threadIdx.x != 0) return;
   const double insites = 1.0 / ns;
   const int ctn = n.ctn;
@@ -247,14 +257,14 @@ __global__ void __launch_bounds__(kNucReduceThreads) k_nucl_reduce(KP p, int slo
       const double *c = n.cc + 3 * 0 + a;  // anchors: cc[3*entry + axis]
       if (j == 0) {
         if (n.qunsplit) {
-          double con = tot[8 + a] * insites * 2.0 - c[3 * i];
+          double con = tot6[a] * insites * 2.0 - c[3 * i];
           cf[a] -= kv * con * insites * 2.0;
           econ = econ + 0.5 * kv * (con * con);
-          con = tot[11 + a] * insites * 2.0 - c[3 * ctn];
+          con = tot6[3 + a] * insites * 2.0 - c[3 * ctn];
           cf[3 + a] -= kv * con * insites * 2.0;
           econ = econ + 0.5 * kv * (con * con);
         } else {
-          const double con = tot[8 + a] * insites - c[3 * i];
+          const double con = tot6[a] * insites - c[3 * i];
           cf[a] -= kv * con * insites;
           econ = econ + 0.5 * kv * (con * con);
         }
@@ -269,7 +279,6 @@ __global__ void __launch_bounds__(kNucReduceThreads) k_nucl_reduce(KP p, int slo
   for (int k = 0; k < 6; ++k) n.cf[k] = cf[k];
   double *dst = p.epart + (size_t)slot * kNTerms;
   for (int k = 0; k < kNTerms; ++k) dst[k] = 0.0;
-  for (int k = 0; k < 8; ++k) dst[14 + k] = tot[k];
   dst[22] = econ;
 }
 
@@ -451,20 +460,28 @@ int launch_notrans(const KP &p, bool fp32, cudaStream_t stream) {
   return 1;
 }
 
+// Energy slots of the DNA terms: one per term block, one for CONTRANS.
+int nucl_slots(const KP &p) {
+  const NucDev &n = p.nuc;
+  return (n.nterm + kNucThreads - 1) / kNucThreads + (n.ctn > 0 ? 1 : 0);
+}
+
 int launch_nucl(const KP &p, bool fp32, uint32_t mask, int qforces, int accum, int slot,
                 cudaStream_t stream) {
   const NucDev &n = p.nuc;
   if (n.nterm <= 0 && n.ctn <= 0) return 0;
   int nk = 0;
-  if (n.nterm > 0) {
-    const int nb = (n.nterm + kNucThreads - 1) / kNucThreads;
+  const int nb = (n.nterm + kNucThreads - 1) / kNucThreads;
+  if (nb > 0) {
     (fp32 ? k_nucl_terms<true> : k_nucl_terms<false>)<<<nb, kNucThreads, 0, stream>>>(
-        p, mask, qforces);
+        p, mask, qforces, slot);
     ++nk;
   }
-  (fp32 ? k_nucl_reduce<true> : k_nucl_reduce<false>)<<<1, kNucReduceThreads, 0, stream>>>(
-      p, slot);
-  ++nk;
+  if (n.ctn > 0) {
+    (fp32 ? k_nucl_reduce<true> : k_nucl_reduce<false>)<<<1, kNucReduceThreads, 0, stream>>>(
+        p, slot + nb);
+    ++nk;
+  }
   if (qforces) {
     const int nb = (p.nsites + kNucGatherWarps - 1) / kNucGatherWarps;
     (fp32 ? k_nucl_gather<true> : k_nucl_gather<false>)<<<nb, 32 * kNucGatherWarps, 0,

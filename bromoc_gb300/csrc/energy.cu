@@ -477,6 +477,7 @@ __global__ void __launch_bounds__(32 * kIsWarps)
     int bj = 1 << 30;
     float seed[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     __syncwarp();
+#pragma unroll 4
     for (int k = 0; k < 32; ++k) {
       const int m = (lane + k) & 31;
       float g0 = 0.f, g1 = 0.f, g2 = 0.f;
@@ -565,7 +566,7 @@ __global__ void __launch_bounds__(32 * kIsWarps)
 
 // Ion forces: the site tiles' partials in tile order; PROXDIFF: the first
 // site's record, replaced by the smallest later one (smaller j on ties) only
-// when it is below; site forces: the ion tiles' partials in tile order.
+// when it is below.
 __global__ void __launch_bounds__(256) k_ionsite_sum(KP p, int qforces, int S, int T) {
   const int k = blockIdx.x * blockDim.x + threadIdx.x;
   const int ntot = p.st->ntot, ns = p.nsites;
@@ -606,18 +607,29 @@ __global__ void __launch_bounds__(256) k_ionsite_sum(KP p, int qforces, int S, i
       }
       for (int c = 0; c < 5; ++c) p.dids[5 * (size_t)i + c] = (double)d[c];
     }
-  } else if (k < nion + ns) {
-    const int j = k - nion;
-    float f[3] = {0.f, 0.f, 0.f};
-    if (qforces && p.stfree[j])
-      for (int t = 0; t < T; ++t) {
-        const float *o = p.isp_site + (size_t)t * 3 * ns;
-#pragma unroll
-        for (int c = 0; c < 3; ++c) f[c] += o[c * ns + j];
-      }
-#pragma unroll
-    for (int c = 0; c < 3; ++c) p.fis_f[c * cap + j] = f[c];
   }
+}
+
+// Site forces: one warp per site, lanes over the ion tiles (lane l takes
+// tiles l, l + 32, ...), then a fixed shuffle tree.
+__global__ void __launch_bounds__(256) k_ionsite_sites(KP p, int qforces, int T) {
+  const int j = blockIdx.x * 8 + (threadIdx.x >> 5), lane = threadIdx.x & 31;
+  const int ns = p.nsites;
+  if (j >= ns) return;  // warp-uniform
+  float f[3] = {0.f, 0.f, 0.f};
+  if (qforces && p.stfree[j])
+    for (int t = lane; t < T; t += 32) {
+      const float *o = p.isp_site + (size_t)t * 3 * ns;
+#pragma unroll
+      for (int c = 0; c < 3; ++c) f[c] += o[c * ns + j];
+    }
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) f[c] += __shfl_xor_sync(0xffffffffu, f[c], o);
+  if (lane == 0)
+#pragma unroll
+    for (int c = 0; c < 3; ++c) p.fis_f[c * (size_t)p.cap + j] = f[c];
 }
 
 int ionsite_tile_blocks(const KP &p, int nub) {
@@ -871,9 +883,10 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
       const int S = (p.nsites + 31) / 32, T = (nion_ub + 31) / 32;
       const int tb = ionsite_tile_blocks(p, nub);
       k_ionsite_tiles<<<tb, 32 * kIsWarps, 0, stream>>>(p, qforces, slot, S, S * T);
-      k_ionsite_sum<<<(nion_ub + p.nsites + 255) / 256, 256, 0, stream>>>(p, qforces, S, T);
+      k_ionsite_sum<<<(nion_ub + 255) / 256, 256, 0, stream>>>(p, qforces, S, T);
+      k_ionsite_sites<<<(p.nsites + 7) / 8, 256, 0, stream>>>(p, qforces, T);
       slot += tb;
-      nk += 2;
+      nk += 3;
     } else {
       if (plan.fp32) {
         const size_t smem = (size_t)p.nsites * 2 * sizeof(float4);

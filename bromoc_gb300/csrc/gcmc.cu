@@ -1302,21 +1302,36 @@ __device__ bool apply_move(const KP &p, bool rf_on, int a, GrandState &g) {
   } else {
     if (guard_bad(p.st, tr.j - 1, ntot, 23) || guard_bad(p.st, ntot - 1, p.cap, 24)) return false;
     const int iat = tr.j - 1, last = ntot - 1;
-    const int bz = p.ibuffer[last];  // the ion the freed slot receives
+    // every read of the last ion first, then the writes into the freed slot:
+    // the reads then overlap instead of each waiting behind a write
+    const int bz = __ldcg(p.ibuffer + last);  // the ion the freed slot receives
+    const int tz = __ldcg(p.typei + last);
+    float4 r1 = make_float4(0.f, 0.f, 0.f, 0.f), r2 = r1, r3 = r1, rr = r1;
+    double dx = 0.0, dy = 0.0, dz = 0.0;
+    if (g.ff) {
+      r1 = __ldcg(p.pk1 + last);
+      r2 = __ldcg(p.pk2 + last);
+      r3 = __ldcg(p.pk3 + last);
+    } else {
+      dx = __ldcg(p.x + last);
+      dy = __ldcg(p.y + last);
+      dz = __ldcg(p.z + last);
+    }
+    if (rf_on) rr = __ldcg(p.gc_rff + last);
     g.dener_sum -= f2_dbl(de);
     g.nremove[b] += 1;
     if (g.ff) {
-      p.pk1[iat] = __ldcg(p.pk1 + last);
-      p.pk2[iat] = __ldcg(p.pk2 + last);
-      p.pk3[iat] = __ldcg(p.pk3 + last);
+      p.pk1[iat] = r1;
+      p.pk2[iat] = r2;
+      p.pk3[iat] = r3;
     } else {
-      p.x[iat] = p.x[last];
-      p.y[iat] = p.y[last];
-      p.z[iat] = p.z[last];
+      p.x[iat] = dx;
+      p.y[iat] = dy;
+      p.z[iat] = dz;
     }
-    p.typei[iat] = p.typei[last];
+    p.typei[iat] = tz;
     p.ibuffer[iat] = bz;
-    if (rf_on) p.gc_rff[iat] = __ldcg(p.gc_rff + last);
+    if (rf_on) p.gc_rff[iat] = rr;
     g.nat[b] = nat - 1;
     g.ntot = ntot - 1;
     g.chg[g.nchg++] = iat;
@@ -1431,6 +1446,8 @@ __global__ void __launch_bounds__(kGrandThreads)
       g.ff = ffpos;
       g.nbuf = nb;
       g.nchg = 0;
+      g.nacc = 0;  // evaluate's view before the first settle
+      g.touched = 0;
     }
     __syncthreads();
     int a0 = 0;

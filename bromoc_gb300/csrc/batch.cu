@@ -68,7 +68,7 @@ __global__ void __launch_bounds__(32 * W)
   const int2 wk = work[widx];
   const RepDev &R = rep[wk.x];
   const PairSys ps{p.pk1 + R.off, p.pk2 + R.off, p.pk3 + R.off, tpf + (size_t)R.poff * 64,
-                   tpb + (size_t)R.poff * 64, 0, 0, R.n, (R.n + 31) >> 5};
+                   tpb + (size_t)R.poff * 64, 0, 0, R.n, (R.n + 31) >> 5, R.rows};
   float e[kRowTerms] = {0.f, 0.f, 0.f, 0.f, 0.f};
   n3_tile<true, RF, false>(p, ps, wk.y, 1, nw[w], tab, e);
   e[1] *= 1.0f / 6.0f;  // the tile sums 6 x elj
@@ -237,9 +237,9 @@ void drop_graph(bromoc_batch *b) {
   b->g_nsteps = b->g_rf = -1;
 }
 
-// work items: every tile pair (replica, q) and every tile (replica, t) of the
-// live particles, bucket by bucket and replica by replica within a bucket;
-// w0, w1 bound each replica's tile pairs
+// work items: every pair-tile item (replica, n3_item index) and every tile
+// (replica, t) of the live particles, bucket by bucket and replica by
+// replica within a bucket; w0, w1 bound each replica's pair-tile items
 int rebuild_work(bromoc_batch *b, bool retune = true) {
   std::vector<int2> items, tiles;
   for (int k = 0; k < kBuckets; ++k) {
@@ -249,7 +249,8 @@ int rebuild_work(bromoc_batch *b, bool retune = true) {
       if (size_bucket(b->n[r]) != k) continue;
       const int T = (b->n[r] + 31) / 32;
       b->rep_h[r].w0 = (int)items.size();
-      for (int q = 0; q < n3_pairs(T); ++q) items.push_back(make_int2(r, q));
+      b->rep_h[r].rows = n3_rows(T);
+      for (int q = 0; q < n3_work(T, b->rep_h[r].rows); ++q) items.push_back(make_int2(r, q));
       b->rep_h[r].w1 = (int)items.size();
       for (int t = 0; t < T; ++t) tiles.push_back(make_int2(r, t));
     }

@@ -10,7 +10,8 @@ namespace bgpu {
 // of the batch arrays (off a multiple of 32), the first n of them live.
 struct RepDev {
   int off, n, cap;
-  int w0, w1;      // its tile-pair work items [w0, w1) in the work list
+  int w0, w1;      // its pair-tile work items [w0, w1) in the work list
+  int rows;        // row tiles per item (n3_rows of its tiles, as a single context)
   int poff;        // its first tile pair in the partial buffers (capacity-sized)
   uint64_t seed;   // BD noise key of this replica
   BoxF box;        // fixcoor constants

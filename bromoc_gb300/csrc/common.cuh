@@ -84,6 +84,9 @@ struct DevState {
   unsigned bar_gen;         // a generation flag and the blocks that have
   unsigned bar_exit;        // finished; all zero between launches (the last
                             // block out of a launch clears them)
+  int count_acc[kMaxBuffers];  // COUNT: the blocks' nat sums and the blocks
+  unsigned count_done;         // done; zero between launches (the last block
+                               // publishes nat and clears them)
 };
 
 // GCMC trial of one attempt (written by the proposal kernel).

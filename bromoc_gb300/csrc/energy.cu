@@ -236,7 +236,7 @@ constexpr int kN3Warps = 4;
 
 template <bool II, bool RF, bool EFP, bool PBC = false>
 __global__ void __launch_bounds__(32 * kN3Warps)
-    k_pairs32n(KP p, int qforces, int slot0) {
+    k_pairs32n(KP p, int qforces, int slot0, int rows) {
   __shared__ N3Warp<RF> nw[kN3Warps];
   __shared__ float4 tab[EFP ? 1 : kIpqMax];
   __shared__ float red[kN3Warps * 5];
@@ -247,10 +247,10 @@ __global__ void __launch_bounds__(32 * kN3Warps)
   __syncthreads();
   const int w = threadIdx.x >> 5;
   const int T = p.ntile;
-  const int q = blockIdx.x * kN3Warps + w;
+  const int it = blockIdx.x * kN3Warps + w;
   float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};  // ecoul, elj, esrpmf, eefpot, erfpar
-  if (q < n3_pairs(T))  // warp-uniform
-    n3_tile<II, RF, EFP, PBC>(p, pair_sys(p, p.st->ntot, T), q, qforces, nw[w], tab, e);
+  if (it < n3_work(T, rows))  // warp-uniform
+    n3_tile<II, RF, EFP, PBC>(p, pair_sys(p, p.st->ntot, T, rows), it, qforces, nw[w], tab, e);
   block_sum_f<5>(e, red, tot);
   if (threadIdx.x == 0) {
     double *dst = p.epart + (size_t)(slot0 + blockIdx.x) * kNTerms;
@@ -263,7 +263,19 @@ __global__ void __launch_bounds__(32 * kN3Warps)
   }
 }
 
-int n3_blocks(int ntile) { return (n3_pairs(ntile) + kN3Warps - 1) / kN3Warps; }
+int n3_rows(int T) {
+  static int nsm[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!nsm[dev] &&
+      cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev) != cudaSuccess)
+    nsm[dev] = 1;
+  return n3_pairs(T) > 16 * nsm[dev] ? 2 : 1;
+}
+
+int n3_blocks(int ntile) {
+  return (n3_work(ntile, n3_rows(ntile)) + kN3Warps - 1) / kN3Warps;
+}
 
 // ---------------------------------------------------------------------------
 // Ion-site pairs, ion-centred (energy.mono.f90:585-687): each ion walks the
@@ -835,20 +847,20 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->b, stream);
     slot += cell_pair_blocks(p, nub);
   } else if (plan.fp32 && plan.ntile > 0 && (pc.ii || pc.rf)) {
-    const int nb = n3_blocks(plan.ntile);
+    const int nb = n3_blocks(plan.ntile), rows = n3_rows(plan.ntile);
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->a, stream);
     const bool efp = !p.ipq_ok;
     if (p.periodic)  // extension mode: ion-ion only (no RFPAR)
       (efp ? k_pairs32n<true, false, true, true> : k_pairs32n<true, false, false, true>)
-          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot);
+          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot, rows);
     else if (pc.ii && pc.rf)
       (efp ? k_pairs32n<true, true, true> : k_pairs32n<true, true, false>)
-          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot);
+          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot, rows);
     else if (pc.ii)
       (efp ? k_pairs32n<true, false, true> : k_pairs32n<true, false, false>)
-          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot);
+          <<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot, rows);
     else
-      k_pairs32n<false, true, true><<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot);
+      k_pairs32n<false, true, true><<<nb, 32 * kN3Warps, 0, stream>>>(p, qforces, slot, rows);
     if (plan.t_pairs) cudaEventRecord(plan.t_pairs->b, stream);
     slot += nb;
     ++nk;

@@ -1620,10 +1620,6 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
 // buffer ion outside the system (the reference's fatal error) raises
 // kErrOutside.
 // ---------------------------------------------------------------------------
-__global__ void k_count_zero(KP p) {
-  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) p.st->nat[b] = 0;
-}
-
 // One particle's COUNT: its buffer (0 none); adds to nat[b - 1] and fixes
 // the sign of its type.
 template <bool FF>
@@ -1659,46 +1655,52 @@ __device__ __forceinline__ int count_one(const KP &p, int i, int *nat) {
   return ib;
 }
 
+// The whole COUNT in one launch over many blocks: the range tests are FP64
+// (a few FP64 operations a clock per SM), so the particles are spread over
+// the SMs.  Each block sums its nat in shared memory and adds it to
+// DevState::count_acc; the last block to finish (a ticket after a fence)
+// publishes nat, adds it to ntotat and clears the scratch for the next
+// launch.  Integer sums: exact in any order.
+constexpr int kCountThreads = 128;
 template <bool FF>
-__global__ void __launch_bounds__(256) k_count(KP p) {
-  const int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= p.st->ntot) return;
-  p.ibuffer[i] = count_one<FF>(p, i, p.st->nat);
-}
-
-// The whole COUNT in one block (systems up to kCountOne ions): nat in shared
-// memory, then nat and ntotat in the device record.
-constexpr int kCountOne = 16384;
-template <bool FF>
-__global__ void __launch_bounds__(1024) k_count_block(KP p) {
+__global__ void __launch_bounds__(kCountThreads) k_count_grid(KP p) {
   __shared__ int nat[kMaxBuffers];
+  __shared__ bool last;
   for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) nat[b] = 0;
   __syncthreads();
   const int ntot = p.st->ntot;
-  for (int i = p.nsites + threadIdx.x; i < ntot; i += blockDim.x)
+  for (int i = p.nsites + blockIdx.x * blockDim.x + threadIdx.x; i < ntot;
+       i += gridDim.x * blockDim.x)
     p.ibuffer[i] = count_one<FF>(p, i, nat);
   __syncthreads();
+  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x)
+    if (nat[b]) atomicAdd(&p.st->count_acc[b], nat[b]);
+  __threadfence();
+  __syncthreads();
+  if (threadIdx.x == 0) last = atomicAdd(&p.st->count_done, 1u) == gridDim.x - 1;
+  __syncthreads();
+  if (!last) return;
+  __threadfence();
   for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) {
-    p.st->nat[b] = nat[b];
-    p.st->ntotat[b] += nat[b];
+    const int v = atomicExch(&p.st->count_acc[b], 0);
+    p.st->nat[b] = v;
+    p.st->ntotat[b] += v;
   }
-}
-
-__global__ void k_count_fin(KP p) {
-  for (int b = threadIdx.x; b < p.nbuffer; b += blockDim.x) p.st->ntotat[b] += p.st->nat[b];
+  if (threadIdx.x == 0) p.st->count_done = 0u;
 }
 
 int launch_count(const KP &p, bool ff, int ntot_ub, cudaStream_t stream) {
   if (p.nbuffer < 1) return 0;
-  const int n = ntot_ub - p.nsites;
-  if (n <= kCountOne) {
-    (ff ? k_count_block<true> : k_count_block<false>)<<<1, 1024, 0, stream>>>(p);
-    return 1;
-  }
-  k_count_zero<<<1, 64, 0, stream>>>(p);
-  (ff ? k_count<true> : k_count<false>)<<<(n + 255) / 256, 256, 0, stream>>>(p);
-  k_count_fin<<<1, 64, 0, stream>>>(p);
-  return 3;
+  static int nsm[64] = {};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  if (!nsm[dev] && cudaDeviceGetAttribute(&nsm[dev], cudaDevAttrMultiProcessorCount, dev) !=
+                       cudaSuccess)
+    nsm[dev] = 1;
+  const int n = std::max(1, ntot_ub - p.nsites);
+  const int grid = std::max(1, std::min(nsm[dev], (n + kCountThreads - 1) / kCountThreads));
+  (ff ? k_count_grid<true> : k_count_grid<false>)<<<grid, kCountThreads, 0, stream>>>(p);
+  return 1;
 }
 
 // ---------------------------------------------------------------------------

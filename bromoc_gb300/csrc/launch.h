@@ -29,6 +29,39 @@ __host__ __device__ inline int n3_pairs(int T) { return T * (T + 1) / 2; }
 __host__ __device__ inline int n3_index(int T, int I, int J) {
   return I * T - I * (I - 1) / 2 + (J - I);
 }
+// Work items of the Newton-3 pair kernels, column tile by column tile:
+// column J's off-diagonal row tiles 0..J-1 go in pairs (2s, 2s+1), one item
+// of 64 row ions against the column's 32 entries; when J is odd, row tile
+// J-1 is an item of its own; the diagonal tile pair (J, J) comes last.
+// Items before column J: J + floor(J^2 / 4).
+__host__ __device__ inline int n3_items_before(int J) { return J + J * J / 4; }
+__host__ __device__ inline int n3_items(int T) { return n3_items_before(T); }
+// Tile pair q of the row-major list: (I, J).
+__host__ __device__ inline void n3_pair(int T, int q, int &I, int &J) {
+  const float b = 2.0f * T + 1.0f;
+  int i = (int)((b - sqrtf(b * b - 8.0f * q)) * 0.5f);
+  i = i < 0 ? 0 : (i > T - 1 ? T - 1 : i);
+  while (i > 0 && n3_index(T, i, i) > q) --i;
+  while (i + 1 < T && n3_index(T, i + 1, i + 1) <= q) ++i;
+  I = i;
+  J = i + (q - n3_index(T, i, i));
+}
+// Item it of T tiles: column J and row tiles I, I2 (I2 < 0: one row tile).
+__host__ __device__ inline void n3_item(int T, int it, int &I, int &I2, int &J) {
+  int j = (int)(2.0f * (sqrtf((float)it + 1.0f) - 1.0f));
+  j = j < 0 ? 0 : (j > T - 1 ? T - 1 : j);
+  while (j > 0 && n3_items_before(j) > it) --j;
+  while (j + 1 < T && n3_items_before(j + 1) <= it) ++j;
+  const int s = it - n3_items_before(j), nd = j >> 1;
+  J = j;
+  I2 = -1;
+  if (s < nd) {
+    I = 2 * s;
+    I2 = 2 * s + 1;
+  } else {
+    I = (j & 1) && s == nd ? j - 1 : j;
+  }
+}
 
 // Targets of the FP32 pair kernel: ion-ion terms act on mobile ions, the
 // RFPAR cross term on every ion in the map, so with RFPAR on the targets
@@ -111,6 +144,12 @@ int energy_slots(const KP &p, const EnergyPlan &plan, uint32_t mask);
 // (block partial energies from `slot`); returns the kernels launched
 int launch_cells(const KP &p, int ntot_ub, int qforces, int slot, cudaStream_t stream);
 int cell_pair_blocks(const KP &p, int ntot_ub);
+// Row tiles per work item of the Newton-3 pair kernels for T tiles: two
+// (n3_item) when the tile pairs outnumber one wave of warps (16 a SM), so a
+// column read serves more pairs; else one (each tile pair an item, the
+// row-major list), for the shorter chain per warp.
+int n3_rows(int T);
+__host__ __device__ inline int n3_work(int T, int rows) { return rows == 2 ? n3_items(T) : n3_pairs(T); }
 int n3_blocks(int ntile);  // blocks (energy slots) of the Newton-3 pair kernel
 
 // dyn.cu: force assembly, optionally fused with the BD update

@@ -38,7 +38,7 @@ union LoopSmem {
 template <bool II, bool RF, bool EFP, bool PBC>
 __global__ void __launch_bounds__(32 * kLoopWarps, 1)
     k_bd_loop(const __grid_constant__ KP p, AssembleFlags fl, uint32_t mask, int variant,
-              uint64_t seed, uint64_t step0, int nsteps, int fields_first) {
+              uint64_t seed, uint64_t step0, int nsteps, int fields_first, int rows) {
   extern __shared__ __align__(16) unsigned char loop_dsm[];  // sizeof(LoopSmem<RF>)
   LoopSmem<RF> &sm = *reinterpret_cast<LoopSmem<RF> *>(loop_dsm);
   __shared__ float4 tab[EFP ? 1 : kIpqMax];
@@ -55,8 +55,8 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   // work slot of this warp: consecutive work items go to consecutive blocks
   const int slot = w * G + blockIdx.x, nslot = G * kLoopWarps;
   const int ntot = p.st->ntot;  // constant during BD
-  const int T = fl.ntile, npair = n3_pairs(T);
-  const PairSys ps = pair_sys(p, ntot, T);
+  const int T = fl.ntile, nwork = n3_work(T, rows);
+  const PairSys ps = pair_sys(p, ntot, T, rows);
   const AsmSys as = ctx_asm_sys(p, T, seed);
   const int m0 = p.nsites + p.nfix;
   unsigned bar = 0;
@@ -72,8 +72,8 @@ __global__ void __launch_bounds__(32 * kLoopWarps, 1)
   }
   for (int s = 0; s < nsteps; ++s) {
     float e[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-    for (int q = slot; q < npair; q += nslot)
-      n3_tile<II, RF, EFP, PBC>(p, ps, q, 1, sm.nw[w], tab, e);
+    for (int it = slot; it < nwork; it += nslot)
+      n3_tile<II, RF, EFP, PBC>(p, ps, it, 1, sm.nw[w], tab, e);
     if (!grid_barrier(&p.st->bar_count, ++bar, p.st, &flag)) goto done;
     for (int it = blockIdx.x; it < nitem; it += G) {
       const int t = halves ? it >> 1 : it, h = halves ? it & 1 : -1;
@@ -123,8 +123,10 @@ static cudaError_t launch_loop_t(const KP &p, const AssembleFlags &fl, uint32_t 
   const int grid = std::max(1, std::min(max_res[dev], std::max(n3_pairs(T), T)));
   KP pc = p;  // the barrier counters are zero between launches (launch_exit)
   AssembleFlags fc = fl;
-  void *args[] = {(void *)&pc, (void *)&fc, (void *)&mask, (void *)&variant,
-                  (void *)&seed, (void *)&step0, (void *)&nsteps, (void *)&fields_first};
+  int rows = n3_rows(T);  // as the per-kernel steps' pair launch
+  void *args[] = {(void *)&pc,    (void *)&fc,     (void *)&mask,         (void *)&variant,
+                  (void *)&seed,  (void *)&step0,  (void *)&nsteps,       (void *)&fields_first,
+                  (void *)&rows};
   return cudaLaunchCooperativeKernel((const void *)kern, dim3(grid), dim3(32 * kLoopWarps), args,
                                      dsm, stream);
 }

@@ -225,7 +225,7 @@ __device__ __forceinline__ void n3_fast(const KP &p, N3Warp<RF> &w, const float4
                                         const N3Row (&r)[NR], N3Sum (&S)[NR], float e[5]) {
   constexpr unsigned kAll = 0xffffffffu;
   constexpr int kStep = 64 * NR;  // SRPMF entries one step can queue
-  constexpr int kUnroll = NR == 1 ? 2 : 1;
+  constexpr int kUnroll = 2;
   const int lane = threadIdx.x & 31;
   float2 THX[NR], THY[NR], THZ[NR], TLX[NR], TLY[NR], TLZ[NR], SRT[NR], RFT[NR], CT[NR];
   const float4 *tr[NR];

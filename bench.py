@@ -419,7 +419,8 @@ def adjoint_measure(sh):
     nbins, r0, dr, sig = 150, 0.05, 0.1, 0.1
     rb = r0 + dr * np.arange(nbins)
     loss = RdfLoss(2, [ADJ_N // 2] * 2, L ** 3, ADJ_STEPS, rb, np.ones((3, nbins)))
-    fd = adjoint_fd_check(sh, spec, loss, (nbins, r0, dr, sig))
+    fd = adjoint_fd_check(sh, spec, (nbins, r0, dr, sig))
+    fd += adjoint_fd_check(sh, spec, (nbins, r0, dr, sig), steps=200)
     stream = torch.cuda.current_stream()
     ev = [torch.cuda.Event(enable_timing=True) for _ in range(3)]
     torch.cuda.synchronize()
@@ -445,15 +446,23 @@ def adjoint_measure(sh):
             "fd_check": fd}
 
 
-def adjoint_fd_check(sh, spec, loss, hist_args, h=1e-4):
+def adjoint_fd_check(sh, spec, hist_args, steps=None, hs=(3e-5, 1e-4, 3e-4)):
     """The C5 segment's knot gradients against central differences of the
     same frozen-noise loss, untimed: for the K-K and K-Cl knot the loss
     feels most, the FP64 adjoint, the FP32 adjoint, and the difference
-    quotient with h = 1e-4 kcal/mol of FP64 forward runs."""
+    quotients of FP64 forward runs at each step h (kcal/mol).  Clamp and
+    wall events and the tables' piece boundaries make the loss piecewise
+    smooth; over long segments they put a scatter of a few 1e-4 into the
+    difference quotients themselves (fd_spread: their range over hs,
+    relative), so the same check also runs on the first 200 steps."""
     import copy
     from bromoc_gb300 import _lib
-    from bromoc_gb300.adjoint import Adjoint, knot_gradient, knot_jacobians
+    from bromoc_gb300.adjoint import Adjoint, RdfLoss, knot_gradient, knot_jacobians
     nbins, r0, dr, sig = hist_args
+    steps = steps or ADJ_STEPS
+    L = float(spec.lx)
+    loss = RdfLoss(2, [ADJ_N // 2] * 2, L ** 3, steps, r0 + dr * np.arange(nbins),
+                   np.ones((3, nbins)))
     grads, runs = {}, {}
     for prec in (abi.FP64, abi.FP32):
         s = copy.copy(spec)
@@ -466,7 +475,7 @@ def adjoint_fd_check(sh, spec, loss, hist_args, h=1e-4):
         def run(s=s, proto=proto, adj=adj):
             s.push(proto)
             adj.set_particles(s.x, s.y, s.z, s.typei)
-            return adj.forward(ADJ_STEPS, ADJ_CKPT, SEED, 0, nbins, r0, dr, sig, 3)
+            return adj.forward(steps, ADJ_CKPT, SEED, 0, nbins, r0, dr, sig, 3)
 
         _, dl = loss.loss_grad(run())
         pt = s.pair_tables()
@@ -480,19 +489,26 @@ def adjoint_fd_check(sh, spec, loss, hist_args, h=1e-4):
         m = int(np.argmax(np.abs(g64)))
         r, u0 = s64.efpot_knots[key]
         u0 = np.asarray(u0, float)
-        vals = []
-        for sgn in (1, -1):
-            u = u0.copy()
-            u[m] += sgn * h
-            s64.efpot_knots[key] = (r, u)
-            vals.append(loss.loss_grad(run64())[0])
+        fds = []
+        for h in hs:
+            vals = []
+            for sgn in (1, -1):
+                u = u0.copy()
+                u[m] += sgn * h
+                s64.efpot_knots[key] = (r, u)
+                vals.append(loss.loss_grad(run64())[0])
+            fds.append((vals[0] - vals[1]) / (2 * h))
         s64.efpot_knots[key] = (r, u0)
-        fdv = (vals[0] - vals[1]) / (2 * h)
         g32 = float(grads[abi.FP32][key][m])
-        out.append({"pair": "-".join(key), "knot_r": float(r[m]), "adjoint_fp64": float(g64[m]),
-                    "adjoint_fp32": g32, "central_difference": fdv, "h": h,
-                    "rel_err_fp64_vs_fd": abs(float(g64[m]) - fdv) / abs(fdv),
-                    "rel_err_fp32_vs_fd": abs(g32 - fdv) / abs(fdv)})
+        fd = fds[list(hs).index(1e-4)]
+        out.append({"pair": "-".join(key), "knot_r": float(r[m]), "steps": steps,
+                    "adjoint_fp64": float(g64[m]), "adjoint_fp32": g32,
+                    "central_difference": fd, "h": 1e-4,
+                    "central_difference_by_h": {f"{h:g}": v for h, v in zip(hs, fds)},
+                    "fd_spread": (max(fds) - min(fds)) / abs(np.mean(fds)),
+                    "rel_err_fp64_vs_fd": abs(float(g64[m]) - fd) / abs(fd),
+                    "rel_err_fp32_vs_fd": abs(g32 - fd) / abs(fd),
+                    "rel_err_fp32_vs_fp64": abs(g32 - float(g64[m])) / abs(float(g64[m]))})
     for _, _, adj, _ in runs.values():
         adj.close()
     return out

@@ -8,10 +8,14 @@ command lines):
                                            k_pairs32n, k_assemble_tiles
   python -m bromoc_gb300.cases loop        the nanopore workload (2000 ions,
                                            4 GCMC buffers): 4 cycles of
-                                           GRAND(4) + a 10-step k_bd_loop
+                                           GRAND(4) + a 10-step k_bd_loop +
+                                           COUNT
   python -m bromoc_gb300.cases cells N     FP32 BD steps of N ions of 1 M KCl
                                            in a periodic cube, 20 A cutoff
                                            (the cell-list kernels), 3 steps
+  python -m bromoc_gb300.cases adjoint N   the adjoint engine on N ions of 1 M
+                                           KCl with tabulated laws: a 20-step
+                                           forward (RDF deposit) and backward
   python -m bromoc_gb300.cases ssdna       FP32 BD steps of 40 nt x 3 free sites
                                            with their bonded terms and ~5000
                                            ions in the 120x120x180 pore maps,
@@ -43,6 +47,7 @@ def loop():
     for c in range(4):
         g.grand(4, 1234, c + 1, dener=False)
         g.bd_steps(10, seed=1234, step0=10 * c, energies=False)
+        g.count()
     g.live_ntot()
 
 
@@ -71,9 +76,37 @@ def ssdna():
     g.live_ntot()
 
 
+def adjoint(n: int):
+    from .adjoint import Adjoint, RdfLoss
+    rng = np.random.default_rng(7)
+    L = (n / (2 * 6.02214e-4)) ** (1.0 / 3.0)
+    spec = synth.bulk_kcl(seed=7, n_per=2, L=L, precision=abi.FP32)
+    p = synth.jittered_lattice(rng, n, -0.5 * L + 0.5, 0.5 * L - 0.5)
+    spec.x, spec.y, spec.z = p[:, 0].copy(), p[:, 1].copy(), p[:, 2].copy()
+    spec.typei = np.array([1, 2] * (n // 2), np.int32)
+    spec.efpot_res = 0.05
+    for key, (sg, ep) in ((("K", "K"), (3.1, 0.09)), (("K", "Cl"), (3.6, 0.11)),
+                          (("Cl", "Cl"), (4.0, 0.15))):
+        spec.efpot_knots[key] = synth.efpot_knots(rng, sg, ep, r0=1.05, r1=16.0, res=0.05)
+    proto = _lib.create(n + 64, abi.FP32)
+    spec.push(proto)
+    adj = Adjoint(proto, n, abi.FP32)
+    adj.set_particles(spec.x, spec.y, spec.z, spec.typei)
+    nbins, r0, dr, sig, steps = 150, 0.05, 0.1, 0.1, 20
+    rb = r0 + dr * np.arange(nbins)
+    loss = RdfLoss(2, [n // 2] * 2, L ** 3, steps, rb, np.ones((3, nbins)))
+    hist = adj.forward(steps, 10, 11, 0, nbins, r0, dr, sig, 3)
+    _, dl = loss.loss_grad(hist)
+    pt = spec.pair_tables()
+    adj.backward(dl, int(pt["cnt"]), int(pt["ntc"]))
+    adj.close()
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "loop"
-    if what == "pairs":
+    if what == "adjoint":
+        adjoint(int(argv[2]) if len(argv) > 2 else 4096)
+    elif what == "pairs":
         pairs(int(argv[2]) if len(argv) > 2 else 8000)
     elif what == "cells":
         cells(int(argv[2]) if len(argv) > 2 else 20000)

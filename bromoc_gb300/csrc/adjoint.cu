@@ -39,8 +39,9 @@
 
 namespace bgpu {
 
-constexpr int kAdjThreads = 64;     // targets per block == source tile
-constexpr int kAdjMaxIonTypes = 4;  // per-thread tail accumulators
+constexpr int kAdjTileWarps = 4;    // tile pairs (warps) per block of the pair sweep
+constexpr int kAdjMaxIonTypes = 4;  // per-lane tail accumulators
+constexpr int kAdjTypePairs = kAdjMaxIonTypes * kAdjMaxIonTypes;
 constexpr double kHistScale = 68719476736.0;  // 2^36 fixed point
 
 enum AdjMode { kModeForce = 0, kModeBack = 1, kModeHist = 2 };
@@ -48,12 +49,15 @@ enum AdjMode { kModeForce = 0, kModeBack = 1, kModeHist = 2 };
 struct AdjArgs {
   const float4 *h, *l;       // positions (hi + type code, lo) of the configuration
   const void *v;             // backward: c bdmask mu, R[3][n]
-  void *out;                 // R[nchunk][3][n]: partial forces / J v + dL/dx
+  void *out;                 // R[tile pair][side][3][32]: partial forces / J v + dL/dx
+  void *tail;                // backward: R[kAdjTypePairs][tile pair] tail sums
   double *g_ep, *g_sc;       // backward: dL/d(p1,p2,p3) [3 cnt], dL/d(sc) [3 ntc]
   unsigned long long *hist;  // [ntypes2][nbins] fixed-point smoothed histogram
   const double *sbin;        // backward: dL/dH [ntypes2][nbins]
-  int n, nchunk, chunk, nbins;
+  int n, nbins;
+  int deposit;               // force: also the histogram deposit of the configuration
   float r0, dr, sigma;       // bin centres r0 + b dr, kernel width
+  double ia;                 // 1 / (sqrt(2 pi) sigma), sigma as the float above
   float rcut2;               // observable range (last centre + 5 sigma)^2, 0: none
   int theta;                 // backward: accumulate dL/dtheta
 };
@@ -64,25 +68,46 @@ __device__ __forceinline__ int tpair(int a, int b, int nt) {
   return lo * nt - lo * (lo - 1) / 2 + (hi - lo);
 }
 
+// r, 1/r and 1/r^2 from r^2 as the adjoint's laws take them: FP64 through
+// the square root, FP32 through the reciprocal square root.
+template <typename R>
+__device__ __forceinline__ void efp_r(R x2, R &r, R &ir, R &ir2) {
+  if constexpr (sizeof(R) == 8) {
+    r = sqrt(x2);
+    ir = 1.0 / r;
+  } else {
+    ir = rsqrtf(x2);
+    r = x2 * ir;
+  }
+  ir2 = ir * ir;
+}
+
+// The analytic tail of a tabulated law (r^2 above the table): g, g' from
+// sc2 / r^6 and, with a charge term, fct / r (fct zero without one).
+template <typename R>
+__device__ __forceinline__ void efp_tail(R sc2, R fct, R ir, R ir2, R &g, R &gp) {
+  const R i8 = ir2 * ir2 * ir2 * ir2;
+  const R f = fct * ir2 * ir;
+  g = (R)6 * sc2 * i8 + f;
+  gp = ((R)-48 * sc2 * i8 - (R)3 * f) * ir;
+}
+
 // g = -(dU/dr)/r, gp = dg/dr of the tabulated law of pair type is at r^2;
 // region 0 table piece `piece`, 1 core, 2 tail.
 template <typename R>
 __device__ __forceinline__ void efp_adj(const KP &p, int is, R x2, R &g, R &gp, R &r,
                                         int &region, int &piece) {
+  R ir, ir2;
+  efp_r<R>(x2, r, ir, ir2);
   if constexpr (sizeof(R) == 8) {
     const PairParam &q = p.pp[is];
-    r = sqrt(x2);
-    const R ir = 1.0 / r, ir2 = ir * ir;
     if (x2 < q.dm2lo) {
       const R i6 = ir2 * ir2 * ir2;
       g = 12.0 * q.sc0 * i6 * i6 * ir2;
       gp = -14.0 * g * ir;
       region = 1;
     } else if (x2 > q.dm2hi) {
-      const R i8 = ir2 * ir2 * ir2 * ir2;
-      const R f = (q.flags & kChr) ? q.fct * ir2 * ir : 0.0;
-      g = 6.0 * q.sc2 * i8 + f;
-      gp = (-48.0 * q.sc2 * i8 - 3.0 * f) * ir;
+      efp_tail<R>(q.sc2, (q.flags & kChr) ? q.fct : 0.0, ir, ir2, g, gp);
       region = 2;
     } else {
       int i = (int)((r - q.dmi) * p.ires) + q.nxi;
@@ -95,18 +120,13 @@ __device__ __forceinline__ void efp_adj(const KP &p, int is, R x2, R &g, R &gp, 
     }
   } else {
     const PairParamF &q = p.ppf[is];
-    const R ir = rsqrtf(x2), ir2 = ir * ir;
-    r = x2 * ir;
     if (x2 < q.dm2lo) {
       const R i6 = ir2 * ir2 * ir2;
       g = 12.0f * q.sc0 * i6 * i6 * ir2;
       gp = -14.0f * g * ir;
       region = 1;
     } else if (x2 > q.dm2hi) {
-      const R i8 = ir2 * ir2 * ir2 * ir2;
-      const R f = (q.flags & kChr) ? q.fct * ir2 * ir : 0.0f;
-      g = 6.0f * q.sc2 * i8 + f;
-      gp = (-48.0f * q.sc2 * i8 - 3.0f * f) * ir;
+      efp_tail<R>(q.sc2, (q.flags & kChr) ? q.fct : 0.0f, ir, ir2, g, gp);
       region = 2;
     } else {
       const int nxi = q.nxi, last = nxi + (q.flags >> 8) - 1;
@@ -130,22 +150,120 @@ __device__ __forceinline__ R to_r(float hi, float lo) {
     return hi;
 }
 
-// Pair kernel of the adjoint engine.  Block (tx, cy): 64 targets x source
-// chunk cy, sources staged in shared memory.  Per mode:
-//   force: out = sum_j g d_ij                    (forces of the forward step)
-//   back:  out = sum_j [g dv + (g'/r) (d.dv) d] + dL/dr d/r   (J v + dL/dx)
-//          and dL/dtheta (i < j only), FP64 atomics per piece, per-thread
-//          tail sums per source type
-//   hist:  cloud-in-cell deposit of r_ij (i < j, r < rcut) into hist
+// Pair sweep of the adjoint engine on Newton-3 tile pairs: each unordered
+// pair once.  One warp per tile pair (I, J), I <= J (row-major, n3_pair);
+// lane l holds row ion I*32 + l, the column tile's records, v (backward) and
+// sums sit in the warp's shared memory and are visited in the rotating order
+// m = (l + k) mod 32, so the lanes of one step touch distinct entries
+// (k = 0..31 off the diagonal; on it k = 1..16, the last step by lanes
+// 0..15).  Every per-pair term is odd in the separation d (and in dv): the
+// row ion gets it, the column entry its negative.  Per mode:
+//   force: g d; with deposit, also the smoothed-histogram deposit
+//   back:  g dv + (g'/r) (d.dv) d + dL/dr d/r   (J v + dL/dx), and with
+//          theta dL/dtheta: table pieces and core constants by FP64 atomics,
+//          tail constants per (row type, column type) summed over the warp
+//          into tail[type pair][tile pair] (reduced in fixed order by
+//          k_adj_tails)
+//   hist:  the deposit alone
+// Most pairs of a segment lie beyond the table, on the analytic tail, and
+// outside the histogram's range: the loop evaluates those itself and queues
+// the rest (table and core pairs, pairs the histogram sees) per warp; the
+// queue is evaluated 32 pairs at a time, one a lane, and the terms added in
+// queue order (deterministic).
+// Output: out[tile pair][side][3][32] (side 0 the row ions, 1 the column
+// entries), gathered per particle in fixed order (adj_gather).
+constexpr int kAdjQ = 64;  // queue: room for two steps
+template <typename R>
+struct AdjWarp {
+  float4 h[32], l[32];
+  R v[3][32];
+  R s[3][32];
+  int q[kAdjQ];  // row lane | column entry << 5
+};
+// the analytic tail of one (row type, column type) law: x2 > dm2hi
+template <typename R>
+struct AdjTail {
+  R dm2hi, sc2, fct;
+};
+
+template <typename R>
+__device__ __forceinline__ void adj_deposit(const KP &p, const AdjArgs &a, int ta, int scode,
+                                            R r) {
+  const int tp = tpair(ta, scode - p.ndna, p.nion_t);
+  unsigned long long *hb = a.hist + (size_t)tp * a.nbins;
+  const R sg = (R)a.sigma, ia = (R)a.ia;
+  const int b0 = max(0, (int)ceil((r - 5 * sg - (R)a.r0) / (R)a.dr));
+  const int b1 = min(a.nbins - 1, (int)floor((r + 5 * sg - (R)a.r0) / (R)a.dr));
+  for (int b = b0; b <= b1; ++b) {
+    const R u = ((R)a.r0 + b * (R)a.dr - r) / sg;
+    const R k = ia * exp(-(R)0.5 * u * u);
+    unsigned long long q;
+    if constexpr (sizeof(R) == 8)
+      q = (unsigned long long)(k * kHistScale + 0.5);
+    else  // FP32 run: the fixed-point value formed on the FP32 pipe
+      q = __float2ull_rn(k * (float)kHistScale);
+    atomicAdd(hb + b, q);
+  }
+}
+
+// dL/dr of the observable at r for the type pair of (ta, scode)
+template <typename R>
+__device__ __forceinline__ R adj_dldr(const KP &p, const AdjArgs &a, int ta, int scode, R r) {
+  const int tp = tpair(ta, scode - p.ndna, p.nion_t);
+  const double *sb = a.sbin + (size_t)tp * a.nbins;
+  const R sg = (R)a.sigma, ia = (R)a.ia;
+  const int b0 = max(0, (int)ceil((r - 5 * sg - (R)a.r0) / (R)a.dr));
+  const int b1 = min(a.nbins - 1, (int)floor((r + 5 * sg - (R)a.r0) / (R)a.dr));
+  R dldr = 0;
+  for (int b = b0; b <= b1; ++b) {
+    const R u = ((R)a.r0 + b * (R)a.dr - r) / sg;
+    dldr += (R)sb[b] * ia * exp(-(R)0.5 * u * u) * u / sg;
+  }
+  return dldr;
+}
+
 template <typename R, int MODE>
-__global__ void __launch_bounds__(kAdjThreads) k_adj_pairs(KP p, AdjArgs a) {
-  __shared__ float4 sh[kAdjThreads], sl[kAdjThreads];
-  __shared__ R sv[3][kAdjThreads];
+__global__ void __launch_bounds__(32 * kAdjTileWarps) k_adj_tiles(KP p, AdjArgs a) {
+  __shared__ AdjWarp<R> ws[kAdjTileWarps];
+  __shared__ AdjTail<R> tails[kAdjTypePairs];
+  const int nt = p.nion_t;
+  if (MODE != kModeHist)
+    for (int c = threadIdx.x; c < nt * nt; c += blockDim.x) {
+      const int is = p.pidx[(c / nt + p.ndna) * p.nttyp + p.ndna + c % nt];
+      AdjTail<R> t;
+      if constexpr (sizeof(R) == 8) {
+        const PairParam &q = p.pp[is];
+        t = AdjTail<R>{q.dm2hi, q.sc2, (q.flags & kChr) ? q.fct : 0.0};
+      } else {
+        const PairParamF &q = p.ppf[is];
+        t = AdjTail<R>{q.dm2hi, q.sc2, (q.flags & kChr) ? q.fct : 0.0f};
+      }
+      tails[(c / nt) * kAdjMaxIonTypes + c % nt] = t;
+    }
+  __syncthreads();
+  constexpr unsigned kAll = 0xffffffffu;
+  const int lane = threadIdx.x & 31, wi = threadIdx.x >> 5;
+  const int n = a.n, T = (n + 31) >> 5;
+  const int q = blockIdx.x * kAdjTileWarps + wi;
+  if (q >= n3_pairs(T)) return;  // warp-uniform; no block barrier follows
+  AdjWarp<R> &w = ws[wi];
+  int I, J;
+  n3_pair(T, q, I, J);
+  const bool diag = I == J;
   const R *vin = (const R *)a.v;
-  const int n = a.n;
-  const int t = blockIdx.x * kAdjThreads + threadIdx.x;
+  const int j = J * 32 + lane, ncol = min(32, n - J * 32);
+  if (j < n) {
+    w.h[lane] = a.h[j];
+    w.l[lane] = a.l[j];
+    if (MODE == kModeBack) {
+      w.v[0][lane] = vin[j];
+      w.v[1][lane] = vin[n + j];
+      w.v[2][lane] = vin[2 * n + j];
+    }
+  }
+  w.s[0][lane] = w.s[1][lane] = w.s[2][lane] = (R)0;
+  const int t = I * 32 + lane;
   const bool tv = t < n;
-  const int s0 = blockIdx.y * a.chunk, s1 = min(n, s0 + a.chunk);
   float4 th = make_float4(0.f, 0.f, 0.f, 0.f), tl = th;
   R tvx = 0, tvy = 0, tvz = 0;
   if (tv) {
@@ -159,139 +277,256 @@ __global__ void __launch_bounds__(kAdjThreads) k_adj_pairs(KP p, AdjArgs a) {
   }
   const int tcode = __float_as_int(th.w) & 0xffff;
   const int ta = tcode - p.ndna;
-  const int row = tcode * p.nttyp;
+  const bool dep = MODE == kModeHist || (MODE == kModeForce && a.deposit);
+  const R rcut2 = MODE == kModeForce && !a.deposit ? (R)0 : (R)a.rcut2;
+  const unsigned below = (1u << lane) - 1u;
   R ox = 0, oy = 0, oz = 0;
-  double tail[kAdjMaxIonTypes] = {0.0, 0.0, 0.0, 0.0};
-  for (int base = s0; base < s1; base += kAdjThreads) {
-    const int s = base + threadIdx.x;
-    __syncthreads();
-    if (s < s1) {
-      sh[threadIdx.x] = a.h[s];
-      sl[threadIdx.x] = a.l[s];
-      if (MODE == kModeBack) {
-        sv[0][threadIdx.x] = vin[s];
-        sv[1][threadIdx.x] = vin[n + s];
-        sv[2][threadIdx.x] = vin[2 * n + s];
-      }
-    }
-    __syncthreads();
-    const int cnt = min(kAdjThreads, s1 - base);
-    R ttail[kAdjMaxIonTypes] = {0, 0, 0, 0};
-    if (tv) {
-      for (int k = 0; k < cnt; ++k) {
-        const int s = base + k;
-        if (s == t) continue;
-        const float4 h = sh[k], l = sl[k];
-        const R dx = (to_r<R>(th.x, tl.x) - to_r<R>(h.x, l.x)) +
-                     (sizeof(R) == 8 ? R(0) : R(tl.x - l.x));
-        const R dy = (to_r<R>(th.y, tl.y) - to_r<R>(h.y, l.y)) +
-                     (sizeof(R) == 8 ? R(0) : R(tl.y - l.y));
-        const R dz = (to_r<R>(th.z, tl.z) - to_r<R>(h.z, l.z)) +
-                     (sizeof(R) == 8 ? R(0) : R(tl.z - l.z));
+  R ttail[kAdjMaxIonTypes] = {0, 0, 0, 0};
+  int qn = 0;  // queued pairs (warp-uniform)
+  // separation of row ion (h0, l0) and column entry m, as the FP32 path forms it
+  auto sep = [&](const float4 &h0, const float4 &l0, int m, R &dx, R &dy, R &dz) {
+    const float4 h = w.h[m], l = w.l[m];
+    dx = (to_r<R>(h0.x, l0.x) - to_r<R>(h.x, l.x)) + (sizeof(R) == 8 ? R(0) : R(l0.x - l.x));
+    dy = (to_r<R>(h0.y, l0.y) - to_r<R>(h.y, l.y)) + (sizeof(R) == 8 ? R(0) : R(l0.y - l.y));
+    dz = (to_r<R>(h0.z, l0.z) - to_r<R>(h.z, l.z)) + (sizeof(R) == 8 ? R(0) : R(l0.z - l.z));
+  };
+  auto add_tail = [&](int tb, R v) {
+#pragma unroll
+    for (int m = 0; m < kAdjMaxIonTypes; ++m)
+      if (m == tb) ttail[m] += v;
+  };
+  auto flush = [&]() {  // warp-uniform
+    for (int b = 0; b < qn; b += 32) {
+      const int idx = b + lane;
+      const bool act = idx < qn;
+      const int ent = act ? w.q[idx] : 0;
+      const int rl = ent & 31, m = ent >> 5;
+      // the row ion: lane rl's records
+      const float4 h0 = make_float4(__shfl_sync(kAll, th.x, rl), __shfl_sync(kAll, th.y, rl),
+                                    __shfl_sync(kAll, th.z, rl), 0.f);
+      const float4 l0 = make_float4(__shfl_sync(kAll, tl.x, rl), __shfl_sync(kAll, tl.y, rl),
+                                    __shfl_sync(kAll, tl.z, rl), 0.f);
+      const int rcode = __shfl_sync(kAll, tcode, rl), ra = rcode - p.ndna;
+      const R rvx = __shfl_sync(kAll, tvx, rl), rvy = __shfl_sync(kAll, tvy, rl),
+              rvz = __shfl_sync(kAll, tvz, rl);
+      R px = 0, py = 0, pz = 0, pt = 0;
+      int tb = 0;
+      if (act) {
+        R dx, dy, dz;
+        sep(h0, l0, m, dx, dy, dz);
         const R x2 = dx * dx + dy * dy + dz * dz;
-        const int scode = __float_as_int(h.w) & 0xffff;
+        const int scode = __float_as_int(w.h[m].w) & 0xffff;
+        tb = scode - p.ndna;
         if (MODE == kModeHist) {
-          if (t < s && x2 < (R)a.rcut2) {
-            const R r = sqrt(x2);
-            const int tp = tpair(ta, scode - p.ndna, p.nion_t);
-            unsigned long long *hb = a.hist + (size_t)tp * a.nbins;
-            const R sg = (R)a.sigma, ia = (R)(0.3989422804014327 / a.sigma);
-            const int b0 = max(0, (int)ceil((r - 5 * sg - (R)a.r0) / (R)a.dr));
-            const int b1 = min(a.nbins - 1, (int)floor((r + 5 * sg - (R)a.r0) / (R)a.dr));
-            for (int b = b0; b <= b1; ++b) {
-              const R u = ((R)a.r0 + b * (R)a.dr - r) / sg;
-              const R k = ia * exp(-(R)0.5 * u * u);
-              unsigned long long q;
-              if constexpr (sizeof(R) == 8)
-                q = (unsigned long long)(k * kHistScale + 0.5);
-              else  // FP32 run: the fixed-point value formed on the FP32 pipe
-                q = __float2ull_rn(k * (float)kHistScale);
-              atomicAdd(hb + b, q);
+          adj_deposit<R>(p, a, ra, scode, sqrt(x2));
+        } else {
+          const int is = p.pidx[rcode * p.nttyp + scode];
+          R g, gp, r;
+          int region, piece = 0;
+          efp_adj<R>(p, is, x2, g, gp, r, region, piece);
+          if (MODE == kModeForce) {
+            if (dep && x2 < rcut2) adj_deposit<R>(p, a, ra, scode, r);
+            px = g * dx;
+            py = g * dy;
+            pz = g * dz;
+          } else {
+            const R vx = rvx - w.v[0][m], vy = rvy - w.v[1][m], vz = rvz - w.v[2][m];
+            const R qv = dx * vx + dy * vy + dz * vz;
+            R r_, ir, ir2;
+            efp_r<R>(x2, r_, ir, ir2);
+            const R c = gp * ir * qv;
+            px = g * vx + c * dx;
+            py = g * vy + c * dy;
+            pz = g * vz + c * dz;
+            if (a.theta) {
+              if (region == 0) {
+                atomicAdd(a.g_ep + 3 * piece + 1, (double)(-qv * ir));
+                atomicAdd(a.g_ep + 3 * piece + 2, (double)(-2 * qv));
+              } else if (region == 1) {
+                const R i6 = ir2 * ir2 * ir2;
+                atomicAdd(a.g_sc + 3 * is, (double)(12 * i6 * i6 * ir2 * qv));
+              } else {
+                pt = 6 * ir2 * ir2 * ir2 * ir2 * qv;
+              }
+            }
+            if (x2 < rcut2) {
+              const R dldr = adj_dldr<R>(p, a, ra, scode, r);
+              px += dldr * dx * ir;
+              py += dldr * dy * ir;
+              pz += dldr * dz * ir;
             }
           }
-          continue;
         }
-        const int is = p.pidx[row + scode];
-        R g, gp, r;
-        int region, piece = 0;
-        efp_adj<R>(p, is, x2, g, gp, r, region, piece);
-        if (MODE == kModeForce) {
-          ox += g * dx;
-          oy += g * dy;
-          oz += g * dz;
-          continue;
-        }
-        // backward: J v, dL/dtheta, dL/dx of the observable
-        const R vx = tvx - sv[0][k], vy = tvy - sv[1][k], vz = tvz - sv[2][k];
-        const R q = dx * vx + dy * vy + dz * vz;
-        const R ir = (R)1 / r;
-        const R c = gp * ir * q;
-        ox += g * vx + c * dx;
-        oy += g * vy + c * dy;
-        oz += g * vz + c * dz;
-        if (a.theta && t < s) {
-          if (region == 0) {
-            atomicAdd(a.g_ep + 3 * piece + 1, (double)(-q * ir));
-            atomicAdd(a.g_ep + 3 * piece + 2, (double)(-2 * q));
-          } else if (region == 1) {
-            const R ir2 = ir * ir, i6 = ir2 * ir2 * ir2;
-            atomicAdd(a.g_sc + 3 * is, (double)(12 * i6 * i6 * ir2 * q));
-          } else {
-            const R ir2 = ir * ir;
-            const int tb = scode - p.ndna;
-            if (tb < kAdjMaxIonTypes) ttail[tb] += 6 * ir2 * ir2 * ir2 * ir2 * q;
+      }
+      if (MODE != kModeHist) {
+        const int nb = min(32, qn - b);
+        for (int u = 0; u < nb; ++u) {  // queue order
+          const int rt = __shfl_sync(kAll, rl, u), mt = __shfl_sync(kAll, m, u),
+                    tbt = __shfl_sync(kAll, tb, u);
+          const R vx = __shfl_sync(kAll, px, u), vy = __shfl_sync(kAll, py, u),
+                  vz = __shfl_sync(kAll, pz, u), vt = __shfl_sync(kAll, pt, u);
+          if (lane == rt) {
+            ox += vx;
+            oy += vy;
+            oz += vz;
+            w.s[0][mt] -= vx;
+            w.s[1][mt] -= vy;
+            w.s[2][mt] -= vz;
+            if (MODE == kModeBack) add_tail(tbt, vt);
           }
-        }
-        if (x2 < (R)a.rcut2) {  // observable: dL/dr d / r
-          const int tp = tpair(ta, scode - p.ndna, p.nion_t);
-          const double *sb = a.sbin + (size_t)tp * a.nbins;
-          const R sg = (R)a.sigma, ia = (R)(0.3989422804014327 / a.sigma);
-          const int b0 = max(0, (int)ceil((r - 5 * sg - (R)a.r0) / (R)a.dr));
-          const int b1 = min(a.nbins - 1, (int)floor((r + 5 * sg - (R)a.r0) / (R)a.dr));
-          R dldr = 0;
-          for (int b = b0; b <= b1; ++b) {
-            const R u = ((R)a.r0 + b * (R)a.dr - r) / sg;
-            dldr += (R)sb[b] * ia * exp(-(R)0.5 * u * u) * u / sg;
-          }
-          ox += dldr * dx * ir;
-          oy += dldr * dy * ir;
-          oz += dldr * dz * ir;
+          __syncwarp();
         }
       }
     }
-    if (MODE == kModeBack)
-      for (int m = 0; m < kAdjMaxIonTypes; ++m) tail[m] += (double)ttail[m];
-  }
-  if (MODE == kModeBack && tv) {
-    for (int m = 0; m < kAdjMaxIonTypes && m < p.nion_t; ++m)
-      if (tail[m] != 0.0) {
-        const int is = p.pidx[row + p.ndna + m];
-        atomicAdd(a.g_sc + 3 * is + 2, tail[m]);
+    qn = 0;
+  };
+  __syncwarp();
+  const int k0 = diag ? 1 : 0, k1 = diag ? 16 : 31;
+  for (int k = k0; k <= k1; ++k) {
+    const int mm = (lane + k) & 31;
+    bool slow = false;
+    if (tv && mm < ncol && !(diag && k == 16 && lane >= 16)) {
+      R dx, dy, dz;
+      sep(th, tl, mm, dx, dy, dz);
+      const R x2 = dx * dx + dy * dy + dz * dz;
+      if (MODE == kModeHist) {
+        slow = x2 < rcut2;
+      } else {
+        const int tb = (__float_as_int(w.h[mm].w) & 0xffff) - p.ndna;
+        const AdjTail<R> L = tails[ta * kAdjMaxIonTypes + tb];
+        slow = !(x2 > L.dm2hi) || x2 < rcut2;
+        if (!slow) {  // the analytic tail, outside the histogram's range
+          R r, ir, ir2, g, gp;
+          efp_r<R>(x2, r, ir, ir2);
+          efp_tail<R>(L.sc2, L.fct, ir, ir2, g, gp);
+          R px, py, pz;
+          if (MODE == kModeForce) {
+            px = g * dx;
+            py = g * dy;
+            pz = g * dz;
+          } else {
+            const R vx = tvx - w.v[0][mm], vy = tvy - w.v[1][mm], vz = tvz - w.v[2][mm];
+            const R qv = dx * vx + dy * vy + dz * vz;
+            const R c = gp * ir * qv;
+            px = g * vx + c * dx;
+            py = g * vy + c * dy;
+            pz = g * vz + c * dz;
+            if (a.theta) add_tail(tb, 6 * ir2 * ir2 * ir2 * ir2 * qv);
+          }
+          ox += px;
+          oy += py;
+          oz += pz;
+          w.s[0][mm] -= px;
+          w.s[1][mm] -= py;
+          w.s[2][mm] -= pz;
+        }
       }
+    }
+    const unsigned bs = __ballot_sync(kAll, slow);
+    if (slow) w.q[qn + __popc(bs & below)] = lane | (mm << 5);
+    qn += __popc(bs);
+    __syncwarp();
+    if (qn > kAdjQ - 32) flush();
   }
-  if (MODE != kModeHist && tv) {
-    R *o = (R *)a.out + (size_t)blockIdx.y * 3 * n;
-    o[t] = ox;
-    o[n + t] = oy;
-    o[2 * n + t] = oz;
+  if (qn) flush();
+  if (MODE == kModeHist) return;
+  R *o = (R *)a.out + (size_t)q * 192;
+  o[lane] = tv ? ox : (R)0;
+  o[32 + lane] = tv ? oy : (R)0;
+  o[64 + lane] = tv ? oz : (R)0;
+  o[96 + lane] = w.s[0][lane];
+  o[128 + lane] = w.s[1][lane];
+  o[160 + lane] = w.s[2][lane];
+  if (MODE == kModeBack && a.theta) {
+    // the tail sums per (row type, column type), over the warp in a fixed
+    // shuffle tree
+    R *tq = (R *)a.tail + q;
+    const size_t np = n3_pairs(T);
+#pragma unroll
+    for (int m = 0; m < kAdjMaxIonTypes; ++m) {
+      if (m >= nt) break;
+      for (int ra = 0; ra < nt; ++ra) {
+        R v = ra == ta && tv ? ttail[m] : (R)0;
+#pragma unroll
+        for (int o2 = 16; o2 > 0; o2 >>= 1) v += __shfl_xor_sync(kAll, v, o2);
+        if (lane == 0) tq[(ra * kAdjMaxIonTypes + m) * np] = v;
+      }
+    }
   }
 }
 
-// Forward step: forces from the chunk partials (fixed order), the BD move
-// of dynamics0 with frozen noise, the box clamp, and the clamp masks of the
-// step (bit k: bdmax clamp of component k; bit 3 + k: wall clamp).
+// dL/dtheta of the tail constants: per (row type, column type) the sum over
+// the tile pairs in a fixed order (a strided pass, then a fixed tree), added
+// to g_sc one type pair after another by one thread.
+constexpr int kTailThreads = 1024;
 template <typename R>
-__global__ void k_adj_move(KP p, const float4 *h, const float4 *l, const R *part, int nchunk,
-                           int n, float4 *hn, float4 *ln, uint8_t *mask, BoxF box,
-                           uint64_t seed, uint64_t step) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  R F[3];
-  for (int k = 0; k < 3; ++k) {
-    R v = 0;
-    for (int c = 0; c < nchunk; ++c) v += part[((size_t)c * 3 + k) * n + i];
-    F[k] = v;
+__global__ void __launch_bounds__(kTailThreads) k_adj_tails(KP p, const R *tail, int npair,
+                                                            double *g_sc) {
+  __shared__ double part[kAdjTypePairs][kTailThreads / 32];
+  const int nt = p.nion_t, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = 0; c < nt * nt; ++c) {
+    const int off = (c / nt) * kAdjMaxIonTypes + c % nt;
+    double v = 0.0;
+#pragma unroll 8
+    for (int k = threadIdx.x; k < npair; k += kTailThreads)
+      v += (double)tail[(size_t)off * npair + k];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) part[c][w] = v;
   }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int c = 0; c < nt * nt; ++c) {
+      double v = 0.0;
+      for (int k = 0; k < kTailThreads / 32; ++k) v += part[c][k];
+      const int is = p.pidx[(c / nt + p.ndna) * p.nttyp + p.ndna + c % nt];
+      g_sc[3 * is + 2] += v;
+    }
+}
+
+// The sums of tile t's 32 particles over their tile-pair partials, in a
+// fixed order: block of kGatherWarps warps, warp w takes the tile pairs (u,
+// t) and (t, u) of u = w, w + kGatherWarps, ... in order, then warp 0 adds
+// the warps' sums in order w = 0, 1, ... (lane l: particle 32 t + l).
+constexpr int kGatherWarps = 8;
+template <typename R>
+__device__ __forceinline__ void adj_gather_tile(const R *tp, int n, int t, R (&F)[3]) {
+  __shared__ R sh[kGatherWarps][3][32];
+  const int T = (n + 31) >> 5, lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  R v[3] = {0, 0, 0};
+#pragma unroll 4
+  for (int u = w; u < T; u += kGatherWarps) {
+    const R *e = tp + (size_t)(u <= t ? n3_index(T, u, t) : n3_index(T, t, u)) * 192 + lane;
+    for (int k = 0; k < 3; ++k) {
+      if (u < t)
+        v[k] += e[96 + 32 * k];
+      else if (u > t)
+        v[k] += e[32 * k];
+      else
+        v[k] += e[32 * k] + e[96 + 32 * k];
+    }
+  }
+  for (int k = 0; k < 3; ++k) sh[w][k][lane] = v[k];
+  __syncthreads();
+  for (int k = 0; k < 3; ++k) {
+    R s = 0;
+    for (int x = 0; x < kGatherWarps; ++x) s += sh[x][k][lane];
+    F[k] = s;
+  }
+}
+
+// Forward step, a block per tile: forces from the tile-pair partials (fixed
+// order), the BD move of dynamics0 with frozen noise, the box clamp, and the
+// clamp masks of the step (bit k: bdmax clamp of component k; bit 3 + k:
+// wall clamp).
+template <typename R>
+__global__ void __launch_bounds__(32 * kGatherWarps)
+    k_adj_move(KP p, const float4 *h, const float4 *l, const R *part, int n, float4 *hn,
+               float4 *ln, uint8_t *mask, BoxF box, uint64_t seed, uint64_t step) {
+  R F[3];
+  adj_gather_tile(part, n, blockIdx.x, F);
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  if (threadIdx.x >= 32 || i >= n) return;
   const int it = abs(p.typei[i]);
   R fact1, fact2;
   if constexpr (sizeof(R) == 8) {
@@ -364,16 +599,16 @@ __global__ void k_adj_prep(KP p, const R *a, const uint8_t *mask, int n, R *mu, 
   }
 }
 
-// Backward, after the pair sweep: a = mu + sum of the chunk partials.
+// Backward, after the pair sweep, a block per tile: a = mu + the tile-pair
+// partials.
 template <typename R>
-__global__ void k_adj_combine(const R *mu, const R *part, int nchunk, int n, R *a) {
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= n) return;
-  for (int k = 0; k < 3; ++k) {
-    R v = mu ? mu[(size_t)k * n + i] : (R)0;
-    for (int c = 0; c < nchunk; ++c) v += part[((size_t)c * 3 + k) * n + i];
-    a[(size_t)k * n + i] = v;
-  }
+__global__ void __launch_bounds__(32 * kGatherWarps)
+    k_adj_combine(const R *mu, const R *part, int n, R *a) {
+  R F[3];
+  adj_gather_tile(part, n, blockIdx.x, F);
+  const int i = blockIdx.x * 32 + threadIdx.x;
+  if (threadIdx.x >= 32 || i >= n) return;
+  for (int k = 0; k < 3; ++k) a[(size_t)k * n + i] = (mu ? mu[(size_t)k * n + i] : (R)0) + F[k];
 }
 
 }  // namespace bgpu
@@ -387,7 +622,8 @@ struct bromoc_adj {
   int precision = BROMOC_FP32;
   std::string err;
   int cap = 0, n = 0, nt = 0, ntp = 0;
-  int nchunk = 1, chunk = 64;
+  size_t part_bytes = 0, tail_bytes = 0;  // tile-pair partials (grow-only)
+  void *tail = nullptr;
   int *typei = nullptr;
   float4 *x0h = nullptr, *x0l = nullptr;    // initial configuration
   float4 *xfh = nullptr, *xfl = nullptr;    // final configuration of the forward run
@@ -425,6 +661,23 @@ int aset(bromoc_adj *a, int code, const char *fmt, ...) {
       return aset(ad, BROMOC_E_CUDA, "%s: %s", #call, cudaGetErrorString(e_)); \
   } while (0)
 
+// (re)allocates *p for at least `bytes` (grow-only); `have` tracks its size
+int agrow(bromoc_adj *ad, void **p, size_t &have, size_t bytes) {
+  if (*p && bytes <= have) return BROMOC_OK;
+  if (*p) {
+    cudaFree(*p);
+    ad->allocs.erase(std::find(ad->allocs.begin(), ad->allocs.end(), *p));
+    *p = nullptr;
+    have = 0;
+  }
+  cudaError_t e = cudaMalloc(p, std::max<size_t>(bytes, 1));
+  if (e != cudaSuccess)
+    return aset(ad, BROMOC_E_NOMEM, "cudaMalloc(%zu bytes): %s", bytes, cudaGetErrorString(e));
+  ad->allocs.push_back(*p);
+  have = bytes;
+  return BROMOC_OK;
+}
+
 template <class T>
 int aalloc(bromoc_adj *ad, T **p, size_t count) {
   *p = nullptr;
@@ -450,41 +703,49 @@ int view(bromoc_adj *ad, KP &p) {
 
 template <typename R>
 void run_pairs(bromoc_adj *ad, const KP &p, int mode, const float4 *h, const float4 *l,
-               const void *v, bool obs, bool theta) {
+               const void *v, bool obs, bool theta, bool deposit = false) {
   AdjArgs a{};
   a.h = h;
   a.l = l;
   a.v = v;
   a.out = ad->part;
+  a.tail = ad->tail;
   a.g_ep = ad->g_ep;
   a.g_sc = ad->g_sc;
   a.hist = ad->hist;
   a.sbin = ad->sbin;
   a.n = ad->n;
-  a.nchunk = ad->nchunk;
-  a.chunk = ad->chunk;
   a.nbins = ad->nbins;
+  a.deposit = deposit ? 1 : 0;
   a.r0 = (float)ad->r0;
   a.dr = (float)ad->dr;
   a.sigma = (float)ad->sigma;
+  a.ia = 0.3989422804014327 / (double)a.sigma;
   const double rc = ad->r0 + ad->dr * (ad->nbins - 1) + 5.0 * ad->sigma;
-  a.rcut2 = obs ? (float)(rc * rc) : 0.0f;
+  a.rcut2 = obs || deposit ? (float)(rc * rc) : 0.0f;
   a.theta = theta ? 1 : 0;
-  const dim3 g((ad->n + kAdjThreads - 1) / kAdjThreads, ad->nchunk);
-  if (mode == kModeForce)
-    k_adj_pairs<R, kModeForce><<<g, kAdjThreads, 0, ad->stream>>>(p, a);
-  else if (mode == kModeBack)
-    k_adj_pairs<R, kModeBack><<<g, kAdjThreads, 0, ad->stream>>>(p, a);
-  else
-    k_adj_pairs<R, kModeHist><<<g, kAdjThreads, 0, ad->stream>>>(p, a);
+  const int npair = n3_pairs((ad->n + 31) / 32);
+  const int g = (npair + kAdjTileWarps - 1) / kAdjTileWarps, b = 32 * kAdjTileWarps;
+  if (mode == kModeForce) {
+    k_adj_tiles<R, kModeForce><<<g, b, 0, ad->stream>>>(p, a);
+  } else if (mode == kModeBack) {
+    k_adj_tiles<R, kModeBack><<<g, b, 0, ad->stream>>>(p, a);
+    if (theta)
+      k_adj_tails<R><<<1, kTailThreads, 0, ad->stream>>>(p, (const R *)ad->tail, npair,
+                                                        ad->g_sc);
+  } else {
+    k_adj_tiles<R, kModeHist><<<g, b, 0, ad->stream>>>(p, a);
+  }
 }
 
+// one forward step from (h, l); deposit: the histogram of (h, l) in the same
+// pair sweep
 template <typename R>
 void step_forward(bromoc_adj *ad, const KP &p, const float4 *h, const float4 *l, float4 *hn,
-                  float4 *ln, uint8_t *mask, uint64_t step) {
-  run_pairs<R>(ad, p, kModeForce, h, l, nullptr, false, false);
-  k_adj_move<R><<<(ad->n + 127) / 128, 128, 0, ad->stream>>>(
-      p, h, l, (const R *)ad->part, ad->nchunk, ad->n, hn, ln, mask, p.f.box, ad->seed, step);
+                  float4 *ln, uint8_t *mask, uint64_t step, bool deposit = false) {
+  run_pairs<R>(ad, p, kModeForce, h, l, nullptr, false, false, deposit);
+  k_adj_move<R><<<(ad->n + 31) / 32, 32 * kGatherWarps, 0, ad->stream>>>(
+      p, h, l, (const R *)ad->part, ad->n, hn, ln, mask, p.f.box, ad->seed, step);
 }
 
 template <typename R>
@@ -496,11 +757,12 @@ int forward_impl(bromoc_adj *ad, const KP &p, double *hist_out) {
                       ad->stream));
   ACU(cudaMemcpyAsync(ad->ckl[0], ad->x0l, n * sizeof(float4), cudaMemcpyDeviceToDevice,
                       ad->stream));
+  // the histogram of x_1 .. x_T: x_t's deposit rides on step t's force
+  // sweep, x_T's is a sweep of its own
   const float4 *h = ad->x0h, *l = ad->x0l;
   for (int t = 0; t < ad->nsteps; ++t) {
     float4 *hn = ad->trh[(t + 1) & 1], *ln = ad->trl[(t + 1) & 1];
-    step_forward<R>(ad, p, h, l, hn, ln, nullptr, ad->step0 + t);
-    run_pairs<R>(ad, p, kModeHist, hn, ln, nullptr, true, false);  // RDF of x_{t+1}
+    step_forward<R>(ad, p, h, l, hn, ln, nullptr, ad->step0 + t, t >= 1);
     if ((t + 1) % ad->ckpt == 0 && t + 1 < ad->nsteps) {
       const int c = (t + 1) / ad->ckpt;
       ACU(cudaMemcpyAsync(ad->ckh[c], hn, n * sizeof(float4), cudaMemcpyDeviceToDevice,
@@ -511,6 +773,7 @@ int forward_impl(bromoc_adj *ad, const KP &p, double *hist_out) {
     h = hn;
     l = ln;
   }
+  run_pairs<R>(ad, p, kModeHist, h, l, nullptr, true, false);
   ACU(cudaMemcpyAsync(ad->xfh, h, n * sizeof(float4), cudaMemcpyDeviceToDevice, ad->stream));
   ACU(cudaMemcpyAsync(ad->xfl, l, n * sizeof(float4), cudaMemcpyDeviceToDevice, ad->stream));
   std::vector<unsigned long long> hh((size_t)ad->ntp * ad->nbins);
@@ -529,8 +792,8 @@ int backward_impl(bromoc_adj *ad, const KP &p) {
   // a = dL/dx_T (observable of the last configuration only)
   ACU(cudaMemsetAsync(ad->v, 0, 3 * (size_t)n * sizeof(R), ad->stream));
   run_pairs<R>(ad, p, kModeBack, ad->xfh, ad->xfl, ad->v, true, false);
-  k_adj_combine<R><<<nb, 128, 0, ad->stream>>>(nullptr, (const R *)ad->part, ad->nchunk, n,
-                                               (R *)ad->a);
+  const int ntile = (n + 31) / 32, gb = 32 * kGatherWarps;
+  k_adj_combine<R><<<ntile, gb, 0, ad->stream>>>(nullptr, (const R *)ad->part, n, (R *)ad->a);
   const int nseg = (T + K - 1) / K;
   for (int seg = nseg - 1; seg >= 0; --seg) {
     const int t0 = seg * K, t1 = std::min(T, t0 + K);
@@ -549,8 +812,8 @@ int backward_impl(bromoc_adj *ad, const KP &p) {
                                                 ad->mask + (size_t)k * ad->cap, n,
                                                 (R *)ad->mu, (R *)ad->v);
       run_pairs<R>(ad, p, kModeBack, ad->trh[k], ad->trl[k], ad->v, t >= 1, true);
-      k_adj_combine<R><<<nb, 128, 0, ad->stream>>>((const R *)ad->mu, (const R *)ad->part,
-                                                   ad->nchunk, n, (R *)ad->a);
+      k_adj_combine<R><<<ntile, gb, 0, ad->stream>>>((const R *)ad->mu, (const R *)ad->part, n,
+                                                     (R *)ad->a);
     }
   }
   ACU(cudaGetLastError());
@@ -604,12 +867,11 @@ int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
   if (!rc) rc = aalloc(ad, &ad->xfh, cap);
   if (!rc) rc = aalloc(ad, &ad->xfl, cap);
   char *buf = nullptr;
-  if (!rc) rc = aalloc(ad, &buf, rs * 3 * cap * 35);  // part (32 chunks) + a, mu, v
+  if (!rc) rc = aalloc(ad, &buf, rs * 3 * cap * 3);  // a, mu, v
   if (!rc) {
-    ad->part = buf;
-    ad->a = buf + rs * 3 * cap * 32;
-    ad->mu = buf + rs * 3 * cap * 33;
-    ad->v = buf + rs * 3 * cap * 34;
+    ad->a = buf;
+    ad->mu = buf + rs * 3 * cap;
+    ad->v = buf + rs * 3 * cap * 2;
   }
   if (!rc) rc = aalloc(ad, &ad->g_ep, 3 * (size_t)std::max(pk->cnt, 1));
   if (!rc) rc = aalloc(ad, &ad->g_sc, 3 * (size_t)pk->ntc);
@@ -675,13 +937,12 @@ int bromoc_adj_set_particles(bromoc_adj *ad, int32_t n, const double *x, const d
   ACU(cudaMemcpy(ad->x0h, h.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
   ACU(cudaMemcpy(ad->x0l, l.data(), n * sizeof(float4), cudaMemcpyHostToDevice));
   ACU(cudaMemcpy(ad->typei, typei, n * sizeof(int), cudaMemcpyHostToDevice));
+  // tile-pair partials: [tile pair][side][3][32] and the tail sums
+  const size_t npair = n3_pairs((n + 31) / 32), rs = ad->precision == BROMOC_FP64 ? 8 : 4;
+  if ((rc = agrow(ad, &ad->part, ad->part_bytes, npair * 192 * rs)) ||
+      (rc = agrow(ad, &ad->tail, ad->tail_bytes, npair * kAdjTypePairs * rs)))
+    return rc;
   ad->n = n;
-  // source chunks: ~8 blocks per SM, at most 32
-  const int tiles = (n + kAdjThreads - 1) / kAdjThreads;
-  int want = std::max(1, std::min(32, (8 * 152 + tiles - 1) / tiles));
-  want = std::min(want, tiles);
-  ad->chunk = (tiles + want - 1) / want * kAdjThreads;
-  ad->nchunk = (n + ad->chunk - 1) / ad->chunk;
   ad->have_forward = false;
   return BROMOC_OK;
 }

@@ -50,22 +50,13 @@ def _grad(spec, proto, adj, loss, ckpt=None):
     return value, knot_gradient(jac, g_ep, g_sc)
 
 
-def test_adjoint_matches_finite_differences(gpu_lib):
-    """Central differences with h = 1e-5 kcal/mol, FP64 arithmetic.  The
-    tables keep the reference's knot-spacing quirk (fixdy), which leaves
-    ~1e-5 jumps of U and U' at piece boundaries; a trajectory whose pair
-    crosses a boundary at a different step in the +h and -h runs picks one
-    up, so steps of 1e-4 mix in such events, while at 1e-5 the two agree to
-    ~1e-7."""
-    spec, proto, adj, loss = _setup(gpu_lib, abi.FP64)
-    value, grads = _grad(spec, proto, adj, loss)
-    h = 1e-5
-    rng = np.random.default_rng(0)
-    for key in spec.efpot_knots:
+def _central_differences(spec, proto, adj, loss, picks, h=1e-5):
+    """FP64 central differences of the loss at the given knots {key: [m]}."""
+    out = {}
+    for key, ms in picks.items():
         r, u0 = spec.efpot_knots[key]
         u0 = np.array(u0)
-        big = np.argsort(-np.abs(grads[key]))[:6]  # the knots the loss feels most
-        for m in list(big) + list(rng.integers(0, len(u0), 2)):
+        for m in ms:
             vals = []
             for sgn in (1, -1):
                 u = u0.copy()
@@ -73,9 +64,45 @@ def test_adjoint_matches_finite_differences(gpu_lib):
                 spec.efpot_knots[key] = (r, u)
                 vals.append(loss.loss_grad(_run(spec, proto, adj, loss))[0])
             spec.efpot_knots[key] = (r, u0)
-            fd = (vals[0] - vals[1]) / (2 * h)
-            scale = max(np.abs(grads[key]).max(), 1e-30)
-            assert abs(fd - grads[key][m]) <= 1e-4 * scale, (key, m, fd, grads[key][m])
+            out[key, int(m)] = (vals[0] - vals[1]) / (2 * h)
+    return out
+
+
+def test_adjoint_matches_finite_differences(gpu_lib):
+    """Central differences with h = 1e-5 kcal/mol, FP64 arithmetic.  The
+    tables keep the reference's knot-spacing quirk (fixdy), which leaves
+    ~1e-5 jumps of U and U' at piece boundaries; a trajectory whose pair
+    crosses a boundary at a different step in the +h and -h runs picks one
+    up, so steps of 1e-4 mix in such events, while at 1e-5 the two agree to
+    ~1e-7.  The knots the loss feels most: each within 1e-5 of its own
+    value; two random knots (gradients possibly near zero): within 1e-5 of
+    the largest component."""
+    spec, proto, adj, loss = _setup(gpu_lib, abi.FP64)
+    value, grads = _grad(spec, proto, adj, loss)
+    rng = np.random.default_rng(0)
+    big = {k: list(np.argsort(-np.abs(grads[k]))[:6]) for k in spec.efpot_knots}
+    rnd = {k: list(rng.integers(0, len(spec.efpot_knots[k][1]), 2)) for k in spec.efpot_knots}
+    fd = _central_differences(spec, proto, adj, loss, big)
+    for (key, m), v in fd.items():
+        assert abs(v - grads[key][m]) <= 1e-5 * abs(grads[key][m]), (key, m, v, grads[key][m])
+    fd = _central_differences(spec, proto, adj, loss, rnd)
+    for (key, m), v in fd.items():
+        scale = max(np.abs(grads[key]).max(), 1e-30)
+        assert abs(v - grads[key][m]) <= 1e-5 * scale, (key, m, v, grads[key][m])
+
+
+def test_adjoint_fp32_matches_finite_differences(gpu_lib):
+    """The FP32 adjoint (FP32 pairs, FP64 accumulators) against FP64 central
+    differences (h = 1e-5) at the knots the loss feels most: each within
+    1e-4 of its own value."""
+    spec64, proto64, adj64, loss64 = _setup(gpu_lib, abi.FP64)
+    _, g64 = _grad(spec64, proto64, adj64, loss64)
+    spec32, proto32, adj32, loss32 = _setup(gpu_lib, abi.FP32)
+    _, g32 = _grad(spec32, proto32, adj32, loss32)
+    big = {k: list(np.argsort(-np.abs(g64[k]))[:6]) for k in spec64.efpot_knots}
+    fd = _central_differences(spec64, proto64, adj64, loss64, big)
+    for (key, m), v in fd.items():
+        assert abs(g32[key][m] - v) <= 1e-4 * abs(v), (key, m, g32[key][m], v)
 
 
 def test_adjoint_fp32_close_to_fp64(gpu_lib):

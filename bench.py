@@ -256,7 +256,7 @@ def batch_measure(sh, flush, steps=10, warm=3, plain_steps=3):
                               "the pair and assembly launches)"},
             "autotuner": {"buckets": ["<1000", "1000-4000", ">4000"],
                           "pair_warps_per_block": [int(v) for v in tw],
-                          "tile_pairs": [int(v) for v in tn],
+                          "pair_items": [int(v) for v in tn],
                           "pair_pass_ms_by_warps_2_4_8": [[float(x) for x in row] for row in tms]},
             "per_bucket": buckets}
 
@@ -284,8 +284,13 @@ def pair_scaling(sh, peak_fp32, sizes=(2000, 4000, 8000), reps=10):
         pairs = n_ion * (n_ion - 1) / 2
         t = ms / nl * 1e-3
         a = (PAIR_FLOP + RF_FLOP) * pairs / t / 1e12
-        out.append({"ions": n_ion, "launch_us": t * 1e6, "achieved_tflops": a,
-                    "frac": a / peak_fp32})
+        row = {"ions": n_ion, "launch_us": t * 1e6, "achieved_tflops": a,
+               "frac": a / peak_fp32}
+        traffic, prof = profile_traffic(f"k_pairs32n/{n}")
+        if traffic is not None:
+            row["traffic"] = traffic
+            row["traffic_source"] = prof
+        out.append(row)
         del g
     return out
 
@@ -525,7 +530,7 @@ def profile_traffic(kernel: str):
     """DRAM bytes per launch of `kernel` from the committed ncu summary."""
     for f in sorted((ROOT / "profiles").glob("*.md")):
         txt = f.read_text()
-        m = re.search(r"^traffic_bytes_per_launch\[%s\]:\s*([0-9.eE+]+)" % kernel,
+        m = re.search(r"^traffic_bytes_per_launch\[%s\]:\s*([0-9.eE+]+)" % re.escape(kernel),
                       txt, re.M)
         if m:
             return float(m.group(1)), f.name
@@ -821,8 +826,7 @@ def run_gpu(args, rank, world, local_rank):
         ms, nl = kt_split["pairs"]
         a = per * pairs / (ms / nl * 1e-3) / 1e12
         pair_roof = {"kernel": "k_pairs32n (one launch per BD step)", "achieved": a,
-                     "unit": "TFLOP/s", "frac": a / peak_fp32, "launch_ms": ms / nl,
-                     "traffic": profile_traffic("k_pairs32n")[0]}
+                     "unit": "TFLOP/s", "frac": a / peak_fp32, "launch_ms": ms / nl}
     gathers = None
     if "fields" in kt_split:
         # single-particle terms: 8 static-field corners (32 B), 8 repulsion

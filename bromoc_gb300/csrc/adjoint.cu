@@ -456,31 +456,53 @@ __global__ void __launch_bounds__(32 * kAdjTileWarps) k_adj_tiles(KP p, AdjArgs 
 }
 
 // dL/dtheta of the tail constants: per (row type, column type) the sum over
-// the tile pairs in a fixed order (a strided pass, then a fixed tree), added
-// to g_sc one type pair after another by one thread.
-constexpr int kTailThreads = 1024;
+// the tile pairs in a fixed order -- kTailBlocks blocks each sum a stretch of
+// tile pairs (a strided pass, then a fixed shuffle and warp order) into
+// part[block][type pair], then a warp per type pair adds the blocks' sums
+// (a fixed shuffle tree) and one thread adds each type pair's total to g_sc,
+// one type pair after another.
+// FP64 sums spread over the SMs (the FP64 rate of one SM is low).
+constexpr int kTailBlocks = 64, kTailThreads = 256;
 template <typename R>
-__global__ void __launch_bounds__(kTailThreads) k_adj_tails(KP p, const R *tail, int npair,
-                                                            double *g_sc) {
-  __shared__ double part[kAdjTypePairs][kTailThreads / 32];
+__global__ void __launch_bounds__(kTailThreads)
+    k_adj_tails(KP p, const R *tail, int npair, double *part) {
+  __shared__ double wsum[kAdjTypePairs][kTailThreads / 32];
   const int nt = p.nion_t, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int per = (npair + kTailBlocks - 1) / kTailBlocks;
+  const int k0 = blockIdx.x * per, k1 = min(npair, k0 + per);
   for (int c = 0; c < nt * nt; ++c) {
     const int off = (c / nt) * kAdjMaxIonTypes + c % nt;
     double v = 0.0;
-#pragma unroll 8
-    for (int k = threadIdx.x; k < npair; k += kTailThreads)
+    for (int k = k0 + threadIdx.x; k < k1; k += kTailThreads)
       v += (double)tail[(size_t)off * npair + k];
 #pragma unroll
     for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
-    if (lane == 0) part[c][w] = v;
+    if (lane == 0) wsum[c][w] = v;
+  }
+  __syncthreads();
+  if (threadIdx.x < nt * nt) {
+    double v = 0.0;
+    for (int k = 0; k < kTailThreads / 32; ++k) v += wsum[threadIdx.x][k];
+    part[(size_t)blockIdx.x * kAdjTypePairs + threadIdx.x] = v;
+  }
+}
+
+__global__ void k_adj_tails_fin(KP p, const double *part, double *g_sc) {
+  static_assert(kTailBlocks == 64, "two block sums a lane");
+  __shared__ double tot[kAdjTypePairs];
+  const int nt = p.nion_t, w = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  for (int c = w; c < nt * nt; c += blockDim.x >> 5) {  // a warp per type pair
+    double v = part[(size_t)lane * kAdjTypePairs + c] +
+               part[(size_t)(lane + 32) * kAdjTypePairs + c];
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+    if (lane == 0) tot[c] = v;
   }
   __syncthreads();
   if (threadIdx.x == 0)
     for (int c = 0; c < nt * nt; ++c) {
-      double v = 0.0;
-      for (int k = 0; k < kTailThreads / 32; ++k) v += part[c][k];
       const int is = p.pidx[(c / nt + p.ndna) * p.nttyp + p.ndna + c % nt];
-      g_sc[3 * is + 2] += v;
+      g_sc[3 * is + 2] += tot[c];
     }
 }
 
@@ -633,6 +655,7 @@ struct bromoc_adj {
   void *part = nullptr, *a = nullptr, *mu = nullptr, *v = nullptr;
   unsigned long long *hist = nullptr;
   double *sbin = nullptr, *g_ep = nullptr, *g_sc = nullptr;
+  double *tail_part = nullptr;  // [kTailBlocks][kAdjTypePairs]
   int nbins = 0;
   double r0 = 0.0, dr = 0.0, sigma = 0.0;
   // the last forward run
@@ -730,9 +753,11 @@ void run_pairs(bromoc_adj *ad, const KP &p, int mode, const float4 *h, const flo
     k_adj_tiles<R, kModeForce><<<g, b, 0, ad->stream>>>(p, a);
   } else if (mode == kModeBack) {
     k_adj_tiles<R, kModeBack><<<g, b, 0, ad->stream>>>(p, a);
-    if (theta)
-      k_adj_tails<R><<<1, kTailThreads, 0, ad->stream>>>(p, (const R *)ad->tail, npair,
-                                                        ad->g_sc);
+    if (theta) {
+      k_adj_tails<R><<<kTailBlocks, kTailThreads, 0, ad->stream>>>(p, (const R *)ad->tail,
+                                                                   npair, ad->tail_part);
+      k_adj_tails_fin<<<1, 32 * kAdjTypePairs, 0, ad->stream>>>(p, ad->tail_part, ad->g_sc);
+    }
   } else {
     k_adj_tiles<R, kModeHist><<<g, b, 0, ad->stream>>>(p, a);
   }
@@ -875,6 +900,7 @@ int bromoc_adj_create(bromoc_ctx *proto, int32_t capacity, int32_t precision,
   }
   if (!rc) rc = aalloc(ad, &ad->g_ep, 3 * (size_t)std::max(pk->cnt, 1));
   if (!rc) rc = aalloc(ad, &ad->g_sc, 3 * (size_t)pk->ntc);
+  if (!rc) rc = aalloc(ad, &ad->tail_part, (size_t)kTailBlocks * kAdjTypePairs);
   if (rc) {
     const std::string msg = ad->err;
     bromoc_adj_destroy(ad);

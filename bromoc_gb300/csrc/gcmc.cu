@@ -1661,7 +1661,7 @@ __device__ __forceinline__ int count_one(const KP &p, int i, int *nat) {
 // DevState::count_acc; the last block to finish (a ticket after a fence)
 // publishes nat, adds it to ntotat and clears the scratch for the next
 // launch.  Integer sums: exact in any order.
-constexpr int kCountThreads = 128;
+constexpr int kCountThreads = 32;
 template <bool FF>
 __global__ void __launch_bounds__(kCountThreads) k_count_grid(KP p) {
   __shared__ int nat[kMaxBuffers];

@@ -1822,13 +1822,12 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   KP &p = ctx->kp;
   if (ngcmc < 0 || cycle < 1) return set_err(ctx, BROMOC_E_ARG, "grand: bad ngcmc or cycle");
   if (p.nbuffer < 1) return set_err(ctx, BROMOC_E_STATE, "grand: no buffers");
-  if (p.mm.on && (terms & BROMOC_M_MMIJ))
-    return set_err(ctx, BROMOC_E_STATE,
-                   "grand: the MMIJ reaction field is not built into GRAND (INTERACT and "
-                   "METROPOLIS have it)");
+  // with the MMIJ reaction field the attempts run one after another
+  // through INTERACT (launch_grand_seq), on the FP64 arrays
+  const bool seq = p.mm.on && (terms & BROMOC_M_MMIJ);
   // FP32 mode: GRAND works on the float-float records (the current
   // positions while BD runs), FP64 mode on the FP64 arrays
-  const bool ff = ctx->precision == BROMOC_FP32;
+  const bool ff = ctx->precision == BROMOC_FP32 && !seq;
   if ((rc = ff ? ensure_ff(ctx) : ensure_dbl(ctx))) return rc;
   if (ngcmc > 0) {
     if (ff)
@@ -1875,10 +1874,15 @@ int bromoc_gpu_grand(bromoc_ctx *ctx, uint32_t terms, int32_t ngcmc, uint64_t se
   if (ngcmc > 0) {
     KTimer *tg = next_timer(ctx, BROMOC_K_GRAND);
     if (tg) cudaEventRecord(tg->a, ctx->stream);
-    CU(launch_grand(p, ntot_ub(ctx), ctx->ipart_slots, terms, seed, cycle, ngcmc, ff ? 1 : 0,
-                    ctx->stream));
+    if (seq) {
+      ctx->launches += launch_grand_seq(p, ntot_ub(ctx), terms, seed, cycle, ngcmc,
+                                        ctx->d_dener, ctx->stream);
+    } else {
+      CU(launch_grand(p, ntot_ub(ctx), ctx->ipart_slots, terms, seed, cycle, ngcmc, ff ? 1 : 0,
+                      ctx->stream));
+      ctx->launches += 1;
+    }
     if (tg) cudaEventRecord(tg->b, ctx->stream);
-    ctx->launches += 1;
     ctx->attempts_total += ngcmc;
   }
   CU(cudaGetLastError());

@@ -287,13 +287,20 @@ __device__ double interact_total(const KP &p, const Trial &tr, int nblk, double 
   return tr.e_single + tot[0];
 }
 
-// INTERACT entry: the host wrote the trial; one warp fills its single part.
+// INTERACT entry: the trial is written; one warp fills its single part.
+// qalert < 0: a deletion trial counts its warnings, an insertion none
+// (grand.f90:48,86).  An invalid trial gets no terms.
 __global__ void __launch_bounds__(32) k_interact_prep(KP p, uint32_t mask, int qalert) {
   __shared__ Trial s;
   if (threadIdx.x == 0) s = *p.trial;
   __syncwarp();
   Trial t = s;
-  trial_single_warp(p, t, mask, qalert);
+  if (!t.valid) {
+    t.e_single = t.srfe = t.reff = 0.0;
+    t.rf_in = 0;
+  } else {
+    trial_single_warp(p, t, mask, qalert < 0 ? !t.insert : qalert);
+  }
   if (threadIdx.x == 0) *p.trial = t;
 }
 
@@ -900,9 +907,11 @@ struct Draws {
 // The random part of one attempt's proposal (grand.f90:42-86): insertion
 // or deletion, the buffer, for an insertion its point by rejection sampling
 // inside the buffer (insert.f90), for a deletion the uniform its rank is
-// drawn from (find.f90).  None depends on the state.
+// drawn from (find.f90).  None depends on the state.  S: the buffer
+// parameters (nbuf, and 1-based avnum, ibfftyp, lzmin, lzmax, rmin, rmax).
+template <class S>
 __device__ void propose_draws(const KP &p, uint64_t seed, uint64_t cycle, uint32_t attempt,
-                              const GrandState &g, Trial &t, double &u_rank) {
+                              const S &g, Trial &t, double &u_rank) {
   t = Trial{};
   Draws d{seed, cycle, attempt};
   const int nbuf = g.nbuf;
@@ -1177,8 +1186,10 @@ __device__ void round_sums(const KP &p, int na, GrandState &g) {
 }
 
 // Im-Roux acceptance probability of trial tr with total ΔE de in the
-// current state (grand.f90:88-116).
-__device__ double accept_rate(const KP &p, const GrandState &g, const Trial &tr, double de,
+// current state (grand.f90:88-116).  S: the counts (0-based nat, ntotat)
+// and the 1-based buffer parameters (avnum, mu, kbb, qbias).
+template <class S>
+__device__ double accept_rate(const KP &p, const S &g, const Trial &tr, double de,
                               uint64_t cycle) {
   const int ib = tr.ib, b = ib - 1;
   const int nat = g.nat[b];
@@ -1610,6 +1621,160 @@ cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mas
                   (void *)&ffpos};
   return cudaLaunchCooperativeKernel((const void *)k_grand, dim3(grid), dim3(kGrandThreads),
                                      args, 0, stream);
+}
+
+// ---------------------------------------------------------------------------
+// GRAND one attempt after another (grand.f90:19-121, insert.f90, find.f90
+// as the reference runs them), for systems with a ΔE term the round kernel
+// does not form: the MMIJ reaction field, which every ion feels through the
+// basis coefficients.  Per attempt, in stream order:
+//   k_gseq_propose  one block: the draws (propose_draws), a deletion's
+//                   target by a block scan of the buffer tags in slot
+//                   order; writes the trial;
+//   INTERACT        launch_interact with its MMIJ term, a deletion trial
+//                   counting its warnings;
+//   k_gseq_accept   one thread: the acceptance draw and rule (accept_rate),
+//                   the move on the FP64 arrays, prob(ib, nat(ib)) += 1.
+// The draws and the rule are k_grand's, so on a system both can run the two
+// make the same moves.
+// ---------------------------------------------------------------------------
+// The context's buffer parameters and counts as propose_draws / accept_rate
+// read them.
+struct KPBuf {
+  int nbuf;
+  const double *avnum, *mu, *kbb, *lzmin, *lzmax, *rmin, *rmax;
+  const int *ibfftyp;
+  const uint8_t *qbias;
+  const int *nat, *ntotat;
+};
+__device__ __forceinline__ KPBuf kp_buf(const KP &p) {
+  return KPBuf{p.nbuffer, p.avnum, p.mu, p.kbb, p.lzmin, p.lzmax, p.rmin, p.rmax,
+               p.ibfftyp, p.qbufferbias, p.st->nat, p.st->ntotat};
+}
+
+constexpr int kGseqThreads = 256;
+
+__global__ void __launch_bounds__(kGseqThreads)
+    k_gseq_propose(KP p, uint64_t seed, uint64_t cycle, int a) {
+  __shared__ Trial s_tr;
+  __shared__ int s_rank, s_found, s_cnt[kGseqThreads / 32];
+  const int tid = threadIdx.x;
+  const int ntot = p.st->ntot;
+  if (tid == 0) {
+    Trial t;
+    double u = 0.0;
+    propose_draws(p, seed, cycle, (uint32_t)a, kp_buf(p), t, u);
+    t.ntot = ntot;
+    t.chg = -1;
+    s_rank = 0;
+    if (t.insert) {
+      t.j = ntot + 1;
+    } else {
+      const int ib = t.ib;
+      const int natb = ib <= p.nbuffer ? p.st->nat[ib - 1] : 0;
+      const int ip = (int)((double)natb * u) + 1;
+      t.valid = 0;
+      if (ib <= p.nbuffer && ip <= natb) {
+        t.itype = p.ibfftyp[ib];
+        t.valid = 1;
+        s_rank = ip;
+      }
+    }
+    s_tr = t;
+    s_found = -1;
+  }
+  __syncthreads();
+  if (s_rank > 0) {  // find.f90: the s_rank-th ion of the buffer in slot order
+    const int ib = s_tr.ib, rank = s_rank;
+    int before = 0;
+    for (int c0 = p.nsites + p.nfix; c0 < ntot && before < rank; c0 += kGseqThreads) {
+      const int i = c0 + tid;
+      const bool m = i < ntot && p.ibuffer[i] == ib;
+      const unsigned bal = __ballot_sync(0xffffffffu, m);
+      if ((tid & 31) == 0) s_cnt[tid >> 5] = __popc(bal);
+      __syncthreads();
+      int wb = 0, all = 0;
+      for (int w = 0; w < kGseqThreads / 32; ++w) {
+        if (w < (tid >> 5)) wb += s_cnt[w];
+        all += s_cnt[w];
+      }
+      if (m && before + wb + __popc(bal & ((1u << (tid & 31)) - 1u)) + 1 == rank) s_found = i;
+      before += all;  // the same on every thread: the loop ends together
+      __syncthreads();
+    }
+    if (tid == 0) {
+      const int k = s_found;
+      if (k < 0 || guard_bad(p.st, k, ntot, 11)) {
+        s_tr.valid = 0;
+        atomicOr(&p.st->err, kErrFind);
+      } else {
+        s_tr.j = k + 1;
+        s_tr.x = p.x[k];
+        s_tr.y = p.y[k];
+        s_tr.z = p.z[k];
+      }
+    }
+  }
+  __syncthreads();
+  if (tid == 0) *p.trial = s_tr;
+}
+
+__global__ void k_gseq_accept(KP p, uint64_t seed, uint64_t cycle, int a, const double *de_dev) {
+  if (threadIdx.x != 0) return;
+  DevState *st = p.st;
+  const Trial t = *p.trial;
+  const int nb = p.nbuffer;
+  if (t.valid && !guard_bad(st, t.ib - 1, nb, 21)) {
+    const double de = *de_dev;
+    const int ib = t.ib, b = ib - 1, nat = st->nat[b], ntot = st->ntot;
+    const double rate = accept_rate(p, kp_buf(p), t, de, cycle);
+    if (gcmc_uniform(seed, cycle, (uint32_t)a, (uint32_t)t.draw) <= rate) {
+      if (t.insert) {
+        if (ntot + 1 > p.cap) {
+          atomicOr(&st->err, kErrCapacity);
+        } else {
+          p.x[ntot] = t.x;
+          p.y[ntot] = t.y;
+          p.z[ntot] = t.z;
+          p.typei[ntot] = t.z < p.cz ? -t.itype : t.itype;
+          p.ibuffer[ntot] = ib;
+          st->nat[b] = nat + 1;
+          st->ninsert[b] += 1;
+          st->dener_sum += de;
+          st->ntot = ntot + 1;
+        }
+      } else if (!guard_bad(st, t.j - 1, ntot, 23)) {
+        const int iat = t.j - 1, last = ntot - 1;
+        p.x[iat] = p.x[last];
+        p.y[iat] = p.y[last];
+        p.z[iat] = p.z[last];
+        p.typei[iat] = p.typei[last];
+        p.ibuffer[iat] = p.ibuffer[last];
+        st->nat[b] = nat - 1;
+        st->nremove[b] += 1;
+        st->dener_sum -= de;
+        st->ntot = ntot - 1;
+      }
+    }
+  }
+  for (int b = 0; b < nb; ++b) {  // grand.f90:117-119
+    const int n = st->nat[b];
+    if (!guard_bad(st, n, p.cap + 1, 25)) p.prob[(size_t)b * (p.cap + 1) + n] += 1;
+  }
+}
+
+int launch_grand_seq(const KP &p, int ntot_ub, uint32_t mask, uint64_t seed, uint64_t cycle,
+                     int ngcmc, double *de_dev, cudaStream_t stream) {
+  cudaMemsetAsync(&p.st->dener_sum, 0, sizeof(double), stream);
+  int nl = 0;
+  for (int a = 0; a < ngcmc; ++a) {
+    const int ub = std::min(p.cap, ntot_ub + a);  // each attempt adds at most one ion
+    k_gseq_propose<<<1, kGseqThreads, 0, stream>>>(p, seed, cycle, a);
+    launch_interact(p, ub, mask, -1, de_dev, stream);
+    k_gseq_accept<<<1, 32, 0, stream>>>(p, seed, cycle, a, de_dev);
+    nl += 5 + ((mask & 16u) && p.qrfpar ? 1 : 0) + ((mask & 64u) && p.mm.on ? 5 : 0);
+  }
+  return nl;
 }
 
 // ---------------------------------------------------------------------------

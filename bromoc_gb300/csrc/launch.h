@@ -177,6 +177,11 @@ int launch_metropolis(const KP &p, int ntot, uint32_t mask, int nmcm, double mcm
 
 void launch_interact(const KP &p, int ntot_ub, uint32_t mask, int qalert,
                      double *dener_dev, cudaStream_t stream);
+// gcmc.cu: GRAND one attempt after another (systems with the MMIJ reaction
+// field): proposal, INTERACT into *de_dev, acceptance, per attempt; the
+// FP64 arrays move; returns the launches
+int launch_grand_seq(const KP &p, int ntot_ub, uint32_t mask, uint64_t seed, uint64_t cycle,
+                     int ngcmc, double *de_dev, cudaStream_t stream);
 // GRAND: ngcmc attempts in one cooperative launch (gcmc.cu)
 // ffpos: FP32 mode, positions in the float-float records (pk1, pk2)
 cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,

@@ -1,7 +1,7 @@
 """The MMIJ reaction field on the GPU against the oracle (rect_rf1/rf0,
 sphe_rf1/rf0): ENERGY and forces run in test_gpu_parity's family sweep;
 here INTERACT of present ions, insertion trials and sites, BD steps,
-METROPOLIS, the mask and GRAND's refusal."""
+METROPOLIS, GRAND and the mask."""
 import numpy as np
 import pytest
 
@@ -66,20 +66,72 @@ def test_fp32_bd_steps_skip_the_fused_loop(gpu_lib, oracle_mod):
     assert np.abs(pg - po).max() <= 1e-5
 
 
-def test_mask_and_grand(gpu_lib, oracle_mod):
+def test_mask(gpu_lib, oracle_mod):
     spec = systems.mmij("rect", precision=abi.FP64)
     g, o = _engines(spec, gpu_lib, oracle_mod)
     off = abi.M_ALL & ~abi.M_MMIJ
     tg = g.energy(off)[0]
     to = o.energy(off)[0]
     assert tg["egsbpb"] == 0.0 and abs(tg["ener"] - to["ener"]) <= 1e-10 * abs(to["ener"])
-    spec_b = systems.mmij("rect", precision=abi.FP64, buffers=True)
-    gb = gpu_lib.create(CAP, abi.FP64)
-    spec_b.push(gb)
-    with pytest.raises(abi.BromocError) as e:
-        gb.grand(2, seed=1, cycle=1)
-    assert e.value.code == abi.E_STATE and "MMIJ" in str(e.value)
-    gb.grand(2, seed=1, cycle=1, terms=abi.M_ALL & ~abi.M_MMIJ)  # without the term it runs
+
+
+def _compare_gcmc(g, o, atol):
+    ng, nig, nrg, prg = g.get_buffers()
+    no, nio, nro, pro = o.get_buffers()
+    np.testing.assert_array_equal(ng, no)
+    np.testing.assert_array_equal(nig, nio)
+    np.testing.assert_array_equal(nrg, nro)
+    np.testing.assert_array_equal(prg, pro)
+    assert nig.sum() + nrg.sum() > 0
+    xg, yg, zg, tg, ibg = g.get_particles()
+    xo, yo, zo, to, ibo = o.get_particles()
+    np.testing.assert_array_equal(tg, to)
+    np.testing.assert_array_equal(ibg, ibo)
+    np.testing.assert_allclose(np.stack([xg, yg, zg]), np.stack([xo, yo, zo]), atol=atol)
+
+
+@pytest.mark.parametrize("shape", ["rect", "sphere"])
+@pytest.mark.parametrize("prec", [abi.FP64, abi.FP32])
+def test_grand_with_the_reaction_field(gpu_lib, oracle_mod, shape, prec):
+    """GRAND with the MMIJ term (the attempts one after another through
+    INTERACT): the oracle's insertions and deletions, counters and
+    histogram exact, its energy sums, the same particles after BD steps and
+    COUNT between the calls."""
+    spec = systems.mmij(shape, precision=prec, buffers=True)
+    g, o = _engines(spec, gpu_lib, oracle_mod)
+    # FP32 BD steps between the calls leave the positions ~1e-6 A from the
+    # oracle's, and the energy sums follow
+    tol = 1e-8 if prec == abi.FP64 else 1e-5
+    for cyc in range(1, 9):
+        dg = g.grand(6, 4242, cyc)
+        do = o.grand(6, 4242, cyc)
+        assert abs(dg - do) <= tol * max(1.0, abs(do)), (cyc, dg, do)
+        g.bd_steps(2, seed=7, step0=2 * cyc, energies=False)
+        o.bd_steps(2, seed=7, step0=2 * cyc)
+        g.count()
+        o.count()
+    _compare_gcmc(g, o, 1e-7 if prec == abi.FP64 else 1e-5)
+
+
+def test_grand_one_by_one_makes_the_round_kernels_moves(gpu_lib):
+    """With a zero MMIJ matrix the term vanishes: GRAND one attempt after
+    another (MMIJ on) and the round kernel (MMIJ masked out) make the same
+    moves from the same draws."""
+    spec = systems.mmij("rect", precision=abi.FP64, buffers=True)
+    spec.mmij = dict(spec.mmij, mmij=np.zeros_like(spec.mmij["mmij"]))
+    a = gpu_lib.create(CAP, abi.FP64)
+    b = gpu_lib.create(CAP, abi.FP64)
+    spec.push(a)
+    spec.push(b)
+    for cyc in range(1, 9):
+        da = a.grand(6, 99, cyc)
+        db = b.grand(6, 99, cyc, terms=abi.M_ALL & ~abi.M_MMIJ)
+        assert abs(da - db) <= 1e-9 * max(1.0, abs(db)), (cyc, da, db)
+        a.bd_steps(2, seed=3, step0=2 * cyc, energies=False)
+        b.bd_steps(2, seed=3, step0=2 * cyc, energies=False)
+        a.count()
+        b.count()
+    _compare_gcmc(a, b, 0.0)
 
 
 def test_metropolis_with_the_reaction_field(gpu_lib, oracle_mod):

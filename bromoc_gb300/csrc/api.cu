@@ -1004,7 +1004,7 @@ int bromoc_gpu_set_sites(bromoc_ctx *ctx, const bromoc_sites *s) {
       dfree(ctx, a);
     p.isp_ion = p.isp_site = p.isp_dids = p.isp_seed = nullptr;
     p.isp_tcap = 0;
-    const size_t S = (s->nsites + 31) / 32, cap = p.cap;
+    const size_t S = (s->nsites + kIsSiteTile - 1) / kIsSiteTile, cap = p.cap;
     const int T = (int)((cap + 31) / 32);
     rc = dalloc(ctx, &p.isp_ion, S * 3 * cap);
     if (!rc) rc = dalloc(ctx, &p.isp_dids, S * 6 * cap);

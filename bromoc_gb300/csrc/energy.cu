@@ -445,10 +445,13 @@ __global__ void __launch_bounds__(kPairThreads)
   }
 }
 
-// Ion-site pairs as tiles: one warp per (ion tile of 32, site tile of 32),
-// lane l holds ion 32 t + l and meets site (l + k) mod 32 at step k, so in
-// each step the lanes touch distinct site slots and the site sums need no
-// atomics.  The same per-pair law, energies and forces as k_ionsite32 /
+// Ion-site pairs as tiles: one warp per (ion tile of 32, site tile of
+// kIsSiteTile), lane l holds ion 32 t + l and meets the tile's sites one
+// after another (the same site on every lane: one broadcast read), keeping
+// its term on each site in registers; each site's sum over the tile's ions
+// is a fixed shuffle tree (no atomics).  Small site tiles give the warps of
+// a few thousand ions against ~100 sites enough work items to fill the
+// SMs.  The same per-pair law, energies and forces as k_ionsite32 /
 // k_siteforce32 (the pair's r^2 and de are the same numbers on both sides);
 // the PROXDIFF record keeps, per site tile, the smallest dist - mindist over
 // sites j >= 1 (ties: the smaller j), and the first site's own record, which
@@ -458,8 +461,8 @@ constexpr int kIsWarps = 4;
 
 __global__ void __launch_bounds__(32 * kIsWarps)
     k_ionsite_tiles(KP p, int qforces, int slot0, int S, int nwork) {
-  __shared__ float4 sh[kIsWarps][32], sl[kIsWarps][32];
-  __shared__ float sf[kIsWarps][3][32];
+  constexpr int W = kIsSiteTile;
+  __shared__ float4 sh[kIsWarps][W], sl[kIsWarps][W];
   __shared__ float red[kIsWarps * 4];
   __shared__ float tot[4];
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
@@ -469,11 +472,12 @@ __global__ void __launch_bounds__(32 * kIsWarps)
   int err = 0;
   if (wi < nwork) {  // warp-uniform
     const int t = wi / S, s = wi - t * S;
-    const int j0 = 32 * s, jl = j0 + lane;
-    const bool jv = jl < ns;
-    sh[w][lane] = jv ? p.pk1[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
-    sl[w][lane] = jv ? p.pk2[jl] : make_float4(0.f, 0.f, 0.f, 0.f);
-    sf[w][0][lane] = sf[w][1][lane] = sf[w][2][lane] = 0.f;
+    const int j0 = W * s, nj = min(W, ns - j0);
+    if (lane < W) {
+      const bool jv = lane < nj;
+      sh[w][lane] = jv ? p.pk1[j0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+      sl[w][lane] = jv ? p.pk2[j0 + lane] : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
     const int i = ns + 32 * t + lane;
     const bool iv = i < ntot;
     const bool mobile = i >= ns + p.nfix;
@@ -483,25 +487,24 @@ __global__ void __launch_bounds__(32 * kIsWarps)
       tl = p.pk2[i];
     }
     const int row = (__float_as_int(th.w) & 0xffff) * p.nttyp;
-    const int nj = min(32, ns - j0);
     float f[3] = {0.f, 0.f, 0.f};
+    float gs[3] = {0.f, 0.f, 0.f};  // lane k: site k's sum over the tile's ions
     float bv = 3.4e38f, bd = 0.f, bx = 0.f, by = 0.f, bz = 0.f;  // best j >= 1
     int bj = 1 << 30;
     float seed[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
     __syncwarp();
-#pragma unroll 4
-    for (int k = 0; k < 32; ++k) {
-      const int m = (lane + k) & 31;
-      float g0 = 0.f, g1 = 0.f, g2 = 0.f;
-      if (iv && m < nj) {
-        const float4 h = sh[w][m], l = sl[w][m];
+#pragma unroll 1
+    for (int k = 0; k < nj; ++k) {  // warp-uniform
+      float g[3] = {0.f, 0.f, 0.f};  // this lane's term on site k
+      if (iv) {
+        const float4 h = sh[w][k], l = sl[w][k];  // the same site on every lane
         const int is = p.pidx[row + (__float_as_int(h.w) & 0xffff)];
         const PairParamF &q = p.ppf[is];
         const float dx = ff_diff(th.x, tl.x, h.x, l.x), dy = ff_diff(th.y, tl.y, h.y, l.y),
                     dz = ff_diff(th.z, tl.z, h.z, l.z);
         const float r2 = fmaf(dx, dx, fmaf(dy, dy, dz * dz));
         const float de = law32(p, q, r2, 1.0f, e, err, [&] { return r2_ff64(th, tl, h, l); });
-        const int j = j0 + m;
+        const int j = j0 + k;
         if (p.qproxdiff && (q.flags & kEfp) && r2 >= q.dm2lo && r2 <= q.dm2hi) {
           const float dist = sqrtf(r2);
           const float dm = dist - q.dmi;
@@ -528,16 +531,18 @@ __global__ void __launch_bounds__(32 * kIsWarps)
           f[2] = fmaf(de, dz, f[2]);
         }
         if (qforces && p.stfree[j]) {
-          g0 = -de * dx;
-          g1 = -de * dy;
-          g2 = -de * dz;
+          g[0] = -de * dx;
+          g[1] = -de * dy;
+          g[2] = -de * dz;
         }
       }
-      // slot m is this lane's alone in this step
-      sf[w][0][m] += g0;
-      sf[w][1][m] += g1;
-      sf[w][2][m] += g2;
-      __syncwarp();
+#pragma unroll
+      for (int c = 0; c < 3; ++c) {  // a fixed shuffle tree over the ions
+        float v = g[c];
+#pragma unroll
+        for (int x = 16; x > 0; x >>= 1) v += __shfl_xor_sync(0xffffffffu, v, x);
+        if (lane == k) gs[c] = v;
+      }
     }
     if (iv) {
       const size_t cap = p.cap;
@@ -557,11 +562,10 @@ __global__ void __launch_bounds__(32 * kIsWarps)
           for (int c = 0; c < 5; ++c) p.isp_seed[c * cap + i] = seed[c];
       }
     }
-    if (jl < ns) {
+    if (lane < nj) {
       float *o = p.isp_site + (size_t)t * 3 * ns;
-      o[jl] = sf[w][0][lane];
-      o[ns + jl] = sf[w][1][lane];
-      o[2 * ns + jl] = sf[w][2][lane];
+#pragma unroll
+      for (int c = 0; c < 3; ++c) o[c * ns + j0 + lane] = gs[c];
     }
   }
   if (err) atomicOr(&p.st->err, err);
@@ -645,7 +649,8 @@ __global__ void __launch_bounds__(256) k_ionsite_sites(KP p, int qforces, int T)
 }
 
 int ionsite_tile_blocks(const KP &p, int nub) {
-  const int S = (p.nsites + 31) / 32, T = (std::max(0, nub - p.nsites) + 31) / 32;
+  const int S = (p.nsites + kIsSiteTile - 1) / kIsSiteTile;
+  const int T = (std::max(0, nub - p.nsites) + 31) / 32;
   return (S * T + kIsWarps - 1) / kIsWarps;
 }
 
@@ -891,8 +896,8 @@ int launch_energy(const KP &p, const EnergyPlan &plan, uint32_t mask,
   if (nonbond && p.nsites > 0 && nub > p.nsites) {
     const int nion_ub = nub - p.nsites;
     const int nb = (nion_ub + kPairThreads - 1) / kPairThreads;
-    if (ionsite_tiled(p, plan.fp32, nub)) {  // FP32: 32 x 32 tiles
-      const int S = (p.nsites + 31) / 32, T = (nion_ub + 31) / 32;
+    if (ionsite_tiled(p, plan.fp32, nub)) {  // FP32: tiles of 32 ions x kIsSiteTile sites
+      const int S = (p.nsites + kIsSiteTile - 1) / kIsSiteTile, T = (nion_ub + 31) / 32;
       const int tb = ionsite_tile_blocks(p, nub);
       k_ionsite_tiles<<<tb, 32 * kIsWarps, 0, stream>>>(p, qforces, slot, S, S * T);
       k_ionsite_sum<<<(nion_ub + 255) / 256, 256, 0, stream>>>(p, qforces, S, T);

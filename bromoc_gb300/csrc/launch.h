@@ -25,6 +25,9 @@ struct EnergyPlan {
 // Tile pairs (I <= J) of the Newton-3 pair kernel, row-major: row I holds
 // J = I..T-1 and starts at offset I T - I (I - 1) / 2.
 constexpr int kN3MaxTiles = 256;  // up to 8192 ions; beyond, the chunked kernel
+// Sites per tile of the FP32 ion-site pair kernel: a warp's 32 ions meet
+// them one after another.
+constexpr int kIsSiteTile = 8;
 __host__ __device__ inline int n3_pairs(int T) { return T * (T + 1) / 2; }
 __host__ __device__ inline int n3_index(int T, int I, int J) {
   return I * T - I * (I - 1) / 2 + (J - I);

@@ -13,6 +13,8 @@ command lines):
   python -m bromoc_gb300.cases cells N     FP32 BD steps of N ions of 1 M KCl
                                            in a periodic cube, 20 A cutoff
                                            (the cell-list kernels), 3 steps
+  python -m bromoc_gb300.cases batch       the bench's replica batch (256 bulk
+                                           KCl replicas, 1.08 M ions): 3 BD steps
   python -m bromoc_gb300.cases adjoint N   the adjoint engine on N ions of 1 M
                                            KCl with tabulated laws: a 20-step
                                            forward (RDF deposit) and backward
@@ -102,9 +104,36 @@ def adjoint(n: int):
     adj.close()
 
 
+def batch(nrep: int = 256):
+    """256 bulk KCl replicas, N uniform in [200, 8000], sharing the pore maps:
+    3 tuned, graph-replayed BD steps (the bench's batch workload)."""
+    from .batch import Batch
+    spec = synth.pore(seed=3, nions=2000, maps=synth.pore_maps(seed=102), precision=abi.FP32,
+                      buffers=False)
+    counts, edges, parts = synth.batch_replicas(nrep=nrep)
+    systems = []
+    for L in edges:
+        sy = spec.system_struct()
+        sy.lx = sy.ly = sy.lz = float(L)
+        sy.cx = sy.cy = sy.cz = 0.0
+        systems.append(sy)
+    proto = _lib.create(2064, abi.FP32)
+    spec.push(proto)
+    b = Batch(proto, counts)
+    b.set_systems(systems)
+    for r, (x, y, z, t) in enumerate(parts):
+        b.set_particles(r, x, y, z, t)
+    seeds = np.arange(nrep, dtype=np.uint64) + 1234
+    for k in range(3):
+        b.bd_steps(1, seeds, k)
+    b.close()
+
+
 def main(argv):
     what = argv[1] if len(argv) > 1 else "loop"
-    if what == "adjoint":
+    if what == "batch":
+        batch()
+    elif what == "adjoint":
         adjoint(int(argv[2]) if len(argv) > 2 else 4096)
     elif what == "pairs":
         pairs(int(argv[2]) if len(argv) > 2 else 8000)

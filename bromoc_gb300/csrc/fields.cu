@@ -317,8 +317,24 @@ void launch_pack(const KP &p, int ntot_ub, bool to_records, cudaStream_t stream)
     k_unpack<<<nb, 128, 0, stream>>>(p);
 }
 
-// Replica batches: one warp per slot of the batch arrays; slots past their
-// replica's live count return at once.
+// Replica batches: one thread per slot of the batch arrays (one warp per
+// slot with a B-spline repulsion map); slots past their replica's live count
+// return at once.
+constexpr int kBatchFieldThreads = 128;
+__global__ void __launch_bounds__(kBatchFieldThreads)
+    k_batch_fields_t(const __grid_constant__ KP p, const int *rep_of, const RepDev *rep,
+                     float4 *pe, int nslots, uint32_t mask, int qforces) {
+  __shared__ AxisF ax[12];
+  stage_axes(p, ax);
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= nslots) return;
+  const RepDev &R = rep[rep_of[i]];
+  if (i - R.off >= R.n) return;
+  float eo[4] = {0.0f, 0.0f, 0.0f, 0.0f};
+  fields_one_thread(p, i, mask, qforces, eo, ax);
+  pe[i] = make_float4(eo[0], eo[1], eo[2], eo[3]);
+}
+
 __global__ void __launch_bounds__(32 * kFieldWarps)
     k_batch_fields(const __grid_constant__ KP p, const int *rep_of, const RepDev *rep,
                    float4 *pe, int nslots, uint32_t mask, int qforces) {
@@ -335,10 +351,16 @@ __global__ void __launch_bounds__(32 * kFieldWarps)
 
 void launch_batch_fields(const KP &p, const int *rep_of, const RepDev *rep, float4 *pe,
                          int nslots, uint32_t mask, int qforces, cudaStream_t stream) {
-  const int nb = (nslots + kFieldWarps - 1) / kFieldWarps;
-  if (nb > 0)
+  if (nslots <= 0) return;
+  if ((mask & 8u) && p.qphiv && !p.qtrln) {
+    const int nb = (nslots + kFieldWarps - 1) / kFieldWarps;
     k_batch_fields<<<nb, 32 * kFieldWarps, 0, stream>>>(p, rep_of, rep, pe, nslots, mask,
                                                          qforces);
+  } else {
+    const int nb = (nslots + kBatchFieldThreads - 1) / kBatchFieldThreads;
+    k_batch_fields_t<<<nb, kBatchFieldThreads, 0, stream>>>(p, rep_of, rep, pe, nslots, mask,
+                                                            qforces);
+  }
 }
 
 int fields_blocks(int ntot_ub) { return (ntot_ub + kFieldWarps - 1) / kFieldWarps; }

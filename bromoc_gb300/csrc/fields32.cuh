@@ -258,4 +258,169 @@ __device__ __forceinline__ void fields_one_f32(const KP &p, int i, bool site, bo
   }
 }
 
+// ---------------------------------------------------------------------------
+// The same terms with one thread per particle, for ions that are neither
+// sites nor fixed, with a trilinear repulsion map (replica batches, where a
+// warp per slot leaves most lanes idle in the cell search and the sums).  The thread does every lane's
+// arithmetic of fields_one_f32 with the same expressions, and forms each
+// shuffle-tree sum in the tree's order -- IEEE addition commutes, so every
+// lane of an xor butterfly holds the same fixed-order sum -- so the results
+// are the warp version's bit for bit (a batch replica's step equals a single
+// context's).
+// ---------------------------------------------------------------------------
+// seg8_sum's value: levels xor 4, 2, 1
+__device__ __forceinline__ float tree8(const float v[8]) {
+  const float w0 = v[0] + v[4], w1 = v[1] + v[5], w2 = v[2] + v[6], w3 = v[3] + v[7];
+  return (w0 + w2) + (w1 + w3);
+}
+__device__ __forceinline__ void fields_one_thread(const KP &p, int i, uint32_t mask, int qforces,
+                                                  float eo[4], const AxisF *ax) {
+  const float4 h4 = p.pk1[i], l4 = p.pk2[i];
+  const float charge = p.pk3[i].y;
+  const int code = __float_as_int(h4.w);
+  const int itype2 = (code & 0xffff) + 1;
+  const int mobile = (code >> 16) & 1;
+  const int iontype = abs(p.typei[i]);
+  const bool qf = qforces != 0;
+  // the cells of lanes 0..11
+  int cix[12], cin[12];
+  float cfr[12];
+#pragma unroll
+  for (int k = 0; k < 12; ++k) {
+    const AxisF &A = ax[k];
+    const int a = k % 3;
+    const float ph = a == 0 ? h4.x : (a == 1 ? h4.y : h4.z);
+    const float pl = a == 0 ? l4.x : (a == 1 ? l4.y : l4.z);
+    cfr[k] = ff_cell(A, ph, pl, k >= 9, cix[k]);
+    cin[k] = k < 9 && ff_inside(A, ph, pl);
+  }
+  const int in1 = cin[0] & cin[1] & cin[2], in2 = cin[3] & cin[4] & cin[5],
+            in3 = cin[6] & cin[7] & cin[8];
+  const bool do_phix = (mask & 4u) && p.qphix && in1;
+  const bool phiv_ok = (mask & 8u) && p.qphiv && in2;
+  const bool do_rf = (mask & 16u) && p.qrfpar && in3;
+  const size_t vifir = phiv_ok ? phiv_ifir(p, i, iontype) : 0;
+  const float esvdw = phiv_ok ? p.esvdw_f[itype2] : 0.0f;
+  // pass A: group g = 0 static field, 1 repulsion, 2 gsrfen, 3 greff; corner c
+  float se[4], sf0[4], sf1[4], sf2[4], ssum[4];
+#pragma unroll
+  for (int g = 0; g < 4; ++g) {
+    const int src = 3 * (g < 2 ? g : 2);
+    const int ix = cix[src], iy = cix[src + 1], iz = cix[src + 2];
+    const float fx = cfr[src], fy = cfr[src + 1], fz = cfr[src + 2];
+    float le[8], lf0[8], lf1[8], lf2[8], ls[8], gs[8];
+    bool act[8];
+    float val[8], vf[8];
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int ca = (c >> 2) & 1, cb = (c >> 1) & 1, cc = c & 1;
+      val[c] = 0.0f;
+      vf[c] = 0.0f;
+      ls[c] = 0.0f;
+      gs[c] = 0.0f;
+      act[c] = false;
+      if (g == 0 && do_phix) {
+        const Grid3 &gg = p.g1;
+        const size_t node = (size_t)(ix + ca) * gg.ncly * gg.nclz + (size_t)(iy + cb) * gg.nclz +
+                            iz + cc;
+        val[c] = __ldg(p.phix + node) * (p.f.celec * charge);
+        vf[c] = val[c] * p.f.ax[0].idc;
+        act[c] = true;
+      } else if (g == 1 && phiv_ok && p.qtrln) {
+        const Grid3 &gg = p.g2;
+        const size_t node = vifir + (size_t)(ix + ca) * gg.ncly * gg.nclz +
+                            (size_t)(iy + cb) * gg.nclz + iz + cc;
+        ls[c] = (float)__ldg(p.phiv + node);
+        val[c] = ls[c] * esvdw;
+        vf[c] = val[c] * p.f.ax[3].idc;
+        act[c] = true;
+      } else if (g >= 2 && do_rf) {
+        const Grid3 &gg = p.g3;
+        const size_t node = rfpar_ifir(p, iontype) + (size_t)(ix + ca) * gg.ncly * gg.nclz +
+                            (size_t)(iy + cb) * gg.nclz + iz + cc;
+        gs[c] = __ldg(p.gsrfen + node);
+        val[c] = g == 2 ? gs[c] : p.f.sqrfac * __ldg(p.greff + node);
+        vf[c] = -val[c] * p.f.ax[6].idc;
+        act[c] = true;
+      }
+    }
+#pragma unroll
+    for (int c = 0; c < 8; ++c) {
+      const int ca = (c >> 2) & 1, cb = (c >> 1) & 1, cc = c & 1;
+      const float dxa = fx - (float)ca, dyb = fy - (float)cb, dzc = fz - (float)cc;
+      const float ai = 1.0f - fabsf(dxa), bi = 1.0f - fabsf(dyb), ci = 1.0f - fabsf(dzc);
+      const float as = dxa >= 0.0f ? 1.0f : -1.0f, bs = dyb >= 0.0f ? 1.0f : -1.0f,
+                  cs = dzc >= 0.0f ? 1.0f : -1.0f;
+      bool a = act[c];
+      const float gs_c0 = gs[c & ~1];  // rfpar.f90:121
+      if (g >= 2 && a && !(gs_c0 != 0.0f && (cc == 0 || gs[c] != 0.0f))) a = false;
+      le[c] = lf0[c] = lf1[c] = lf2[c] = 0.0f;
+      if (a) {
+        le[c] = ai * bi * ci * val[c];
+        if (qf) {
+          const float lo = (float)kRsmall, hi = 1.0f - (float)kRsmall;
+          if (ai < hi && ai > lo) lf0[c] = as * bi * ci * vf[c];
+          if (bi < hi && bi > lo) lf1[c] = bs * ai * ci * vf[c];
+          if (ci < hi && ci > lo) lf2[c] = cs * ai * bi * vf[c];
+        }
+      }
+    }
+    se[g] = tree8(le);
+    sf0[g] = tree8(lf0);
+    sf1[g] = tree8(lf1);
+    sf2[g] = tree8(lf2);
+    ssum[g] = tree8(ls);
+  }
+  float ff0 = 0.0f, ff1 = 0.0f, ff2 = 0.0f;
+  if ((mask & 2u) && p.qmemb) {  // membrane in FP64 (an option off the hot path)
+    double f[3] = {0.0, 0.0, 0.0}, em = 0.0;
+    if (membrane_one(p, itype2, p.cg[iontype], (double)h4.x + (double)l4.x,
+                     (double)h4.y + (double)l4.y, (double)h4.z + (double)l4.z, qf, false, em,
+                     f))
+      atomicAdd(&p.warn[itype2], 1);
+    eo[0] = (float)em;
+    ff0 = (float)f[0];
+    ff1 = (float)f[1];
+    ff2 = (float)f[2];
+  }
+  if (do_phix) {
+    eo[1] = se[0];
+    ff0 += sf0[0];
+    ff1 += sf1[0];
+    ff2 += sf2[0];
+  }
+  if (phiv_ok) {  // trilinear (the caller keeps B-spline maps on the warp version)
+    eo[2] = se[1];
+    ff0 += sf0[1];
+    ff1 += sf1[1];
+    ff2 += sf2[1];
+    if (ssum[1] >= p.f.thold8) atomicAdd(&p.warn[itype2], 1);
+  }
+  const float srfe = se[2], reff = se[3];
+  if ((mask & 16u) && p.qrfpar) {
+    p.rfd[2 * (size_t)i] = do_rf ? make_float4(sf0[2], sf1[2], sf2[2], 0.0f)
+                                 : make_float4(0.f, 0.f, 0.f, 0.f);
+    p.rfd[2 * (size_t)i + 1] = do_rf ? make_float4(sf0[3], sf1[3], sf2[3], 0.0f)
+                                     : make_float4(0.f, 0.f, 0.f, 0.f);
+    if (do_rf) {  // self term, rfpar.f90:161-176
+      const float aux = p.f.celec * charge * charge * srfe;
+      eo[3] = 0.5f * aux * srfe;
+      if (qf) {
+        ff0 -= aux * sf0[2];
+        ff1 -= aux * sf1[2];
+        ff2 -= aux * sf2[2];
+      }
+    }
+  }
+  if (p.qproxdiff)
+    for (int m = 0; m < 5; ++m) p.dids[5 * (size_t)i + m] = 0.0;
+  p.ffield_f[i] = ff0;
+  p.ffield_f[p.cap + i] = ff1;
+  p.ffield_f[2 * p.cap + i] = ff2;
+  p.pk2[i].w = do_rf ? srfe : 0.0f;
+  const int rfl = (do_rf ? 1 : 0) | (mobile << 1) | ((do_rf && mobile) ? 4 : 0) |
+                  ((do_rf && srfe != 0.0f) ? 8 : 0);
+  p.pk3[i] = make_float4(do_rf ? reff : 0.0f, charge, __int_as_float(rfl), 0.0f);
+}
+
 }  // namespace bgpu

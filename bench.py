@@ -295,10 +295,10 @@ def pair_scaling(sh, peak_fp32, sizes=(2000, 4000, 8000), reps=10):
     return out
 
 
-C1_STEPS = 2000
+BULK_STEPS = 2000
 
 
-def c1_measure(sh, steps=C1_STEPS):
+def bulk_measure(sh, steps=BULK_STEPS):
     """The bulk configuration: 130 K+ and 130 Cl- in a 60 A cube, FP64,
     dt 0.02 ps; reference semantics (hard walls, all pairs) and the
     extension mode (periodic, 20 A cutoff).  GPU: `steps` BD steps per call
@@ -341,10 +341,10 @@ def c1_measure(sh, steps=C1_STEPS):
     return out
 
 
-C3_STEPS = 200
+SSDNA_STEPS = 200
 
 
-def c3_measure(sh, steps=C3_STEPS):
+def ssdna_measure(sh, steps=SSDNA_STEPS):
     """The ssDNA configuration: 40 nt x 3 sites (free, with their bonded and
     Go-like terms) in the 120x120x180 pore maps with ~5000 K+/Cl-, FP32
     pairs, dynamics0 / dynamics0nuc.  GPU: `steps` BD steps (ENERGY forces +
@@ -452,7 +452,7 @@ def adjoint_measure(sh):
 
 
 def adjoint_fd_check(sh, spec, hist_args, steps=None, hs=(3e-5, 1e-4, 3e-4)):
-    """The C5 segment's knot gradients against central differences of the
+    """The segment's knot gradients against central differences of the
     same frozen-noise loss, untimed: for the K-K and K-Cl knot the loss
     feels most, the FP64 adjoint, the FP32 adjoint, and the difference
     quotients of FP64 forward runs at each step h (kcal/mol).  Clamp and
@@ -885,8 +885,8 @@ def run_gpu(args, rank, world, local_rank):
     scaling_pairs = pair_scaling(sh, peak_fp32)
     batched = batch_measure(sh, flush)
     adjoint = adjoint_measure(sh)
-    bulk_c1 = c1_measure(sh)
-    ssdna_c3 = c3_measure(sh)
+    bulk_kcl260 = bulk_measure(sh)
+    ssdna40 = ssdna_measure(sh)
     # the oracle leg: CPU baselines, then the oracle as the checker
     budget = float(os.environ.get("BROMOC_CPU_SAMPLE_S", "15"))
     cpu = oracle_baseline(budget)
@@ -916,8 +916,8 @@ def run_gpu(args, rank, world, local_rank):
             "pair_kernel_scaling": scaling_pairs,
             "batched": batched,
             "adjoint": adjoint,
-            "bulk_c1": bulk_c1,
-            "ssdna_c3": ssdna_c3,
+            "bulk_kcl260": bulk_kcl260,
+            "ssdna40": ssdna40,
             "wall_s": wall, "clocks": clocks}
     print(json.dumps(line), flush=True)
     if dist:

@@ -1,7 +1,7 @@
 // Adjoint of a Brownian-dynamics segment with respect to the tabulated
-// effective-potential tables (scope-table configuration C5).  No reference
-// counterpart: the reference fits effective potentials with the IMC
-// covariance method (imc-macro.f90) instead of differentiating dynamics.
+// effective-potential tables.  No reference counterpart: the reference fits
+// effective potentials with the IMC covariance method (imc-macro.f90)
+// instead of differentiating dynamics.
 //
 // System: ions only, tabulated (EFPOT) ion-ion laws (polynom.f90:197-230),
 // a box with hard walls (fixcoor.f90 clamp), dynamics0 with frozen noise

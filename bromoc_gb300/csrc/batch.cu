@@ -1,5 +1,5 @@
-// Replica batches on the device (scope-table configuration C4): many
-// independent systems of uneven size advance together.
+// Replica batches on the device: many independent systems of uneven size
+// advance together.
 //
 //   k_batch_fields (fields.cu): the FP32 field terms of every live slot.
 //   k_batch_pairs: every tile pair of every replica, one warp each, through

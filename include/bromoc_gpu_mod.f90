@@ -516,6 +516,60 @@ module bromoc_gpu
       integer(c_int) :: rc
     end function
 
+    function bromoc_gpu_metropolis(ctx, terms, nmcm, mcmax, seed, cycle, naccept, dener_sum) &
+         bind(C, name="bromoc_gpu_metropolis") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_int64_t, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: terms, nmcm
+      real(c_double), value :: mcmax
+      integer(c_int64_t), value :: seed, cycle
+      integer(c_int32_t), intent(out) :: naccept
+      real(c_double), intent(out) :: dener_sum
+      integer(c_int) :: rc
+    end function
+
+    ! ---- measurement hooks and self-tests ----------------------------------
+    function bromoc_gpu_kernel_timing(ctx, on) bind(C, name="bromoc_gpu_kernel_timing") result(rc)
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: on
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_kernel_time(ctx, which, total_ms, launches) &
+         bind(C, name="bromoc_gpu_kernel_time") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_int64_t, c_double
+      type(c_ptr), value :: ctx
+      integer(c_int32_t), value :: which
+      real(c_double), intent(out) :: total_ms
+      integer(c_int64_t), intent(out) :: launches
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_launch_count(ctx) bind(C, name="bromoc_gpu_launch_count") result(n)
+      import :: c_ptr, c_int64_t
+      type(c_ptr), value :: ctx
+      integer(c_int64_t) :: n
+    end function
+    function bromoc_gpu_fp32_peak(stream, tflops) bind(C, name="bromoc_gpu_fp32_peak") result(rc)
+      import :: c_int, c_ptr, c_double
+      type(c_ptr), value :: stream
+      real(c_double), intent(out) :: tflops
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_ff_check(fn, n, x, out) bind(C, name="bromoc_gpu_ff_check") result(rc)
+      import :: c_int, c_int32_t, c_double
+      integer(c_int32_t), value :: fn, n
+      real(c_double), intent(in) :: x(*)
+      real(c_double), intent(out) :: out(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_gpu_wait_selftest(spins, arrive, err_word) &
+         bind(C, name="bromoc_gpu_wait_selftest") result(rc)
+      import :: c_int, c_int32_t
+      integer(c_int32_t), value :: spins, arrive
+      integer(c_int32_t), intent(out) :: err_word
+      integer(c_int) :: rc
+    end function
+
     ! ---- replica batches ----------------------------------------------------
     function bromoc_batch_create(proto, nrep, capacity, b) &
          bind(C, name="bromoc_batch_create") result(rc)
@@ -580,6 +634,72 @@ module bromoc_gpu
       integer(c_int) :: off
     end function
 
+    function bromoc_batch_last_error(b) bind(C, name="bromoc_batch_last_error") result(msg)
+      import :: c_ptr
+      type(c_ptr), value :: b
+      type(c_ptr) :: msg
+    end function
+    function bromoc_batch_slots(b) bind(C, name="bromoc_batch_slots") result(n)
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b
+      integer(c_int) :: n
+    end function
+    function bromoc_batch_set_graph(b, on) bind(C, name="bromoc_batch_set_graph") result(rc)
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: b
+      integer(c_int32_t), value :: on
+      integer(c_int) :: rc
+    end function
+    function bromoc_batch_tuning(b, warps, items, ms) bind(C, name="bromoc_batch_tuning") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_double
+      type(c_ptr), value :: b
+      integer(c_int32_t), intent(out) :: warps(*), items(*)
+      real(c_double), intent(out) :: ms(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_batch_graph_launches(b) bind(C, name="bromoc_batch_graph_launches") result(n)
+      import :: c_ptr, c_int64_t
+      type(c_ptr), value :: b
+      integer(c_int64_t) :: n
+    end function
+    function bromoc_batch_launch_count(b) bind(C, name="bromoc_batch_launch_count") result(n)
+      import :: c_ptr, c_int64_t
+      type(c_ptr), value :: b
+      integer(c_int64_t) :: n
+    end function
+    function bromoc_batch_set_buffers(b, r, buf, ibuffer) &
+         bind(C, name="bromoc_batch_set_buffers") result(rc)
+      import :: c_int, c_ptr, c_int32_t, bromoc_buffers
+      type(c_ptr), value :: b
+      integer(c_int32_t), value :: r
+      type(bromoc_buffers), intent(in) :: buf
+      integer(c_int32_t), intent(in) :: ibuffer(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_batch_grand(b, terms, ngcmc, seeds, cycle, dener) &
+         bind(C, name="bromoc_batch_grand") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_int64_t, c_double
+      type(c_ptr), value :: b
+      integer(c_int32_t), value :: terms, ngcmc
+      integer(c_int64_t), intent(in) :: seeds(*)
+      integer(c_int64_t), value :: cycle
+      real(c_double), intent(out) :: dener(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_batch_count(b) bind(C, name="bromoc_batch_count") result(rc)
+      import :: c_int, c_ptr
+      type(c_ptr), value :: b
+      integer(c_int) :: rc
+    end function
+    function bromoc_batch_get_buffers(b, r, nat, ninsert, nremove, typei, ibuffer) &
+         bind(C, name="bromoc_batch_get_buffers") result(rc)
+      import :: c_int, c_ptr, c_int32_t
+      type(c_ptr), value :: b
+      integer(c_int32_t), value :: r
+      integer(c_int32_t), intent(out) :: nat(*), ninsert(*), nremove(*), typei(*), ibuffer(*)
+      integer(c_int) :: rc
+    end function
+
     ! ---- adjoint of a BD segment ------------------------------------------
     function bromoc_adj_create(proto, capacity, precision, a) &
          bind(C, name="bromoc_adj_create") result(rc)
@@ -621,6 +741,19 @@ module bromoc_gpu
       real(c_double), intent(in) :: dl_dhist(*)
       real(c_double), intent(out) :: g_ep(*), g_sc(*)
       integer(c_int) :: rc
+    end function
+    function bromoc_adj_get_particles(a, which, x, y, z) &
+         bind(C, name="bromoc_adj_get_particles") result(rc)
+      import :: c_int, c_ptr, c_int32_t, c_double
+      type(c_ptr), value :: a
+      integer(c_int32_t), value :: which
+      real(c_double), intent(out) :: x(*), y(*), z(*)
+      integer(c_int) :: rc
+    end function
+    function bromoc_adj_last_error(a) bind(C, name="bromoc_adj_last_error") result(msg)
+      import :: c_ptr
+      type(c_ptr), value :: a
+      type(c_ptr) :: msg
     end function
   end interface
 

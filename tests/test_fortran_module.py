@@ -164,6 +164,12 @@ def test_hot_path_entry_points_bound():
         assert "bromoc_gpu_" + name in fi, name
 
 
+def test_every_entry_point_bound():
+    """The module binds every entry point the header declares."""
+    missing = set(c_functions()) - set(f_interfaces())
+    assert not missing, sorted(missing)
+
+
 def test_types_match_structs():
     cs, ft = c_structs(), f_types()
     assert set(ft) == set(cs), (set(ft) ^ set(cs))

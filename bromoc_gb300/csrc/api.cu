@@ -314,9 +314,12 @@ int ensure_scratch(bromoc_ctx *ctx) {
   // + ion-site (tiles)
   ctx->nslot_cap = fields_blocks((int)cap) + tiles * (2 * kMaxChunks + 4) + 8;
   if ((rc = dalloc(ctx, &p.epart, (size_t)ctx->nslot_cap * kNTerms))) return rc;
-  if ((rc = dalloc(ctx, &p.ipart, ((size_t)tiles + 2) * kSpec))) return rc;
-  if ((rc = dalloc(ctx, &p.ierr, ((size_t)tiles + 2) * kSpec))) return rc;
-  ctx->ipart_slots = tiles + 2;
+  // block partials of INTERACT (a double per block) and GRAND (kSpec per
+  // block): enough for GRAND's widest grid, a lane per particle and attempt
+  const int islots = std::max(tiles + 2, grand_slots((int)cap));
+  if ((rc = dalloc(ctx, &p.ipart, (size_t)islots * kSpec))) return rc;
+  if ((rc = dalloc(ctx, &p.ierr, (size_t)islots * kSpec))) return rc;
+  ctx->ipart_slots = islots;
   if ((rc = dalloc(ctx, &p.gc_rf, cap))) return rc;
   if ((rc = dalloc(ctx, &p.gc_rff, cap))) return rc;
   if ((rc = dalloc(ctx, &p.tff, kSpec))) return rc;

@@ -1591,10 +1591,18 @@ __global__ void __launch_bounds__(kGrandThreads)
   launch_exit(st);
 }
 
+// The widest GRAND grid at capacity cap: a lane per (particle, attempt) at
+// the most attempts a round holds (kSpec, the fewest particles a block
+// takes), the attempts' new slots, and the coordinator.
+int grand_slots(int cap) {
+  const int per_blk = kGrandWarps * (32 / kSpec);
+  return (cap + kSpec + per_blk - 1) / per_blk + 1;
+}
+
 // Blocks of the GRAND launch: the coordinator and enough blocks for a lane
 // per (particle, attempt of a round), all co-resident, at most the partial
-// slots the context holds (ipart_slots); with fewer, a lane takes several
-// particles.
+// slots the context holds (ipart_slots, grand_slots of its capacity); with
+// fewer, a lane takes several particles.
 cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
                          uint64_t seed, uint64_t cycle, int ngcmc, int ffpos,
                          cudaStream_t stream) {

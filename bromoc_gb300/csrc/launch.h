@@ -190,6 +190,9 @@ int launch_grand_seq(const KP &p, int ntot_ub, uint32_t mask, uint64_t seed, uin
 cudaError_t launch_grand(const KP &p, int ntot_ub, int ipart_slots, uint32_t mask,
                          uint64_t seed, uint64_t cycle, int ngcmc, int ffpos,
                          cudaStream_t stream);
+// partial slots for GRAND's widest grid at capacity cap (a lane per
+// particle and attempt); INTERACT's need at cap is smaller
+int grand_slots(int cap);
 int interact_slots(int ntot_ub);
 
 }  // namespace bgpu

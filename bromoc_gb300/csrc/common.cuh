@@ -46,6 +46,12 @@ __device__ __forceinline__ float2 v2sub(float2 a, float2 b) {
 __device__ __forceinline__ float2 v2(float a, float b) { return make_float2(a, b); }
 __device__ __forceinline__ float2 v2(float a) { return make_float2(a, a); }
 
+// Hint to bring the line holding *a into L2 (no result; a lies inside an
+// allocation).
+__device__ __forceinline__ void prefetch_l2(const void *a) {
+  asm volatile("prefetch.global.L2 [%0];" ::"l"(a));
+}
+
 // error flags raised by kernels (bit mask in DevState::err)
 enum : int {
   kErrCapacity = 1,     // an insertion would exceed capacity

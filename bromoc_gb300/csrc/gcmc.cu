@@ -1426,6 +1426,21 @@ __global__ void __launch_bounds__(kGrandThreads)
   const bool rf_on = (mask & 16u) && p.qrfpar;
   const int ntot0 = st->ntot;
   bool ok = true;
+  if (blockIdx.x == 0 && ntot0 > 0 && ntot0 <= p.cap) {
+    // into L2 while the tables, the state and the draws are loaded and
+    // formed: the buffer tags the deletion-target scan reads (a line of 32
+    // a thread), and the last ion's records, which a deletion moves into
+    // the freed slot
+    const int t = threadIdx.x, last = ntot0 - 1;
+    for (int s = p.nsites + p.nfix + 32 * t; s < ntot0; s += 32 * (int)blockDim.x)
+      prefetch_l2(p.ibuffer + s);
+    if (t == 0) prefetch_l2(p.ibuffer + last);
+    if (t == 1) prefetch_l2(p.typei + last);
+    if (t == 2) prefetch_l2(ffpos ? (const void *)(p.pk1 + last) : (const void *)(p.x + last));
+    if (t == 3) prefetch_l2(ffpos ? (const void *)(p.pk2 + last) : (const void *)(p.y + last));
+    if (t == 4) prefetch_l2(ffpos ? (const void *)(p.pk3 + last) : (const void *)(p.z + last));
+    if (t == 5 && (mask & 16u) && p.qrfpar) prefetch_l2(p.gc_rff + last);
+  }
   TypeRefs T;
   PairRefs P;
   load_tabs(p, tabs, T, P);

@@ -408,7 +408,8 @@ int bromoc_gpu_simul_cycles_host(bromoc_ctx *ctx, uint32_t terms,
  * of the process -- make that first call before any stream capture; after a
  * device reset the library is not used again in the process.  Each call waits
  * on its stream before it returns (it reads back an error word), so the
- * results are written when it returns; n == 0 writes zero energies (the
+ * results are written when it returns and no call can be made inside a
+ * stream capture; n == 0 writes zero energies (the
  * per-ion arrays may then be null). */
 int bromoc_gpu_pair_energy_static(bromoc_ctx *ctx, int32_t n, int32_t nfix,
                                   const double *x, const double *y,
